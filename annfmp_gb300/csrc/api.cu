@@ -1,0 +1,267 @@
+// api.cu -- the extern "C" entry points declared in include/annf_gb300.h.
+#include <cusolverDn.h>
+
+#include <atomic>
+#include <string>
+
+#include "common.cuh"
+#include "handle.cuh"
+
+namespace annf {
+
+static thread_local std::string g_last_error;
+void set_error(const std::string& msg) { g_last_error = msg; }
+
+static std::atomic<long long> g_launches{0};
+void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+
+// implemented in tree_build.cu / search.cu / pca.cu
+int build_tree(annf_handle* h, const void* points, int n, int d, int real_type, int depth, int splitting,
+               cudaStream_t st);
+int process_rows_generic(annf_handle* h, int* final_idx, const PatchSrc& A, const PatchSrc& B, const void* ared,
+                         int n_rows, int n_cols, int K, int propagate, int select_best, int* knn_out,
+                         float* dist_out, cudaStream_t st);
+int kneighbors_generic(annf_handle* h, const void* Q, int nq, int K, void* dist, int* idx, cudaStream_t st);
+int pca_fit(annf_handle* h, const uint8_t* img_a, int ha, int wa, const int* pos_a, int n_a, const uint8_t* img_b,
+            int hb, int wb, const int* pos_b, int n_b, int c, int psize, int ncomp, double* comps, double* mean,
+            cudaStream_t st);
+int project(annf_handle* h, const uint8_t* img, int H, int W, int c, int psize, const double* comps,
+            const double* mean, int ncomp, int real_type, void* out, cudaStream_t st);
+
+}  // namespace annf
+
+using namespace annf;
+
+static constexpr int kMaxK = 32;
+
+#define ANNF_API_HANDLE(h)                                   \
+  do {                                                       \
+    if (!(h)) {                                              \
+      set_error("handle is NULL");                           \
+      return ANNF_ERR_INVALID;                               \
+    }                                                        \
+    cudaError_t e_ = cudaSetDevice((h)->device);             \
+    if (e_ != cudaSuccess) {                                 \
+      set_error(std::string("cudaSetDevice: ") + cudaGetErrorString(e_)); \
+      return ANNF_ERR_CUDA;                                  \
+    }                                                        \
+  } while (0)
+
+extern "C" {
+
+int annf_version(void) { return 10000; }
+
+const char* annf_last_error(void) { return g_last_error.c_str(); }
+
+int annf_create(annf_handle** out, int device) {
+  if (!out) {
+    set_error("annf_create: out is NULL");
+    return ANNF_ERR_INVALID;
+  }
+  *out = nullptr;
+  int ndev = 0;
+  cudaError_t e = cudaGetDeviceCount(&ndev);
+  if (e != cudaSuccess || ndev == 0) {
+    set_error(std::string("annf_create: no CUDA device: ") + cudaGetErrorString(e));
+    return ANNF_ERR_CUDA;
+  }
+  if (device < 0 || device >= ndev) {
+    set_error("annf_create: device index out of range");
+    return ANNF_ERR_INVALID;
+  }
+  ANNF_CUDA_TRY(cudaSetDevice(device));
+  annf_handle* h = new annf_handle();
+  h->device = device;
+  if (h->status.ensure(sizeof(unsigned)) != ANNF_OK) {
+    delete h;
+    return ANNF_ERR_ALLOC;
+  }
+  ANNF_CUDA_TRY(cudaMemset(h->status.p, 0, sizeof(unsigned)));
+  *out = h;
+  return ANNF_OK;
+}
+
+void annf_destroy(annf_handle* h) {
+  if (!h) return;
+  cudaSetDevice(h->device);
+  if (h->solver) cusolverDnDestroy(reinterpret_cast<cusolverDnHandle_t>(h->solver));
+  DevBuf* bufs[] = {&h->pts, &h->pts_tmp, &h->perm, &h->perm_tmp, &h->node_axis, &h->node_split, &h->leaf_begin,
+                    &h->point_leaf, &h->bmin, &h->bmax, &h->axis, &h->keys, &h->hist, &h->sel_prefix,
+                    &h->sel_rank, &h->sel_nlt, &h->sel_neq, &h->blk_lt, &h->blk_eq, &h->off_lt, &h->off_eq,
+                    &h->eqpos, &h->nat_keys, &h->nat_pos, &h->lists, &h->next_range, &h->part_keys,
+                    &h->part_pos, &h->gram, &h->colsum, &h->subset_t, &h->cov, &h->eigval, &h->digits,
+                    &h->meanproj, &h->solver_ws, &h->solver_info, &h->status};
+  for (DevBuf* b : bufs) b->release();
+  for (int i = 0; i < annf_handle::kMaxMarks; ++i)
+    if (h->prof_ev[i]) cudaEventDestroy(h->prof_ev[i]);
+  delete h;
+}
+
+int annf_build_tree(annf_handle* h, const void* points, int n, int d, int real_type, int depth,
+                    int splitting_type, void* stream) {
+  ANNF_API_HANDLE(h);
+  return build_tree(h, points, n, d, real_type, depth, splitting_type, static_cast<cudaStream_t>(stream));
+}
+
+int annf_tree_get(const annf_handle* h, annf_tree_view* out) {
+  if (!h || !out) {
+    set_error("annf_tree_get: NULL argument");
+    return ANNF_ERR_INVALID;
+  }
+  if (!h->built) {
+    set_error("annf_tree_get: no tree has been built");
+    return ANNF_ERR_STATE;
+  }
+  out->n = h->n;
+  out->d = h->d;
+  out->depth = h->depth;
+  out->real_type = h->real_type;
+  out->n_leaves = 1 << h->depth;
+  out->points = h->pts.p;
+  out->perm = h->perm.as<int>();
+  out->node_axis = h->node_axis.as<int>();
+  out->node_split = h->node_split.p;
+  out->leaf_begin = h->leaf_begin.as<int>();
+  out->point_leaf = h->point_leaf.as<int>();
+  return ANNF_OK;
+}
+
+static int check_k(const annf_handle* h, int k, long long max_leaves) {
+  if (!h->built) {
+    set_error("no tree has been built (call annf_build_tree first)");
+    return ANNF_ERR_STATE;
+  }
+  if (k < 1 || k > 1000) {  // reference limit, helper.c:32-35
+    set_error("k must be in [1, 1000]");
+    return ANNF_ERR_INVALID;
+  }
+  if (k > kMaxK) {
+    set_error("k > 32 is not supported by the GPU kernels");
+    return ANNF_ERR_UNSUPPORTED;
+  }
+  if (max_leaves < (1LL << h->depth)) {
+    set_error("a leaf budget smaller than the number of leaves (approximate first-row search) is not supported");
+    return ANNF_ERR_UNSUPPORTED;
+  }
+  return ANNF_OK;
+}
+
+int annf_kneighbors(annf_handle* h, const void* queries, int nq, int k, long long max_leaves, void* distances,
+                    int* indices, void* stream) {
+  ANNF_API_HANDLE(h);
+  int rc = check_k(h, k, max_leaves);
+  if (rc != ANNF_OK) return rc;
+  ANNF_REQUIRE(nq >= 0, "annf_kneighbors: nq < 0");
+  if (nq == 0) return ANNF_OK;
+  ANNF_REQUIRE(queries && distances && indices, "annf_kneighbors: NULL array");
+  return kneighbors_generic(h, queries, nq, k, distances, indices, static_cast<cudaStream_t>(stream));
+}
+
+static int rows_common_checks(annf_handle* h, int* final_idx, const void* ared, int n_rows, int n_cols, int k,
+                              long long max_leaves) {
+  int rc = check_k(h, k, max_leaves);
+  if (rc != ANNF_OK) return rc;
+  ANNF_REQUIRE(final_idx && ared, "process_rows: NULL output or reduced-patch array");
+  ANNF_REQUIRE(n_rows >= 1 && n_cols >= 1, "process_rows: empty patch grid");
+  ANNF_REQUIRE((long long)n_rows * n_cols <= 0x7fffffffLL, "process_rows: patch grid too large");
+  return ANNF_OK;
+}
+
+int annf_process_rows(annf_handle* h, int* final_idx, const uint8_t* patches_a, int n_a, const uint8_t* patches_b,
+                      int n_b, int P, const void* ared, int n_rows, int n_cols, int k, int propagate,
+                      int select_best, long long max_leaves, int* knn_out, float* dist_out, void* stream) {
+  ANNF_API_HANDLE(h);
+  int rc = rows_common_checks(h, final_idx, ared, n_rows, n_cols, k, max_leaves);
+  if (rc != ANNF_OK) return rc;
+  if (select_best) {
+    ANNF_REQUIRE(patches_a && patches_b && P >= 1, "annf_process_rows: select_best needs both patch arrays");
+    ANNF_REQUIRE(n_a == n_rows * n_cols, "annf_process_rows: patches_a must have n_rows*n_cols rows");
+    ANNF_REQUIRE(n_b == h->n, "annf_process_rows: patches_b must have one row per tree point");
+  }
+  PatchSrc A{patches_a, 0, P, 1, 0, false}, B{patches_b, 0, P, 1, 0, false};
+  return process_rows_generic(h, final_idx, A, B, ared, n_rows, n_cols, k, propagate, select_best, knn_out,
+                              dist_out, static_cast<cudaStream_t>(stream));
+}
+
+int annf_process_rows_img(annf_handle* h, int* final_idx, const uint8_t* img_a, int ha, int wa, const uint8_t* img_b,
+                          int hb, int wb, int channels, int psize, const void* ared, int n_rows, int n_cols, int k,
+                          int propagate, int select_best, long long max_leaves, int* knn_out, float* dist_out,
+                          void* stream) {
+  ANNF_API_HANDLE(h);
+  int rc = rows_common_checks(h, final_idx, ared, n_rows, n_cols, k, max_leaves);
+  if (rc != ANNF_OK) return rc;
+  if (select_best) {
+    ANNF_REQUIRE(img_a && img_b && channels >= 1 && psize >= 1, "annf_process_rows_img: NULL image or bad geometry");
+    ANNF_REQUIRE(ha - psize + 1 == n_rows && wa - psize + 1 == n_cols,
+                 "annf_process_rows_img: n_rows/n_cols must match image A and psize");
+    ANNF_REQUIRE((long long)(hb - psize + 1) * (wb - psize + 1) == h->n,
+                 "annf_process_rows_img: the tree must hold every patch of image B");
+  }
+  PatchSrc A{img_a, wa, channels, psize, wa - psize + 1, true};
+  PatchSrc B{img_b, wb, channels, psize, wb - psize + 1, true};
+  return process_rows_generic(h, final_idx, A, B, ared, n_rows, n_cols, k, propagate, select_best, knn_out,
+                              dist_out, static_cast<cudaStream_t>(stream));
+}
+
+int annf_pca_fit(annf_handle* h, const uint8_t* img_a, int ha, int wa, const int* pos_a, int n_a,
+                 const uint8_t* img_b, int hb, int wb, const int* pos_b, int n_b, int channels, int psize,
+                 int n_components, double* components_out, double* mean_out, void* stream) {
+  ANNF_API_HANDLE(h);
+  ANNF_REQUIRE(img_a && img_b && components_out && mean_out, "annf_pca_fit: NULL argument");
+  ANNF_REQUIRE((n_a == 0 || pos_a) && (n_b == 0 || pos_b), "annf_pca_fit: NULL positions");
+  ANNF_REQUIRE(n_a >= 0 && n_b >= 0 && channels >= 1 && psize >= 1, "annf_pca_fit: bad sizes");
+  ANNF_REQUIRE(psize <= ha && psize <= wa && psize <= hb && psize <= wb, "annf_pca_fit: patch larger than image");
+  return pca_fit(h, img_a, ha, wa, pos_a, n_a, img_b, hb, wb, pos_b, n_b, channels, psize, n_components,
+                 components_out, mean_out, static_cast<cudaStream_t>(stream));
+}
+
+int annf_project(annf_handle* h, const uint8_t* img, int hgt, int wid, int channels, int psize,
+                 const double* components, const double* mean, int n_components, int real_type, void* out,
+                 void* stream) {
+  ANNF_API_HANDLE(h);
+  ANNF_REQUIRE(img && components && mean && out, "annf_project: NULL argument");
+  ANNF_REQUIRE(channels >= 1 && psize >= 1 && psize <= hgt && psize <= wid, "annf_project: bad geometry");
+  ANNF_REQUIRE(real_type == ANNF_REAL_F32 || real_type == ANNF_REAL_F64, "annf_project: bad real_type");
+  return project(h, img, hgt, wid, channels, psize, components, mean, n_components, real_type, out,
+                 static_cast<cudaStream_t>(stream));
+}
+
+int annf_device_status(annf_handle* h, void* stream, unsigned* bits_out) {
+  ANNF_API_HANDLE(h);
+  unsigned bits = 0;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  ANNF_CUDA_TRY(cudaMemcpyAsync(&bits, h->status.p, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+  ANNF_CUDA_TRY(cudaStreamSynchronize(st));
+  ANNF_CUDA_TRY(cudaMemsetAsync(h->status.p, 0, sizeof(unsigned), st));
+  if (bits_out) *bits_out = bits;
+  if (bits) {
+    set_error("device bounds check tripped (status bits " + std::to_string(bits) + ")");
+    return ANNF_ERR_DEVICE;
+  }
+  return ANNF_OK;
+}
+
+long long annf_launch_count(void) { return g_launches.load(std::memory_order_relaxed); }
+
+int annf_profile_enable(annf_handle* h, int on) {
+  ANNF_API_HANDLE(h);
+  h->prof_on = on ? 1 : 0;
+  h->prof_used = 0;
+  return ANNF_OK;
+}
+
+int annf_profile_read(annf_handle* h, void* stream, int cap, float* ms, const char** names) {
+  ANNF_API_HANDLE(h);
+  ANNF_CUDA_TRY(cudaStreamSynchronize(static_cast<cudaStream_t>(stream)));
+  int n = 0;
+  for (int i = 1; i < h->prof_used && n < cap; ++i, ++n) {
+    float t = 0.f;
+    ANNF_CUDA_TRY(cudaEventElapsedTime(&t, h->prof_ev[i - 1], h->prof_ev[i]));
+    if (ms) ms[n] = t;
+    if (names) names[n] = h->prof_name[i];
+  }
+  h->prof_used = 0;
+  return n;
+}
+
+}  // extern "C"

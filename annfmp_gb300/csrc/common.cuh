@@ -1,0 +1,171 @@
+// common.cuh -- shared definitions of the annf_gb300 CUDA library (sm_103a).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cfloat>
+#include <string>
+
+#include "../../include/annf_gb300.h"
+
+namespace annf {
+
+// ------------------------------------------------------------------------------------------
+// error plumbing: every entry point returns a status; the message is kept per thread
+// ------------------------------------------------------------------------------------------
+void set_error(const std::string& msg);
+
+#define ANNF_CUDA_TRY(expr)                                                                  \
+  do {                                                                                       \
+    cudaError_t e_ = (expr);                                                                 \
+    if (e_ != cudaSuccess) {                                                                 \
+      ::annf::set_error(std::string(#expr) + ": " + cudaGetErrorString(e_));                 \
+      return ANNF_ERR_CUDA;                                                                  \
+    }                                                                                        \
+  } while (0)
+
+void count_launch();
+
+// called once after every kernel launch: counts it and reports a launch error
+#define ANNF_CHECK_LAUNCH()                                                                  \
+  do {                                                                                       \
+    ::annf::count_launch();                                                                  \
+    cudaError_t e_ = cudaGetLastError();                                                     \
+    if (e_ != cudaSuccess) {                                                                 \
+      ::annf::set_error(std::string("kernel launch: ") + cudaGetErrorString(e_));            \
+      return ANNF_ERR_CUDA;                                                                  \
+    }                                                                                        \
+  } while (0)
+
+#define ANNF_REQUIRE(cond, msg)                                                              \
+  do {                                                                                       \
+    if (!(cond)) {                                                                           \
+      ::annf::set_error(msg);                                                                \
+      return ANNF_ERR_INVALID;                                                               \
+    }                                                                                        \
+  } while (0)
+
+// device-side status bits (bounds checks that skip the access instead of faulting)
+enum : unsigned {
+  DEV_BAD_INDEX = 1u,
+  DEV_BAD_LEAF = 2u,
+  DEV_LIST_OVERFLOW = 4u,
+};
+
+// ------------------------------------------------------------------------------------------
+// scalar traits
+// ------------------------------------------------------------------------------------------
+template <typename T> struct real_traits;
+template <> struct real_traits<float> {
+  static constexpr float big() { return FLT_MAX; }
+  __device__ static float sub(float a, float b) { return __fsub_rn(a, b); }
+  __device__ static float mul(float a, float b) { return __fmul_rn(a, b); }
+  __device__ static float add(float a, float b) { return __fadd_rn(a, b); }
+  __device__ static float sqrt_(float a) { return __fsqrt_rn(a); }
+};
+template <> struct real_traits<double> {
+  static constexpr double big() { return DBL_MAX; }
+  __device__ static double sub(double a, double b) { return __dsub_rn(a, b); }
+  __device__ static double mul(double a, double b) { return __dmul_rn(a, b); }
+  __device__ static double add(double a, double b) { return __dadd_rn(a, b); }
+  __device__ static double sqrt_(double a) { return __dsqrt_rn(a); }
+};
+
+// Order-preserving unsigned image of a float with -0.0 folded onto +0.0, so that key equality is
+// IEEE equality and key order is IEEE order (NaN-free inputs).
+__device__ __forceinline__ uint32_t ord_key(float f) {
+  uint32_t b = __float_as_uint(f);
+  if (b == 0x80000000u) b = 0u;
+  return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+__device__ __forceinline__ float key_to_float(uint32_t k) {
+  uint32_t b = (k & 0x80000000u) ? (k & 0x7fffffffu) : ~k;
+  return __uint_as_float(b);
+}
+__device__ __forceinline__ unsigned long long ord_key(double f) {
+  unsigned long long b = __double_as_longlong(f);
+  if (b == 0x8000000000000000ull) b = 0ull;
+  return (b & 0x8000000000000000ull) ? ~b : (b | 0x8000000000000000ull);
+}
+__device__ __forceinline__ double key_to_real(unsigned long long k) {
+  unsigned long long b = (k & 0x8000000000000000ull) ? (k & 0x7fffffffffffffffull) : ~k;
+  return __longlong_as_double(b);
+}
+
+template <typename T> struct key_of;
+template <> struct key_of<float> { using type = uint32_t; static constexpr int bits = 32; };
+template <> struct key_of<double> { using type = unsigned long long; static constexpr int bits = 64; };
+
+// Sort key of a candidate: the distance's bits (non-negative reals order like their bits), then
+// a tie-break that reproduces the reference's visiting order. 64 bits for float distances; for
+// double distances the key is a pair.
+template <typename T> struct cand_key;
+template <> struct cand_key<float> {
+  using type = unsigned long long;
+  __device__ static type make(float d, uint32_t tie) {
+    return ((unsigned long long)__float_as_uint(d) << 32) | tie;
+  }
+  __device__ static float dist(type k) { return __uint_as_float((uint32_t)(k >> 32)); }
+  static constexpr type init_key() { return ((unsigned long long)0x7f7fffffu << 32); }  // FLT_MAX, tie 0
+};
+
+struct dkey {  // double distance + tie
+  unsigned long long d;
+  uint32_t tie;
+};
+__device__ __forceinline__ bool operator<(const dkey& a, const dkey& b) {
+  return a.d < b.d || (a.d == b.d && a.tie < b.tie);
+}
+template <> struct cand_key<double> {
+  using type = dkey;
+  __device__ static type make(double d, uint32_t tie) {
+    return dkey{(unsigned long long)__double_as_longlong(d), tie};
+  }
+  __device__ static double dist(type k) { return __longlong_as_double((long long)k.d); }
+  __host__ __device__ static type init_key() { return dkey{0x7fefffffffffffffull, 0u}; }  // DBL_MAX
+};
+
+__device__ __forceinline__ unsigned long long shfl_xor_u64(unsigned long long v, int m) {
+  return __shfl_xor_sync(0xffffffffu, v, m);
+}
+__device__ __forceinline__ dkey shfl_xor_dk(dkey v, int m) {
+  return dkey{__shfl_xor_sync(0xffffffffu, v.d, m), __shfl_xor_sync(0xffffffffu, v.tie, m)};
+}
+__device__ __forceinline__ unsigned long long shfl_u64(unsigned long long v, int src) {
+  return __shfl_sync(0xffffffffu, v, src);
+}
+
+// ------------------------------------------------------------------------------------------
+// device tree view (structure of arrays, heap-ordered nodes)
+// ------------------------------------------------------------------------------------------
+template <typename T>
+struct TreeView {
+  int n, d, depth;
+  int leaf_bits;            // bits needed for an offset inside any leaf
+  const T* pts;             // [n*d] tree order
+  const int* perm;          // [n] tree position -> original index
+  const int* node_axis;     // [2^depth-1]
+  const T* node_split;      // [2^depth-1]
+  const int* leaf_begin;    // [2^depth+1] (leaf l spans [leaf_begin[l], leaf_begin[l+1]))
+  const int* point_leaf;    // [n] original index -> leaf
+};
+
+// Source of raw uint8 patches: an HxWxC image (patch index = y*ncols + x) or a patch array
+// ([n*P] bytes, described as psize=1, c=P).
+struct PatchSrc {
+  const uint8_t* img;  // image (HxWxC) or patch array ([n*P])
+  int w, c, psize, ncols;
+  bool is_img;
+  __device__ __forceinline__ const uint8_t* row(long long idx, int r) const {
+    if (is_img) {
+      const long long y = idx / ncols, x = idx - y * ncols;
+      return img + ((y + r) * w + x) * c;
+    }
+    return img + idx * (long long)psize * psize * c + (long long)r * psize * c;
+  }
+};
+
+inline int ceil_div(long long a, long long b) { return (int)((a + b - 1) / b); }
+
+}  // namespace annf

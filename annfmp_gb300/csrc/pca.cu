@@ -1,0 +1,405 @@
+// pca.cu -- PCA fit and patch projection on the GPU (sm_103a).
+//
+// Fit (annfmp/openmp/base.py:168-191 -> scikit-learn PCA, covariance_eigh solver):
+//   G = X^T X and the column sums are integer sums of uint8 products, accumulated EXACTLY with
+//   dp4a into int32 partials that are flushed to 64-bit integers; the covariance is then finished
+//   in FP64 in the solver's own operation order (mean = sum / n; C = G - (n*mean_i)*mean_j;
+//   C /= n-1), so C is bit-identical to the CPU's; eigen-decomposition by cuSOLVER (FP64),
+//   eigenvectors reordered by decreasing eigenvalue and signed so that each component's largest
+//   |entry| is positive (sklearn svd_flip with u_based_decision=False).
+// Projection (annfmp/openmp/base.py:193-200 -> X @ C^T - mean @ C^T in FP64, cast):
+//   each FP64 coefficient is split into 8 signed 7-bit digits (c = 2^-E * sum_k s_k 2^-7k, exact
+//   to ~2^-55 of the component's largest entry); every patch . digit-vector product is an exact
+//   int32 dp4a sum over the uint8 patch bytes, read straight from the image; the partial sums are
+//   recombined in FP64, the mean term subtracted, and the result rounded once to FP32.
+#include <cusolverDn.h>
+
+#include <algorithm>
+
+#include "common.cuh"
+#include "handle.cuh"
+
+namespace annf {
+
+__device__ __forceinline__ int dp4a_us(unsigned a, int b, int c) {
+  int d;
+  asm("dp4a.u32.s32 %0, %1, %2, %3;" : "=r"(d) : "r"(a), "r"(b), "r"(c));
+  return d;
+}
+__device__ __forceinline__ unsigned dp4a_uu(unsigned a, unsigned b, unsigned c) {
+  unsigned d;
+  asm("dp4a.u32.u32 %0, %1, %2, %3;" : "=r"(d) : "r"(a), "r"(b), "r"(c));
+  return d;
+}
+
+// ---------------------------------------------------------------------------------------------
+// fit
+// ---------------------------------------------------------------------------------------------
+// XT[f][s] (feature-major, samples padded to a multiple of 4 with zeros); feature P is a row of
+// ones (so that G[i][P] = column sum i and G[P][P] = n), features P+1..F-1 are zero.
+__global__ void gather_subset_kernel(const uint8_t* __restrict__ img_a, int wa, const int* __restrict__ pos_a, int n_a,
+                                     const uint8_t* __restrict__ img_b, int wb, const int* __restrict__ pos_b, int n_b,
+                                     int c, int psize, int F, int ns_pad, uint8_t* __restrict__ XT) {
+  const int P = psize * psize * c;
+  const long long total = (long long)F * ns_pad;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x) {
+    const int f = (int)(e / ns_pad), s = (int)(e - (long long)f * ns_pad);
+    uint8_t v = 0;
+    if (s < n_a + n_b) {
+      if (f < P) {
+        const int r = f / (psize * c), rem = f - r * psize * c;
+        const int col = rem / c, ch = rem - col * c;
+        if (s < n_a) {
+          const int y = pos_a[2 * s], x = pos_a[2 * s + 1];
+          v = img_a[((long long)(y + r) * wa + (x + col)) * c + ch];
+        } else {
+          const int t = s - n_a;
+          const int y = pos_b[2 * t], x = pos_b[2 * t + 1];
+          v = img_b[((long long)(y + r) * wb + (x + col)) * c + ch];
+        }
+      } else if (f == P) {
+        v = 1;
+      }
+    }
+    XT[e] = v;
+  }
+}
+
+// G += XT XT^T over a sample-word range; 64x64 output tile per block, 4x4 per thread
+constexpr int kGT = 64;       // output tile
+constexpr int kGW = 16;       // sample words per smem stage
+constexpr int kGramSplitWords = 8192;  // words per split: int32 partials stay below 2^31
+
+__global__ void __launch_bounds__(256) gram_kernel(const unsigned* __restrict__ XTw, int F, int nwords,
+                                                   unsigned long long* __restrict__ G) {
+  __shared__ unsigned sa[kGW][kGT + 1], sb[kGW][kGT + 1];
+  const int ti = blockIdx.x, tj = blockIdx.y;
+  if (tj < ti) return;  // upper triangle of tiles only; mirrored at the end
+  const int w0 = blockIdx.z * kGramSplitWords, w1 = min(nwords, w0 + kGramSplitWords);
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  unsigned acc[4][4];
+#pragma unroll
+  for (int a = 0; a < 4; ++a)
+#pragma unroll
+    for (int b = 0; b < 4; ++b) acc[a][b] = 0;
+  for (int w = w0; w < w1; w += kGW) {
+    for (int e = threadIdx.x; e < kGW * kGT; e += blockDim.x) {
+      const int ww = e % kGW, f = e / kGW;
+      const int gw = w + ww;
+      const int fi = ti * kGT + f, fj = tj * kGT + f;
+      sa[ww][f] = (gw < w1 && fi < F) ? XTw[(long long)fi * nwords + gw] : 0u;
+      sb[ww][f] = (gw < w1 && fj < F) ? XTw[(long long)fj * nwords + gw] : 0u;
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int ww = 0; ww < kGW; ++ww) {
+      unsigned ra[4], rb[4];
+#pragma unroll
+      for (int a = 0; a < 4; ++a) ra[a] = sa[ww][ty * 4 + a];
+#pragma unroll
+      for (int b = 0; b < 4; ++b) rb[b] = sb[ww][tx * 4 + b];
+#pragma unroll
+      for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b) acc[a][b] = dp4a_uu(ra[a], rb[b], acc[a][b]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int a = 0; a < 4; ++a)
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+      const int i = ti * kGT + ty * 4 + a, j = tj * kGT + tx * 4 + b;
+      if (i < F && j < F && acc[a][b]) atomicAdd(&G[(long long)i * F + j], (unsigned long long)acc[a][b]);
+    }
+}
+
+// covariance in FP64 exactly as the CPU solver computes it; also the mean
+__global__ void cov_finish_kernel(const unsigned long long* __restrict__ G, int F, int P, double* __restrict__ C,
+                                  double* __restrict__ mean) {
+  const unsigned long long n_ll = G[(long long)P * F + P];
+  const double n = (double)n_ll;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < (long long)P * P; e += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(e / P), j = (int)(e - (long long)i * P);
+    const int a = min(i, j), b = max(i, j);
+    const double g = (double)G[(long long)a * F + b];
+    const double mi = __ddiv_rn((double)G[(long long)i * F + P], n);
+    const double mj = __ddiv_rn((double)G[(long long)j * F + P], n);
+    const double outer = __dmul_rn(__dmul_rn(n, mi), mj);
+    C[e] = __ddiv_rn(__dsub_rn(g, outer), n - 1.0);
+    if (i == 0) mean[j] = mj;
+  }
+}
+
+// components: eigenvectors by decreasing eigenvalue, sign of the largest |entry| made positive
+__global__ void flip_kernel(const double* __restrict__ V, int P, int ncomp, double* __restrict__ comps) {
+  const int c = blockIdx.x;
+  const double* v = V + (long long)(P - 1 - c) * P;  // column-major: eigenvector k is column k
+  __shared__ double sbest[256];
+  __shared__ int sidx[256];
+  double best = -1.0;
+  int bi = 0x7fffffff;
+  for (int i = threadIdx.x; i < P; i += blockDim.x) {
+    const double a = fabs(v[i]);
+    if (a > best || (a == best && i < bi)) {
+      best = a;
+      bi = i;
+    }
+  }
+  sbest[threadIdx.x] = best;
+  sidx[threadIdx.x] = bi;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o; o >>= 1) {
+    if ((int)threadIdx.x < o) {
+      const double ob = sbest[threadIdx.x + o];
+      const int oi = sidx[threadIdx.x + o];
+      if (ob > sbest[threadIdx.x] || (ob == sbest[threadIdx.x] && oi < sidx[threadIdx.x])) {
+        sbest[threadIdx.x] = ob;
+        sidx[threadIdx.x] = oi;
+      }
+    }
+    __syncthreads();
+  }
+  const double piv = v[sidx[0]];
+  const double sg = piv > 0 ? 1.0 : (piv < 0 ? -1.0 : 0.0);
+  for (int i = threadIdx.x; i < P; i += blockDim.x) comps[(long long)c * P + i] = __dmul_rn(v[i], sg);
+}
+
+// ---------------------------------------------------------------------------------------------
+// projection
+// ---------------------------------------------------------------------------------------------
+constexpr int kSlices = 8;  // signed 7-bit digits per coefficient
+
+// digits[j][k][word*4 + byte] laid out over the padded patch (row r occupies rw bytes, rw =
+// round_up(psize*c, 4)), total W4 words (multiple of 4). Also scale exponent per component and
+// the FP64 mean term m_j = mean . c_j.
+__global__ void digits_kernel(const double* __restrict__ comps, const double* __restrict__ mean, int P, int psize,
+                              int c, int rw, int W4, int8_t* __restrict__ digits, int* __restrict__ expo,
+                              double* __restrict__ mproj) {
+  const int j = blockIdx.x;
+  const double* cj = comps + (long long)j * P;
+  __shared__ double smax[256];
+  __shared__ double sm[256];
+  double mx = 0.0, mm = 0.0;
+  for (int i = threadIdx.x; i < P; i += blockDim.x) mx = fmax(mx, fabs(cj[i]));
+  smax[threadIdx.x] = mx;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o; o >>= 1) {
+    if ((int)threadIdx.x < o) smax[threadIdx.x] = fmax(smax[threadIdx.x], smax[threadIdx.x + o]);
+    __syncthreads();
+  }
+  mx = smax[0];
+  int E = 0;
+  if (mx > 0) {
+    int e2;
+    frexp(mx, &e2);  // mx in [2^(e2-1), 2^e2)
+    E = 6 - e2;      // mx * 2^E in [32, 64)
+  }
+  if (threadIdx.x == 0) expo[j] = E;
+  int8_t* dj = digits + (long long)j * kSlices * W4 * 4;
+  for (int e = threadIdx.x; e < W4 * 4; e += blockDim.x) {
+    const int r = e / rw, within = e - r * rw;
+    double v = 0.0;
+    if (r < psize && within < psize * c) v = ldexp(cj[r * psize * c + within], E);
+#pragma unroll
+    for (int k = 0; k < kSlices; ++k) {
+      const double s = rint(v);
+      dj[(long long)k * W4 * 4 + e] = (int8_t)(int)s;
+      v = (v - s) * 128.0;  // exact
+    }
+  }
+  // mean term in FP64 (sequential order)
+  if (threadIdx.x == 0) {
+    double acc = 0.0;
+    for (int i = 0; i < P; ++i) acc = __dadd_rn(acc, __dmul_rn(mean[i], cj[i]));
+    mproj[j] = acc;
+  }
+  (void)sm;
+  (void)mm;
+}
+
+constexpr int kPTW = 32, kPTH = 4;  // projection tile: 32 x 4 pixels, one thread per pixel
+
+__device__ __forceinline__ unsigned load_u32_unaligned_smem(const unsigned* base_words, int byte_off) {
+  const int w = byte_off >> 2, sh = (byte_off & 3) * 8;
+  const unsigned lo = base_words[w], hi = base_words[w + 1];
+  return sh ? __funnelshift_r(lo, hi, sh) : lo;
+}
+
+template <typename OutT, int W4>
+__global__ void __launch_bounds__(kPTW * kPTH) project_kernel(const uint8_t* __restrict__ img, int H, int W, int c,
+                                                               int psize, int rw, int ncomp,
+                                                               const int8_t* __restrict__ digits,
+                                                               const int* __restrict__ expo,
+                                                               const double* __restrict__ mproj, OutT* __restrict__ out) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int nrows = H - psize + 1, ncols = W - psize + 1;
+  const int x0 = blockIdx.x * kPTW, y0 = blockIdx.y * kPTH;
+  const int tx = threadIdx.x % kPTW, ty = threadIdx.x / kPTW;
+  // digits for all components
+  const int dig_words = ncomp * kSlices * W4;
+  int* sdig = reinterpret_cast<int*>(smem);
+  for (int e = threadIdx.x; e < dig_words; e += blockDim.x) sdig[e] = reinterpret_cast<const int*>(digits)[e];
+  // image region
+  const int reg_rows = kPTH + psize - 1;
+  const int reg_bytes = (kPTW + psize - 1) * c;
+  const int reg_stride = ((reg_bytes + 7) / 4 + 1) * 4;  // bytes, word aligned, with slack
+  unsigned* sreg = reinterpret_cast<unsigned*>(sdig + dig_words);
+  uint8_t* sregb = reinterpret_cast<uint8_t*>(sreg);
+  for (int e = threadIdx.x; e < reg_rows * reg_stride; e += blockDim.x) {
+    const int rr = e / reg_stride, bb = e - rr * reg_stride;
+    const int gy = y0 + rr, gxb = x0 * c + bb;
+    uint8_t v = 0;
+    if (gy < H && bb < reg_bytes && gxb < W * c) v = img[(long long)gy * W * c + gxb];
+    sregb[e] = v;
+  }
+  __syncthreads();
+  const int x = x0 + tx, y = y0 + ty;
+  if (x >= ncols || y >= nrows) return;
+  // this patch's bytes, row by row, each row padded to rw bytes
+  unsigned xw[W4];
+  const int wpr = rw / 4;
+#pragma unroll
+  for (int w = 0; w < W4; ++w) {
+    const int r = w / wpr, wi = w - r * wpr;
+    xw[w] = (r < psize) ? load_u32_unaligned_smem(sreg, (ty + r) * reg_stride + tx * c + wi * 4) : 0u;
+  }
+  const long long pix = (long long)y * ncols + x;
+  for (int j = 0; j < ncomp; ++j) {
+    double acc = 0.0;
+    const int4* dj = reinterpret_cast<const int4*>(sdig + j * kSlices * W4);
+#pragma unroll
+    for (int k = kSlices - 1; k >= 0; --k) {
+      int s = 0;
+#pragma unroll
+      for (int w = 0; w < W4; w += 4) {
+        const int4 dd = dj[(k * W4 + w) / 4];
+        s = dp4a_us(xw[w + 0], dd.x, s);
+        s = dp4a_us(xw[w + 1], dd.y, s);
+        s = dp4a_us(xw[w + 2], dd.z, s);
+        s = dp4a_us(xw[w + 3], dd.w, s);
+      }
+      acc = __dadd_rn(__dmul_rn(acc, 0.0078125), (double)s);  // Horner in base 2^-7
+    }
+    const double xc = ldexp(acc, -__ldg(expo + j));
+    const double yv = __dsub_rn(xc, __ldg(mproj + j));
+    out[pix * ncomp + j] = (OutT)yv;
+  }
+}
+
+static int round_up(int a, int b) { return (a + b - 1) / b * b; }
+
+int pca_fit(annf_handle* h, const uint8_t* img_a, int ha, int wa, const int* pos_a, int n_a, const uint8_t* img_b,
+            int hb, int wb, const int* pos_b, int n_b, int c, int psize, int ncomp, double* comps, double* mean,
+            cudaStream_t st) {
+  (void)ha;
+  (void)hb;
+  const int P = psize * psize * c;
+  const int ns = n_a + n_b;
+  ANNF_REQUIRE(ns >= 2, "annf_pca_fit: need at least two samples");
+  ANNF_REQUIRE(ncomp >= 1 && ncomp <= P, "annf_pca_fit: n_components out of range");
+  ANNF_REQUIRE(P + 1 <= 4096, "annf_pca_fit: patch too large");
+  const int F = P + 1;
+  const int ns_pad = round_up(ns, 4);
+  const int nwords = ns_pad / 4;
+  ANNF_ENSURE(h->subset_t, (size_t)F * ns_pad);
+  ANNF_ENSURE(h->gram, (size_t)F * F * sizeof(unsigned long long));
+  ANNF_ENSURE(h->cov, (size_t)P * P * sizeof(double));
+  ANNF_ENSURE(h->eigval, (size_t)P * sizeof(double));
+  ANNF_ENSURE(h->solver_info, sizeof(int));
+  prof_mark(h, "pca:begin", st);
+  gather_subset_kernel<<<std::min(ceil_div((long long)F * ns_pad, 256), 8192), 256, 0, st>>>(
+      img_a, wa, pos_a, n_a, img_b, wb, pos_b, n_b, c, psize, F, ns_pad, h->subset_t.as<uint8_t>());
+  ANNF_CHECK_LAUNCH();
+  ANNF_CUDA_TRY(cudaMemsetAsync(h->gram.p, 0, (size_t)F * F * sizeof(unsigned long long), st));
+  const int tiles = ceil_div(F, kGT);
+  dim3 g(tiles, tiles, ceil_div(nwords, kGramSplitWords));
+  gram_kernel<<<g, 256, 0, st>>>(reinterpret_cast<const unsigned*>(h->subset_t.p), F, nwords,
+                                 h->gram.as<unsigned long long>());
+  ANNF_CHECK_LAUNCH();
+  prof_mark(h, "pca_gram", st);
+  cov_finish_kernel<<<std::min(ceil_div((long long)P * P, 256), 1024), 256, 0, st>>>(
+      h->gram.as<unsigned long long>(), F, P, h->cov.as<double>(), mean);
+  ANNF_CHECK_LAUNCH();
+  if (!h->solver) {
+    cusolverDnHandle_t sh;
+    if (cusolverDnCreate(&sh) != CUSOLVER_STATUS_SUCCESS) {
+      set_error("cusolverDnCreate failed");
+      return ANNF_ERR_SOLVER;
+    }
+    h->solver = reinterpret_cast<cusolverDnContext*>(sh);
+  }
+  cusolverDnHandle_t sh = reinterpret_cast<cusolverDnHandle_t>(h->solver);
+  if (cusolverDnSetStream(sh, st) != CUSOLVER_STATUS_SUCCESS) {
+    set_error("cusolverDnSetStream failed");
+    return ANNF_ERR_SOLVER;
+  }
+  int lwork = 0;
+  if (cusolverDnDsyevd_bufferSize(sh, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, P, h->cov.as<double>(), P,
+                                  h->eigval.as<double>(), &lwork) != CUSOLVER_STATUS_SUCCESS) {
+    set_error("cusolverDnDsyevd_bufferSize failed");
+    return ANNF_ERR_SOLVER;
+  }
+  ANNF_ENSURE(h->solver_ws, (size_t)std::max(lwork, 1) * sizeof(double));
+  if (cusolverDnDsyevd(sh, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, P, h->cov.as<double>(), P,
+                       h->eigval.as<double>(), h->solver_ws.as<double>(), lwork, h->solver_info.as<int>()) !=
+      CUSOLVER_STATUS_SUCCESS) {
+    set_error("cusolverDnDsyevd failed");
+    return ANNF_ERR_SOLVER;
+  }
+  prof_mark(h, "pca_eigh", st);
+  flip_kernel<<<ncomp, 256, 0, st>>>(h->cov.as<double>(), P, ncomp, comps);
+  ANNF_CHECK_LAUNCH();
+  return ANNF_OK;
+}
+
+#define ANNF_W4_CASES(X) X(8) X(12) X(16) X(20) X(24) X(28) X(32) X(36) X(40) X(44) X(48) X(52) X(56) X(60) X(64)
+
+int project(annf_handle* h, const uint8_t* img, int H, int W, int c, int psize, const double* comps,
+            const double* mean, int ncomp, int real_type, void* out, cudaStream_t st) {
+  const int P = psize * psize * c;
+  const int rw = round_up(psize * c, 4);
+  const int W4 = round_up(std::max(psize * rw / 4, 8), 4);
+  ANNF_REQUIRE(W4 <= 64, "annf_project: patch rows larger than 256 bytes are not supported");
+  ANNF_REQUIRE(ncomp >= 1 && ncomp <= P, "annf_project: n_components out of range");
+  ANNF_ENSURE(h->digits, (size_t)ncomp * kSlices * W4 * 4 + (size_t)ncomp * sizeof(int));
+  ANNF_ENSURE(h->meanproj, (size_t)ncomp * sizeof(double));
+  prof_mark(h, "project:begin", st);
+  int8_t* dig = h->digits.as<int8_t>();
+  int* expo = reinterpret_cast<int*>(dig + (size_t)ncomp * kSlices * W4 * 4);
+  digits_kernel<<<ncomp, 256, 0, st>>>(comps, mean, P, psize, c, rw, W4, dig, expo, h->meanproj.as<double>());
+  ANNF_CHECK_LAUNCH();
+  const int nrows = H - psize + 1, ncols = W - psize + 1;
+  dim3 grid(ceil_div(ncols, kPTW), ceil_div(nrows, kPTH));
+  const int reg_rows = kPTH + psize - 1;
+  const int reg_bytes = (kPTW + psize - 1) * c;
+  const int reg_stride = ((reg_bytes + 7) / 4 + 1) * 4;
+  const size_t smem = (size_t)ncomp * kSlices * W4 * 4 + (size_t)reg_rows * reg_stride + 16;
+  ANNF_REQUIRE(smem <= 200 * 1024, "annf_project: too many components for the shared-memory digit table");
+#define ANNF_LAUNCH_PROJ(WV)                                                                                     \
+  case WV:                                                                                                       \
+    if (real_type == ANNF_REAL_F32) {                                                                            \
+      ANNF_CUDA_TRY(cudaFuncSetAttribute(project_kernel<float, WV>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                                         (int)smem));                                                            \
+      project_kernel<float, WV><<<grid, kPTW * kPTH, smem, st>>>(img, H, W, c, psize, rw, ncomp, dig, expo,       \
+                                                                  h->meanproj.as<double>(), (float*)out);        \
+    } else {                                                                                                     \
+      ANNF_CUDA_TRY(cudaFuncSetAttribute(project_kernel<double, WV>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                                         (int)smem));                                                            \
+      project_kernel<double, WV><<<grid, kPTW * kPTH, smem, st>>>(img, H, W, c, psize, rw, ncomp, dig, expo,      \
+                                                                   h->meanproj.as<double>(), (double*)out);      \
+    }                                                                                                            \
+    break;
+  switch (W4) {
+    ANNF_W4_CASES(ANNF_LAUNCH_PROJ)
+    default:
+      set_error("annf_project: unsupported patch geometry");
+      return ANNF_ERR_UNSUPPORTED;
+  }
+#undef ANNF_LAUNCH_PROJ
+  ANNF_CHECK_LAUNCH();
+  prof_mark(h, "project", st);
+  return ANNF_OK;
+}
+
+}  // namespace annf

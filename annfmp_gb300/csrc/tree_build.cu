@@ -1,0 +1,703 @@
+// tree_build.cu -- level-synchronous k-d tree build on the GPU (sm_103a).
+//
+// Reproduces the reference build bit for bit (annfmp/openmp/kdtree/src/kdtree.c:76-117, 363-489,
+// helper.c:63-113, util.c:146-186):
+//   * node ranges are data-independent: a node over count points gives its left child the first
+//     count/2 positions and its right child the rest;
+//   * axis = first axis whose bounding-box width (max - min, rounded) is strictly the largest;
+//   * pivot = the order statistic of rank count/2 on that axis (any exact selection agrees);
+//   * element order after the split: "< pivot" elements in input order, then ">= pivot" elements
+//     in reverse input order, then a forward pass that swaps the elements equal to the pivot, in
+//     the order met, to the front of the ">=" block; split value = element at position count/2.
+//
+// Large segments (top levels) are processed by many CTAs per segment: bounding box (atomics on
+// order-preserving keys), an 8-bit-digit radix select, per-chunk counts + scan + a stable scatter,
+// and a one-warp fix-up for the equal elements. When a level's segments fit in shared memory, one
+// CTA per segment finishes the whole subtree in shared memory (bounding box, radix select and
+// stable partition on a 16-bit index permutation) and writes the points out once, in leaf order.
+#include <algorithm>
+#include <vector>
+
+#include "common.cuh"
+#include "handle.cuh"
+
+namespace annf {
+
+constexpr int kChunk = 4096;     // positions per CTA in the global levels
+constexpr int kThreads = 256;
+constexpr int kItems = kChunk / kThreads;
+
+// [lo, hi) of node j (0-based within its level) at level t of a tree over n points
+__device__ __forceinline__ void seg_range(int n, int t, int j, int& lo, int& hi) {
+  int a = 0, c = n;
+  for (int b = t - 1; b >= 0; --b) {
+    int half = c >> 1;
+    if ((j >> b) & 1) {
+      a += half;
+      c -= half;
+    } else {
+      c = half;
+    }
+  }
+  lo = a;
+  hi = a + c;
+}
+
+template <typename K> __device__ __forceinline__ K key_max();
+template <> __device__ __forceinline__ uint32_t key_max<uint32_t>() { return 0xffffffffu; }
+template <> __device__ __forceinline__ unsigned long long key_max<unsigned long long>() { return ~0ull; }
+
+template <typename K>
+__global__ void fill_keys_kernel(K* a, long long cnt, K v) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < cnt; i += (long long)gridDim.x * blockDim.x) a[i] = v;
+}
+
+__global__ void iota_kernel(int* a, int n) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) a[i] = i;
+}
+
+// ---------------------------------------------------------------------------------------------
+// global levels
+// ---------------------------------------------------------------------------------------------
+// bounding box: threads are laid out so that each one always reads the same dimension
+template <typename T>
+__global__ void bbox_kernel(int n, int d, int t, int B, const T* __restrict__ pts,
+                            typename key_of<T>::type* gmin, typename key_of<T>::type* gmax) {
+  using K = typename key_of<T>::type;
+  __shared__ K smin[kThreads], smax[kThreads];
+  const int s = blockIdx.x / B, bb = blockIdx.x % B;
+  int lo, hi;
+  seg_range(n, t, s, lo, hi);
+  const int c0 = lo + bb * kChunk, c1 = min(hi, c0 + kChunk);
+  const int used = (kThreads / d) * d;  // stride that keeps each thread on one dimension
+  K kmn = key_max<K>(), kmx = 0;
+  if ((int)threadIdx.x < used && c0 < c1) {
+    const long long e0 = (long long)c0 * d, e1 = (long long)c1 * d;
+    for (long long e = e0 + threadIdx.x; e < e1; e += used) {
+      K k = ord_key(pts[e]);
+      kmn = k < kmn ? k : kmn;
+      kmx = k > kmx ? k : kmx;
+    }
+  }
+  smin[threadIdx.x] = kmn;
+  smax[threadIdx.x] = kmx;
+  __syncthreads();
+  if ((int)threadIdx.x < d && c0 < c1) {
+    for (int u = threadIdx.x + d; u < used; u += d) {
+      kmn = smin[u] < kmn ? smin[u] : kmn;
+      kmx = smax[u] > kmx ? smax[u] : kmx;
+    }
+    atomicMin(&gmin[(long long)s * d + threadIdx.x], kmn);
+    atomicMax(&gmax[(long long)s * d + threadIdx.x], kmx);
+  }
+}
+
+template <typename T>
+__global__ void axis_kernel(int n, int d, int t, int S, int splitting, const typename key_of<T>::type* gmin,
+                            const typename key_of<T>::type* gmax, int* axis,
+                            typename key_of<T>::type* prefix, int* rank, int* nlt) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= S) return;
+  int lo, hi;
+  seg_range(n, t, s, lo, hi);
+  T best = 0;
+  int ax = 0;
+  for (int j = 0; j < d; ++j) {
+    T mn, mx;
+    if constexpr (sizeof(T) == 4) {
+      mn = key_to_float((uint32_t)gmin[(long long)s * d + j]);
+      mx = key_to_float((uint32_t)gmax[(long long)s * d + j]);
+    } else {
+      mn = key_to_real(gmin[(long long)s * d + j]);
+      mx = key_to_real(gmax[(long long)s * d + j]);
+    }
+    T w = real_traits<T>::sub(mx, mn);
+    if (w > best) {
+      best = w;
+      ax = j;
+    }
+  }
+  axis[s] = splitting == 0 ? t % d : ax;  // cyclic: node depth mod d (kdtree.c:369-371)
+  prefix[s] = 0;
+  rank[s] = (hi - lo) / 2;
+  nlt[s] = 0;
+}
+
+template <typename T>
+__global__ void extract_keys_kernel(int n, int d, int t, int B, const T* __restrict__ pts,
+                                    const int* __restrict__ axis, typename key_of<T>::type* keys) {
+  const int s = blockIdx.x / B, bb = blockIdx.x % B;
+  int lo, hi;
+  seg_range(n, t, s, lo, hi);
+  const int c0 = lo + bb * kChunk, c1 = min(hi, c0 + kChunk);
+  const int ax = axis[s];
+  for (int i = c0 + threadIdx.x; i < c1; i += blockDim.x) keys[i] = ord_key(pts[(long long)i * d + ax]);
+}
+
+template <typename K>
+__global__ void hist_kernel(int n, int t, int B, int shift, const K* __restrict__ keys,
+                            const K* __restrict__ prefix, unsigned* ghist) {
+  __shared__ unsigned h[256];
+  const int s = blockIdx.x / B, bb = blockIdx.x % B;
+  int lo, hi;
+  seg_range(n, t, s, lo, hi);
+  const int c0 = lo + bb * kChunk, c1 = min(hi, c0 + kChunk);
+  h[threadIdx.x] = 0;
+  __syncthreads();
+  const K pre = prefix[s];
+  const K hmask = (shift + 8 >= (int)(8 * sizeof(K))) ? (K)0 : (~(K)0 << (shift + 8));
+  for (int i = c0 + threadIdx.x; i < c1; i += blockDim.x) {
+    K k = keys[i];
+    if (((k ^ pre) & hmask) == 0) atomicAdd(&h[(unsigned)(k >> shift) & 255u], 1u);
+  }
+  __syncthreads();
+  unsigned v = h[threadIdx.x];
+  if (v) atomicAdd(&ghist[(long long)s * 256 + threadIdx.x], v);
+}
+
+// block-wide exclusive scan of two counters (kThreads threads)
+__device__ __forceinline__ void block_excl_scan2(int a, int b, int& ea, int& eb, int& ta, int& tb) {
+  __shared__ int wa[kThreads / 32], wb[kThreads / 32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  int ia = a, ib = b;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    int xa = __shfl_up_sync(0xffffffffu, ia, o), xb = __shfl_up_sync(0xffffffffu, ib, o);
+    if (lane >= o) {
+      ia += xa;
+      ib += xb;
+    }
+  }
+  if (lane == 31) {
+    wa[w] = ia;
+    wb[w] = ib;
+  }
+  __syncthreads();
+  int pa = 0, pb = 0, sa = 0, sb = 0;
+  for (int u = 0; u < kThreads / 32; ++u) {
+    if (u < w) {
+      pa += wa[u];
+      pb += wb[u];
+    }
+    sa += wa[u];
+    sb += wb[u];
+  }
+  ea = pa + ia - a;
+  eb = pb + ib - b;
+  ta = sa;
+  tb = sb;
+  __syncthreads();
+}
+
+template <typename K>
+__global__ void pick_kernel(int shift, bool last, unsigned* ghist, K* prefix, int* rank, int* nlt,
+                            int* neq) {
+  const int s = blockIdx.x;
+  unsigned* h = ghist + (long long)s * 256;
+  int c = (int)h[threadIdx.x];
+  h[threadIdx.x] = 0;  // ready for the next pass
+  int ex, dummy_e, tot, dummy_t;
+  block_excl_scan2(c, 0, ex, dummy_e, tot, dummy_t);
+  const int r = rank[s];
+  __syncthreads();
+  if (ex <= r && r < ex + c) {
+    prefix[s] |= ((K)threadIdx.x) << shift;
+    rank[s] = r - ex;
+    nlt[s] += ex;
+    if (last) neq[s] = c;
+  }
+}
+
+template <typename K>
+__global__ void count_kernel(int n, int t, int B, const K* __restrict__ keys, const K* __restrict__ pivot,
+                             int* blk_lt, int* blk_eq) {
+  const int s = blockIdx.x / B, bb = blockIdx.x % B;
+  int lo, hi;
+  seg_range(n, t, s, lo, hi);
+  const int c0 = lo + bb * kChunk, c1 = min(hi, c0 + kChunk);
+  const K pv = pivot[s];
+  int lt = 0, eq = 0;
+  for (int i = c0 + threadIdx.x; i < c1; i += blockDim.x) {
+    K k = keys[i];
+    lt += k < pv;
+    eq += k == pv;
+  }
+  int e1, e2, t1, t2;
+  block_excl_scan2(lt, eq, e1, e2, t1, t2);
+  if (threadIdx.x == 0) {
+    blk_lt[blockIdx.x] = t1;
+    blk_eq[blockIdx.x] = t2;
+  }
+}
+
+__global__ void seg_scan_kernel(int S, int B, const int* blk_lt, const int* blk_eq, int* off_lt, int* off_eq) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= S) return;
+  int a = 0, b = 0;
+  for (int u = 0; u < B; ++u) {
+    off_lt[(long long)s * B + u] = a;
+    off_eq[(long long)s * B + u] = b;
+    a += blk_lt[(long long)s * B + u];
+    b += blk_eq[(long long)s * B + u];
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kThreads) scatter_kernel(
+    int n, int d, int t, int B, const typename key_of<T>::type* __restrict__ keys,
+    const typename key_of<T>::type* __restrict__ pivot, const int* __restrict__ nlt,
+    const int* __restrict__ neq, const int* __restrict__ off_lt, const int* __restrict__ off_eq,
+    const T* __restrict__ pts_in, const int* __restrict__ perm_in, T* __restrict__ pts_out,
+    int* __restrict__ perm_out, int* __restrict__ eqpos) {
+  using K = typename key_of<T>::type;
+  __shared__ int sdst[kChunk];
+  const int s = blockIdx.x / B, bb = blockIdx.x % B;
+  int lo, hi;
+  seg_range(n, t, s, lo, hi);
+  const int c0 = lo + bb * kChunk, c1 = min(hi, c0 + kChunk);
+  const int m = c1 - c0;
+  if (m <= 0) return;  // uniform per block
+  const K pv = pivot[s];
+  const int base = threadIdx.x * kItems;
+  unsigned flt = 0, feq = 0;
+  int mlt = 0, meq = 0;
+#pragma unroll
+  for (int q = 0; q < kItems; ++q) {
+    int i = base + q;
+    if (i < m) {
+      K k = keys[c0 + i];
+      if (k < pv) {
+        flt |= 1u << q;
+        ++mlt;
+      } else if (k == pv) {
+        feq |= 1u << q;
+        ++meq;
+      }
+    }
+  }
+  int elt, eeq, tl, te;
+  block_excl_scan2(mlt, meq, elt, eeq, tl, te);
+  int lt_before = off_lt[blockIdx.x] + elt;
+  int eq_before = off_eq[blockIdx.x] + eeq;
+  const int seg_neq = neq[s];
+#pragma unroll
+  for (int q = 0; q < kItems; ++q) {
+    int i = base + q;
+    if (i < m) {
+      int r = (c0 - lo) + i;  // rank of the element in its segment (input order)
+      int dst;
+      if ((flt >> q) & 1u) {
+        dst = lo + lt_before;
+        ++lt_before;
+      } else {
+        dst = hi - 1 - (r - lt_before);  // ">=" elements fill from the back
+        if ((feq >> q) & 1u) {
+          eqpos[lo + (seg_neq - 1 - eq_before)] = dst;  // ascending position order
+          ++eq_before;
+        }
+      }
+      sdst[i] = dst;
+    }
+  }
+  __syncthreads();
+  const long long tot = (long long)m * d;
+  for (long long e = threadIdx.x; e < tot; e += blockDim.x) {
+    int r = (int)(e / d), c = (int)(e - (long long)r * d);
+    pts_out[(long long)sdst[r] * d + c] = pts_in[(long long)(c0 + r) * d + c];
+  }
+  for (int i = threadIdx.x; i < m; i += blockDim.x) perm_out[sdst[i]] = perm_in[c0 + i];
+  (void)nlt;
+}
+
+// one warp per segment: the reference's forward swap pass over the equal elements, then the node
+template <typename T>
+__global__ void fixup_kernel(int n, int d, int t, int S, const int* __restrict__ axis,
+                             const int* __restrict__ nlt, const int* __restrict__ neq,
+                             const int* __restrict__ eqpos, T* pts, int* perm, int* node_axis,
+                             T* node_split) {
+  const int s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (s >= S) return;
+  int lo, hi;
+  seg_range(n, t, s, lo, hi);
+  const int m = neq[s], h0 = lo + nlt[s];
+  for (int j = 0; j < m; ++j) {
+    const int p = eqpos[lo + j], q = h0 + j;
+    if (p != q) {
+      for (int c = lane; c < d; c += 32) {
+        T a = pts[(long long)p * d + c];
+        pts[(long long)p * d + c] = pts[(long long)q * d + c];
+        pts[(long long)q * d + c] = a;
+      }
+      if (lane == 0) {
+        int a = perm[p];
+        perm[p] = perm[q];
+        perm[q] = a;
+      }
+    }
+    __syncwarp();
+  }
+  if (lane == 0) {
+    const int node = (1 << t) - 1 + s;
+    const int ax = axis[s];
+    node_axis[node] = ax;
+    node_split[node] = pts[(long long)(lo + (hi - lo) / 2) * d + ax];
+  }
+}
+
+// leaves produced by the global levels (depth reached without the shared-memory finisher)
+__global__ void leaves_kernel(int n, int depth, int B, const int* __restrict__ perm, int* leaf_begin,
+                              int* point_leaf) {
+  const int s = blockIdx.x / B, bb = blockIdx.x % B;
+  int lo, hi;
+  seg_range(n, depth, s, lo, hi);
+  const int c0 = lo + bb * kChunk, c1 = min(hi, c0 + kChunk);
+  if (bb == 0 && threadIdx.x == 0) {
+    leaf_begin[s] = lo;
+    if (s == (1 << depth) - 1) leaf_begin[s + 1] = n;
+  }
+  for (int i = c0 + threadIdx.x; i < c1; i += blockDim.x) point_leaf[perm[i]] = s;
+}
+
+// ---------------------------------------------------------------------------------------------
+// shared-memory subtree finisher: one CTA per segment of level t0, levels t0..depth-1
+// ---------------------------------------------------------------------------------------------
+constexpr int kSubThreads = 256;
+constexpr int kSubWarps = kSubThreads / 32;
+
+template <typename T>
+__global__ void __launch_bounds__(kSubThreads) subtree_kernel(
+    int n, int d, int depth, int t0, int smax, int splitting, const T* __restrict__ pts_in,
+    const int* __restrict__ perm_in, T* __restrict__ pts_out, int* __restrict__ perm_out,
+    int* __restrict__ node_axis, T* __restrict__ node_split, int* __restrict__ leaf_begin,
+    int* __restrict__ point_leaf) {
+  using K = typename key_of<T>::type;
+  extern __shared__ __align__(16) unsigned char smem[];
+  T* spts = reinterpret_cast<T*>(smem);
+  K* skey = reinterpret_cast<K*>(spts + (size_t)smax * d);
+  int* sperm = reinterpret_cast<int*>(skey + smax);
+  unsigned* shist = reinterpret_cast<unsigned*>(sperm + smax);
+  uint16_t* sidx0 = reinterpret_cast<uint16_t*>(shist + kSubWarps * 256);
+  uint16_t* sidx1 = sidx0 + smax;
+
+  const int s = blockIdx.x;
+  int lo, hi;
+  seg_range(n, t0, s, lo, hi);
+  const int cnt = hi - lo;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+
+  for (long long e = threadIdx.x; e < (long long)cnt * d; e += blockDim.x) spts[e] = pts_in[(long long)lo * d + e];
+  for (int i = threadIdx.x; i < cnt; i += blockDim.x) {
+    sperm[i] = perm_in[lo + i];
+    sidx0[i] = (uint16_t)i;
+  }
+  __syncthreads();
+
+  uint16_t* cur = sidx0;
+  uint16_t* nxt = sidx1;
+  unsigned* hist = shist + warp * 256;
+  constexpr int kBits = 8 * sizeof(K);
+
+  for (int l = t0; l < depth; ++l) {
+    const int nsub = 1 << (l - t0);
+    for (int u = warp; u < nsub; u += kSubWarps) {
+      int a, b;
+      seg_range(cnt, l - t0, u, a, b);
+      const int m = b - a, half = m / 2;
+      // --- widest axis (or cyclic) ---
+      T best = 0;
+      int axis = splitting == 0 ? l % d : 0;
+      for (int j = 0; splitting != 0 && j < d; ++j) {
+        T mn = real_traits<T>::big(), mx = -real_traits<T>::big();
+        for (int i = a + lane; i < b; i += 32) {
+          T v = spts[(size_t)cur[i] * d + j];
+          mn = v < mn ? v : mn;
+          mx = v > mx ? v : mx;
+        }
+#pragma unroll
+        for (int o = 16; o; o >>= 1) {
+          T omn = __shfl_xor_sync(0xffffffffu, mn, o), omx = __shfl_xor_sync(0xffffffffu, mx, o);
+          mn = omn < mn ? omn : mn;
+          mx = omx > mx ? omx : mx;
+        }
+        T w = real_traits<T>::sub(mx, mn);
+        if (w > best) {
+          best = w;
+          axis = j;
+        }
+      }
+      // --- keys + radix select of rank 'half' ---
+      for (int i = a + lane; i < b; i += 32) skey[i] = ord_key(spts[(size_t)cur[i] * d + axis]);
+      K prefix = 0;
+      int rank = half, nlt = 0;
+      for (int shift = kBits - 8; shift >= 0; shift -= 8) {
+        for (int z = lane; z < 256; z += 32) hist[z] = 0;
+        __syncwarp();
+        const K hmask = (shift + 8 >= kBits) ? (K)0 : (~(K)0 << (shift + 8));
+        for (int i = a + lane; i < b; i += 32) {
+          K k = skey[i];
+          if (((k ^ prefix) & hmask) == 0) atomicAdd(&hist[(unsigned)(k >> shift) & 255u], 1u);
+        }
+        __syncwarp();
+        // lane owns bins [8*lane, 8*lane+8)
+        int c[8], tot = 0;
+#pragma unroll
+        for (int z = 0; z < 8; ++z) {
+          c[z] = (int)hist[8 * lane + z];
+          tot += c[z];
+        }
+        int inc = tot;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          int x = __shfl_up_sync(0xffffffffu, inc, o);
+          if (lane >= o) inc += x;
+        }
+        int ex = inc - tot;
+        unsigned own = __ballot_sync(0xffffffffu, ex <= rank && rank < inc);
+        int src = __ffs(own) - 1;
+        int bin = 0, before = 0;
+        if (lane == src) {
+          int run = ex;
+#pragma unroll
+          for (int z = 0; z < 8; ++z) {
+            if (run <= rank && rank < run + c[z]) {
+              bin = 8 * lane + z;
+              before = run;
+            }
+            run += c[z];
+          }
+        }
+        bin = __shfl_sync(0xffffffffu, bin, src);
+        before = __shfl_sync(0xffffffffu, before, src);
+        prefix |= ((K)bin) << shift;
+        nlt += before;
+        rank -= before;
+        __syncwarp();
+      }
+      const K pivot = prefix;
+      // --- stable partition: "<" forward, ">=" from the back ---
+      int ltb = 0, geb = 0;
+      for (int base = a; base < b; base += 32) {
+        const int i = base + lane;
+        const bool valid = i < b;
+        const K k = valid ? skey[i] : (K)0;
+        const bool lt = valid && (k < pivot), ge = valid && !(k < pivot);
+        const unsigned mlt = __ballot_sync(0xffffffffu, lt), mge = __ballot_sync(0xffffffffu, ge);
+        const unsigned below = (1u << lane) - 1u;
+        if (lt) nxt[a + ltb + __popc(mlt & below)] = cur[i];
+        if (ge) nxt[b - 1 - (geb + __popc(mge & below))] = cur[i];
+        ltb += __popc(mlt);
+        geb += __popc(mge);
+      }
+      __syncwarp();
+      // --- forward swap pass of the equal elements over the ">=" block ---
+      int w = a + nlt;
+      for (int base = a + nlt; base < b; base += 32) {
+        const int i = base + lane;
+        const bool eq = i < b && ord_key(spts[(size_t)nxt[i] * d + axis]) == pivot;
+        unsigned msk = __ballot_sync(0xffffffffu, eq);
+        while (msk) {
+          const int p = base + __ffs(msk) - 1;
+          msk &= msk - 1;
+          if (lane == 0 && p != w) {
+            uint16_t tmp = nxt[p];
+            nxt[p] = nxt[w];
+            nxt[w] = tmp;
+          }
+          ++w;
+          __syncwarp();
+        }
+      }
+      if (lane == 0) {
+        const int node = (1 << l) - 1 + (s << (l - t0)) + u;
+        node_axis[node] = axis;
+        node_split[node] = spts[(size_t)nxt[a + half] * d + axis];
+      }
+      // positions of this sub-segment that were not rewritten keep nothing stale: every position
+      // in [a,b) was written by the partition above
+    }
+    __syncthreads();
+    uint16_t* tmp = cur;
+    cur = nxt;
+    nxt = tmp;
+  }
+  // leaves of this subtree
+  const int nleaf = 1 << (depth - t0);
+  for (int u = warp; u < nleaf; u += kSubWarps) {
+    int a, b;
+    seg_range(cnt, depth - t0, u, a, b);
+    const int leaf = (s << (depth - t0)) + u;
+    if (lane == 0) {
+      leaf_begin[leaf] = lo + a;
+      if (leaf == (1 << depth) - 1) leaf_begin[leaf + 1] = n;
+    }
+    for (int i = a + lane; i < b; i += 32) point_leaf[sperm[cur[i]]] = leaf;
+  }
+  for (long long e = threadIdx.x; e < (long long)cnt * d; e += blockDim.x) {
+    const int r = (int)(e / d), c = (int)(e - (long long)r * d);
+    pts_out[(long long)(lo + r) * d + c] = spts[(size_t)cur[r] * d + c];
+  }
+  for (int i = threadIdx.x; i < cnt; i += blockDim.x) perm_out[lo + i] = sperm[cur[i]];
+}
+
+template <typename T>
+static size_t subtree_smem(int smax, int d) {
+  using K = typename key_of<T>::type;
+  return (size_t)smax * d * sizeof(T) + (size_t)smax * sizeof(K) + (size_t)smax * sizeof(int) +
+         kSubWarps * 256 * sizeof(unsigned) + 2 * (size_t)smax * sizeof(uint16_t);
+}
+
+template <typename T>
+static int subtree_capacity(int d) {
+  const size_t budget = 200 * 1024;
+  int smax = 4096;
+  while (smax > 1 && subtree_smem<T>(smax, d) > budget) smax >>= 1;
+  return smax;
+}
+
+template <typename T>
+static int build_impl(annf_handle* h, const T* points, int n, int d, int depth, int splitting, cudaStream_t st) {
+  using K = typename key_of<T>::type;
+  const int L = 1 << depth;
+  ANNF_ENSURE(h->pts, (size_t)n * d * sizeof(T));
+  ANNF_ENSURE(h->pts_tmp, (size_t)n * d * sizeof(T));
+  ANNF_ENSURE(h->perm, (size_t)n * sizeof(int));
+  ANNF_ENSURE(h->perm_tmp, (size_t)n * sizeof(int));
+  ANNF_ENSURE(h->node_axis, (size_t)std::max(L - 1, 1) * sizeof(int));
+  ANNF_ENSURE(h->node_split, (size_t)std::max(L - 1, 1) * sizeof(T));
+  ANNF_ENSURE(h->leaf_begin, (size_t)(L + 1) * sizeof(int));
+  ANNF_ENSURE(h->point_leaf, (size_t)n * sizeof(int));
+  ANNF_ENSURE(h->keys, (size_t)n * sizeof(K));
+  ANNF_ENSURE(h->eqpos, (size_t)n * sizeof(int));
+
+  T* cur_pts = h->pts.as<T>();
+  T* alt_pts = h->pts_tmp.as<T>();
+  int* cur_perm = h->perm.as<int>();
+  int* alt_perm = h->perm_tmp.as<int>();
+  prof_mark(h, "build:begin", st);
+  ANNF_CUDA_TRY(cudaMemcpyAsync(cur_pts, points, (size_t)n * d * sizeof(T), cudaMemcpyDeviceToDevice, st));
+  iota_kernel<<<std::min(ceil_div(n, 256), 4096), 256, 0, st>>>(cur_perm, n);
+  ANNF_CHECK_LAUNCH();
+
+  const int smax = subtree_capacity<T>(d);
+  const size_t sub_smem = subtree_smem<T>(smax, d);
+  bool finished = false;
+  for (int t = 0; t < depth; ++t) {
+    const int S = 1 << t;
+    const int maxcnt = (int)(((long long)n + S - 1) / S);
+    if (maxcnt <= smax) {
+      ANNF_CUDA_TRY(cudaFuncSetAttribute(subtree_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sub_smem));
+      subtree_kernel<T><<<S, kSubThreads, sub_smem, st>>>(
+          n, d, depth, t, smax, splitting, cur_pts, cur_perm, alt_pts, alt_perm, h->node_axis.as<int>(),
+          h->node_split.as<T>(), h->leaf_begin.as<int>(), h->point_leaf.as<int>());
+      ANNF_CHECK_LAUNCH();
+      std::swap(cur_pts, alt_pts);
+      std::swap(cur_perm, alt_perm);
+      finished = true;
+      prof_mark(h, "build_subtree", st);
+      break;
+    }
+    const int B = ceil_div(maxcnt, kChunk);
+    const long long nblk = (long long)S * B;
+    if (nblk > 0x7fffffffLL) {
+      set_error("tree too large for the level kernels");
+      return ANNF_ERR_UNSUPPORTED;
+    }
+    ANNF_ENSURE(h->bmin, (size_t)S * d * sizeof(K));
+    ANNF_ENSURE(h->bmax, (size_t)S * d * sizeof(K));
+    ANNF_ENSURE(h->axis, (size_t)S * sizeof(int));
+    ANNF_ENSURE(h->sel_prefix, (size_t)S * sizeof(K));
+    ANNF_ENSURE(h->sel_rank, (size_t)S * sizeof(int));
+    ANNF_ENSURE(h->sel_nlt, (size_t)S * sizeof(int));
+    ANNF_ENSURE(h->sel_neq, (size_t)S * sizeof(int));
+    ANNF_ENSURE(h->hist, (size_t)S * 256 * sizeof(unsigned));
+    ANNF_ENSURE(h->blk_lt, (size_t)nblk * sizeof(int));
+    ANNF_ENSURE(h->blk_eq, (size_t)nblk * sizeof(int));
+    ANNF_ENSURE(h->off_lt, (size_t)nblk * sizeof(int));
+    ANNF_ENSURE(h->off_eq, (size_t)nblk * sizeof(int));
+    K* gmin = h->bmin.as<K>();
+    K* gmax = h->bmax.as<K>();
+    const int fb = std::min(ceil_div((long long)S * d, 256), 4096);
+    fill_keys_kernel<K><<<fb, 256, 0, st>>>(gmin, (long long)S * d, ~(K)0);
+    ANNF_CHECK_LAUNCH();
+    fill_keys_kernel<K><<<fb, 256, 0, st>>>(gmax, (long long)S * d, (K)0);
+    ANNF_CHECK_LAUNCH();
+    ANNF_CUDA_TRY(cudaMemsetAsync(h->hist.p, 0, (size_t)S * 256 * sizeof(unsigned), st));
+    bbox_kernel<T><<<(unsigned)nblk, kThreads, 0, st>>>(n, d, t, B, cur_pts, gmin, gmax);
+    ANNF_CHECK_LAUNCH();
+    axis_kernel<T><<<ceil_div(S, 128), 128, 0, st>>>(n, d, t, S, splitting, gmin, gmax, h->axis.as<int>(),
+                                                   h->sel_prefix.as<K>(), h->sel_rank.as<int>(),
+                                                   h->sel_nlt.as<int>());
+    ANNF_CHECK_LAUNCH();
+    extract_keys_kernel<T><<<(unsigned)nblk, kThreads, 0, st>>>(n, d, t, B, cur_pts, h->axis.as<int>(), h->keys.as<K>());
+    ANNF_CHECK_LAUNCH();
+    constexpr int kBits = 8 * sizeof(K);
+    for (int shift = kBits - 8; shift >= 0; shift -= 8) {
+      hist_kernel<K><<<(unsigned)nblk, 256, 0, st>>>(n, t, B, shift, h->keys.as<K>(), h->sel_prefix.as<K>(), h->hist.as<unsigned>());
+      ANNF_CHECK_LAUNCH();
+      pick_kernel<K><<<S, 256, 0, st>>>(shift, shift == 0, h->hist.as<unsigned>(), h->sel_prefix.as<K>(),
+                                        h->sel_rank.as<int>(), h->sel_nlt.as<int>(), h->sel_neq.as<int>());
+      ANNF_CHECK_LAUNCH();
+    }
+    count_kernel<K><<<(unsigned)nblk, kThreads, 0, st>>>(n, t, B, h->keys.as<K>(), h->sel_prefix.as<K>(),
+                                                        h->blk_lt.as<int>(), h->blk_eq.as<int>());
+    ANNF_CHECK_LAUNCH();
+    seg_scan_kernel<<<ceil_div(S, 128), 128, 0, st>>>(S, B, h->blk_lt.as<int>(), h->blk_eq.as<int>(),
+                                                      h->off_lt.as<int>(), h->off_eq.as<int>());
+    ANNF_CHECK_LAUNCH();
+    scatter_kernel<T><<<(unsigned)nblk, kThreads, 0, st>>>(
+        n, d, t, B, h->keys.as<K>(), h->sel_prefix.as<K>(), h->sel_nlt.as<int>(), h->sel_neq.as<int>(),
+        h->off_lt.as<int>(), h->off_eq.as<int>(), cur_pts, cur_perm, alt_pts, alt_perm, h->eqpos.as<int>());
+    ANNF_CHECK_LAUNCH();
+    fixup_kernel<T><<<ceil_div((long long)S * 32, 256), 256, 0, st>>>(
+        n, d, t, S, h->axis.as<int>(), h->sel_nlt.as<int>(), h->sel_neq.as<int>(), h->eqpos.as<int>(),
+        alt_pts, alt_perm, h->node_axis.as<int>(), h->node_split.as<T>());
+    ANNF_CHECK_LAUNCH();
+    std::swap(cur_pts, alt_pts);
+    std::swap(cur_perm, alt_perm);
+    prof_mark(h, "build_level", st);
+  }
+  if (!finished) {
+    const int S = L;
+    const int maxcnt = (int)(((long long)n + S - 1) / S);
+    const int B = ceil_div(maxcnt, kChunk);
+    leaves_kernel<<<(unsigned)((long long)S * B), kThreads, 0, st>>>(n, depth, B, cur_perm,
+                                                                    h->leaf_begin.as<int>(), h->point_leaf.as<int>());
+    ANNF_CHECK_LAUNCH();
+  }
+  // the final arrays live in h->pts / h->perm
+  if (cur_pts != h->pts.as<T>()) std::swap(h->pts, h->pts_tmp);
+  if (cur_perm != h->perm.as<int>()) std::swap(h->perm, h->perm_tmp);
+  const int maxleaf = (int)(((long long)n + L - 1) / L);
+  int bits = 1;
+  while ((1LL << bits) <= maxleaf) ++bits;
+  h->leaf_bits = bits;
+  h->max_leaf = maxleaf;
+  return ANNF_OK;
+}
+
+int build_tree(annf_handle* h, const void* points, int n, int d, int real_type, int depth, int splitting,
+               cudaStream_t st) {
+  ANNF_REQUIRE(points != nullptr, "annf_build_tree: points is NULL");
+  ANNF_REQUIRE(n >= 1 && d >= 1, "annf_build_tree: need n >= 1 and d >= 1");
+  ANNF_REQUIRE(d <= 128, "annf_build_tree: d > 128 is not supported");
+  ANNF_REQUIRE(depth >= 0 && depth <= 30 && (1LL << depth) <= n,
+               "annf_build_tree: depth must satisfy 0 <= depth and 2^depth <= n");
+  ANNF_REQUIRE(real_type == ANNF_REAL_F32 || real_type == ANNF_REAL_F64, "annf_build_tree: bad real_type");
+  ANNF_REQUIRE(splitting == ANNF_SPLIT_CYCLIC || splitting == ANNF_SPLIT_LONGEST, "annf_build_tree: bad splitting_type");
+  h->built = 0;
+  int rc = (real_type == ANNF_REAL_F32) ? build_impl<float>(h, static_cast<const float*>(points), n, d, depth, splitting, st)
+                                        : build_impl<double>(h, static_cast<const double*>(points), n, d, depth, splitting, st);
+  if (rc != ANNF_OK) return rc;
+  h->n = n;
+  h->d = d;
+  h->depth = depth;
+  h->real_type = real_type;
+  if (depth + h->leaf_bits > 32) {
+    set_error("annf_build_tree: depth + log2(leaf size) exceeds 32 bits of tie-break");
+    return ANNF_ERR_UNSUPPORTED;
+  }
+  h->built = 1;
+  return ANNF_OK;
+}
+
+}  // namespace annf

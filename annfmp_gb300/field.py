@@ -1,0 +1,198 @@
+"""ANNFieldPropKDTreeGB300: the reference's OpenMP NNF pipeline (annfmp/openmp/base.py:16-218),
+re-built for one GB300 GPU.
+
+Same constructor parameters, ``fit(image_a, image_b)`` returning one int32 B-patch index per A
+pixel (row-major), ``patches_a`` / ``patches_b`` properties and per-stage ``_timers``. Stages:
+
+1. PCA fit on n_subset/2 sampled patches of A (RandomState(seed)) and of B (seed+1), exactly as
+   scikit-learn's extract_patches_2d samples them; exact Gram matrix, FP64 covariance, FP64 eigh,
+   all on the GPU (``annf_pca_fit``);
+2. patch extraction fused into the projection: every patch of A and B is projected straight from
+   the image (``annf_project``) -- the reference's 1 GB-scale uint8 patch arrays and 8 GB FP64
+   copies never exist;
+3. k-d tree over B's reduced patches (``annf_build_tree``, longest-axis splits);
+4. exact first row, row propagation, raw-patch re-rank (``annf_process_rows_img``).
+
+Extensions (not in the reference): ``nn_distances_`` (raw-patch L2 of each chosen index),
+``knn_indices_`` (each pixel's k-list), torch CUDA tensors accepted as images (results then stay
+on the device).
+"""
+from __future__ import annotations
+
+import collections
+
+import numpy
+import torch
+
+from . import _lib
+from ._torch import is_numpy, ptr, require_cuda, stream_ptr, to_device
+from .kdtree import KDTree
+
+
+class _SubsetCache:
+    """Sampled patch positions depend only on (patch grid, count, seed): keep them on the device."""
+
+    def __init__(self):
+        self._d = collections.OrderedDict()
+
+    def get(self, n_h, n_w, m, seed, device):
+        key = (n_h, n_w, m, seed, str(device))
+        if key in self._d:
+            self._d.move_to_end(key)
+            return self._d[key]
+        total = n_h * n_w
+        if not m or m >= total:  # sklearn _compute_n_patches: every patch
+            yy, xx = torch.meshgrid(torch.arange(n_h, device=device, dtype=torch.int32),
+                                    torch.arange(n_w, device=device, dtype=torch.int32), indexing="ij")
+            pos = torch.stack([yy.reshape(-1), xx.reshape(-1)], dim=1).contiguous()
+        else:
+            rs = numpy.random.RandomState(seed)
+            i_s = rs.randint(n_h, size=m)
+            j_s = rs.randint(n_w, size=m)
+            pos = torch.from_numpy(numpy.stack([i_s, j_s], axis=1).astype(numpy.int32)).to(device)
+        self._d[key] = pos
+        while len(self._d) > 16:
+            self._d.popitem(last=False)
+        return pos
+
+
+_SUBSETS = _SubsetCache()
+
+
+class ANNFieldPropKDTreeGB300:
+    def __init__(self, n_neighbors=3, psize=8, dim_reduced=5, n_subset=1000, leaf_size=64, n_jobs=-1,
+                 propagate=True, select_best_nn=True, float_type="float", verbose=1, seed=0, device=0):
+        self.n_neighbors = n_neighbors
+        self.psize = psize
+        self.dim_reduced = dim_reduced
+        self.n_subset = n_subset
+        self.leaf_size = leaf_size
+        self.n_jobs = n_jobs
+        self.propagate = propagate
+        self.select_best_nn = select_best_nn
+        self.float_type = float_type
+        self.verbose = verbose
+        self.seed = seed
+        self.device = device
+
+    def _get_torch_float_type(self):
+        if self.float_type == "float":
+            return torch.float32
+        elif self.float_type == "double":
+            return torch.float64
+        raise Exception("Unknown float type: {}".format(self.float_type))
+
+    def fit(self, image_a, image_b):
+        """image_a and image_b have shape (h, w, c), uint8 (numpy or torch)."""
+        numpy.random.seed(self.seed)  # annfmp/openmp/base.py:60
+        dev = require_cuda(self.device)
+        real = self._get_torch_float_type()
+        real_type = _lib.ANNF_REAL_F32 if real == torch.float32 else _lib.ANNF_REAL_F64
+        numpy_io = is_numpy(image_a)
+        self.image_a = image_a
+        self.image_b = image_b
+        A = to_device(image_a, torch.uint8, dev)
+        B = to_device(image_b, torch.uint8, dev)
+        if A.dim() == 2:
+            A = A.unsqueeze(-1)
+        if B.dim() == 2:
+            B = B.unsqueeze(-1)
+        if A.shape[2] != B.shape[2]:
+            raise ValueError("images must have the same number of channels")
+        ha, wa, c = A.shape
+        hb, wb, _ = B.shape
+        p = int(self.psize)
+        if p > min(ha, wa, hb, wb):
+            raise ValueError("Height/width of the patch should be less than the height/width of the image.")
+        self._n_cols = wa - p + 1
+        self._n_rows = ha - p + 1
+        n_a = self._n_rows * self._n_cols
+        n_b = (hb - p + 1) * (wb - p + 1)
+        P = p * p * c
+        d = int(self.dim_reduced)
+        st = stream_ptr(dev)
+        if not hasattr(self, "_tree") or self._tree is None:
+            self._tree = KDTree(n_neighbors=self.n_neighbors, leaf_size=self.leaf_size, splitting_type="longest",
+                                n_jobs=self.n_jobs, float_type=self.float_type, verbose=0, device=dev.index)
+        tree = self._tree
+        tree.n_neighbors = self.n_neighbors
+        tree.leaf_size = self.leaf_size
+        tree.float_type = self.float_type
+        h = tree.handle
+        ev = {k: torch.cuda.Event(enable_timing=True) for k in ("t0", "t1", "t2", "t3", "t4")}
+        ev["t0"].record()
+
+        # (1) PCA fit on the sampled subset (annfmp/openmp/base.py:168-191)
+        m = int(self.n_subset / 2)
+        pos_a = _SUBSETS.get(self._n_rows, self._n_cols, m, self.seed, dev)
+        pos_b = _SUBSETS.get(hb - p + 1, wb - p + 1, m, self.seed + 1, dev)
+        self.components_ = torch.empty((d, P), dtype=torch.float64, device=dev)
+        self.mean_ = torch.empty(P, dtype=torch.float64, device=dev)
+        h.call("annf_pca_fit", ptr(A), ha, wa, ptr(pos_a), pos_a.shape[0], ptr(B), hb, wb, ptr(pos_b),
+               pos_b.shape[0], c, p, d, ptr(self.components_), ptr(self.mean_), st)
+        ev["t1"].record()
+
+        # (2)+(3) patches projected straight from the images (annfmp/openmp/base.py:152-166, 193-200)
+        self.patches_a_reduced_ = torch.empty((n_a, d), dtype=real, device=dev)
+        self.patches_b_reduced_ = torch.empty((n_b, d), dtype=real, device=dev)
+        h.call("annf_project", ptr(A), ha, wa, c, p, ptr(self.components_), ptr(self.mean_), d, real_type,
+               ptr(self.patches_a_reduced_), st)
+        h.call("annf_project", ptr(B), hb, wb, c, p, ptr(self.components_), ptr(self.mean_), d, real_type,
+               ptr(self.patches_b_reduced_), st)
+        ev["t2"].record()
+
+        # (4) k-d tree over B (annfmp/openmp/base.py:95-103)
+        tree.fit(self.patches_b_reduced_)
+        ev["t3"].record()
+
+        # (5) rows (annfmp/openmp/base.py:113-125)
+        assert self.leaf_size > self.n_neighbors
+        k = int(self.n_neighbors)
+        nn = torch.empty(n_a, dtype=torch.int32, device=dev)
+        self.knn_indices_ = torch.empty((n_a, k), dtype=torch.int32, device=dev)
+        self.nn_distances_ = torch.empty(n_a, dtype=torch.float32, device=dev)
+        h.call("annf_process_rows_img", ptr(nn), ptr(A), ha, wa, ptr(B), hb, wb, c, p,
+               ptr(self.patches_a_reduced_), self._n_rows, self._n_cols, k, int(bool(self.propagate)),
+               int(bool(self.select_best_nn)), tree._final_max_leaves(), ptr(self.knn_indices_),
+               ptr(self.nn_distances_), st)
+        ev["t4"].record()
+        tree.check_device()  # synchronises and raises if a kernel's bounds check tripped
+        self._timers = collections.OrderedDict()
+        self._timers["pca_fit"] = ev["t0"].elapsed_time(ev["t1"]) / 1e3
+        self._timers["extracting_patches"] = 0.0  # fused into pca_apply
+        self._timers["pca_apply"] = ev["t1"].elapsed_time(ev["t2"]) / 1e3
+        self._timers["kdtree_fit"] = ev["t2"].elapsed_time(ev["t3"]) / 1e3
+        self._timers["remaining_rows"] = ev["t3"].elapsed_time(ev["t4"]) / 1e3
+        self.kdtree = tree
+        if self.verbose > 0:
+            print("-----------------------------------------")
+            print("--------------- RUNTIMES ----------------")
+            print("-----------------------------------------")
+            for name, key in (("Extraction of patches", "extracting_patches"), ("PCA fit", "pca_fit"),
+                              ("PCA apply", "pca_apply"), ("K-D Tree (fitting)", "kdtree_fit"),
+                              ("Remaining rows", "remaining_rows")):
+                print("{}:\t{}".format(name, self._timers[key]))
+            print("Total runtime:\t\t{}".format(sum(self._timers.values())))
+            print("-----------------------------------------")
+        self._A, self._B = A, B
+        if numpy_io:
+            return nn.cpu().numpy()
+        return nn
+
+    # patch arrays as the reference exposes them (annfmp/openmp/base.py:211-218), built on the host
+    def _create_patches(self, img):
+        img = img.cpu().numpy() if isinstance(img, torch.Tensor) else numpy.asarray(img)
+        if img.ndim == 2:
+            img = img[:, :, None]
+        p = self.psize
+        h, w, c = img.shape
+        win = numpy.lib.stride_tricks.sliding_window_view(img, (p, p, c))[:, :, 0]
+        return numpy.ascontiguousarray(win.reshape((h - p + 1) * (w - p + 1), p * p * c))
+
+    @property
+    def patches_a(self):
+        return self._create_patches(self.image_a)
+
+    @property
+    def patches_b(self):
+        return self._create_patches(self.image_b)

@@ -1,0 +1,350 @@
+"""Benchmark: query patches/s of the NNF hot path on one GB300 (or N replicas).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+                    [--workload large|small] [--form plain]
+
+A step is one full NNF of one image pair, from device-resident uint8 images to the device-resident
+NNF: PCA fit (sampled subset, exact Gram, FP64 eigh), projection of every A and B patch, k-d tree
+build, exact first row, row propagation and the raw-patch re-rank. value = query patches (A patch
+positions) per second over all ranks. e2e = the same through the public API from pinned host
+images to the host NNF. The L2 cache (129 MB) is flushed between timed steps by writing 256 MB.
+
+--impl reference times the CPU path (the oracle: a C restatement of the reference's OpenMP core with
+OpenMP on all host cores, plus the numpy restatement of its PCA) on a bounded sample of the same
+workload: every per-pair stage on the full pair, and the row loop on the first ROWS_SAMPLE rows,
+extrapolated to all rows.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOADS = {
+    # 2048x2048 flow-warped pair (seed 1): psize 9 (243-dim), PCA 16, leaf 64, k 4
+    "large": dict(size=2048, seed=1, kind="flow", n_neighbors=4, psize=9, dim_reduced=16, leaf_size=64),
+    # 512x512 affine pair (seed 0): psize 7 (147-dim), PCA 8, leaf 32, k 1
+    "small": dict(size=512, seed=0, kind="affine", n_neighbors=1, psize=7, dim_reduced=8, leaf_size=32),
+}
+ROWS_SAMPLE = 32
+L2_FLUSH_BYTES = 256 << 20
+
+
+def make_pair(w):
+    from annfmp_gb300 import gen
+    if w["kind"] == "flow":
+        return gen.pair_flow(w["seed"], w["size"])
+    return gen.pair_small(w["seed"], w["size"])
+
+
+def params_of(w):
+    n_b = (w["size"] - w["psize"] + 1) ** 2
+    return dict(n_neighbors=w["n_neighbors"], psize=w["psize"], dim_reduced=w["dim_reduced"],
+                n_subset=int(round(0.1 * n_b)), leaf_size=w["leaf_size"], seed=w["seed"])
+
+
+# ---------------------------------------------------------------------------------------------
+# clocks during the timed region
+# ---------------------------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.lines = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx = max(mx, float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[4:8]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx or None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------------------------
+# algorithmic bytes per launch of each stage ("roofline")
+# ---------------------------------------------------------------------------------------------
+def stage_bytes(stage, w, n_a, n_b, depth, n_cols):
+    d, k, P = w["dim_reduced"], w["n_neighbors"], w["psize"] ** 2 * 3
+    ppl = n_b / float(1 << depth)
+    rows_q = n_a - n_cols
+    if stage == "chain":  # per query: query + k propagated leaves + leaf spans + natural list + k-list out
+        return rows_q * (4 * d + k * ppl * 4 * d + 8 * k + 12 * k + 4 * k)
+    if stage == "natural_knn":  # query + node path + natural leaf + list out
+        return rows_q * (4 * d + 8 * depth + ppl * 4 * d + 12 * k)
+    if stage == "select_best":  # k A/B patch pairs + list in + index/distance out
+        return n_a * (k * 2 * P + 4 * k + 8)
+    if stage == "first_row":  # every point once per 128-query tile
+        return -(-n_cols // 128) * n_b * 4 * d + n_cols * 4 * d
+    if stage == "project":
+        return (w["size"] ** 2) * 3 + n_b * 4 * d
+    return None
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            j = json.load(f)
+        return float(j["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def load_traffic():
+    p = os.path.join(ROOT, "profiles", "ncu_traffic.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return json.load(f)
+    return {}
+
+
+# ---------------------------------------------------------------------------------------------
+# CPU arm (oracle)
+# ---------------------------------------------------------------------------------------------
+def cpu_sample(a, b, w, rows=ROWS_SAMPLE):
+    """Time the oracle on the pair: PCA fit, projection of B and of the sampled A rows, tree,
+    first row + `rows` later rows; returns (seconds extrapolated to the whole pair, detail)."""
+    from oracle import oracle as O
+    prm = params_of(w)
+    p = w["psize"]
+    n_rows, n_cols = a.shape[0] - p + 1, a.shape[1] - p + 1
+    r = min(rows + 1, n_rows)
+    t0 = time.perf_counter()
+    comps, mean = O.pca_fit(a, b, p, prm["dim_reduced"], prm["n_subset"], prm["seed"])
+    t1 = time.perf_counter()
+    pb = O.extract_patches(b, p)
+    bred = np.concatenate([O.pca_transform(pb[i:i + 262144], comps, mean) for i in range(0, len(pb), 262144)])
+    t2 = time.perf_counter()
+    pa = O.extract_patches(np.ascontiguousarray(a[: r + p - 1]), p)
+    ared = O.pca_transform(pa, comps, mean)
+    t3 = time.perf_counter()
+    tree = O.OracleTree(bred, O.tree_depth(len(bred), prm["leaf_size"]))
+    t4 = time.perf_counter()
+    tree.process_rows(ared[:n_cols], pa[:n_cols], pb, 1, n_cols, prm["n_neighbors"])
+    t5 = time.perf_counter()
+    tree.process_rows(ared, pa, pb, r, n_cols, prm["n_neighbors"])
+    t6 = time.perf_counter()
+    first_row = t5 - t4
+    later = max((t6 - t5) - first_row, 0.0)  # rows 1..r-1 with their re-rank
+    proj_a = (t3 - t2) * n_rows / r
+    rows_all = later * (n_rows - 1) / max(r - 1, 1)
+    total = (t1 - t0) + (t2 - t1) + proj_a + (t4 - t3) + first_row + rows_all
+    det = dict(pca_fit=round(t1 - t0, 3), project_b=round(t2 - t1, 3), project_a=round(proj_a, 3),
+               tree=round(t4 - t3, 3), first_row=round(first_row, 3), rows=round(rows_all, 3),
+               rows_sampled=r - 1)
+    return total, det
+
+
+def run_reference(args, w, rank, world):
+    if rank != 0:
+        return
+    a, b = make_pair(w)
+    p = w["psize"]
+    n_a = (a.shape[0] - p + 1) * (a.shape[1] - p + 1)
+    for _ in range(args.warmup):
+        cpu_sample(a, b, w)
+    times = []
+    for _ in range(args.steps):
+        t, det = cpu_sample(a, b, w)
+        times.append(t)
+    t = float(np.mean(times))
+    cores = os.cpu_count()
+    val = n_a / t
+    line = {"metric": "query patches/s", "value": val, "unit": "query patches/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "impl": "reference", "config": config_of(w, args),
+            "cpu_baseline": {"value": val, "unit": "query patches/s", "cores": cores, "kind": "port",
+                             "sample": f"full-pair PCA fit, projection, tree and first row; {ROWS_SAMPLE} later "
+                                       f"rows timed and extrapolated to all rows (last step: {det})"},
+            "e2e": {"value": val, "unit": "query patches/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def config_of(w, args):
+    prm = params_of(w)
+    return {"workload": f"{w['size']}x{w['size']}x3 {w['kind']} pair seed {w['seed']}, patch {w['psize']}x"
+                        f"{w['psize']}x3, PCA {w['dim_reduced']}, leaf {w['leaf_size']}, k {w['n_neighbors']}",
+            "form": args.form, "n_subset": prm["n_subset"], "pairs_per_rank": 1,
+            "l2": "flushed between timed steps (256 MB write)", "parallelism": f"replicas x{args.gpus}"}
+
+
+# ---------------------------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------------------------
+def run_gpu(args, w, rank, world, local_rank):
+    import torch
+    import torch.distributed as dist
+
+    from annfmp_gb300 import ANNFieldPropKDTreeGB300, _lib
+    dev = torch.device("cuda", local_rank)
+    torch.cuda.set_device(dev)
+    a, b = make_pair(w)
+    prm = params_of(w)
+    p = w["psize"]
+    n_rows, n_cols = a.shape[0] - p + 1, a.shape[1] - p + 1
+    n_a = n_rows * n_cols
+    n_b = (b.shape[0] - p + 1) * (b.shape[1] - p + 1)
+    A = torch.from_numpy(a).to(dev)
+    B = torch.from_numpy(b).to(dev)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+    model = ANNFieldPropKDTreeGB300(verbose=0, device=local_rank, **prm)
+
+    for _ in range(args.warmup):
+        model.fit(A, B)
+    torch.cuda.synchronize(dev)
+    h = model.kdtree.handle
+    h.profile(True)
+    h.profile_read(torch.cuda.current_stream(dev).cuda_stream)
+    stages = {}
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize(dev)
+    launches0 = _lib.launch_count()
+    with ClockSampler(dev.index) as clocks:
+        t_wall0 = time.perf_counter()
+        for i in range(args.steps):
+            flush.fill_(float(i))
+            ev[i][0].record()
+            model.fit(A, B)
+            ev[i][1].record()
+            for name, ms in h.profile_read(torch.cuda.current_stream(dev).cuda_stream):
+                stages.setdefault(name, []).append(ms)
+        torch.cuda.synchronize(dev)
+        t_wall = time.perf_counter() - t_wall0
+    launches = _lib.launch_count() - launches0
+    h.profile(False)
+    ms = sum(s.elapsed_time(e) for s, e in ev) / args.steps
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+        dist.barrier()
+
+    # end to end through the public API: pinned host images in, host NNF out
+    a_pin = torch.from_numpy(a).pin_memory()
+    b_pin = torch.from_numpy(b).pin_memory()
+    e2e_times = []
+    for i in range(max(2, args.steps)):
+        flush.fill_(float(i))
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        nn = model.fit(a_pin, b_pin)
+        nn_host = nn.cpu()
+        e2e_times.append(time.perf_counter() - t0)
+    e2e_s = float(np.median(e2e_times))
+    if world > 1:
+        t = torch.tensor([e2e_s], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+
+    if rank != 0:
+        return
+    stage_ms = {k: float(np.mean(v)) for k, v in stages.items()}
+    kernel_stages = {k: v for k, v in stage_ms.items() if not k.endswith(":begin")}
+    depth = model.kdtree.final_tree_depth_
+    peak, peak_kind = load_peaks()
+    dom = max((k for k in kernel_stages if stage_bytes(k, w, n_a, n_b, depth, n_cols)), key=lambda k: kernel_stages[k])
+    by = stage_bytes(dom, w, n_a, n_b, depth, n_cols)
+    achieved = by / (kernel_stages[dom] / 1e3) / 1e9
+    traffic = load_traffic().get(f"{args.workload}:{args.form}:{dom}")
+    value = world * n_a / (ms / 1e3)
+    line = {
+        "metric": "query patches/s", "value": value, "unit": "query patches/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": config_of(w, args),
+        "e2e": {"value": world * n_a / e2e_s, "unit": "query patches/s", "h2d_bytes_per_step": int(a.nbytes + b.nbytes),
+                "d2h_bytes_per_step": int(nn_host.numel() * nn_host.element_size())},
+        "gpu_launches": int(launches),
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_kind": peak_kind, "algorithmic_bytes": by,
+                     "traffic": traffic},
+        "stages_ms": stage_ms, "wall_ms_per_step": t_wall * 1e3 / args.steps,
+        "clocks": clocks.summary(),
+    }
+    if world == 1 and not args.no_cpu_baseline:
+        t_cpu, det = cpu_sample(a, b, w)
+        line["cpu_baseline"] = {"value": n_a / t_cpu, "unit": "query patches/s", "cores": os.cpu_count(),
+                                "kind": "port", "sample": f"oracle: full-pair PCA fit, projection, tree, first row; "
+                                                          f"{ROWS_SAMPLE} later rows extrapolated ({det})"}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="large", choices=sorted(WORKLOADS))
+    ap.add_argument("--form", default="plain", choices=["plain"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 0)
+    w = WORKLOADS[args.workload]
+    rank = int(os.environ.get("RANK", 0))
+    world = int(os.environ.get("WORLD_SIZE", 1))
+    local_rank = int(os.environ.get("LOCAL_RANK", 0))
+    if args.impl == "reference":
+        run_reference(args, w, rank, world)
+        return
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if os.environ.get("ANNF_PG", "nccl") == "nccl" else "gloo")
+    try:
+        run_gpu(args, w, rank, world, local_rank)
+    finally:
+        if world > 1:
+            import torch.distributed as dist
+            dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

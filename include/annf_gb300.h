@@ -1,0 +1,141 @@
+/*
+ * annf_gb300.h -- C ABI of the GB300 (sm_103a) nearest-neighbour-field library.
+ *
+ * The library replaces the native core of annfmp's OpenMP backend. Each entry point below names
+ * the reference interface it stands in for (paths within the annfmp project). All pointers to
+ * array data are DEVICE pointers unless a parameter says "host"; the caller owns every input and
+ * output buffer. A handle owns the device tree and its scratch memory and frees them in
+ * annf_destroy. Calls are asynchronous on the given CUDA stream (NULL = legacy default stream);
+ * a handle must not be used from two host threads at once.
+ *
+ * Every function returns ANNF_OK (0) or a negative status; annf_last_error() then describes the
+ * failure (thread-local). The reference prints and calls exit() instead
+ * (annfmp/openmp/kdtree/src/helper.c:30-52, kdtree.c:403-407).
+ */
+#ifndef ANNF_GB300_H_
+#define ANNF_GB300_H_
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ANNF_OK 0
+#define ANNF_ERR_INVALID -1     /* bad argument (shape, range, null pointer) */
+#define ANNF_ERR_UNSUPPORTED -2 /* valid for the reference, not supported here (e.g. k > 32) */
+#define ANNF_ERR_CUDA -3        /* a CUDA runtime call or launch failed */
+#define ANNF_ERR_ALLOC -4       /* device allocation failed */
+#define ANNF_ERR_STATE -5       /* call order (e.g. query before a tree was built) */
+#define ANNF_ERR_DEVICE -6      /* a kernel's own bounds check tripped (see annf_device_status) */
+#define ANNF_ERR_SOLVER -7      /* the eigen-solver reported failure */
+
+/* scalar type of reduced patches / tree points (reference FLOAT_TYPE, include/float.h:16-26) */
+#define ANNF_REAL_F32 0
+#define ANNF_REAL_F64 1
+
+/* split-axis rule (reference SPLITTING_TYPE_*, annfmp/openmp/kdtree/src/include/global.h:18-19) */
+#define ANNF_SPLIT_CYCLIC 0  /* axis = node depth mod d */
+#define ANNF_SPLIT_LONGEST 1 /* first axis of strictly largest bounding-box width */
+
+/* leaf-distance precision of annf_process_rows* (the plain form is ANNF_LEAF_EXACT) */
+#define ANNF_LEAF_EXACT 0 /* FP32/FP64 with the reference's summation order */
+
+typedef struct annf_handle annf_handle;
+
+/* Tree arrays as device pointers (structure-of-arrays form of the reference KD_TREE_RECORD,
+ * annfmp/openmp/kdtree/src/include/global.h:40-50). */
+typedef struct {
+  int n, d, depth, real_type;
+  int n_leaves;            /* 2^depth */
+  const void* points;      /* [n*d] points in tree order (reference XI float part) */
+  const int* perm;         /* [n] tree position -> original index (reference XI index part) */
+  const int* node_axis;    /* [2^depth-1] heap order (reference nodes[].axis) */
+  const void* node_split;  /* [2^depth-1] (reference nodes[].splitting_value) */
+  const int* leaf_begin;   /* [2^depth+1]; leaf l = [leaf_begin[l], leaf_begin[l+1]) (reference leaves[]) */
+  const int* point_leaf;   /* [n] original index -> leaf (reference points_leaf_indices) */
+} annf_tree_view;
+
+int annf_version(void);
+const char* annf_last_error(void);
+
+/* Create / destroy a handle bound to a CUDA device. Stands in for the parameter/record setup of
+ * init_extern (annfmp/openmp/kdtree/src/base.c:22-43, include/base.h:36-42). */
+int annf_create(annf_handle** out, int device);
+void annf_destroy(annf_handle* h);
+
+/* Build the k-d tree over n points of dimension d (row-major device array, real_type scalars) to
+ * the given depth: longest-bounding-box axis, split at the order statistic of rank count/2,
+ * reference element order. Replaces fit_extern (annfmp/openmp/kdtree/src/base.c:54-69,
+ * include/base.h:55-60). Tree depth is chosen by the caller as the reference Python does
+ * (annfmp/openmp/kdtree/base.py:260-300). */
+int annf_build_tree(annf_handle* h, const void* points, int n, int d, int real_type, int depth,
+                    int splitting_type, void* stream);
+
+/* Device pointers of the current tree (valid until the next build or annf_destroy). */
+int annf_tree_get(const annf_handle* h, annf_tree_view* out);
+
+/* Exact k nearest neighbours of nq queries ([nq*d], real_type of the tree). distances [nq*k]
+ * (Euclidean, i.e. square-rooted) and indices [nq*k] (original point indices), best first.
+ * max_leaves must be >= the number of leaves (exact search); smaller budgets are unsupported.
+ * Replaces neighbors_extern (annfmp/openmp/kdtree/src/base.c:88-132, include/base.h:67-78). */
+int annf_kneighbors(annf_handle* h, const void* queries, int nq, int k, long long max_leaves,
+                    void* distances, int* indices, void* stream);
+
+/* The row-propagation NNF over an n_rows x n_cols grid of A patches (reduced, [n_rows*n_cols*d]
+ * real_type, row-major pixels). Raw uint8 patches come as arrays: patches_a [n_a*P],
+ * patches_b [n_b*P] (may be NULL when select_best == 0).
+ *   final_idx  [n_rows*n_cols]  chosen B index per pixel (output)
+ *   knn_out    [n_rows*n_cols*k] optional (NULL): each pixel's k-list as original B indices
+ *   dist_out   [n_rows*n_cols]   optional (NULL): raw-patch L2 of the chosen index (select_best)
+ * Replaces process_rows_extern (annfmp/openmp/kdtree/src/base.c:150-360, include/base.h:81-98). */
+int annf_process_rows(annf_handle* h, int* final_idx, const uint8_t* patches_a, int n_a,
+                      const uint8_t* patches_b, int n_b, int P, const void* ared, int n_rows,
+                      int n_cols, int k, int propagate, int select_best, long long max_leaves,
+                      int* knn_out, float* dist_out, void* stream);
+
+/* As annf_process_rows, but raw patches are read from the images themselves (uint8 HxWxC,
+ * row-major, channel fastest; patch (y,x) = rows y..y+psize-1, cols x..x+psize-1), so the
+ * 1 GB-scale patch arrays of the reference are never materialised. */
+int annf_process_rows_img(annf_handle* h, int* final_idx, const uint8_t* img_a, int ha, int wa,
+                          const uint8_t* img_b, int hb, int wb, int channels, int psize,
+                          const void* ared, int n_rows, int n_cols, int k, int propagate,
+                          int select_best, long long max_leaves, int* knn_out, float* dist_out,
+                          void* stream);
+
+/* PCA fit on sampled patches of both images (annfmp/openmp/base.py:168-191 with scikit-learn's
+ * covariance_eigh solver): Gram matrix accumulated exactly, covariance finished in FP64 in the
+ * solver's own operation order, FP64 symmetric eigendecomposition on the GPU, components sorted
+ * by decreasing eigenvalue with the sign convention "largest |entry| positive".
+ *   pos_a [n_a*2], pos_b [n_b*2]: (row, col) of the sampled patches (int32, device)
+ *   components_out [n_components*P] FP64, mean_out [P] FP64 (device) */
+int annf_pca_fit(annf_handle* h, const uint8_t* img_a, int ha, int wa, const int* pos_a, int n_a,
+                 const uint8_t* img_b, int hb, int wb, const int* pos_b, int n_b, int channels,
+                 int psize, int n_components, double* components_out, double* mean_out,
+                 void* stream);
+
+/* Project every psize x psize patch of an image onto the components
+ * (annfmp/openmp/base.py:193-200: X @ C^T - mean @ C^T in FP64, cast to real_type). The
+ * product is evaluated exactly in integer arithmetic on split coefficients, so the result is the
+ * FP64 value rounded once. out [(h-psize+1)*(w-psize+1)*n_components], row-major pixels. */
+int annf_project(annf_handle* h, const uint8_t* img, int hgt, int wid, int channels, int psize,
+                 const double* components, const double* mean, int n_components, int real_type,
+                 void* out, void* stream);
+
+/* Synchronise the stream and report (and clear) the kernels' bounds-check status bits. */
+int annf_device_status(annf_handle* h, void* stream, unsigned* bits_out);
+
+/* Instrumentation (no counterpart in the reference, whose only timing is wall-clock per Python
+ * stage, annfmp/openmp/base.py:73-126). With profiling on, every call records CUDA events on its
+ * stream at stage boundaries; annf_profile_read synchronises the stream and returns the number of
+ * intervals (ms[i] = time from the previous mark to mark i, names[i] = the stage that ended there),
+ * then clears the marks. annf_launch_count returns the kernels this library has launched. */
+int annf_profile_enable(annf_handle* h, int on);
+int annf_profile_read(annf_handle* h, void* stream, int cap, float* ms, const char** names);
+long long annf_launch_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* ANNF_GB300_H_ */

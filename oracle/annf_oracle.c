@@ -46,6 +46,7 @@ typedef struct {
     int n;            /* number of points */
     int d;            /* dimension */
     int depth;        /* tree depth (number of internal levels) */
+    int splitting;    /* 0: cyclic axis (level mod d), 1: longest bounding-box side */
     REAL *pts;        /* [n*d] */
     int *perm;        /* [n] */
     int *node_axis;   /* [2^depth - 1] */
@@ -195,7 +196,8 @@ static void build_rec(ora_tree *t, build_scratch *s, int lo, int hi, int node, i
         for (int p = lo; p < hi; ++p) t->point_leaf[t->perm[p]] = leaf;
         return;
     }
-    int axis = widest_axis(t, lo, hi, s->mn, s->mx);
+    /* reference kdtree.c:369-371 (cyclic) and 373-417 (longest) */
+    int axis = t->splitting == 0 ? level % d : widest_axis(t, lo, hi, s->mn, s->mx);
     int m = hi - lo, half = m / 2;
     for (int i = 0; i < m; ++i) s->vals[i] = t->pts[(size_t)(lo + i) * d + axis];
     REAL piv = select_rank(s->vals, m, half);

@@ -44,6 +44,7 @@ class _OraTree(ctypes.Structure):
         ("n", ctypes.c_int),
         ("d", ctypes.c_int),
         ("depth", ctypes.c_int),
+        ("splitting", ctypes.c_int),
         ("pts", ctypes.c_void_p),
         ("perm", ctypes.c_void_p),
         ("node_axis", ctypes.c_void_p),
@@ -110,7 +111,7 @@ def tree_depth(n: int, leaf_size: int, tree_depth_param=None) -> int:
 class OracleTree:
     """A k-d tree built by the C restatement; arrays are numpy (see annf_oracle.c header)."""
 
-    def __init__(self, X: np.ndarray, depth: int):
+    def __init__(self, X: np.ndarray, depth: int, splitting: int = 1):
         X = np.ascontiguousarray(X)
         if X.dtype not in (np.float32, np.float64):
             raise TypeError("X must be float32 or float64")
@@ -124,7 +125,7 @@ class OracleTree:
         self.node_split = np.zeros(max(L - 1, 0), X.dtype)
         self.leaf_bounds = np.empty(2 * L, np.int32)
         self.point_leaf = np.empty(n, np.int32)
-        self._s = _OraTree(n, d, depth, self.pts.ctypes.data, self.perm.ctypes.data,
+        self._s = _OraTree(n, d, depth, splitting, self.pts.ctypes.data, self.perm.ctypes.data,
                            self.node_axis.ctypes.data if L > 1 else None,
                            self.node_split.ctypes.data if L > 1 else None,
                            self.leaf_bounds.ctypes.data, self.point_leaf.ctypes.data)

@@ -1,0 +1,293 @@
+"""GPU parity: the CUDA kernels (through the C ABI) against the oracle and the reference's golden
+outputs. Integer/index outputs must match bit for bit; the one floating-point tolerance (end to end,
+where the GPU fits its own PCA) is stated where it is used."""
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+
+def _bits(a):
+    a = np.ascontiguousarray(a)
+    return a.view(np.uint32) if a.dtype == np.float32 else a.view(np.uint64)
+
+
+def gpu_tree(X, depth, splitting="longest", K=1):
+    from annfmp_gb300 import KDTree
+    ft = "float" if X.dtype == np.float32 else "double"
+    kd = KDTree(n_neighbors=K, tree_depth=depth, float_type=ft, splitting_type=splitting)
+    kd.fit(X)
+    return kd
+
+
+def assert_tree_equal(arrs, perm, node_axis, node_split, leaf_bounds, point_leaf, X, tag=""):
+    assert np.array_equal(arrs["perm"], perm), tag
+    assert np.array_equal(_bits(arrs["points"]), _bits(X[perm])), tag
+    assert np.array_equal(arrs["node_axis"], node_axis), tag
+    assert np.array_equal(_bits(arrs["node_split"]), _bits(node_split)), tag
+    assert np.array_equal(arrs["leaves"], leaf_bounds), tag
+    assert np.array_equal(arrs["point_leaf"], point_leaf), tag
+
+
+# ---------------------------------------------------------------------------------------------
+# tree build
+# ---------------------------------------------------------------------------------------------
+def test_tree_golden(gpu_lib, golden):
+    z = golden("ref_trees.npz")
+    for ci in range(int(z["n_cases"])):
+        n, d, depth, split = (int(v) for v in z[f"c{ci}_meta"])
+        X = z[f"c{ci}_X"]
+        kd = gpu_tree(X, depth, "longest" if split else "cyclic")
+        assert_tree_equal(kd.tree_arrays(), z[f"c{ci}_perm"], z[f"c{ci}_node_axis"], z[f"c{ci}_node_split"],
+                          z[f"c{ci}_leaf_bounds"], z[f"c{ci}_point_leaf"], X, f"golden case {ci}")
+
+
+@pytest.mark.parametrize("n,d,leaf,kind,dtype", [
+    (1, 3, 2, "normal", np.float32), (2, 1, 2, "normal", np.float32), (37, 5, 3, "normal", np.float32),
+    (5000, 8, 32, "ties", np.float32), (70000, 16, 64, "normal", np.float32), (70000, 8, 16, "dups", np.float32),
+    (300000, 16, 64, "normal", np.float32), (131072, 12, 32, "negzero", np.float32),
+    (20000, 7, 8, "normal", np.float64), (90000, 16, 64, "ties", np.float64), (40000, 30, 16, "normal", np.float32),
+    (10000, 4, 10, "constant", np.float32),
+])
+@pytest.mark.parametrize("splitting", ["longest", "cyclic"])
+def test_tree_vs_oracle(gpu_lib, oracle_mod, n, d, leaf, kind, dtype, splitting):
+    O = oracle_mod
+    rng = np.random.default_rng(n * 31 + d)
+    X = (rng.standard_normal((n, d)) * 10).astype(dtype)
+    if kind == "ties":
+        X = np.round(X / 3).astype(dtype)
+    elif kind == "dups":
+        X[::3] = X[0]
+    elif kind == "negzero":
+        X = np.round(X / 25).astype(dtype)
+        X[::2] *= -1
+    elif kind == "constant":
+        X[:] = 1.5
+    depth = O.tree_depth(n, leaf)
+    ot = O.OracleTree(X, depth, 1 if splitting == "longest" else 0)
+    kd = gpu_tree(X, depth, splitting)
+    assert_tree_equal(kd.tree_arrays(), ot.perm, ot.node_axis, ot.node_split, ot.leaf_bounds, ot.point_leaf, X,
+                      f"{n},{d},{kind},{splitting}")
+
+
+# ---------------------------------------------------------------------------------------------
+# exact kNN (reference neighbors_extern)
+# ---------------------------------------------------------------------------------------------
+def test_kneighbors_golden(gpu_lib, golden):
+    z = golden("ref_trees.npz")
+    for ci in range(int(z["n_cases"])):
+        n, d, depth, split = (int(v) for v in z[f"c{ci}_meta"])
+        K = int(z[f"c{ci}_K"])
+        kd = gpu_tree(z[f"c{ci}_X"], depth, "longest" if split else "cyclic", K=K)
+        dist, idx = kd.kneighbors(z[f"c{ci}_Q"])
+        assert np.array_equal(idx, z[f"c{ci}_knn_idx"]), ci
+        assert np.array_equal(_bits(dist), _bits(z[f"c{ci}_knn_dist"])), ci
+
+
+@pytest.mark.parametrize("K", [1, 3, 4, 8, 17, 32])
+@pytest.mark.parametrize("dtype,d", [(np.float32, 8), (np.float32, 16), (np.float32, 5), (np.float64, 6)])
+def test_kneighbors_vs_oracle(gpu_lib, oracle_mod, K, dtype, d):
+    O = oracle_mod
+    rng = np.random.default_rng(K * 7 + d)
+    n = 30000
+    X = (rng.standard_normal((n, d)) * 5).astype(dtype)
+    X[::7] = np.round(X[::7])
+    Q = (rng.standard_normal((300, d)) * 5).astype(dtype)
+    Q[::3] = X[rng.integers(0, n, 100)]  # exact hits -> zero distances and ties
+    depth = O.tree_depth(n, 32)
+    ot = O.OracleTree(X, depth)
+    kd = gpu_tree(X, depth, K=K)
+    dg, ig = kd.kneighbors(Q)
+    do, io = ot.kneighbors(Q, K)
+    assert np.array_equal(ig, io)
+    assert np.array_equal(_bits(dg), _bits(do))
+
+
+# ---------------------------------------------------------------------------------------------
+# row propagation (reference process_rows_extern)
+# ---------------------------------------------------------------------------------------------
+def test_process_rows_golden(gpu_lib, golden):
+    z = golden("ref_rows.npz")
+    for ci in range(int(z["n_cases"])):
+        nr, nc, d, P, K, depth, prop, sel = (int(v) for v in z[f"r{ci}_meta"])
+        kd = gpu_tree(z[f"r{ci}_X"], depth, K=K)
+        out = np.zeros(nr * nc, np.int32)
+        kd.process_rows(out, z[f"r{ci}_pa"], z[f"r{ci}_pb"], z[f"r{ci}_A"], nr, nc, K, bool(prop), bool(sel))
+        assert np.array_equal(out, z[f"r{ci}_final"]), ci
+
+
+@pytest.mark.parametrize("nr,nc,d,K,leaf,prop,sel,dtype", [
+    (60, 70, 8, 1, 32, True, True, np.float32), (90, 64, 16, 4, 64, True, True, np.float32),
+    (50, 80, 12, 8, 32, True, True, np.float32), (40, 33, 16, 4, 16, False, True, np.float32),
+    (45, 51, 8, 2, 8, True, False, np.float32), (40, 40, 6, 3, 8, True, True, np.float64),
+    (30, 90, 5, 16, 32, True, True, np.float32), (128, 128, 16, 4, 64, True, True, np.float32),
+])
+def test_process_rows_vs_oracle(gpu_lib, oracle_mod, nr, nc, d, K, leaf, prop, sel, dtype):
+    O = oracle_mod
+    rng = np.random.default_rng(nr * nc + K)
+    nA = nr * nc
+    X = (rng.standard_normal((nA, d)) * 10).astype(dtype)
+    # A resembles B shifted by a few pixels, like an image pair, so that propagation matters
+    A = np.roll(X.reshape(nr, nc, d), (2, 3), axis=(0, 1)).reshape(nA, d) + rng.standard_normal((nA, d)).astype(dtype)
+    A = A.astype(dtype)
+    if K == 2:
+        X, A = np.round(X / 2).astype(dtype), np.round(A / 2).astype(dtype)
+    P = 27
+    pa = rng.integers(0, 256, (nA, P), dtype=np.uint8)
+    pb = rng.integers(0, 256, (nA, P), dtype=np.uint8)
+    depth = O.tree_depth(nA, leaf)
+    ot = O.OracleTree(X, depth)
+    fo, ko = ot.process_rows(A, pa, pb, nr, nc, K, prop, sel)
+    kd = gpu_tree(X, depth, K=K)
+    out = np.zeros(nA, np.int32)
+    kd.process_rows(out, pa, pb, A, nr, nc, K, prop, sel)
+    assert np.array_equal(kd.knn_indices_.cpu().numpy(), ko)
+    assert np.array_equal(out, fo)
+
+
+# ---------------------------------------------------------------------------------------------
+# PCA + projection + end to end
+# ---------------------------------------------------------------------------------------------
+PIPES = ["ref_pipeline_affine128.npz", "ref_pipeline_flow160.npz", "ref_pipeline_k3_noprop.npz"]
+
+
+def _fit_gpu(z):
+    from annfmp_gb300 import ANNFieldPropKDTreeGB300
+    k, psize, d, n_subset, leaf, prop, sel, seed = (int(v) for v in z["params"])
+    m = ANNFieldPropKDTreeGB300(n_neighbors=k, psize=psize, dim_reduced=d, n_subset=n_subset, leaf_size=leaf,
+                                propagate=bool(prop), select_best_nn=bool(sel), seed=seed, verbose=0)
+    nn = m.fit(z["a"], z["b"])
+    return m, nn
+
+
+@pytest.mark.parametrize("name", PIPES)
+def test_pca_fit_vs_reference(gpu_lib, golden, name):
+    z = golden(name)
+    m, _ = _fit_gpu(z)
+    # mean is exact (integer sums, one division); components agree to FP64 eigen-solver accuracy
+    assert np.array_equal(m.mean_.cpu().numpy(), z["mean"])
+    comps = m.components_.cpu().numpy()
+    assert np.allclose(comps, z["components"], rtol=0, atol=1e-9), np.abs(comps - z["components"]).max()
+
+
+@pytest.mark.parametrize("name", PIPES)
+def test_projection_rounds_like_fp64(gpu_lib, oracle_mod, golden, name):
+    """GPU projection with the reference's own components vs the FP64 transform rounded to FP32:
+    at most 1 ulp apart, and bit-identical on >= 99.99% of the coordinates."""
+    O = oracle_mod
+    z = golden(name)
+    m, _ = _fit_gpu(z)
+    from annfmp_gb300 import _lib
+    from annfmp_gb300._torch import ptr, stream_ptr
+    dev = torch.device("cuda", 0)
+    comps = torch.from_numpy(z["components"]).to(dev)
+    mean = torch.from_numpy(z["mean"]).to(dev)
+    psize = int(z["params"][1])
+    img = torch.from_numpy(z["a"]).to(dev)
+    h, w, c = z["a"].shape
+    out = torch.empty(((h - psize + 1) * (w - psize + 1), comps.shape[0]), dtype=torch.float32, device=dev)
+    m.kdtree.handle.call("annf_project", ptr(img), h, w, c, psize, ptr(comps), ptr(mean), comps.shape[0],
+                         _lib.ANNF_REAL_F32, ptr(out), stream_ptr(dev))
+    got = out.cpu().numpy()
+    want = O.pca_transform(O.extract_patches(z["a"], psize), z["components"], z["mean"])
+    ulps = np.abs(got.view(np.int32).astype(np.int64) - want.view(np.int32).astype(np.int64))
+    assert ulps.max() <= 1
+    assert (ulps == 0).mean() >= 0.9999
+
+
+@pytest.mark.parametrize("name", PIPES)
+def test_rows_on_reference_reduced_arrays(gpu_lib, oracle_mod, golden, name):
+    """Tree + rows on the reference's reduced patches (numpy FP64 transform of the reference's
+    components): GPU == oracle bit for bit, and == the reference's NNF."""
+    O = oracle_mod
+    from annfmp_gb300 import KDTree
+    z = golden(name)
+    k, psize, d, n_subset, leaf, prop, sel, seed = (int(v) for v in z["params"])
+    pa, pb = O.extract_patches(z["a"], psize), O.extract_patches(z["b"], psize)
+    ared = O.pca_transform(pa, z["components"], z["mean"])
+    bred = O.pca_transform(pb, z["components"], z["mean"])
+    nr, nc = z["a"].shape[0] - psize + 1, z["a"].shape[1] - psize + 1
+    ot = O.OracleTree(bred, O.tree_depth(len(bred), leaf))
+    fo, _ = ot.process_rows(ared, pa, pb, nr, nc, k, bool(prop), bool(sel))
+    kd = KDTree(n_neighbors=k, leaf_size=leaf, splitting_type="longest", float_type="float").fit(bred)
+    out = np.zeros(nr * nc, np.int32)
+    kd.process_rows(out, pa, pb, ared, nr, nc, k, bool(prop), bool(sel))
+    assert np.array_equal(out, fo)
+    assert (out == z["nn"]).mean() >= 0.999
+
+
+def _relative_excess(a, b, psize, nn_x, nn_y):
+    """raw-patch L2 of A's pixels under two NNFs (int64 exact)."""
+    from oracle import oracle as O
+    pa, pb = O.extract_patches(a, psize).astype(np.int64), O.extract_patches(b, psize).astype(np.int64)
+    dx = np.sqrt(((pa - pb[nn_x]) ** 2).sum(1))
+    dy = np.sqrt(((pa - pb[nn_y]) ** 2).sum(1))
+    return dx, dy
+
+
+@pytest.mark.parametrize("name", PIPES)
+def test_pipeline_vs_reference(gpu_lib, golden, name):
+    """End to end from the images (GPU PCA fit, projection, tree, rows, re-rank) vs the reference's
+    NNF: identical on >= 99.9% of the pixels."""
+    z = golden(name)
+    m, nn = _fit_gpu(z)
+    agree = (nn == z["nn"]).mean()
+    assert agree >= 0.999, agree
+    psize = int(z["params"][1])
+    dg, dr = _relative_excess(z["a"], z["b"], psize, nn, z["nn"])
+    # the per-pixel distance the GPU reports is the raw-patch L2 of its choice
+    assert np.allclose(m.nn_distances_.cpu().numpy(), dg, rtol=1e-6)
+
+
+@pytest.mark.slow
+def test_small_pair_workload_vs_oracle(gpu_lib, oracle_mod):
+    """The 512x512 workload (psize 7, PCA 8, leaf 32, k 1, n_subset 10%) end to end vs the oracle
+    pipeline on the same images: >= 99.9% identical."""
+    O = oracle_mod
+    from annfmp_gb300 import ANNFieldPropKDTreeGB300, gen
+    a, b = gen.pair_small(0, 512)
+    nsub = int(round(0.1 * 506 * 506))
+    m = ANNFieldPropKDTreeGB300(n_neighbors=1, psize=7, dim_reduced=8, n_subset=nsub, leaf_size=32, seed=0, verbose=0)
+    nn = m.fit(a, b)
+    nn_o = O.oracle_fit(a, b, n_neighbors=1, psize=7, dim_reduced=8, n_subset=nsub, leaf_size=32, seed=0)
+    agree = (nn == nn_o).mean()
+    assert agree >= 0.999, agree
+
+
+def test_image_and_array_paths_agree(gpu_lib, golden):
+    """annf_process_rows_img (patches read from the images) == annf_process_rows (patch arrays)."""
+    from oracle import oracle as O
+    from annfmp_gb300 import KDTree
+    z = golden("ref_pipeline_flow160.npz")
+    m, nn = _fit_gpu(z)
+    k, psize = int(z["params"][0]), int(z["params"][1])
+    pa, pb = O.extract_patches(z["a"], psize), O.extract_patches(z["b"], psize)
+    nr, nc = z["a"].shape[0] - psize + 1, z["a"].shape[1] - psize + 1
+    kd = KDTree(n_neighbors=k, leaf_size=int(z["params"][4]), splitting_type="longest", float_type="float")
+    kd.fit(m.patches_b_reduced_)
+    out = np.zeros(nr * nc, np.int32)
+    kd.process_rows(out, pa, pb, m.patches_a_reduced_, nr, nc, k, True, True)
+    assert np.array_equal(out, nn)
+
+
+# ---------------------------------------------------------------------------------------------
+# errors are raised, not silently worked around
+# ---------------------------------------------------------------------------------------------
+def test_errors(gpu_lib):
+    from annfmp_gb300 import ANNFieldPropKDTreeGB300, KDTree, _lib
+    X = np.random.default_rng(0).standard_normal((1000, 4)).astype(np.float32)
+    kd = KDTree(n_neighbors=33, leaf_size=64, float_type="float").fit(X)
+    with pytest.raises(NotImplementedError):
+        kd.kneighbors(X[:5])
+    kd = KDTree(n_neighbors=2, leaf_size=8, float_type="float", max_leaves=3).fit(X)
+    with pytest.raises(NotImplementedError):
+        kd.kneighbors(X[:5])
+    with pytest.raises(ValueError):
+        KDTree(n_neighbors=0).fit(X)
+    a = np.zeros((40, 40, 3), np.uint8)
+    with pytest.raises(AssertionError):  # annfmp/openmp/base.py:113
+        ANNFieldPropKDTreeGB300(n_neighbors=8, leaf_size=8, psize=5, dim_reduced=4, n_subset=2000, verbose=0).fit(a, a)
+    h = _lib.Handle(0)
+    with pytest.raises(_lib.AnnfError):
+        h.call("annf_kneighbors", None, 1, 1, 2147483640, None, None, None)  # no tree yet

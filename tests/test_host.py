@@ -1,0 +1,125 @@
+"""CPU-only checks of the host side: the C-ABI library builds and exports every declared symbol,
+the Python mirror of the reference interface keeps its parameters, and the product fails loudly
+without its CUDA library (no CPU fallback)."""
+import ctypes
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+
+
+def _declared_symbols():
+    hdr = open(os.path.join(ROOT, "include", "annf_gb300.h")).read()
+    hdr = re.sub(r"/\*.*?\*/", "", hdr, flags=re.S)
+    return sorted(set(re.findall(r"\b(annf_[a-z0-9_]+)\s*\(", hdr)))
+
+
+@pytest.fixture(scope="module")
+def built_lib():
+    from annfmp_gb300 import build as B
+    try:
+        B.nvcc()
+    except RuntimeError:
+        pytest.skip("nvcc not available")
+    return B.build()
+
+
+def test_library_exports_every_declared_symbol(built_lib):
+    syms = _declared_symbols()
+    assert "annf_process_rows" in syms and "annf_build_tree" in syms
+    out = subprocess.run(["nm", "-D", "--defined-only", built_lib], capture_output=True, text=True).stdout
+    exported = set(re.findall(r"\bT (annf_\w+)", out))
+    missing = [s for s in syms if s not in exported]
+    assert not missing, missing
+    lib = ctypes.CDLL(built_lib)  # loads without a GPU
+    for s in syms:
+        assert hasattr(lib, s)
+
+
+def test_binding_covers_header(built_lib):
+    from annfmp_gb300 import _lib
+    assert sorted(_lib.SIGNATURES) == _declared_symbols()
+    lib = _lib.load(built_lib)
+    assert lib.annf_version() >= 10000
+
+
+def test_no_cuda_device_is_an_error(built_lib):
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    from annfmp_gb300 import ANNFieldPropKDTreeGB300, KDTree
+    with pytest.raises(RuntimeError):
+        KDTree().fit(np.zeros((10, 2), np.float32))
+    with pytest.raises(RuntimeError):
+        ANNFieldPropKDTreeGB300(verbose=0).fit(np.zeros((20, 20, 3), np.uint8), np.zeros((20, 20, 3), np.uint8))
+    from annfmp_gb300 import _lib
+    h = ctypes.c_void_p()
+    assert _lib.load().annf_create(ctypes.byref(h), 0) == _lib.ANNF_ERR_CUDA
+
+
+def test_missing_library_fails_loudly(tmp_path):
+    from annfmp_gb300 import _lib
+    saved = _lib._lib
+    try:
+        _lib._lib = None
+        with pytest.raises(ImportError):
+            _lib.load(str(tmp_path / "nope.so"))
+    finally:
+        _lib._lib = saved
+
+
+def test_facade_parameters_mirror_reference():
+    from annfmp_gb300 import ANNField, ANNFieldPropKDTreeGB300, KDTree
+    f = ANNField()
+    assert f.get_params() == {"n_neighbors": 1, "psize": 8, "dim_reduced": 24, "n_subset": 1000,
+                              "algorithm": "gb300", "leaf_size": 64, "n_jobs": -1, "propagate": True,
+                              "select_best_nn": True, "verbose": 1, "seed": 0}
+    f.set_params(algorithm="openmp")
+    with pytest.raises(Exception, match="Unknown algorithm 'openmp'!"):
+        f.fit(np.zeros((8, 8, 3), np.uint8), np.zeros((8, 8, 3), np.uint8))
+    m = ANNFieldPropKDTreeGB300()
+    assert (m.n_neighbors, m.psize, m.dim_reduced, m.n_subset, m.leaf_size, m.float_type) == (3, 8, 5, 1000, 64, "float")
+    kd = KDTree()
+    assert kd.get_params() == {"n_neighbors": 5, "leaf_size": 30, "max_leaves": None, "tree_depth": None,
+                               "float_type": "double", "splitting_type": "cyclic", "n_jobs": 1, "verbose": 0}
+    assert kd._compute_final_tree_depth(4161600, 64, None) == 15
+    with pytest.warns(UserWarning):
+        assert kd._compute_final_tree_depth(100, 30, 99) == 6
+
+
+def test_patch_arrays_match_reference_layout(oracle_mod):
+    from annfmp_gb300 import ANNFieldPropKDTreeGB300
+    rng = np.random.default_rng(1)
+    a = rng.integers(0, 256, (23, 31, 3), dtype=np.uint8)
+    m = ANNFieldPropKDTreeGB300(psize=5)
+    m.image_a = a
+    assert np.array_equal(m.patches_a, oracle_mod.extract_patches(a, 5))
+
+
+def test_subset_positions_match_sklearn_sampling():
+    from annfmp_gb300.field import _SubsetCache
+    sk = pytest.importorskip("sklearn.feature_extraction.image")
+    import torch
+    img = np.arange(30 * 40 * 3, dtype=np.int64).reshape(30, 40, 3) % 251
+    img = img.astype(np.uint8)
+    pos = _SubsetCache().get(26, 36, 50, 7, torch.device("cpu")).numpy()
+    ref = sk.extract_patches_2d(img, (5, 5), max_patches=50, random_state=7)
+    got = np.stack([img[y:y + 5, x:x + 5] for y, x in pos])
+    assert np.array_equal(got, ref)
+
+
+def test_generators_are_seeded():
+    from annfmp_gb300 import gen
+    a1, b1 = gen.pair_small(0, 64)
+    a2, b2 = gen.pair_small(0, 64)
+    assert a1.dtype == np.uint8 and a1.shape == (64, 64, 3)
+    assert np.array_equal(a1, a2) and np.array_equal(b1, b2)
+    a3, _ = gen.pair_small(1, 64)
+    assert not np.array_equal(a1, a3)
+    a, b = gen.pair_flow(1, 96, sigma=8.0)
+    assert a.shape == b.shape == (96, 96, 3)
+    assert a.min() == 0 and a.max() == 255
