@@ -19,9 +19,10 @@ void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 int build_tree(annf_handle* h, const void* points, int n, int d, int real_type, int depth, int splitting,
                cudaStream_t st);
 int process_rows_generic(annf_handle* h, int* final_idx, const PatchSrc& A, const PatchSrc& B, const void* ared,
-                         int n_rows, int n_cols, int K, int propagate, int select_best, int* knn_out,
-                         float* dist_out, cudaStream_t st);
-int kneighbors_generic(annf_handle* h, const void* Q, int nq, int K, void* dist, int* idx, cudaStream_t st);
+                         int n_rows, int n_cols, int K, int propagate, int select_best, long long max_leaves,
+                         int* knn_out, float* dist_out, cudaStream_t st);
+int kneighbors_generic(annf_handle* h, const void* Q, int nq, int K, long long max_leaves, void* dist, int* idx,
+                       cudaStream_t st);
 int pca_fit(annf_handle* h, const uint8_t* img_a, int ha, int wa, const int* pos_a, int n_a, const uint8_t* img_b,
             int hb, int wb, const int* pos_b, int n_b, int c, int psize, int ncomp, double* comps, double* mean,
             cudaStream_t st);
@@ -139,9 +140,9 @@ static int check_k(const annf_handle* h, int k, long long max_leaves) {
     set_error("k > 32 is not supported by the GPU kernels");
     return ANNF_ERR_UNSUPPORTED;
   }
-  if (max_leaves < (1LL << h->depth)) {
-    set_error("a leaf budget smaller than the number of leaves (approximate first-row search) is not supported");
-    return ANNF_ERR_UNSUPPORTED;
+  if (max_leaves < 0) {  // annfmp/openmp/kdtree/base.py:129-130
+    set_error("max_leaves must be a positive integer");
+    return ANNF_ERR_INVALID;
   }
   return ANNF_OK;
 }
@@ -154,7 +155,7 @@ int annf_kneighbors(annf_handle* h, const void* queries, int nq, int k, long lon
   ANNF_REQUIRE(nq >= 0, "annf_kneighbors: nq < 0");
   if (nq == 0) return ANNF_OK;
   ANNF_REQUIRE(queries && distances && indices, "annf_kneighbors: NULL array");
-  return kneighbors_generic(h, queries, nq, k, distances, indices, static_cast<cudaStream_t>(stream));
+  return kneighbors_generic(h, queries, nq, k, max_leaves, distances, indices, static_cast<cudaStream_t>(stream));
 }
 
 static int rows_common_checks(annf_handle* h, int* final_idx, const void* ared, int n_rows, int n_cols, int k,
@@ -179,8 +180,8 @@ int annf_process_rows(annf_handle* h, int* final_idx, const uint8_t* patches_a, 
     ANNF_REQUIRE(n_b == h->n, "annf_process_rows: patches_b must have one row per tree point");
   }
   PatchSrc A{patches_a, 0, P, 1, 0, false}, B{patches_b, 0, P, 1, 0, false};
-  return process_rows_generic(h, final_idx, A, B, ared, n_rows, n_cols, k, propagate, select_best, knn_out,
-                              dist_out, static_cast<cudaStream_t>(stream));
+  return process_rows_generic(h, final_idx, A, B, ared, n_rows, n_cols, k, propagate, select_best, max_leaves,
+                              knn_out, dist_out, static_cast<cudaStream_t>(stream));
 }
 
 int annf_process_rows_img(annf_handle* h, int* final_idx, const uint8_t* img_a, int ha, int wa, const uint8_t* img_b,
@@ -199,8 +200,8 @@ int annf_process_rows_img(annf_handle* h, int* final_idx, const uint8_t* img_a, 
   }
   PatchSrc A{img_a, wa, channels, psize, wa - psize + 1, true};
   PatchSrc B{img_b, wb, channels, psize, wb - psize + 1, true};
-  return process_rows_generic(h, final_idx, A, B, ared, n_rows, n_cols, k, propagate, select_best, knn_out,
-                              dist_out, static_cast<cudaStream_t>(stream));
+  return process_rows_generic(h, final_idx, A, B, ared, n_rows, n_cols, k, propagate, select_best, max_leaves,
+                              knn_out, dist_out, static_cast<cudaStream_t>(stream));
 }
 
 int annf_pca_fit(annf_handle* h, const uint8_t* img_a, int ha, int wa, const int* pos_a, int n_a,

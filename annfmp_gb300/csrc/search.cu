@@ -4,18 +4,20 @@
 // Candidate order. The reference keeps a sorted K-list and inserts candidates one by one with a
 // strict '<' (annfmp/openmp/kdtree/src/kdtree.c:502-532), so the final list is the first K of the
 // candidates sorted stably by distance in visiting order; a point met twice is listed twice. Here
-// every candidate carries a 64-bit key (distance bits, tie) whose tie field encodes the visiting
-// order, so any parallel top-K over keys returns exactly the reference list:
+// every candidate carries a key (distance bits, tie) whose tie field encodes the visiting order, so
+// a top-K over keys, computed in any order, returns exactly the reference list:
 //   * row propagation (kdtree.c:305-352): tie = slot << leaf_bits | offset in leaf, slot 1 = the
 //     natural leaf, slots 2.. = the propagated leaves in neighbour order;
-//   * exact search (kdtree.c:129-268): the backtracking search visits leaves depth first, near
-//     child first, and prunes only subtrees whose every point is strictly farther than the current
-//     K-th distance, so its result equals the brute-force top-K with tie = dfs_rank(leaf) <<
-//     leaf_bits | offset, dfs_rank being the leaf's position in that query's visiting order
-//     (bit t = the leaf's branch at level t XOR the query's near side there);
+//   * exact search (kdtree.c:129-268): tie = dfs_rank(leaf) << leaf_bits | offset, dfs_rank being
+//     the leaf's position in that query's depth-first, near-child-first visiting order;
 //   * the K initial entries (K-th distance = max real, position 0; kdtree.c:141-144) carry tie 0.
 // Distances use the reference's order of operations with explicit round-to-nearest intrinsics so
 // that nothing is contracted into an FMA (helper.c:164-179).
+//
+// Lists. A warp owns one query at a time and keeps its K-list distributed over lanes (lane j holds
+// entry j, sorted); each batch of 32 candidates is checked against the K-th key with one ballot
+// and the few that qualify are inserted with a shuffle-shift, so the pruning threshold is always
+// exact.
 #include <algorithm>
 
 #include "common.cuh"
@@ -26,7 +28,7 @@ namespace annf {
 constexpr unsigned kFull = 0xffffffffu;
 
 // ---------------------------------------------------------------------------------------------
-// per-lane sorted list of KM (key, position) pairs and the warp-wide top-K merge
+// keys
 // ---------------------------------------------------------------------------------------------
 template <typename T> struct KeyOps;
 template <> struct KeyOps<float> {
@@ -37,6 +39,8 @@ template <> struct KeyOps<float> {
   __device__ static float dist(K k) { return __uint_as_float((uint32_t)(k >> 32)); }
   __device__ static bool lt(K a, K b) { return a < b; }
   __device__ static bool eq(K a, K b) { return a == b; }
+  __device__ static K shfl(K v, int src) { return __shfl_sync(kFull, v, src); }
+  __device__ static K shfl_up(K v, int d) { return __shfl_up_sync(kFull, v, d); }
   __device__ static K shfl_xor(K v, int m) { return __shfl_xor_sync(kFull, v, m); }
 };
 template <> struct KeyOps<double> {
@@ -47,9 +51,55 @@ template <> struct KeyOps<double> {
   __device__ static double dist(K k) { return __longlong_as_double((long long)k.d); }
   __device__ static bool lt(K a, K b) { return a.d < b.d || (a.d == b.d && a.tie < b.tie); }
   __device__ static bool eq(K a, K b) { return a.d == b.d && a.tie == b.tie; }
+  __device__ static K shfl(K v, int src) { return dkey{__shfl_sync(kFull, v.d, src), __shfl_sync(kFull, v.tie, src)}; }
+  __device__ static K shfl_up(K v, int d) { return dkey{__shfl_up_sync(kFull, v.d, d), __shfl_up_sync(kFull, v.tie, d)}; }
   __device__ static K shfl_xor(K v, int m) { return dkey{__shfl_xor_sync(kFull, v.d, m), __shfl_xor_sync(kFull, v.tie, m)}; }
 };
 
+// K-list distributed over the warp: lane j < K holds entry j (ascending); other lanes hold +inf
+template <typename T>
+struct WarpList {
+  using Ops = KeyOps<T>;
+  using Kt = typename Ops::K;
+  Kt key;
+  int pos;
+  Kt thr;  // entry K-1 (uniform)
+  int K, lane;
+  __device__ __forceinline__ void init(int K_, int lane_) {
+    K = K_;
+    lane = lane_;
+    key = lane < K ? Ops::init() : Ops::inf();
+    pos = 0;
+    thr = Ops::init();
+  }
+  __device__ __forceinline__ void insert(Kt c, int p) {  // c < thr, warp-uniform
+    const unsigned m = __ballot_sync(kFull, lane < K && Ops::lt(c, key));
+    const int ins = __ffs(m) - 1;
+    const Kt up = Ops::shfl_up(key, 1);
+    const int pup = __shfl_up_sync(kFull, pos, 1);
+    if (lane < K && lane > ins) {
+      key = up;
+      pos = pup;
+    }
+    if (lane == ins) {
+      key = c;
+      pos = p;
+    }
+    thr = Ops::shfl(key, K - 1);
+  }
+  // every lane offers at most one candidate; all that beat the K-th entry are inserted
+  __device__ __forceinline__ void offer(bool valid, Kt c, int p) {
+    unsigned m = __ballot_sync(kFull, valid && Ops::lt(c, thr));
+    while (m) {
+      const int src = __ffs(m) - 1;
+      insert(Ops::shfl(c, src), __shfl_sync(kFull, p, src));
+      m &= m - 1;
+      m &= __ballot_sync(kFull, valid && Ops::lt(c, thr));
+    }
+  }
+};
+
+// per-lane sorted list of KM entries + warp merge (used where every lane scans many candidates)
 template <typename T, int KM>
 struct LaneList {
   using Ops = KeyOps<T>;
@@ -60,13 +110,6 @@ struct LaneList {
 #pragma unroll
     for (int j = 0; j < KM; ++j) {
       key[j] = Ops::init();
-      pos[j] = 0;
-    }
-  }
-  __device__ void init_inf() {
-#pragma unroll
-    for (int j = 0; j < KM; ++j) {
-      key[j] = Ops::inf();
       pos[j] = 0;
     }
   }
@@ -150,12 +193,6 @@ struct QReg {
     }
     return acc;
   }
-  __device__ __forceinline__ T coord(int j) const {  // runtime index: rarely used
-    T r = v[0];
-#pragma unroll
-    for (int i = 1; i < D; ++i) r = (i == j) ? v[i] : r;
-    return r;
-  }
 };
 
 // runtime dimension: the query sits in a per-warp shared-memory slot
@@ -174,173 +211,216 @@ struct QReg<T, 0> {
     }
     return acc;
   }
-  __device__ __forceinline__ T coord(int j) const { return v[j]; }
 };
 
+// ---------------------------------------------------------------------------------------------
+// nodes: the top levels are cached in shared memory by the kernels that descend
+// ---------------------------------------------------------------------------------------------
+constexpr int kCacheLevels = 11;  // 2047 nodes
+
 template <typename T>
-__device__ __forceinline__ int natural_leaf(const TreeView<T>& tv, const T* __restrict__ q) {
+struct NodeCache {
+  int* axis;
+  T* split;
+  int n;  // cached nodes
+  __device__ void fill(const TreeView<T>& tv) {
+    const int lv = tv.depth < kCacheLevels ? tv.depth : kCacheLevels;
+    n = (1 << lv) - 1;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+      axis[i] = __ldg(tv.node_axis + i);
+      split[i] = __ldg(tv.node_split + i);
+    }
+  }
+  __device__ __forceinline__ void get(const TreeView<T>& tv, int node, int& ax, T& s) const {
+    if (node < n) {
+      ax = axis[node];
+      s = split[node];
+    } else {
+      ax = __ldg(tv.node_axis + node);
+      s = __ldg(tv.node_split + node);
+    }
+  }
+  static size_t bytes(int depth) {
+    const int lv = depth < kCacheLevels ? depth : kCacheLevels;
+    const size_t m = (size_t)(1 << lv);
+    return m * sizeof(int) + m * sizeof(T) + 32;
+  }
+  __device__ void carve(unsigned char*& p, int depth) {
+    const int lv = depth < kCacheLevels ? depth : kCacheLevels;
+    const int m = 1 << lv;
+    axis = reinterpret_cast<int*>(p);
+    split = reinterpret_cast<T*>(((uintptr_t)(axis + m) + 7) & ~uintptr_t(7));
+    p = reinterpret_cast<unsigned char*>(((uintptr_t)(split + m) + 15) & ~uintptr_t(15));
+  }
+};
+
+// leaf reached by descent: right when q[axis] - split >= 0 (kdtree.c:204)
+template <typename T>
+__device__ __forceinline__ int descend(const TreeView<T>& tv, const NodeCache<T>& nc, const T* q) {
   int node = 0;
   for (int l = 0; l < tv.depth; ++l) {
-    const int ax = __ldg(tv.node_axis + node);
-    const T s = __ldg(tv.node_split + node);
-    node = (q[ax] >= s) ? 2 * node + 2 : 2 * node + 1;  // q - split >= 0 (kdtree.c:204)
+    int ax;
+    T s;
+    nc.get(tv, node, ax, s);
+    node = (q[ax] >= s) ? 2 * node + 2 : 2 * node + 1;
   }
   return node - ((1 << tv.depth) - 1);
 }
 
-// ---------------------------------------------------------------------------------------------
-// natural leaf of every query + its top-K (slot 1)
-// ---------------------------------------------------------------------------------------------
+// natural leaf span of every query (thread per query)
+template <typename T>
+__global__ void __launch_bounds__(256) natural_leaf_kernel(TreeView<T> tv, const T* __restrict__ Q, long long q0,
+                                                           long long nq, int2* __restrict__ out) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  unsigned char* p = smem_raw;
+  NodeCache<T> nc;
+  nc.carve(p, tv.depth);
+  nc.fill(tv);
+  __syncthreads();
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < nq; i += (long long)gridDim.x * blockDim.x) {
+    const int lf = descend(tv, nc, Q + (q0 + i) * tv.d);
+    out[i] = make_int2(__ldg(tv.leaf_begin + lf), __ldg(tv.leaf_begin + lf + 1));
+  }
+}
+
+// natural leaf + its top-K for every query (warp per query); used when propagation is off
 template <typename T, int D, int KM>
 __global__ void __launch_bounds__(256) natural_knn_kernel(TreeView<T> tv, const T* __restrict__ Q, long long q0,
-                                                          long long nq, int K, typename KeyOps<T>::K* __restrict__ out_key,
-                                                          int* __restrict__ out_pos) {
-  __shared__ T sq[8][D > 0 ? 1 : kMaxDynD];
-  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+                                                          long long nq, int K, int* __restrict__ out_pos) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  unsigned char* p = smem_raw;
+  NodeCache<T> nc;
+  nc.carve(p, tv.depth);
+  T* sq = reinterpret_cast<T*>(p) + (threadIdx.x >> 5) * kMaxDynD;
+  nc.fill(tv);
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
   const long long gw = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
   const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
   const int d = tv.d;
   for (long long qi = q0 + gw; qi < q0 + nq; qi += nw) {
     const T* q = Q + qi * d;
+    __syncwarp();
+    for (int j = lane; j < d; j += 32) sq[j] = q[j];
+    __syncwarp();
     QReg<T, D> qr;
     if constexpr (D == 0) {
-      for (int j = lane; j < d; j += 32) sq[wib][j] = q[j];
-      __syncwarp();
-      qr.v = sq[wib];
+      qr.v = sq;
       qr.d = d;
     } else {
-      qr.load(q, d);
+      qr.load(sq, d);
     }
-    const int leaf = natural_leaf(tv, D == 0 ? sq[wib] : q);
+    const int leaf = descend(tv, nc, sq);
     const int beg = __ldg(tv.leaf_begin + leaf), end = __ldg(tv.leaf_begin + leaf + 1);
     LaneList<T, KM> L;
     L.init_entries();
     const uint32_t slot = 1u << tv.leaf_bits;
-    for (int p = beg + lane; p < end; p += 32) {
-      const T dd = qr.dist(tv.pts + (long long)p * d, d);
-      L.offer(KeyOps<T>::make(dd, slot | (uint32_t)(p - beg)), p);
+    for (int pp = beg + lane; pp < end; pp += 32) {
+      const T dd = qr.dist(tv.pts + (long long)pp * d, d);
+      L.offer(KeyOps<T>::make(dd, slot | (uint32_t)(pp - beg)), pp);
     }
     typename KeyOps<T>::K k;
-    int pos;
+    int pos = 0;
     warp_topk<T, KM>(L, K, lane, k, pos);
-    if (lane < K) {
-      if (out_key) out_key[qi * K + lane] = k;
-      out_pos[qi * K + lane] = pos;
-    }
-    if constexpr (D == 0) __syncwarp();
+    if (lane < K) out_pos[qi * K + lane] = pos;
   }
 }
 
 // ---------------------------------------------------------------------------------------------
-// exact kNN by brute force in the reference's visiting order: thread per query, leaves staged in
-// shared memory, leaf ranges split over blockIdx.y; partial lists merged afterwards
+// exact kNN with backtracking (first row, kneighbors): warp per query, DFS near child first,
+// far child pruned when (q[axis]-split)^2 > K-th distance, at most max_leaves leaves scanned --
+// the reference's traversal (kdtree.c:129-268), leaf scans spread over the lanes
 // ---------------------------------------------------------------------------------------------
-constexpr int kExactThreads = 128;
+constexpr int kDfsWarps = 8;
 
-template <typename T, int D, int KM>
-__global__ void __launch_bounds__(kExactThreads) exact_part_kernel(
-    TreeView<T> tv, const T* __restrict__ Q, int nq, int K, int leaves_per_split, int stage_pts,
-    typename KeyOps<T>::K* __restrict__ part_key, int* __restrict__ part_pos) {
+template <typename T, int D>
+__global__ void __launch_bounds__(32 * kDfsWarps) exact_dfs_kernel(TreeView<T> tv, const T* __restrict__ Q, int nq,
+                                                                    int K, long long max_leaves, int mode,
+                                                                    int* __restrict__ out_pos, T* __restrict__ out_dist,
+                                                                    int* __restrict__ out_idx) {
   using Ops = KeyOps<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int d = tv.d;
-  const int dstride = d + 1;  // padded row for runtime-axis reads without bank conflicts
-  T* sq = reinterpret_cast<T*>(smem_raw);                       // [kExactThreads][d+1]
-  T* spts = sq + kExactThreads * dstride;                       // [stage_pts][d]
-  spts = reinterpret_cast<T*>((reinterpret_cast<uintptr_t>(spts) + 15) & ~uintptr_t(15));
-  const int qi = blockIdx.x * kExactThreads + threadIdx.x;
-  const bool active = qi < nq;
-  for (int j = 0; j < d; ++j) sq[threadIdx.x * dstride + j] = active ? Q[(long long)qi * d + j] : T(0);
-  QReg<T, D> qr;
-  if constexpr (D == 0) {
-    qr.v = sq + threadIdx.x * dstride;
-    qr.d = d;
-  } else {
-#pragma unroll
-    for (int j = 0; j < D; ++j) qr.v[j] = sq[threadIdx.x * dstride + j];
-  }
-  LaneList<T, KM> L;
-  L.init_entries();
-  const int nleaves = 1 << tv.depth;
-  const int l0 = blockIdx.y * leaves_per_split, l1 = min(nleaves, l0 + leaves_per_split);
-  for (int lf = l0; lf < l1; ++lf) {
-    const int beg = __ldg(tv.leaf_begin + lf), end = __ldg(tv.leaf_begin + lf + 1);
-    const int cnt = end - beg;
-    __syncthreads();
-    for (int e = threadIdx.x; e < cnt * d; e += blockDim.x) spts[e] = tv.pts[(long long)beg * d + e];
-    __syncthreads();
-    // dfs rank of this leaf for this query
-    uint32_t rank = 0;
-    for (int t = 0; t < tv.depth; ++t) {
-      const int node = (1 << t) - 1 + (lf >> (tv.depth - t));
-      const int dir = (lf >> (tv.depth - 1 - t)) & 1;
-      const int ax = __ldg(tv.node_axis + node);
-      const int side = sq[threadIdx.x * dstride + ax] >= __ldg(tv.node_split + node) ? 1 : 0;
-      rank = (rank << 1) | (uint32_t)(dir ^ side);
+  unsigned char* p = smem_raw;
+  NodeCache<T> nc;
+  nc.carve(p, tv.depth);
+  const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  T* sq = reinterpret_cast<T*>(p) + wib * kMaxDynD;
+  p += kDfsWarps * kMaxDynD * sizeof(T);
+  T* sbound = reinterpret_cast<T*>(p) + wib * 32;
+  p += kDfsWarps * 32 * sizeof(T);
+  int* snode = reinterpret_cast<int*>(p) + wib * 32;
+  p += kDfsWarps * 32 * sizeof(int);
+  uint32_t* srank = reinterpret_cast<uint32_t*>(p) + wib * 32;
+  nc.fill(tv);
+  __syncthreads();
+  const int d = tv.d, depth = tv.depth;
+  const int first_leaf = (1 << depth) - 1;
+  for (int qi = blockIdx.x * kDfsWarps + wib; qi < nq; qi += gridDim.x * kDfsWarps) {
+    __syncwarp();
+    for (int j = lane; j < d; j += 32) sq[j] = Q[(long long)qi * d + j];
+    __syncwarp();
+    QReg<T, D> qr;
+    if constexpr (D == 0) {
+      qr.v = sq;
+      qr.d = d;
+    } else {
+      qr.load(sq, d);
     }
-    const uint32_t hi = rank << tv.leaf_bits;
-    if (active) {
-      for (int p = 0; p < cnt; ++p) {
-        T dd;
-        if constexpr (D > 0) {
-          using R = real_traits<T>;
-          const T* pp = spts + p * D;
-          T acc = 0;
-#pragma unroll
-          for (int j = 0; j < D; ++j) {
-            T t = R::sub(pp[j], qr.v[j]);
-            acc = R::add(acc, R::mul(t, t));
-          }
-          dd = acc;
-        } else {
-          using R = real_traits<T>;
-          const T* pp = spts + p * d;
-          T acc = 0;
-          for (int j = 0; j < d; ++j) {
-            T t = R::sub(pp[j], qr.v[j]);
-            acc = R::add(acc, R::mul(t, t));
-          }
-          dd = acc;
+    WarpList<T> L;
+    L.init(K, lane);
+    long long budget = max_leaves;
+    // stack of pending far children: node, dfs-rank prefix, lower bound on their distances
+    if (lane == 0) {
+      snode[0] = 0;
+      srank[0] = 0;
+      sbound[0] = T(0);
+    }
+    int sp = 1;
+    __syncwarp();
+    while (sp > 0) {
+      --sp;
+      int node = snode[sp];
+      uint32_t rank = srank[sp];
+      const T bound = sbound[sp];
+      __syncwarp();
+      if (bound > Ops::dist(L.thr)) continue;  // (q-s)^2 > d_min[K-1]: skip (kdtree.c:219, 236)
+      int level = 31 - __clz(node + 1);         // depth of 'node'
+      while (level < depth) {
+        int ax;
+        T s;
+        nc.get(tv, node, ax, s);
+        const T diff = real_traits<T>::sub(sq[ax], s);
+        const bool right = diff >= T(0);
+        if (lane == 0) {
+          snode[sp] = right ? 2 * node + 1 : 2 * node + 2;
+          srank[sp] = (rank << 1) | 1u;
+          sbound[sp] = real_traits<T>::mul(diff, diff);
         }
-        L.offer(Ops::make(dd, hi | (uint32_t)p), beg + p);
+        ++sp;
+        node = right ? 2 * node + 2 : 2 * node + 1;
+        rank <<= 1;
+        ++level;
+      }
+      __syncwarp();
+      if (budget <= 0) break;  // the reference stops at the leaf that exceeds max_leaves
+      --budget;
+      const int lf = node - first_leaf;
+      const int beg = __ldg(tv.leaf_begin + lf), end = __ldg(tv.leaf_begin + lf + 1);
+      const uint32_t hi = rank << tv.leaf_bits;
+      for (int base = beg; base < end; base += 32) {
+        const int pp = base + lane;
+        const bool valid = pp < end;
+        const T dd = valid ? qr.dist(tv.pts + (long long)pp * d, d) : T(0);
+        L.offer(valid, Ops::make(dd, hi | (uint32_t)(pp - beg)), pp);
       }
     }
-  }
-  if (active) {
-    const long long base = ((long long)blockIdx.y * nq + qi) * K;
-    for (int j = 0; j < K && j < KM; ++j) {
-      part_key[base + j] = L.key[j];
-      part_pos[base + j] = L.pos[j];
-    }
-  }
-}
-
-// merge the per-split lists: warp per query. mode 0: tree positions to out_pos; mode 1: square
-// rooted distances + original indices (kneighbors)
-template <typename T, int KM>
-__global__ void exact_merge_kernel(TreeView<T> tv, int nq, int K, int nsplit,
-                                   const typename KeyOps<T>::K* __restrict__ part_key,
-                                   const int* __restrict__ part_pos, int mode, int* __restrict__ out_pos,
-                                   T* __restrict__ out_dist, int* __restrict__ out_idx) {
-  const int lane = threadIdx.x & 31;
-  const long long qi = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
-  if (qi >= nq) return;
-  LaneList<T, KM> L;
-  L.init_entries();
-  for (int e = lane; e < nsplit * K; e += 32) {
-    const int sp = e / K, j = e - sp * K;
-    const long long src = ((long long)sp * nq + qi) * K + j;
-    L.offer(part_key[src], part_pos[src]);
-  }
-  typename KeyOps<T>::K k;
-  int pos;
-  warp_topk<T, KM>(L, K, lane, k, pos);
-  if (lane < K) {
-    if (mode == 0) {
-      out_pos[qi * K + lane] = pos;
-    } else {
-      out_dist[qi * K + lane] = real_traits<T>::sqrt_(KeyOps<T>::dist(k));
-      out_idx[qi * K + lane] = __ldg(tv.perm + pos);
+    if (lane < K) {
+      if (mode == 0) {
+        out_pos[(long long)qi * K + lane] = L.pos;
+      } else {
+        out_dist[(long long)qi * K + lane] = real_traits<T>::sqrt_(Ops::dist(L.key));
+        out_idx[(long long)qi * K + lane] = __ldg(tv.perm + L.pos);
+      }
     }
   }
 }
@@ -364,62 +444,99 @@ __global__ void next_range_kernel(TreeView<T> tv, int n_cols, long long nA, int2
   }
 }
 
-// one warp per column walks the rows downwards; lane j < K carries entry j of the row above
-template <typename T, int D, int KM>
+// One warp per column walks the rows downwards (row y depends only on row y-1 of the same column).
+// Per step: the natural leaf (span precomputed for every pixel) and the K propagated leaves; a
+// leaf that several slots share is scanned once and its points are offered once per slot.
+template <typename T, int D>
 __global__ void __launch_bounds__(128) chain_kernel(TreeView<T> tv, const T* __restrict__ Q, int n_rows, int n_cols,
-                                                    int K, const typename KeyOps<T>::K* __restrict__ nat_key,
-                                                    const int* __restrict__ nat_pos, const int2* __restrict__ next_range,
-                                                    int* __restrict__ lists) {
+                                                    int K, const int2* __restrict__ nat_range,
+                                                    const int2* __restrict__ next_range, int* __restrict__ lists) {
   using Ops = KeyOps<T>;
-  __shared__ T sq[4][D > 0 ? 1 : kMaxDynD];
+  __shared__ T sqbuf[4][D > 0 ? 1 : kMaxDynD];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const int x = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (x >= n_cols) return;
   const int d = tv.d;
+  const int lb = tv.leaf_bits;
   int my_pos = lane < K ? lists[(long long)x * K + lane] : 0;
-  for (int y = 1; y < n_rows; ++y) {
-    const long long qi = (long long)y * n_cols + x;
-    const T* q = Q + qi * d;
+  // nat_range is indexed from row 1: entry (y-1)*n_cols + x
+  int2 nat_next = __ldg(nat_range + x);
+  QReg<T, D> q_next;
+  if constexpr (D > 0) q_next.load(Q + ((long long)n_cols + x) * d, d);
+  long long qi = (long long)n_cols + x;
+  for (int y = 1; y < n_rows; ++y, qi += n_cols) {
+    const int2 nat = nat_next;
     QReg<T, D> qr;
-    if constexpr (D == 0) {
-      __syncwarp();
-      for (int j = lane; j < d; j += 32) sq[wib][j] = q[j];
-      __syncwarp();
-      qr.v = sq[wib];
-      qr.d = d;
+    if constexpr (D > 0) {
+      qr = q_next;
+      if (y + 1 < n_rows) {
+        q_next.load(Q + (qi + n_cols) * d, d);
+        nat_next = __ldg(nat_range + qi);  // row y+1
+      }
     } else {
-      qr.load(q, d);
+      __syncwarp();
+      for (int j = lane; j < d; j += 32) sqbuf[wib][j] = Q[qi * d + j];
+      __syncwarp();
+      qr.v = sqbuf[wib];
+      qr.d = d;
+      if (y + 1 < n_rows) nat_next = __ldg(nat_range + qi);
     }
-    typename Ops::K nk = Ops::inf();
-    int np = 0;
-    if (lane < K) {
-      nk = nat_key[qi * K + lane];
-      np = nat_pos[qi * K + lane];
-    }
-    const int2 my_rng = lane < K ? __ldg(next_range + my_pos) : make_int2(0, 0);
-    LaneList<T, KM> L;
-    L.init_entries();
-    L.offer(nk, np);
-    for (int j = 0; j < K; ++j) {
-      const int beg = __shfl_sync(kFull, my_rng.x, j), end = __shfl_sync(kFull, my_rng.y, j);
-      const uint32_t slot = (uint32_t)(j + 2) << tv.leaf_bits;
-      for (int p = beg + lane; p < end; p += 32) {
-        const T dd = qr.dist(tv.pts + (long long)p * d, d);
-        L.offer(Ops::make(dd, slot | (uint32_t)(p - beg)), p);
+    const int2 rng = lane < K ? __ldg(next_range + my_pos) : make_int2(-1, -1);
+    WarpList<T> L;
+    L.init(K, lane);
+    // slots: bit 0 = natural leaf, bit j+1 = propagated neighbour j
+    unsigned todo = (2u << K) - 1u;
+    while (todo) {
+      const int s0 = __ffs(todo) - 1;
+      const int b = s0 == 0 ? nat.x : __shfl_sync(kFull, rng.x, s0 - 1);
+      const int e = s0 == 0 ? nat.y : __shfl_sync(kFull, rng.y, s0 - 1);
+      const unsigned same = ((nat.x == b ? 1u : 0u) | (__ballot_sync(kFull, lane < K && rng.x == b) << 1)) & todo;
+      todo &= ~same;
+      for (int base = b; base < e; base += 32) {
+        const int pp = base + lane;
+        const bool valid = pp < e;
+        const T dd = valid ? qr.dist(tv.pts + (long long)pp * d, d) : T(0);
+        const uint32_t off = (uint32_t)(pp - b);
+        unsigned sl = same;
+        while (sl) {
+          const int s = __ffs(sl) - 1;
+          sl &= sl - 1;
+          L.offer(valid, Ops::make(dd, ((uint32_t)(s + 1) << lb) | off), pp);
+        }
       }
     }
-    typename Ops::K k;
-    int pos = 0;
-    warp_topk<T, KM>(L, K, lane, k, pos);
-    if (lane < K) lists[qi * K + lane] = pos;
-    my_pos = pos;
+    if (lane < K) lists[qi * K + lane] = L.pos;
+    my_pos = L.pos;
   }
 }
 
 // ---------------------------------------------------------------------------------------------
 // tree positions -> original indices, and the raw-patch re-rank (base.c:309-353, 362-374)
 // ---------------------------------------------------------------------------------------------
+// bytes [off, off+4) of a byte stream read through aligned 32-bit loads
+__device__ __forceinline__ unsigned load_word_at(const uint8_t* base, long long off) {
+  const unsigned* w = reinterpret_cast<const unsigned*>(base + (off & ~3LL));
+  const int sh = (int)(off & 3) * 8;
+  const unsigned lo = __ldg(w);
+  if (!sh) return lo;
+  return __funnelshift_r(lo, __ldg(w + 1), sh);
+}
 
+// sum over a row of n bytes of (a-b)^2, exact in int
+__device__ __forceinline__ int row_ssd(const uint8_t* abase, long long aoff, const uint8_t* bbase, long long boff,
+                                       int n) {
+  int s = 0;
+  int e = 0;
+  for (; e + 4 <= n; e += 4) {
+    const unsigned x = __vabsdiffu4(load_word_at(abase, aoff + e), load_word_at(bbase, boff + e));
+    s = (int)__dp4a(x, x, (unsigned)s);
+  }
+  for (; e < n; ++e) {
+    const int t = (int)__ldg(abase + aoff + e) - (int)__ldg(bbase + boff + e);
+    s += t * t;
+  }
+  return s;
+}
 
 template <typename T>
 __device__ __forceinline__ T patch_dist(const PatchSrc& A, long long ia, const PatchSrc& B, long long ib) {
@@ -428,14 +545,8 @@ __device__ __forceinline__ T patch_dist(const PatchSrc& A, long long ia, const P
   if (sizeof(T) == 8 || (long long)P * 65025 < (1LL << 24)) {
     long long acc = 0;  // every partial sum is exact in the reference's accumulator
     for (int r = 0; r < A.psize; ++r) {
-      const uint8_t* a = A.row(ia, r);
-      const uint8_t* b = B.row(ib, r);
-      int s = 0;
-      for (int e = 0; e < rowlen; ++e) {
-        const int t = (int)__ldg(a + e) - (int)__ldg(b + e);
-        s += t * t;
-      }
-      acc += s;
+      const long long ao = A.row(ia, r) - A.img, bo = B.row(ib, r) - B.img;
+      acc += row_ssd(A.img, ao, B.img, bo, rowlen);
     }
     return real_traits<T>::sqrt_((T)acc);
   } else {  // large patches: replay the reference's rounding of the running sum
@@ -499,7 +610,7 @@ static TreeView<T> view_of(const annf_handle* h) {
 
 static int pick_km(int K) { return K <= 1 ? 1 : K <= 4 ? 4 : K <= 8 ? 8 : K <= 16 ? 16 : 32; }
 
-static int num_sms() {
+int num_sms() {
   static int sms = 0;
   if (!sms) {
     int dev = 0;
@@ -510,116 +621,110 @@ static int num_sms() {
   return sms;
 }
 
-// dispatch on (D, KM) for float and KM for double
-#define ANNF_DISPATCH_KM(KMV, ...)                         \
-  switch (KMV) {                                           \
-    case 1: { constexpr int KM = 1; __VA_ARGS__; } break;  \
-    case 4: { constexpr int KM = 4; __VA_ARGS__; } break;  \
-    case 8: { constexpr int KM = 8; __VA_ARGS__; } break;  \
+#define ANNF_DISPATCH_KM(KMV, ...)                          \
+  switch (KMV) {                                            \
+    case 1: { constexpr int KM = 1; __VA_ARGS__; } break;   \
+    case 4: { constexpr int KM = 4; __VA_ARGS__; } break;   \
+    case 8: { constexpr int KM = 8; __VA_ARGS__; } break;   \
     case 16: { constexpr int KM = 16; __VA_ARGS__; } break; \
     default: { constexpr int KM = 32; __VA_ARGS__; } break; \
   }
 
-template <typename T, int D, int KM>
-static int exact_knn_typed(annf_handle* h, const T* Q, int nq, int K, int mode, int* out_pos, T* out_dist,
-                           int* out_idx, cudaStream_t st) {
-  using Kt = typename KeyOps<T>::K;
+// compile-time dimension for the common reduced sizes (FP32), runtime dimension otherwise
+#define ANNF_DISPATCH_D(T, dval, ...)                                         \
+  do {                                                                        \
+    bool done_ = false;                                                       \
+    if constexpr (sizeof(T) == 4) {                                           \
+      switch (dval) {                                                         \
+        case 8: { constexpr int D = 8; __VA_ARGS__; done_ = true; } break;    \
+        case 12: { constexpr int D = 12; __VA_ARGS__; done_ = true; } break;  \
+        case 16: { constexpr int D = 16; __VA_ARGS__; done_ = true; } break;  \
+        default: break;                                                       \
+      }                                                                       \
+    }                                                                         \
+    if (!done_) { constexpr int D = 0; __VA_ARGS__; }                         \
+  } while (0)
+
+template <typename T, int D>
+static int exact_knn_typed(annf_handle* h, const T* Q, int nq, int K, long long max_leaves, int mode, int* out_pos,
+                           T* out_dist, int* out_idx, cudaStream_t st) {
   TreeView<T> tv = view_of<T>(h);
-  const int nleaves = 1 << h->depth;
-  const int tiles = ceil_div(nq, kExactThreads);
-  int want = std::max(1, (8 * num_sms()) / tiles);
-  int lps = std::max(1, ceil_div(nleaves, want));
-  int nsplit = ceil_div(nleaves, lps);
-  ANNF_ENSURE(h->part_keys, (size_t)nsplit * nq * K * sizeof(Kt));
-  ANNF_ENSURE(h->part_pos, (size_t)nsplit * nq * K * sizeof(int));
-  const size_t smem = (size_t)kExactThreads * (h->d + 1) * sizeof(T) + 16 + (size_t)h->max_leaf * h->d * sizeof(T);
-  if (smem > 200 * 1024) {
-    set_error("exact search: leaf too large to stage in shared memory");
-    return ANNF_ERR_UNSUPPORTED;
-  }
-  ANNF_CUDA_TRY(cudaFuncSetAttribute(exact_part_kernel<T, D, KM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  dim3 grid(tiles, nsplit);
-  exact_part_kernel<T, D, KM><<<grid, kExactThreads, smem, st>>>(tv, Q, nq, K, lps, h->max_leaf,
-                                                                  h->part_keys.as<Kt>(), h->part_pos.as<int>());
-  ANNF_CHECK_LAUNCH();
-  exact_merge_kernel<T, KM><<<ceil_div((long long)nq * 32, 256), 256, 0, st>>>(
-      tv, nq, K, nsplit, h->part_keys.as<Kt>(), h->part_pos.as<int>(), mode, out_pos, out_dist, out_idx);
+  const size_t smem = NodeCache<T>::bytes(h->depth) + kDfsWarps * (kMaxDynD * sizeof(T) + 32 * sizeof(T) + 64) + 64;
+  ANNF_CUDA_TRY(cudaFuncSetAttribute(exact_dfs_kernel<T, D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  const int blocks = std::max(1, std::min(ceil_div(nq, kDfsWarps), 32 * num_sms()));
+  exact_dfs_kernel<T, D><<<blocks, 32 * kDfsWarps, smem, st>>>(tv, Q, nq, K, max_leaves, mode, out_pos, out_dist,
+                                                                 out_idx);
   ANNF_CHECK_LAUNCH();
   return ANNF_OK;
 }
 
 template <typename T>
-static int exact_knn(annf_handle* h, const T* Q, int nq, int K, int mode, int* out_pos, T* out_dist, int* out_idx,
-                     cudaStream_t st) {
-  const int km = pick_km(K);
-  if constexpr (sizeof(T) == 4) {
-    switch (h->d) {
-      case 8: ANNF_DISPATCH_KM(km, return exact_knn_typed<T, 8, KM>(h, Q, nq, K, mode, out_pos, out_dist, out_idx, st));
-      case 12: ANNF_DISPATCH_KM(km, return exact_knn_typed<T, 12, KM>(h, Q, nq, K, mode, out_pos, out_dist, out_idx, st));
-      case 16: ANNF_DISPATCH_KM(km, return exact_knn_typed<T, 16, KM>(h, Q, nq, K, mode, out_pos, out_dist, out_idx, st));
-      default: break;
-    }
-  }
-  ANNF_DISPATCH_KM(km, return exact_knn_typed<T, 0, KM>(h, Q, nq, K, mode, out_pos, out_dist, out_idx, st));
-  return ANNF_OK;
+static int exact_knn(annf_handle* h, const T* Q, int nq, int K, long long max_leaves, int mode, int* out_pos,
+                     T* out_dist, int* out_idx, cudaStream_t st) {
+  int rc = ANNF_OK;
+  ANNF_DISPATCH_D(T, h->d, rc = (exact_knn_typed<T, D>(h, Q, nq, K, max_leaves, mode, out_pos, out_dist, out_idx, st)));
+  return rc;
 }
 
-template <typename T, int D, int KM>
+template <typename T, int D>
 static int rows_typed(annf_handle* h, const T* ared, int n_rows, int n_cols, int K, int propagate, cudaStream_t st) {
-  using Kt = typename KeyOps<T>::K;
   TreeView<T> tv = view_of<T>(h);
   const long long nA = (long long)n_rows * n_cols;
   int* lists = h->lists.as<int>();
-  if (n_rows > 1) {
-    const long long nq = nA - n_cols;
+  if (n_rows <= 1) return ANNF_OK;
+  const long long nq = nA - n_cols;
+  if (propagate) {
+    ANNF_ENSURE(h->nat_pos, (size_t)nq * sizeof(int2));
+    const size_t smem = NodeCache<T>::bytes(h->depth);
+    natural_leaf_kernel<T><<<(int)std::min<long long>(ceil_div(nq, 256), 16LL * num_sms()), 256, smem, st>>>(
+        tv, ared, n_cols, nq, h->nat_pos.as<int2>());
+    ANNF_CHECK_LAUNCH();
+    prof_mark(h, "natural_leaf", st);
+    ANNF_ENSURE(h->next_range, (size_t)h->n * sizeof(int2));
+    next_range_kernel<T><<<std::min(ceil_div(h->n, 256), 16 * num_sms()), 256, 0, st>>>(
+        tv, n_cols, nA, h->next_range.as<int2>(), h->status.as<unsigned>());
+    ANNF_CHECK_LAUNCH();
+    prof_mark(h, "next_range", st);
+    chain_kernel<T, D><<<ceil_div((long long)n_cols * 32, 128), 128, 0, st>>>(
+        tv, ared, n_rows, n_cols, K, h->nat_pos.as<int2>(), h->next_range.as<int2>(), lists);
+    ANNF_CHECK_LAUNCH();
+    prof_mark(h, "chain", st);
+  } else {
+    const size_t smem = NodeCache<T>::bytes(h->depth) + 8 * kMaxDynD * sizeof(T);
     const int blocks = (int)std::min<long long>(ceil_div(nq * 32, 256), 64LL * num_sms());
-    if (propagate) {
-      ANNF_ENSURE(h->nat_keys, (size_t)nA * K * sizeof(Kt));
-      ANNF_ENSURE(h->nat_pos, (size_t)nA * K * sizeof(int));
-      natural_knn_kernel<T, D, KM><<<blocks, 256, 0, st>>>(tv, ared, n_cols, nq, K, h->nat_keys.as<Kt>(), h->nat_pos.as<int>());
-      ANNF_CHECK_LAUNCH();
-      prof_mark(h, "natural_knn", st);
-      ANNF_ENSURE(h->next_range, (size_t)h->n * sizeof(int2));
-      next_range_kernel<T><<<std::min(ceil_div(h->n, 256), 16 * num_sms()), 256, 0, st>>>(
-          tv, n_cols, nA, h->next_range.as<int2>(), h->status.as<unsigned>());
-      ANNF_CHECK_LAUNCH();
-      prof_mark(h, "next_range", st);
-      chain_kernel<T, D, KM><<<ceil_div((long long)n_cols * 32, 128), 128, 0, st>>>(
-          tv, ared, n_rows, n_cols, K, h->nat_keys.as<Kt>(), h->nat_pos.as<int>(), h->next_range.as<int2>(), lists);
-      ANNF_CHECK_LAUNCH();
-      prof_mark(h, "chain", st);
-    } else {
-      natural_knn_kernel<T, D, KM><<<blocks, 256, 0, st>>>(tv, ared, n_cols, nq, K, nullptr, lists);
-      ANNF_CHECK_LAUNCH();
-      prof_mark(h, "natural_knn", st);
+    const int km = pick_km(K);
+    int rc = ANNF_OK;
+    ANNF_DISPATCH_KM(km, {
+      cudaError_t e = cudaFuncSetAttribute(natural_knn_kernel<T, D, KM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)smem);
+      if (e != cudaSuccess) rc = ANNF_ERR_CUDA;
+      natural_knn_kernel<T, D, KM><<<blocks, 256, smem, st>>>(tv, ared, n_cols, nq, K, lists);
+    });
+    if (rc != ANNF_OK) {
+      set_error("natural_knn_kernel: cudaFuncSetAttribute failed");
+      return rc;
     }
+    ANNF_CHECK_LAUNCH();
+    prof_mark(h, "natural_knn", st);
   }
   return ANNF_OK;
 }
 
 template <typename T>
 static int rows_dispatch(annf_handle* h, const T* ared, int n_rows, int n_cols, int K, int propagate, cudaStream_t st) {
-  const int km = pick_km(K);
-  if constexpr (sizeof(T) == 4) {
-    switch (h->d) {
-      case 8: ANNF_DISPATCH_KM(km, return rows_typed<T, 8, KM>(h, ared, n_rows, n_cols, K, propagate, st));
-      case 12: ANNF_DISPATCH_KM(km, return rows_typed<T, 12, KM>(h, ared, n_rows, n_cols, K, propagate, st));
-      case 16: ANNF_DISPATCH_KM(km, return rows_typed<T, 16, KM>(h, ared, n_rows, n_cols, K, propagate, st));
-      default: break;
-    }
-  }
-  ANNF_DISPATCH_KM(km, return rows_typed<T, 0, KM>(h, ared, n_rows, n_cols, K, propagate, st));
-  return ANNF_OK;
+  int rc = ANNF_OK;
+  ANNF_DISPATCH_D(T, h->d, rc = (rows_typed<T, D>(h, ared, n_rows, n_cols, K, propagate, st)));
+  return rc;
 }
 
 template <typename T>
 static int process_rows_impl(annf_handle* h, int* final_idx, PatchSrc A, PatchSrc B, const T* ared, int n_rows,
-                             int n_cols, int K, int propagate, int select_best, int* knn_out, float* dist_out,
-                             cudaStream_t st) {
+                             int n_cols, int K, int propagate, int select_best, long long max_leaves, int* knn_out,
+                             float* dist_out, cudaStream_t st) {
   const long long nA = (long long)n_rows * n_cols;
   ANNF_ENSURE(h->lists, (size_t)nA * K * sizeof(int));
   prof_mark(h, "rows:begin", st);
-  int rc = exact_knn<T>(h, ared, n_cols, K, 0, h->lists.as<int>(), nullptr, nullptr, st);
+  int rc = exact_knn<T>(h, ared, n_cols, K, max_leaves, 0, h->lists.as<int>(), nullptr, nullptr, st);
   if (rc != ANNF_OK) return rc;
   prof_mark(h, "first_row", st);
   rc = rows_dispatch<T>(h, ared, n_rows, n_cols, K, propagate, st);
@@ -633,19 +738,22 @@ static int process_rows_impl(annf_handle* h, int* final_idx, PatchSrc A, PatchSr
 }
 
 int process_rows_generic(annf_handle* h, int* final_idx, const PatchSrc& A, const PatchSrc& B, const void* ared,
-                         int n_rows, int n_cols, int K, int propagate, int select_best, int* knn_out,
-                         float* dist_out, cudaStream_t st) {
+                         int n_rows, int n_cols, int K, int propagate, int select_best, long long max_leaves,
+                         int* knn_out, float* dist_out, cudaStream_t st) {
   if (h->real_type == ANNF_REAL_F32)
     return process_rows_impl<float>(h, final_idx, A, B, static_cast<const float*>(ared), n_rows, n_cols, K, propagate,
-                                    select_best, knn_out, dist_out, st);
+                                    select_best, max_leaves, knn_out, dist_out, st);
   return process_rows_impl<double>(h, final_idx, A, B, static_cast<const double*>(ared), n_rows, n_cols, K, propagate,
-                                   select_best, knn_out, dist_out, st);
+                                   select_best, max_leaves, knn_out, dist_out, st);
 }
 
-int kneighbors_generic(annf_handle* h, const void* Q, int nq, int K, void* dist, int* idx, cudaStream_t st) {
+int kneighbors_generic(annf_handle* h, const void* Q, int nq, int K, long long max_leaves, void* dist, int* idx,
+                       cudaStream_t st) {
   if (h->real_type == ANNF_REAL_F32)
-    return exact_knn<float>(h, static_cast<const float*>(Q), nq, K, 1, nullptr, static_cast<float*>(dist), idx, st);
-  return exact_knn<double>(h, static_cast<const double*>(Q), nq, K, 1, nullptr, static_cast<double*>(dist), idx, st);
+    return exact_knn<float>(h, static_cast<const float*>(Q), nq, K, max_leaves, 1, nullptr, static_cast<float*>(dist),
+                            idx, st);
+  return exact_knn<double>(h, static_cast<const double*>(Q), nq, K, max_leaves, 1, nullptr,
+                           static_cast<double*>(dist), idx, st);
 }
 
 }  // namespace annf

@@ -187,7 +187,7 @@ class _DevArray:
 
     def __init__(self, p: int, shape, dtype):
         self.__cuda_array_interface__ = {"shape": tuple(shape), "typestr": np.dtype(dtype).str,
-                                         "data": (int(p), True), "version": 2, "strides": None}
+                                         "data": (int(p), False), "version": 2, "strides": None}
 
 
 def device_view(p: int, shape, dtype, device) -> torch.Tensor:

@@ -77,7 +77,8 @@ int annf_tree_get(const annf_handle* h, annf_tree_view* out);
 
 /* Exact k nearest neighbours of nq queries ([nq*d], real_type of the tree). distances [nq*k]
  * (Euclidean, i.e. square-rooted) and indices [nq*k] (original point indices), best first.
- * max_leaves must be >= the number of leaves (exact search); smaller budgets are unsupported.
+ * At most max_leaves leaves are scanned, in the reference's depth-first order (exact when
+ * max_leaves >= 2^depth; the reference's default is 2147483640).
  * Replaces neighbors_extern (annfmp/openmp/kdtree/src/base.c:88-132, include/base.h:67-78). */
 int annf_kneighbors(annf_handle* h, const void* queries, int nq, int k, long long max_leaves,
                     void* distances, int* indices, void* stream);

@@ -104,6 +104,25 @@ def test_kneighbors_vs_oracle(gpu_lib, oracle_mod, K, dtype, d):
     assert np.array_equal(_bits(dg), _bits(do))
 
 
+@pytest.mark.parametrize("max_leaves", [0, 1, 3, 17, 200])
+@pytest.mark.parametrize("K", [1, 4])
+def test_kneighbors_leaf_budget_vs_oracle(gpu_lib, oracle_mod, max_leaves, K):
+    """A leaf budget cuts the search after the same leaves as the reference's traversal."""
+    from annfmp_gb300 import KDTree
+    O = oracle_mod
+    rng = np.random.default_rng(max_leaves + 11 * K)
+    X = (rng.standard_normal((20000, 8)) * 5).astype(np.float32)
+    Q = (rng.standard_normal((257, 8)) * 5).astype(np.float32)
+    depth = O.tree_depth(20000, 16)
+    ot = O.OracleTree(X, depth)
+    kd = KDTree(n_neighbors=K, tree_depth=depth, float_type="float", splitting_type="longest",
+                max_leaves=max_leaves).fit(X)
+    dg, ig = kd.kneighbors(Q)
+    do, io = ot.kneighbors(Q, K, max_leaves=max_leaves)
+    assert np.array_equal(ig, io)
+    assert np.array_equal(_bits(dg), _bits(do))
+
+
 # ---------------------------------------------------------------------------------------------
 # row propagation (reference process_rows_extern)
 # ---------------------------------------------------------------------------------------------
@@ -181,7 +200,7 @@ def test_projection_rounds_like_fp64(gpu_lib, oracle_mod, golden, name):
     from annfmp_gb300 import _lib
     from annfmp_gb300._torch import ptr, stream_ptr
     dev = torch.device("cuda", 0)
-    comps = torch.from_numpy(z["components"]).to(dev)
+    comps = torch.from_numpy(np.ascontiguousarray(z["components"])).to(dev)
     mean = torch.from_numpy(z["mean"]).to(dev)
     psize = int(z["params"][1])
     img = torch.from_numpy(z["a"]).to(dev)
@@ -280,9 +299,8 @@ def test_errors(gpu_lib):
     kd = KDTree(n_neighbors=33, leaf_size=64, float_type="float").fit(X)
     with pytest.raises(NotImplementedError):
         kd.kneighbors(X[:5])
-    kd = KDTree(n_neighbors=2, leaf_size=8, float_type="float", max_leaves=3).fit(X)
-    with pytest.raises(NotImplementedError):
-        kd.kneighbors(X[:5])
+    with pytest.raises(Exception, match="max_leaves"):
+        KDTree(n_neighbors=2, leaf_size=8, float_type="float", max_leaves=-1).fit(X)
     with pytest.raises(ValueError):
         KDTree(n_neighbors=0).fit(X)
     a = np.zeros((40, 40, 3), np.uint8)
