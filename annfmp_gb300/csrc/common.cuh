@@ -51,7 +51,25 @@ enum : unsigned {
   DEV_BAD_INDEX = 1u,
   DEV_BAD_LEAF = 2u,
   DEV_LIST_OVERFLOW = 4u,
+  DEV_SMEM_CARVE = 8u,  // a kernel's shared-memory carve exceeded its launch allocation
 };
+
+__device__ __forceinline__ unsigned dyn_smem_size() {
+  unsigned r;
+  asm("mov.u32 %0, %%dynamic_smem_size;" : "=r"(r));
+  return r;
+}
+
+// true (and the status bit set) when the carve [base, end) does not fit the dynamic allocation;
+// the caller returns before touching shared memory
+__device__ __forceinline__ bool smem_overrun(const void* base, const void* end, unsigned* status) {
+  const size_t used = (size_t)((const unsigned char*)end - (const unsigned char*)base);
+  if (used > dyn_smem_size()) {
+    if (threadIdx.x == 0 && status) atomicOr(status, DEV_SMEM_CARVE);
+    return true;
+  }
+  return false;
+}
 
 // ------------------------------------------------------------------------------------------
 // scalar traits
@@ -149,6 +167,7 @@ struct TreeView {
   const T* node_split;      // [2^depth-1]
   const int* leaf_begin;    // [2^depth+1] (leaf l spans [leaf_begin[l], leaf_begin[l+1]))
   const int* point_leaf;    // [n] original index -> leaf
+  unsigned* status;         // device status word (bounds checks)
 };
 
 // Source of raw uint8 patches: an HxWxC image (patch index = y*ncols + x) or a patch array

@@ -231,7 +231,8 @@ __global__ void __launch_bounds__(kPTW * kPTH) project_kernel(const uint8_t* __r
                                                                int psize, int rw, int ncomp,
                                                                const int8_t* __restrict__ digits,
                                                                const int* __restrict__ expo,
-                                                               const double* __restrict__ mproj, OutT* __restrict__ out) {
+                                                               const double* __restrict__ mproj, OutT* __restrict__ out,
+                                                               unsigned* status) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int nrows = H - psize + 1, ncols = W - psize + 1;
   const int x0 = blockIdx.x * kPTW, y0 = blockIdx.y * kPTH;
@@ -246,6 +247,7 @@ __global__ void __launch_bounds__(kPTW * kPTH) project_kernel(const uint8_t* __r
   const int reg_stride = ((reg_bytes + 7) / 4 + 1) * 4;  // bytes, word aligned, with slack
   unsigned* sreg = reinterpret_cast<unsigned*>(sdig + dig_words);
   uint8_t* sregb = reinterpret_cast<uint8_t*>(sreg);
+  if (smem_overrun(smem, sregb + reg_rows * reg_stride, status)) return;
   for (int e = threadIdx.x; e < reg_rows * reg_stride; e += blockDim.x) {
     const int rr = e / reg_stride, bb = e - rr * reg_stride;
     const int gy = y0 + rr, gxb = x0 * c + bb;
@@ -382,12 +384,14 @@ int project(annf_handle* h, const uint8_t* img, int H, int W, int c, int psize, 
       ANNF_CUDA_TRY(cudaFuncSetAttribute(project_kernel<float, WV>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
                                          (int)smem));                                                            \
       project_kernel<float, WV><<<grid, kPTW * kPTH, smem, st>>>(img, H, W, c, psize, rw, ncomp, dig, expo,       \
-                                                                  h->meanproj.as<double>(), (float*)out);        \
+                                                                  h->meanproj.as<double>(), (float*)out,      \
+                                                                  h->status.as<unsigned>());        \
     } else {                                                                                                     \
       ANNF_CUDA_TRY(cudaFuncSetAttribute(project_kernel<double, WV>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
                                          (int)smem));                                                            \
       project_kernel<double, WV><<<grid, kPTW * kPTH, smem, st>>>(img, H, W, c, psize, rw, ncomp, dig, expo,      \
-                                                                   h->meanproj.as<double>(), (double*)out);      \
+                                                                   h->meanproj.as<double>(), (double*)out,    \
+                                                                   h->status.as<unsigned>());      \
     }                                                                                                            \
     break;
   switch (W4) {

@@ -275,6 +275,7 @@ __global__ void __launch_bounds__(256) natural_leaf_kernel(TreeView<T> tv, const
   unsigned char* p = smem_raw;
   NodeCache<T> nc;
   nc.carve(p, tv.depth);
+  if (smem_overrun(smem_raw, p, tv.status)) return;
   nc.fill(tv);
   __syncthreads();
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < nq; i += (long long)gridDim.x * blockDim.x) {
@@ -292,6 +293,7 @@ __global__ void __launch_bounds__(256) natural_knn_kernel(TreeView<T> tv, const 
   NodeCache<T> nc;
   nc.carve(p, tv.depth);
   T* sq = reinterpret_cast<T*>(p) + (threadIdx.x >> 5) * kMaxDynD;
+  if (smem_overrun(smem_raw, reinterpret_cast<T*>(p) + (blockDim.x >> 5) * kMaxDynD, tv.status)) return;
   nc.fill(tv);
   __syncthreads();
   const int lane = threadIdx.x & 31;
@@ -351,6 +353,8 @@ __global__ void __launch_bounds__(32 * kDfsWarps) exact_dfs_kernel(TreeView<T> t
   int* snode = reinterpret_cast<int*>(p) + wib * 32;
   p += kDfsWarps * 32 * sizeof(int);
   uint32_t* srank = reinterpret_cast<uint32_t*>(p) + wib * 32;
+  p += kDfsWarps * 32 * sizeof(uint32_t);
+  if (smem_overrun(smem_raw, p, tv.status)) return;
   nc.fill(tv);
   __syncthreads();
   const int d = tv.d, depth = tv.depth;
@@ -605,6 +609,7 @@ static TreeView<T> view_of(const annf_handle* h) {
   tv.node_split = h->node_split.as<T>();
   tv.leaf_begin = h->leaf_begin.as<int>();
   tv.point_leaf = h->point_leaf.as<int>();
+  tv.status = h->status.as<unsigned>();
   return tv;
 }
 
@@ -649,7 +654,9 @@ template <typename T, int D>
 static int exact_knn_typed(annf_handle* h, const T* Q, int nq, int K, long long max_leaves, int mode, int* out_pos,
                            T* out_dist, int* out_idx, cudaStream_t st) {
   TreeView<T> tv = view_of<T>(h);
-  const size_t smem = NodeCache<T>::bytes(h->depth) + kDfsWarps * (kMaxDynD * sizeof(T) + 32 * sizeof(T) + 64) + 64;
+  // node cache + per warp: query copy, stack of bounds, stack of nodes, stack of rank prefixes
+  const size_t smem = NodeCache<T>::bytes(h->depth) +
+                      kDfsWarps * (kMaxDynD * sizeof(T) + 32 * sizeof(T) + 32 * sizeof(int) + 32 * sizeof(uint32_t)) + 64;
   ANNF_CUDA_TRY(cudaFuncSetAttribute(exact_dfs_kernel<T, D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   const int blocks = std::max(1, std::min(ceil_div(nq, kDfsWarps), 32 * num_sms()));
   exact_dfs_kernel<T, D><<<blocks, 32 * kDfsWarps, smem, st>>>(tv, Q, nq, K, max_leaves, mode, out_pos, out_dist,

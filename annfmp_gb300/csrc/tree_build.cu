@@ -369,7 +369,7 @@ __global__ void __launch_bounds__(kSubThreads) subtree_kernel(
     int n, int d, int depth, int t0, int smax, int splitting, const T* __restrict__ pts_in,
     const int* __restrict__ perm_in, T* __restrict__ pts_out, int* __restrict__ perm_out,
     int* __restrict__ node_axis, T* __restrict__ node_split, int* __restrict__ leaf_begin,
-    int* __restrict__ point_leaf) {
+    int* __restrict__ point_leaf, unsigned* status) {
   using K = typename key_of<T>::type;
   extern __shared__ __align__(16) unsigned char smem[];
   T* spts = reinterpret_cast<T*>(smem);
@@ -378,6 +378,7 @@ __global__ void __launch_bounds__(kSubThreads) subtree_kernel(
   unsigned* shist = reinterpret_cast<unsigned*>(sperm + smax);
   uint16_t* sidx0 = reinterpret_cast<uint16_t*>(shist + kSubWarps * 256);
   uint16_t* sidx1 = sidx0 + smax;
+  if (smem_overrun(smem, sidx1 + smax, status)) return;
 
   const int s = blockIdx.x;
   int lo, hi;
@@ -588,7 +589,7 @@ static int build_impl(annf_handle* h, const T* points, int n, int d, int depth, 
       ANNF_CUDA_TRY(cudaFuncSetAttribute(subtree_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sub_smem));
       subtree_kernel<T><<<S, kSubThreads, sub_smem, st>>>(
           n, d, depth, t, smax, splitting, cur_pts, cur_perm, alt_pts, alt_perm, h->node_axis.as<int>(),
-          h->node_split.as<T>(), h->leaf_begin.as<int>(), h->point_leaf.as<int>());
+          h->node_split.as<T>(), h->leaf_begin.as<int>(), h->point_leaf.as<int>(), h->status.as<unsigned>());
       ANNF_CHECK_LAUNCH();
       std::swap(cur_pts, alt_pts);
       std::swap(cur_perm, alt_perm);
