@@ -168,6 +168,7 @@ struct TreeView {
   const int* leaf_begin;    // [2^depth+1] (leaf l spans [leaf_begin[l], leaf_begin[l+1]))
   const int* point_leaf;    // [n] original index -> leaf
   unsigned* status;         // device status word (bounds checks)
+  const T* leaf_box;        // [2^depth][2][d] per-leaf min / max
 };
 
 // Source of raw uint8 patches: an HxWxC image (patch index = y*ncols + x) or a patch array

@@ -51,7 +51,7 @@ struct annf_handle {
   // ---- current tree ----
   int built = 0;
   int n = 0, d = 0, depth = 0, real_type = ANNF_REAL_F32, leaf_bits = 1, max_leaf = 0;
-  annf::DevBuf pts, pts_tmp, perm, perm_tmp, node_axis, node_split, leaf_begin, point_leaf;
+  annf::DevBuf pts, pts_tmp, perm, perm_tmp, node_axis, node_split, leaf_begin, point_leaf, leaf_box;
   // ---- build scratch ----
   annf::DevBuf bmin, bmax, axis, keys, hist, sel_prefix, sel_rank, sel_nlt, sel_neq, blk_lt, blk_eq,
       off_lt, off_eq, eqpos;

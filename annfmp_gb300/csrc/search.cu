@@ -287,7 +287,8 @@ __global__ void __launch_bounds__(256) natural_leaf_kernel(TreeView<T> tv, const
 // natural leaf + its top-K for every query (warp per query); used when propagation is off
 template <typename T, int D, int KM>
 __global__ void __launch_bounds__(256) natural_knn_kernel(TreeView<T> tv, const T* __restrict__ Q, long long q0,
-                                                          long long nq, int K, int* __restrict__ out_pos) {
+                                                          long long nq, int K, int* __restrict__ out_pos,
+                                                          typename KeyOps<T>::K* __restrict__ out_key) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   unsigned char* p = smem_raw;
   NodeCache<T> nc;
@@ -324,7 +325,10 @@ __global__ void __launch_bounds__(256) natural_knn_kernel(TreeView<T> tv, const 
     typename KeyOps<T>::K k;
     int pos = 0;
     warp_topk<T, KM>(L, K, lane, k, pos);
-    if (lane < K) out_pos[qi * K + lane] = pos;
+    if (lane < K) {
+      out_pos[qi * K + lane] = pos;
+      if (out_key) out_key[qi * K + lane] = k;
+    }
   }
 }
 
@@ -430,6 +434,135 @@ __global__ void __launch_bounds__(32 * kDfsWarps) exact_dfs_kernel(TreeView<T> t
 }
 
 // ---------------------------------------------------------------------------------------------
+// exact kNN without a leaf budget: the same result as the backtracking search (top-K by key over
+// all points), computed as a tiled brute force over the leaves that cannot be skipped. A leaf is
+// skipped when the distance from the query to its bounding box, evaluated with the same rounded
+// operations as the point distances (so it bounds every point's distance from below), exceeds the
+// query's current K-th distance; the natural leaf's K-th distance seeds that threshold. Thread
+// per query (128-query tiles of adjacent pixels), leaf ranges split over blockIdx.y, partial
+// lists merged by exact_merge_kernel.
+// ---------------------------------------------------------------------------------------------
+constexpr int kBoxThreads = 128;
+
+template <typename T, int D, int KM>
+__global__ void __launch_bounds__(kBoxThreads) exact_box_kernel(
+    TreeView<T> tv, const T* __restrict__ Q, int nq, int K, const typename KeyOps<T>::K* __restrict__ seed_key,
+    int leaves_per_split, typename KeyOps<T>::K* __restrict__ part_key, int* __restrict__ part_pos) {
+  using Ops = KeyOps<T>;
+  using R = real_traits<T>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int d = tv.d;
+  const int dstride = d + 1;
+  unsigned char* p = smem_raw;
+  NodeCache<T> nc;
+  nc.carve(p, tv.depth);
+  T* sq = reinterpret_cast<T*>(p);                       // [kBoxThreads][d+1]
+  T* sbox = sq + kBoxThreads * dstride;                  // [2][d]
+  T* spts = reinterpret_cast<T*>(((uintptr_t)(sbox + 2 * d) + 15) & ~uintptr_t(15));  // [max_leaf][d]
+  const int max_leaf = (int)(((long long)tv.n + (1 << tv.depth) - 1) >> tv.depth);
+  if (smem_overrun(smem_raw, spts + (size_t)max_leaf * d, tv.status)) return;
+  nc.fill(tv);
+  const int qi = blockIdx.x * kBoxThreads + threadIdx.x;
+  const bool active = qi < nq;
+  for (int j = 0; j < d; ++j) sq[threadIdx.x * dstride + j] = active ? Q[(long long)qi * d + j] : T(0);
+  QReg<T, D> qr;
+  if constexpr (D == 0) {
+    qr.v = sq + threadIdx.x * dstride;
+    qr.d = d;
+  } else {
+#pragma unroll
+    for (int j = 0; j < D; ++j) qr.v[j] = sq[threadIdx.x * dstride + j];
+  }
+  // every candidate of the global top-K is at most the seed list's K-th distance away
+  const T seed = (active && seed_key) ? Ops::dist(seed_key[(long long)qi * K + K - 1]) : real_traits<T>::big();
+  LaneList<T, KM> L;
+  L.init_entries();
+  const int nleaves = 1 << tv.depth;
+  const int l0 = blockIdx.y * leaves_per_split, l1 = min(nleaves, l0 + leaves_per_split);
+  __syncthreads();
+  for (int lf = l0; lf < l1; ++lf) {
+    for (int e = threadIdx.x; e < 2 * d; e += blockDim.x) sbox[e] = __ldg(tv.leaf_box + (long long)lf * 2 * d + e);
+    __syncthreads();
+    T lb = 0;
+    for (int j = 0; j < (D > 0 ? D : d); ++j) {
+      const T qv = sq[threadIdx.x * dstride + j];
+      const T lo = sbox[j], hi = sbox[d + j];
+      const T g = qv < lo ? R::sub(lo, qv) : (qv > hi ? R::sub(qv, hi) : T(0));
+      lb = R::add(lb, R::mul(g, g));
+    }
+    const T kth = Ops::dist(L.key[KM - 1]);
+    const T thr = kth < seed ? kth : seed;
+    const bool need = active && !(lb > thr);
+    if (__syncthreads_or(need)) {
+      const int beg = __ldg(tv.leaf_begin + lf), end = __ldg(tv.leaf_begin + lf + 1);
+      const int cnt = end - beg;
+      for (int e = threadIdx.x; e < cnt * d; e += blockDim.x) spts[e] = tv.pts[(long long)beg * d + e];
+      __syncthreads();
+      if (need) {
+        uint32_t rank = 0;  // this leaf's position in the query's depth-first visiting order
+        for (int t = 0; t < tv.depth; ++t) {
+          const int node = (1 << t) - 1 + (lf >> (tv.depth - t));
+          const int dir = (lf >> (tv.depth - 1 - t)) & 1;
+          int ax;
+          T s;
+          nc.get(tv, node, ax, s);
+          const int side = sq[threadIdx.x * dstride + ax] >= s ? 1 : 0;
+          rank = (rank << 1) | (uint32_t)(dir ^ side);
+        }
+        const uint32_t hi = rank << tv.leaf_bits;
+        for (int pp = 0; pp < cnt; ++pp) {
+          const T* pt = spts + pp * d;
+          T acc = 0;
+          for (int j = 0; j < (D > 0 ? D : d); ++j) {
+            const T t = R::sub(pt[j], sq[threadIdx.x * dstride + j]);
+            acc = R::add(acc, R::mul(t, t));
+          }
+          if (!(acc > seed)) L.offer(Ops::make(acc, hi | (uint32_t)pp), beg + pp);
+        }
+      }
+    }
+    __syncthreads();
+  }
+  if (active) {
+    const long long base = ((long long)blockIdx.y * nq + qi) * K;
+    for (int j = 0; j < K && j < KM; ++j) {
+      part_key[base + j] = L.key[j];
+      part_pos[base + j] = L.pos[j];
+    }
+  }
+}
+
+// merge the per-split lists: warp per query. mode 0: tree positions to out_pos; mode 1: square
+// rooted distances + original indices (kneighbors)
+template <typename T, int KM>
+__global__ void exact_merge_kernel(TreeView<T> tv, int nq, int K, int nsplit,
+                                   const typename KeyOps<T>::K* __restrict__ part_key,
+                                   const int* __restrict__ part_pos, int mode, int* __restrict__ out_pos,
+                                   T* __restrict__ out_dist, int* __restrict__ out_idx) {
+  const int lane = threadIdx.x & 31;
+  const long long qi = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+  if (qi >= nq) return;
+  LaneList<T, KM> L;
+  L.init_entries();
+  for (int e = lane; e < nsplit * K; e += 32) {
+    const int sp = e / K, j = e - sp * K;
+    const long long src = ((long long)sp * nq + qi) * K + j;
+    L.offer(part_key[src], part_pos[src]);
+  }
+  typename KeyOps<T>::K k;
+  int pos = 0;
+  warp_topk<T, KM>(L, K, lane, k, pos);
+  if (lane < K) {
+    if (mode == 0) {
+      out_pos[qi * K + lane] = pos;
+    } else {
+      out_dist[qi * K + lane] = real_traits<T>::sqrt_(KeyOps<T>::dist(k));
+      out_idx[qi * K + lane] = __ldg(tv.perm + pos);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------------------------
 // row propagation
 // ---------------------------------------------------------------------------------------------
 // for every tree position: the leaf span of its point's "one row below" index (base.c:260-277)
@@ -446,6 +579,15 @@ __global__ void next_range_kernel(TreeView<T> tv, int n_cols, long long nA, int2
     const int lf = __ldg(tv.point_leaf + b);
     out[p] = make_int2(__ldg(tv.leaf_begin + lf), __ldg(tv.leaf_begin + lf + 1));
   }
+}
+
+// L2 prefetch of the points [b, e) (contiguous in tree order), one 128-byte line per lane per pass
+template <typename T>
+__device__ __forceinline__ void prefetch_span_l2(const T* pts, int b, int e, int d, int lane) {
+  if (e <= b) return;
+  const char* base = reinterpret_cast<const char*>(pts + (long long)b * d);
+  const int bytes = (e - b) * d * (int)sizeof(T);
+  for (int off = lane * 128; off < bytes; off += 32 * 128) asm volatile("prefetch.global.L2 [%0];" ::"l"(base + off));
 }
 
 // One warp per column walks the rows downwards (row y depends only on row y-1 of the same column).
@@ -486,6 +628,10 @@ __global__ void __launch_bounds__(128) chain_kernel(TreeView<T> tv, const T* __r
       if (y + 1 < n_rows) nat_next = __ldg(nat_range + qi);
     }
     const int2 rng = lane < K ? __ldg(next_range + my_pos) : make_int2(-1, -1);
+    // start every propagated leaf on its way to L2 before the first distance needs it
+    for (int j = 0; j < K; ++j) prefetch_span_l2(tv.pts, __shfl_sync(kFull, rng.x, j), __shfl_sync(kFull, rng.y, j), d, lane);
+    // and the next row's natural leaf, which does not depend on this step
+    if (y + 1 < n_rows) prefetch_span_l2(tv.pts, nat_next.x, nat_next.y, d, lane);
     WarpList<T> L;
     L.init(K, lane);
     // slots: bit 0 = natural leaf, bit j+1 = propagated neighbour j
@@ -610,6 +756,7 @@ static TreeView<T> view_of(const annf_handle* h) {
   tv.leaf_begin = h->leaf_begin.as<int>();
   tv.point_leaf = h->point_leaf.as<int>();
   tv.status = h->status.as<unsigned>();
+  tv.leaf_box = h->leaf_box.as<T>();
   return tv;
 }
 
@@ -651,8 +798,8 @@ int num_sms() {
   } while (0)
 
 template <typename T, int D>
-static int exact_knn_typed(annf_handle* h, const T* Q, int nq, int K, long long max_leaves, int mode, int* out_pos,
-                           T* out_dist, int* out_idx, cudaStream_t st) {
+static int exact_dfs_launch(annf_handle* h, const T* Q, int nq, int K, long long max_leaves, int mode, int* out_pos,
+                            T* out_dist, int* out_idx, cudaStream_t st) {
   TreeView<T> tv = view_of<T>(h);
   // node cache + per warp: query copy, stack of bounds, stack of nodes, stack of rank prefixes
   const size_t smem = NodeCache<T>::bytes(h->depth) +
@@ -663,6 +810,50 @@ static int exact_knn_typed(annf_handle* h, const T* Q, int nq, int K, long long 
                                                                  out_idx);
   ANNF_CHECK_LAUNCH();
   return ANNF_OK;
+}
+
+template <typename T, int D, int KM>
+static int exact_box_launch(annf_handle* h, const T* Q, int nq, int K, int mode, int* out_pos, T* out_dist,
+                            int* out_idx, cudaStream_t st) {
+  using Kt = typename KeyOps<T>::K;
+  TreeView<T> tv = view_of<T>(h);
+  const int nleaves = 1 << h->depth;
+  // seeds: each query's natural-leaf top-K
+  ANNF_ENSURE(h->nat_keys, (size_t)nq * K * sizeof(Kt));
+  ANNF_ENSURE(h->nat_pos, (size_t)nq * K * sizeof(int));
+  const size_t nsm = NodeCache<T>::bytes(h->depth) + 8 * kMaxDynD * sizeof(T);
+  ANNF_CUDA_TRY(cudaFuncSetAttribute(natural_knn_kernel<T, D, KM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)nsm));
+  natural_knn_kernel<T, D, KM><<<(int)std::min<long long>(ceil_div((long long)nq * 32, 256), 64LL * num_sms()), 256, nsm,
+                                 st>>>(tv, Q, 0, nq, K, h->nat_pos.as<int>(), h->nat_keys.as<Kt>());
+  ANNF_CHECK_LAUNCH();
+  const int tiles = ceil_div(nq, kBoxThreads);
+  const int want = std::max(1, (4 * num_sms()) / tiles);
+  const int lps = std::max(1, ceil_div(nleaves, want));
+  const int nsplit = ceil_div(nleaves, lps);
+  ANNF_ENSURE(h->part_keys, (size_t)nsplit * nq * K * sizeof(Kt));
+  ANNF_ENSURE(h->part_pos, (size_t)nsplit * nq * K * sizeof(int));
+  const size_t smem = NodeCache<T>::bytes(h->depth) + (size_t)kBoxThreads * (h->d + 1) * sizeof(T) +
+                      2 * h->d * sizeof(T) + 32 + (size_t)h->max_leaf * h->d * sizeof(T) + 64;
+  ANNF_CUDA_TRY(cudaFuncSetAttribute(exact_box_kernel<T, D, KM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  exact_box_kernel<T, D, KM><<<dim3(tiles, nsplit), kBoxThreads, smem, st>>>(tv, Q, nq, K, h->nat_keys.as<Kt>(), lps,
+                                                                             h->part_keys.as<Kt>(), h->part_pos.as<int>());
+  ANNF_CHECK_LAUNCH();
+  exact_merge_kernel<T, KM><<<ceil_div((long long)nq * 32, 256), 256, 0, st>>>(
+      tv, nq, K, nsplit, h->part_keys.as<Kt>(), h->part_pos.as<int>(), mode, out_pos, out_dist, out_idx);
+  ANNF_CHECK_LAUNCH();
+  return ANNF_OK;
+}
+
+template <typename T, int D>
+static int exact_knn_typed(annf_handle* h, const T* Q, int nq, int K, long long max_leaves, int mode, int* out_pos,
+                           T* out_dist, int* out_idx, cudaStream_t st) {
+  const size_t box_smem = NodeCache<T>::bytes(h->depth) + (size_t)kBoxThreads * (h->d + 1) * sizeof(T) +
+                          2 * h->d * sizeof(T) + 32 + (size_t)h->max_leaf * h->d * sizeof(T) + 64;
+  if (max_leaves < (1LL << h->depth) || box_smem > 200 * 1024)  // budgeted search: the reference's order
+    return exact_dfs_launch<T, D>(h, Q, nq, K, max_leaves, mode, out_pos, out_dist, out_idx, st);
+  int rc = ANNF_OK;
+  ANNF_DISPATCH_KM(pick_km(K), rc = (exact_box_launch<T, D, KM>(h, Q, nq, K, mode, out_pos, out_dist, out_idx, st)));
+  return rc;
 }
 
 template <typename T>
@@ -705,7 +896,7 @@ static int rows_typed(annf_handle* h, const T* ared, int n_rows, int n_cols, int
       cudaError_t e = cudaFuncSetAttribute(natural_knn_kernel<T, D, KM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            (int)smem);
       if (e != cudaSuccess) rc = ANNF_ERR_CUDA;
-      natural_knn_kernel<T, D, KM><<<blocks, 256, smem, st>>>(tv, ared, n_cols, nq, K, lists);
+      natural_knn_kernel<T, D, KM><<<blocks, 256, smem, st>>>(tv, ared, n_cols, nq, K, lists, nullptr);
     });
     if (rc != ANNF_OK) {
       set_error("natural_knn_kernel: cudaFuncSetAttribute failed");

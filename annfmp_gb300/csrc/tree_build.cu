@@ -358,6 +358,33 @@ __global__ void leaves_kernel(int n, int depth, int B, const int* __restrict__ p
   for (int i = c0 + threadIdx.x; i < c1; i += blockDim.x) point_leaf[perm[i]] = s;
 }
 
+// per-leaf bounding box (warp per leaf): box[l][0][j] = min, box[l][1][j] = max over the leaf
+template <typename T>
+__global__ void leaf_box_kernel(int L, int d, const T* __restrict__ pts, const int* __restrict__ leaf_begin,
+                                T* __restrict__ box) {
+  const int l = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (l >= L) return;
+  const int beg = leaf_begin[l], end = leaf_begin[l + 1];
+  for (int j = 0; j < d; ++j) {
+    T mn = real_traits<T>::big(), mx = -real_traits<T>::big();
+    for (int p = beg + lane; p < end; p += 32) {
+      const T v = pts[(long long)p * d + j];
+      mn = v < mn ? v : mn;
+      mx = v > mx ? v : mx;
+    }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+      const T a = __shfl_xor_sync(0xffffffffu, mn, o), b = __shfl_xor_sync(0xffffffffu, mx, o);
+      mn = a < mn ? a : mn;
+      mx = b > mx ? b : mx;
+    }
+    if (lane == 0) {
+      box[((long long)l * 2) * d + j] = mn;
+      box[((long long)l * 2 + 1) * d + j] = mx;
+    }
+  }
+}
+
 // ---------------------------------------------------------------------------------------------
 // shared-memory subtree finisher: one CTA per segment of level t0, levels t0..depth-1
 // ---------------------------------------------------------------------------------------------
@@ -668,6 +695,12 @@ static int build_impl(annf_handle* h, const T* points, int n, int d, int depth, 
   // the final arrays live in h->pts / h->perm
   if (cur_pts != h->pts.as<T>()) std::swap(h->pts, h->pts_tmp);
   if (cur_perm != h->perm.as<int>()) std::swap(h->perm, h->perm_tmp);
+  // per-leaf bounding boxes: lower bounds for the exact search
+  ANNF_ENSURE(h->leaf_box, (size_t)2 * L * d * sizeof(T));
+  leaf_box_kernel<T><<<ceil_div((long long)L * 32, 256), 256, 0, st>>>(L, d, h->pts.as<T>(), h->leaf_begin.as<int>(),
+                                                                     h->leaf_box.as<T>());
+  ANNF_CHECK_LAUNCH();
+  prof_mark(h, "build_leafbox", st);
   const int maxleaf = (int)(((long long)n + L - 1) / L);
   int bits = 1;
   while ((1LL << bits) <= maxleaf) ++bits;
