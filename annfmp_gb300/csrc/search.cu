@@ -213,6 +213,46 @@ struct QReg<T, 0> {
   }
 };
 
+// Four distances at once. Each keeps the reference's dimension order, but the four dependent
+// add chains are interleaved, so a lane has four independent instructions in flight instead of
+// one (a distance is a chain of d dependent rounded adds). kSmem: points in shared memory.
+template <bool kSmem, typename T, int D>
+__device__ __forceinline__ void dist4(const QReg<T, D>& q, const T* p0, const T* p1, const T* p2, const T* p3, int d,
+                                      T (&acc)[4]) {
+  using R = real_traits<T>;
+  const T* p[4] = {p0, p1, p2, p3};
+#pragma unroll
+  for (int u = 0; u < 4; ++u) acc[u] = T(0);
+  if constexpr (D > 0 && sizeof(T) == 4 && D % 4 == 0) {
+#pragma unroll
+    for (int j = 0; j < D / 4; ++j) {
+      float4 w[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+        w[u] = kSmem ? reinterpret_cast<const float4*>(p[u])[j] : __ldg(reinterpret_cast<const float4*>(p[u]) + j);
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        float t;
+        t = R::sub(w[u].x, q.v[4 * j + 0]); acc[u] = R::add(acc[u], R::mul(t, t));
+        t = R::sub(w[u].y, q.v[4 * j + 1]); acc[u] = R::add(acc[u], R::mul(t, t));
+        t = R::sub(w[u].z, q.v[4 * j + 2]); acc[u] = R::add(acc[u], R::mul(t, t));
+        t = R::sub(w[u].w, q.v[4 * j + 3]); acc[u] = R::add(acc[u], R::mul(t, t));
+      }
+    }
+  } else {
+    const int dd = D > 0 ? D : d;
+#pragma unroll(D > 0 ? D : 1)
+    for (int j = 0; j < dd; ++j) {
+      const T qj = q.v[j];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const T t = R::sub(kSmem ? p[u][j] : __ldg(p[u] + j), qj);
+        acc[u] = R::add(acc[u], R::mul(t, t));
+      }
+    }
+  }
+}
+
 // ---------------------------------------------------------------------------------------------
 // nodes: the top levels are cached in shared memory by the kernels that descend
 // ---------------------------------------------------------------------------------------------
@@ -318,9 +358,16 @@ __global__ void __launch_bounds__(256) natural_knn_kernel(TreeView<T> tv, const 
     LaneList<T, KM> L;
     L.init_entries();
     const uint32_t slot = 1u << tv.leaf_bits;
-    for (int pp = beg + lane; pp < end; pp += 32) {
-      const T dd = qr.dist(tv.pts + (long long)pp * d, d);
-      L.offer(KeyOps<T>::make(dd, slot | (uint32_t)(pp - beg)), pp);
+    for (int base = beg; base < end; base += 128) {  // four candidates per lane per pass
+      int pp[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) pp[u] = base + lane + 32 * u;
+      T dd[4];
+      dist4<false>(qr, tv.pts + (long long)min(pp[0], end - 1) * d, tv.pts + (long long)min(pp[1], end - 1) * d,
+                   tv.pts + (long long)min(pp[2], end - 1) * d, tv.pts + (long long)min(pp[3], end - 1) * d, d, dd);
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+        if (pp[u] < end) L.offer(KeyOps<T>::make(dd[u], slot | (uint32_t)(pp[u] - beg)), pp[u]);
     }
     typename KeyOps<T>::K k;
     int pos = 0;
@@ -510,14 +557,14 @@ __global__ void __launch_bounds__(kBoxThreads) exact_box_kernel(
           rank = (rank << 1) | (uint32_t)(dir ^ side);
         }
         const uint32_t hi = rank << tv.leaf_bits;
-        for (int pp = 0; pp < cnt; ++pp) {
-          const T* pt = spts + pp * d;
-          T acc = 0;
-          for (int j = 0; j < (D > 0 ? D : d); ++j) {
-            const T t = R::sub(pt[j], sq[threadIdx.x * dstride + j]);
-            acc = R::add(acc, R::mul(t, t));
-          }
-          if (!(acc > seed)) L.offer(Ops::make(acc, hi | (uint32_t)pp), beg + pp);
+        for (int pp = 0; pp < cnt; pp += 4) {
+          const int last = cnt - 1;
+          T acc[4];
+          dist4<true>(qr, spts + min(pp, last) * d, spts + min(pp + 1, last) * d, spts + min(pp + 2, last) * d,
+                      spts + min(pp + 3, last) * d, d, acc);
+#pragma unroll
+          for (int u = 0; u < 4; ++u)
+            if (pp + u < cnt && !(acc[u] > seed)) L.offer(Ops::make(acc[u], hi | (uint32_t)(pp + u)), beg + pp + u);
         }
       }
     }
@@ -594,7 +641,7 @@ __device__ __forceinline__ void prefetch_span_l2(const T* pts, int b, int e, int
 // Per step: the natural leaf (span precomputed for every pixel) and the K propagated leaves; a
 // leaf that several slots share is scanned once and its points are offered once per slot.
 template <typename T, int D>
-__global__ void __launch_bounds__(128) chain_kernel(TreeView<T> tv, const T* __restrict__ Q, int n_rows, int n_cols,
+__global__ void __launch_bounds__(128, 1) chain_kernel(TreeView<T> tv, const T* __restrict__ Q, int n_rows, int n_cols,
                                                     int K, const int2* __restrict__ nat_range,
                                                     const int2* __restrict__ next_range, int* __restrict__ lists) {
   using Ops = KeyOps<T>;
@@ -642,16 +689,24 @@ __global__ void __launch_bounds__(128) chain_kernel(TreeView<T> tv, const T* __r
       const int e = s0 == 0 ? nat.y : __shfl_sync(kFull, rng.y, s0 - 1);
       const unsigned same = ((nat.x == b ? 1u : 0u) | (__ballot_sync(kFull, lane < K && rng.x == b) << 1)) & todo;
       todo &= ~same;
-      for (int base = b; base < e; base += 32) {
-        const int pp = base + lane;
-        const bool valid = pp < e;
-        const T dd = valid ? qr.dist(tv.pts + (long long)pp * d, d) : T(0);
-        const uint32_t off = (uint32_t)(pp - b);
+      for (int base = b; base < e; base += 128) {  // four candidates per lane per pass
+        int pp[4];
+        bool valid[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          pp[u] = base + lane + 32 * u;
+          valid[u] = pp[u] < e;
+        }
+        T dd[4];
+        dist4<false>(qr, tv.pts + (long long)(valid[0] ? pp[0] : b) * d, tv.pts + (long long)(valid[1] ? pp[1] : b) * d,
+                     tv.pts + (long long)(valid[2] ? pp[2] : b) * d, tv.pts + (long long)(valid[3] ? pp[3] : b) * d, d, dd);
         unsigned sl = same;
         while (sl) {
           const int s = __ffs(sl) - 1;
           sl &= sl - 1;
-          L.offer(valid, Ops::make(dd, ((uint32_t)(s + 1) << lb) | off), pp);
+          const uint32_t hi = (uint32_t)(s + 1) << lb;
+#pragma unroll
+          for (int u = 0; u < 4; ++u) L.offer(valid[u], Ops::make(dd[u], hi | (uint32_t)(pp[u] - b)), pp[u]);
         }
       }
     }
