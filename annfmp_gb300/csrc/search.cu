@@ -253,6 +253,39 @@ __device__ __forceinline__ void dist4(const QReg<T, D>& q, const T* p0, const T*
   }
 }
 
+// N distances at once (N interleaved chains), points in global memory
+template <int N, typename T, int D>
+__device__ __forceinline__ void distN(const QReg<T, D>& q, const T* const (&p)[N], T (&acc)[N]) {
+  using R = real_traits<T>;
+#pragma unroll
+  for (int u = 0; u < N; ++u) acc[u] = T(0);
+  if constexpr (sizeof(T) == 4 && D % 4 == 0) {
+#pragma unroll
+    for (int j = 0; j < D / 4; ++j) {
+      float4 w[N];
+#pragma unroll
+      for (int u = 0; u < N; ++u) w[u] = __ldg(reinterpret_cast<const float4*>(p[u]) + j);
+#pragma unroll
+      for (int u = 0; u < N; ++u) {
+        float t;
+        t = R::sub(w[u].x, q.v[4 * j + 0]); acc[u] = R::add(acc[u], R::mul(t, t));
+        t = R::sub(w[u].y, q.v[4 * j + 1]); acc[u] = R::add(acc[u], R::mul(t, t));
+        t = R::sub(w[u].z, q.v[4 * j + 2]); acc[u] = R::add(acc[u], R::mul(t, t));
+        t = R::sub(w[u].w, q.v[4 * j + 3]); acc[u] = R::add(acc[u], R::mul(t, t));
+      }
+    }
+  } else {
+#pragma unroll
+    for (int j = 0; j < D; ++j) {
+#pragma unroll
+      for (int u = 0; u < N; ++u) {
+        const T t = R::sub(__ldg(p[u] + j), q.v[j]);
+        acc[u] = R::add(acc[u], R::mul(t, t));
+      }
+    }
+  }
+}
+
 // ---------------------------------------------------------------------------------------------
 // nodes: the top levels are cached in shared memory by the kernels that descend
 // ---------------------------------------------------------------------------------------------
@@ -715,6 +748,132 @@ __global__ void __launch_bounds__(128, 1) chain_kernel(TreeView<T> tv, const T* 
   }
 }
 
+// The same step with compile-time bounds (FP32, fixed dimension, at most LM distinct leaves per
+// step, at most 32*CPL points per leaf). All distinct leaves' distances are computed up front --
+// their loads overlap -- and the K-list is then selected by K rounds of a warp-wide minimum over
+// per-candidate keys. A candidate whose leaf serves several slots carries the mask of those slots
+// and re-enters with its next slot once extracted, so points met twice are listed twice exactly
+// as the reference's insertion does.
+template <int D, int CPL, int LM>
+__global__ void __launch_bounds__(128, 1) chain_sel_kernel(TreeView<float> tv, const float* __restrict__ Q, int n_rows,
+                                                            int n_cols, int K, const int2* __restrict__ nat_range,
+                                                            const int2* __restrict__ next_range, int* __restrict__ lists) {
+  using Ops = KeyOps<float>;
+  using Kt = Ops::K;
+  const int lane = threadIdx.x & 31;
+  const int x = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (x >= n_cols) return;
+  const int lb = tv.leaf_bits;
+  int my_pos = lane < K ? lists[(long long)x * K + lane] : 0;
+  int2 nat_next = __ldg(nat_range + x);  // nat_range is indexed from row 1
+  QReg<float, D> q_next;
+  q_next.load(Q + ((long long)n_cols + x) * D, D);
+  long long qi = (long long)n_cols + x;
+  for (int y = 1; y < n_rows; ++y, qi += n_cols) {
+    const int2 nat = nat_next;
+    const QReg<float, D> qr = q_next;
+    if (y + 1 < n_rows) {
+      q_next.load(Q + (qi + n_cols) * D, D);
+      nat_next = __ldg(nat_range + qi);
+    }
+    const int2 rng = lane < K ? __ldg(next_range + my_pos) : make_int2(-1, -1);
+    if (y + 1 < n_rows) prefetch_span_l2(tv.pts, nat_next.x, nat_next.y, D, lane);
+    // distinct leaves: slot bit 0 = natural leaf, bit j+1 = propagated neighbour j
+    int lbeg[LM], lend[LM];
+    unsigned lmask[LM];
+    unsigned todo = (2u << K) - 1u;
+#pragma unroll
+    for (int i = 0; i < LM; ++i) {
+      lbeg[i] = 0;
+      lend[i] = 0;
+      lmask[i] = 0;
+      if (todo) {
+        const int s0 = __ffs(todo) - 1;
+        const int b = s0 == 0 ? nat.x : __shfl_sync(kFull, rng.x, s0 - 1);
+        const int e = s0 == 0 ? nat.y : __shfl_sync(kFull, rng.y, s0 - 1);
+        const unsigned same = ((nat.x == b ? 1u : 0u) | (__ballot_sync(kFull, lane < K && rng.x == b) << 1)) & todo;
+        todo &= ~same;
+        lbeg[i] = b;
+        lend[i] = e;
+        lmask[i] = same;
+      }
+    }
+    // per-lane sorted list of its KM best (key, position, remaining slots)
+    constexpr int KM = LM <= 2 ? 1 : (LM <= 5 ? 4 : 8);
+    Kt lk[KM];
+    int lp[KM];
+    unsigned lr[KM];
+#pragma unroll
+    for (int j = 0; j < KM; ++j) {
+      lk[j] = Ops::inf();
+      lp[j] = 0;
+      lr[j] = 0;
+    }
+    auto lane_offer = [&](Kt k, int p, unsigned r) {
+      if (!(k < lk[KM - 1])) return;
+#pragma unroll
+      for (int j = KM - 1; j >= 0; --j) {
+        if (j > 0 && k < lk[j - 1]) {
+          lk[j] = lk[j - 1];
+          lp[j] = lp[j - 1];
+          lr[j] = lr[j - 1];
+        } else if (k < lk[j]) {
+          lk[j] = k;
+          lp[j] = p;
+          lr[j] = r;
+        }
+      }
+    };
+#pragma unroll
+    for (int i = 0; i < LM; ++i) {
+      if (lend[i] > lbeg[i]) {
+        const float* pp[CPL];
+#pragma unroll
+        for (int u = 0; u < CPL; ++u) {
+          const int p = lbeg[i] + lane + 32 * u;
+          pp[u] = tv.pts + (long long)(p < lend[i] ? p : lbeg[i]) * D;
+        }
+        float dd[CPL];
+        distN<CPL>(qr, pp, dd);
+        const uint32_t slot = (uint32_t)__ffs(lmask[i]) << lb;
+#pragma unroll
+        for (int u = 0; u < CPL; ++u)
+          if (lbeg[i] + lane + 32 * u < lend[i])
+            lane_offer(Ops::make(dd[u], slot | (uint32_t)(lane + 32 * u)), lbeg[i] + lane + 32 * u, lmask[i]);
+      }
+    }
+    // K rounds of warp-wide minimum over the lane heads; the initial entries (max real,
+    // position 0) fill any shortfall
+    const Kt low_mask = (Kt)((1u << lb) - 1u);
+    int outpos = 0;
+    for (int r = 0; r < K; ++r) {
+      Kt wmin = lk[0];
+#pragma unroll
+      for (int o = 16; o; o >>= 1) {
+        const Kt t = Ops::shfl_xor(wmin, o);
+        wmin = t < wmin ? t : wmin;
+      }
+      if (!(wmin < Ops::init())) break;  // remaining entries stay (max real, position 0)
+      const int winner = __ffs(__ballot_sync(kFull, lk[0] == wmin)) - 1;
+      const int pos = __shfl_sync(kFull, lp[0], winner);
+      if (lane == winner) {
+        const unsigned nr = lr[0] & (lr[0] - 1u);  // next slot of the same point, if any
+#pragma unroll
+        for (int j = 0; j < KM - 1; ++j) {
+          lk[j] = lk[j + 1];
+          lp[j] = lp[j + 1];
+          lr[j] = lr[j + 1];
+        }
+        lk[KM - 1] = Ops::inf();
+        if (nr) lane_offer((wmin & ~(Kt)0xffffffffu) | ((Kt)((uint32_t)__ffs(nr) << lb)) | (wmin & low_mask), pos, nr);
+      }
+      if (lane == r) outpos = pos;
+    }
+    if (lane < K) lists[qi * K + lane] = outpos;
+    my_pos = outpos;
+  }
+}
+
 // ---------------------------------------------------------------------------------------------
 // tree positions -> original indices, and the raw-patch re-rank (base.c:309-353, 362-374)
 // ---------------------------------------------------------------------------------------------
@@ -938,8 +1097,29 @@ static int rows_typed(annf_handle* h, const T* ared, int n_rows, int n_cols, int
         tv, n_cols, nA, h->next_range.as<int2>(), h->status.as<unsigned>());
     ANNF_CHECK_LAUNCH();
     prof_mark(h, "next_range", st);
-    chain_kernel<T, D><<<ceil_div((long long)n_cols * 32, 128), 128, 0, st>>>(
-        tv, ared, n_rows, n_cols, K, h->nat_pos.as<int2>(), h->next_range.as<int2>(), lists);
+    const int cblocks = ceil_div((long long)n_cols * 32, 128);
+    bool launched = false;
+    if constexpr (sizeof(T) == 4 && D > 0) {
+      if (K <= 8 && h->max_leaf <= 128) {
+        const int2* nr = h->nat_pos.as<int2>();
+        const int2* xr = h->next_range.as<int2>();
+        const bool small_leaf = h->max_leaf <= 64;
+#define ANNF_CHAIN_SEL(CPLV, LMV) \
+  chain_sel_kernel<D, CPLV, LMV><<<cblocks, 128, 0, st>>>(tv, ared, n_rows, n_cols, K, nr, xr, lists)
+        if (K == 1) {
+          if (small_leaf) ANNF_CHAIN_SEL(2, 2); else ANNF_CHAIN_SEL(4, 2);
+        } else if (K <= 4) {
+          if (small_leaf) ANNF_CHAIN_SEL(2, 5); else ANNF_CHAIN_SEL(4, 5);
+        } else {
+          if (small_leaf) ANNF_CHAIN_SEL(2, 9); else ANNF_CHAIN_SEL(4, 9);
+        }
+#undef ANNF_CHAIN_SEL
+        launched = true;
+      }
+    }
+    if (!launched)
+      chain_kernel<T, D><<<cblocks, 128, 0, st>>>(tv, ared, n_rows, n_cols, K, h->nat_pos.as<int2>(),
+                                                  h->next_range.as<int2>(), lists);
     ANNF_CHECK_LAUNCH();
     prof_mark(h, "chain", st);
   } else {
