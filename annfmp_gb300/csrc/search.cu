@@ -612,6 +612,97 @@ __global__ void __launch_bounds__(kBoxThreads) exact_box_kernel(
   }
 }
 
+// Exact kNN for a moderate number of queries: warp per query; the lanes test 32 leaf boxes at a
+// time and the warp scans only the leaves whose box lies within the query's current K-th distance
+// (seeded by the natural leaf's K-th distance). The K-list lives distributed over the lanes, so
+// the threshold is exact after every leaf.
+template <typename T, int D>
+__global__ void __launch_bounds__(256) exact_scan_kernel(TreeView<T> tv, const T* __restrict__ Q, int nq, int K,
+                                                         const typename KeyOps<T>::K* __restrict__ seed_key, int mode,
+                                                         int* __restrict__ out_pos, T* __restrict__ out_dist,
+                                                         int* __restrict__ out_idx) {
+  using Ops = KeyOps<T>;
+  using R = real_traits<T>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  unsigned char* p = smem_raw;
+  NodeCache<T> nc;
+  nc.carve(p, tv.depth);
+  const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  T* sq = reinterpret_cast<T*>(p) + wib * kMaxDynD;
+  if (smem_overrun(smem_raw, reinterpret_cast<T*>(p) + (blockDim.x >> 5) * kMaxDynD, tv.status)) return;
+  nc.fill(tv);
+  __syncthreads();
+  const int d = tv.d, depth = tv.depth;
+  const int nleaves = 1 << depth;
+  const int nw = gridDim.x * (blockDim.x >> 5);
+  for (int qi = blockIdx.x * (blockDim.x >> 5) + wib; qi < nq; qi += nw) {
+    __syncwarp();
+    for (int j = lane; j < d; j += 32) sq[j] = Q[(long long)qi * d + j];
+    __syncwarp();
+    QReg<T, D> qr;
+    if constexpr (D == 0) {
+      qr.v = sq;
+      qr.d = d;
+    } else {
+      qr.load(sq, d);
+    }
+    const T seed = seed_key ? Ops::dist(seed_key[(long long)qi * K + K - 1]) : real_traits<T>::big();
+    WarpList<T> L;
+    L.init(K, lane);
+    for (int base = 0; base < nleaves; base += 32) {
+      const int lf = base + lane;
+      T lb = real_traits<T>::big();
+      if (lf < nleaves) {
+        const T* box = tv.leaf_box + (long long)lf * 2 * d;
+        lb = T(0);
+        for (int j = 0; j < d; ++j) {
+          const T qv = sq[j], lo = __ldg(box + j), hi = __ldg(box + d + j);
+          const T g = qv < lo ? R::sub(lo, qv) : (qv > hi ? R::sub(qv, hi) : T(0));
+          lb = R::add(lb, R::mul(g, g));
+        }
+      }
+      T kth = Ops::dist(L.thr);
+      unsigned m = __ballot_sync(kFull, lf < nleaves && !(lb > (kth < seed ? kth : seed)));
+      while (m) {
+        const int src = __ffs(m) - 1;
+        m &= m - 1;
+        kth = Ops::dist(L.thr);
+        if (__shfl_sync(kFull, lb, src) > (kth < seed ? kth : seed)) continue;  // pruned by now
+        const int leaf = base + src;
+        uint32_t rank = 0;  // the leaf's position in this query's depth-first visiting order
+        for (int t = 0; t < depth; ++t) {
+          const int node = (1 << t) - 1 + (leaf >> (depth - t));
+          int ax;
+          T s;
+          nc.get(tv, node, ax, s);
+          rank = (rank << 1) | (uint32_t)(((leaf >> (depth - 1 - t)) & 1) ^ (sq[ax] >= s ? 1 : 0));
+        }
+        const uint32_t hi = rank << tv.leaf_bits;
+        const int beg = __ldg(tv.leaf_begin + leaf), end = __ldg(tv.leaf_begin + leaf + 1);
+        for (int pb = beg; pb < end; pb += 128) {
+          int pp[4];
+#pragma unroll
+          for (int u = 0; u < 4; ++u) pp[u] = pb + lane + 32 * u;
+          T dd[4];
+          dist4<false>(qr, tv.pts + (long long)min(pp[0], end - 1) * d, tv.pts + (long long)min(pp[1], end - 1) * d,
+                       tv.pts + (long long)min(pp[2], end - 1) * d, tv.pts + (long long)min(pp[3], end - 1) * d, d, dd);
+#pragma unroll
+          for (int u = 0; u < 4; ++u)
+            L.offer(pp[u] < end && !(dd[u] > seed), Ops::make(dd[u], hi | (uint32_t)(pp[u] - beg)), pp[u]);
+        }
+      }
+    }
+    if (lane < K) {
+      if (mode == 0) {
+        out_pos[(long long)qi * K + lane] = L.pos;
+      } else {
+        out_dist[(long long)qi * K + lane] = R::sqrt_(Ops::dist(L.key));
+        out_idx[(long long)qi * K + lane] = __ldg(tv.perm + L.pos);
+      }
+    }
+  }
+}
+
 // merge the per-split lists: warp per query. mode 0: tree positions to out_pos; mode 1: square
 // rooted distances + original indices (kneighbors)
 template <typename T, int KM>
@@ -1040,6 +1131,14 @@ static int exact_box_launch(annf_handle* h, const T* Q, int nq, int K, int mode,
   natural_knn_kernel<T, D, KM><<<(int)std::min<long long>(ceil_div((long long)nq * 32, 256), 64LL * num_sms()), 256, nsm,
                                  st>>>(tv, Q, 0, nq, K, h->nat_pos.as<int>(), h->nat_keys.as<Kt>());
   ANNF_CHECK_LAUNCH();
+  if ((long long)nq * nleaves <= (1LL << 28)) {  // few queries: warp per query over the leaf boxes
+    const size_t ssm = NodeCache<T>::bytes(h->depth) + 8 * kMaxDynD * sizeof(T) + 64;
+    ANNF_CUDA_TRY(cudaFuncSetAttribute(exact_scan_kernel<T, D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ssm));
+    exact_scan_kernel<T, D><<<std::max(1, std::min(ceil_div(nq, 8), 32 * num_sms())), 256, ssm, st>>>(
+        tv, Q, nq, K, h->nat_keys.as<Kt>(), mode, out_pos, out_dist, out_idx);
+    ANNF_CHECK_LAUNCH();
+    return ANNF_OK;
+  }
   const int tiles = ceil_div(nq, kBoxThreads);
   const int want = std::max(1, (4 * num_sms()) / tiles);
   const int lps = std::max(1, ceil_div(nleaves, want));
