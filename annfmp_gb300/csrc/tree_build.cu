@@ -123,20 +123,14 @@ __global__ void axis_kernel(int n, int d, int t, int S, int splitting, const typ
   nlt[s] = 0;
 }
 
+// one radix-select pass: histogram of the current digit over the keys that match the prefix found
+// so far. The first pass reads the split axis from the points and writes the keys. Lanes of a warp
+// that hit the same bin (common: a segment's keys share their high digits) add once, together.
 template <typename T>
-__global__ void extract_keys_kernel(int n, int d, int t, int B, const T* __restrict__ pts,
-                                    const int* __restrict__ axis, typename key_of<T>::type* keys) {
-  const int s = blockIdx.x / B, bb = blockIdx.x % B;
-  int lo, hi;
-  seg_range(n, t, s, lo, hi);
-  const int c0 = lo + bb * kChunk, c1 = min(hi, c0 + kChunk);
-  const int ax = axis[s];
-  for (int i = c0 + threadIdx.x; i < c1; i += blockDim.x) keys[i] = ord_key(pts[(long long)i * d + ax]);
-}
-
-template <typename K>
-__global__ void hist_kernel(int n, int t, int B, int shift, const K* __restrict__ keys,
-                            const K* __restrict__ prefix, unsigned* ghist) {
+__global__ void hist_kernel(int n, int d, int t, int B, int shift, bool extract, const T* __restrict__ pts,
+                            const int* __restrict__ axis, typename key_of<T>::type* __restrict__ keys,
+                            const typename key_of<T>::type* __restrict__ prefix, unsigned* ghist) {
+  using K = typename key_of<T>::type;
   __shared__ unsigned h[256];
   const int s = blockIdx.x / B, bb = blockIdx.x % B;
   int lo, hi;
@@ -146,9 +140,23 @@ __global__ void hist_kernel(int n, int t, int B, int shift, const K* __restrict_
   __syncthreads();
   const K pre = prefix[s];
   const K hmask = (shift + 8 >= (int)(8 * sizeof(K))) ? (K)0 : (~(K)0 << (shift + 8));
-  for (int i = c0 + threadIdx.x; i < c1; i += blockDim.x) {
-    K k = keys[i];
-    if (((k ^ pre) & hmask) == 0) atomicAdd(&h[(unsigned)(k >> shift) & 255u], 1u);
+  const int ax = axis[s];
+  const int lane = threadIdx.x & 31;
+  for (int base = c0 + (int)(threadIdx.x & ~31u); base < c1; base += blockDim.x) {
+    const int i = base + lane;
+    unsigned bin = 256u;
+    if (i < c1) {
+      K k;
+      if (extract) {
+        k = ord_key(pts[(long long)i * d + ax]);
+        keys[i] = k;
+      } else {
+        k = keys[i];
+      }
+      if (((k ^ pre) & hmask) == 0) bin = (unsigned)(k >> shift) & 255u;
+    }
+    const unsigned peers = __match_any_sync(0xffffffffu, bin);
+    if (bin != 256u && lane == __ffs(peers) - 1) atomicAdd(&h[bin], (unsigned)__popc(peers));
   }
   __syncthreads();
   unsigned v = h[threadIdx.x];
@@ -230,23 +238,11 @@ __global__ void count_kernel(int n, int t, int B, const K* __restrict__ keys, co
   }
 }
 
-__global__ void seg_scan_kernel(int S, int B, const int* blk_lt, const int* blk_eq, int* off_lt, int* off_eq) {
-  const int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= S) return;
-  int a = 0, b = 0;
-  for (int u = 0; u < B; ++u) {
-    off_lt[(long long)s * B + u] = a;
-    off_eq[(long long)s * B + u] = b;
-    a += blk_lt[(long long)s * B + u];
-    b += blk_eq[(long long)s * B + u];
-  }
-}
-
 template <typename T>
 __global__ void __launch_bounds__(kThreads) scatter_kernel(
     int n, int d, int t, int B, const typename key_of<T>::type* __restrict__ keys,
     const typename key_of<T>::type* __restrict__ pivot, const int* __restrict__ nlt,
-    const int* __restrict__ neq, const int* __restrict__ off_lt, const int* __restrict__ off_eq,
+    const int* __restrict__ neq, const int* __restrict__ blk_lt, const int* __restrict__ blk_eq,
     const T* __restrict__ pts_in, const int* __restrict__ perm_in, T* __restrict__ pts_out,
     int* __restrict__ perm_out, int* __restrict__ eqpos) {
   using K = typename key_of<T>::type;
@@ -275,10 +271,18 @@ __global__ void __launch_bounds__(kThreads) scatter_kernel(
       }
     }
   }
+  // this chunk's offsets among its segment's chunks: a block-wide sum over the chunks before it
+  int pl = 0, pe = 0;
+  for (int u = threadIdx.x; u < bb; u += blockDim.x) {
+    pl += blk_lt[(long long)s * B + u];
+    pe += blk_eq[(long long)s * B + u];
+  }
+  int d1, d2, sum_lt, sum_eq;
+  block_excl_scan2(pl, pe, d1, d2, sum_lt, sum_eq);
   int elt, eeq, tl, te;
   block_excl_scan2(mlt, meq, elt, eeq, tl, te);
-  int lt_before = off_lt[blockIdx.x] + elt;
-  int eq_before = off_eq[blockIdx.x] + eeq;
+  int lt_before = sum_lt + elt;
+  int eq_before = sum_eq + eeq;
   const int seg_neq = neq[s];
 #pragma unroll
   for (int q = 0; q < kItems; ++q) {
@@ -461,9 +465,15 @@ __global__ void __launch_bounds__(kSubThreads) subtree_kernel(
         for (int z = lane; z < 256; z += 32) hist[z] = 0;
         __syncwarp();
         const K hmask = (shift + 8 >= kBits) ? (K)0 : (~(K)0 << (shift + 8));
-        for (int i = a + lane; i < b; i += 32) {
-          K k = skey[i];
-          if (((k ^ prefix) & hmask) == 0) atomicAdd(&hist[(unsigned)(k >> shift) & 255u], 1u);
+        for (int base = a; base < b; base += 32) {
+          const int i = base + lane;
+          unsigned bin = 256u;
+          if (i < b) {
+            const K k = skey[i];
+            if (((k ^ prefix) & hmask) == 0) bin = (unsigned)(k >> shift) & 255u;
+          }
+          const unsigned peers = __match_any_sync(0xffffffffu, bin);
+          if (bin != 256u && lane == __ffs(peers) - 1) atomicAdd(&hist[bin], (unsigned)__popc(peers));
         }
         __syncwarp();
         // lane owns bins [8*lane, 8*lane+8)
@@ -640,8 +650,6 @@ static int build_impl(annf_handle* h, const T* points, int n, int d, int depth, 
     ANNF_ENSURE(h->hist, (size_t)S * 256 * sizeof(unsigned));
     ANNF_ENSURE(h->blk_lt, (size_t)nblk * sizeof(int));
     ANNF_ENSURE(h->blk_eq, (size_t)nblk * sizeof(int));
-    ANNF_ENSURE(h->off_lt, (size_t)nblk * sizeof(int));
-    ANNF_ENSURE(h->off_eq, (size_t)nblk * sizeof(int));
     K* gmin = h->bmin.as<K>();
     K* gmax = h->bmax.as<K>();
     const int fb = std::min(ceil_div((long long)S * d, 256), 4096);
@@ -656,11 +664,10 @@ static int build_impl(annf_handle* h, const T* points, int n, int d, int depth, 
                                                    h->sel_prefix.as<K>(), h->sel_rank.as<int>(),
                                                    h->sel_nlt.as<int>());
     ANNF_CHECK_LAUNCH();
-    extract_keys_kernel<T><<<(unsigned)nblk, kThreads, 0, st>>>(n, d, t, B, cur_pts, h->axis.as<int>(), h->keys.as<K>());
-    ANNF_CHECK_LAUNCH();
     constexpr int kBits = 8 * sizeof(K);
     for (int shift = kBits - 8; shift >= 0; shift -= 8) {
-      hist_kernel<K><<<(unsigned)nblk, 256, 0, st>>>(n, t, B, shift, h->keys.as<K>(), h->sel_prefix.as<K>(), h->hist.as<unsigned>());
+      hist_kernel<T><<<(unsigned)nblk, 256, 0, st>>>(n, d, t, B, shift, shift == kBits - 8, cur_pts, h->axis.as<int>(),
+                                                     h->keys.as<K>(), h->sel_prefix.as<K>(), h->hist.as<unsigned>());
       ANNF_CHECK_LAUNCH();
       pick_kernel<K><<<S, 256, 0, st>>>(shift, shift == 0, h->hist.as<unsigned>(), h->sel_prefix.as<K>(),
                                         h->sel_rank.as<int>(), h->sel_nlt.as<int>(), h->sel_neq.as<int>());
@@ -669,12 +676,9 @@ static int build_impl(annf_handle* h, const T* points, int n, int d, int depth, 
     count_kernel<K><<<(unsigned)nblk, kThreads, 0, st>>>(n, t, B, h->keys.as<K>(), h->sel_prefix.as<K>(),
                                                         h->blk_lt.as<int>(), h->blk_eq.as<int>());
     ANNF_CHECK_LAUNCH();
-    seg_scan_kernel<<<ceil_div(S, 128), 128, 0, st>>>(S, B, h->blk_lt.as<int>(), h->blk_eq.as<int>(),
-                                                      h->off_lt.as<int>(), h->off_eq.as<int>());
-    ANNF_CHECK_LAUNCH();
     scatter_kernel<T><<<(unsigned)nblk, kThreads, 0, st>>>(
         n, d, t, B, h->keys.as<K>(), h->sel_prefix.as<K>(), h->sel_nlt.as<int>(), h->sel_neq.as<int>(),
-        h->off_lt.as<int>(), h->off_eq.as<int>(), cur_pts, cur_perm, alt_pts, alt_perm, h->eqpos.as<int>());
+        h->blk_lt.as<int>(), h->blk_eq.as<int>(), cur_pts, cur_perm, alt_pts, alt_perm, h->eqpos.as<int>());
     ANNF_CHECK_LAUNCH();
     fixup_kernel<T><<<ceil_div((long long)S * 32, 256), 256, 0, st>>>(
         n, d, t, S, h->axis.as<int>(), h->sel_nlt.as<int>(), h->sel_neq.as<int>(), h->eqpos.as<int>(),
