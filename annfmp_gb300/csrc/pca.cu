@@ -65,6 +65,46 @@ __global__ void gather_subset_kernel(const uint8_t* __restrict__ img_a, int wa, 
   }
 }
 
+// Same layout, built 64 samples per block: whole patch rows are copied from the image into shared
+// memory, then every feature row of XT is written with coalesced stores (for F <= 1024).
+constexpr int kGatherS = 64;
+__global__ void __launch_bounds__(256) gather_subset_tiled_kernel(
+    const uint8_t* __restrict__ img_a, int wa, const int* __restrict__ pos_a, int n_a, const uint8_t* __restrict__ img_b,
+    int wb, const int* __restrict__ pos_b, int n_b, int c, int psize, int F, int ns_pad, uint8_t* __restrict__ XT,
+    unsigned* status) {
+  extern __shared__ __align__(16) uint8_t sp[];  // [kGatherS][F]
+  if (smem_overrun(sp, sp + (size_t)kGatherS * F, status)) return;
+  const int P = psize * psize * c, rowlen = psize * c, ns = n_a + n_b;
+  const int s0 = blockIdx.x * kGatherS;
+  for (int task = threadIdx.x; task < kGatherS * psize; task += blockDim.x) {
+    const int i = task / psize, r = task - i * psize;
+    const int s = s0 + i;
+    uint8_t* dst = sp + (size_t)i * F + r * rowlen;
+    if (s < ns) {
+      const uint8_t* src;
+      if (s < n_a) {
+        src = img_a + ((long long)(pos_a[2 * s] + r) * wa + pos_a[2 * s + 1]) * c;
+      } else {
+        const int t = s - n_a;
+        src = img_b + ((long long)(pos_b[2 * t] + r) * wb + pos_b[2 * t + 1]) * c;
+      }
+      for (int e = 0; e < rowlen; ++e) dst[e] = src[e];
+    } else {
+      for (int e = 0; e < rowlen; ++e) dst[e] = 0;
+    }
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < F * kGatherS; e += blockDim.x) {
+    const int f = e / kGatherS, i = e - f * kGatherS;
+    const int s = s0 + i;
+    if (s >= ns_pad) continue;
+    uint8_t v = 0;
+    if (f < P) v = sp[(size_t)i * F + f];
+    else if (f == P) v = s < ns ? 1 : 0;
+    XT[(long long)f * ns_pad + s] = v;
+  }
+}
+
 // G += XT XT^T over a sample-word range; 64x64 output tile per block, 4x4 per thread
 constexpr int kGT = 64;       // output tile
 constexpr int kGW = 16;       // sample words per smem stage
@@ -310,8 +350,16 @@ int pca_fit(annf_handle* h, const uint8_t* img_a, int ha, int wa, const int* pos
   ANNF_ENSURE(h->eigval, (size_t)P * sizeof(double));
   ANNF_ENSURE(h->solver_info, sizeof(int));
   prof_mark(h, "pca:begin", st);
-  gather_subset_kernel<<<std::min(ceil_div((long long)F * ns_pad, 256), 8192), 256, 0, st>>>(
-      img_a, wa, pos_a, n_a, img_b, wb, pos_b, n_b, c, psize, F, ns_pad, h->subset_t.as<uint8_t>());
+  if (F <= 1024) {
+    const size_t gsm = (size_t)kGatherS * F;
+    ANNF_CUDA_TRY(cudaFuncSetAttribute(gather_subset_tiled_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gsm));
+    gather_subset_tiled_kernel<<<ceil_div(ns_pad, kGatherS), 256, gsm, st>>>(
+        img_a, wa, pos_a, n_a, img_b, wb, pos_b, n_b, c, psize, F, ns_pad, h->subset_t.as<uint8_t>(),
+        h->status.as<unsigned>());
+  } else {
+    gather_subset_kernel<<<std::min(ceil_div((long long)F * ns_pad, 256), 8192), 256, 0, st>>>(
+        img_a, wa, pos_a, n_a, img_b, wb, pos_b, n_b, c, psize, F, ns_pad, h->subset_t.as<uint8_t>());
+  }
   ANNF_CHECK_LAUNCH();
   ANNF_CUDA_TRY(cudaMemsetAsync(h->gram.p, 0, (size_t)F * F * sizeof(unsigned long long), st));
   const int tiles = ceil_div(F, kGT);
