@@ -108,7 +108,7 @@ __global__ void __launch_bounds__(256) gather_subset_tiled_kernel(
 // G += XT XT^T over a sample-word range; 64x64 output tile per block, 4x4 per thread
 constexpr int kGT = 64;       // output tile
 constexpr int kGW = 16;       // sample words per smem stage
-constexpr int kGramSplitWords = 8192;  // words per split: int32 partials stay below 2^31
+constexpr int kGramSplitWords = 2048;  // words per split: partials stay far below 2^32; enough blocks to fill the GPU
 
 __global__ void __launch_bounds__(256) gram_kernel(const unsigned* __restrict__ XTw, int F, int nwords,
                                                    unsigned long long* __restrict__ G) {

@@ -254,6 +254,9 @@ __global__ void __launch_bounds__(kThreads) scatter_kernel(
   const int m = c1 - c0;
   if (m <= 0) return;  // uniform per block
   const K pv = pivot[s];
+  __shared__ K skeys[kChunk];
+  for (int i = threadIdx.x; i < m; i += blockDim.x) skeys[i] = keys[c0 + i];  // coalesced
+  __syncthreads();
   const int base = threadIdx.x * kItems;
   unsigned flt = 0, feq = 0;
   int mlt = 0, meq = 0;
@@ -261,7 +264,7 @@ __global__ void __launch_bounds__(kThreads) scatter_kernel(
   for (int q = 0; q < kItems; ++q) {
     int i = base + q;
     if (i < m) {
-      K k = keys[c0 + i];
+      K k = skeys[i];
       if (k < pv) {
         flt |= 1u << q;
         ++mlt;
@@ -304,10 +307,20 @@ __global__ void __launch_bounds__(kThreads) scatter_kernel(
     }
   }
   __syncthreads();
-  const long long tot = (long long)m * d;
-  for (long long e = threadIdx.x; e < tot; e += blockDim.x) {
-    int r = (int)(e / d), c = (int)(e - (long long)r * d);
-    pts_out[(long long)sdst[r] * d + c] = pts_in[(long long)(c0 + r) * d + c];
+  // rows move whole: a group of lanes per row, 16-byte words when rows allow it
+  if (sizeof(T) == 4 && (d & 3) == 0) {
+    const int w = d >> 2;  // float4 words per row
+    const float4* src = reinterpret_cast<const float4*>(pts_in) + (long long)c0 * w;
+    float4* dst4 = reinterpret_cast<float4*>(pts_out);
+    for (int e = threadIdx.x; e < m * w; e += blockDim.x) {
+      const int r = e / w, c = e - r * w;
+      dst4[(long long)sdst[r] * w + c] = src[e];
+    }
+  } else {
+    for (int e = threadIdx.x; e < m * d; e += blockDim.x) {
+      const int r = e / d, c = e - r * d;
+      pts_out[(long long)sdst[r] * d + c] = pts_in[(long long)(c0 + r) * d + c];
+    }
   }
   for (int i = threadIdx.x; i < m; i += blockDim.x) perm_out[sdst[i]] = perm_in[c0 + i];
   (void)nlt;

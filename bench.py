@@ -34,6 +34,8 @@ WORKLOADS = {
     "large": dict(size=2048, seed=1, kind="flow", n_neighbors=4, psize=9, dim_reduced=16, leaf_size=64),
     # 512x512 affine pair (seed 0): psize 7 (147-dim), PCA 8, leaf 32, k 1
     "small": dict(size=512, seed=0, kind="affine", n_neighbors=1, psize=7, dim_reduced=8, leaf_size=32),
+    # 1024x1024 version of the large pair (same generator and parameters): bounded profiler captures
+    "medium": dict(size=1024, seed=1, kind="flow", n_neighbors=4, psize=9, dim_reduced=16, leaf_size=64),
 }
 ROWS_SAMPLE = 32
 L2_FLUSH_BYTES = 256 << 20
