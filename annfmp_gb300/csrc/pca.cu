@@ -213,9 +213,11 @@ constexpr int kSlices = 8;  // signed 7-bit digits per coefficient
 // digits[j][k][word*4 + byte] laid out over the padded patch (row r occupies rw bytes, rw =
 // round_up(psize*c, 4)), total W4 words (multiple of 4). Also scale exponent per component and
 // the FP64 mean term m_j = mean . c_j.
+__device__ __forceinline__ __int128 double_to_fixed(double m, int sh);
+
 __global__ void digits_kernel(const double* __restrict__ comps, const double* __restrict__ mean, int P, int psize,
                               int c, int rw, int W4, int8_t* __restrict__ digits, int* __restrict__ expo,
-                              double* __restrict__ mproj) {
+                              double* __restrict__ mproj, unsigned long long* __restrict__ mfix) {
   const int j = blockIdx.x;
   const double* cj = comps + (long long)j * P;
   __shared__ double smax[256];
@@ -253,12 +255,59 @@ __global__ void digits_kernel(const double* __restrict__ comps, const double* __
     double acc = 0.0;
     for (int i = 0; i < P; ++i) acc = __dadd_rn(acc, __dmul_rn(mean[i], cj[i]));
     mproj[j] = acc;
+    const __int128 M = double_to_fixed(acc, 7 * (kSlices - 1) + E);  // the projection's fixed point
+    mfix[2 * j] = (unsigned long long)M;
+    mfix[2 * j + 1] = (unsigned long long)(M >> 64);
   }
   (void)sm;
   (void)mm;
 }
 
 constexpr int kPTW = 32, kPTH = 4;  // projection tile: 32 x 4 pixels, one thread per pixel
+
+// D * 2^-sh rounded to the nearest float (ties to even), integer arithmetic only
+__device__ __forceinline__ float fixed_to_float(__int128 D, int sh) {
+  if (D == 0) return 0.0f;
+  const bool neg = D < 0;
+  const unsigned __int128 A = neg ? (unsigned __int128)(-D) : (unsigned __int128)D;
+  const unsigned long long hi = (unsigned long long)(A >> 64), lo = (unsigned long long)A;
+  const int p = hi ? 127 - __clzll((long long)hi) : 63 - __clzll((long long)lo);  // top bit
+  unsigned long long mant;
+  int e;
+  if (p <= 23) {
+    mant = lo;
+    e = -sh;
+  } else {
+    const int s = p - 23;
+    const unsigned __int128 q = A >> s;
+    const unsigned __int128 r = A - (q << s);
+    const unsigned __int128 half = (unsigned __int128)1 << (s - 1);
+    mant = (unsigned long long)q;
+    if (r > half || (r == half && (mant & 1ull))) ++mant;  // may reach 2^24: still exact below
+    e = s - sh;
+  }
+  const float f = ldexpf((float)mant, e);
+  return neg ? -f : f;
+}
+
+// m * 2^sh rounded to an integer (m FP64); exact whenever m's last bit weighs at least 2^-sh
+__device__ __forceinline__ __int128 double_to_fixed(double m, int sh) {
+  if (m == 0.0) return 0;
+  int e;
+  const double f = frexp(fabs(m), &e);                          // |m| = f 2^e, f in [0.5, 1)
+  const long long mant = (long long)ldexp(f, 53);                // exact 53-bit integer
+  const int s = e - 53 + sh;                                     // |m| 2^sh = mant 2^s
+  __int128 v;
+  if (s >= 0) {
+    v = (__int128)mant << s;
+  } else if (s > -64) {
+    const long long q = mant >> (-s), r = mant - (q << (-s)), half = 1LL << (-s - 1);
+    v = q + ((r > half || (r == half && (q & 1))) ? 1 : 0);
+  } else {
+    v = 0;
+  }
+  return m < 0 ? -v : v;
+}
 
 __device__ __forceinline__ unsigned load_u32_unaligned_smem(const unsigned* base_words, int byte_off) {
   const int w = byte_off >> 2, sh = (byte_off & 3) * 8;
@@ -271,8 +320,9 @@ __global__ void __launch_bounds__(kPTW * kPTH) project_kernel(const uint8_t* __r
                                                                int psize, int rw, int ncomp,
                                                                const int8_t* __restrict__ digits,
                                                                const int* __restrict__ expo,
-                                                               const double* __restrict__ mproj, OutT* __restrict__ out,
-                                                               unsigned* status) {
+                                                               const double* __restrict__ mproj,
+                                                               const unsigned long long* __restrict__ mfix,
+                                                               OutT* __restrict__ out, unsigned* status) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int nrows = H - psize + 1, ncols = W - psize + 1;
   const int x0 = blockIdx.x * kPTW, y0 = blockIdx.y * kPTH;
@@ -308,10 +358,10 @@ __global__ void __launch_bounds__(kPTW * kPTH) project_kernel(const uint8_t* __r
   }
   const long long pix = (long long)y * ncols + x;
   for (int j = 0; j < ncomp; ++j) {
-    double acc = 0.0;
     const int4* dj = reinterpret_cast<const int4*>(sdig + j * kSlices * W4);
+    int slice[kSlices];
 #pragma unroll
-    for (int k = kSlices - 1; k >= 0; --k) {
+    for (int k = 0; k < kSlices; ++k) {
       int s = 0;
 #pragma unroll
       for (int w = 0; w < W4; w += 4) {
@@ -321,11 +371,23 @@ __global__ void __launch_bounds__(kPTW * kPTH) project_kernel(const uint8_t* __r
         s = dp4a_us(xw[w + 2], dd.z, s);
         s = dp4a_us(xw[w + 3], dd.w, s);
       }
-      acc = __dadd_rn(__dmul_rn(acc, 0.0078125), (double)s);  // Horner in base 2^-7
+      slice[k] = s;
     }
-    const double xc = ldexp(acc, -__ldg(expo + j));
-    const double yv = __dsub_rn(xc, __ldg(mproj + j));
-    out[pix * ncomp + j] = (OutT)yv;
+    if constexpr (sizeof(OutT) == 4) {
+      // exact: X = sum_k slice_k 2^(7(7-k)) = patch.c * 2^(49+E); subtract the mean term as the same
+      // fixed-point integer and round once to FP32 -- no FP64 arithmetic on this path
+      __int128 X = slice[0];
+#pragma unroll
+      for (int k = 1; k < kSlices; ++k) X = (X << 7) + slice[k];
+      const __int128 M = ((__int128)(long long)__ldg(mfix + 2 * j + 1) << 64) | (unsigned long long)__ldg(mfix + 2 * j);
+      out[pix * ncomp + j] = fixed_to_float(X - M, 7 * (kSlices - 1) + __ldg(expo + j));
+    } else {
+      double acc = 0.0;
+#pragma unroll
+      for (int k = 0; k < kSlices; ++k) acc = __dadd_rn(__dmul_rn(acc, 128.0), (double)slice[k]);  // exact: < 2^53
+      const double xc = ldexp(acc, -(7 * (kSlices - 1)) - __ldg(expo + j));
+      out[pix * ncomp + j] = (OutT)__dsub_rn(xc, __ldg(mproj + j));
+    }
   }
 }
 
@@ -412,12 +474,15 @@ int project(annf_handle* h, const uint8_t* img, int H, int W, int c, int psize, 
   const int W4 = round_up(std::max(psize * rw / 4, 8), 4);
   ANNF_REQUIRE(W4 <= 64, "annf_project: patch rows larger than 256 bytes are not supported");
   ANNF_REQUIRE(ncomp >= 1 && ncomp <= P, "annf_project: n_components out of range");
-  ANNF_ENSURE(h->digits, (size_t)ncomp * kSlices * W4 * 4 + (size_t)ncomp * sizeof(int));
+  ANNF_ENSURE(h->digits, (size_t)ncomp * kSlices * W4 * 4 + (size_t)ncomp * sizeof(int) + 16 +
+                             (size_t)ncomp * 2 * sizeof(unsigned long long));
   ANNF_ENSURE(h->meanproj, (size_t)ncomp * sizeof(double));
   prof_mark(h, "project:begin", st);
   int8_t* dig = h->digits.as<int8_t>();
   int* expo = reinterpret_cast<int*>(dig + (size_t)ncomp * kSlices * W4 * 4);
-  digits_kernel<<<ncomp, 256, 0, st>>>(comps, mean, P, psize, c, rw, W4, dig, expo, h->meanproj.as<double>());
+  unsigned long long* mfix = reinterpret_cast<unsigned long long*>(
+      (reinterpret_cast<uintptr_t>(expo + ncomp) + 15) & ~uintptr_t(15));
+  digits_kernel<<<ncomp, 256, 0, st>>>(comps, mean, P, psize, c, rw, W4, dig, expo, h->meanproj.as<double>(), mfix);
   ANNF_CHECK_LAUNCH();
   const int nrows = H - psize + 1, ncols = W - psize + 1;
   dim3 grid(ceil_div(ncols, kPTW), ceil_div(nrows, kPTH));
@@ -432,13 +497,13 @@ int project(annf_handle* h, const uint8_t* img, int H, int W, int c, int psize, 
       ANNF_CUDA_TRY(cudaFuncSetAttribute(project_kernel<float, WV>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
                                          (int)smem));                                                            \
       project_kernel<float, WV><<<grid, kPTW * kPTH, smem, st>>>(img, H, W, c, psize, rw, ncomp, dig, expo,       \
-                                                                  h->meanproj.as<double>(), (float*)out,      \
+                                                                  h->meanproj.as<double>(), mfix, (float*)out,      \
                                                                   h->status.as<unsigned>());        \
     } else {                                                                                                     \
       ANNF_CUDA_TRY(cudaFuncSetAttribute(project_kernel<double, WV>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
                                          (int)smem));                                                            \
       project_kernel<double, WV><<<grid, kPTW * kPTH, smem, st>>>(img, H, W, c, psize, rw, ncomp, dig, expo,      \
-                                                                   h->meanproj.as<double>(), (double*)out,    \
+                                                                   h->meanproj.as<double>(), mfix, (double*)out,    \
                                                                    h->status.as<unsigned>());      \
     }                                                                                                            \
     break;

@@ -23,7 +23,7 @@
 
 namespace annf {
 
-constexpr int kChunk = 4096;     // positions per CTA in the global levels
+constexpr int kChunk = 2048;     // positions per CTA in the global levels
 constexpr int kThreads = 256;
 constexpr int kItems = kChunk / kThreads;
 
@@ -599,7 +599,7 @@ static size_t subtree_smem(int smax, int d) {
 
 template <typename T>
 static int subtree_capacity(int d) {
-  const size_t budget = 200 * 1024;
+  const size_t budget = 100 * 1024;  // two finisher CTAs per SM
   int smax = 4096;
   while (smax > 1 && subtree_smem<T>(smax, d) > budget) smax >>= 1;
   return smax;
