@@ -62,6 +62,7 @@ SIGNATURES = {
     "annf_build_tree": (_i, [_vp, _vp, _i, _i, _i, _i, _i, _vp]),
     "annf_tree_get": (_i, [_vp, ctypes.POINTER(TreeView)]),
     "annf_kneighbors": (_i, [_vp, _vp, _i, _i, _ll, _vp, _vp, _vp]),
+    "annf_kneighbors_noalloc": (_i, [_vp, _vp, _i, _i, _ll, _vp, _vp, _vp]),
     "annf_process_rows": (_i, [_vp, _vp, _vp, _i, _vp, _i, _i, _vp, _i, _i, _i, _i, _i, _ll, _vp, _vp, _vp]),
     "annf_process_rows_img": (_i, [_vp, _vp, _vp, _i, _i, _vp, _i, _i, _i, _i, _vp, _i, _i, _i, _i, _i, _ll,
                                    _vp, _vp, _vp]),

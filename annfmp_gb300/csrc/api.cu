@@ -23,6 +23,8 @@ int process_rows_generic(annf_handle* h, int* final_idx, const PatchSrc& A, cons
                          int* knn_out, float* dist_out, cudaStream_t st);
 int kneighbors_generic(annf_handle* h, const void* Q, int nq, int K, long long max_leaves, void* dist, int* idx,
                        cudaStream_t st);
+int kneighbors_noalloc(annf_handle* h, const void* Q, int nq, int K, long long max_leaves, void* dist, int* idx,
+                       cudaStream_t st);
 int pca_fit(annf_handle* h, const uint8_t* img_a, int ha, int wa, const int* pos_a, int n_a, const uint8_t* img_b,
             int hb, int wb, const int* pos_b, int n_b, int c, int psize, int ncomp, double* comps, double* mean,
             cudaStream_t st);
@@ -240,6 +242,17 @@ int annf_device_status(annf_handle* h, void* stream, unsigned* bits_out) {
     return ANNF_ERR_DEVICE;
   }
   return ANNF_OK;
+}
+
+int annf_kneighbors_noalloc(annf_handle* h, const void* queries, int nq, int k, long long max_leaves, void* distances,
+                            int* indices, void* stream) {
+  ANNF_API_HANDLE(h);
+  int rc = check_k(h, k, max_leaves);
+  if (rc != ANNF_OK) return rc;
+  ANNF_REQUIRE(nq >= 0, "annf_kneighbors_noalloc: nq < 0");
+  if (nq == 0) return ANNF_OK;
+  ANNF_REQUIRE(queries && distances && indices, "annf_kneighbors_noalloc: NULL array");
+  return kneighbors_noalloc(h, queries, nq, k, max_leaves, distances, indices, static_cast<cudaStream_t>(stream));
 }
 
 long long annf_launch_count(void) { return g_launches.load(std::memory_order_relaxed); }

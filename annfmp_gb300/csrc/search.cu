@@ -1288,4 +1288,103 @@ int kneighbors_generic(annf_handle* h, const void* Q, int nq, int K, long long m
                            static_cast<double*>(dist), idx, st);
 }
 
+// ---------------------------------------------------------------------------------------------
+// Exact kNN that allocates nothing.
+//
+// Some callers cannot allocate device memory at query time: a query issued while a stream is
+// being captured into a CUDA graph (cudaMalloc is not capturable), a serving process whose device
+// memory was reserved up front, or a caller running under an allocator that forbids growth. They
+// build the tree once (that call allocates), and then query with this variant, whose only scratch
+// -- the natural-leaf seeds of every query -- lives in one fixed array in device memory. The array
+// is statically sized (kNoAllocMaxEntries query*k entries of 12 bytes, 3 MiB), exists on every
+// GPU that loads the library until the process exits, and is shared by all calls: two calls that
+// overlap on the GPU (different streams, no ordering) race on it. Nothing in it needs clearing:
+// every entry a call reads was written earlier in the same call.
+// ---------------------------------------------------------------------------------------------
+constexpr long long kNoAllocMaxEntries = 1LL << 18;  // queries * k per call
+constexpr size_t kNoAllocKeyBytes = (size_t)kNoAllocMaxEntries * 8;
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocKeyBytes + (size_t)kNoAllocMaxEntries * 4];
+
+// device address of g_noalloc_scratch per device, looked up once (a host-side stand-in, not the
+// symbol itself, must be passed to kernels)
+static unsigned char* g_noalloc_addr[64] = {};
+
+static int noalloc_scratch(int device, unsigned char** out) {
+  if (device < 0 || device >= 64) {
+    set_error("annf_kneighbors_noalloc: device index out of range");
+    return ANNF_ERR_INVALID;
+  }
+  if (!g_noalloc_addr[device]) {  // first call on this device (the device is current)
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p) {
+      set_error(std::string("annf_kneighbors_noalloc: cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+      return ANNF_ERR_CUDA;
+    }
+    g_noalloc_addr[device] = static_cast<unsigned char*>(p);
+  }
+  *out = g_noalloc_addr[device];
+  return ANNF_OK;
+}
+
+template <typename T, int D>
+static int noalloc_typed(annf_handle* h, unsigned char* scratch, const T* Q, int nq, int K, long long max_leaves,
+                         T* dist, int* idx, cudaStream_t st) {
+  using Kt = typename KeyOps<T>::K;
+  TreeView<T> tv = view_of<T>(h);
+  if (max_leaves < (1LL << h->depth)) {  // budgeted search needs no scratch at all
+    const size_t smem = NodeCache<T>::bytes(h->depth) +
+                        kDfsWarps * (kMaxDynD * sizeof(T) + 32 * sizeof(T) + 32 * sizeof(int) + 32 * sizeof(uint32_t)) + 64;
+    exact_dfs_kernel<T, D><<<std::max(1, std::min(ceil_div(nq, kDfsWarps), 32 * num_sms())), 32 * kDfsWarps, smem, st>>>(
+        tv, Q, nq, K, max_leaves, 1, nullptr, dist, idx);
+    ANNF_CHECK_LAUNCH();
+    return ANNF_OK;
+  }
+  Kt* seed_key = reinterpret_cast<Kt*>(scratch);
+  int* seed_pos = reinterpret_cast<int*>(scratch + kNoAllocKeyBytes);
+  int rc = ANNF_OK;
+  const size_t nsm = NodeCache<T>::bytes(h->depth) + 8 * kMaxDynD * sizeof(T);
+  ANNF_DISPATCH_KM(pick_km(K), {
+    natural_knn_kernel<T, D, KM><<<(int)std::min<long long>(ceil_div((long long)nq * 32, 256), 64LL * num_sms()), 256,
+                                   nsm, st>>>(tv, Q, 0, nq, K, seed_pos, seed_key);
+  });
+  ANNF_CHECK_LAUNCH();
+  const size_t ssm = NodeCache<T>::bytes(h->depth) + 8 * kMaxDynD * sizeof(T) + 64;
+  exact_scan_kernel<T, D><<<std::max(1, std::min(ceil_div(nq, 8), 32 * num_sms())), 256, ssm, st>>>(
+      tv, Q, nq, K, seed_key, 1, nullptr, dist, idx);
+  ANNF_CHECK_LAUNCH();
+  return rc;
+}
+
+int kneighbors_noalloc(annf_handle* h, const void* Q, int nq, int K, long long max_leaves, void* dist, int* idx,
+                       cudaStream_t st) {
+  if ((long long)nq * K > kNoAllocMaxEntries) {
+    set_error("annf_kneighbors_noalloc: n_queries * k exceeds the fixed scratch of " +
+              std::to_string(kNoAllocMaxEntries) + " entries; split the queries or use annf_kneighbors");
+    return ANNF_ERR_INVALID;
+  }
+  // every shared-memory footprint used below stays under the 48 KiB default, so no launch needs
+  // an attribute change; check it rather than assume it
+  const size_t sz = h->real_type == ANNF_REAL_F32 ? sizeof(float) : sizeof(double);
+  const int lv = h->depth < kCacheLevels ? h->depth : kCacheLevels;
+  const size_t worst = (size_t)(1 << lv) * (4 + sz) + 32 + 8 * kMaxDynD * sz +
+                       kDfsWarps * (32 * sz + 32 * sizeof(int) + 32 * sizeof(uint32_t)) + 64;
+  if (worst > 48 * 1024) {
+    set_error("annf_kneighbors_noalloc: shared-memory footprint too large for this tree");
+    return ANNF_ERR_UNSUPPORTED;
+  }
+  unsigned char* scratch = nullptr;
+  int rc = noalloc_scratch(h->device, &scratch);
+  if (rc != ANNF_OK) return rc;
+  if (h->real_type == ANNF_REAL_F32) {
+    ANNF_DISPATCH_D(float, h->d,
+                    rc = (noalloc_typed<float, D>(h, scratch, static_cast<const float*>(Q), nq, K, max_leaves,
+                                                  static_cast<float*>(dist), idx, st)));
+  } else {
+    rc = noalloc_typed<double, 0>(h, scratch, static_cast<const double*>(Q), nq, K, max_leaves,
+                                  static_cast<double*>(dist), idx, st);
+  }
+  return rc;
+}
+
 }  // namespace annf

@@ -83,6 +83,18 @@ int annf_tree_get(const annf_handle* h, annf_tree_view* out);
 int annf_kneighbors(annf_handle* h, const void* queries, int nq, int k, long long max_leaves,
                     void* distances, int* indices, void* stream);
 
+/* No counterpart in the reference. The same exact k nearest neighbours as annf_kneighbors (same
+ * results), for callers that must not allocate device memory while they query: work issued under
+ * CUDA stream capture (cudaMalloc cannot be captured), serving processes whose device memory is
+ * reserved ahead of time, or allocators that refuse to grow. Build the tree first (that allocates);
+ * this call then allocates nothing. Its scratch is one static device array shared by all calls,
+ * sized for nq * k <= 262144 (3 MiB, held by every GPU that loads the library until exit); larger
+ * requests fail with ANNF_ERR_INVALID. The first call on each device looks the array's device
+ * address up (cudaGetSymbolAddress), so make that first call before any stream capture. Calls that
+ * overlap on the GPU (unordered streams) race on the shared scratch. */
+int annf_kneighbors_noalloc(annf_handle* h, const void* queries, int nq, int k, long long max_leaves,
+                            void* distances, int* indices, void* stream);
+
 /* The row-propagation NNF over an n_rows x n_cols grid of A patches (reduced, [n_rows*n_cols*d]
  * real_type, row-major pixels). Raw uint8 patches come as arrays: patches_a [n_a*P],
  * patches_b [n_b*P] (may be NULL when select_best == 0).
