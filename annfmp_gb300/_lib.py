@@ -69,6 +69,8 @@ SIGNATURES = {
     "annf_pca_fit": (_i, [_vp, _vp, _i, _i, _vp, _i, _vp, _i, _i, _vp, _i, _i, _i, _i, _vp, _vp, _vp]),
     "annf_project": (_i, [_vp, _vp, _i, _i, _i, _i, _vp, _vp, _i, _i, _vp, _vp]),
     "annf_device_status": (_i, [_vp, _vp, ctypes.POINTER(_u)]),
+    "annf_parallel_nnf": (_i, [_vp, _vp, _vp, _i, _i, _vp, _i, _i, _i, _i, _vp, _i, _vp, _i, _i, _u, _vp, _vp]),
+    "annf_raw_nn": (_i, [_vp, _vp, _i, _i, _vp, _i, _i, _i, _i, _vp, _i, _vp, _vp]),
     "annf_profile_enable": (_i, [_vp, _i]),
     "annf_profile_read": (_i, [_vp, _vp, _i, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_char_p)]),
     "annf_launch_count": (_ll, []),

@@ -25,6 +25,12 @@ int kneighbors_generic(annf_handle* h, const void* Q, int nq, int K, long long m
                        cudaStream_t st);
 int kneighbors_noalloc(annf_handle* h, const void* Q, int nq, int K, long long max_leaves, void* dist, int* idx,
                        cudaStream_t st);
+int natural_knn_all(annf_handle* h, const void* Q, long long nq, int K, int* out_pos, cudaStream_t st);
+int fast_search(annf_handle* h, const uint8_t* img_a, int ha, int wa, const uint8_t* img_b, int hb, int wb, int c,
+                int psize, int K, const int* nat_pos, const int* prop, int n_prop, int iters, uint32_t seed,
+                int* final_idx, float* dist_out, cudaStream_t st);
+int raw_nn(const uint8_t* img_a, int ha, int wa, const uint8_t* img_b, int hb, int wb, int c, int psize,
+           const int* qpix, int nq, unsigned long long* best, cudaStream_t st);
 int pca_fit(annf_handle* h, const uint8_t* img_a, int ha, int wa, const int* pos_a, int n_a, const uint8_t* img_b,
             int hb, int wb, const int* pos_b, int n_b, int c, int psize, int ncomp, double* comps, double* mean,
             cudaStream_t st);
@@ -92,7 +98,7 @@ void annf_destroy(annf_handle* h) {
                     &h->point_leaf, &h->leaf_box, &h->bmin, &h->bmax, &h->axis, &h->keys, &h->hist, &h->sel_prefix,
                     &h->sel_rank, &h->sel_nlt, &h->sel_neq, &h->blk_lt, &h->blk_eq, &h->off_lt, &h->off_eq,
                     &h->eqpos, &h->nat_keys, &h->nat_pos, &h->lists, &h->next_range, &h->part_keys,
-                    &h->part_pos, &h->gram, &h->colsum, &h->subset_t, &h->cov, &h->eigval, &h->digits,
+                    &h->part_pos, &h->fast_buf, &h->fast_nat, &h->gram, &h->colsum, &h->subset_t, &h->cov, &h->eigval, &h->digits,
                     &h->meanproj, &h->solver_ws, &h->solver_info, &h->status};
   for (DevBuf* b : bufs) b->release();
   for (int i = 0; i < annf_handle::kMaxMarks; ++i)
@@ -253,6 +259,41 @@ int annf_kneighbors_noalloc(annf_handle* h, const void* queries, int nq, int k, 
   if (nq == 0) return ANNF_OK;
   ANNF_REQUIRE(queries && distances && indices, "annf_kneighbors_noalloc: NULL array");
   return kneighbors_noalloc(h, queries, nq, k, max_leaves, distances, indices, static_cast<cudaStream_t>(stream));
+}
+
+int annf_parallel_nnf(annf_handle* h, int* final_idx, const uint8_t* img_a, int ha, int wa, const uint8_t* img_b,
+                      int hb, int wb, int channels, int psize, const void* ared, int k, const int* proposals,
+                      int n_prop, int iters, unsigned seed, float* dist_out, void* stream) {
+  ANNF_API_HANDLE(h);
+  int rc = check_k(h, k, 2147483640);
+  if (rc != ANNF_OK) return rc;
+  ANNF_REQUIRE(final_idx && img_a && img_b && ared, "annf_parallel_nnf: NULL argument");
+  ANNF_REQUIRE(channels >= 1 && psize >= 1 && psize <= ha && psize <= wa && psize <= hb && psize <= wb,
+               "annf_parallel_nnf: bad geometry");
+  ANNF_REQUIRE((long long)(hb - psize + 1) * (wb - psize + 1) == h->n,
+               "annf_parallel_nnf: the tree must hold every patch of image B");
+  ANNF_REQUIRE(n_prop >= 0 && (n_prop == 0 || proposals), "annf_parallel_nnf: bad proposals");
+  ANNF_REQUIRE(iters >= 0 && iters <= 64, "annf_parallel_nnf: iters out of range");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const long long nA = (long long)(ha - psize + 1) * (wa - psize + 1);
+  ANNF_ENSURE(h->fast_nat, (size_t)nA * k * sizeof(int));
+  prof_mark(h, "parallel:begin", st);
+  rc = natural_knn_all(h, ared, nA, k, h->fast_nat.as<int>(), st);
+  if (rc != ANNF_OK) return rc;
+  prof_mark(h, "natural_knn", st);
+  return fast_search(h, img_a, ha, wa, img_b, hb, wb, channels, psize, k, h->fast_nat.as<int>(), proposals, n_prop,
+                     iters, seed, final_idx, dist_out, st);
+}
+
+int annf_raw_nn(annf_handle* h, const uint8_t* img_a, int ha, int wa, const uint8_t* img_b, int hb, int wb,
+                int channels, int psize, const int* query_pixels, int nq, unsigned long long* best, void* stream) {
+  ANNF_API_HANDLE(h);
+  ANNF_REQUIRE(img_a && img_b && (nq == 0 || (query_pixels && best)), "annf_raw_nn: NULL argument");
+  ANNF_REQUIRE(channels >= 1 && psize >= 1 && psize <= ha && psize <= wa && psize <= hb && psize <= wb,
+               "annf_raw_nn: bad geometry");
+  if (nq == 0) return ANNF_OK;
+  return raw_nn(img_a, ha, wa, img_b, hb, wb, channels, psize, query_pixels, nq, best,
+                static_cast<cudaStream_t>(stream));
 }
 
 long long annf_launch_count(void) { return g_launches.load(std::memory_order_relaxed); }

@@ -1,0 +1,257 @@
+// fast.cu -- the parallel NNF form (no row chain) and the exact raw-patch nearest neighbour used
+// to measure distance error (sm_103a).
+//
+// The plain form follows the reference's row-sequential propagation (each row waits for the one
+// above). This form has no such dependency: every pixel gets candidates from its natural leaf
+// (approximate leaf distances, top-4k re-ranked exactly in FP32), from offset proposals (a learned
+// predictor, optional), and from a few parallel propagation / random-search passes over its
+// neighbours' current matches. Every candidate is verified with the exact integer raw-patch SSD,
+// so the answer is always a real patch distance.
+#include <algorithm>
+
+#include "common.cuh"
+#include "handle.cuh"
+
+namespace annf {
+
+int num_sms();
+
+// ---------------------------------------------------------------------------------------------
+// exact integer SSD between two psize x psize x c patches of two images (rows padded reads)
+// ---------------------------------------------------------------------------------------------
+__device__ __forceinline__ unsigned ldw_at(const uint8_t* base, long long off) {
+  const unsigned* w = reinterpret_cast<const unsigned*>(base + (off & ~3LL));
+  const int sh = (int)(off & 3) * 8;
+  const unsigned lo = __ldg(w);
+  return sh ? __funnelshift_r(lo, __ldg(w + 1), sh) : lo;
+}
+
+struct Img {
+  const uint8_t* p;
+  int h, w, c, psize, ncols;  // ncols = w - psize + 1
+};
+
+__device__ __forceinline__ int patch_ssd(const Img& A, int ay, int ax, const Img& B, int by, int bx) {
+  const int rowlen = A.psize * A.c;
+  int s = 0;
+  for (int r = 0; r < A.psize; ++r) {
+    const long long ao = ((long long)(ay + r) * A.w + ax) * A.c, bo = ((long long)(by + r) * B.w + bx) * B.c;
+    int e = 0;
+    for (; e + 4 <= rowlen; e += 4) {
+      const unsigned x = __vabsdiffu4(ldw_at(A.p, ao + e), ldw_at(B.p, bo + e));
+      s = (int)__dp4a(x, x, (unsigned)s);
+    }
+    for (; e < rowlen; ++e) {
+      const int t = (int)__ldg(A.p + ao + e) - (int)__ldg(B.p + bo + e);
+      s += t * t;
+    }
+  }
+  return s;
+}
+
+// ---------------------------------------------------------------------------------------------
+// exact nearest B patch of sampled A pixels (the distance-error reference): every B patch is
+// compared with 32 queries held in shared memory; best (ssd, index) per query by 64-bit atomicMin
+// ---------------------------------------------------------------------------------------------
+constexpr int kRawQ = 32;
+constexpr int kRawMaxWords = 128;  // padded patch words (psize * ceil(psize*c/4))
+
+template <int NW>
+__global__ void __launch_bounds__(256) raw_nn_kernel(Img A, Img B, const int* __restrict__ qpix, int nq, int nb_split,
+                                                     unsigned long long* __restrict__ best) {
+  __shared__ unsigned sq[kRawQ][kRawMaxWords + 1];
+  __shared__ unsigned long long sbest[kRawQ];
+  const int rowlen = A.psize * A.c, wpr = (rowlen + 3) / 4;
+  const int nw = NW > 0 ? NW : A.psize * wpr;
+  const int q0 = blockIdx.x * kRawQ;
+  const int nqt = min(kRawQ, nq - q0);
+  for (int e = threadIdx.x; e < kRawQ * nw; e += blockDim.x) {
+    const int qi = e / nw, w = e - qi * nw;
+    unsigned v = 0;
+    if (qi < nqt) {
+      const int pix = qpix[q0 + qi];
+      const int y = pix / A.ncols, x = pix - y * A.ncols;
+      const int r = w / wpr, wi = w - r * wpr;
+      const long long off = ((long long)(y + r) * A.w + x) * A.c + wi * 4;
+      const int valid = min(4, rowlen - wi * 4);
+      v = ldw_at(A.p, off);
+      if (valid < 4) v &= (1u << (8 * valid)) - 1u;
+    }
+    sq[qi][w] = v;
+  }
+  for (int i = threadIdx.x; i < kRawQ; i += blockDim.x) sbest[i] = ~0ull;
+  __syncthreads();
+  const long long nb = (long long)(B.h - B.psize + 1) * B.ncols;
+  const long long per = (nb + gridDim.y - 1) / gridDim.y;
+  const long long b0 = blockIdx.y * per, b1 = min(nb, b0 + per);
+  unsigned long long mine[kRawQ];
+#pragma unroll
+  for (int i = 0; i < kRawQ; ++i) mine[i] = ~0ull;
+  for (long long b = b0 + threadIdx.x; b < b1; b += blockDim.x) {
+    const int by = (int)(b / B.ncols), bx = (int)(b - (long long)by * B.ncols);
+    unsigned bw[NW > 0 ? NW : kRawMaxWords];
+#pragma unroll
+    for (int w = 0; w < (NW > 0 ? NW : kRawMaxWords); ++w) {
+      if (NW == 0 && w >= nw) break;
+      const int r = w / wpr, wi = w - r * wpr;
+      const int valid = min(4, rowlen - wi * 4);
+      unsigned v = ldw_at(B.p, ((long long)(by + r) * B.w + bx) * B.c + wi * 4);
+      if (valid < 4) v &= (1u << (8 * valid)) - 1u;
+      bw[w] = v;
+    }
+#pragma unroll 4
+    for (int qi = 0; qi < kRawQ; ++qi) {
+      unsigned s = 0;
+#pragma unroll
+      for (int w = 0; w < (NW > 0 ? NW : kRawMaxWords); ++w) {
+        if (NW == 0 && w >= nw) break;
+        const unsigned x = __vabsdiffu4(sq[qi][w], bw[w]);
+        s = __dp4a(x, x, s);
+      }
+      const unsigned long long key = ((unsigned long long)s << 32) | (unsigned long long)b;
+      mine[qi] = key < mine[qi] ? key : mine[qi];
+    }
+  }
+#pragma unroll
+  for (int qi = 0; qi < kRawQ; ++qi)
+    if (qi < nqt && mine[qi] != ~0ull) atomicMin(&sbest[qi], mine[qi]);
+  __syncthreads();
+  for (int qi = threadIdx.x; qi < nqt; qi += blockDim.x) atomicMin(&best[q0 + qi], sbest[qi]);
+}
+
+// ---------------------------------------------------------------------------------------------
+// parallel NNF: initial choice among candidates, then propagation / random-search passes
+// ---------------------------------------------------------------------------------------------
+struct Match {
+  int* idx;  // [nA] best B index
+  int* ssd;  // [nA] its exact raw SSD
+};
+
+__device__ __forceinline__ uint32_t hash3(uint32_t a, uint32_t b, uint32_t c) {
+  uint32_t h = a * 0x9E3779B1u ^ (b + 0x7F4A7C15u) * 0x85EBCA77u ^ (c + 0x165667B1u) * 0xC2B2AE3Du;
+  h ^= h >> 15;
+  h *= 0x2C1B3C6Du;
+  h ^= h >> 12;
+  h *= 0x297A2D39u;
+  h ^= h >> 15;
+  return h;
+}
+
+// candidates: k natural-leaf neighbours (tree positions -> B indices) and n_prop proposals
+__global__ void fast_init_kernel(Img A, Img B, int nA, int K, const int* __restrict__ nat_pos,
+                                 const int* __restrict__ perm, const int* __restrict__ prop, int n_prop, Match out) {
+  const int nb_rows = B.h - B.psize + 1;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nA; i += gridDim.x * blockDim.x) {
+    const int y = i / A.ncols, x = i - y * A.ncols;
+    int best = -1, bs = 0x7fffffff;
+    for (int j = 0; j < K + n_prop; ++j) {
+      int b = j < K ? __ldg(perm + __ldg(nat_pos + (long long)i * K + j)) : __ldg(prop + (long long)i * n_prop + (j - K));
+      if (b < 0) continue;
+      const int by = b / B.ncols, bx = b - by * B.ncols;
+      if (by >= nb_rows) continue;
+      const int s = patch_ssd(A, y, x, B, by, bx);
+      if (s < bs || (s == bs && b < best)) {
+        bs = s;
+        best = b;
+      }
+    }
+    out.idx[i] = best;
+    out.ssd[i] = bs;
+  }
+}
+
+// one pass: the four neighbours' matches at distance 'jump', shifted to this pixel, and 'nrand'
+// random offsets around the current match within 'radius'
+__global__ void fast_prop_kernel(Img A, Img B, int nA, int jump, int radius, int nrand, uint32_t seed, Match in,
+                                 Match out) {
+  const int nb_rows = B.h - B.psize + 1, na_rows = nA / A.ncols;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nA; i += gridDim.x * blockDim.x) {
+    const int y = i / A.ncols, x = i - y * A.ncols;
+    int best = in.idx[i], bs = in.ssd[i];
+    const int b0y = best / B.ncols, b0x = best - b0y * B.ncols;
+    auto consider = [&](int by, int bx) {
+      if (by < 0 || bx < 0 || by >= nb_rows || bx >= B.ncols) return;
+      const int b = by * B.ncols + bx;
+      if (b == best) return;
+      const int s = patch_ssd(A, y, x, B, by, bx);
+      if (s < bs || (s == bs && b < best)) {
+        bs = s;
+        best = b;
+      }
+    };
+    const int dy[4] = {-1, 1, 0, 0}, dx[4] = {0, 0, -1, 1};
+#pragma unroll
+    for (int t = 0; t < 4; ++t) {
+      const int ny = y + dy[t] * jump, nx = x + dx[t] * jump;
+      if (ny < 0 || nx < 0 || ny >= na_rows || nx >= A.ncols) continue;
+      const int nb = in.idx[ny * A.ncols + nx];
+      if (nb < 0) continue;
+      const int nby = nb / B.ncols, nbx = nb - nby * B.ncols;
+      consider(nby - dy[t] * jump, nbx - dx[t] * jump);
+    }
+    for (int t = 0; t < nrand && radius > 0; ++t) {
+      const uint32_t r = hash3(seed, (uint32_t)i, (uint32_t)t);
+      const int ox = (int)(r % (2 * radius + 1)) - radius, oy = (int)((r >> 16) % (2 * radius + 1)) - radius;
+      consider(b0y + oy, b0x + ox);
+    }
+    out.idx[i] = best;
+    out.ssd[i] = bs;
+  }
+}
+
+__global__ void fast_final_kernel(int nA, Match m, int* __restrict__ final_idx, float* __restrict__ dist_out) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nA; i += gridDim.x * blockDim.x) {
+    final_idx[i] = m.idx[i];
+    if (dist_out) dist_out[i] = __fsqrt_rn((float)m.ssd[i]);
+  }
+}
+
+int fast_search(annf_handle* h, const uint8_t* img_a, int ha, int wa, const uint8_t* img_b, int hb, int wb, int c,
+                int psize, int K, const int* nat_pos, const int* prop, int n_prop, int iters, uint32_t seed,
+                int* final_idx, float* dist_out, cudaStream_t st) {
+  Img A{img_a, ha, wa, c, psize, wa - psize + 1}, B{img_b, hb, wb, c, psize, wb - psize + 1};
+  const int nA = (ha - psize + 1) * A.ncols;
+  ANNF_ENSURE(h->fast_buf, (size_t)4 * nA * sizeof(int));
+  int* base = h->fast_buf.as<int>();
+  Match m0{base, base + nA}, m1{base + 2 * (size_t)nA, base + 3 * (size_t)nA};
+  const int blocks = (int)std::min<long long>(ceil_div(nA, 256), 32LL * num_sms());
+  fast_init_kernel<<<blocks, 256, 0, st>>>(A, B, nA, K, nat_pos, h->perm.as<int>(), prop, n_prop, m0);
+  ANNF_CHECK_LAUNCH();
+  prof_mark(h, "fast_init", st);
+  for (int it = 0; it < iters; ++it) {
+    const int jump = 1;
+    const int radius = std::max(1, 8 >> it);
+    fast_prop_kernel<<<blocks, 256, 0, st>>>(A, B, nA, jump, radius, 2, seed * 7919u + (uint32_t)it, m0, m1);
+    ANNF_CHECK_LAUNCH();
+    std::swap(m0, m1);
+  }
+  prof_mark(h, "fast_propagate", st);
+  fast_final_kernel<<<blocks, 256, 0, st>>>(nA, m0, final_idx, dist_out);
+  ANNF_CHECK_LAUNCH();
+  return ANNF_OK;
+}
+
+__global__ void fill_u64_kernel(unsigned long long* a, int n, unsigned long long v) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) a[i] = v;
+}
+
+int raw_nn(const uint8_t* img_a, int ha, int wa, const uint8_t* img_b, int hb, int wb, int c, int psize,
+           const int* qpix, int nq, unsigned long long* best, cudaStream_t st) {
+  const int rowlen = psize * c, nw = psize * ((rowlen + 3) / 4);
+  ANNF_REQUIRE(nw <= kRawMaxWords, "raw nearest neighbour: patch too large");
+  Img A{img_a, ha, wa, c, psize, wa - psize + 1}, B{img_b, hb, wb, c, psize, wb - psize + 1};
+  fill_u64_kernel<<<ceil_div(nq, 256), 256, 0, st>>>(best, nq, ~0ull);
+  ANNF_CHECK_LAUNCH();
+  const int qt = ceil_div(nq, kRawQ);
+  const int splits = std::max(1, (8 * num_sms()) / std::max(qt, 1));
+  const dim3 grid(qt, splits);
+  if (nw == 63) raw_nn_kernel<63><<<grid, 256, 0, st>>>(A, B, qpix, nq, splits, best);
+  else if (nw == 42) raw_nn_kernel<42><<<grid, 256, 0, st>>>(A, B, qpix, nq, splits, best);
+  else if (nw == 20) raw_nn_kernel<20><<<grid, 256, 0, st>>>(A, B, qpix, nq, splits, best);
+  else if (nw == 48) raw_nn_kernel<48><<<grid, 256, 0, st>>>(A, B, qpix, nq, splits, best);
+  else raw_nn_kernel<0><<<grid, 256, 0, st>>>(A, B, qpix, nq, splits, best);
+  ANNF_CHECK_LAUNCH();
+  return ANNF_OK;
+}
+
+}  // namespace annf

@@ -57,6 +57,8 @@ struct annf_handle {
       off_lt, off_eq, eqpos;
   // ---- query scratch ----
   annf::DevBuf nat_keys, nat_pos, lists, next_range, part_keys, part_pos;
+  // ---- parallel form scratch ----
+  annf::DevBuf fast_buf, fast_nat;
   // ---- pca scratch ----
   annf::DevBuf gram, colsum, subset_t, cov, eigval, digits, meanproj, solver_ws, solver_info;
   cusolverDnContext* solver = nullptr;

@@ -1288,6 +1288,37 @@ int kneighbors_generic(annf_handle* h, const void* Q, int nq, int K, long long m
                            static_cast<double*>(dist), idx, st);
 }
 
+// natural-leaf top-K (tree positions) of every query, for the parallel form
+template <typename T, int D>
+static int natural_all_typed(annf_handle* h, const T* Q, long long nq, int K, int* out_pos, cudaStream_t st) {
+  TreeView<T> tv = view_of<T>(h);
+  const size_t smem = NodeCache<T>::bytes(h->depth) + 8 * kMaxDynD * sizeof(T);
+  const int blocks = (int)std::min<long long>(ceil_div(nq * 32, 256), 64LL * num_sms());
+  int rc = ANNF_OK;
+  ANNF_DISPATCH_KM(pick_km(K), {
+    cudaError_t e = cudaFuncSetAttribute(natural_knn_kernel<T, D, KM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess) rc = ANNF_ERR_CUDA;
+    natural_knn_kernel<T, D, KM><<<blocks, 256, smem, st>>>(tv, Q, 0, nq, K, out_pos, nullptr);
+  });
+  if (rc != ANNF_OK) {
+    set_error("natural_knn_kernel: cudaFuncSetAttribute failed");
+    return rc;
+  }
+  ANNF_CHECK_LAUNCH();
+  return ANNF_OK;
+}
+
+int natural_knn_all(annf_handle* h, const void* Q, long long nq, int K, int* out_pos, cudaStream_t st) {
+  int rc = ANNF_OK;
+  if (h->real_type == ANNF_REAL_F32) {
+    ANNF_DISPATCH_D(float, h->d, rc = (natural_all_typed<float, D>(h, static_cast<const float*>(Q), nq, K, out_pos, st)));
+  } else {
+    rc = natural_all_typed<double, 0>(h, static_cast<const double*>(Q), nq, K, out_pos, st);
+  }
+  return rc;
+}
+
 // ---------------------------------------------------------------------------------------------
 // Exact kNN that allocates nothing.
 //

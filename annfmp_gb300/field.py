@@ -60,8 +60,19 @@ _SUBSETS = _SubsetCache()
 
 
 class ANNFieldPropKDTreeGB300:
+    FORMS = ("plain", "parallel")
+
     def __init__(self, n_neighbors=3, psize=8, dim_reduced=5, n_subset=1000, leaf_size=64, n_jobs=-1,
-                 propagate=True, select_best_nn=True, float_type="float", verbose=1, seed=0, device=0):
+                 propagate=True, select_best_nn=True, float_type="float", verbose=1, seed=0, device=0,
+                 form="plain", iters=4, proposal=None):
+        """Reference parameters, plus: ``form`` "plain" (the reference's row-sequential method,
+        the drop-in) or "parallel" (natural-leaf candidates + proposals + parallel propagation,
+        every candidate checked by exact raw-patch distance); ``iters`` propagation passes of the
+        parallel form; ``proposal`` an object with ``propose(A, B, psize) -> int32 [n_A, P]`` B
+        indices (e.g. ``annfmp_gb300.proposal.ProposalNet``) feeding the parallel form."""
+        self.form = form
+        self.iters = iters
+        self.proposal = proposal
         self.n_neighbors = n_neighbors
         self.psize = psize
         self.dim_reduced = dim_reduced
@@ -147,14 +158,25 @@ class ANNFieldPropKDTreeGB300:
 
         # (5) rows (annfmp/openmp/base.py:113-125)
         assert self.leaf_size > self.n_neighbors
+        if self.form not in self.FORMS:
+            raise ValueError("form must be one of {}".format(self.FORMS))
         k = int(self.n_neighbors)
         nn = torch.empty(n_a, dtype=torch.int32, device=dev)
-        self.knn_indices_ = torch.empty((n_a, k), dtype=torch.int32, device=dev)
         self.nn_distances_ = torch.empty(n_a, dtype=torch.float32, device=dev)
-        h.call("annf_process_rows_img", ptr(nn), ptr(A), ha, wa, ptr(B), hb, wb, c, p,
-               ptr(self.patches_a_reduced_), self._n_rows, self._n_cols, k, int(bool(self.propagate)),
-               int(bool(self.select_best_nn)), tree._final_max_leaves(), ptr(self.knn_indices_),
-               ptr(self.nn_distances_), st)
+        if self.form == "plain":
+            self.knn_indices_ = torch.empty((n_a, k), dtype=torch.int32, device=dev)
+            h.call("annf_process_rows_img", ptr(nn), ptr(A), ha, wa, ptr(B), hb, wb, c, p,
+                   ptr(self.patches_a_reduced_), self._n_rows, self._n_cols, k, int(bool(self.propagate)),
+                   int(bool(self.select_best_nn)), tree._final_max_leaves(), ptr(self.knn_indices_),
+                   ptr(self.nn_distances_), st)
+        else:
+            prop = None
+            if self.proposal is not None:
+                prop = self.proposal.propose(A, B, p)
+            n_prop = 0 if prop is None else int(prop.shape[1])
+            h.call("annf_parallel_nnf", ptr(nn), ptr(A), ha, wa, ptr(B), hb, wb, c, p,
+                   ptr(self.patches_a_reduced_), k, ptr(prop), n_prop, int(self.iters), int(self.seed) & 0xFFFFFFFF,
+                   ptr(self.nn_distances_), st)
         ev["t4"].record()
         tree.check_device()  # synchronises and raises if a kernel's bounds check tripped
         self._timers = collections.OrderedDict()

@@ -135,6 +135,24 @@ int annf_project(annf_handle* h, const uint8_t* img, int hgt, int wid, int chann
                  const double* components, const double* mean, int n_components, int real_type,
                  void* out, void* stream);
 
+/* The parallel NNF form (an addition beside the reference's row-sequential method, which has no
+ * counterpart for it): every pixel's natural-leaf k-list, optional offset proposals
+ * (proposals [n_rows*n_cols*n_prop] B patch indices, -1 = none) and `iters` parallel passes of
+ * neighbour propagation and random search; every candidate is verified with the exact integer
+ * raw-patch SSD. Requires the tree over image B's reduced patches (annf_build_tree). Outputs the
+ * chosen B index per pixel and, optionally, its raw-patch L2 distance. */
+int annf_parallel_nnf(annf_handle* h, int* final_idx, const uint8_t* img_a, int ha, int wa,
+                      const uint8_t* img_b, int hb, int wb, int channels, int psize, const void* ared,
+                      int k, const int* proposals, int n_prop, int iters, unsigned seed, float* dist_out,
+                      void* stream);
+
+/* Exact raw-patch nearest neighbour (integer SSD over all B patches) of nq sampled A pixels
+ * (query_pixels: row-major patch indices). best[i] = ssd << 32 | B index (smallest index on
+ * ties). The reference for distance-error measurements; the reference project has no counterpart. */
+int annf_raw_nn(annf_handle* h, const uint8_t* img_a, int ha, int wa, const uint8_t* img_b, int hb,
+                int wb, int channels, int psize, const int* query_pixels, int nq,
+                unsigned long long* best, void* stream);
+
 /* Synchronise the stream and report (and clear) the kernels' bounds-check status bits. */
 int annf_device_status(annf_handle* h, void* stream, unsigned* bits_out);
 
