@@ -1,7 +1,7 @@
 """Benchmark: query patches/s of the NNF hot path on one GB300 (or N replicas).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
-                    [--workload large|small] [--form plain]
+                    [--workload large|medium|small] [--form plain|parallel] [--iters N]
 
 A step is one full NNF of one image pair, from device-resident uint8 images to the device-resident
 NNF: PCA fit (sampled subset, exact Gram, FP64 eigh), projection of every A and B patch, k-d tree
@@ -112,14 +112,18 @@ class ClockSampler:
 # ---------------------------------------------------------------------------------------------
 # algorithmic bytes per launch of each stage ("roofline")
 # ---------------------------------------------------------------------------------------------
-def stage_bytes(stage, w, n_a, n_b, depth, n_cols):
+def stage_bytes(stage, w, n_a, n_b, depth, n_cols, it=1):
     d, k, P = w["dim_reduced"], w["n_neighbors"], w["psize"] ** 2 * 3
     ppl = n_b / float(1 << depth)
     rows_q = n_a - n_cols
     if stage == "chain":  # per query: query + k propagated leaves + leaf spans + natural list + k-list out
         return rows_q * (4 * d + k * ppl * 4 * d + 8 * k + 12 * k + 4 * k)
     if stage == "natural_knn":  # query + node path + natural leaf + list out
-        return rows_q * (4 * d + 8 * depth + ppl * 4 * d + 12 * k)
+        return n_a * (4 * d + 8 * depth + ppl * 4 * d + 4 * k)
+    if stage == "fast_init":  # k candidate positions + A patch + k B patches + match out
+        return n_a * (4 * k + (k + 1) * P + 8)
+    if stage == "fast_propagate":  # per pass: match in/out, 4 neighbour matches, A patch, 6 B patches
+        return n_a * (8 + 16 + 7 * P + 8) * max(it, 1)
     if stage == "select_best":  # k A/B patch pairs + list in + index/distance out
         return n_a * (k * 2 * P + 4 * k + 8)
     if stage == "first_row":  # every point once per 128-query tile
@@ -213,7 +217,8 @@ def config_of(w, args):
     prm = params_of(w)
     return {"workload": f"{w['size']}x{w['size']}x3 {w['kind']} pair seed {w['seed']}, patch {w['psize']}x"
                         f"{w['psize']}x3, PCA {w['dim_reduced']}, leaf {w['leaf_size']}, k {w['n_neighbors']}",
-            "form": args.form, "n_subset": prm["n_subset"], "pairs_per_rank": 1,
+            "form": args.form, "iters": args.iters if args.form != "plain" else None,
+            "n_subset": prm["n_subset"], "pairs_per_rank": 1,
             "l2": "flushed between timed steps (256 MB write)", "parallelism": f"replicas x{args.gpus}"}
 
 
@@ -236,7 +241,7 @@ def run_gpu(args, w, rank, world, local_rank):
     A = torch.from_numpy(a).to(dev)
     B = torch.from_numpy(b).to(dev)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
-    model = ANNFieldPropKDTreeGB300(verbose=0, device=local_rank, **prm)
+    model = ANNFieldPropKDTreeGB300(verbose=0, device=local_rank, form=args.form, iters=args.iters, **prm)
 
     for _ in range(args.warmup):
         model.fit(A, B)
@@ -255,7 +260,7 @@ def run_gpu(args, w, rank, world, local_rank):
         for i in range(args.steps):
             flush.fill_(float(i))
             ev[i][0].record()
-            model.fit(A, B)
+            nn_dev = model.fit(A, B)
             ev[i][1].record()
             for name, ms in h.profile_read(torch.cuda.current_stream(dev).cuda_stream):
                 stages.setdefault(name, []).append(ms)
@@ -293,8 +298,12 @@ def run_gpu(args, w, rank, world, local_rank):
     kernel_stages = {k: v for k, v in stage_ms.items() if not k.endswith(":begin")}
     depth = model.kdtree.final_tree_depth_
     peak, peak_kind = load_peaks()
-    dom = max((k for k in kernel_stages if stage_bytes(k, w, n_a, n_b, depth, n_cols)), key=lambda k: kernel_stages[k])
-    by = stage_bytes(dom, w, n_a, n_b, depth, n_cols)
+    sb = lambda k: stage_bytes(k, w, n_a, n_b, depth, n_cols, args.iters)  # noqa: E731
+    dom = max((k for k in kernel_stages if sb(k)), key=lambda k: kernel_stages[k])
+    by = sb(dom)
+    # distance error of the last timed NNF against the exact raw-patch nearest neighbour
+    from annfmp_gb300 import metrics
+    quality = metrics.distance_ratio_error(a, b, nn_dev, p, n_samples=4096, seed=w["seed"] + 7, device=local_rank)
     achieved = by / (kernel_stages[dom] / 1e3) / 1e9
     traffic = load_traffic().get(f"{args.workload}:{args.form}:{dom}")
     value = world * n_a / (ms / 1e3)
@@ -308,6 +317,7 @@ def run_gpu(args, w, rank, world, local_rank):
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_kind": peak_kind, "algorithmic_bytes": by,
                      "traffic": traffic},
+        "distance_error": quality,
         "stages_ms": stage_ms, "wall_ms_per_step": t_wall * 1e3 / args.steps,
         "clocks": clocks.summary(),
     }
@@ -326,7 +336,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="large", choices=sorted(WORKLOADS))
-    ap.add_argument("--form", default="plain", choices=["plain"])
+    ap.add_argument("--form", default="plain", choices=["plain", "parallel"])
+    ap.add_argument("--iters", type=int, default=4, help="propagation passes of the parallel form")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 0)
