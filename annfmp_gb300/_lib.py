@@ -25,6 +25,9 @@ ANNF_REAL_F32 = 0
 ANNF_REAL_F64 = 1
 ANNF_SPLIT_CYCLIC = 0
 ANNF_SPLIT_LONGEST = 1
+ANNF_LEAF_EXACT = 0
+ANNF_LEAF_BF16 = 1
+ANNF_LEAF_FP16 = 2
 
 
 class AnnfError(RuntimeError):
@@ -67,9 +70,23 @@ SIGNATURES = {
     "annf_process_rows_img": (_i, [_vp, _vp, _vp, _i, _i, _vp, _i, _i, _i, _i, _vp, _i, _i, _i, _i, _i, _ll,
                                    _vp, _vp, _vp]),
     "annf_pca_fit": (_i, [_vp, _vp, _i, _i, _vp, _i, _vp, _i, _i, _vp, _i, _i, _i, _i, _vp, _vp, _vp]),
+    "annf_pca_fit_subspace": (_i, [_vp, _vp, _i, _i, _vp, _i, _vp, _i, _i, _vp, _i, _i, _i, _i, _i, _vp, _vp, _vp]),
     "annf_project": (_i, [_vp, _vp, _i, _i, _i, _i, _vp, _vp, _i, _i, _vp, _vp]),
     "annf_device_status": (_i, [_vp, _vp, ctypes.POINTER(_u)]),
-    "annf_parallel_nnf": (_i, [_vp, _vp, _vp, _i, _i, _vp, _i, _i, _i, _i, _vp, _i, _vp, _i, _i, _u, _vp, _vp]),
+    "annf_parallel_nnf": (_i, [_vp, _vp, _vp, _i, _i, _vp, _i, _i, _i, _i, _vp, _i, _vp, _i, _i, _u, _i, _vp, _vp]),
+    "annf_tc_tile": (_i, [_vp, _vp, _vp, _i, _i, _vp, _vp]),
+    "annf_natural_knn": (_i, [_vp, _vp, ctypes.c_longlong, _i, _i, _vp, _vp]),
+    "annf_project_bf16": (_i, [_vp, _vp, _i, _i, _i, _i, _vp, _vp, _i, _vp, _vp]),
+    "annf_cnn_input": (_i, [_vp, _vp, _vp, _i, _i, _vp, _vp]),
+    "annf_cnn_prep_weights": (_i, [_vp, _vp, _i, _i, _vp, _vp, _vp]),
+    "annf_cnn_conv_forward": (_i, [_vp, _vp, _i, _i, _i, _i, _i, _vp, _vp, _i, _vp, _vp]),
+    "annf_cnn_conv_backward_data": (_i, [_vp, _vp, _vp, _i, _i, _i, _i, _i, _vp, _vp, _vp]),
+    "annf_cnn_conv_backward_weights": (_i, [_vp, _vp, _vp, _vp, _i, _i, _i, _i, _i, _vp, _vp, _vp]),
+    "annf_cnn_wta_loss": (_i, [_vp, _vp, _vp, _vp, ctypes.c_longlong, ctypes.c_float, _vp, _vp, _vp]),
+    "annf_cnn_adam": (_i, [_vp, _vp, _vp, _vp, _vp, _i, ctypes.c_float, ctypes.c_float, ctypes.c_float,
+                           ctypes.c_float, _i, _vp]),
+    "annf_cnn_targets": (_i, [_vp, _vp, _i, _i, _i, _i, _vp, _vp, _vp]),
+    "annf_cnn_proposals": (_i, [_vp, _vp, _i, _i, _i, _i, _i, _i, _i, _vp, _vp]),
     "annf_raw_nn": (_i, [_vp, _vp, _i, _i, _vp, _i, _i, _i, _i, _vp, _i, _vp, _vp]),
     "annf_profile_enable": (_i, [_vp, _i]),
     "annf_profile_read": (_i, [_vp, _vp, _i, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_char_p)]),

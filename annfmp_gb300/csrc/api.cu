@@ -29,11 +29,32 @@ int natural_knn_all(annf_handle* h, const void* Q, long long nq, int K, int* out
 int fast_search(annf_handle* h, const uint8_t* img_a, int ha, int wa, const uint8_t* img_b, int hb, int wb, int c,
                 int psize, int K, const int* nat_pos, const int* prop, int n_prop, int iters, uint32_t seed,
                 int* final_idx, float* dist_out, cudaStream_t st);
+bool leaf_tc_supported(const annf_handle* h, int K);
+int natural_knn_tc(annf_handle* h, const float* Q, long long nq, int K, int prec, int* out_pos, cudaStream_t st);
+int tc_tile(const uint16_t* A, const uint16_t* B, int N, int K, float* D, unsigned* status, cudaStream_t st);
+int cnn_input(const uint8_t* A, const uint8_t* B, int H, int W, void* X, cudaStream_t st);
+int cnn_prep_weights(const float* W, int co, int ci, float* wf, float* wb, cudaStream_t st);
+int cnn_conv_forward(const void* X, int nimg, int h, int w, int ci, int co, const float* wf, const float* bias,
+                     int relu, void* Y, unsigned* status, cudaStream_t st);
+int cnn_conv_backward_data(const float* G, const void* mask, int nimg, int h, int w, int co, int ci, const float* wb,
+                           float* dX, unsigned* status, cudaStream_t st);
+int cnn_conv_backward_weights(const void* X, const float* G, const void* mask, int nimg, int h, int w, int ci, int co,
+                              float* dW, float* db, unsigned* status, cudaStream_t st);
+int cnn_wta_loss(const float* out, const float* tgt, const uint8_t* valid, long long npix, float inv_nv, float* dout,
+                 float* loss_sum, cudaStream_t st);
+int cnn_adam(float* p, const float* g, float* m, float* v, int n, float lr, float b1, float b2, float eps, int step,
+             cudaStream_t st);
+int cnn_targets(const int* nnf, int H, int W, int Wb, int psize, float* tgt, uint8_t* valid, cudaStream_t st);
+int cnn_proposals(const float* out, int h4, int w4, int H, int W, int Hb, int Wb, int psize, int* props,
+                  cudaStream_t st);
+bool project_tc_supported(int psize, int c, int ncomp);
+int project_tc(annf_handle* h, const uint8_t* img, int H, int W, int c, int psize, const double* comps,
+               const double* mean, int ncomp, float* out, cudaStream_t st);
 int raw_nn(const uint8_t* img_a, int ha, int wa, const uint8_t* img_b, int hb, int wb, int c, int psize,
            const int* qpix, int nq, unsigned long long* best, cudaStream_t st);
 int pca_fit(annf_handle* h, const uint8_t* img_a, int ha, int wa, const int* pos_a, int n_a, const uint8_t* img_b,
             int hb, int wb, const int* pos_b, int n_b, int c, int psize, int ncomp, double* comps, double* mean,
-            cudaStream_t st);
+            int solver, cudaStream_t st);
 int project(annf_handle* h, const uint8_t* img, int H, int W, int c, int psize, const double* comps,
             const double* mean, int ncomp, int real_type, void* out, cudaStream_t st);
 
@@ -98,8 +119,8 @@ void annf_destroy(annf_handle* h) {
                     &h->point_leaf, &h->leaf_box, &h->bmin, &h->bmax, &h->axis, &h->keys, &h->hist, &h->sel_prefix,
                     &h->sel_rank, &h->sel_nlt, &h->sel_neq, &h->blk_lt, &h->blk_eq, &h->off_lt, &h->off_eq,
                     &h->eqpos, &h->nat_keys, &h->nat_pos, &h->lists, &h->next_range, &h->part_keys,
-                    &h->part_pos, &h->fast_buf, &h->fast_nat, &h->gram, &h->colsum, &h->subset_t, &h->cov, &h->eigval, &h->digits,
-                    &h->meanproj, &h->solver_ws, &h->solver_info, &h->status};
+                    &h->part_pos, &h->fast_buf, &h->fast_nat, &h->tc_buf, &h->pj_buf, &h->gram, &h->colsum, &h->subset_t, &h->cov, &h->eigval, &h->digits,
+                    &h->meanproj, &h->solver_ws, &h->solver_info, &h->eig_ws, &h->status};
   for (DevBuf* b : bufs) b->release();
   for (int i = 0; i < annf_handle::kMaxMarks; ++i)
     if (h->prof_ev[i]) cudaEventDestroy(h->prof_ev[i]);
@@ -221,7 +242,21 @@ int annf_pca_fit(annf_handle* h, const uint8_t* img_a, int ha, int wa, const int
   ANNF_REQUIRE(n_a >= 0 && n_b >= 0 && channels >= 1 && psize >= 1, "annf_pca_fit: bad sizes");
   ANNF_REQUIRE(psize <= ha && psize <= wa && psize <= hb && psize <= wb, "annf_pca_fit: patch larger than image");
   return pca_fit(h, img_a, ha, wa, pos_a, n_a, img_b, hb, wb, pos_b, n_b, channels, psize, n_components,
-                 components_out, mean_out, static_cast<cudaStream_t>(stream));
+                 components_out, mean_out, 0, static_cast<cudaStream_t>(stream));
+}
+
+int annf_pca_fit_subspace(annf_handle* h, const uint8_t* img_a, int ha, int wa, const int* pos_a, int n_a,
+                          const uint8_t* img_b, int hb, int wb, const int* pos_b, int n_b, int channels, int psize,
+                          int n_components, int iters, double* components_out, double* mean_out, void* stream) {
+  ANNF_API_HANDLE(h);
+  ANNF_REQUIRE(img_a && img_b && components_out && mean_out, "annf_pca_fit_subspace: NULL argument");
+  ANNF_REQUIRE((n_a == 0 || pos_a) && (n_b == 0 || pos_b), "annf_pca_fit_subspace: NULL positions");
+  ANNF_REQUIRE(n_a >= 0 && n_b >= 0 && channels >= 1 && psize >= 1, "annf_pca_fit_subspace: bad sizes");
+  ANNF_REQUIRE(psize <= ha && psize <= wa && psize <= hb && psize <= wb,
+               "annf_pca_fit_subspace: patch larger than image");
+  ANNF_REQUIRE(iters >= 1 && iters <= 100, "annf_pca_fit_subspace: iters out of range");
+  return pca_fit(h, img_a, ha, wa, pos_a, n_a, img_b, hb, wb, pos_b, n_b, channels, psize, n_components,
+                 components_out, mean_out, iters, static_cast<cudaStream_t>(stream));
 }
 
 int annf_project(annf_handle* h, const uint8_t* img, int hgt, int wid, int channels, int psize,
@@ -263,7 +298,7 @@ int annf_kneighbors_noalloc(annf_handle* h, const void* queries, int nq, int k, 
 
 int annf_parallel_nnf(annf_handle* h, int* final_idx, const uint8_t* img_a, int ha, int wa, const uint8_t* img_b,
                       int hb, int wb, int channels, int psize, const void* ared, int k, const int* proposals,
-                      int n_prop, int iters, unsigned seed, float* dist_out, void* stream) {
+                      int n_prop, int iters, unsigned seed, int leaf_precision, float* dist_out, void* stream) {
   ANNF_API_HANDLE(h);
   int rc = check_k(h, k, 2147483640);
   if (rc != ANNF_OK) return rc;
@@ -277,8 +312,17 @@ int annf_parallel_nnf(annf_handle* h, int* final_idx, const uint8_t* img_a, int 
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   const long long nA = (long long)(ha - psize + 1) * (wa - psize + 1);
   ANNF_ENSURE(h->fast_nat, (size_t)nA * k * sizeof(int));
+  ANNF_REQUIRE(leaf_precision == ANNF_LEAF_EXACT || leaf_precision == ANNF_LEAF_BF16 ||
+                   leaf_precision == ANNF_LEAF_FP16,
+               "annf_parallel_nnf: bad leaf_precision");
+  ANNF_REQUIRE(leaf_precision == ANNF_LEAF_EXACT || leaf_tc_supported(h, k),
+               "annf_parallel_nnf: tensor-core leaf distances need FP32 points, d <= 32, leaves <= 256, k <= 32");
   prof_mark(h, "parallel:begin", st);
-  rc = natural_knn_all(h, ared, nA, k, h->fast_nat.as<int>(), st);
+  if (leaf_precision != ANNF_LEAF_EXACT)
+    rc = natural_knn_tc(h, static_cast<const float*>(ared), nA, k, leaf_precision == ANNF_LEAF_FP16 ? 1 : 0,
+                        h->fast_nat.as<int>(), st);
+  else
+    rc = natural_knn_all(h, ared, nA, k, h->fast_nat.as<int>(), st);
   if (rc != ANNF_OK) return rc;
   prof_mark(h, "natural_knn", st);
   return fast_search(h, img_a, ha, wa, img_b, hb, wb, channels, psize, k, h->fast_nat.as<int>(), proposals, n_prop,
@@ -294,6 +338,121 @@ int annf_raw_nn(annf_handle* h, const uint8_t* img_a, int ha, int wa, const uint
   if (nq == 0) return ANNF_OK;
   return raw_nn(img_a, ha, wa, img_b, hb, wb, channels, psize, query_pixels, nq, best,
                 static_cast<cudaStream_t>(stream));
+}
+
+int annf_project_bf16(annf_handle* h, const uint8_t* img, int hgt, int wid, int channels, int psize,
+                      const double* components, const double* mean, int n_components, float* out, void* stream) {
+  ANNF_API_HANDLE(h);
+  ANNF_REQUIRE(img && components && mean && out, "annf_project_bf16: NULL argument");
+  ANNF_REQUIRE(channels >= 1 && psize >= 1 && psize <= hgt && psize <= wid, "annf_project_bf16: bad geometry");
+  if (!project_tc_supported(psize, channels, n_components)) {
+    set_error("annf_project_bf16: needs psize*psize*channels <= 256 and n_components <= 32");
+    return ANNF_ERR_UNSUPPORTED;
+  }
+  return project_tc(h, img, hgt, wid, channels, psize, components, mean, n_components, out,
+                    static_cast<cudaStream_t>(stream));
+}
+
+int annf_natural_knn(annf_handle* h, const void* queries, long long nq, int k, int leaf_precision, int* out_pos,
+                     void* stream) {
+  ANNF_API_HANDLE(h);
+  int rc = check_k(h, k, 2147483640);
+  if (rc != ANNF_OK) return rc;
+  ANNF_REQUIRE(nq >= 0, "annf_natural_knn: nq < 0");
+  if (nq == 0) return ANNF_OK;
+  ANNF_REQUIRE(queries && out_pos, "annf_natural_knn: NULL argument");
+  ANNF_REQUIRE(leaf_precision == ANNF_LEAF_EXACT || leaf_precision == ANNF_LEAF_BF16 ||
+                   leaf_precision == ANNF_LEAF_FP16,
+               "annf_natural_knn: bad leaf_precision");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (leaf_precision != ANNF_LEAF_EXACT) {
+    ANNF_REQUIRE(leaf_tc_supported(h, k), "annf_natural_knn: tensor-core leaf distances need FP32 points, "
+                                          "d <= 32, leaves <= 256, k <= 32");
+    return natural_knn_tc(h, static_cast<const float*>(queries), nq, k, leaf_precision == ANNF_LEAF_FP16 ? 1 : 0,
+                          out_pos, st);
+  }
+  return natural_knn_all(h, queries, nq, k, out_pos, st);
+}
+
+int annf_tc_tile(annf_handle* h, const uint16_t* a, const uint16_t* b, int n, int kdim, float* d, void* stream) {
+  ANNF_API_HANDLE(h);
+  ANNF_REQUIRE(a && b && d, "annf_tc_tile: NULL argument");
+  return tc_tile(a, b, n, kdim, d, h->status.as<unsigned>(), static_cast<cudaStream_t>(stream));
+}
+
+// ---- offset-proposal network ----
+#define ANNF_CNN_DIMS(nimg, h, w) \
+  ANNF_REQUIRE((nimg) >= 1 && (h) >= 1 && (w) >= 1, "annf_cnn: bad tensor shape")
+
+int annf_cnn_input(annf_handle* h, const uint8_t* img_a, const uint8_t* img_b, int hgt, int wid, void* x_out,
+                   void* stream) {
+  ANNF_API_HANDLE(h);
+  ANNF_REQUIRE(img_a && img_b && x_out, "annf_cnn_input: NULL argument");
+  return cnn_input(img_a, img_b, hgt, wid, x_out, static_cast<cudaStream_t>(stream));
+}
+
+int annf_cnn_prep_weights(annf_handle* h, const float* w, int co, int ci, float* w_fwd, float* w_bwd, void* stream) {
+  ANNF_API_HANDLE(h);
+  ANNF_REQUIRE(w && w_fwd && co >= 1 && ci >= 1, "annf_cnn_prep_weights: bad argument");
+  return cnn_prep_weights(w, co, ci, w_fwd, w_bwd, static_cast<cudaStream_t>(stream));
+}
+
+int annf_cnn_conv_forward(annf_handle* h, const void* x, int nimg, int hgt, int wid, int ci, int co,
+                          const float* w_fwd, const float* bias, int relu, void* y, void* stream) {
+  ANNF_API_HANDLE(h);
+  ANNF_REQUIRE(x && w_fwd && bias && y, "annf_cnn_conv_forward: NULL argument");
+  ANNF_CNN_DIMS(nimg, hgt, wid);
+  return cnn_conv_forward(x, nimg, hgt, wid, ci, co, w_fwd, bias, relu, y, h->status.as<unsigned>(),
+                          static_cast<cudaStream_t>(stream));
+}
+
+int annf_cnn_conv_backward_data(annf_handle* h, const float* g, const void* mask, int nimg, int hgt, int wid, int co,
+                                int ci, const float* w_bwd, float* dx, void* stream) {
+  ANNF_API_HANDLE(h);
+  ANNF_REQUIRE(g && w_bwd && dx, "annf_cnn_conv_backward_data: NULL argument");
+  ANNF_CNN_DIMS(nimg, hgt, wid);
+  return cnn_conv_backward_data(g, mask, nimg, hgt, wid, co, ci, w_bwd, dx, h->status.as<unsigned>(),
+                                static_cast<cudaStream_t>(stream));
+}
+
+int annf_cnn_conv_backward_weights(annf_handle* h, const void* x, const float* g, const void* mask, int nimg, int hgt,
+                                   int wid, int ci, int co, float* dw, float* db, void* stream) {
+  ANNF_API_HANDLE(h);
+  ANNF_REQUIRE(x && g && dw && db, "annf_cnn_conv_backward_weights: NULL argument");
+  ANNF_CNN_DIMS(nimg, hgt, wid);
+  return cnn_conv_backward_weights(x, g, mask, nimg, hgt, wid, ci, co, dw, db, h->status.as<unsigned>(),
+                                   static_cast<cudaStream_t>(stream));
+}
+
+int annf_cnn_wta_loss(annf_handle* h, const float* out, const float* tgt, const uint8_t* valid, long long npix,
+                      float inv_nvalid, float* dout, float* loss_sum, void* stream) {
+  ANNF_API_HANDLE(h);
+  ANNF_REQUIRE(out && tgt && valid && dout && loss_sum && npix >= 0, "annf_cnn_wta_loss: bad argument");
+  return cnn_wta_loss(out, tgt, valid, npix, inv_nvalid, dout, loss_sum, static_cast<cudaStream_t>(stream));
+}
+
+int annf_cnn_adam(annf_handle* h, float* param, const float* grad, float* m, float* v, int n, float lr, float beta1,
+                  float beta2, float eps, int step, void* stream) {
+  ANNF_API_HANDLE(h);
+  ANNF_REQUIRE(param && grad && m && v && n >= 0 && step >= 1, "annf_cnn_adam: bad argument");
+  return cnn_adam(param, grad, m, v, n, lr, beta1, beta2, eps, step, static_cast<cudaStream_t>(stream));
+}
+
+int annf_cnn_targets(annf_handle* h, const int* nnf, int ha, int wa, int wb, int psize, float* tgt, uint8_t* valid,
+                     void* stream) {
+  ANNF_API_HANDLE(h);
+  ANNF_REQUIRE(nnf && tgt && valid && psize >= 1 && psize <= ha && psize <= wa && ha >= 4 && wa >= 4,
+               "annf_cnn_targets: bad argument");
+  return cnn_targets(nnf, ha, wa, wb, psize, tgt, valid, static_cast<cudaStream_t>(stream));
+}
+
+int annf_cnn_proposals(annf_handle* h, const float* out, int h4, int w4, int ha, int wa, int hb, int wb, int psize,
+                       int* props, void* stream) {
+  ANNF_API_HANDLE(h);
+  ANNF_REQUIRE(out && props && h4 >= 1 && w4 >= 1 && psize >= 1 && psize <= ha && psize <= wa && psize <= hb &&
+                   psize <= wb,
+               "annf_cnn_proposals: bad argument");
+  return cnn_proposals(out, h4, w4, ha, wa, hb, wb, psize, props, static_cast<cudaStream_t>(stream));
 }
 
 long long annf_launch_count(void) { return g_launches.load(std::memory_order_relaxed); }

@@ -1,0 +1,471 @@
+// cnn.cu -- the offset-proposal network: input, 3x3 convolutions (forward, backward-data,
+// backward-weights), relaxed winner-takes-all truncated L1 loss, Adam, training targets and inference
+// proposals (sm_103a).
+//
+// Network (an addition of this project; the reference's only propagation candidates are the row
+// above, annfmp/openmp/kdtree/src/base.c:255-282): the pair at 1/4 resolution (4x4 box mean of A
+// and of B, (v - 127.5) / 64, 6 channels + 2 zero) through six 3x3 convolutions (8->32, 32->32 x4,
+// 32->8), zero padding, bias, ReLU after the first five. Activations are stored NHWC in BF16,
+// weights are used BF16-rounded, every sum is FP32. The 8 outputs of a low-resolution pixel are 4
+// hypotheses (dx, dy) in units of 16 full-resolution pixels.
+//
+// One generic convolution kernel serves the forward pass and the input gradient:
+//   out[n][p][o] = sum_tap sum_i in[n][p + d(tap)][i] * Wg[tap][i][o]  (+ bias, ReLU)
+// with Wg[tap][ci][co] = W[co][tap][ci] forward and Wg[tap][co][ci] = W[co][8 - tap][ci] for the
+// input gradient (correlation with the flipped kernel). A 16x16 output tile per CTA: the 18x18 input
+// halo sits channel-major in shared memory (row stride 325 floats: conflict-free), the weights as
+// FP32 [9][I][O]; each of 128 threads computes two pixels x O outputs.
+#include <cuda_bf16.h>
+
+#include <algorithm>
+
+#include "common.cuh"
+#include "handle.cuh"
+
+namespace annf {
+
+int num_sms();
+
+constexpr int kCT = 16;             // output tile side
+constexpr int kCH = kCT + 2;        // halo tile side
+constexpr int kCS = kCH * kCH + 1;  // channel stride of the halo tile in shared memory
+constexpr float kOutScale = 16.0f;
+constexpr float kWtaEps = 0.05f;
+constexpr float kWtaTrunc = 40.0f;  // px: a hypothesis farther than this from the target gets no gradient
+
+__device__ __forceinline__ float ld_act(const __nv_bfloat16* p) { return __bfloat162float(*p); }
+__device__ __forceinline__ float ld_act(const float* p) { return *p; }
+
+// ---------------------------------------------------------------------------------------------
+// input: X[h4][w4][8] = ((4x4 mean of A.rgb, B.rgb) - 127.5) / 64, 0, 0
+// ---------------------------------------------------------------------------------------------
+__global__ void cnn_input_kernel(const uint8_t* __restrict__ A, const uint8_t* __restrict__ B, int H, int W, int h4,
+                                 int w4, __nv_bfloat16* __restrict__ X) {
+  const int n = h4 * w4;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int y = i / w4, x = i - y * w4;
+    float v[8];
+#pragma unroll
+    for (int s = 0; s < 2; ++s) {
+      const uint8_t* img = s ? B : A;
+      int acc[3] = {0, 0, 0};
+      for (int u = 0; u < 4; ++u) {
+        const uint8_t* row = img + ((size_t)(4 * y + u) * W + 4 * x) * 3;
+#pragma unroll
+        for (int t = 0; t < 12; ++t) acc[t % 3] += row[t];
+      }
+#pragma unroll
+      for (int c = 0; c < 3; ++c) v[3 * s + c] = ((float)acc[c] * 0.0625f - 127.5f) * 0.015625f;
+    }
+    v[6] = v[7] = 0.f;
+    __nv_bfloat16* o = X + (size_t)i * 8;
+#pragma unroll
+    for (int c = 0; c < 8; ++c) o[c] = __float2bfloat16_rn(v[c]);
+  }
+  (void)H;
+}
+
+// ---------------------------------------------------------------------------------------------
+// weights: master FP32 W[co][9][ci] -> Wg forward [9][ci][co] and input-gradient [9][co][ci],
+// both BF16-rounded (kept FP32)
+// ---------------------------------------------------------------------------------------------
+__global__ void cnn_prep_weights_kernel(const float* __restrict__ W, int co_n, int ci_n, float* __restrict__ wf,
+                                        float* __restrict__ wb) {
+  const int n = co_n * 9 * ci_n;
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
+    const int co = e / (9 * ci_n), r = e - co * 9 * ci_n, tap = r / ci_n, ci = r - tap * ci_n;
+    const float w = __bfloat162float(__float2bfloat16_rn(W[e]));
+    wf[((size_t)tap * ci_n + ci) * co_n + co] = w;
+    if (wb) wb[((size_t)(8 - tap) * co_n + co) * ci_n + ci] = w;
+  }
+}
+
+// ---------------------------------------------------------------------------------------------
+// generic 3x3 convolution (see the file comment). MODE 0: bias + ReLU, BF16 out; MODE 1: bias,
+// FP32 out; MODE 2: no bias, FP32 out (input gradient). MASK: input multiplied by (mask > 0).
+// ---------------------------------------------------------------------------------------------
+template <int CI, int CO, typename TIN, bool MASK, int MODE>
+__global__ void __launch_bounds__(128) cnn_conv_kernel(const TIN* __restrict__ in, const __nv_bfloat16* __restrict__ mask,
+                                                       int h, int w, const float* __restrict__ wg,
+                                                       const float* __restrict__ bias, void* __restrict__ out,
+                                                       unsigned* status) {
+  extern __shared__ __align__(16) float csm[];
+  float* xs = csm;                   // [CI][kCS]
+  float* ws = csm + CI * kCS;        // [9][CI][CO]
+  ws = reinterpret_cast<float*>(((uintptr_t)ws + 15) & ~uintptr_t(15));
+  if (smem_overrun(csm, ws + 9 * CI * CO, status)) return;
+  const int n = blockIdx.z, y0 = blockIdx.y * kCT, x0 = blockIdx.x * kCT;
+  const size_t img = (size_t)n * h * w;
+  for (int e = threadIdx.x; e < kCH * kCH * CI; e += blockDim.x) {
+    const int q = e / CI, c = e - q * CI;
+    const int qy = q / kCH, qx = q - qy * kCH;
+    const int y = y0 + qy - 1, x = x0 + qx - 1;
+    float v = 0.f;
+    if (y >= 0 && y < h && x >= 0 && x < w) {
+      const size_t off = (img + (size_t)y * w + x) * CI + c;
+      v = ld_act(in + off);
+      if (MASK && !(__bfloat162float(mask[off]) > 0.f)) v = 0.f;
+    }
+    xs[c * kCS + q] = v;
+  }
+  for (int e = threadIdx.x; e < 9 * CI * CO; e += blockDim.x) ws[e] = wg[e];
+  __syncthreads();
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;  // pixels (ty, tx) and (ty + 8, tx)
+  float a0[CO], a1[CO];
+#pragma unroll
+  for (int o = 0; o < CO; ++o) {
+    const float b = (MODE == 2) ? 0.f : bias[o];
+    a0[o] = b;
+    a1[o] = b;
+  }
+#pragma unroll 1
+  for (int tap = 0; tap < 9; ++tap) {
+    const int ky = tap / 3, kx = tap - ky * 3;
+    const float* i0 = xs + (ty + ky) * kCH + tx + kx;
+    const float* wt = ws + tap * CI * CO;
+#pragma unroll 4
+    for (int c = 0; c < CI; ++c) {
+      const float x0v = i0[c * kCS], x1v = i0[c * kCS + 8 * kCH];
+      const float4* w4 = reinterpret_cast<const float4*>(wt + c * CO);
+#pragma unroll
+      for (int o4 = 0; o4 < CO / 4; ++o4) {
+        const float4 wv = w4[o4];
+        a0[4 * o4 + 0] = fmaf(x0v, wv.x, a0[4 * o4 + 0]);
+        a0[4 * o4 + 1] = fmaf(x0v, wv.y, a0[4 * o4 + 1]);
+        a0[4 * o4 + 2] = fmaf(x0v, wv.z, a0[4 * o4 + 2]);
+        a0[4 * o4 + 3] = fmaf(x0v, wv.w, a0[4 * o4 + 3]);
+        a1[4 * o4 + 0] = fmaf(x1v, wv.x, a1[4 * o4 + 0]);
+        a1[4 * o4 + 1] = fmaf(x1v, wv.y, a1[4 * o4 + 1]);
+        a1[4 * o4 + 2] = fmaf(x1v, wv.z, a1[4 * o4 + 2]);
+        a1[4 * o4 + 3] = fmaf(x1v, wv.w, a1[4 * o4 + 3]);
+      }
+    }
+  }
+#pragma unroll
+  for (int r = 0; r < 2; ++r) {
+    const int y = y0 + ty + 8 * r, x = x0 + tx;
+    if (y >= h || x >= w) continue;
+    const float* a = r ? a1 : a0;
+    const size_t off = (img + (size_t)y * w + x) * CO;
+    if (MODE == 0) {
+      __nv_bfloat16* o = static_cast<__nv_bfloat16*>(out) + off;
+#pragma unroll
+      for (int c = 0; c < CO; c += 2)
+        *reinterpret_cast<__nv_bfloat162*>(o + c) = __floats2bfloat162_rn(fmaxf(a[c], 0.f), fmaxf(a[c + 1], 0.f));
+    } else {
+      float* o = static_cast<float*>(out) + off;
+#pragma unroll
+      for (int c = 0; c < CO; c += 4) *reinterpret_cast<float4*>(o + c) = make_float4(a[c], a[c + 1], a[c + 2], a[c + 3]);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------------------------
+// weight and bias gradients: dW[co][tap][ci] += sum_p G[p][co] * X[p + d(tap)][ci],
+// db[co] += sum_p G[p][co], G = upstream gradient (times (mask > 0) when MASK). One thread per
+// (tap, ci) with CO accumulators; CTAs loop over 16x16 tiles and add their sums once at the end.
+// ---------------------------------------------------------------------------------------------
+template <int CI, int CO, bool MASK>
+__global__ void __launch_bounds__(9 * CI) cnn_wgrad_kernel(const __nv_bfloat16* __restrict__ X, const float* __restrict__ G,
+                                                           const __nv_bfloat16* __restrict__ mask, int nimg, int h,
+                                                           int w, float* __restrict__ dW, float* __restrict__ db,
+                                                           unsigned* status) {
+  extern __shared__ __align__(16) float csm[];
+  float* xs = csm;                                    // [CI][kCS]
+  float* gs = csm + ((CI * kCS + 3) & ~3);            // [256][CO]
+  if (smem_overrun(csm, gs + kCT * kCT * CO, status)) return;
+  const int tid = threadIdx.x, tap = tid / CI, ci = tid - tap * CI;
+  const int ky = tap / 3, kx = tap - ky * 3;
+  const int tiles_x = (w + kCT - 1) / kCT, tiles_y = (h + kCT - 1) / kCT;
+  const long long ntiles = (long long)tiles_x * tiles_y * nimg;
+  float acc[CO], bacc[CO];
+#pragma unroll
+  for (int o = 0; o < CO; ++o) acc[o] = bacc[o] = 0.f;
+  for (long long t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const int n = (int)(t / ((long long)tiles_x * tiles_y));
+    const int r = (int)(t - (long long)n * tiles_x * tiles_y);
+    const int y0 = (r / tiles_x) * kCT, x0 = (r % tiles_x) * kCT;
+    const size_t img = (size_t)n * h * w;
+    __syncthreads();
+    for (int e = tid; e < kCH * kCH * CI; e += blockDim.x) {
+      const int q = e / CI, c = e - q * CI;
+      const int qy = q / kCH, qx = q - qy * kCH;
+      const int y = y0 + qy - 1, x = x0 + qx - 1;
+      xs[c * kCS + q] = (y >= 0 && y < h && x >= 0 && x < w) ? __bfloat162float(X[(img + (size_t)y * w + x) * CI + c]) : 0.f;
+    }
+    for (int e = tid; e < kCT * kCT * CO; e += blockDim.x) {
+      const int q = e / CO, c = e - q * CO;
+      const int y = y0 + q / kCT, x = x0 + q % kCT;
+      float g = 0.f;
+      if (y < h && x < w) {
+        const size_t off = (img + (size_t)y * w + x) * CO + c;
+        g = G[off];
+        if (MASK && !(__bfloat162float(mask[off]) > 0.f)) g = 0.f;
+      }
+      gs[e] = g;
+    }
+    __syncthreads();
+    const float* xb = xs + ci * kCS + ky * kCH + kx;
+#pragma unroll 2
+    for (int p = 0; p < kCT * kCT; ++p) {
+      const float xv = xb[(p >> 4) * kCH + (p & 15)];
+      const float4* g4 = reinterpret_cast<const float4*>(gs + p * CO);
+#pragma unroll
+      for (int o4 = 0; o4 < CO / 4; ++o4) {
+        const float4 gv = g4[o4];
+        acc[4 * o4 + 0] = fmaf(xv, gv.x, acc[4 * o4 + 0]);
+        acc[4 * o4 + 1] = fmaf(xv, gv.y, acc[4 * o4 + 1]);
+        acc[4 * o4 + 2] = fmaf(xv, gv.z, acc[4 * o4 + 2]);
+        acc[4 * o4 + 3] = fmaf(xv, gv.w, acc[4 * o4 + 3]);
+        if (tid == 0) {
+          bacc[4 * o4 + 0] += gv.x;
+          bacc[4 * o4 + 1] += gv.y;
+          bacc[4 * o4 + 2] += gv.z;
+          bacc[4 * o4 + 3] += gv.w;
+        }
+      }
+    }
+  }
+#pragma unroll
+  for (int o = 0; o < CO; ++o) atomicAdd(dW + ((size_t)o * 9 + tap) * CI + ci, acc[o]);
+  if (tid == 0) {
+#pragma unroll
+    for (int o = 0; o < CO; ++o) atomicAdd(db + o, bacc[o]);
+  }
+}
+
+// ---------------------------------------------------------------------------------------------
+// relaxed winner-takes-all truncated L1 loss and its gradient; loss_sum += the batch loss
+// ---------------------------------------------------------------------------------------------
+__global__ void cnn_wta_kernel(const float* __restrict__ out, const float* __restrict__ tgt,
+                               const uint8_t* __restrict__ valid, long long npix, float inv_nv,
+                               float* __restrict__ dout, float* __restrict__ loss_sum) {
+  float lsum = 0.f;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < npix; i += (long long)gridDim.x * blockDim.x) {
+    const float* o = out + i * 8;
+    float* d = dout + i * 8;
+    if (!valid[i]) {
+#pragma unroll
+      for (int c = 0; c < 8; ++c) d[c] = 0.f;
+      continue;
+    }
+    const float tx = tgt[2 * i], ty = tgt[2 * i + 1];
+    float e[4];
+    int js = 0;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      e[j] = fabsf(kOutScale * o[2 * j] - tx) + fabsf(kOutScale * o[2 * j + 1] - ty);
+      if (e[j] < e[js]) js = j;
+    }
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const float wj = (j == js ? 1.f : kWtaEps) * inv_nv;
+      const bool live = e[j] < kWtaTrunc;
+      lsum += wj * (live ? e[j] : kWtaTrunc);
+      const float dx = kOutScale * o[2 * j] - tx, dy = kOutScale * o[2 * j + 1] - ty;
+      const float g = live ? wj * kOutScale : 0.f;
+      d[2 * j] = g * (dx > 0.f ? 1.f : (dx < 0.f ? -1.f : 0.f));
+      d[2 * j + 1] = g * (dy > 0.f ? 1.f : (dy < 0.f ? -1.f : 0.f));
+    }
+  }
+#pragma unroll
+  for (int o = 16; o; o >>= 1) lsum += __shfl_xor_sync(0xffffffffu, lsum, o);
+  if ((threadIdx.x & 31) == 0 && lsum != 0.f) atomicAdd(loss_sum, lsum);
+}
+
+// Adam (bias-corrected), in place on FP32 master parameters
+__global__ void cnn_adam_kernel(float* __restrict__ p, const float* __restrict__ g, float* __restrict__ m,
+                                float* __restrict__ v, int n, float lr, float b1, float b2, float eps, float c1,
+                                float c2) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const float gi = g[i];
+    const float mi = b1 * m[i] + (1.f - b1) * gi;
+    const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+    m[i] = mi;
+    v[i] = vi;
+    p[i] -= lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+  }
+}
+
+// ---------------------------------------------------------------------------------------------
+// training targets from an NNF and inference proposals
+// ---------------------------------------------------------------------------------------------
+__device__ __forceinline__ float median16(float (&v)[16]) {
+#pragma unroll
+  for (int i = 1; i < 16; ++i) {
+#pragma unroll
+    for (int j = i; j > 0; --j) {
+      const float a = v[j - 1], b = v[j];
+      v[j - 1] = fminf(a, b);
+      v[j] = fmaxf(a, b);
+    }
+  }
+  return 0.5f * (v[7] + v[8]);
+}
+
+__global__ void cnn_targets_kernel(const int* __restrict__ nnf, int H, int W, int Wb, int psize, int h4, int w4,
+                                   float* __restrict__ tgt, uint8_t* __restrict__ valid) {
+  const int n_cols = W - psize + 1, n_rows = H - psize + 1, ncb = Wb - psize + 1, half = psize / 2;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < h4 * w4; i += gridDim.x * blockDim.x) {
+    const int yy = i / w4, xx = i - yy * w4;
+    float dx[16], dy[16];
+    bool ok = true;
+#pragma unroll
+    for (int u = 0; u < 16; ++u) {
+      const int y = 4 * yy + (u >> 2) - half, x = 4 * xx + (u & 3) - half;
+      if (y < 0 || y >= n_rows || x < 0 || x >= n_cols) {
+        ok = false;
+        dx[u] = dy[u] = 0.f;
+        continue;
+      }
+      const int b = nnf[(size_t)y * n_cols + x];
+      const int by = b / ncb, bx = b - by * ncb;
+      dx[u] = (float)(bx - x);
+      dy[u] = (float)(by - y);
+    }
+    valid[i] = ok ? 1 : 0;
+    tgt[2 * i] = ok ? median16(dx) : 0.f;
+    tgt[2 * i + 1] = ok ? median16(dy) : 0.f;
+  }
+}
+
+__global__ void cnn_proposals_kernel(const float* __restrict__ out, int h4, int w4, int n_rows, int n_cols, int nrb,
+                                     int ncb, int psize, int* __restrict__ props) {
+  const long long nA = (long long)n_rows * n_cols;
+  const int half = psize / 2;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < nA; i += (long long)gridDim.x * blockDim.x) {
+    const int y = (int)(i / n_cols), x = (int)(i - (long long)y * n_cols);
+    const int li = min((y + half) >> 2, h4 - 1), lj = min((x + half) >> 2, w4 - 1);
+    const float* o = out + ((size_t)li * w4 + lj) * 8;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int by = min(max(y + __float2int_rn(o[2 * j + 1] * kOutScale), 0), nrb - 1);
+      const int bx = min(max(x + __float2int_rn(o[2 * j] * kOutScale), 0), ncb - 1);
+      props[i * 4 + j] = by * ncb + bx;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------------------------
+// host wrappers
+// ---------------------------------------------------------------------------------------------
+static int grid_for(long long n, int block) { return (int)std::max(1LL, std::min<long long>((n + block - 1) / block, 16LL * num_sms())); }
+
+int cnn_input(const uint8_t* A, const uint8_t* B, int H, int W, void* X, cudaStream_t st) {
+  ANNF_REQUIRE(H >= 4 && W >= 4, "annf_cnn_input: image smaller than 4x4");
+  const int h4 = H / 4, w4 = W / 4;
+  cnn_input_kernel<<<grid_for((long long)h4 * w4, 256), 256, 0, st>>>(A, B, H, W, h4, w4,
+                                                                       static_cast<__nv_bfloat16*>(X));
+  ANNF_CHECK_LAUNCH();
+  return ANNF_OK;
+}
+
+int cnn_prep_weights(const float* W, int co, int ci, float* wf, float* wb, cudaStream_t st) {
+  cnn_prep_weights_kernel<<<grid_for((long long)co * 9 * ci, 256), 256, 0, st>>>(W, co, ci, wf, wb);
+  ANNF_CHECK_LAUNCH();
+  return ANNF_OK;
+}
+
+template <int CI, int CO, typename TIN, bool MASK, int MODE>
+static int launch_conv(const TIN* in, const __nv_bfloat16* mask, int nimg, int h, int w, const float* wg,
+                       const float* bias, void* out, unsigned* status, cudaStream_t st) {
+  const size_t smem = ((size_t)CI * kCS + 4) * sizeof(float) + (size_t)9 * CI * CO * sizeof(float);
+  ANNF_CUDA_TRY(cudaFuncSetAttribute(cnn_conv_kernel<CI, CO, TIN, MASK, MODE>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  dim3 grid((w + kCT - 1) / kCT, (h + kCT - 1) / kCT, nimg);
+  cnn_conv_kernel<CI, CO, TIN, MASK, MODE><<<grid, 128, smem, st>>>(in, mask, h, w, wg, bias, out, status);
+  ANNF_CHECK_LAUNCH();
+  return ANNF_OK;
+}
+
+// forward convolution: ci in {8, 32}, co in {8, 32}; relu -> BF16 out, else FP32 out
+int cnn_conv_forward(const void* X, int nimg, int h, int w, int ci, int co, const float* wf, const float* bias,
+                     int relu, void* Y, unsigned* status, cudaStream_t st) {
+  const __nv_bfloat16* x = static_cast<const __nv_bfloat16*>(X);
+  if (ci == 8 && co == 32 && relu) return launch_conv<8, 32, __nv_bfloat16, false, 0>(x, nullptr, nimg, h, w, wf, bias, Y, status, st);
+  if (ci == 32 && co == 32 && relu) return launch_conv<32, 32, __nv_bfloat16, false, 0>(x, nullptr, nimg, h, w, wf, bias, Y, status, st);
+  if (ci == 32 && co == 8 && !relu) return launch_conv<32, 8, __nv_bfloat16, false, 1>(x, nullptr, nimg, h, w, wf, bias, Y, status, st);
+  set_error("annf_cnn_conv_forward: unsupported layer shape");
+  return ANNF_ERR_UNSUPPORTED;
+}
+
+// input gradient: G [nimg,h,w,co] FP32 (times (mask > 0) if mask) -> dX [nimg,h,w,ci] FP32
+int cnn_conv_backward_data(const float* G, const void* mask, int nimg, int h, int w, int co, int ci, const float* wb,
+                           float* dX, unsigned* status, cudaStream_t st) {
+  const __nv_bfloat16* m = static_cast<const __nv_bfloat16*>(mask);
+  if (co == 32 && ci == 32) {
+    return m ? launch_conv<32, 32, float, true, 2>(G, m, nimg, h, w, wb, nullptr, dX, status, st)
+             : launch_conv<32, 32, float, false, 2>(G, m, nimg, h, w, wb, nullptr, dX, status, st);
+  }
+  if (co == 8 && ci == 32 && !m) return launch_conv<8, 32, float, false, 2>(G, m, nimg, h, w, wb, nullptr, dX, status, st);
+  if (co == 32 && ci == 8) {
+    return m ? launch_conv<32, 8, float, true, 2>(G, m, nimg, h, w, wb, nullptr, dX, status, st)
+             : launch_conv<32, 8, float, false, 2>(G, m, nimg, h, w, wb, nullptr, dX, status, st);
+  }
+  set_error("annf_cnn_conv_backward_data: unsupported layer shape");
+  return ANNF_ERR_UNSUPPORTED;
+}
+
+template <int CI, int CO, bool MASK>
+static int launch_wgrad(const __nv_bfloat16* X, const float* G, const __nv_bfloat16* mask, int nimg, int h, int w,
+                        float* dW, float* db, unsigned* status, cudaStream_t st) {
+  const size_t smem = ((size_t)((CI * kCS + 3) & ~3) + (size_t)kCT * kCT * CO) * sizeof(float);
+  ANNF_CUDA_TRY(cudaFuncSetAttribute(cnn_wgrad_kernel<CI, CO, MASK>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)smem));
+  const long long tiles = (long long)((w + kCT - 1) / kCT) * ((h + kCT - 1) / kCT) * nimg;
+  const int grid = (int)std::max(1LL, std::min<long long>(tiles, 2LL * num_sms()));
+  cnn_wgrad_kernel<CI, CO, MASK><<<grid, 9 * CI, smem, st>>>(X, G, mask, nimg, h, w, dW, db, status);
+  ANNF_CHECK_LAUNCH();
+  return ANNF_OK;
+}
+
+// weight / bias gradients (accumulated into dW [co][9][ci], db [co])
+int cnn_conv_backward_weights(const void* X, const float* G, const void* mask, int nimg, int h, int w, int ci, int co,
+                              float* dW, float* db, unsigned* status, cudaStream_t st) {
+  const __nv_bfloat16* x = static_cast<const __nv_bfloat16*>(X);
+  const __nv_bfloat16* m = static_cast<const __nv_bfloat16*>(mask);
+  if (ci == 8 && co == 32) {
+    return m ? launch_wgrad<8, 32, true>(x, G, m, nimg, h, w, dW, db, status, st)
+             : launch_wgrad<8, 32, false>(x, G, m, nimg, h, w, dW, db, status, st);
+  }
+  if (ci == 32 && co == 32) {
+    return m ? launch_wgrad<32, 32, true>(x, G, m, nimg, h, w, dW, db, status, st)
+             : launch_wgrad<32, 32, false>(x, G, m, nimg, h, w, dW, db, status, st);
+  }
+  if (ci == 32 && co == 8 && !m) return launch_wgrad<32, 8, false>(x, G, m, nimg, h, w, dW, db, status, st);
+  set_error("annf_cnn_conv_backward_weights: unsupported layer shape");
+  return ANNF_ERR_UNSUPPORTED;
+}
+
+int cnn_wta_loss(const float* out, const float* tgt, const uint8_t* valid, long long npix, float inv_nv, float* dout,
+                 float* loss_sum, cudaStream_t st) {
+  cnn_wta_kernel<<<grid_for(npix, 256), 256, 0, st>>>(out, tgt, valid, npix, inv_nv, dout, loss_sum);
+  ANNF_CHECK_LAUNCH();
+  return ANNF_OK;
+}
+
+int cnn_adam(float* p, const float* g, float* m, float* v, int n, float lr, float b1, float b2, float eps, int step,
+             cudaStream_t st) {
+  const float c1 = 1.f - powf(b1, (float)step), c2 = 1.f - powf(b2, (float)step);
+  cnn_adam_kernel<<<grid_for(n, 256), 256, 0, st>>>(p, g, m, v, n, lr, b1, b2, eps, c1, c2);
+  ANNF_CHECK_LAUNCH();
+  return ANNF_OK;
+}
+
+int cnn_targets(const int* nnf, int H, int W, int Wb, int psize, float* tgt, uint8_t* valid, cudaStream_t st) {
+  const int h4 = H / 4, w4 = W / 4;
+  cnn_targets_kernel<<<grid_for((long long)h4 * w4, 128), 128, 0, st>>>(nnf, H, W, Wb, psize, h4, w4, tgt, valid);
+  ANNF_CHECK_LAUNCH();
+  return ANNF_OK;
+}
+
+int cnn_proposals(const float* out, int h4, int w4, int H, int W, int Hb, int Wb, int psize, int* props,
+                  cudaStream_t st) {
+  const int n_rows = H - psize + 1, n_cols = W - psize + 1;
+  cnn_proposals_kernel<<<grid_for((long long)n_rows * n_cols, 256), 256, 0, st>>>(
+      out, h4, w4, n_rows, n_cols, Hb - psize + 1, Wb - psize + 1, psize, props);
+  ANNF_CHECK_LAUNCH();
+  return ANNF_OK;
+}
+
+}  // namespace annf

@@ -52,6 +52,7 @@ enum : unsigned {
   DEV_BAD_LEAF = 2u,
   DEV_LIST_OVERFLOW = 4u,
   DEV_SMEM_CARVE = 8u,  // a kernel's shared-memory carve exceeded its launch allocation
+  DEV_TC_TIMEOUT = 16u, // a tensor-core kernel's bounded wait on its MMA ran out
 };
 
 __device__ __forceinline__ unsigned dyn_smem_size() {

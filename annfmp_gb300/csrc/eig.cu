@@ -1,0 +1,419 @@
+// eig.cu -- leading eigenvectors of the patch covariance by subspace iteration (sm_103a).
+//
+// The full FP64 eigendecomposition of the P x P covariance (P = 243 for 9x9x3 patches) costs
+// milliseconds in a library solver, while the NNF only needs the top n_components. This solver:
+//   1. simultaneous (subspace) iteration in FP32 on a block of b >= n_components vectors, one CTA:
+//      Z = C Q, then modified Gram-Schmidt, `iters` times (C kept in FP32 in global memory, L2-hot);
+//   2. Rayleigh-Ritz in FP64 on span(Q): W = C Q, G = Q^T Q, T = Q^T W over many CTAs;
+//   3. the b x b generalised problem T y = lambda G y in FP64 on one CTA: Cholesky G = R^T R
+//      (columns with a vanishing pivot are dropped), T~ = R^-T T R^-1, cyclic Jacobi on T~, and
+//      coefficients x = R^-1 y;
+//   4. components = Q x, in decreasing Ritz value, each signed so that its largest |entry| is
+//      positive (the sign convention of the exact solver).
+// The covariance and the small eigenproblem stay in FP64; only the power steps that find the
+// subspace run in FP32. Used by the approximate NNF forms; the plain form keeps the exact solver.
+#include <algorithm>
+
+#include "common.cuh"
+#include "handle.cuh"
+
+namespace annf {
+
+constexpr int kSubThreads = 1024;
+constexpr int kMaxBlock = 40;  // three b x b FP64 matrices in static shared memory (<= 48 KB)
+
+__device__ __forceinline__ float warp_sum_f(float v) {
+#pragma unroll
+  for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ __forceinline__ double warp_sum_d(double v) {
+#pragma unroll
+  for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+__device__ __forceinline__ uint32_t mix32(uint32_t x) {
+  x ^= x >> 16;
+  x *= 0x7feb352dU;
+  x ^= x >> 15;
+  x *= 0x846ca68bU;
+  x ^= x >> 16;
+  return x;
+}
+
+// modified Gram-Schmidt over the b columns of Z (column-major [b][P] in shared memory)
+__device__ void mgs_columns(float* Z, int P, int b) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  __shared__ float s_inv;
+  for (int j = 0; j < b; ++j) {
+    float* zj = Z + (size_t)j * P;
+    if (warp == 0) {
+      float s = 0.f;
+      for (int i = lane; i < P; i += 32) s = fmaf(zj[i], zj[i], s);
+      s = warp_sum_f(s);
+      if (lane == 0) s_inv = s > 1e-30f ? rsqrtf(s) : 0.f;
+    }
+    __syncthreads();
+    const float inv = s_inv;
+    if (inv == 0.f) {  // vanished column: restart it from a basis vector
+      for (int i = threadIdx.x; i < P; i += blockDim.x) zj[i] = (i == (j * 7 + 3) % P) ? 1.f : 0.f;
+    } else {
+      for (int i = threadIdx.x; i < P; i += blockDim.x) zj[i] *= inv;
+    }
+    __syncthreads();
+    for (int l = j + 1 + warp; l < b; l += nw) {
+      float* zl = Z + (size_t)l * P;
+      float r = 0.f;
+      for (int i = lane; i < P; i += 32) r = fmaf(zj[i], zl[i], r);
+      r = warp_sum_f(r);
+      for (int i = lane; i < P; i += 32) zl[i] = fmaf(-r, zj[i], zl[i]);
+    }
+    __syncthreads();
+  }
+}
+
+// step 1: one CTA. C32 is scratch [P*P]; Qout [b][P] FP32.
+__global__ void __launch_bounds__(kSubThreads) subspace_iter_kernel(const double* __restrict__ C, int P, int b,
+                                                                    int iters, float* C32, float* __restrict__ Qout,
+                                                                    unsigned* status) {
+  extern __shared__ __align__(16) float sm[];
+  float* Q = sm;
+  float* Z = sm + (size_t)b * P;
+  if (smem_overrun(sm, Z + (size_t)b * P, status)) return;
+  for (long long e = threadIdx.x; e < (long long)P * P; e += blockDim.x) C32[e] = (float)C[e];
+  for (int e = threadIdx.x; e < b * P; e += blockDim.x)
+    Q[e] = (float)(mix32((uint32_t)e * 2654435761u + 12345u) >> 8) * (1.0f / 16777216.0f) - 0.5f;
+  __syncthreads();
+  mgs_columns(Q, P, b);
+  const int groups = b >> 3;
+  for (int it = 0; it < iters; ++it) {
+    // Z = C Q (C symmetric: row i of C read as column i, coalesced across i)
+    for (int item = threadIdx.x; item < groups * P; item += blockDim.x) {
+      const int g = item / P, i = item - g * P;
+      float acc[8];
+#pragma unroll
+      for (int c = 0; c < 8; ++c) acc[c] = 0.f;
+      const float* q = Q + (size_t)(g * 8) * P;
+#pragma unroll 8
+      for (int k = 0; k < P; ++k) {
+        const float cv = C32[(size_t)k * P + i];
+#pragma unroll
+        for (int c = 0; c < 8; ++c) acc[c] = fmaf(cv, q[(size_t)c * P + k], acc[c]);
+      }
+#pragma unroll
+      for (int c = 0; c < 8; ++c) Z[(size_t)(g * 8 + c) * P + i] = acc[c];
+    }
+    __syncthreads();
+    mgs_columns(Z, P, b);
+    float* t = Q;
+    Q = Z;
+    Z = t;
+  }
+  mgs_columns(Q, P, b);  // second pass: orthogonal to working precision
+  for (int e = threadIdx.x; e < b * P; e += blockDim.x) Qout[e] = Q[e];
+}
+
+// step 2a: W[j][i] = sum_k C[i][k] Q[j][k] in FP64, one warp per (j, i)
+__global__ void rr_cq_kernel(const double* __restrict__ C, int P, int b, const float* __restrict__ Q,
+                             double* __restrict__ W) {
+  const long long wid = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (wid >= (long long)b * P) return;
+  const int j = (int)(wid / P), i = (int)(wid - (long long)j * P);
+  const double* c = C + (size_t)i * P;
+  const float* q = Q + (size_t)j * P;
+  double s = 0.0;
+  for (int k = lane; k < P; k += 32) s = fma(c[k], (double)q[k], s);
+  s = warp_sum_d(s);
+  if (lane == 0) W[(size_t)j * P + i] = s;
+}
+
+// step 2b: G = Q^T Q and T = Q^T W (b x b, FP64), one warp per entry
+__global__ void rr_gram_kernel(int P, int b, const float* __restrict__ Q, const double* __restrict__ W,
+                               double* __restrict__ G, double* __restrict__ T) {
+  const long long wid = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (wid >= 2LL * b * b) return;
+  const int which = (int)(wid / (b * b)), e = (int)(wid - (long long)which * b * b);
+  const int i = e / b, j = e - i * b;
+  const float* qi = Q + (size_t)i * P;
+  double s = 0.0;
+  if (which == 0) {
+    const float* qj = Q + (size_t)j * P;
+    for (int k = lane; k < P; k += 32) s = fma((double)qi[k], (double)qj[k], s);
+  } else {
+    const double* wj = W + (size_t)j * P;
+    for (int k = lane; k < P; k += 32) s = fma((double)qi[k], wj[k], s);
+  }
+  s = warp_sum_d(s);
+  if (lane == 0) (which == 0 ? G : T)[e] = s;
+}
+
+// step 3: one CTA, FP64. Writes X [ncomp][b] (coefficients of each component in the Q basis).
+__global__ void __launch_bounds__(256) rr_solve_kernel(int b, int ncomp, const double* __restrict__ Gg,
+                                                       const double* __restrict__ Tg, double* __restrict__ Xout,
+                                                       double* __restrict__ lambda_out) {
+  __shared__ double G[kMaxBlock * kMaxBlock], T[kMaxBlock * kMaxBlock], V[kMaxBlock * kMaxBlock];
+  __shared__ double lam[kMaxBlock];
+  __shared__ int keep[kMaxBlock], order[kMaxBlock];
+  __shared__ int s_m;
+  __shared__ double s_off, s_tot;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  for (int e = tid; e < b * b; e += nt) {
+    const int i = e / b, j = e - i * b;
+    G[e] = 0.5 * (Gg[i * b + j] + Gg[j * b + i]);
+    T[e] = 0.5 * (Tg[i * b + j] + Tg[j * b + i]);
+  }
+  __syncthreads();
+  // Cholesky G = R^T R in place, right-looking (upper triangle holds R; the trailing block is
+  // updated by all threads); vanishing pivots drop their column
+  __shared__ double s_gmax, s_piv;
+  if (tid == 0) {
+    double gmax = 0.0;
+    for (int i = 0; i < b; ++i) gmax = fmax(gmax, G[i * b + i]);
+    s_gmax = gmax;
+    s_m = 0;
+  }
+  __syncthreads();
+  for (int k = 0; k < b; ++k) {
+    if (tid == 0) {
+      const double piv = G[k * b + k];
+      const bool ok = piv > 1e-10 * s_gmax && piv > 0.0;
+      keep[k] = ok ? s_m++ : -1;
+      s_piv = ok ? sqrt(piv) : 0.0;
+    }
+    __syncthreads();
+    const double r = s_piv;
+    for (int j = k + tid; j < b; j += nt) G[k * b + j] = r > 0.0 ? (j == k ? r : G[k * b + j] / r) : 0.0;
+    __syncthreads();
+    if (r > 0.0) {
+      const int tw = b - k - 1;
+      for (int e = tid; e < tw * tw; e += nt) {
+        const int i = k + 1 + e / tw, j = k + 1 + e % tw;
+        if (j >= i) G[i * b + j] -= G[k * b + i] * G[k * b + j];
+      }
+    }
+    __syncthreads();
+  }
+  const int m = s_m;
+  // compact the kept columns: R~ (m x m upper), T (m x m); V <- T restricted
+  // (kept column k maps to keep[k]); reuse V as scratch for the compacted T
+  for (int e = tid; e < b * b; e += nt) {
+    const int i = e / b, j = e - i * b;
+    if (keep[i] >= 0 && keep[j] >= 0) V[keep[i] * m + keep[j]] = T[e];
+  }
+  __syncthreads();
+  for (int e = tid; e < b * b; e += nt) {
+    const int i = e / b, j = e - i * b;
+    if (keep[i] >= 0 && keep[j] >= 0) T[keep[i] * m + keep[j]] = (j >= i) ? G[e] : 0.0;  // T now holds R~
+  }
+  __syncthreads();
+  for (int e = tid; e < m * m; e += nt) G[e] = T[e];  // G = R~ (m x m, upper)
+  __syncthreads();
+  // X = R~^-T Tm : forward substitution per column (R~^T lower)
+  for (int c = tid; c < m; c += nt) {
+    for (int i = 0; i < m; ++i) {
+      double v = V[i * m + c];
+      for (int t = 0; t < i; ++t) v -= G[t * m + i] * T[t * m + c];
+      T[i * m + c] = v / G[i * m + i];
+    }
+  }
+  __syncthreads();
+  // T~ = X R~^-1 : solve T~ R~ = X row by row
+  for (int r = tid; r < m; r += nt) {
+    for (int j = 0; j < m; ++j) {
+      double v = T[r * m + j];
+      for (int t = 0; t < j; ++t) v -= V[r * m + t] * G[t * m + j];
+      V[r * m + j] = v / G[j * m + j];
+    }
+  }
+  __syncthreads();
+  // symmetrise into T, V = I
+  for (int e = tid; e < m * m; e += nt) {
+    const int i = e / m, j = e - i * m;
+    T[e] = 0.5 * (V[i * m + j] + V[j * m + i]);
+  }
+  __syncthreads();
+  for (int e = tid; e < m * m; e += nt) V[e] = (e / m == e % m) ? 1.0 : 0.0;
+  __syncthreads();
+  // parallel Jacobi, round-robin ordering: each round rotates M/2 disjoint pairs at once (M = m
+  // rounded up to even; a pair with the phantom index M-1 >= m is skipped). Rotation angles are
+  // computed by one thread per pair from the matrix before the round, then all row updates, then
+  // all column updates (disjoint rotations commute).
+  __shared__ double s_cs[kMaxBlock / 2], s_sn[kMaxBlock / 2];
+  __shared__ int s_p[kMaxBlock / 2], s_q[kMaxBlock / 2];
+  const int M = (m + 1) & ~1, half = M / 2;
+  for (int sweep = 0; sweep < 15 && m > 1; ++sweep) {
+    if (tid < 32) {
+      double off = 0.0, tot = 0.0;
+      for (int e = tid; e < m * m; e += 32) {
+        const double v = T[e] * T[e];
+        tot += v;
+        if (e / m != e % m) off += v;
+      }
+      off = warp_sum_d(off);
+      tot = warp_sum_d(tot);
+      if (tid == 0) {
+        s_off = off;
+        s_tot = tot;
+      }
+    }
+    __syncthreads();
+    if (!(s_off > 1e-24 * s_tot)) break;
+    for (int round = 0; round < M - 1; ++round) {
+      if (tid < half) {
+        auto player = [&](int j) { return j == 0 ? 0 : 1 + (j - 1 + round) % (M - 1); };
+        int p = player(tid), q = player(M - 1 - tid);
+        if (p > q) {
+          const int t = p;
+          p = q;
+          q = t;
+        }
+        double cs = 1.0, sn = 0.0;
+        if (q < m) {
+          const double apq = T[p * m + q];
+          const double app = T[p * m + p], aqq = T[q * m + q];
+          if (fabs(apq) > 1e-300 && fabs(apq) > 1e-15 * sqrt(fabs(app * aqq))) {
+            const double theta = (aqq - app) / (2.0 * apq);
+            const double t = (theta >= 0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
+            cs = 1.0 / sqrt(t * t + 1.0);
+            sn = t * cs;
+          }
+        }
+        s_p[tid] = p;
+        s_q[tid] = q < m ? q : -1;
+        s_cs[tid] = cs;
+        s_sn[tid] = sn;
+      }
+      __syncthreads();
+      for (int e = tid; e < half * m; e += nt) {  // rows p, q
+        const int i = e / m, k = e - i * m;
+        const int p = s_p[i], q = s_q[i];
+        if (q < 0 || s_sn[i] == 0.0) continue;
+        const double cs = s_cs[i], sn = s_sn[i];
+        const double tp = T[p * m + k], tq = T[q * m + k];
+        T[p * m + k] = cs * tp - sn * tq;
+        T[q * m + k] = sn * tp + cs * tq;
+      }
+      __syncthreads();
+      for (int e = tid; e < half * m; e += nt) {  // columns p, q and the eigenvectors
+        const int i = e / m, k = e - i * m;
+        const int p = s_p[i], q = s_q[i];
+        if (q < 0 || s_sn[i] == 0.0) continue;
+        const double cs = s_cs[i], sn = s_sn[i];
+        const double tp = T[k * m + p], tq = T[k * m + q];
+        T[k * m + p] = cs * tp - sn * tq;
+        T[k * m + q] = sn * tp + cs * tq;
+        const double vp = V[k * m + p], vq = V[k * m + q];
+        V[k * m + p] = cs * vp - sn * vq;
+        V[k * m + q] = sn * vp + cs * vq;
+      }
+      __syncthreads();
+    }
+  }
+  for (int i = tid; i < m; i += nt) lam[i] = T[i * m + i];
+  __syncthreads();
+  // decreasing Ritz value (stable on ties)
+  for (int i = tid; i < m; i += nt) {
+    int r = 0;
+    for (int j = 0; j < m; ++j) r += (lam[j] > lam[i]) || (lam[j] == lam[i] && j < i);
+    order[r] = i;
+  }
+  __syncthreads();
+  // x = R~^-1 y for the selected Ritz vectors, scattered back to the b kept columns
+  for (int c = tid; c < ncomp; c += nt) {
+    double* x = Xout + (size_t)c * b;
+    for (int k = 0; k < b; ++k) x[k] = 0.0;
+    if (c >= m) continue;  // fewer independent directions than components: zero component
+    const int col = order[c];
+    double xs[kMaxBlock];
+    for (int i = m - 1; i >= 0; --i) {
+      double v = V[i * m + col];
+      for (int t = i + 1; t < m; ++t) v -= G[i * m + t] * xs[t];
+      xs[i] = v / G[i * m + i];
+    }
+    for (int k = 0; k < b; ++k)
+      if (keep[k] >= 0) x[k] = xs[keep[k]];
+    if (lambda_out) lambda_out[c] = lam[col];
+  }
+}
+
+// step 4: comps[c] = Q x_c (FP64), signed so that the largest |entry| (first on ties) is positive
+__global__ void rr_comps_kernel(int P, int b, const float* __restrict__ Q, const double* __restrict__ X,
+                                double* __restrict__ comps) {
+  const int c = blockIdx.x;
+  const double* x = X + (size_t)c * b;
+  double* out = comps + (size_t)c * P;
+  __shared__ double sbest[256];
+  __shared__ int sidx[256];
+  double best = -1.0;
+  int bi = 0x7fffffff;
+  for (int i = threadIdx.x; i < P; i += blockDim.x) {
+    double s = 0.0;
+    for (int k = 0; k < b; ++k) s = fma((double)Q[(size_t)k * P + i], x[k], s);
+    out[i] = s;
+    const double a = fabs(s);
+    if (a > best || (a == best && i < bi)) {
+      best = a;
+      bi = i;
+    }
+  }
+  sbest[threadIdx.x] = best;
+  sidx[threadIdx.x] = bi;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o; o >>= 1) {
+    if ((int)threadIdx.x < o) {
+      const double ob = sbest[threadIdx.x + o];
+      const int oi = sidx[threadIdx.x + o];
+      if (ob > sbest[threadIdx.x] || (ob == sbest[threadIdx.x] && oi < sidx[threadIdx.x])) {
+        sbest[threadIdx.x] = ob;
+        sidx[threadIdx.x] = oi;
+      }
+    }
+    __syncthreads();
+  }
+  const double piv = sidx[0] < P ? out[sidx[0]] : 0.0;
+  __syncthreads();
+  if (piv < 0)
+    for (int i = threadIdx.x; i < P; i += blockDim.x) out[i] = -out[i];
+}
+
+// block size for n components: b >= ncomp + max(8, ncomp / 2), a multiple of 8
+int subspace_block(int P, int ncomp) {
+  int b = ncomp + std::max(8, ncomp / 2);
+  b = (b + 7) / 8 * 8;
+  if (b > kMaxBlock || 2 * b > P) return 0;  // the exact solver handles these sizes
+  return b;
+}
+
+// C [P*P] FP64 covariance (device) -> comps [ncomp*P] FP64
+int eig_top_subspace(annf_handle* h, const double* C, int P, int ncomp, int iters, double* comps, cudaStream_t st) {
+  const int b = subspace_block(P, ncomp);
+  ANNF_REQUIRE(b > 0, "subspace eigensolver: unsupported size");
+  const size_t smem = (size_t)2 * b * P * sizeof(float);
+  ANNF_REQUIRE(smem <= 200 * 1024, "subspace eigensolver: block too large for shared memory");
+  const size_t f32_bytes = ((size_t)P * P + (size_t)b * P) * sizeof(float);
+  const size_t f64_bytes = ((size_t)b * P + 2 * (size_t)b * b + (size_t)ncomp * b) * sizeof(double);
+  ANNF_ENSURE(h->eig_ws, f64_bytes + f32_bytes + 256);
+  double* W = h->eig_ws.as<double>();
+  double* G = W + (size_t)b * P;
+  double* T = G + (size_t)b * b;
+  double* X = T + (size_t)b * b;
+  float* C32 = reinterpret_cast<float*>(X + (size_t)ncomp * b);
+  float* Q = C32 + (size_t)P * P;
+  ANNF_CUDA_TRY(cudaFuncSetAttribute(subspace_iter_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  subspace_iter_kernel<<<1, kSubThreads, smem, st>>>(C, P, b, iters, C32, Q, h->status.as<unsigned>());
+  ANNF_CHECK_LAUNCH();
+  rr_cq_kernel<<<ceil_div((long long)b * P * 32, 256), 256, 0, st>>>(C, P, b, Q, W);
+  ANNF_CHECK_LAUNCH();
+  rr_gram_kernel<<<ceil_div(2LL * b * b * 32, 256), 256, 0, st>>>(P, b, Q, W, G, T);
+  ANNF_CHECK_LAUNCH();
+  rr_solve_kernel<<<1, 256, 0, st>>>(b, ncomp, G, T, X, nullptr);
+  ANNF_CHECK_LAUNCH();
+  rr_comps_kernel<<<ncomp, 256, 0, st>>>(P, b, Q, X, comps);
+  ANNF_CHECK_LAUNCH();
+  return ANNF_OK;
+}
+
+}  // namespace annf

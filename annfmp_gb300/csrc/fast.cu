@@ -29,6 +29,7 @@ __device__ __forceinline__ unsigned ldw_at(const uint8_t* base, long long off) {
 struct Img {
   const uint8_t* p;
   int h, w, c, psize, ncols;  // ncols = w - psize + 1
+  long long bytes;            // h * w * c
 };
 
 __device__ __forceinline__ int patch_ssd(const Img& A, int ay, int ax, const Img& B, int by, int bx) {
@@ -206,25 +207,186 @@ __global__ void fast_final_kernel(int nA, Match m, int* __restrict__ final_idx, 
   }
 }
 
+// ---------------------------------------------------------------------------------------------
+// the same kernels for common patch shapes (rows of RL <= 33 bytes): a patch row is three aligned
+// 16-byte loads shifted into word alignment; the A patch stays in registers for all candidates,
+// and a candidate's sum stops once it exceeds the current best
+// ---------------------------------------------------------------------------------------------
+template <int RL>
+__device__ __forceinline__ void row_words(const uint8_t* __restrict__ img, long long off, long long nbytes,
+                                          unsigned (&w)[(RL + 3) / 4]) {
+  constexpr int NW = (RL + 3) / 4;
+  static_assert(RL <= 33, "row too long for three 16-byte loads");
+  const long long c0 = off & ~15LL;
+  const int s = (int)(off - c0);
+  if (c0 + 48 <= nbytes) {
+    const uint4 q0 = __ldg(reinterpret_cast<const uint4*>(img + c0));
+    const uint4 q1 = __ldg(reinterpret_cast<const uint4*>(img + c0 + 16));
+    const uint4 q2 = __ldg(reinterpret_cast<const uint4*>(img + c0 + 32));
+    const unsigned x[13] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w, q2.x, q2.y, q2.z, q2.w, 0u};
+    const int sh = (s & 3) * 8;
+    switch (s >> 2) {
+#define ANNF_ROWW_CASE(Q)                                                                  \
+  case Q:                                                                                  \
+    _Pragma("unroll") for (int j = 0; j < NW; ++j) w[j] = __funnelshift_r(x[j + Q], x[j + Q + 1], sh); \
+    break;
+      ANNF_ROWW_CASE(0)
+      ANNF_ROWW_CASE(1)
+      ANNF_ROWW_CASE(2)
+      default:
+        ANNF_ROWW_CASE(3)
+#undef ANNF_ROWW_CASE
+    }
+  } else {  // the last bytes of the image: byte loads, all in bounds
+#pragma unroll
+    for (int j = 0; j < NW; ++j) {
+      unsigned v = 0;
+#pragma unroll
+      for (int b = 0; b < 4; ++b)
+        if (4 * j + b < RL) v |= (unsigned)__ldg(img + off + 4 * j + b) << (8 * b);
+      w[j] = v;
+    }
+  }
+  if (RL % 4) w[NW - 1] &= (1u << (8 * (RL % 4))) - 1u;
+}
+
+template <int PS, int RL>
+__device__ __forceinline__ void load_patch(const Img& I, int y, int x, unsigned (&w)[PS][(RL + 3) / 4]) {
+#pragma unroll
+  for (int r = 0; r < PS; ++r) row_words<RL>(I.p, ((long long)(y + r) * I.w + x) * I.c, I.bytes, w[r]);
+}
+
+// exact SSD of the cached A patch against B patch (by, bx); stops (returning a value > limit) as
+// soon as the partial sum exceeds limit
+template <int PS, int RL>
+__device__ __forceinline__ int ssd_limit(const unsigned (&aw)[PS][(RL + 3) / 4], const Img& B, int by, int bx,
+                                         int limit) {
+  constexpr int NW = (RL + 3) / 4;
+  unsigned s = 0;
+#pragma unroll
+  for (int r = 0; r < PS; ++r) {
+    unsigned bw[NW];
+    row_words<RL>(B.p, ((long long)(by + r) * B.w + bx) * B.c, B.bytes, bw);
+#pragma unroll
+    for (int j = 0; j < NW; ++j) {
+      const unsigned x = __vabsdiffu4(aw[r][j], bw[j]);
+      s = __dp4a(x, x, s);
+    }
+    if ((int)s > limit) return (int)s;
+  }
+  return (int)s;
+}
+
+template <int PS, int RL>
+__global__ void __launch_bounds__(256, 2) fast_init_t_kernel(Img A, Img B, int nA, int K, const int* __restrict__ nat_pos,
+                                                          const int* __restrict__ perm, const int* __restrict__ prop,
+                                                          int n_prop, Match out) {
+  const int nb_rows = B.h - B.psize + 1;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nA; i += gridDim.x * blockDim.x) {
+    const int y = i / A.ncols, x = i - y * A.ncols;
+    unsigned aw[PS][(RL + 3) / 4];
+    load_patch<PS, RL>(A, y, x, aw);
+    int best = -1, bs = 0x7fffffff;
+    for (int j = 0; j < K + n_prop; ++j) {
+      int b = j < K ? __ldg(perm + __ldg(nat_pos + (long long)i * K + j)) : __ldg(prop + (long long)i * n_prop + (j - K));
+      if (b < 0 || b == best) continue;
+      const int by = b / B.ncols, bx = b - by * B.ncols;
+      if (by >= nb_rows) continue;
+      const int s = ssd_limit<PS, RL>(aw, B, by, bx, bs);
+      if (s < bs || (s == bs && b < best)) {
+        bs = s;
+        best = b;
+      }
+    }
+    out.idx[i] = best;
+    out.ssd[i] = bs;
+  }
+}
+
+template <int PS, int RL>
+__global__ void __launch_bounds__(256, 2) fast_prop_t_kernel(Img A, Img B, int nA, int jump, int radius, int nrand,
+                                                          uint32_t seed, Match in, Match out) {
+  const int nb_rows = B.h - B.psize + 1, na_rows = nA / A.ncols;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nA; i += gridDim.x * blockDim.x) {
+    const int y = i / A.ncols, x = i - y * A.ncols;
+    int best = in.idx[i], bs = in.ssd[i];
+    const int b0y = best / B.ncols, b0x = best - b0y * B.ncols;
+    unsigned aw[PS][(RL + 3) / 4];
+    load_patch<PS, RL>(A, y, x, aw);
+    auto consider = [&](int by, int bx) {
+      if (by < 0 || bx < 0 || by >= nb_rows || bx >= B.ncols) return;
+      const int b = by * B.ncols + bx;
+      if (b == best) return;
+      const int s = ssd_limit<PS, RL>(aw, B, by, bx, bs);
+      if (s < bs || (s == bs && b < best)) {
+        bs = s;
+        best = b;
+      }
+    };
+    const int dy[4] = {-1, 1, 0, 0}, dx[4] = {0, 0, -1, 1};
+#pragma unroll
+    for (int t = 0; t < 4; ++t) {
+      const int ny = y + dy[t] * jump, nx = x + dx[t] * jump;
+      if (ny < 0 || nx < 0 || ny >= na_rows || nx >= A.ncols) continue;
+      const int nb = in.idx[ny * A.ncols + nx];
+      if (nb < 0) continue;
+      const int nby = nb / B.ncols, nbx = nb - nby * B.ncols;
+      consider(nby - dy[t] * jump, nbx - dx[t] * jump);
+    }
+    for (int t = 0; t < nrand && radius > 0; ++t) {
+      const uint32_t r = hash3(seed, (uint32_t)i, (uint32_t)t);
+      const int ox = (int)(r % (2 * radius + 1)) - radius, oy = (int)((r >> 16) % (2 * radius + 1)) - radius;
+      consider(b0y + oy, b0x + ox);
+    }
+    out.idx[i] = best;
+    out.ssd[i] = bs;
+  }
+}
+
 int fast_search(annf_handle* h, const uint8_t* img_a, int ha, int wa, const uint8_t* img_b, int hb, int wb, int c,
                 int psize, int K, const int* nat_pos, const int* prop, int n_prop, int iters, uint32_t seed,
                 int* final_idx, float* dist_out, cudaStream_t st) {
-  Img A{img_a, ha, wa, c, psize, wa - psize + 1}, B{img_b, hb, wb, c, psize, wb - psize + 1};
+  Img A{img_a, ha, wa, c, psize, wa - psize + 1, (long long)ha * wa * c};
+  Img B{img_b, hb, wb, c, psize, wb - psize + 1, (long long)hb * wb * c};
   const int nA = (ha - psize + 1) * A.ncols;
   ANNF_ENSURE(h->fast_buf, (size_t)4 * nA * sizeof(int));
   int* base = h->fast_buf.as<int>();
   Match m0{base, base + nA}, m1{base + 2 * (size_t)nA, base + 3 * (size_t)nA};
   const int blocks = (int)std::min<long long>(ceil_div(nA, 256), 32LL * num_sms());
-  fast_init_kernel<<<blocks, 256, 0, st>>>(A, B, nA, K, nat_pos, h->perm.as<int>(), prop, n_prop, m0);
+  // shape-specialised kernels for the common patches, the generic ones otherwise
+  const int shape = psize * 100 + psize * c;
+  const bool special = shape == 927 || shape == 721 || shape == 515 || shape == 1133;
+#define ANNF_FAST_INIT(PS, RL) fast_init_t_kernel<PS, RL><<<blocks, 256, 0, st>>>(A, B, nA, K, nat_pos, h->perm.as<int>(), prop, n_prop, m0)
+#define ANNF_FAST_PROP(PS, RL, ...) fast_prop_t_kernel<PS, RL><<<blocks, 256, 0, st>>>(__VA_ARGS__)
+  switch (shape) {
+    case 927: ANNF_FAST_INIT(9, 27); break;
+    case 721: ANNF_FAST_INIT(7, 21); break;
+    case 515: ANNF_FAST_INIT(5, 15); break;
+    case 1133: ANNF_FAST_INIT(11, 33); break;
+    default:
+      fast_init_kernel<<<blocks, 256, 0, st>>>(A, B, nA, K, nat_pos, h->perm.as<int>(), prop, n_prop, m0);
+  }
   ANNF_CHECK_LAUNCH();
   prof_mark(h, "fast_init", st);
   for (int it = 0; it < iters; ++it) {
     const int jump = 1;
     const int radius = std::max(1, 8 >> it);
-    fast_prop_kernel<<<blocks, 256, 0, st>>>(A, B, nA, jump, radius, 2, seed * 7919u + (uint32_t)it, m0, m1);
+    const uint32_t sd = seed * 7919u + (uint32_t)it;
+    if (special) {
+      switch (shape) {
+        case 927: ANNF_FAST_PROP(9, 27, A, B, nA, jump, radius, 2, sd, m0, m1); break;
+        case 721: ANNF_FAST_PROP(7, 21, A, B, nA, jump, radius, 2, sd, m0, m1); break;
+        case 515: ANNF_FAST_PROP(5, 15, A, B, nA, jump, radius, 2, sd, m0, m1); break;
+        default: ANNF_FAST_PROP(11, 33, A, B, nA, jump, radius, 2, sd, m0, m1); break;
+      }
+    } else {
+      fast_prop_kernel<<<blocks, 256, 0, st>>>(A, B, nA, jump, radius, 2, sd, m0, m1);
+    }
     ANNF_CHECK_LAUNCH();
     std::swap(m0, m1);
   }
+#undef ANNF_FAST_INIT
+#undef ANNF_FAST_PROP
   prof_mark(h, "fast_propagate", st);
   fast_final_kernel<<<blocks, 256, 0, st>>>(nA, m0, final_idx, dist_out);
   ANNF_CHECK_LAUNCH();
@@ -239,7 +401,8 @@ int raw_nn(const uint8_t* img_a, int ha, int wa, const uint8_t* img_b, int hb, i
            const int* qpix, int nq, unsigned long long* best, cudaStream_t st) {
   const int rowlen = psize * c, nw = psize * ((rowlen + 3) / 4);
   ANNF_REQUIRE(nw <= kRawMaxWords, "raw nearest neighbour: patch too large");
-  Img A{img_a, ha, wa, c, psize, wa - psize + 1}, B{img_b, hb, wb, c, psize, wb - psize + 1};
+  Img A{img_a, ha, wa, c, psize, wa - psize + 1, (long long)ha * wa * c};
+  Img B{img_b, hb, wb, c, psize, wb - psize + 1, (long long)hb * wb * c};
   fill_u64_kernel<<<ceil_div(nq, 256), 256, 0, st>>>(best, nq, ~0ull);
   ANNF_CHECK_LAUNCH();
   const int qt = ceil_div(nq, kRawQ);

@@ -58,9 +58,9 @@ struct annf_handle {
   // ---- query scratch ----
   annf::DevBuf nat_keys, nat_pos, lists, next_range, part_keys, part_pos;
   // ---- parallel form scratch ----
-  annf::DevBuf fast_buf, fast_nat;
+  annf::DevBuf fast_buf, fast_nat, tc_buf, pj_buf;
   // ---- pca scratch ----
-  annf::DevBuf gram, colsum, subset_t, cov, eigval, digits, meanproj, solver_ws, solver_info;
+  annf::DevBuf gram, colsum, subset_t, cov, eigval, digits, meanproj, solver_ws, solver_info, eig_ws;
   cusolverDnContext* solver = nullptr;
   // ---- device status word ----
   annf::DevBuf status;

@@ -1,0 +1,619 @@
+// leaf_tc.cu -- natural-leaf k nearest neighbours on the fifth-generation tensor cores (sm_103a).
+//
+// Queries are grouped by the leaf their descent reaches (counting sort on the leaf id). For each
+// leaf, the leaf's points (<= 256) and up to 128 of its queries are centred on the leaf's bounding
+// box midpoint, rounded to BF16 and staged in shared memory as K-major core-matrix tiles; one
+// tcgen05.mma (M = 128 queries, N = leaf points, K = 16 or 32 dims) per 16 dims leaves a . b in an
+// FP32 TMEM accumulator. Each thread owns one query (one TMEM lane): it reads its row with
+// tcgen05.ld and re-ranks with the exact FP32 distance (reference operation order) only the points
+// whose BF16 estimate passes a proven error bound (below), so the k-list written equals the FP32
+// leaf scan's. Centring keeps the BF16 products free of the cancellation that |a|^2 + |b|^2 - 2 a.b
+// suffers on uncentred reduced coordinates.
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+
+#include <algorithm>
+
+#include "common.cuh"
+#include "handle.cuh"
+#include "tc.cuh"
+#include "tree_walk.cuh"
+
+namespace annf {
+
+int num_sms();
+
+constexpr int kTcThreads = 128;                    // one warpgroup: thread t <-> TMEM lane t <-> query t
+constexpr long long kTcWaitCycles = 2000000000LL;  // ~1 s at 2 GHz: bound of every mbarrier wait
+
+// operand precision of the leaf tiles: BF16 (8-bit significand) or FP16 (11-bit significand)
+template <int PREC> struct TcPrec;
+template <> struct TcPrec<0> {
+  static constexpr float kEta = 0.001955f;  // 2^-9 (1 + 2^-10): BF16 rounding of the centred values
+  __device__ static float round(float x) { return __bfloat162float(__float2bfloat16_rn(x)); }
+  __device__ static uint32_t pack(float lo, float hi) {
+    __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+    return *reinterpret_cast<uint32_t*>(&v);
+  }
+  static constexpr uint32_t idesc(int M, int N) { return tc::idesc_bf16(M, N); }
+};
+template <> struct TcPrec<1> {
+  static constexpr float kEta = 0.000489f;  // 2^-11 (1 + 2^-10): FP16 rounding (values far below 65504)
+  __device__ static float round(float x) { return __half2float(__float2half_rn(x)); }
+  __device__ static uint32_t pack(float lo, float hi) {
+    __half2 v = __floats2half2_rn(lo, hi);
+    return *reinterpret_cast<uint32_t*>(&v);
+  }
+  static constexpr uint32_t idesc(int M, int N) { return tc::idesc_f16(M, N); }
+};
+
+__device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
+  __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+  return *reinterpret_cast<uint32_t*>(&v);
+}
+__device__ __forceinline__ float bf16_round(float x) { return __bfloat162float(__float2bfloat16_rn(x)); }
+
+// bounded wait on an mbarrier phase (clock-limited); false on time-out
+__device__ __forceinline__ bool mbar_wait_clock(uint64_t* mbar, uint32_t phase) {
+  const long long t0 = clock64();
+  while (!tc::mbar_try_wait(mbar, phase)) {
+    if (clock64() - t0 > kTcWaitCycles) return false;
+  }
+  return true;
+}
+
+// ---------------------------------------------------------------------------------------------
+// grouping queries by natural leaf
+// ---------------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) qleaf_kernel(TreeView<float> tv, const float* __restrict__ Q, long long nq,
+                                                    int* __restrict__ qleaf, int* __restrict__ cnt) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  unsigned char* p = smem_raw;
+  NodeCache<float> nc;
+  nc.carve(p, tv.depth);
+  if (smem_overrun(smem_raw, p, tv.status)) return;
+  nc.fill(tv);
+  __syncthreads();
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < nq; i += (long long)gridDim.x * blockDim.x) {
+    const int lf = descend(tv, nc, Q + i * tv.d);
+    qleaf[i] = lf;
+    atomicAdd(cnt + lf, 1);
+  }
+}
+
+// exclusive scan of cnt[L] into off[L+1] and cursor[L] (one CTA of 1024 threads)
+__global__ void __launch_bounds__(1024) leaf_scan_kernel(const int* __restrict__ cnt, int L, int* __restrict__ off,
+                                                         int* __restrict__ cursor) {
+  __shared__ int warp_tot[32];
+  const int per = (L + blockDim.x - 1) / blockDim.x;
+  const int b0 = threadIdx.x * per, b1 = min(L, b0 + per);
+  int s = 0;
+  for (int i = b0; i < b1; ++i) s += cnt[i];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  int x = s;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) warp_tot[w] = x;
+  __syncthreads();
+  if (w == 0) {
+    int t = warp_tot[lane];
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, t, o);
+      if (lane >= o) t += y;
+    }
+    warp_tot[lane] = t;
+  }
+  __syncthreads();
+  int run = x - s + (w ? warp_tot[w - 1] : 0);
+  for (int i = b0; i < b1; ++i) {
+    off[i] = run;
+    cursor[i] = run;
+    run += cnt[i];
+  }
+  if (threadIdx.x == blockDim.x - 1) off[L] = run;
+}
+
+__global__ void qscatter_kernel(const int* __restrict__ qleaf, long long nq, int* __restrict__ cursor,
+                                int* __restrict__ qorder) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < nq; i += (long long)gridDim.x * blockDim.x)
+    qorder[atomicAdd(cursor + qleaf[i], 1)] = (int)i;
+}
+
+// ---------------------------------------------------------------------------------------------
+// the tensor-core leaf kernel
+//
+// Selection with a proven BF16 error bound. With centre c, a' = bf16(a - c), b' = bf16(b - c):
+// |(a'-b') - (a-b)| <= eta = 2^-9 (|a - c| + R) (R bounds |b - c| over the leaf), so the BF16
+// distance E_j = |a' - b'_j| is within eta of the true D_j = |a - b_j|. If E_(k) is the k-th smallest
+// E, every point of the true (and of the FP32-computed) k nearest has E_j <= E_(k) + 2 eta, up to
+// FP32 rounding. Pass 1 finds E_(k) from the tile (est_j = |b'_j|^2 - 2 a'.b'_j = E_j^2 - |a'|^2);
+// pass 2 re-ranks exactly (FP32, reference order) every point whose estimate passes that bound.
+// The result equals the FP32 leaf scan; the exact work is usually a handful of points.
+// ---------------------------------------------------------------------------------------------
+template <int KM>
+__device__ __forceinline__ void sorted_insert(float (&dv)[KM], int (&iv)[KM], float v, int c) {
+  if (!(v < dv[KM - 1])) return;
+#pragma unroll
+  for (int j = KM - 1; j > 0; --j) {
+    const bool shift = v < dv[j - 1];
+    const bool here = !shift && v < dv[j];
+    if (shift) {
+      dv[j] = dv[j - 1];
+      iv[j] = iv[j - 1];
+    } else if (here) {
+      dv[j] = v;
+      iv[j] = c;
+    }
+  }
+  if (v < dv[0]) {
+    dv[0] = v;
+    iv[0] = c;
+  }
+}
+
+struct TcLeafArgs {
+  TreeView<float> tv;
+  const float* Q;
+  const int* qoff;    // [L+1] queries of leaf l: qorder[qoff[l] .. qoff[l+1])
+  const int* qorder;  // [nq]
+  int K;              // neighbours written per query (<= KM)
+  int npad;           // point rows staged per leaf (multiple of 16, >= largest leaf, <= 256)
+  int ncols;          // TMEM columns allocated (power of two >= max(32, npad))
+  int* out_pos;       // [nq*K] tree positions
+  int* work;          // leaf counter (zeroed before launch)
+};
+
+template <int KM, int KPAD, int PREC>
+__global__ void __launch_bounds__(kTcThreads) leaf_tc_kernel(TcLeafArgs a) {
+  using PR = TcPrec<PREC>;
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  const TreeView<float>& tv = a.tv;
+  const int d = tv.d, L = 1 << tv.depth, npad = a.npad, K = a.K;
+  // carve: A tile, B tile (core-matrix layouts), FP32 leaf points, norms, centre, barrier, TMEM slot
+  unsigned char* p = smem_raw;
+  unsigned char* sA = p;
+  p += kTcThreads * KPAD * 2;
+  unsigned char* sB = p;
+  p += (size_t)npad * KPAD * 2;
+  float* sP = reinterpret_cast<float*>(p);  // [npad][KPAD] FP32 leaf points (zero padded)
+  p += (size_t)npad * KPAD * 4;
+  float* sN = reinterpret_cast<float*>(p);
+  p += (size_t)npad * 4;
+  float* sC = reinterpret_cast<float*>(p);  // [KPAD] centre, then [KPAD] = R
+  p += (KPAD + 4) * 4;
+  p = reinterpret_cast<unsigned char*>(((uintptr_t)p + 15) & ~uintptr_t(15));
+  uint64_t* mbar = reinterpret_cast<uint64_t*>(p);
+  p += 8;
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(p);
+  p += 8;
+  int* sflag = reinterpret_cast<int*>(p);  // [0] leaf, [1] abort
+  p += 8;
+  if (smem_overrun(smem_raw, p, tv.status)) return;
+
+  const int tid = threadIdx.x, warp = tid >> 5;
+  if (warp == 0) {
+    tc::tmem_alloc(tslot, (uint32_t)a.ncols);
+    tc::tmem_relinquish();
+  }
+  if (tid == 0) {
+    tc::mbar_init(mbar, 1);
+    tc::mbar_fence_init();
+    sflag[1] = 0;
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = *tslot;
+  const uint32_t idesc = PR::idesc(128, npad);
+  const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
+  uint32_t phase = 0;
+  bool aborted = false;
+  const bool vec4 = (d & 3) == 0;
+
+  for (;;) {
+    __syncthreads();  // every thread has read the previous leaf id
+    if (tid == 0) sflag[0] = atomicAdd(a.work, 1);
+    __syncthreads();
+    const int l = sflag[0];
+    if (l >= L) break;
+    const int qb = __ldg(a.qoff + l), qe = __ldg(a.qoff + l + 1);
+    if (qb == qe) continue;  // uniform: every thread read the same leaf
+    const int pb = __ldg(tv.leaf_begin + l);
+    int np = __ldg(tv.leaf_begin + l + 1) - pb;
+    if (np > npad) {
+      if (tid == 0) atomicOr(tv.status, DEV_BAD_LEAF);
+      np = npad;
+    }
+    // centre (box midpoint) and half-diagonal R of the leaf box
+    if (tid < 32) {
+      float r2 = 0.f;
+      for (int j = tid; j < KPAD; j += 32) {
+        float c = 0.f;
+        if (j < d) {
+          const float lo = __ldg(tv.leaf_box + (size_t)l * 2 * d + j), hi = __ldg(tv.leaf_box + (size_t)l * 2 * d + d + j);
+          c = 0.5f * (lo + hi);
+          const float e = 0.5f * (hi - lo);
+          r2 = fmaf(e, e, r2);
+        }
+        sC[j] = c;
+      }
+#pragma unroll
+      for (int o = 16; o; o >>= 1) r2 += __shfl_xor_sync(0xffffffffu, r2, o);
+      if (tid == 0) sC[KPAD] = sqrtf(r2) * 1.000001f + 1e-30f;
+    }
+    __syncthreads();
+    // the leaf's points: FP32 copy, BF16 centred tile, BF16 norms
+    for (int r = tid; r < npad; r += kTcThreads) {
+      float f[KPAD];
+      const float* src = tv.pts + (size_t)(pb + r) * d;
+      if (r < np && vec4) {
+#pragma unroll
+        for (int j = 0; j < KPAD; j += 4) {
+          if (j < d) {
+            const float4 v = __ldg(reinterpret_cast<const float4*>(src + j));
+            f[j] = v.x;
+            f[j + 1] = v.y;
+            f[j + 2] = v.z;
+            f[j + 3] = v.w;
+          } else {
+            f[j] = f[j + 1] = f[j + 2] = f[j + 3] = 0.f;
+          }
+        }
+      } else {
+#pragma unroll
+        for (int j = 0; j < KPAD; ++j) f[j] = (r < np && j < d) ? __ldg(src + j) : 0.f;
+      }
+      float nrm = 0.f;
+#pragma unroll
+      for (int k8 = 0; k8 < KPAD; k8 += 8) {
+        float v[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          const int j = k8 + u;
+          v[u] = (r < np && j < d) ? PR::round(f[j] - sC[j]) : 0.f;
+          nrm = fmaf(v[u], v[u], nrm);
+        }
+        uint4 w;
+        w.x = PR::pack(v[0], v[1]);
+        w.y = PR::pack(v[2], v[3]);
+        w.z = PR::pack(v[4], v[5]);
+        w.w = PR::pack(v[6], v[7]);
+        *reinterpret_cast<uint4*>(sB + tc::core_offset(r, k8, KPAD)) = w;
+      }
+#pragma unroll
+      for (int j = 0; j < KPAD; j += 4)
+        *reinterpret_cast<float4*>(sP + r * KPAD + j) = make_float4(f[j], f[j + 1], f[j + 2], f[j + 3]);
+      sN[r] = r < np ? nrm : FLT_MAX;
+    }
+    const float R = sC[KPAD];
+    for (int q0 = qb; q0 < qe; q0 += kTcThreads) {
+      const int qi = (q0 + tid < qe) ? __ldg(a.qorder + q0 + tid) : -1;
+      float qf[KPAD];
+      if (qi >= 0 && vec4) {
+#pragma unroll
+        for (int j = 0; j < KPAD; j += 4) {
+          if (j < d) {
+            const float4 v = __ldg(reinterpret_cast<const float4*>(a.Q + (size_t)qi * d + j));
+            qf[j] = v.x;
+            qf[j + 1] = v.y;
+            qf[j + 2] = v.z;
+            qf[j + 3] = v.w;
+          } else {
+            qf[j] = qf[j + 1] = qf[j + 2] = qf[j + 3] = 0.f;
+          }
+        }
+      } else {
+#pragma unroll
+        for (int j = 0; j < KPAD; ++j) qf[j] = (qi >= 0 && j < d) ? __ldg(a.Q + (size_t)qi * d + j) : 0.f;
+      }
+      float a2 = 0.f, ac2 = 0.f, amax = 0.f;
+#pragma unroll
+      for (int k8 = 0; k8 < KPAD; k8 += 8) {
+        float v[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          const float t = (k8 + u < d) ? qf[k8 + u] - sC[k8 + u] : 0.f;
+          ac2 = fmaf(t, t, ac2);
+          amax = fmaxf(amax, fabsf(t));
+          v[u] = (qi >= 0) ? PR::round(t) : 0.f;
+          a2 = fmaf(v[u], v[u], a2);
+        }
+        uint4 w;
+        w.x = PR::pack(v[0], v[1]);
+        w.y = PR::pack(v[2], v[3]);
+        w.z = PR::pack(v[4], v[5]);
+        w.w = PR::pack(v[6], v[7]);
+        *reinterpret_cast<uint4*>(sA + tc::core_offset(tid, k8, KPAD)) = w;
+      }
+      tc::fence_async_smem();
+      tc::fence_before_sync();
+      __syncthreads();
+      if (tid == 0) {
+        tc::fence_after_sync();
+#pragma unroll
+        for (int kk = 0; kk < KPAD / 16; ++kk) {
+          const uint64_t ad = tc::sdesc(sA + kk * 256, 128, (KPAD / 8) * 128);
+          const uint64_t bd = tc::sdesc(sB + kk * 256, 128, (KPAD / 8) * 128);
+          tc::mma_bf16(tmem, ad, bd, idesc, kk > 0 ? 1u : 0u);
+        }
+        tc::mma_commit(mbar);
+      }
+      if (!mbar_wait_clock(mbar, phase)) sflag[1] = 1;
+      phase ^= 1u;
+      __syncthreads();
+      if (sflag[1]) {
+        aborted = true;
+        break;
+      }
+      tc::fence_after_sync();
+      // pass 1: the KM smallest estimates
+      float ev[KM];
+      int ei[KM];
+#pragma unroll
+      for (int j = 0; j < KM; ++j) {
+        ev[j] = FLT_MAX;
+        ei[j] = -1;
+      }
+      for (int c0 = 0; c0 < npad; c0 += 16) {
+        uint32_t r[16];
+        tc::tmem_ld16(trow + (uint32_t)c0, r);
+        tc::tmem_wait_ld();
+        if (qi >= 0) {
+#pragma unroll
+          for (int j = 0; j < 16; ++j) {
+            const float est = fmaf(-2.f, __uint_as_float(r[j]), sN[c0 + j]);
+            if (c0 + j < np) sorted_insert<KM>(ev, ei, est, c0 + j);
+          }
+        }
+      }
+      // bound: est_j <= (sqrt(est_(k) + |a'|^2 + s) + 2 eta)^2 (1 + 4e-6) - |a'|^2 + s
+      const float eta = PR::kEta * (sqrtf(ac2) * 1.000001f + R);  // rounding bound x (|a-c| + R)
+      const float slack = 1.53e-5f * (a2 + R * R * 1.01f);        // ~2^-16 (|a'|^2 + |b'|^2 max)
+      float evk = FLT_MAX;
+#pragma unroll
+      for (int j = 0; j < KM; ++j)
+        if (j == K - 1) evk = ev[j];
+      const float ek = evk >= FLT_MAX ? FLT_MAX : sqrtf(fmaxf(evk + a2 + slack, 0.f));
+      // FP16 cannot hold centred values beyond its range: such queries and leaves take every point
+      const bool unsafe = PREC == 1 && (amax > 60000.f || R > 60000.f);
+      const float tau = (ek >= FLT_MAX || unsafe) ? FLT_MAX : (ek + 2.f * eta) * (ek + 2.f * eta) * 1.000004f - a2 + slack;
+      // pass 2: exact FP32 distance (reference order) of every point passing the bound
+      float xv[KM];
+      int xi[KM];
+#pragma unroll
+      for (int j = 0; j < KM; ++j) {
+        xv[j] = FLT_MAX;
+        xi[j] = -1;
+      }
+      for (int c0 = 0; c0 < npad; c0 += 16) {
+        uint32_t r[16];
+        tc::tmem_ld16(trow + (uint32_t)c0, r);
+        tc::tmem_wait_ld();
+        if (qi >= 0) {
+          unsigned pass = 0;
+#pragma unroll
+          for (int j = 0; j < 16; ++j) {
+            const float est = fmaf(-2.f, __uint_as_float(r[j]), sN[c0 + j]);
+            pass |= (c0 + j < np && (est <= tau || tau == FLT_MAX)) ? (1u << j) : 0u;
+          }
+          while (pass) {
+            const int col = c0 + __ffs(pass) - 1;
+            pass &= pass - 1;
+            {
+              const float* pp = sP + col * KPAD;
+              float s = 0.f;
+#pragma unroll
+              for (int u = 0; u < KPAD; ++u) {
+                if (u < d) {
+                  const float t = __fsub_rn(qf[u], pp[u]);
+                  s = __fadd_rn(s, __fmul_rn(t, t));
+                }
+              }
+              sorted_insert<KM>(xv, xi, s, col);
+            }
+          }
+        }
+      }
+      if (qi >= 0) {
+        int* out = a.out_pos + (size_t)qi * K;
+        const int first = xi[0] >= 0 ? xi[0] : 0;
+#pragma unroll
+        for (int t = 0; t < KM; ++t)
+          if (t < K) out[t] = min(max(pb + (xi[t] >= 0 ? xi[t] : first), 0), tv.n - 1);
+      }
+      tc::fence_before_sync();
+      __syncthreads();
+    }
+    if (aborted) break;
+    __syncthreads();
+  }
+  if (aborted) {  // let the MMA in flight finish (bounded) before the columns are freed
+    if (tid == 0) atomicOr(tv.status, DEV_TC_TIMEOUT);
+    mbar_wait_clock(mbar, phase);
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) tc::tmem_dealloc(tmem, (uint32_t)a.ncols);
+}
+
+template <int KM, int KPAD, int PREC>
+static int launch_leaf_tc(const TcLeafArgs& args, size_t smem, int grid, cudaStream_t st) {
+  ANNF_CUDA_TRY(cudaFuncSetAttribute(leaf_tc_kernel<KM, KPAD, PREC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)smem));
+  leaf_tc_kernel<KM, KPAD, PREC><<<grid, kTcThreads, smem, st>>>(args);
+  ANNF_CHECK_LAUNCH();
+  return ANNF_OK;
+}
+
+static int next_pow2(int x) {
+  int p = 1;
+  while (p < x) p <<= 1;
+  return p;
+}
+
+// true when the tree's shape fits the tensor-core kernel (FP32 points, d <= 32, leaves <= 256)
+bool leaf_tc_supported(const annf_handle* h, int K) {
+  return h->real_type == ANNF_REAL_F32 && h->d >= 1 && h->d <= 32 && h->max_leaf >= 1 && h->max_leaf <= 256 &&
+         K >= 1 && K <= 32;
+}
+
+int natural_knn_tc(annf_handle* h, const float* Q, long long nq, int K, int prec, int* out_pos, cudaStream_t st) {
+  ANNF_REQUIRE(leaf_tc_supported(h, K), "tensor-core leaf kNN: unsupported tree shape");
+  ANNF_REQUIRE(nq <= 0x7fffffffLL, "tensor-core leaf kNN: too many queries");
+  const int L = 1 << h->depth;
+  TreeView<float> tv;
+  tv.n = h->n;
+  tv.d = h->d;
+  tv.depth = h->depth;
+  tv.leaf_bits = h->leaf_bits;
+  tv.pts = h->pts.as<float>();
+  tv.perm = h->perm.as<int>();
+  tv.node_axis = h->node_axis.as<int>();
+  tv.node_split = h->node_split.as<float>();
+  tv.leaf_begin = h->leaf_begin.as<int>();
+  tv.point_leaf = h->point_leaf.as<int>();
+  tv.status = h->status.as<unsigned>();
+  tv.leaf_box = h->leaf_box.as<float>();
+  // scratch: qleaf[nq], qorder[nq], cnt[L], off[L+1], cursor[L], work counter
+  const size_t need = ((size_t)2 * nq + 3 * (size_t)L + 8) * sizeof(int);
+  ANNF_ENSURE(h->tc_buf, need);
+  int* qleaf = h->tc_buf.as<int>();
+  int* qorder = qleaf + nq;
+  int* cnt = qorder + nq;
+  int* off = cnt + L;
+  int* cursor = off + L + 1;
+  int* work = cursor + L;
+  ANNF_CUDA_TRY(cudaMemsetAsync(cnt, 0, (size_t)L * sizeof(int), st));
+  ANNF_CUDA_TRY(cudaMemsetAsync(work, 0, sizeof(int), st));
+  const size_t ncs = NodeCache<float>::bytes(h->depth);
+  ANNF_CUDA_TRY(cudaFuncSetAttribute(qleaf_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ncs));
+  const int blocks = (int)std::min<long long>(ceil_div(nq, 256), 8LL * num_sms());
+  qleaf_kernel<<<blocks, 256, ncs, st>>>(tv, Q, nq, qleaf, cnt);
+  ANNF_CHECK_LAUNCH();
+  leaf_scan_kernel<<<1, 1024, 0, st>>>(cnt, L, off, cursor);
+  ANNF_CHECK_LAUNCH();
+  qscatter_kernel<<<blocks, 256, 0, st>>>(qleaf, nq, cursor, qorder);
+  ANNF_CHECK_LAUNCH();
+  prof_mark(h, "tc_group", st);
+
+  TcLeafArgs args;
+  args.tv = tv;
+  args.Q = Q;
+  args.qoff = off;
+  args.qorder = qorder;
+  args.K = K;
+  args.npad = (h->max_leaf + 15) / 16 * 16;
+  args.ncols = std::max(32, next_pow2(args.npad));
+  args.out_pos = out_pos;
+  args.work = work;
+  const int kpad = h->d <= 16 ? 16 : 32;
+  const size_t carve = (size_t)kTcThreads * kpad * 2 + (size_t)args.npad * kpad * 2 + (size_t)args.npad * kpad * 4 +
+                       (size_t)args.npad * 4 + (kpad + 4) * 4 + 16 + 24 + 64;
+  // at most 512 / ncols CTAs may hold TMEM on one SM: pad the shared memory so no more fit
+  const int per_sm = std::max(1, 512 / args.ncols);
+  const size_t cap = 227 * 1024;
+  const size_t floor_smem = (size_t)233472 / (per_sm + 1) + 1024;
+  const size_t smem = std::min(cap, std::max(carve, floor_smem));
+  ANNF_REQUIRE(carve <= cap, "tensor-core leaf kNN: leaf too large for shared memory");
+  const int grid = std::max(1, std::min(per_sm * num_sms(), L));
+  const int km = K <= 1 ? 1 : K <= 4 ? 4 : K <= 8 ? 8 : K <= 16 ? 16 : 32;
+  int rc;
+#define ANNF_TC_LAUNCH(KMV)                                                                            \
+  case KMV:                                                                                            \
+    if (prec == 0)                                                                                     \
+      rc = kpad == 16 ? launch_leaf_tc<KMV, 16, 0>(args, smem, grid, st) : launch_leaf_tc<KMV, 32, 0>(args, smem, grid, st); \
+    else                                                                                               \
+      rc = kpad == 16 ? launch_leaf_tc<KMV, 16, 1>(args, smem, grid, st) : launch_leaf_tc<KMV, 32, 1>(args, smem, grid, st); \
+    break;
+  switch (km) {
+    ANNF_TC_LAUNCH(1)
+    ANNF_TC_LAUNCH(4)
+    ANNF_TC_LAUNCH(8)
+    ANNF_TC_LAUNCH(16)
+    ANNF_TC_LAUNCH(32)
+    default:
+      rc = ANNF_ERR_UNSUPPORTED;
+  }
+#undef ANNF_TC_LAUNCH
+  return rc;
+}
+
+// ---------------------------------------------------------------------------------------------
+// single-tile check of the tcgen05 path: D[128][N] = A[128][K] . B[N][K]^T (BF16 in, FP32 out)
+// ---------------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(kTcThreads) tc_tile_kernel(const uint16_t* __restrict__ A, const uint16_t* __restrict__ B,
+                                                             int N, int K, int ncols, float* __restrict__ D,
+                                                             unsigned* status) {
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  unsigned char* sA = smem_raw;
+  unsigned char* sB = sA + (size_t)128 * K * 2;
+  uint64_t* mbar = reinterpret_cast<uint64_t*>(sB + (size_t)N * K * 2);
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(mbar + 1);
+  int* sflag = reinterpret_cast<int*>(tslot + 2);
+  if (smem_overrun(smem_raw, sflag + 2, status)) return;
+  const int tid = threadIdx.x, warp = tid >> 5;
+  if (warp == 0) {
+    tc::tmem_alloc(tslot, (uint32_t)ncols);
+    tc::tmem_relinquish();
+  }
+  if (tid == 0) {
+    tc::mbar_init(mbar, 1);
+    tc::mbar_fence_init();
+    sflag[0] = 0;
+  }
+  for (int e = tid; e < 128 * (K / 8); e += kTcThreads) {
+    const int r = e / (K / 8), k8 = (e - r * (K / 8)) * 8;
+    *reinterpret_cast<uint4*>(sA + tc::core_offset(r, k8, K)) = *reinterpret_cast<const uint4*>(A + (size_t)r * K + k8);
+  }
+  for (int e = tid; e < N * (K / 8); e += kTcThreads) {
+    const int r = e / (K / 8), k8 = (e - r * (K / 8)) * 8;
+    *reinterpret_cast<uint4*>(sB + tc::core_offset(r, k8, K)) = *reinterpret_cast<const uint4*>(B + (size_t)r * K + k8);
+  }
+  tc::fence_async_smem();
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = *tslot;
+  if (tid == 0) {
+    const uint32_t idesc = tc::idesc_bf16(128, N);
+    for (int kk = 0; kk < K / 16; ++kk)
+      tc::mma_bf16(tmem, tc::sdesc(sA + kk * 256, 128, (K / 8) * 128), tc::sdesc(sB + kk * 256, 128, (K / 8) * 128),
+                   idesc, kk > 0 ? 1u : 0u);
+    tc::mma_commit(mbar);
+  }
+  if (!mbar_wait_clock(mbar, 0)) sflag[0] = 1;
+  __syncthreads();
+  if (sflag[0]) {
+    if (tid == 0) atomicOr(status, DEV_TC_TIMEOUT);
+    mbar_wait_clock(mbar, 0);
+  } else {
+    tc::fence_after_sync();
+    const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
+    for (int c0 = 0; c0 < N; c0 += 16) {
+      uint32_t r[16];
+      tc::tmem_ld16(trow + (uint32_t)c0, r);
+      tc::tmem_wait_ld();
+#pragma unroll
+      for (int j = 0; j < 16; ++j) D[(size_t)tid * N + c0 + j] = __uint_as_float(r[j]);
+    }
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) tc::tmem_dealloc(tmem, (uint32_t)ncols);
+}
+
+int tc_tile(const uint16_t* A, const uint16_t* B, int N, int K, float* D, unsigned* status, cudaStream_t st) {
+  ANNF_REQUIRE(N >= 16 && N <= 256 && N % 16 == 0, "annf_tc_tile: N must be a multiple of 16 in [16, 256]");
+  ANNF_REQUIRE(K >= 16 && K <= 256 && K % 16 == 0, "annf_tc_tile: K must be a multiple of 16 in [16, 256]");
+  const size_t smem = (size_t)128 * K * 2 + (size_t)N * K * 2 + 64;
+  ANNF_CUDA_TRY(cudaFuncSetAttribute(tc_tile_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  tc_tile_kernel<<<1, kTcThreads, smem, st>>>(A, B, N, K, std::max(32, next_pow2(N)), D, status);
+  ANNF_CHECK_LAUNCH();
+  return ANNF_OK;
+}
+
+}  // namespace annf

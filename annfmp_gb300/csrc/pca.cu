@@ -393,9 +393,12 @@ __global__ void __launch_bounds__(kPTW * kPTH) project_kernel(const uint8_t* __r
 
 static int round_up(int a, int b) { return (a + b - 1) / b * b; }
 
+int subspace_block(int P, int ncomp);
+int eig_top_subspace(annf_handle* h, const double* C, int P, int ncomp, int iters, double* comps, cudaStream_t st);
+
 int pca_fit(annf_handle* h, const uint8_t* img_a, int ha, int wa, const int* pos_a, int n_a, const uint8_t* img_b,
             int hb, int wb, const int* pos_b, int n_b, int c, int psize, int ncomp, double* comps, double* mean,
-            cudaStream_t st) {
+            int solver, cudaStream_t st) {
   (void)ha;
   (void)hb;
   const int P = psize * psize * c;
@@ -433,6 +436,11 @@ int pca_fit(annf_handle* h, const uint8_t* img_a, int ha, int wa, const int* pos
   cov_finish_kernel<<<std::min(ceil_div((long long)P * P, 256), 1024), 256, 0, st>>>(
       h->gram.as<unsigned long long>(), F, P, h->cov.as<double>(), mean);
   ANNF_CHECK_LAUNCH();
+  if (solver > 0 && subspace_block(P, ncomp) > 0) {  // leading components only (approximate forms)
+    int rc = eig_top_subspace(h, h->cov.as<double>(), P, ncomp, solver, comps, st);
+    prof_mark(h, "pca_eigh", st);
+    return rc;
+  }
   if (!h->solver) {
     cusolverDnHandle_t sh;
     if (cusolverDnCreate(&sh) != CUSOLVER_STATUS_SUCCESS) {

@@ -1,0 +1,233 @@
+// proj_tc.cu -- patch extraction fused with the PCA projection on the tensor cores (sm_103a).
+//
+// For the approximate NNF forms: every psize x psize x c patch of an image times the BF16-rounded
+// components, FP32 accumulation, minus the projected mean. One tile = 128 consecutive patches of one
+// row: the psize image rows they cover are staged in shared memory, each thread pair expands one
+// patch into the K-major BF16 A tile (core-matrix layout, K = P rounded up to 16), and tcgen05.mma
+// (M = 128, N = components rounded up to 16) accumulates in TMEM; the epilogue reads TMEM, subtracts
+// the mean term and writes FP32 reduced patches. Pixel values 0..255 are exact in BF16 and every
+// product is exact in FP32, so the only rounding beyond FP32 summation is that of the components.
+// The exact projection (pca.cu) remains the drop-in path.
+#include <cuda_bf16.h>
+
+#include <algorithm>
+
+#include "common.cuh"
+#include "handle.cuh"
+#include "tc.cuh"
+
+namespace annf {
+
+int num_sms();
+
+constexpr int kPjThreads = 256;  // two threads per patch row of the tile
+constexpr long long kPjWaitCycles = 2000000000LL;
+
+__device__ __forceinline__ uint32_t pj_pack(float lo, float hi) {
+  __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+  return *reinterpret_cast<uint32_t*>(&v);
+}
+
+__device__ __forceinline__ bool pj_wait(uint64_t* mbar, uint32_t phase) {
+  const long long t0 = clock64();
+  while (!tc::mbar_try_wait(mbar, phase)) {
+    if (clock64() - t0 > kPjWaitCycles) return false;
+  }
+  return true;
+}
+
+// B operand [npad][kpad] BF16 row-major (zero padded) and the FP32 mean term m_j = sum_k bf16(c_jk) mean_k
+__global__ void pj_prep_kernel(const double* __restrict__ comps, const double* __restrict__ mean, int d, int P,
+                               int npad, int kpad, uint16_t* __restrict__ bmat, float* __restrict__ mterm) {
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < npad * kpad; e += gridDim.x * blockDim.x) {
+    const int j = e / kpad, k = e - j * kpad;
+    const float v = (j < d && k < P) ? (float)comps[(size_t)j * P + k] : 0.f;
+    __nv_bfloat16 b = __float2bfloat16_rn(v);
+    bmat[e] = *reinterpret_cast<uint16_t*>(&b);
+  }
+  if (blockIdx.x == 0) {
+    for (int j = threadIdx.x; j < d; j += blockDim.x) {
+      double s = 0.0;
+      for (int k = 0; k < P; ++k)
+        s += (double)__bfloat162float(__float2bfloat16_rn((float)comps[(size_t)j * P + k])) * mean[k];
+      mterm[j] = (float)s;
+    }
+  }
+}
+
+template <int NPAD>
+__global__ void __launch_bounds__(kPjThreads) project_tc_kernel(const uint8_t* __restrict__ img, int H, int W, int C,
+                                                                int psize, int d, int kpad,
+                                                                const uint16_t* __restrict__ bmat,
+                                                                const float* __restrict__ mterm, float* __restrict__ out,
+                                                                unsigned* status) {
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  const int P = psize * psize * C;
+  const int ncols = W - psize + 1, nrows = H - psize + 1;
+  const int tiles_x = (ncols + 127) / 128;
+  const long long ntiles = (long long)tiles_x * nrows;
+  const int sw = ((128 + psize - 1) * C + 15) & ~15;  // staged row pitch (bytes)
+  unsigned char* p = smem_raw;
+  unsigned char* sA = p;
+  p += (size_t)128 * kpad * 2;
+  unsigned char* sB = p;
+  p += (size_t)NPAD * kpad * 2;
+  uint8_t* sI = p;
+  p += (size_t)psize * sw;
+  p = reinterpret_cast<unsigned char*>(((uintptr_t)p + 3) & ~uintptr_t(3));
+  int16_t* koff = reinterpret_cast<int16_t*>(p);
+  p += (size_t)kpad * 2;
+  p = reinterpret_cast<unsigned char*>(((uintptr_t)p + 15) & ~uintptr_t(15));
+  uint64_t* mbar = reinterpret_cast<uint64_t*>(p);
+  p += 8;
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(p);
+  p += 8;
+  int* sflag = reinterpret_cast<int*>(p);
+  p += 8;
+  if (smem_overrun(smem_raw, p, status)) return;
+  const int tid = threadIdx.x, warp = tid >> 5;
+  if (warp == 0) {
+    tc::tmem_alloc(tslot, 32);
+    tc::tmem_relinquish();
+  }
+  if (tid == 0) {
+    tc::mbar_init(mbar, 1);
+    tc::mbar_fence_init();
+    sflag[0] = 0;
+  }
+  // components tile (core layout) and the patch-element offset table
+  for (int e = tid; e < NPAD * (kpad / 8); e += kPjThreads) {
+    const int r = e / (kpad / 8), k8 = (e - r * (kpad / 8)) * 8;
+    *reinterpret_cast<uint4*>(sB + tc::core_offset(r, k8, kpad)) =
+        *reinterpret_cast<const uint4*>(bmat + (size_t)r * kpad + k8);
+  }
+  for (int k = tid; k < kpad; k += kPjThreads) {
+    int v = -1;
+    if (k < P) {
+      const int r = k / (psize * C), rem = k - r * psize * C;
+      v = r * sw + rem;  // rem = c * C + ch: contiguous within the staged row
+    }
+    koff[k] = (int16_t)v;
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = *tslot;
+  const uint32_t idesc = tc::idesc_bf16(128, NPAD);
+  const int row = tid & 127, half = tid >> 7;  // patch row of the tile; K half (expansion) / column half
+  const int ngrp = kpad / 8;
+  uint32_t phase = 0;
+  for (long long t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const int y = (int)(t / tiles_x), x0 = (int)(t - (long long)y * tiles_x) * 128;
+    const int np = min(128, ncols - x0);
+    const int span = (np + psize - 1) * C;
+    // stage the psize image rows of the tile
+    for (int e = tid; e < psize * span; e += kPjThreads) {
+      const int r = e / span, b = e - r * span;
+      sI[r * sw + b] = img[((size_t)(y + r) * W + x0) * C + b];
+    }
+    __syncthreads();
+    // expand: this thread's half of the K groups of patch `row`
+    const int g0 = half ? ngrp / 2 : 0, g1 = half ? ngrp : ngrp / 2;
+    const int base = row * C;
+    for (int g = g0; g < g1; ++g) {
+      float v[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int o = koff[g * 8 + u];
+        v[u] = (o >= 0 && row < np) ? (float)sI[base + o] : 0.f;
+      }
+      uint4 w;
+      w.x = pj_pack(v[0], v[1]);
+      w.y = pj_pack(v[2], v[3]);
+      w.z = pj_pack(v[4], v[5]);
+      w.w = pj_pack(v[6], v[7]);
+      *reinterpret_cast<uint4*>(sA + tc::core_offset(row, g * 8, kpad)) = w;
+    }
+    tc::fence_async_smem();
+    tc::fence_before_sync();
+    __syncthreads();
+    if (tid == 0) {
+      tc::fence_after_sync();
+      for (int kk = 0; kk < kpad / 16; ++kk)
+        tc::mma_bf16(tmem, tc::sdesc(sA + kk * 256, 128, (kpad / 8) * 128),
+                     tc::sdesc(sB + kk * 256, 128, (kpad / 8) * 128), idesc, kk > 0 ? 1u : 0u);
+      tc::mma_commit(mbar);
+    }
+    if (!pj_wait(mbar, phase)) sflag[0] = 1;
+    phase ^= 1u;
+    __syncthreads();
+    if (sflag[0]) break;
+    tc::fence_after_sync();
+    // epilogue: warp w reads lanes 32 (w & 3).. and column half (w >> 2)
+    {
+      constexpr int HC = NPAD / 2;
+      const int lane_row = (warp & 3) * 32 + (tid & 31);
+      const int c0 = (warp >> 2) * HC;
+      const uint32_t taddr = tmem + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)c0;
+      uint32_t r[HC];
+      if constexpr (HC == 8) {
+        tc::tmem_ld8(taddr, r);
+      } else {
+        uint32_t (&r16)[16] = *reinterpret_cast<uint32_t(*)[16]>(r);
+        tc::tmem_ld16(taddr, r16);
+      }
+      tc::tmem_wait_ld();
+      if (lane_row < np) {
+        float* dst = out + ((size_t)y * ncols + x0 + lane_row) * d;
+#pragma unroll
+        for (int j = 0; j < HC; ++j)
+          if (c0 + j < d) dst[c0 + j] = __uint_as_float(r[j]) - mterm[c0 + j];
+      }
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+  }
+  if (sflag[0]) {
+    if (tid == 0) atomicOr(status, DEV_TC_TIMEOUT);
+    pj_wait(mbar, phase ^ 1u);
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) tc::tmem_dealloc(tmem, 32);
+}
+
+bool project_tc_supported(int psize, int c, int ncomp) {
+  const int P = psize * psize * c;
+  return P >= 1 && P <= 256 && ncomp >= 1 && ncomp <= 32 && (128 + psize - 1) * c <= 4096;
+}
+
+int project_tc(annf_handle* h, const uint8_t* img, int H, int W, int c, int psize, const double* comps,
+               const double* mean, int ncomp, float* out, cudaStream_t st) {
+  ANNF_REQUIRE(project_tc_supported(psize, c, ncomp), "annf_project_bf16: patch or components too large");
+  const int P = psize * psize * c;
+  const int kpad = (P + 15) / 16 * 16;
+  const int npad = ncomp <= 16 ? 16 : 32;
+  ANNF_ENSURE(h->pj_buf, (size_t)npad * kpad * 2 + 64 * sizeof(float) + 256);
+  uint16_t* bmat = h->pj_buf.as<uint16_t>();
+  float* mterm = reinterpret_cast<float*>(reinterpret_cast<unsigned char*>(h->pj_buf.p) + (((size_t)npad * kpad * 2 + 255) & ~size_t(255)));
+  prof_mark(h, "project:begin", st);
+  pj_prep_kernel<<<std::max(1, std::min(ceil_div(npad * kpad, 256), 64)), 256, 0, st>>>(comps, mean, ncomp, P, npad, kpad,
+                                                                                         bmat, mterm);
+  ANNF_CHECK_LAUNCH();
+  const int sw = ((128 + psize - 1) * c + 15) & ~15;
+  const size_t smem = (size_t)128 * kpad * 2 + (size_t)npad * kpad * 2 + (size_t)psize * sw + 4 + (size_t)kpad * 2 + 16 + 24 + 64;
+  ANNF_REQUIRE(smem <= 227 * 1024, "annf_project_bf16: tile too large for shared memory");
+  const long long ntiles = (long long)((W - psize + 1 + 127) / 128) * (H - psize + 1);
+  // TMEM: 32 columns per CTA, so any residency fits; two CTAs per SM by shared memory at P = 243
+  const int grid = (int)std::max(1LL, std::min<long long>(ntiles, 4LL * num_sms()));
+  if (npad == 16) {
+    ANNF_CUDA_TRY(cudaFuncSetAttribute(project_tc_kernel<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    project_tc_kernel<16><<<grid, kPjThreads, smem, st>>>(img, H, W, c, psize, ncomp, kpad, bmat, mterm, out,
+                                                         h->status.as<unsigned>());
+  } else {
+    ANNF_CUDA_TRY(cudaFuncSetAttribute(project_tc_kernel<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    project_tc_kernel<32><<<grid, kPjThreads, smem, st>>>(img, H, W, c, psize, ncomp, kpad, bmat, mterm, out,
+                                                         h->status.as<unsigned>());
+  }
+  ANNF_CHECK_LAUNCH();
+  prof_mark(h, "project", st);
+  return ANNF_OK;
+}
+
+}  // namespace annf

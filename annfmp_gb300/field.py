@@ -64,12 +64,25 @@ class ANNFieldPropKDTreeGB300:
 
     def __init__(self, n_neighbors=3, psize=8, dim_reduced=5, n_subset=1000, leaf_size=64, n_jobs=-1,
                  propagate=True, select_best_nn=True, float_type="float", verbose=1, seed=0, device=0,
-                 form="plain", iters=4, proposal=None):
+                 form="plain", iters=4, proposal=None, pca_solver=None, pca_iters=10, leaf_precision=None,
+                 projection=None):
         """Reference parameters, plus: ``form`` "plain" (the reference's row-sequential method,
         the drop-in) or "parallel" (natural-leaf candidates + proposals + parallel propagation,
         every candidate checked by exact raw-patch distance); ``iters`` propagation passes of the
         parallel form; ``proposal`` an object with ``propose(A, B, psize) -> int32 [n_A, P]`` B
-        indices (e.g. ``annfmp_gb300.proposal.ProposalNet``) feeding the parallel form."""
+        indices (e.g. ``annfmp_gb300.proposal.ProposalNet``) feeding the parallel form;
+        ``pca_solver`` "exact" (full FP64 eigendecomposition, the reference's result) or
+        "subspace" (leading components only: FP32 subspace iteration, ``pca_iters`` steps, with
+        an FP64 Rayleigh-Ritz step); None picks "exact" for the plain form, "subspace" otherwise;
+        ``leaf_precision`` of the parallel form's natural-leaf distances: "bf16" (tensor-core tiles,
+        exact FP32 re-rank of the survivors of a proven BF16 error bound; the default) or "fp32";
+        ``projection`` "exact" (the FP64 result rounded once, the reference's) or "bf16" (BF16
+        components on the tensor cores, FP32 sums); None picks "exact" for the plain form, "bf16"
+        otherwise when the shapes allow it."""
+        self.leaf_precision = leaf_precision
+        self.projection = projection
+        self.pca_solver = pca_solver
+        self.pca_iters = pca_iters
         self.form = form
         self.iters = iters
         self.proposal = proposal
@@ -139,17 +152,36 @@ class ANNFieldPropKDTreeGB300:
         pos_b = _SUBSETS.get(hb - p + 1, wb - p + 1, m, self.seed + 1, dev)
         self.components_ = torch.empty((d, P), dtype=torch.float64, device=dev)
         self.mean_ = torch.empty(P, dtype=torch.float64, device=dev)
-        h.call("annf_pca_fit", ptr(A), ha, wa, ptr(pos_a), pos_a.shape[0], ptr(B), hb, wb, ptr(pos_b),
-               pos_b.shape[0], c, p, d, ptr(self.components_), ptr(self.mean_), st)
+        if self.form not in self.FORMS:
+            raise ValueError("form must be one of {}".format(self.FORMS))
+        solver = self.pca_solver or ("exact" if self.form == "plain" else "subspace")
+        if solver == "exact":
+            h.call("annf_pca_fit", ptr(A), ha, wa, ptr(pos_a), pos_a.shape[0], ptr(B), hb, wb, ptr(pos_b),
+                   pos_b.shape[0], c, p, d, ptr(self.components_), ptr(self.mean_), st)
+        elif solver == "subspace":
+            h.call("annf_pca_fit_subspace", ptr(A), ha, wa, ptr(pos_a), pos_a.shape[0], ptr(B), hb, wb, ptr(pos_b),
+                   pos_b.shape[0], c, p, d, int(self.pca_iters), ptr(self.components_), ptr(self.mean_), st)
+        else:
+            raise ValueError("pca_solver must be 'exact' or 'subspace'")
         ev["t1"].record()
 
         # (2)+(3) patches projected straight from the images (annfmp/openmp/base.py:152-166, 193-200)
         self.patches_a_reduced_ = torch.empty((n_a, d), dtype=real, device=dev)
         self.patches_b_reduced_ = torch.empty((n_b, d), dtype=real, device=dev)
-        h.call("annf_project", ptr(A), ha, wa, c, p, ptr(self.components_), ptr(self.mean_), d, real_type,
-               ptr(self.patches_a_reduced_), st)
-        h.call("annf_project", ptr(B), hb, wb, c, p, ptr(self.components_), ptr(self.mean_), d, real_type,
-               ptr(self.patches_b_reduced_), st)
+        proj = self.projection or "exact"
+        if proj == "bf16":
+            if real != torch.float32:
+                raise ValueError("the BF16 projection needs float_type='float'")
+            for img, hh, ww, dst in ((A, ha, wa, self.patches_a_reduced_), (B, hb, wb, self.patches_b_reduced_)):
+                h.call("annf_project_bf16", ptr(img), hh, ww, c, p, ptr(self.components_), ptr(self.mean_), d,
+                       ptr(dst), st)
+        elif proj == "exact":
+            h.call("annf_project", ptr(A), ha, wa, c, p, ptr(self.components_), ptr(self.mean_), d, real_type,
+                   ptr(self.patches_a_reduced_), st)
+            h.call("annf_project", ptr(B), hb, wb, c, p, ptr(self.components_), ptr(self.mean_), d, real_type,
+                   ptr(self.patches_b_reduced_), st)
+        else:
+            raise ValueError("projection must be 'exact' or 'bf16'")
         ev["t2"].record()
 
         # (4) k-d tree over B (annfmp/openmp/base.py:95-103)
@@ -158,8 +190,6 @@ class ANNFieldPropKDTreeGB300:
 
         # (5) rows (annfmp/openmp/base.py:113-125)
         assert self.leaf_size > self.n_neighbors
-        if self.form not in self.FORMS:
-            raise ValueError("form must be one of {}".format(self.FORMS))
         k = int(self.n_neighbors)
         nn = torch.empty(n_a, dtype=torch.int32, device=dev)
         self.nn_distances_ = torch.empty(n_a, dtype=torch.float32, device=dev)
@@ -174,8 +204,14 @@ class ANNFieldPropKDTreeGB300:
             if self.proposal is not None:
                 prop = self.proposal.propose(A, B, p)
             n_prop = 0 if prop is None else int(prop.shape[1])
+            lp = self.leaf_precision or "bf16"
+            if lp not in ("bf16", "fp16", "fp32"):
+                raise ValueError("leaf_precision must be 'bf16', 'fp16' or 'fp32'")
+            if lp != "fp32" and real != torch.float32:
+                raise ValueError("tensor-core leaf distances need float_type='float'")
             h.call("annf_parallel_nnf", ptr(nn), ptr(A), ha, wa, ptr(B), hb, wb, c, p,
                    ptr(self.patches_a_reduced_), k, ptr(prop), n_prop, int(self.iters), int(self.seed) & 0xFFFFFFFF,
+                   {"bf16": _lib.ANNF_LEAF_BF16, "fp16": _lib.ANNF_LEAF_FP16, "fp32": _lib.ANNF_LEAF_EXACT}[lp],
                    ptr(self.nn_distances_), st)
         ev["t4"].record()
         tree.check_device()  # synchronises and raises if a kernel's bounds check tripped

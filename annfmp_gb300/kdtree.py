@@ -118,6 +118,23 @@ class KDTree(object):
             return dist.cpu().numpy(), idx.cpu().numpy()
         return dist, idx
 
+    def natural_kneighbors(self, X, n_neighbors=None, leaf_precision="fp32"):
+        """Original indices [nq, k] of each query's k nearest points inside the leaf its descent
+        reaches (the reference's traversal with max_leaves=1), nearest first. ``leaf_precision``
+        "fp32" scans the leaf exactly; "bf16" / "fp16" compute tensor-core distance tiles and re-rank
+        exactly (FP32) every point within the tiles' proven rounding bound, so the result is the
+        same."""
+        numpy_out = is_numpy(X)
+        Q = to_device(X, self._torch_dtype(), self._dev)
+        k = int(n_neighbors or self.n_neighbors)
+        prec = {"fp32": _lib.ANNF_LEAF_EXACT, "bf16": _lib.ANNF_LEAF_BF16, "fp16": _lib.ANNF_LEAF_FP16}[leaf_precision]
+        pos = torch.empty((Q.shape[0], k), dtype=torch.int32, device=self._dev)
+        self.handle.call("annf_natural_knn", ptr(Q), Q.shape[0], k, prec, ptr(pos), stream_ptr(self._dev))
+        tv = self.handle.tree_view()
+        perm = device_view(tv.perm, (tv.n,), np.int32, self._dev)
+        idx = perm[pos.long()]
+        return idx.cpu().numpy() if numpy_out else idx
+
     def process_rows(self, nn_indices, patches_a, patches_b, patchesred, n_rows, n_cols, n_neighbors=None,
                      propagate=True, select_best_nn=True):
         """Row-propagation NNF (annfmp/openmp/kdtree/base.py:210-241); the chosen B index of every

@@ -1,13 +1,18 @@
 """Benchmark: query patches/s of the NNF hot path on one GB300 (or N replicas).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
-                    [--workload large|medium|small] [--form plain|parallel] [--iters N]
+                    [--workload large|medium|small] [--form learned|parallel|plain] [--iters N]
 
 A step is one full NNF of one image pair, from device-resident uint8 images to the device-resident
-NNF: PCA fit (sampled subset, exact Gram, FP64 eigh), projection of every A and B patch, k-d tree
-build, exact first row, row propagation and the raw-patch re-rank. value = query patches (A patch
-positions) per second over all ranks. e2e = the same through the public API from pinned host
-images to the host NNF. The L2 cache (129 MB) is flushed between timed steps by writing 256 MB.
+NNF. Forms: "plain" is the reference's method (PCA fit with the exact FP64 eigendecomposition, exact
+projection, k-d tree, exact first row, row propagation, raw-patch re-rank); "parallel" is the BF16
+form (subspace PCA with an FP64 Rayleigh-Ritz step, BF16 tensor-core projection, the same tree,
+BF16 tensor-core natural-leaf tiles with exact FP32 re-rank, parallel propagation with exact
+raw-patch verification); "learned" adds the trained offset-proposal network. value = query patches
+(A patch positions) per second over all ranks; distance_error = mean / p99 of d_found/d_exact - 1
+over 4096 sampled pixels against the exact raw-patch nearest neighbour; "forms" times the other
+forms on the same pair. e2e = the same through the public API from pinned host images to the host
+NNF. The L2 cache (129 MB) is flushed between timed steps by writing 256 MB.
 
 --impl reference times the CPU path (the oracle: a C restatement of the reference's OpenMP core with
 OpenMP on all host cores, plus the numpy restatement of its PCA) on a bounded sample of the same
@@ -225,6 +230,42 @@ def config_of(w, args):
 # ---------------------------------------------------------------------------------------------
 # GPU arm
 # ---------------------------------------------------------------------------------------------
+def learned_available():
+    from annfmp_gb300.proposal import DEFAULT_WEIGHTS
+    return os.path.exists(DEFAULT_WEIGHTS)
+
+
+def make_model(form, args, prm, local_rank):
+    """plain: the reference's method; parallel: subspace PCA, BF16 tensor-core projection and leaf
+    tiles, parallel propagation; learned: parallel + the trained offset-proposal network."""
+    from annfmp_gb300 import ANNFieldPropKDTreeGB300
+    kw = dict(verbose=0, device=local_rank, **prm)
+    if form == "plain":
+        return ANNFieldPropKDTreeGB300(**kw)
+    proposal = None
+    if form == "learned":
+        from annfmp_gb300.proposal import ProposalNet
+        proposal = ProposalNet.pretrained(local_rank)
+    return ANNFieldPropKDTreeGB300(form="parallel", iters=args.iters, proposal=proposal, **kw)
+
+
+def time_form(form, args, prm, local_rank, A, B, flush, steps):
+    """(ms per step, last NNF) of a form on device-resident images, CUDA events, L2 flushed."""
+    import torch
+    model = make_model(form, args, prm, local_rank)
+    for _ in range(max(args.warmup, 1)):
+        model.fit(A, B)
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    torch.cuda.synchronize()
+    for i in range(steps):
+        flush.fill_(float(i))
+        evs[i][0].record()
+        nn = model.fit(A, B)
+        evs[i][1].record()
+    torch.cuda.synchronize()
+    return sum(s.elapsed_time(e) for s, e in evs) / steps, nn
+
+
 def run_gpu(args, w, rank, world, local_rank):
     import torch
     import torch.distributed as dist
@@ -241,7 +282,7 @@ def run_gpu(args, w, rank, world, local_rank):
     A = torch.from_numpy(a).to(dev)
     B = torch.from_numpy(b).to(dev)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
-    model = ANNFieldPropKDTreeGB300(verbose=0, device=local_rank, form=args.form, iters=args.iters, **prm)
+    model = make_model(args.form, args, prm, local_rank)
 
     for _ in range(args.warmup):
         model.fit(A, B)
@@ -304,6 +345,15 @@ def run_gpu(args, w, rank, world, local_rank):
     # distance error of the last timed NNF against the exact raw-patch nearest neighbour
     from annfmp_gb300 import metrics
     quality = metrics.distance_ratio_error(a, b, nn_dev, p, n_samples=4096, seed=w["seed"] + 7, device=local_rank)
+    # the other forms on the same pair, same timing rules (for the speed-up at equal error)
+    forms = {args.form: {"ms_per_step": ms, "value": n_a / (ms / 1e3), "distance_error": quality}}
+    if world == 1 and not args.no_compare:
+        for f in ("plain", "parallel", "learned"):
+            if f == args.form or (f == "learned" and not learned_available()):
+                continue
+            fms, fnn = time_form(f, args, prm, local_rank, A, B, flush, max(2, args.steps // 2))
+            fq = metrics.distance_ratio_error(a, b, fnn, p, n_samples=4096, seed=w["seed"] + 7, device=local_rank)
+            forms[f] = {"ms_per_step": fms, "value": n_a / (fms / 1e3), "distance_error": fq}
     achieved = by / (kernel_stages[dom] / 1e3) / 1e9
     traffic = load_traffic().get(f"{args.workload}:{args.form}:{dom}")
     value = world * n_a / (ms / 1e3)
@@ -318,6 +368,7 @@ def run_gpu(args, w, rank, world, local_rank):
                      "frac": achieved / peak, "peak_kind": peak_kind, "algorithmic_bytes": by,
                      "traffic": traffic},
         "distance_error": quality,
+        "forms": forms,
         "stages_ms": stage_ms, "wall_ms_per_step": t_wall * 1e3 / args.steps,
         "clocks": clocks.summary(),
     }
@@ -336,12 +387,17 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="large", choices=sorted(WORKLOADS))
-    ap.add_argument("--form", default="plain", choices=["plain", "parallel"])
-    ap.add_argument("--iters", type=int, default=4, help="propagation passes of the parallel form")
+    ap.add_argument("--form", default="learned", choices=["plain", "parallel", "learned"],
+                    help="plain: the reference's method; parallel: BF16 tensor-core form; learned: + proposals")
+    ap.add_argument("--iters", type=int, default=4, help="propagation passes of the parallel forms")
+    ap.add_argument("--no-compare", action="store_true", help="time only --form (not the other forms)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 0)
     w = WORKLOADS[args.workload]
+    if args.form == "learned" and not learned_available():
+        print("bench: no trained proposal weights; timing the parallel form", file=sys.stderr)
+        args.form = "parallel"
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))
     local_rank = int(os.environ.get("LOCAL_RANK", 0))

@@ -40,6 +40,8 @@ extern "C" {
 
 /* leaf-distance precision of annf_process_rows* (the plain form is ANNF_LEAF_EXACT) */
 #define ANNF_LEAF_EXACT 0 /* FP32/FP64 with the reference's summation order */
+#define ANNF_LEAF_BF16 1  /* BF16 tensor-core tiles (FP32 accumulate) + exact FP32 re-rank of the survivors */
+#define ANNF_LEAF_FP16 2  /* the same with FP16 tiles (tighter bound, fewer survivors) */
 
 typedef struct annf_handle annf_handle;
 
@@ -127,6 +129,16 @@ int annf_pca_fit(annf_handle* h, const uint8_t* img_a, int ha, int wa, const int
                  int psize, int n_components, double* components_out, double* mean_out,
                  void* stream);
 
+/* As annf_pca_fit, but only the leading n_components are computed (an addition for the
+ * approximate NNF forms; the reference has no counterpart): the same exact Gram matrix and FP64
+ * covariance, then `iters` steps of FP32 subspace iteration on a block of n_components +
+ * max(8, n_components/2) vectors, a Rayleigh-Ritz step and the small eigenproblem in FP64, and the
+ * same sign convention. Falls back to the full solver when P < 2 * block or the block exceeds 40. */
+int annf_pca_fit_subspace(annf_handle* h, const uint8_t* img_a, int ha, int wa, const int* pos_a, int n_a,
+                          const uint8_t* img_b, int hb, int wb, const int* pos_b, int n_b, int channels,
+                          int psize, int n_components, int iters, double* components_out,
+                          double* mean_out, void* stream);
+
 /* Project every psize x psize patch of an image onto the components
  * (annfmp/openmp/base.py:193-200: X @ C^T - mean @ C^T in FP64, cast to real_type). The
  * product is evaluated exactly in integer arithmetic on split coefficients, so the result is the
@@ -135,16 +147,25 @@ int annf_project(annf_handle* h, const uint8_t* img, int hgt, int wid, int chann
                  const double* components, const double* mean, int n_components, int real_type,
                  void* out, void* stream);
 
+/* Approximate counterpart of annf_project for the approximate NNF forms (no reference
+ * counterpart): the same patches times the components rounded to BF16, FP32 accumulation on the
+ * tensor cores (tcgen05), minus the projected mean; out FP32 [(h-psize+1)*(w-psize+1)*n_components].
+ * Needs psize*psize*channels <= 256 and n_components <= 32 (else ANNF_ERR_UNSUPPORTED). */
+int annf_project_bf16(annf_handle* h, const uint8_t* img, int hgt, int wid, int channels, int psize,
+                      const double* components, const double* mean, int n_components, float* out, void* stream);
+
 /* The parallel NNF form (an addition beside the reference's row-sequential method, which has no
- * counterpart for it): every pixel's natural-leaf k-list, optional offset proposals
+ * counterpart for it): every pixel's natural-leaf k-list (leaf_precision ANNF_LEAF_EXACT: FP32
+ * leaf scan; ANNF_LEAF_BF16: queries grouped by leaf, BF16 tensor-core distance tiles, exact FP32
+ * re-rank of the 4k best), optional offset proposals
  * (proposals [n_rows*n_cols*n_prop] B patch indices, -1 = none) and `iters` parallel passes of
  * neighbour propagation and random search; every candidate is verified with the exact integer
  * raw-patch SSD. Requires the tree over image B's reduced patches (annf_build_tree). Outputs the
  * chosen B index per pixel and, optionally, its raw-patch L2 distance. */
 int annf_parallel_nnf(annf_handle* h, int* final_idx, const uint8_t* img_a, int ha, int wa,
                       const uint8_t* img_b, int hb, int wb, int channels, int psize, const void* ared,
-                      int k, const int* proposals, int n_prop, int iters, unsigned seed, float* dist_out,
-                      void* stream);
+                      int k, const int* proposals, int n_prop, int iters, unsigned seed,
+                      int leaf_precision, float* dist_out, void* stream);
 
 /* Exact raw-patch nearest neighbour (integer SSD over all B patches) of nq sampled A pixels
  * (query_pixels: row-major patch indices). best[i] = ssd << 32 | B index (smallest index on
@@ -152,6 +173,60 @@ int annf_parallel_nnf(annf_handle* h, int* final_idx, const uint8_t* img_a, int 
 int annf_raw_nn(annf_handle* h, const uint8_t* img_a, int ha, int wa, const uint8_t* img_b, int hb,
                 int wb, int channels, int psize, const int* query_pixels, int nq,
                 unsigned long long* best, void* stream);
+
+/* The k nearest points of each query inside the leaf its descent reaches (no backtracking; the
+ * reference's traversal with max_leaves = 1, kdtree.c:129-268 with only_leaf_idx). out_pos
+ * [nq*k] tree positions (annf_tree_view.perm maps them to original indices), nearest first.
+ * ANNF_LEAF_EXACT scans the leaf in FP32 (reference order); ANNF_LEAF_BF16 groups the queries by
+ * leaf and computes BF16 tensor-core distance tiles, re-ranking the best 4k exactly in FP32. */
+int annf_natural_knn(annf_handle* h, const void* queries, long long nq, int k, int leaf_precision,
+                     int* out_pos, void* stream);
+
+/* One 128 x n tile of the tensor-core path, for numerics checks (no counterpart in the reference):
+ * d[128][n] = a[128][kdim] . b[n][kdim]^T, a and b BF16 (raw 16-bit, row-major), d FP32, computed by
+ * tcgen05.mma from shared-memory core-matrix tiles into tensor memory. n, kdim multiples of 16,
+ * n <= 256, kdim <= 256. */
+int annf_tc_tile(annf_handle* h, const uint16_t* a, const uint16_t* b, int n, int kdim, float* d,
+                 void* stream);
+
+/* ---- offset-proposal network (an addition: the reference's only propagation candidates are the
+ * row above, annfmp/openmp/kdtree/src/base.c:255-282). Tensors are NHWC, activations BF16 (raw
+ * 16-bit), gradients and weights FP32; six 3x3 layers 8->32, 32->32 x4, 32->8. ---- */
+
+/* x_out [hgt/4][wid/4][8] BF16: 4x4 box means of A.rgb and B.rgb, (v - 127.5) / 64, then 0, 0. */
+int annf_cnn_input(annf_handle* h, const uint8_t* img_a, const uint8_t* img_b, int hgt, int wid, void* x_out,
+                   void* stream);
+/* w [co][3][3][ci] FP32 -> w_fwd [9][ci][co] and (optional) w_bwd [9][co][ci] (flipped taps), both
+ * rounded to BF16 values. */
+int annf_cnn_prep_weights(annf_handle* h, const float* w, int co, int ci, float* w_fwd, float* w_bwd, void* stream);
+/* y = conv3x3(x) + bias (zero padding); relu=1: ReLU, BF16 y; relu=0: FP32 y. (ci, co) in
+ * {(8,32), (32,32), (32,8)}. */
+int annf_cnn_conv_forward(annf_handle* h, const void* x, int nimg, int hgt, int wid, int ci, int co,
+                          const float* w_fwd, const float* bias, int relu, void* y, void* stream);
+/* dx [nimg,hgt,wid,ci] FP32 = input gradient for upstream g [.., co] FP32, g multiplied by
+ * (mask > 0) when mask (BF16 [.., co], the layer's ReLU output) is given. */
+int annf_cnn_conv_backward_data(annf_handle* h, const float* g, const void* mask, int nimg, int hgt, int wid, int co,
+                                int ci, const float* w_bwd, float* dx, void* stream);
+/* dw [co][9][ci] += sum_p g[p][co] x[p + tap][ci]; db [co] += sum_p g[p][co] (accumulates: zero
+ * them first). */
+int annf_cnn_conv_backward_weights(annf_handle* h, const void* x, const float* g, const void* mask, int nimg,
+                                   int hgt, int wid, int ci, int co, float* dw, float* db, void* stream);
+/* Relaxed winner-takes-all L1 loss over 4 hypotheses (x16 px) per pixel, each hypothesis' error
+ * truncated at 40 px: dout [npix][8] and *loss_sum += loss; pixels with valid[i] == 0 contribute
+ * nothing; inv_nvalid = 1 / valid count. */
+int annf_cnn_wta_loss(annf_handle* h, const float* out, const float* tgt, const uint8_t* valid, long long npix,
+                      float inv_nvalid, float* dout, float* loss_sum, void* stream);
+/* Bias-corrected Adam step (step >= 1) on FP32 parameters, in place. */
+int annf_cnn_adam(annf_handle* h, float* param, const float* grad, float* m, float* v, int n, float lr, float beta1,
+                  float beta2, float eps, int step, void* stream);
+/* Training targets from an NNF of A (ha x wa) into B (width wb): per low-resolution pixel the median
+ * (dx, dy) over its 4x4 block of patch centres, tgt [ha/4][wa/4][2], valid [ha/4][wa/4]. */
+int annf_cnn_targets(annf_handle* h, const int* nnf, int ha, int wa, int wb, int psize, float* tgt, uint8_t* valid,
+                     void* stream);
+/* Proposals [n_A][4] B patch indices from the network output out [h4][w4][8]: each A patch takes
+ * the 4 hypotheses of the low-resolution pixel holding its centre, rounded, clamped to B's grid. */
+int annf_cnn_proposals(annf_handle* h, const float* out, int h4, int w4, int ha, int wa, int hb, int wb, int psize,
+                       int* props, void* stream);
 
 /* Synchronise the stream and report (and clear) the kernels' bounds-check status bits. */
 int annf_device_status(annf_handle* h, void* stream, unsigned* bits_out);

@@ -1,0 +1,139 @@
+"""Components of the approximate NNF forms on the GPU: the subspace eigensolver."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+PIPES = ["ref_pipeline_affine128.npz", "ref_pipeline_flow160.npz", "ref_pipeline_k3_noprop.npz"]
+
+
+def _covariance(O, a, b, psize, n_subset, seed):
+    m = int(n_subset / 2)
+    X = np.concatenate([O.subset_patches(a, psize, m, seed), O.subset_patches(b, psize, m, seed + 1)]).astype(np.float64)
+    mu = X.mean(axis=0)
+    C = X.T @ X - len(X) * np.outer(mu, mu)
+    return C / (len(X) - 1)
+
+
+@pytest.mark.parametrize("name", PIPES)
+def test_subspace_pca_captures_leading_variance(gpu_lib, oracle_mod, golden, name):
+    """Subspace iteration + FP64 Rayleigh-Ritz: orthonormal components in decreasing Ritz value,
+    capturing the top-d variance of the exact eigendecomposition to 1e-4, the leading component
+    equal to the exact one (same sign convention), the mean exact."""
+    from annfmp_gb300 import ANNFieldPropKDTreeGB300
+    z = golden(name)
+    k, psize, d, n_subset, leaf, prop, sel, seed = (int(v) for v in z["params"])
+    m = ANNFieldPropKDTreeGB300(n_neighbors=k, psize=psize, dim_reduced=d, n_subset=n_subset, leaf_size=leaf,
+                                seed=seed, verbose=0, form="parallel", pca_solver="subspace", pca_iters=10)
+    m.fit(z["a"], z["b"])
+    V = m.components_.cpu().numpy()
+    assert np.array_equal(m.mean_.cpu().numpy(), z["mean"])
+    assert np.abs(V @ V.T - np.eye(d)).max() < 1e-9
+    C = _covariance(oracle_mod, z["a"], z["b"], psize, n_subset, seed)
+    w = np.linalg.eigvalsh(C)[::-1]
+    ritz = np.einsum("ij,jk,ik->i", V, C, V)
+    assert np.all(np.diff(ritz) <= 1e-9 * ritz[0])
+    assert ritz.sum() >= w[:d].sum() * (1 - 1e-4), (ritz.sum(), w[:d].sum())
+    assert np.dot(V[0], z["components"][0]) > 1 - 1e-6
+    j = np.argmax(np.abs(V), axis=1)
+    assert np.all(V[np.arange(d), j] > 0)
+
+
+# ---------------------------------------------------------------------------------------------
+# tensor cores: one tcgen05 tile against a torch FP32 matmul of the same BF16 values
+# ---------------------------------------------------------------------------------------------
+def _tc_tile(h, A, B):
+    import torch
+    from annfmp_gb300._torch import ptr, stream_ptr
+    dev = A.device
+    D = torch.empty((128, B.shape[0]), dtype=torch.float32, device=dev)
+    h.call("annf_tc_tile", ptr(A.view(torch.int16)), ptr(B.view(torch.int16)), B.shape[0], A.shape[1], ptr(D),
+           stream_ptr(dev))
+    return D
+
+
+@pytest.mark.parametrize("n,kd", [(16, 16), (128, 16), (256, 32), (64, 64), (144, 48), (256, 256)])
+def test_tc_tile_exact_on_small_integers(gpu_lib, n, kd):
+    """Small integers are exact in BF16 and their dot products exact in FP32: bit-identical."""
+    import torch
+    from annfmp_gb300 import _lib
+    g = torch.Generator().manual_seed(n * 1000 + kd)
+    A = torch.randint(-8, 9, (128, kd), generator=g).to(torch.bfloat16).cuda()
+    B = torch.randint(-8, 9, (n, kd), generator=g).to(torch.bfloat16).cuda()
+    D = _tc_tile(_lib.Handle(0), A, B)
+    want = A.float() @ B.float().T
+    assert torch.equal(D, want), (D - want).abs().max()
+
+
+def test_tc_tile_random_bf16(gpu_lib):
+    """Random BF16 operands: FP32 accumulation, within 1e-5 of the row/column magnitude scale."""
+    import torch
+    from annfmp_gb300 import _lib
+    g = torch.Generator().manual_seed(7)
+    A = torch.randn((128, 32), generator=g).to(torch.bfloat16).cuda()
+    B = torch.randn((96, 32), generator=g).to(torch.bfloat16).cuda()
+    D = _tc_tile(_lib.Handle(0), A, B)
+    want = A.double() @ B.double().T
+    scale = A.double().abs() @ B.double().abs().T
+    assert ((D.double() - want).abs() <= 1e-5 * scale + 1e-30).all()
+
+
+# ---------------------------------------------------------------------------------------------
+# natural-leaf kNN: BF16 tensor-core tiles + FP32 re-rank vs the exact FP32 leaf scan
+# ---------------------------------------------------------------------------------------------
+@pytest.mark.parametrize("n,d,leaf,k,quant", [(60000, 16, 64, 4, 0), (40000, 8, 32, 1, 0), (30000, 6, 8, 3, 0),
+                                              (50000, 24, 64, 8, 0), (20000, 12, 32, 2, 0), (60000, 16, 64, 4, 8)])
+def test_natural_knn_bf16_vs_fp32(gpu_lib, n, d, leaf, k, quant):
+    """The BF16 tiles only filter: every point within the proven BF16 error bound of the k-th best
+    estimate is re-ranked exactly in FP32, so the k-lists equal the FP32 leaf scan's."""
+    import torch
+    from annfmp_gb300 import KDTree
+    rng = np.random.default_rng(n + d)
+    # reduced-patch-like data: offset, anisotropic scales
+    X = (rng.standard_normal((n, d)) * (300.0 / (1 + np.arange(d))) + 500.0).astype(np.float32)
+    Qn = (X[rng.integers(0, n, 8000)] + rng.standard_normal((8000, d)).astype(np.float32) * 3).astype(np.float32)
+    if quant:  # coarse grid: many exactly tied distances
+        X = (np.round(X / quant) * quant).astype(np.float32)
+        Qn = (np.round(Qn / quant) * quant).astype(np.float32)
+    t = KDTree(n_neighbors=k, leaf_size=leaf, float_type="float", splitting_type="longest").fit(torch.from_numpy(X).cuda())
+    Q = torch.from_numpy(Qn).cuda()
+    i32 = t.natural_kneighbors(Q, k, "fp32").cpu().numpy()
+    i16 = t.natural_kneighbors(Q, k, "bf16").cpu().numpy()
+    same = (i32 == i16).all(axis=1)
+    assert same.all(), (same.mean(), np.nonzero(~same)[0][:10])
+    ih = t.natural_kneighbors(Q, k, "fp16").cpu().numpy()
+    assert np.array_equal(ih, i32)
+
+    def d2(idx):
+        diff = X[idx].astype(np.float64) - Qn[:, None, :].astype(np.float64)
+        return (diff * diff).sum(-1)
+    assert np.all(d2(i16)[:, -1] >= d2(i32)[:, -1] * (1 - 1e-6))
+
+
+# ---------------------------------------------------------------------------------------------
+# BF16 tensor-core projection vs the same arithmetic in float64
+# ---------------------------------------------------------------------------------------------
+@pytest.mark.parametrize("name", PIPES)
+def test_project_bf16_matches_bf16_components(gpu_lib, oracle_mod, golden, name):
+    """out = patches . bf16(components)^T - bf16(components) . mean: pixel values and BF16
+    products are exact, so only FP32 summation order separates the GPU from float64."""
+    import torch
+    from annfmp_gb300 import _lib
+    from annfmp_gb300._torch import ptr, stream_ptr
+    from oracle import cnn as C
+    z = golden(name)
+    psize = int(z["params"][1])
+    comps, mean = np.ascontiguousarray(z["components"]), z["mean"]
+    dev = torch.device("cuda", 0)
+    for img in (z["a"], z["b"]):
+        h, w, c = img.shape
+        out = torch.empty(((h - psize + 1) * (w - psize + 1), comps.shape[0]), dtype=torch.float32, device=dev)
+        _lib.Handle(0).call("annf_project_bf16", ptr(torch.from_numpy(img).to(dev)), h, w, c, psize,
+                            ptr(torch.from_numpy(comps).to(dev)), ptr(torch.from_numpy(mean).to(dev)), comps.shape[0],
+                            ptr(out), stream_ptr(dev))
+        cb = C.bf16_round(comps.astype(np.float32)).astype(np.float64)
+        X = oracle_mod.extract_patches(img, psize).astype(np.float64)
+        want = X @ cb.T - cb @ mean
+        scale = X @ np.abs(cb).T + np.abs(cb) @ np.abs(mean)
+        got = out.cpu().numpy()
+        assert np.all(np.abs(got - want) <= 2e-5 * scale + 1e-6), np.abs(got - want).max()
