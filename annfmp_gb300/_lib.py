@@ -73,7 +73,8 @@ SIGNATURES = {
     "annf_pca_fit_subspace": (_i, [_vp, _vp, _i, _i, _vp, _i, _vp, _i, _i, _vp, _i, _i, _i, _i, _i, _vp, _vp, _vp]),
     "annf_project": (_i, [_vp, _vp, _i, _i, _i, _i, _vp, _vp, _i, _i, _vp, _vp]),
     "annf_device_status": (_i, [_vp, _vp, ctypes.POINTER(_u)]),
-    "annf_parallel_nnf": (_i, [_vp, _vp, _vp, _i, _i, _vp, _i, _i, _i, _i, _vp, _i, _vp, _i, _i, _u, _i, _vp, _vp]),
+    "annf_parallel_nnf": (_i, [_vp, _vp, _vp, _i, _i, _vp, _i, _i, _i, _i, _vp, _i, _vp, _i, _i, _u, _i, _i, _i, _vp,
+                               _vp]),
     "annf_tc_tile": (_i, [_vp, _vp, _vp, _i, _i, _vp, _vp]),
     "annf_natural_knn": (_i, [_vp, _vp, ctypes.c_longlong, _i, _i, _vp, _vp]),
     "annf_project_bf16": (_i, [_vp, _vp, _i, _i, _i, _i, _vp, _vp, _i, _vp, _vp]),

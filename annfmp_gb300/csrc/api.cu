@@ -28,7 +28,7 @@ int kneighbors_noalloc(annf_handle* h, const void* Q, int nq, int K, long long m
 int natural_knn_all(annf_handle* h, const void* Q, long long nq, int K, int* out_pos, cudaStream_t st);
 int fast_search(annf_handle* h, const uint8_t* img_a, int ha, int wa, const uint8_t* img_b, int hb, int wb, int c,
                 int psize, int K, const int* nat_pos, const int* prop, int n_prop, int iters, uint32_t seed,
-                int* final_idx, float* dist_out, cudaStream_t st);
+                int rand_samples, int radius0, int* final_idx, float* dist_out, cudaStream_t st);
 bool leaf_tc_supported(const annf_handle* h, int K);
 int natural_knn_tc(annf_handle* h, const float* Q, long long nq, int K, int prec, int* out_pos, cudaStream_t st);
 int tc_tile(const uint16_t* A, const uint16_t* B, int N, int K, float* D, unsigned* status, cudaStream_t st);
@@ -298,7 +298,8 @@ int annf_kneighbors_noalloc(annf_handle* h, const void* queries, int nq, int k, 
 
 int annf_parallel_nnf(annf_handle* h, int* final_idx, const uint8_t* img_a, int ha, int wa, const uint8_t* img_b,
                       int hb, int wb, int channels, int psize, const void* ared, int k, const int* proposals,
-                      int n_prop, int iters, unsigned seed, int leaf_precision, float* dist_out, void* stream) {
+                      int n_prop, int iters, unsigned seed, int leaf_precision, int rand_samples, int radius0,
+                      float* dist_out, void* stream) {
   ANNF_API_HANDLE(h);
   int rc = check_k(h, k, 2147483640);
   if (rc != ANNF_OK) return rc;
@@ -309,6 +310,8 @@ int annf_parallel_nnf(annf_handle* h, int* final_idx, const uint8_t* img_a, int 
                "annf_parallel_nnf: the tree must hold every patch of image B");
   ANNF_REQUIRE(n_prop >= 0 && (n_prop == 0 || proposals), "annf_parallel_nnf: bad proposals");
   ANNF_REQUIRE(iters >= 0 && iters <= 64, "annf_parallel_nnf: iters out of range");
+  ANNF_REQUIRE(rand_samples >= 0 && rand_samples <= 16 && radius0 >= 1 && radius0 <= 4096,
+               "annf_parallel_nnf: bad search schedule");
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   const long long nA = (long long)(ha - psize + 1) * (wa - psize + 1);
   ANNF_ENSURE(h->fast_nat, (size_t)nA * k * sizeof(int));
@@ -326,7 +329,7 @@ int annf_parallel_nnf(annf_handle* h, int* final_idx, const uint8_t* img_a, int 
   if (rc != ANNF_OK) return rc;
   prof_mark(h, "natural_knn", st);
   return fast_search(h, img_a, ha, wa, img_b, hb, wb, channels, psize, k, h->fast_nat.as<int>(), proposals, n_prop,
-                     iters, seed, final_idx, dist_out, st);
+                     iters, seed, rand_samples, radius0, final_idx, dist_out, st);
 }
 
 int annf_raw_nn(annf_handle* h, const uint8_t* img_a, int ha, int wa, const uint8_t* img_b, int hb, int wb,

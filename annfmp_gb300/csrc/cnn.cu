@@ -1,5 +1,6 @@
 // cnn.cu -- the offset-proposal network: input, 3x3 convolutions (forward, backward-data,
-// backward-weights), relaxed winner-takes-all truncated L1 loss, Adam, training targets and inference
+// backward-weights), relaxed winner-takes-all truncated L1 loss over block sub-targets, Adam,
+// training targets and inference
 // proposals (sm_103a).
 //
 // Network (an addition of this project; the reference's only propagation candidates are the row
@@ -235,38 +236,44 @@ __global__ void __launch_bounds__(9 * CI) cnn_wgrad_kernel(const __nv_bfloat16* 
 }
 
 // ---------------------------------------------------------------------------------------------
-// relaxed winner-takes-all truncated L1 loss and its gradient; loss_sum += the batch loss
+// relaxed winner-takes-all truncated L1 loss over each pixel's 16 sub-targets (the matches of the
+// 16 A pixels of its 4x4 block): every valid sub-target pulls its nearest hypothesis (weight 1) and
+// the others (weight kWtaEps); loss_sum += the batch loss
 // ---------------------------------------------------------------------------------------------
 __global__ void cnn_wta_kernel(const float* __restrict__ out, const float* __restrict__ tgt,
                                const uint8_t* __restrict__ valid, long long npix, float inv_nv,
                                float* __restrict__ dout, float* __restrict__ loss_sum) {
   float lsum = 0.f;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < npix; i += (long long)gridDim.x * blockDim.x) {
-    const float* o = out + i * 8;
-    float* d = dout + i * 8;
-    if (!valid[i]) {
+    float o[8], g[8];
 #pragma unroll
-      for (int c = 0; c < 8; ++c) d[c] = 0.f;
-      continue;
+    for (int c = 0; c < 8; ++c) {
+      o[c] = kOutScale * out[i * 8 + c];
+      g[c] = 0.f;
     }
-    const float tx = tgt[2 * i], ty = tgt[2 * i + 1];
-    float e[4];
-    int js = 0;
+    for (int s = 0; s < 16; ++s) {
+      if (!valid[i * 16 + s]) continue;
+      const float tx = tgt[(i * 16 + s) * 2], ty = tgt[(i * 16 + s) * 2 + 1];
+      float e[4];
+      int js = 0;
 #pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      e[j] = fabsf(kOutScale * o[2 * j] - tx) + fabsf(kOutScale * o[2 * j + 1] - ty);
-      if (e[j] < e[js]) js = j;
+      for (int j = 0; j < 4; ++j) {
+        e[j] = fabsf(o[2 * j] - tx) + fabsf(o[2 * j + 1] - ty);
+        if (e[j] < e[js]) js = j;
+      }
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const float wj = (j == js ? 1.f : kWtaEps) * inv_nv;
+        const bool live = e[j] < kWtaTrunc;
+        lsum += wj * (live ? e[j] : kWtaTrunc);
+        const float dx = o[2 * j] - tx, dy = o[2 * j + 1] - ty;
+        const float w = live ? wj * kOutScale : 0.f;
+        g[2 * j] += w * (dx > 0.f ? 1.f : (dx < 0.f ? -1.f : 0.f));
+        g[2 * j + 1] += w * (dy > 0.f ? 1.f : (dy < 0.f ? -1.f : 0.f));
+      }
     }
 #pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      const float wj = (j == js ? 1.f : kWtaEps) * inv_nv;
-      const bool live = e[j] < kWtaTrunc;
-      lsum += wj * (live ? e[j] : kWtaTrunc);
-      const float dx = kOutScale * o[2 * j] - tx, dy = kOutScale * o[2 * j + 1] - ty;
-      const float g = live ? wj * kOutScale : 0.f;
-      d[2 * j] = g * (dx > 0.f ? 1.f : (dx < 0.f ? -1.f : 0.f));
-      d[2 * j + 1] = g * (dy > 0.f ? 1.f : (dy < 0.f ? -1.f : 0.f));
-    }
+    for (int c = 0; c < 8; ++c) dout[i * 8 + c] = g[c];
   }
 #pragma unroll
   for (int o = 16; o; o >>= 1) lsum += __shfl_xor_sync(0xffffffffu, lsum, o);
@@ -290,42 +297,26 @@ __global__ void cnn_adam_kernel(float* __restrict__ p, const float* __restrict__
 // ---------------------------------------------------------------------------------------------
 // training targets from an NNF and inference proposals
 // ---------------------------------------------------------------------------------------------
-__device__ __forceinline__ float median16(float (&v)[16]) {
-#pragma unroll
-  for (int i = 1; i < 16; ++i) {
-#pragma unroll
-    for (int j = i; j > 0; --j) {
-      const float a = v[j - 1], b = v[j];
-      v[j - 1] = fminf(a, b);
-      v[j] = fmaxf(a, b);
-    }
-  }
-  return 0.5f * (v[7] + v[8]);
-}
-
 __global__ void cnn_targets_kernel(const int* __restrict__ nnf, int H, int W, int Wb, int psize, int h4, int w4,
                                    float* __restrict__ tgt, uint8_t* __restrict__ valid) {
   const int n_cols = W - psize + 1, n_rows = H - psize + 1, ncb = Wb - psize + 1, half = psize / 2;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < h4 * w4; i += gridDim.x * blockDim.x) {
     const int yy = i / w4, xx = i - yy * w4;
-    float dx[16], dy[16];
-    bool ok = true;
 #pragma unroll
     for (int u = 0; u < 16; ++u) {
       const int y = 4 * yy + (u >> 2) - half, x = 4 * xx + (u & 3) - half;
-      if (y < 0 || y >= n_rows || x < 0 || x >= n_cols) {
-        ok = false;
-        dx[u] = dy[u] = 0.f;
-        continue;
+      const bool ok = y >= 0 && y < n_rows && x >= 0 && x < n_cols;
+      float dx = 0.f, dy = 0.f;
+      if (ok) {
+        const int b = nnf[(size_t)y * n_cols + x];
+        const int by = b / ncb, bx = b - by * ncb;
+        dx = (float)(bx - x);
+        dy = (float)(by - y);
       }
-      const int b = nnf[(size_t)y * n_cols + x];
-      const int by = b / ncb, bx = b - by * ncb;
-      dx[u] = (float)(bx - x);
-      dy[u] = (float)(by - y);
+      valid[(size_t)i * 16 + u] = ok ? 1 : 0;
+      tgt[((size_t)i * 16 + u) * 2] = dx;
+      tgt[((size_t)i * 16 + u) * 2 + 1] = dy;
     }
-    valid[i] = ok ? 1 : 0;
-    tgt[2 * i] = ok ? median16(dx) : 0.f;
-    tgt[2 * i + 1] = ok ? median16(dy) : 0.f;
   }
 }
 

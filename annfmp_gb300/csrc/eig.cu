@@ -3,7 +3,7 @@
 // The full FP64 eigendecomposition of the P x P covariance (P = 243 for 9x9x3 patches) costs
 // milliseconds in a library solver, while the NNF only needs the top n_components. This solver:
 //   1. simultaneous (subspace) iteration in FP32 on a block of b >= n_components vectors, one CTA:
-//      Z = C Q, then modified Gram-Schmidt, `iters` times (C kept in FP32 in global memory, L2-hot);
+//      Z = C Q, then column-scaled Cholesky-QR, `iters` times (C kept in FP32 in global memory);
 //   2. Rayleigh-Ritz in FP64 on span(Q): W = C Q, G = Q^T Q, T = Q^T W over many CTAs;
 //   3. the b x b generalised problem T y = lambda G y in FP64 on one CTA: Cholesky G = R^T R
 //      (columns with a vanishing pivot are dropped), T~ = R^-T T R^-1, cyclic Jacobi on T~, and
@@ -42,35 +42,55 @@ __device__ __forceinline__ uint32_t mix32(uint32_t x) {
   return x;
 }
 
-// modified Gram-Schmidt over the b columns of Z (column-major [b][P] in shared memory)
-__device__ void mgs_columns(float* Z, int P, int b) {
+// Orthonormalise the b columns of Z (column-major [b][P], shared memory) in place by Cholesky-QR
+// after scaling every column to unit norm: in subspace iteration Z = C Q has nearly orthogonal
+// columns, so the scaled Gram matrix is close to the identity and FP32 Cholesky is stable. G and
+// Rinv are b x b shared scratch. A column whose pivot vanishes is replaced by a basis vector.
+__device__ void cholqr_columns(float* Z, int P, int b, float* G) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-  __shared__ float s_inv;
-  for (int j = 0; j < b; ++j) {
-    float* zj = Z + (size_t)j * P;
-    if (warp == 0) {
-      float s = 0.f;
-      for (int i = lane; i < P; i += 32) s = fmaf(zj[i], zj[i], s);
-      s = warp_sum_f(s);
-      if (lane == 0) s_inv = s > 1e-30f ? rsqrtf(s) : 0.f;
-    }
-    __syncthreads();
-    const float inv = s_inv;
-    if (inv == 0.f) {  // vanished column: restart it from a basis vector
-      for (int i = threadIdx.x; i < P; i += blockDim.x) zj[i] = (i == (j * 7 + 3) % P) ? 1.f : 0.f;
-    } else {
-      for (int i = threadIdx.x; i < P; i += blockDim.x) zj[i] *= inv;
-    }
-    __syncthreads();
-    for (int l = j + 1 + warp; l < b; l += nw) {
-      float* zl = Z + (size_t)l * P;
-      float r = 0.f;
-      for (int i = lane; i < P; i += 32) r = fmaf(zj[i], zl[i], r);
-      r = warp_sum_f(r);
-      for (int i = lane; i < P; i += 32) zl[i] = fmaf(-r, zj[i], zl[i]);
-    }
-    __syncthreads();
+  for (int j = warp; j < b; j += nw) {  // unit columns
+    float* z = Z + (size_t)j * P;
+    float sq = 0.f;
+    for (int i = lane; i < P; i += 32) sq = fmaf(z[i], z[i], sq);
+    sq = warp_sum_f(sq);
+    const float inv = sq > 1e-30f ? rsqrtf(sq) : 0.f;
+    for (int i = lane; i < P; i += 32) z[i] = inv > 0.f ? z[i] * inv : (i == (j * 7 + 3) % P ? 1.f : 0.f);
   }
+  __syncthreads();
+  for (int e = warp; e < b * b; e += nw) {  // Gram matrix (upper triangle), one warp per entry
+    const int r = e / b, c = e - r * b;
+    if (c < r) continue;
+    const float* zr = Z + (size_t)r * P;
+    const float* zc = Z + (size_t)c * P;
+    float s = 0.f;
+    for (int i = lane; i < P; i += 32) s = fmaf(zr[i], zc[i], s);
+    s = warp_sum_f(s);
+    if (lane == 0) G[r * b + c] = s;
+  }
+  __syncthreads();
+  if (warp == 0) {  // Cholesky G = R^T R (upper R in place), lanes over columns
+    for (int k = 0; k < b; ++k) {
+      float piv = G[k * b + k];
+      const float r = piv > 1e-12f ? sqrtf(piv) : 0.f;
+      __syncwarp();
+      for (int j = k + lane; j < b; j += 32) G[k * b + j] = r > 0.f ? (j == k ? r : G[k * b + j] / r) : (j == k ? 1.f : 0.f);
+      __syncwarp();
+      for (int j = k + 1 + lane; j < b; j += 32) {
+        const float rkj = G[k * b + j];
+        for (int i = k + 1; i <= j; ++i) G[i * b + j] = fmaf(-G[k * b + i], rkj, G[i * b + j]);
+      }
+      __syncwarp();
+    }
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < P; i += blockDim.x) {  // each row: q R = z (forward substitution)
+    for (int j = 0; j < b; ++j) {
+      float v = Z[(size_t)j * P + i];
+      for (int t = 0; t < j; ++t) v = fmaf(-Z[(size_t)t * P + i], G[t * b + j], v);
+      Z[(size_t)j * P + i] = v / G[j * b + j];
+    }
+  }
+  __syncthreads();
 }
 
 // step 1: one CTA. C32 is scratch [P*P]; Qout [b][P] FP32.
@@ -80,12 +100,13 @@ __global__ void __launch_bounds__(kSubThreads) subspace_iter_kernel(const double
   extern __shared__ __align__(16) float sm[];
   float* Q = sm;
   float* Z = sm + (size_t)b * P;
-  if (smem_overrun(sm, Z + (size_t)b * P, status)) return;
+  float* G = Z + (size_t)b * P;  // [b][b]
+  if (smem_overrun(sm, G + (size_t)b * b, status)) return;
   for (long long e = threadIdx.x; e < (long long)P * P; e += blockDim.x) C32[e] = (float)C[e];
   for (int e = threadIdx.x; e < b * P; e += blockDim.x)
     Q[e] = (float)(mix32((uint32_t)e * 2654435761u + 12345u) >> 8) * (1.0f / 16777216.0f) - 0.5f;
   __syncthreads();
-  mgs_columns(Q, P, b);
+  cholqr_columns(Q, P, b, G);
   const int groups = b >> 3;
   for (int it = 0; it < iters; ++it) {
     // Z = C Q (C symmetric: row i of C read as column i, coalesced across i)
@@ -105,12 +126,12 @@ __global__ void __launch_bounds__(kSubThreads) subspace_iter_kernel(const double
       for (int c = 0; c < 8; ++c) Z[(size_t)(g * 8 + c) * P + i] = acc[c];
     }
     __syncthreads();
-    mgs_columns(Z, P, b);
+    cholqr_columns(Z, P, b, G);
     float* t = Q;
     Q = Z;
     Z = t;
   }
-  mgs_columns(Q, P, b);  // second pass: orthogonal to working precision
+  cholqr_columns(Q, P, b, G);  // second pass: orthogonal to working precision
   for (int e = threadIdx.x; e < b * P; e += blockDim.x) Qout[e] = Q[e];
 }
 
@@ -244,7 +265,7 @@ __global__ void __launch_bounds__(256) rr_solve_kernel(int b, int ncomp, const d
   __shared__ double s_cs[kMaxBlock / 2], s_sn[kMaxBlock / 2];
   __shared__ int s_p[kMaxBlock / 2], s_q[kMaxBlock / 2];
   const int M = (m + 1) & ~1, half = M / 2;
-  for (int sweep = 0; sweep < 15 && m > 1; ++sweep) {
+  for (int sweep = 0; sweep < 12 && m > 1; ++sweep) {
     if (tid < 32) {
       double off = 0.0, tot = 0.0;
       for (int e = tid; e < m * m; e += 32) {
@@ -260,7 +281,7 @@ __global__ void __launch_bounds__(256) rr_solve_kernel(int b, int ncomp, const d
       }
     }
     __syncthreads();
-    if (!(s_off > 1e-24 * s_tot)) break;
+    if (!(s_off > 1e-20 * s_tot)) break;
     for (int round = 0; round < M - 1; ++round) {
       if (tid < half) {
         auto player = [&](int j) { return j == 0 ? 0 : 1 + (j - 1 + round) % (M - 1); };
@@ -274,11 +295,18 @@ __global__ void __launch_bounds__(256) rr_solve_kernel(int b, int ncomp, const d
         if (q < m) {
           const double apq = T[p * m + q];
           const double app = T[p * m + p], aqq = T[q * m + q];
-          if (fabs(apq) > 1e-300 && fabs(apq) > 1e-15 * sqrt(fabs(app * aqq))) {
-            const double theta = (aqq - app) / (2.0 * apq);
-            const double t = (theta >= 0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
-            cs = 1.0 / sqrt(t * t + 1.0);
-            sn = t * cs;
+          if (fabs(apq) > 1e-300 && fabs(apq) * fabs(apq) > 1e-30 * fabs(app * aqq)) {
+            // tangent of the rotation angle in FP32 (the rotation stays exactly orthogonal in FP64;
+            // an FP32 angle leaves ~1e-7 of apq, removed by the next sweep), cos by one FP64
+            // Newton step on rsqrt, so the loop has no FP64 division or square root
+            const float theta = (float)((aqq - app) / (2.0 * apq));
+            const float tf = (theta >= 0.f ? 1.f : -1.f) / (fabsf(theta) + sqrtf(fmaf(theta, theta, 1.f)));
+            const double t = (double)tf, x = fma(t, t, 1.0);
+            double y = (double)rsqrtf((float)x);
+            y = y * fma(-0.5 * x, y * y, 1.5);
+            y = y * fma(-0.5 * x, y * y, 1.5);
+            cs = y;
+            sn = t * y;
           }
         }
         s_p[tid] = p;
@@ -391,7 +419,7 @@ int subspace_block(int P, int ncomp) {
 int eig_top_subspace(annf_handle* h, const double* C, int P, int ncomp, int iters, double* comps, cudaStream_t st) {
   const int b = subspace_block(P, ncomp);
   ANNF_REQUIRE(b > 0, "subspace eigensolver: unsupported size");
-  const size_t smem = (size_t)2 * b * P * sizeof(float);
+  const size_t smem = ((size_t)2 * b * P + (size_t)b * b) * sizeof(float);
   ANNF_REQUIRE(smem <= 200 * 1024, "subspace eigensolver: block too large for shared memory");
   const size_t f32_bytes = ((size_t)P * P + (size_t)b * P) * sizeof(float);
   const size_t f64_bytes = ((size_t)b * P + 2 * (size_t)b * b + (size_t)ncomp * b) * sizeof(double);

@@ -345,7 +345,7 @@ __global__ void __launch_bounds__(256, 2) fast_prop_t_kernel(Img A, Img B, int n
 
 int fast_search(annf_handle* h, const uint8_t* img_a, int ha, int wa, const uint8_t* img_b, int hb, int wb, int c,
                 int psize, int K, const int* nat_pos, const int* prop, int n_prop, int iters, uint32_t seed,
-                int* final_idx, float* dist_out, cudaStream_t st) {
+                int rand_samples, int radius0, int* final_idx, float* dist_out, cudaStream_t st) {
   Img A{img_a, ha, wa, c, psize, wa - psize + 1, (long long)ha * wa * c};
   Img B{img_b, hb, wb, c, psize, wb - psize + 1, (long long)hb * wb * c};
   const int nA = (ha - psize + 1) * A.ncols;
@@ -370,17 +370,17 @@ int fast_search(annf_handle* h, const uint8_t* img_a, int ha, int wa, const uint
   prof_mark(h, "fast_init", st);
   for (int it = 0; it < iters; ++it) {
     const int jump = 1;
-    const int radius = std::max(1, 8 >> it);
+    const int radius = std::max(1, radius0 >> it);
     const uint32_t sd = seed * 7919u + (uint32_t)it;
     if (special) {
       switch (shape) {
-        case 927: ANNF_FAST_PROP(9, 27, A, B, nA, jump, radius, 2, sd, m0, m1); break;
-        case 721: ANNF_FAST_PROP(7, 21, A, B, nA, jump, radius, 2, sd, m0, m1); break;
-        case 515: ANNF_FAST_PROP(5, 15, A, B, nA, jump, radius, 2, sd, m0, m1); break;
-        default: ANNF_FAST_PROP(11, 33, A, B, nA, jump, radius, 2, sd, m0, m1); break;
+        case 927: ANNF_FAST_PROP(9, 27, A, B, nA, jump, radius, rand_samples, sd, m0, m1); break;
+        case 721: ANNF_FAST_PROP(7, 21, A, B, nA, jump, radius, rand_samples, sd, m0, m1); break;
+        case 515: ANNF_FAST_PROP(5, 15, A, B, nA, jump, radius, rand_samples, sd, m0, m1); break;
+        default: ANNF_FAST_PROP(11, 33, A, B, nA, jump, radius, rand_samples, sd, m0, m1); break;
       }
     } else {
-      fast_prop_kernel<<<blocks, 256, 0, st>>>(A, B, nA, jump, radius, 2, sd, m0, m1);
+      fast_prop_kernel<<<blocks, 256, 0, st>>>(A, B, nA, jump, radius, rand_samples, sd, m0, m1);
     }
     ANNF_CHECK_LAUNCH();
     std::swap(m0, m1);

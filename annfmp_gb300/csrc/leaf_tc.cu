@@ -2,13 +2,13 @@
 //
 // Queries are grouped by the leaf their descent reaches (counting sort on the leaf id). For each
 // leaf, the leaf's points (<= 256) and up to 128 of its queries are centred on the leaf's bounding
-// box midpoint, rounded to BF16 and staged in shared memory as K-major core-matrix tiles; one
-// tcgen05.mma (M = 128 queries, N = leaf points, K = 16 or 32 dims) per 16 dims leaves a . b in an
-// FP32 TMEM accumulator. Each thread owns one query (one TMEM lane): it reads its row with
-// tcgen05.ld and re-ranks with the exact FP32 distance (reference operation order) only the points
-// whose BF16 estimate passes a proven error bound (below), so the k-list written equals the FP32
-// leaf scan's. Centring keeps the BF16 products free of the cancellation that |a|^2 + |b|^2 - 2 a.b
-// suffers on uncentred reduced coordinates.
+// box midpoint and staged in shared memory as K-major core-matrix tiles: BF16 hi/lo splits of each
+// coordinate ([hi|lo|hi] against [hi|hi|lo], three MMAs per 16 dims) or one FP16 term. tcgen05.mma
+// (M = 128 queries, N = leaf points) accumulates a.b in FP32 in TMEM. Each thread owns one query
+// (one TMEM lane): it reads its row with tcgen05.ld and re-ranks with the exact FP32 distance
+// (reference operation order) only the points whose estimate passes a proven error bound (below),
+// so the k-list written equals the FP32 leaf scan's. Centring keeps the products free of the
+// cancellation that |a|^2 + |b|^2 - 2 a.b suffers on uncentred reduced coordinates.
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 
@@ -26,25 +26,37 @@ int num_sms();
 constexpr int kTcThreads = 128;                    // one warpgroup: thread t <-> TMEM lane t <-> query t
 constexpr long long kTcWaitCycles = 2000000000LL;  // ~1 s at 2 GHz: bound of every mbarrier wait
 
-// operand precision of the leaf tiles: BF16 (8-bit significand) or FP16 (11-bit significand)
+// Operand precision of the leaf tiles. BF16 (PREC 0) splits every centred coordinate x into
+// hi = bf16(x) and lo = bf16(x - hi) (|x - hi - lo| <= 2^-16 |x|) and accumulates
+// hi.hi + hi.lo + lo.hi, so that |dot - (a-c).(b-c)| <= (3 * 2^-16 + 2^-20) |a-c| |b-c|; FP16 (PREC 1)
+// uses one term, |dot - (a-c).(b-c)| <= (2^-10 + 2^-20) |a-c| |b-c|. kDot is that coefficient with a
+// margin; the K extent of a tile is kSplit x the padded dimension.
 template <int PREC> struct TcPrec;
 template <> struct TcPrec<0> {
-  static constexpr float kEta = 0.001955f;  // 2^-9 (1 + 2^-10): BF16 rounding of the centred values
-  __device__ static float round(float x) { return __bfloat162float(__float2bfloat16_rn(x)); }
+  static constexpr int kSplit = 3;
+  static constexpr float kDot = 5.0e-5f;  // > 3 * 2^-16 + 2^-20 = 4.67e-5
+  __device__ static void split(float x, float& hi, float& lo) {
+    hi = __bfloat162float(__float2bfloat16_rn(x));
+    lo = __bfloat162float(__float2bfloat16_rn(x - hi));
+  }
   __device__ static uint32_t pack(float lo, float hi) {
     __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
     return *reinterpret_cast<uint32_t*>(&v);
   }
-  static constexpr uint32_t idesc(int M, int N) { return tc::idesc_bf16(M, N); }
+  __host__ __device__ static constexpr uint32_t idesc(int M, int N) { return tc::idesc_bf16(M, N); }
 };
 template <> struct TcPrec<1> {
-  static constexpr float kEta = 0.000489f;  // 2^-11 (1 + 2^-10): FP16 rounding (values far below 65504)
-  __device__ static float round(float x) { return __half2float(__float2half_rn(x)); }
+  static constexpr int kSplit = 1;
+  static constexpr float kDot = 1.0e-3f;  // > 2^-10 + 2^-20 = 9.77e-4 (centred values far below 65504)
+  __device__ static void split(float x, float& hi, float& lo) {
+    hi = __half2float(__float2half_rn(x));
+    lo = 0.f;
+  }
   __device__ static uint32_t pack(float lo, float hi) {
     __half2 v = __floats2half2_rn(lo, hi);
     return *reinterpret_cast<uint32_t*>(&v);
   }
-  static constexpr uint32_t idesc(int M, int N) { return tc::idesc_f16(M, N); }
+  __host__ __device__ static constexpr uint32_t idesc(int M, int N) { return tc::idesc_f16(M, N); }
 };
 
 __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
@@ -81,14 +93,15 @@ __global__ void __launch_bounds__(256) qleaf_kernel(TreeView<float> tv, const fl
   }
 }
 
-// exclusive scan of cnt[L] into off[L+1] and cursor[L] (one CTA of 1024 threads)
-__global__ void __launch_bounds__(1024) leaf_scan_kernel(const int* __restrict__ cnt, int L, int* __restrict__ off,
-                                                         int* __restrict__ cursor) {
+// exclusive scans of cnt[L] into off[L+1] and cursor[L], and of the 128-query chunk counts into
+// choff[L+1] (one CTA of 1024 threads; the chunk scan is a second pass of the same code)
+__device__ void block_exclusive_scan(const int* __restrict__ cnt, int L, bool chunks, int* __restrict__ off,
+                                     int* __restrict__ cursor) {
   __shared__ int warp_tot[32];
   const int per = (L + blockDim.x - 1) / blockDim.x;
   const int b0 = threadIdx.x * per, b1 = min(L, b0 + per);
   int s = 0;
-  for (int i = b0; i < b1; ++i) s += cnt[i];
+  for (int i = b0; i < b1; ++i) s += chunks ? (cnt[i] + kTcThreads - 1) / kTcThreads : cnt[i];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   int x = s;
 #pragma unroll
@@ -111,10 +124,17 @@ __global__ void __launch_bounds__(1024) leaf_scan_kernel(const int* __restrict__
   int run = x - s + (w ? warp_tot[w - 1] : 0);
   for (int i = b0; i < b1; ++i) {
     off[i] = run;
-    cursor[i] = run;
-    run += cnt[i];
+    if (cursor) cursor[i] = run;
+    run += chunks ? (cnt[i] + kTcThreads - 1) / kTcThreads : cnt[i];
   }
   if (threadIdx.x == blockDim.x - 1) off[L] = run;
+  __syncthreads();
+}
+
+__global__ void __launch_bounds__(1024) leaf_scan_kernel(const int* __restrict__ cnt, int L, int* __restrict__ off,
+                                                         int* __restrict__ cursor, int* __restrict__ choff) {
+  block_exclusive_scan(cnt, L, false, off, cursor);
+  block_exclusive_scan(cnt, L, true, choff, nullptr);
 }
 
 __global__ void qscatter_kernel(const int* __restrict__ qleaf, long long nq, int* __restrict__ cursor,
@@ -126,32 +146,43 @@ __global__ void qscatter_kernel(const int* __restrict__ qleaf, long long nq, int
 // ---------------------------------------------------------------------------------------------
 // the tensor-core leaf kernel
 //
-// Selection with a proven BF16 error bound. With centre c, a' = bf16(a - c), b' = bf16(b - c):
-// |(a'-b') - (a-b)| <= eta = 2^-9 (|a - c| + R) (R bounds |b - c| over the leaf), so the BF16
-// distance E_j = |a' - b'_j| is within eta of the true D_j = |a - b_j|. If E_(k) is the k-th smallest
-// E, every point of the true (and of the FP32-computed) k nearest has E_j <= E_(k) + 2 eta, up to
-// FP32 rounding. Pass 1 finds E_(k) from the tile (est_j = |b'_j|^2 - 2 a'.b'_j = E_j^2 - |a'|^2);
-// pass 2 re-ranks exactly (FP32, reference order) every point whose estimate passes that bound.
-// The result equals the FP32 leaf scan; the exact work is usually a handful of points.
+// Selection with a proven error bound. With centre c, est_j = |b_j - c|^2 - 2 dot_j (the norm in
+// FP32 from the FP32 points, dot_j from the tile) estimates D_j^2 - |a - c|^2, D_j = |a - b_j|, to
+// within delta = 2 kDot |a-c| R + FP32 slack (R bounds |b - c| over the leaf). Every point of the
+// true (and of the FP32-computed) k nearest then has est_j <= est_(k) + 2 delta, est_(k) the k-th
+// smallest estimate. Pass 1 finds est_(k) from the tile; pass 2 re-ranks exactly (FP32, reference
+// order) every point within that band, so the k-list equals the FP32 leaf scan's. With the BF16
+// split the band is ~1e-4 |a-c| R, which leaves about k points to re-rank.
 // ---------------------------------------------------------------------------------------------
+// branch-free insertion into an ascending list (lanes of a warp hold different queries, so a
+// data-dependent branch would run the insertion for every column in which any lane inserts)
 template <int KM>
 __device__ __forceinline__ void sorted_insert(float (&dv)[KM], int (&iv)[KM], float v, int c) {
-  if (!(v < dv[KM - 1])) return;
+  // the new entry goes before the first strictly larger one (after equal ones); every entry from
+  // there on shifts one place, keeping the order of equal entries
+  bool shifting = false;
+  float cd = 0.f;
+  int ci = 0;
 #pragma unroll
-  for (int j = KM - 1; j > 0; --j) {
-    const bool shift = v < dv[j - 1];
-    const bool here = !shift && v < dv[j];
-    if (shift) {
-      dv[j] = dv[j - 1];
-      iv[j] = iv[j - 1];
-    } else if (here) {
-      dv[j] = v;
-      iv[j] = c;
-    }
+  for (int j = 0; j < KM; ++j) {
+    const bool put = !shifting && v < dv[j];
+    const float od = dv[j];
+    const int oi = iv[j];
+    dv[j] = put ? v : (shifting ? cd : od);
+    iv[j] = put ? c : (shifting ? ci : oi);
+    cd = od;
+    ci = oi;
+    shifting = shifting || put;
   }
-  if (v < dv[0]) {
-    dv[0] = v;
-    iv[0] = c;
+}
+// the KM smallest values only (min/max network)
+template <int KM>
+__device__ __forceinline__ void smallest_insert(float (&dv)[KM], float v) {
+#pragma unroll
+  for (int j = 0; j < KM; ++j) {
+    const float lo = fminf(v, dv[j]);
+    v = fmaxf(v, dv[j]);
+    dv[j] = lo;
   }
 }
 
@@ -160,6 +191,7 @@ struct TcLeafArgs {
   const float* Q;
   const int* qoff;    // [L+1] queries of leaf l: qorder[qoff[l] .. qoff[l+1])
   const int* qorder;  // [nq]
+  const int* choff;   // [L+1] work items (128-query chunks) of leaf l: choff[l] .. choff[l+1]-1
   int K;              // neighbours written per query (<= KM)
   int npad;           // point rows staged per leaf (multiple of 16, >= largest leaf, <= 256)
   int ncols;          // TMEM columns allocated (power of two >= max(32, npad))
@@ -170,15 +202,16 @@ struct TcLeafArgs {
 template <int KM, int KPAD, int PREC>
 __global__ void __launch_bounds__(kTcThreads) leaf_tc_kernel(TcLeafArgs a) {
   using PR = TcPrec<PREC>;
+  constexpr int KT = PR::kSplit * KPAD;  // K extent of the tiles
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   const TreeView<float>& tv = a.tv;
   const int d = tv.d, L = 1 << tv.depth, npad = a.npad, K = a.K;
   // carve: A tile, B tile (core-matrix layouts), FP32 leaf points, norms, centre, barrier, TMEM slot
   unsigned char* p = smem_raw;
   unsigned char* sA = p;
-  p += kTcThreads * KPAD * 2;
+  p += kTcThreads * KT * 2;
   unsigned char* sB = p;
-  p += (size_t)npad * KPAD * 2;
+  p += (size_t)npad * KT * 2;
   float* sP = reinterpret_cast<float*>(p);  // [npad][KPAD] FP32 leaf points (zero padded)
   p += (size_t)npad * KPAD * 4;
   float* sN = reinterpret_cast<float*>(p);
@@ -214,20 +247,32 @@ __global__ void __launch_bounds__(kTcThreads) leaf_tc_kernel(TcLeafArgs a) {
   bool aborted = false;
   const bool vec4 = (d & 3) == 0;
 
+  const int total = __ldg(a.choff + L);
+  int staged = -1;  // leaf whose points are in shared memory
   for (;;) {
-    __syncthreads();  // every thread has read the previous leaf id
+    __syncthreads();  // every thread has read the previous work item
     if (tid == 0) sflag[0] = atomicAdd(a.work, 1);
     __syncthreads();
-    const int l = sflag[0];
-    if (l >= L) break;
-    const int qb = __ldg(a.qoff + l), qe = __ldg(a.qoff + l + 1);
-    if (qb == qe) continue;  // uniform: every thread read the same leaf
+    const int w = sflag[0];
+    if (w >= total) break;
+    // leaf of work item w: the last l with choff[l] <= w (leaves without queries have no items)
+    int lo = 0, hi = L;
+    while (hi - lo > 1) {
+      const int mid = (lo + hi) >> 1;
+      if (__ldg(a.choff + mid) <= w) lo = mid;
+      else hi = mid;
+    }
+    const int l = lo;
+    const int qlb = __ldg(a.qoff + l), qle = __ldg(a.qoff + l + 1);
+    const int qb = qlb + (w - __ldg(a.choff + l)) * kTcThreads, qe = min(qle, qb + kTcThreads);
     const int pb = __ldg(tv.leaf_begin + l);
     int np = __ldg(tv.leaf_begin + l + 1) - pb;
     if (np > npad) {
-      if (tid == 0) atomicOr(tv.status, DEV_BAD_LEAF);
+      if (tid == 0 && l != staged) atomicOr(tv.status, DEV_BAD_LEAF);
       np = npad;
     }
+    if (l != staged) {  // uniform
+    staged = l;
     // centre (box midpoint) and half-diagonal R of the leaf box
     if (tid < 32) {
       float r2 = 0.f;
@@ -270,27 +315,39 @@ __global__ void __launch_bounds__(kTcThreads) leaf_tc_kernel(TcLeafArgs a) {
       float nrm = 0.f;
 #pragma unroll
       for (int k8 = 0; k8 < KPAD; k8 += 8) {
-        float v[8];
+        float hi[8], lo[8];
 #pragma unroll
         for (int u = 0; u < 8; ++u) {
           const int j = k8 + u;
-          v[u] = (r < np && j < d) ? PR::round(f[j] - sC[j]) : 0.f;
-          nrm = fmaf(v[u], v[u], nrm);
+          const float x = (r < np && j < d) ? f[j] - sC[j] : 0.f;
+          nrm = fmaf(x, x, nrm);
+          PR::split(x, hi[u], lo[u]);
         }
-        uint4 w;
-        w.x = PR::pack(v[0], v[1]);
-        w.y = PR::pack(v[2], v[3]);
-        w.z = PR::pack(v[4], v[5]);
-        w.w = PR::pack(v[6], v[7]);
-        *reinterpret_cast<uint4*>(sB + tc::core_offset(r, k8, KPAD)) = w;
+        uint4 wh, wl;
+        wh.x = PR::pack(hi[0], hi[1]);
+        wh.y = PR::pack(hi[2], hi[3]);
+        wh.z = PR::pack(hi[4], hi[5]);
+        wh.w = PR::pack(hi[6], hi[7]);
+        wl.x = PR::pack(lo[0], lo[1]);
+        wl.y = PR::pack(lo[2], lo[3]);
+        wl.z = PR::pack(lo[4], lo[5]);
+        wl.w = PR::pack(lo[6], lo[7]);
+        // B row: [hi | hi | lo] against A row [hi | lo | hi]
+        *reinterpret_cast<uint4*>(sB + tc::core_offset(r, k8, KT)) = wh;
+        if constexpr (PR::kSplit == 3) {
+          *reinterpret_cast<uint4*>(sB + tc::core_offset(r, KPAD + k8, KT)) = wh;
+          *reinterpret_cast<uint4*>(sB + tc::core_offset(r, 2 * KPAD + k8, KT)) = wl;
+        }
       }
 #pragma unroll
       for (int j = 0; j < KPAD; j += 4)
         *reinterpret_cast<float4*>(sP + r * KPAD + j) = make_float4(f[j], f[j + 1], f[j + 2], f[j + 3]);
       sN[r] = r < np ? nrm : FLT_MAX;
     }
+    }  // staging
     const float R = sC[KPAD];
-    for (int q0 = qb; q0 < qe; q0 += kTcThreads) {
+    {
+      const int q0 = qb;
       const int qi = (q0 + tid < qe) ? __ldg(a.qorder + q0 + tid) : -1;
       float qf[KPAD];
       if (qi >= 0 && vec4) {
@@ -310,24 +367,31 @@ __global__ void __launch_bounds__(kTcThreads) leaf_tc_kernel(TcLeafArgs a) {
 #pragma unroll
         for (int j = 0; j < KPAD; ++j) qf[j] = (qi >= 0 && j < d) ? __ldg(a.Q + (size_t)qi * d + j) : 0.f;
       }
-      float a2 = 0.f, ac2 = 0.f, amax = 0.f;
+      float ac2 = 0.f, amax = 0.f;
 #pragma unroll
       for (int k8 = 0; k8 < KPAD; k8 += 8) {
-        float v[8];
+        float hi[8], lo[8];
 #pragma unroll
         for (int u = 0; u < 8; ++u) {
-          const float t = (k8 + u < d) ? qf[k8 + u] - sC[k8 + u] : 0.f;
+          const float t = (qi >= 0 && k8 + u < d) ? qf[k8 + u] - sC[k8 + u] : 0.f;
           ac2 = fmaf(t, t, ac2);
           amax = fmaxf(amax, fabsf(t));
-          v[u] = (qi >= 0) ? PR::round(t) : 0.f;
-          a2 = fmaf(v[u], v[u], a2);
+          PR::split(t, hi[u], lo[u]);
         }
-        uint4 w;
-        w.x = PR::pack(v[0], v[1]);
-        w.y = PR::pack(v[2], v[3]);
-        w.z = PR::pack(v[4], v[5]);
-        w.w = PR::pack(v[6], v[7]);
-        *reinterpret_cast<uint4*>(sA + tc::core_offset(tid, k8, KPAD)) = w;
+        uint4 wh, wl;
+        wh.x = PR::pack(hi[0], hi[1]);
+        wh.y = PR::pack(hi[2], hi[3]);
+        wh.z = PR::pack(hi[4], hi[5]);
+        wh.w = PR::pack(hi[6], hi[7]);
+        wl.x = PR::pack(lo[0], lo[1]);
+        wl.y = PR::pack(lo[2], lo[3]);
+        wl.z = PR::pack(lo[4], lo[5]);
+        wl.w = PR::pack(lo[6], lo[7]);
+        *reinterpret_cast<uint4*>(sA + tc::core_offset(tid, k8, KT)) = wh;
+        if constexpr (PR::kSplit == 3) {
+          *reinterpret_cast<uint4*>(sA + tc::core_offset(tid, KPAD + k8, KT)) = wl;
+          *reinterpret_cast<uint4*>(sA + tc::core_offset(tid, 2 * KPAD + k8, KT)) = wh;
+        }
       }
       tc::fence_async_smem();
       tc::fence_before_sync();
@@ -335,9 +399,9 @@ __global__ void __launch_bounds__(kTcThreads) leaf_tc_kernel(TcLeafArgs a) {
       if (tid == 0) {
         tc::fence_after_sync();
 #pragma unroll
-        for (int kk = 0; kk < KPAD / 16; ++kk) {
-          const uint64_t ad = tc::sdesc(sA + kk * 256, 128, (KPAD / 8) * 128);
-          const uint64_t bd = tc::sdesc(sB + kk * 256, 128, (KPAD / 8) * 128);
+        for (int kk = 0; kk < KT / 16; ++kk) {
+          const uint64_t ad = tc::sdesc(sA + kk * 256, 128, (KT / 8) * 128);
+          const uint64_t bd = tc::sdesc(sB + kk * 256, 128, (KT / 8) * 128);
           tc::mma_bf16(tmem, ad, bd, idesc, kk > 0 ? 1u : 0u);
         }
         tc::mma_commit(mbar);
@@ -350,37 +414,27 @@ __global__ void __launch_bounds__(kTcThreads) leaf_tc_kernel(TcLeafArgs a) {
         break;
       }
       tc::fence_after_sync();
-      // pass 1: the KM smallest estimates
+      // pass 1: the KM smallest estimates (padding columns carry sN = FLT_MAX)
       float ev[KM];
-      int ei[KM];
 #pragma unroll
-      for (int j = 0; j < KM; ++j) {
-        ev[j] = FLT_MAX;
-        ei[j] = -1;
-      }
+      for (int j = 0; j < KM; ++j) ev[j] = FLT_MAX;
       for (int c0 = 0; c0 < npad; c0 += 16) {
         uint32_t r[16];
         tc::tmem_ld16(trow + (uint32_t)c0, r);
         tc::tmem_wait_ld();
-        if (qi >= 0) {
 #pragma unroll
-          for (int j = 0; j < 16; ++j) {
-            const float est = fmaf(-2.f, __uint_as_float(r[j]), sN[c0 + j]);
-            if (c0 + j < np) sorted_insert<KM>(ev, ei, est, c0 + j);
-          }
-        }
+        for (int j = 0; j < 16; ++j) smallest_insert<KM>(ev, fmaf(-2.f, __uint_as_float(r[j]), sN[c0 + j]));
       }
-      // bound: est_j <= (sqrt(est_(k) + |a'|^2 + s) + 2 eta)^2 (1 + 4e-6) - |a'|^2 + s
-      const float eta = PR::kEta * (sqrtf(ac2) * 1.000001f + R);  // rounding bound x (|a-c| + R)
-      const float slack = 1.53e-5f * (a2 + R * R * 1.01f);        // ~2^-16 (|a'|^2 + |b'|^2 max)
+      // band: est_j <= est_(k) + 2 delta, delta = 2 kDot |a-c| R + FP32 slack
       float evk = FLT_MAX;
 #pragma unroll
       for (int j = 0; j < KM; ++j)
         if (j == K - 1) evk = ev[j];
-      const float ek = evk >= FLT_MAX ? FLT_MAX : sqrtf(fmaxf(evk + a2 + slack, 0.f));
+      const float acn = sqrtf(ac2) * 1.000001f;
+      const float delta = 2.f * PR::kDot * acn * R + 4e-6f * (ac2 + R * R + fabsf(evk));
       // FP16 cannot hold centred values beyond its range: such queries and leaves take every point
       const bool unsafe = PREC == 1 && (amax > 60000.f || R > 60000.f);
-      const float tau = (ek >= FLT_MAX || unsafe) ? FLT_MAX : (ek + 2.f * eta) * (ek + 2.f * eta) * 1.000004f - a2 + slack;
+      const float tau = (evk >= FLT_MAX || unsafe) ? FLT_MAX : evk + 2.f * delta;
       // pass 2: exact FP32 distance (reference order) of every point passing the bound
       float xv[KM];
       int xi[KM];
@@ -429,7 +483,6 @@ __global__ void __launch_bounds__(kTcThreads) leaf_tc_kernel(TcLeafArgs a) {
       __syncthreads();
     }
     if (aborted) break;
-    __syncthreads();
   }
   if (aborted) {  // let the MMA in flight finish (bounded) before the columns are freed
     if (tid == 0) atomicOr(tv.status, DEV_TC_TIMEOUT);
@@ -478,15 +531,16 @@ int natural_knn_tc(annf_handle* h, const float* Q, long long nq, int K, int prec
   tv.point_leaf = h->point_leaf.as<int>();
   tv.status = h->status.as<unsigned>();
   tv.leaf_box = h->leaf_box.as<float>();
-  // scratch: qleaf[nq], qorder[nq], cnt[L], off[L+1], cursor[L], work counter
-  const size_t need = ((size_t)2 * nq + 3 * (size_t)L + 8) * sizeof(int);
+  // scratch: qleaf[nq], qorder[nq], cnt[L], off[L+1], cursor[L], choff[L+1], work counter
+  const size_t need = ((size_t)2 * nq + 4 * (size_t)L + 16) * sizeof(int);
   ANNF_ENSURE(h->tc_buf, need);
   int* qleaf = h->tc_buf.as<int>();
   int* qorder = qleaf + nq;
   int* cnt = qorder + nq;
   int* off = cnt + L;
   int* cursor = off + L + 1;
-  int* work = cursor + L;
+  int* choff = cursor + L;
+  int* work = choff + L + 1;
   ANNF_CUDA_TRY(cudaMemsetAsync(cnt, 0, (size_t)L * sizeof(int), st));
   ANNF_CUDA_TRY(cudaMemsetAsync(work, 0, sizeof(int), st));
   const size_t ncs = NodeCache<float>::bytes(h->depth);
@@ -494,7 +548,7 @@ int natural_knn_tc(annf_handle* h, const float* Q, long long nq, int K, int prec
   const int blocks = (int)std::min<long long>(ceil_div(nq, 256), 8LL * num_sms());
   qleaf_kernel<<<blocks, 256, ncs, st>>>(tv, Q, nq, qleaf, cnt);
   ANNF_CHECK_LAUNCH();
-  leaf_scan_kernel<<<1, 1024, 0, st>>>(cnt, L, off, cursor);
+  leaf_scan_kernel<<<1, 1024, 0, st>>>(cnt, L, off, cursor, choff);
   ANNF_CHECK_LAUNCH();
   qscatter_kernel<<<blocks, 256, 0, st>>>(qleaf, nq, cursor, qorder);
   ANNF_CHECK_LAUNCH();
@@ -505,13 +559,15 @@ int natural_knn_tc(annf_handle* h, const float* Q, long long nq, int K, int prec
   args.Q = Q;
   args.qoff = off;
   args.qorder = qorder;
+  args.choff = choff;
   args.K = K;
   args.npad = (h->max_leaf + 15) / 16 * 16;
   args.ncols = std::max(32, next_pow2(args.npad));
   args.out_pos = out_pos;
   args.work = work;
   const int kpad = h->d <= 16 ? 16 : 32;
-  const size_t carve = (size_t)kTcThreads * kpad * 2 + (size_t)args.npad * kpad * 2 + (size_t)args.npad * kpad * 4 +
+  const int kt = (prec == 0 ? 3 : 1) * kpad;  // K extent of the tiles (BF16 hi/lo split: 3 terms)
+  const size_t carve = (size_t)kTcThreads * kt * 2 + (size_t)args.npad * kt * 2 + (size_t)args.npad * kpad * 4 +
                        (size_t)args.npad * 4 + (kpad + 4) * 4 + 16 + 24 + 64;
   // at most 512 / ncols CTAs may hold TMEM on one SM: pad the shared memory so no more fit
   const int per_sm = std::max(1, 512 / args.ncols);

@@ -2,8 +2,10 @@
 //
 // For the approximate NNF forms: every psize x psize x c patch of an image times the BF16-rounded
 // components, FP32 accumulation, minus the projected mean. One tile = 128 consecutive patches of one
-// row: the psize image rows they cover are staged in shared memory, each thread pair expands one
-// patch into the K-major BF16 A tile (core-matrix layout, K = P rounded up to 16), and tcgen05.mma
+// row: the psize image rows they cover are staged in shared memory (aligned 32-bit loads), each thread
+// pair expands one patch into the K-major BF16 A tile (core-matrix layout; K runs over the patch
+// rows, each padded to a multiple of 8 bytes so that a group of 8 is 8 consecutive image bytes, and
+// the components are permuted to match), and tcgen05.mma
 // (M = 128, N = components rounded up to 16) accumulates in TMEM; the epilogue reads TMEM, subtracts
 // the mean term and writes FP32 reduced patches. Pixel values 0..255 are exact in BF16 and every
 // product is exact in FP32, so the only rounding beyond FP32 summation is that of the components.
@@ -23,11 +25,6 @@ int num_sms();
 constexpr int kPjThreads = 256;  // two threads per patch row of the tile
 constexpr long long kPjWaitCycles = 2000000000LL;
 
-__device__ __forceinline__ uint32_t pj_pack(float lo, float hi) {
-  __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
-  return *reinterpret_cast<uint32_t*>(&v);
-}
-
 __device__ __forceinline__ bool pj_wait(uint64_t* mbar, uint32_t phase) {
   const long long t0 = clock64();
   while (!tc::mbar_try_wait(mbar, phase)) {
@@ -36,12 +33,17 @@ __device__ __forceinline__ bool pj_wait(uint64_t* mbar, uint32_t phase) {
   return true;
 }
 
-// B operand [npad][kpad] BF16 row-major (zero padded) and the FP32 mean term m_j = sum_k bf16(c_jk) mean_k
+// B operand [npad][kpad] BF16 row-major, K in the tile's order (patch row r occupies
+// [r*rs, r*rs + psize*C) with rs = psize*C rounded up to 8; padding zero), and the FP32 mean term
+// m_j = sum_k bf16(c_jk) mean_k
 __global__ void pj_prep_kernel(const double* __restrict__ comps, const double* __restrict__ mean, int d, int P,
-                               int npad, int kpad, uint16_t* __restrict__ bmat, float* __restrict__ mterm) {
+                               int rowlen, int rs, int npad, int kpad, uint16_t* __restrict__ bmat,
+                               float* __restrict__ mterm) {
   for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < npad * kpad; e += gridDim.x * blockDim.x) {
     const int j = e / kpad, k = e - j * kpad;
-    const float v = (j < d && k < P) ? (float)comps[(size_t)j * P + k] : 0.f;
+    const int r = k / rs, el = k - r * rs;
+    const int src = r * rowlen + el;
+    const float v = (j < d && el < rowlen && src < P) ? (float)comps[(size_t)j * P + src] : 0.f;
     __nv_bfloat16 b = __float2bfloat16_rn(v);
     bmat[e] = *reinterpret_cast<uint16_t*>(&b);
   }
@@ -55,6 +57,17 @@ __global__ void pj_prep_kernel(const double* __restrict__ comps, const double* _
   }
 }
 
+// eight BF16 values of eight consecutive bytes (two words), bytes at or beyond `valid` zeroed
+__device__ __forceinline__ uint4 bytes_to_bf16x8(uint32_t w0, uint32_t w1, int valid) {
+  uint32_t v[8];
+#pragma unroll
+  for (int u = 0; u < 8; ++u) {
+    const uint32_t b = ((u < 4 ? w0 : w1) >> (8 * (u & 3))) & 0xFFu;
+    v[u] = u < valid ? (__float_as_uint(__uint2float_rn(b)) >> 16) : 0u;  // exact: b < 256
+  }
+  return make_uint4(v[0] | (v[1] << 16), v[2] | (v[3] << 16), v[4] | (v[5] << 16), v[6] | (v[7] << 16));
+}
+
 template <int NPAD>
 __global__ void __launch_bounds__(kPjThreads) project_tc_kernel(const uint8_t* __restrict__ img, int H, int W, int C,
                                                                 int psize, int d, int kpad,
@@ -62,11 +75,12 @@ __global__ void __launch_bounds__(kPjThreads) project_tc_kernel(const uint8_t* _
                                                                 const float* __restrict__ mterm, float* __restrict__ out,
                                                                 unsigned* status) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
-  const int P = psize * psize * C;
+  const int rowlen = psize * C, rs = (rowlen + 7) & ~7;
   const int ncols = W - psize + 1, nrows = H - psize + 1;
   const int tiles_x = (ncols + 127) / 128;
   const long long ntiles = (long long)tiles_x * nrows;
-  const int sw = ((128 + psize - 1) * C + 15) & ~15;  // staged row pitch (bytes)
+  const long long nbytes = (long long)H * W * C;
+  const int sw = (((128 + psize - 1) * C + 3 + 16) + 15) & ~15;  // staged row pitch: span + alignment shift + slack
   unsigned char* p = smem_raw;
   unsigned char* sA = p;
   p += (size_t)128 * kpad * 2;
@@ -74,9 +88,6 @@ __global__ void __launch_bounds__(kPjThreads) project_tc_kernel(const uint8_t* _
   p += (size_t)NPAD * kpad * 2;
   uint8_t* sI = p;
   p += (size_t)psize * sw;
-  p = reinterpret_cast<unsigned char*>(((uintptr_t)p + 3) & ~uintptr_t(3));
-  int16_t* koff = reinterpret_cast<int16_t*>(p);
-  p += (size_t)kpad * 2;
   p = reinterpret_cast<unsigned char*>(((uintptr_t)p + 15) & ~uintptr_t(15));
   uint64_t* mbar = reinterpret_cast<uint64_t*>(p);
   p += 8;
@@ -95,19 +106,11 @@ __global__ void __launch_bounds__(kPjThreads) project_tc_kernel(const uint8_t* _
     tc::mbar_fence_init();
     sflag[0] = 0;
   }
-  // components tile (core layout) and the patch-element offset table
+  // components tile (core layout)
   for (int e = tid; e < NPAD * (kpad / 8); e += kPjThreads) {
     const int r = e / (kpad / 8), k8 = (e - r * (kpad / 8)) * 8;
     *reinterpret_cast<uint4*>(sB + tc::core_offset(r, k8, kpad)) =
         *reinterpret_cast<const uint4*>(bmat + (size_t)r * kpad + k8);
-  }
-  for (int k = tid; k < kpad; k += kPjThreads) {
-    int v = -1;
-    if (k < P) {
-      const int r = k / (psize * C), rem = k - r * psize * C;
-      v = r * sw + rem;  // rem = c * C + ch: contiguous within the staged row
-    }
-    koff[k] = (int16_t)v;
   }
   tc::fence_before_sync();
   __syncthreads();
@@ -115,33 +118,42 @@ __global__ void __launch_bounds__(kPjThreads) project_tc_kernel(const uint8_t* _
   const uint32_t tmem = *tslot;
   const uint32_t idesc = tc::idesc_bf16(128, NPAD);
   const int row = tid & 127, half = tid >> 7;  // patch row of the tile; K half (expansion) / column half
-  const int ngrp = kpad / 8;
+  const int ngrp = kpad / 8, gpr = rs / 8;     // K groups in all / per patch row
   uint32_t phase = 0;
   for (long long t = blockIdx.x; t < ntiles; t += gridDim.x) {
     const int y = (int)(t / tiles_x), x0 = (int)(t - (long long)y * tiles_x) * 128;
     const int np = min(128, ncols - x0);
+    // stage the psize image rows as aligned words; byte b of row r sits at sI[r*sw + s0 + b]
+    const long long row0 = ((long long)y * W + x0) * C;
+    const int s0 = (int)(row0 & 3);
     const int span = (np + psize - 1) * C;
-    // stage the psize image rows of the tile
-    for (int e = tid; e < psize * span; e += kPjThreads) {
-      const int r = e / span, b = e - r * span;
-      sI[r * sw + b] = img[((size_t)(y + r) * W + x0) * C + b];
+    const int nw = (s0 + span + 3) >> 2;
+    for (int e = tid; e < psize * nw; e += kPjThreads) {
+      const int r = e / nw, wi = e - r * nw;
+      const long long a = row0 + (long long)r * W * C - s0 + 4LL * wi;  // 4-byte aligned
+      uint32_t v;
+      if (a + 4 <= nbytes) {
+        v = __ldg(reinterpret_cast<const uint32_t*>(img + a));
+      } else {  // the image's last bytes
+        v = 0;
+        for (int u = 0; u < 4; ++u)
+          if (a + u < nbytes) v |= (uint32_t)__ldg(img + a + u) << (8 * u);
+      }
+      *reinterpret_cast<uint32_t*>(sI + r * sw + 4 * wi) = v;
     }
     __syncthreads();
-    // expand: this thread's half of the K groups of patch `row`
+    // expand: group g of patch `row` = bytes [e0, e0 + 8) of its patch row r (zero beyond rowlen)
     const int g0 = half ? ngrp / 2 : 0, g1 = half ? ngrp : ngrp / 2;
-    const int base = row * C;
     for (int g = g0; g < g1; ++g) {
-      float v[8];
-#pragma unroll
-      for (int u = 0; u < 8; ++u) {
-        const int o = koff[g * 8 + u];
-        v[u] = (o >= 0 && row < np) ? (float)sI[base + o] : 0.f;
+      const int r = g / gpr, e0 = (g - r * gpr) * 8;
+      uint4 w = make_uint4(0u, 0u, 0u, 0u);
+      if (r < psize && row < np) {
+        const int off = r * sw + s0 + row * C + e0;
+        const uint32_t* wp = reinterpret_cast<const uint32_t*>(sI + (off & ~3));
+        const int sh = (off & 3) * 8;
+        const uint32_t q0 = wp[0], q1 = wp[1], q2 = wp[2];
+        w = bytes_to_bf16x8(__funnelshift_r(q0, q1, sh), __funnelshift_r(q1, q2, sh), rowlen - e0);
       }
-      uint4 w;
-      w.x = pj_pack(v[0], v[1]);
-      w.y = pj_pack(v[2], v[3]);
-      w.z = pj_pack(v[4], v[5]);
-      w.w = pj_pack(v[6], v[7]);
       *reinterpret_cast<uint4*>(sA + tc::core_offset(row, g * 8, kpad)) = w;
     }
     tc::fence_async_smem();
@@ -193,25 +205,26 @@ __global__ void __launch_bounds__(kPjThreads) project_tc_kernel(const uint8_t* _
 }
 
 bool project_tc_supported(int psize, int c, int ncomp) {
-  const int P = psize * psize * c;
-  return P >= 1 && P <= 256 && ncomp >= 1 && ncomp <= 32 && (128 + psize - 1) * c <= 4096;
+  const int rs = (psize * c + 7) & ~7;
+  return psize >= 1 && c >= 1 && psize * rs <= 320 && ncomp >= 1 && ncomp <= 32 && (128 + psize - 1) * c <= 4096;
 }
 
 int project_tc(annf_handle* h, const uint8_t* img, int H, int W, int c, int psize, const double* comps,
                const double* mean, int ncomp, float* out, cudaStream_t st) {
   ANNF_REQUIRE(project_tc_supported(psize, c, ncomp), "annf_project_bf16: patch or components too large");
   const int P = psize * psize * c;
-  const int kpad = (P + 15) / 16 * 16;
+  const int rowlen = psize * c, rs = (rowlen + 7) & ~7;
+  const int kpad = (psize * rs + 15) / 16 * 16;
   const int npad = ncomp <= 16 ? 16 : 32;
   ANNF_ENSURE(h->pj_buf, (size_t)npad * kpad * 2 + 64 * sizeof(float) + 256);
   uint16_t* bmat = h->pj_buf.as<uint16_t>();
   float* mterm = reinterpret_cast<float*>(reinterpret_cast<unsigned char*>(h->pj_buf.p) + (((size_t)npad * kpad * 2 + 255) & ~size_t(255)));
   prof_mark(h, "project:begin", st);
-  pj_prep_kernel<<<std::max(1, std::min(ceil_div(npad * kpad, 256), 64)), 256, 0, st>>>(comps, mean, ncomp, P, npad, kpad,
-                                                                                         bmat, mterm);
+  pj_prep_kernel<<<std::max(1, std::min(ceil_div(npad * kpad, 256), 64)), 256, 0, st>>>(comps, mean, ncomp, P, rowlen,
+                                                                                         rs, npad, kpad, bmat, mterm);
   ANNF_CHECK_LAUNCH();
-  const int sw = ((128 + psize - 1) * c + 15) & ~15;
-  const size_t smem = (size_t)128 * kpad * 2 + (size_t)npad * kpad * 2 + (size_t)psize * sw + 4 + (size_t)kpad * 2 + 16 + 24 + 64;
+  const int sw = (((128 + psize - 1) * c + 3 + 16) + 15) & ~15;
+  const size_t smem = (size_t)128 * kpad * 2 + (size_t)npad * kpad * 2 + (size_t)psize * sw + 16 + 24 + 64;
   ANNF_REQUIRE(smem <= 227 * 1024, "annf_project_bf16: tile too large for shared memory");
   const long long ntiles = (long long)((W - psize + 1 + 127) / 128) * (H - psize + 1);
   // TMEM: 32 columns per CTA, so any residency fits; two CTAs per SM by shared memory at P = 243

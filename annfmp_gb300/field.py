@@ -51,7 +51,7 @@ class _SubsetCache:
             j_s = rs.randint(n_w, size=m)
             pos = torch.from_numpy(numpy.stack([i_s, j_s], axis=1).astype(numpy.int32)).to(device)
         self._d[key] = pos
-        while len(self._d) > 16:
+        while len(self._d) > 1024:
             self._d.popitem(last=False)
         return pos
 
@@ -59,13 +59,26 @@ class _SubsetCache:
 _SUBSETS = _SubsetCache()
 
 
+class _Marks(dict):
+    """Stage events for the timers (no-ops when the call must stay free of host synchronisation)."""
+
+    class _Null:
+        def record(self):
+            pass
+
+    def __init__(self, timing):
+        super().__init__()
+        for k in ("t0", "t1", "t2", "t3", "t4"):
+            self[k] = torch.cuda.Event(enable_timing=True) if timing else _Marks._Null()
+
+
 class ANNFieldPropKDTreeGB300:
     FORMS = ("plain", "parallel")
 
     def __init__(self, n_neighbors=3, psize=8, dim_reduced=5, n_subset=1000, leaf_size=64, n_jobs=-1,
                  propagate=True, select_best_nn=True, float_type="float", verbose=1, seed=0, device=0,
-                 form="plain", iters=4, proposal=None, pca_solver=None, pca_iters=10, leaf_precision=None,
-                 projection=None):
+                 form="plain", iters=4, proposal=None, pca_solver=None, pca_iters=6, leaf_precision=None,
+                 projection=None, search=(2, 8)):
         """Reference parameters, plus: ``form`` "plain" (the reference's row-sequential method,
         the drop-in) or "parallel" (natural-leaf candidates + proposals + parallel propagation,
         every candidate checked by exact raw-patch distance); ``iters`` propagation passes of the
@@ -81,6 +94,7 @@ class ANNFieldPropKDTreeGB300:
         otherwise when the shapes allow it."""
         self.leaf_precision = leaf_precision
         self.projection = projection
+        self.search = search  # parallel form: (random offsets per pass, initial search radius)
         self.pca_solver = pca_solver
         self.pca_iters = pca_iters
         self.form = form
@@ -106,8 +120,11 @@ class ANNFieldPropKDTreeGB300:
             return torch.float64
         raise Exception("Unknown float type: {}".format(self.float_type))
 
-    def fit(self, image_a, image_b):
-        """image_a and image_b have shape (h, w, c), uint8 (numpy or torch)."""
+    def fit(self, image_a, image_b, sync=True):
+        """image_a and image_b have shape (h, w, c), uint8 (numpy or torch). sync=False (device
+        tensors only) enqueues the whole NNF on the current stream without any host
+        synchronisation, timing or status check, so that it can be captured into a CUDA graph; the
+        returned tensor is filled when the stream reaches it."""
         numpy.random.seed(self.seed)  # annfmp/openmp/base.py:60
         dev = require_cuda(self.device)
         real = self._get_torch_float_type()
@@ -143,7 +160,7 @@ class ANNFieldPropKDTreeGB300:
         tree.leaf_size = self.leaf_size
         tree.float_type = self.float_type
         h = tree.handle
-        ev = {k: torch.cuda.Event(enable_timing=True) for k in ("t0", "t1", "t2", "t3", "t4")}
+        ev = _Marks(sync)
         ev["t0"].record()
 
         # (1) PCA fit on the sampled subset (annfmp/openmp/base.py:168-191)
@@ -168,7 +185,9 @@ class ANNFieldPropKDTreeGB300:
         # (2)+(3) patches projected straight from the images (annfmp/openmp/base.py:152-166, 193-200)
         self.patches_a_reduced_ = torch.empty((n_a, d), dtype=real, device=dev)
         self.patches_b_reduced_ = torch.empty((n_b, d), dtype=real, device=dev)
-        proj = self.projection or "exact"
+        proj = self.projection
+        if proj is None:
+            proj = "bf16" if (self.form != "plain" and real == torch.float32 and p * p * c <= 256 and d <= 32) else "exact"
         if proj == "bf16":
             if real != torch.float32:
                 raise ValueError("the BF16 projection needs float_type='float'")
@@ -212,8 +231,12 @@ class ANNFieldPropKDTreeGB300:
             h.call("annf_parallel_nnf", ptr(nn), ptr(A), ha, wa, ptr(B), hb, wb, c, p,
                    ptr(self.patches_a_reduced_), k, ptr(prop), n_prop, int(self.iters), int(self.seed) & 0xFFFFFFFF,
                    {"bf16": _lib.ANNF_LEAF_BF16, "fp16": _lib.ANNF_LEAF_FP16, "fp32": _lib.ANNF_LEAF_EXACT}[lp],
-                   ptr(self.nn_distances_), st)
+                   int(self.search[0]), int(self.search[1]), ptr(self.nn_distances_), st)
         ev["t4"].record()
+        self.kdtree = tree
+        self._A, self._B = A, B
+        if not sync:
+            return nn
         tree.check_device()  # synchronises and raises if a kernel's bounds check tripped
         self._timers = collections.OrderedDict()
         self._timers["pca_fit"] = ev["t0"].elapsed_time(ev["t1"]) / 1e3

@@ -128,3 +128,83 @@ def frame_stream(seed: int = 3, frames: int = 120, h: int = 1080, w: int = 1920)
         f = flow_warp(f, 6.0, 96.0, 3.0, rng)
         out.append(f)
     return out
+
+
+# --------------------------------------------------------------------------------------------
+# the same recipes on the GPU (torch FFT and bilinear sampling; torch's RNG, so not bit-equal to
+# the numpy versions above) for workloads too large to synthesise on the host in a benchmark run
+# --------------------------------------------------------------------------------------------
+def _gpu_spectral(h, w, g, dev):
+    import torch
+    fy = torch.fft.fftfreq(h, device=dev)[:, None]
+    fx = torch.fft.rfftfreq(w, device=dev)[None, :]
+    f2 = fx * fx + fy * fy
+    amp = torch.where(f2 > 0, 1.0 / torch.sqrt(torch.where(f2 > 0, f2, torch.ones_like(f2))), torch.zeros_like(f2))
+    img = torch.fft.irfft2(torch.fft.rfft2(torch.randn((3, h, w), generator=g, device=dev)) * amp, s=(h, w))
+    lo, hi = img.min(), img.max()
+    return torch.clamp(torch.round((img - lo) * (255.0 / torch.clamp(hi - lo, min=1e-12))), 0, 255)
+
+
+def _gpu_flow_warp(a, magnitude, sigma, noise, g):
+    import math
+
+    import torch
+    dev = a.device
+    _, h, w = a.shape
+    fy = torch.fft.fftfreq(h, device=dev)[:, None]
+    fx = torch.fft.rfftfreq(w, device=dev)[None, :]
+    gk = torch.exp(-2.0 * (math.pi ** 2) * sigma * sigma * (fx * fx + fy * fy))
+    u = torch.randn((2, h, w), generator=g, device=dev) * magnitude
+    u = torch.fft.irfft2(torch.fft.rfft2(u) * gk, s=(h, w))
+    u = u * (magnitude / torch.clamp(u.std(dim=(1, 2), keepdim=True), min=1e-12))
+    yy, xx = torch.meshgrid(torch.arange(h, device=dev, dtype=torch.float32),
+                            torch.arange(w, device=dev, dtype=torch.float32), indexing="ij")
+    grid = torch.stack([(xx + u[1]) / (w - 1) * 2 - 1, (yy + u[0]) / (h - 1) * 2 - 1], dim=-1)[None]
+    warped = torch.nn.functional.grid_sample(a[None], grid, mode="bilinear", padding_mode="reflection",
+                                             align_corners=True)[0]
+    return torch.clamp(torch.round(warped + noise * torch.randn(warped.shape, generator=g, device=dev)), 0, 255)
+
+
+def gpu_frame_stream(seed: int = 3, frames: int = 120, h: int = 1080, w: int = 1920, device=0):
+    """frame_stream's recipe on the GPU: a list of uint8 (h, w, 3) CUDA tensors."""
+    import torch
+    dev = torch.device("cuda", device) if isinstance(device, int) else torch.device(device)
+    g = torch.Generator(device=dev)
+    g.manual_seed(int(seed))
+    f = _gpu_spectral(h, w, g, dev)
+    out = [f]
+    for _ in range(frames - 1):
+        f = _gpu_flow_warp(f, 6.0, 96.0, 3.0, g)
+        out.append(f)
+    return [x.permute(1, 2, 0).contiguous().to(torch.uint8) for x in out]
+
+
+def gpu_pairs_uneven(seed: int = 2, count: int = 64, lo: int = 256, hi: int = 1536, device=0):
+    """pairs_uneven's recipe with the image synthesis on the GPU (sizes and affine parameters from
+    the same numpy RNG draws): [(A, B)] uint8 CUDA tensors."""
+    import math
+
+    import torch
+    dev = torch.device("cuda", device) if isinstance(device, int) else torch.device(device)
+    rng = np.random.default_rng(seed)
+    g = torch.Generator(device=dev)
+    g.manual_seed(int(seed))
+    out = []
+    for _ in range(count):
+        side = int(rng.integers(lo, hi + 1))
+        aspect = float(rng.uniform(0.5, 2.0))
+        h, w = side, max(16, int(round(side * aspect)))
+        dx, dy, ang = float(rng.uniform(-40, 40)), float(rng.uniform(-40, 40)), float(rng.uniform(-20, 20))
+        a = _gpu_spectral(h, w, g, dev)
+        cy, cx = (h - 1) / 2.0, (w - 1) / 2.0
+        th = math.radians(ang)
+        yy, xx = torch.meshgrid(torch.arange(h, device=dev, dtype=torch.float32),
+                                torch.arange(w, device=dev, dtype=torch.float32), indexing="ij")
+        ry = (yy - cy) * math.cos(th) - (xx - cx) * math.sin(th) + cy - dy
+        rx = (yy - cy) * math.sin(th) + (xx - cx) * math.cos(th) + cx - dx
+        grid = torch.stack([rx / (w - 1) * 2 - 1, ry / (h - 1) * 2 - 1], dim=-1)[None]
+        warped = torch.nn.functional.grid_sample(a[None], grid, mode="bilinear", padding_mode="reflection",
+                                                 align_corners=True)[0]
+        b = torch.clamp(torch.round(warped + 4.0 * torch.randn(warped.shape, generator=g, device=dev)), 0, 255)
+        out.append((a.permute(1, 2, 0).contiguous().to(torch.uint8), b.permute(1, 2, 0).contiguous().to(torch.uint8)))
+    return out

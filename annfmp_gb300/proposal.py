@@ -15,8 +15,9 @@ the buffers.
 Training (``train``): flow-warped 1024x1024 pairs generated on the GPU with seeds 1000..10999
 (the same recipe as ``gen.pair_flow``: 1/f spectral noise, smooth Gaussian-filtered flow of
 standard deviation 20 px, bilinear warp, N(0, 4^2) noise), targets = the plain method's NNF of each
-pair (patch 7x7, PCA 8, leaf 32, k 1) reduced to the median offset of every 4x4 block, relaxed
-winner-takes-all L1 loss over the four hypotheses, Adam.
+pair (patch 7x7, PCA 8, leaf 32, k 1): each low-resolution pixel's four hypotheses learn to cover
+the 16 offsets of the A patches centred in its 4x4 block (relaxed winner-takes-all L1, truncated at
+40 px), Adam.
 
     python -m annfmp_gb300.proposal train --out annfmp_gb300/weights/proposal_flow.npz
 """
@@ -172,7 +173,7 @@ class ProposalNet:
     def loss(self, out, tgt, valid):
         """(loss tensor [1], dL/d out) of the relaxed winner-takes-all L1 loss."""
         npix = out.shape[0] * out.shape[1] * out.shape[2]
-        nv = max(int(valid.sum().item()), 1)
+        nv = max(int(valid.sum().item()), 1)  # valid sub-targets
         dout = torch.empty_like(out)
         acc = torch.zeros(1, dtype=torch.float32, device=self.dev)
         self.h.call("annf_cnn_wta_loss", ptr(out), ptr(tgt), ptr(valid), npix, 1.0 / nv, ptr(dout), ptr(acc),
@@ -184,9 +185,10 @@ class ProposalNet:
 # training data on the GPU
 # ---------------------------------------------------------------------------------------------
 def gpu_flow_pair(seed: int, size: int = 1024, magnitude: float = 20.0, sigma: float = 64.0, noise: float = 4.0,
-                  device=0):
+                  device=0, return_flow=False):
     """A flow-warped pair generated on the GPU (the recipe of gen.pair_flow with torch's RNG):
-    uint8 (size, size, 3) device tensors A, B."""
+    uint8 (size, size, 3) device tensors A, B (and the flow u [2, size, size], B(p) = A(p + u(p)),
+    when return_flow)."""
     dev = require_cuda(device)
     g = torch.Generator(device=dev)
     g.manual_seed(int(seed))
@@ -209,7 +211,8 @@ def gpu_flow_pair(seed: int, size: int = 1024, magnitude: float = 20.0, sigma: f
     warped = torch.nn.functional.grid_sample(a[None], grid, mode="bilinear", padding_mode="reflection",
                                              align_corners=True)[0]
     b = torch.clamp(torch.round(warped + noise * torch.randn(warped.shape, generator=g, device=dev)), 0, 255)
-    return (a.permute(1, 2, 0).contiguous().to(torch.uint8), b.permute(1, 2, 0).contiguous().to(torch.uint8))
+    A, B = a.permute(1, 2, 0).contiguous().to(torch.uint8), b.permute(1, 2, 0).contiguous().to(torch.uint8)
+    return (A, B, u) if return_flow else (A, B)
 
 
 _PLAIN = {}
@@ -240,8 +243,8 @@ def train(n_pairs=10000, seed0=1000, size=1024, batch=8, lr=2e-3, lr_min=1e-4, d
     v = [torch.zeros_like(p) for p in net.W + net.b]
     h4 = w4 = size // 4
     X = torch.empty((batch, h4, w4, 8), dtype=torch.bfloat16, device=dev)
-    T = torch.empty((batch, h4, w4, 2), dtype=torch.float32, device=dev)
-    V = torch.empty((batch, h4, w4), dtype=torch.uint8, device=dev)
+    T = torch.empty((batch, h4, w4, 16, 2), dtype=torch.float32, device=dev)
+    V = torch.empty((batch, h4, w4, 16), dtype=torch.uint8, device=dev)
     steps = n_pairs // batch
     t0 = time.time()
     hist = []
@@ -275,8 +278,8 @@ def train(n_pairs=10000, seed0=1000, size=1024, batch=8, lr=2e-3, lr_min=1e-4, d
 
 
 def evaluate(net, seeds, size=1024, psize=7, device=0):
-    """Mean loss and the fraction of valid low-resolution pixels whose best hypothesis is within 1.5
-    px (L1) of the target, over held-out pairs."""
+    """Mean loss and the fraction of valid sub-targets (A patches' plain-method offsets) within 1.5
+    px (L1) of one of their block's four hypotheses, over held-out pairs."""
     dev = require_cuda(device)
     h4 = size // 4
     tot, hit, cnt = 0.0, 0, 0
@@ -284,12 +287,12 @@ def evaluate(net, seeds, size=1024, psize=7, device=0):
         A, B = gpu_flow_pair(s, size, device=dev)
         nnf = plain_nnf(A, B, psize=psize, seed=s, device=dev)
         X = net.net_input(A, B).unsqueeze(0)
-        T = torch.empty((1, h4, h4, 2), dtype=torch.float32, device=dev)
-        V = torch.empty((1, h4, h4), dtype=torch.uint8, device=dev)
+        T = torch.empty((1, h4, h4, 16, 2), dtype=torch.float32, device=dev)
+        V = torch.empty((1, h4, h4, 16), dtype=torch.uint8, device=dev)
         net.h.call("annf_cnn_targets", ptr(nnf), size, size, size, psize, ptr(T), ptr(V), stream_ptr(dev))
         out = net.forward(X)
         loss, _ = net.loss(out, T, V)
-        o = out.reshape(1, h4, h4, 4, 2) * 16.0
+        o = out.reshape(1, h4, h4, 1, 4, 2) * 16.0
         e = (o - T[..., None, :]).abs().sum(-1).min(-1).values
         vm = V.bool()
         hit += int((e[vm] <= 1.5).sum().item())

@@ -42,6 +42,16 @@ WORKLOADS = {
     # 1024x1024 version of the large pair (same generator and parameters): bounded profiler captures
     "medium": dict(size=1024, seed=1, kind="flow", n_neighbors=4, psize=9, dim_reduced=16, leaf_size=64),
 }
+# graph workloads (the parallel form under one CUDA graph launch per batch)
+GRAPH_WORKLOADS = {
+    # 64 pairs, sides U(256,1536), aspect U(0.5,2), random affine (seed 2): patch 7, PCA 8, k 1,
+    # leaf size and passes autotuned per size class, all pairs in one graph launch
+    "batch": dict(psize=7, dim_reduced=8, n_neighbors=1, leaf="auto", iters="auto", precision="bf16"),
+    # 120 frames 1920x1080, each the previous warped (sigma 96, magnitude 6) + N(0,3^2) (seed 3):
+    # consecutive pairs, patch 5, PCA 12, leaf 32, k 8, FP16 leaf tiles, learned proposals,
+    # 8 pairs per graph launch
+    "stream": dict(psize=5, dim_reduced=12, n_neighbors=8, leaf=32, iters=2, precision="fp16", per_graph=8),
+}
 ROWS_SAMPLE = 32
 L2_FLUSH_BYTES = 256 << 20
 
@@ -380,13 +390,106 @@ def run_gpu(args, w, rank, world, local_rank):
     print(json.dumps(line), flush=True)
 
 
+def run_graph_workload(args, name, rank, world, local_rank):
+    """Batched pairs under CUDA graphs: value = query patches of all pairs / time of the launches."""
+    import torch
+
+    from annfmp_gb300 import _lib, gen
+    from annfmp_gb300.batch import Autotuner, BatchNNF
+    cfg = GRAPH_WORKLOADS[name]
+    dev = torch.device("cuda", local_rank)
+    torch.cuda.set_device(dev)
+    kw = dict(n_neighbors=cfg["n_neighbors"], psize=cfg["psize"], dim_reduced=cfg["dim_reduced"],
+              leaf_precision=cfg["precision"], seed=0, device=local_rank)
+    p = cfg["psize"]
+    if name == "batch":
+        pairs = gen.gpu_pairs_uneven(2, 64, device=local_rank)
+        t0 = time.perf_counter()
+        groups = [BatchNNF(leaf_size=cfg["leaf"], iters=cfg["iters"], tuner=Autotuner(samples=512, reps=1),
+                           **kw).prepare(pairs)]
+        t_prep = time.perf_counter() - t0
+        feeds = [None]
+    else:
+        from annfmp_gb300.proposal import ProposalNet
+        frames = gen.gpu_frame_stream(3, 120, 1080, 1920, device=local_rank)
+        pairs = [(frames[i], frames[i + 1]) for i in range(len(frames) - 1)]
+        per = cfg["per_graph"]
+        chunks = [pairs[i:i + per] for i in range(0, len(pairs), per)]
+        t0 = time.perf_counter()
+        prop = ProposalNet.pretrained(local_rank) if learned_available() else None
+        groups = [BatchNNF(leaf_size=cfg["leaf"], iters=cfg["iters"], proposal=prop, **kw).prepare(chunks[0])]
+        if len(chunks[-1]) != per:
+            groups.append(BatchNNF(leaf_size=cfg["leaf"], iters=cfg["iters"], proposal=prop, **kw).prepare(chunks[-1]))
+        t_prep = time.perf_counter() - t0
+        feeds = chunks
+    n_a = sum((a.shape[0] - p + 1) * (a.shape[1] - p + 1) for a, _ in pairs)
+
+    def one_pass():
+        if name == "batch":
+            groups[0].run()
+            return
+        for ch in feeds:  # copy each batch of frame pairs into the graph's inputs, then one launch
+            bt = groups[0] if len(ch) == cfg["per_graph"] else groups[-1]
+            for (A, B), (a, b) in zip(bt.inputs, ch):
+                A.copy_(a)
+                B.copy_(b)
+            bt.run()
+
+    for _ in range(max(args.warmup, 1)):
+        one_pass()
+    torch.cuda.synchronize(dev)
+    launches0 = _lib.launch_count()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    with ClockSampler(dev.index) as clocks:
+        for i in range(args.steps):
+            ev[i][0].record()
+            one_pass()
+            ev[i][1].record()
+        torch.cuda.synchronize(dev)
+    ms = sum(a.elapsed_time(b) for a, b in ev) / args.steps
+    # a sample of pairs checked against the exact raw-patch nearest neighbour
+    from annfmp_gb300 import metrics
+    errs = []
+    if name == "batch":
+        outs = groups[0].run()
+        torch.cuda.synchronize(dev)
+        for i in range(0, len(pairs), 16):
+            errs.append(metrics.distance_ratio_error(pairs[i][0], pairs[i][1], outs[i], p, n_samples=1024, seed=9,
+                                                     device=local_rank)["mean"])
+    else:
+        bt = groups[0]
+        for (A, B), (a, b) in zip(bt.inputs, feeds[0]):
+            A.copy_(a)
+            B.copy_(b)
+        outs = bt.run()
+        torch.cuda.synchronize(dev)
+        for i in (0, len(outs) - 1):
+            errs.append(metrics.distance_ratio_error(bt.inputs[i][0], bt.inputs[i][1], outs[i], p, n_samples=1024,
+                                                     seed=9, device=local_rank)["mean"])
+    if rank != 0:
+        return
+    settings = sorted(set(tuple(x) for g in groups for x in g.settings()))
+    line = {
+        "metric": "query patches/s", "value": world * n_a / (ms / 1e3), "unit": "query patches/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": cfg["precision"], "data": "synthetic (generated on the GPU)",
+        "config": {"workload": name, "pairs": len(pairs), "psize": p, "dim_reduced": cfg["dim_reduced"],
+                   "k": cfg["n_neighbors"], "leaf_iters_chosen": settings, "graphs_per_step": len(feeds),
+                   "form": "parallel" + ("+learned" if name == "stream" and learned_available() else ""),
+                   "l2": "inputs of the whole pass exceed L2"},
+        "distance_error_mean_sampled_pairs": errs, "prepare_s": t_prep,
+        "gpu_launches": int(_lib.launch_count() - launches0), "clocks": clocks.summary(),
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="large", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="large", choices=sorted(WORKLOADS) + sorted(GRAPH_WORKLOADS))
     ap.add_argument("--form", default="learned", choices=["plain", "parallel", "learned"],
                     help="plain: the reference's method; parallel: BF16 tensor-core form; learned: + proposals")
     ap.add_argument("--iters", type=int, default=4, help="propagation passes of the parallel forms")
@@ -394,6 +497,13 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 0)
+    if args.workload in GRAPH_WORKLOADS:
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable": "graph workloads have no CPU counterpart"}))
+            return
+        run_graph_workload(args, args.workload, int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)),
+                           int(os.environ.get("LOCAL_RANK", 0)))
+        return
     w = WORKLOADS[args.workload]
     if args.form == "learned" and not learned_available():
         print("bench: no trained proposal weights; timing the parallel form", file=sys.stderr)

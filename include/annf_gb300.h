@@ -159,13 +159,14 @@ int annf_project_bf16(annf_handle* h, const uint8_t* img, int hgt, int wid, int 
  * leaf scan; ANNF_LEAF_BF16: queries grouped by leaf, BF16 tensor-core distance tiles, exact FP32
  * re-rank of the 4k best), optional offset proposals
  * (proposals [n_rows*n_cols*n_prop] B patch indices, -1 = none) and `iters` parallel passes of
- * neighbour propagation and random search; every candidate is verified with the exact integer
+ * neighbour propagation and random search (rand_samples offsets per pass within radius0 >> pass
+ * of the current match, at least 1); every candidate is verified with the exact integer
  * raw-patch SSD. Requires the tree over image B's reduced patches (annf_build_tree). Outputs the
  * chosen B index per pixel and, optionally, its raw-patch L2 distance. */
 int annf_parallel_nnf(annf_handle* h, int* final_idx, const uint8_t* img_a, int ha, int wa,
                       const uint8_t* img_b, int hb, int wb, int channels, int psize, const void* ared,
                       int k, const int* proposals, int n_prop, int iters, unsigned seed,
-                      int leaf_precision, float* dist_out, void* stream);
+                      int leaf_precision, int rand_samples, int radius0, float* dist_out, void* stream);
 
 /* Exact raw-patch nearest neighbour (integer SSD over all B patches) of nq sampled A pixels
  * (query_pixels: row-major patch indices). best[i] = ssd << 32 | B index (smallest index on
@@ -211,16 +212,18 @@ int annf_cnn_conv_backward_data(annf_handle* h, const float* g, const void* mask
  * them first). */
 int annf_cnn_conv_backward_weights(annf_handle* h, const void* x, const float* g, const void* mask, int nimg,
                                    int hgt, int wid, int ci, int co, float* dw, float* db, void* stream);
-/* Relaxed winner-takes-all L1 loss over 4 hypotheses (x16 px) per pixel, each hypothesis' error
- * truncated at 40 px: dout [npix][8] and *loss_sum += loss; pixels with valid[i] == 0 contribute
- * nothing; inv_nvalid = 1 / valid count. */
+/* Relaxed winner-takes-all L1 loss of the 4 hypotheses (x16 px) of each pixel against its 16
+ * sub-targets tgt [npix][16][2] (valid [npix][16]): each sub-target's nearest hypothesis weighs 1,
+ * the others 0.05, errors truncated at 40 px; dout [npix][8], *loss_sum += loss;
+ * inv_nvalid = 1 / number of valid sub-targets. */
 int annf_cnn_wta_loss(annf_handle* h, const float* out, const float* tgt, const uint8_t* valid, long long npix,
                       float inv_nvalid, float* dout, float* loss_sum, void* stream);
 /* Bias-corrected Adam step (step >= 1) on FP32 parameters, in place. */
 int annf_cnn_adam(annf_handle* h, float* param, const float* grad, float* m, float* v, int n, float lr, float beta1,
                   float beta2, float eps, int step, void* stream);
-/* Training targets from an NNF of A (ha x wa) into B (width wb): per low-resolution pixel the median
- * (dx, dy) over its 4x4 block of patch centres, tgt [ha/4][wa/4][2], valid [ha/4][wa/4]. */
+/* Training targets from an NNF of A (ha x wa) into B (width wb): per low-resolution pixel the 16
+ * offsets (dx, dy) of the A patches centred in its 4x4 block, tgt [ha/4][wa/4][16][2], valid
+ * [ha/4][wa/4][16] (0 where the patch leaves the image). */
 int annf_cnn_targets(annf_handle* h, const int* nnf, int ha, int wa, int wb, int psize, float* tgt, uint8_t* valid,
                      void* stream);
 /* Proposals [n_A][4] B patch indices from the network output out [h4][w4][8]: each A patch takes

@@ -11,11 +11,12 @@ project's own definition:
   five; weights and stored activations rounded to BF16, sums in FP32 or wider;
 * output: 4 hypotheses (dx, dy) per low-resolution pixel, in units of OUT_SCALE full-resolution
   pixels;
-* loss: relaxed winner-takes-all truncated L1 -- per pixel e_j = |S o_jx - t_x| + |S o_jy - t_y|
-  (in pixels, S = OUT_SCALE), c_j = min(e_j, TRUNC), loss = c_{j*} + EPS * sum_{j != j*} c_j with
-  j* = argmin e_j (first on ties), averaged over the valid pixels. The plain method's matches are
-  noisy targets (similar patches far from the true displacement); truncation keeps those outliers
-  from dominating the gradient.
+* loss: relaxed winner-takes-all truncated L1 against each low-resolution pixel's 16 sub-targets
+  (the plain method's offsets of the 16 A patches centred in its 4x4 block): for sub-target s,
+  e_js = |S o_jx - t_sx| + |S o_jy - t_sy| (pixels, S = OUT_SCALE), c_js = min(e_js, TRUNC),
+  loss_s = c_{j*s} + EPS * sum_{j != j*} c_js with j* = argmin_j e_js (first on ties); the loss
+  averages loss_s over the valid sub-targets. The four hypotheses thus learn to cover the offsets a
+  block's patches take, and no single noisy match dominates the gradient.
 """
 from __future__ import annotations
 
@@ -92,10 +93,10 @@ def forward(x0: np.ndarray, params, exact: bool = False):
 
 
 def wta_loss(out: np.ndarray, tgt: np.ndarray, valid: np.ndarray):
-    """out [N,h,w,8], tgt [N,h,w,2] (pixels), valid [N,h,w] bool -> (loss, d loss / d out)."""
-    o = out.astype(np.float64).reshape(out.shape[:-1] + (4, 2)) * OUT_SCALE
-    diff = o - tgt.astype(np.float64)[..., None, :]
-    e = np.abs(diff).sum(-1)  # [N,h,w,4]
+    """out [N,h,w,8], tgt [N,h,w,16,2] (pixels), valid [N,h,w,16] bool -> (loss, d loss / d out)."""
+    o = out.astype(np.float64).reshape(out.shape[:-1] + (1, 4, 2)) * OUT_SCALE
+    diff = o - tgt.astype(np.float64)[..., :, None, :]  # [N,h,w,16,4,2]
+    e = np.abs(diff).sum(-1)  # [N,h,w,16,4]
     jstar = np.argmin(e, axis=-1)
     wgt = np.full(e.shape, EPS)
     np.put_along_axis(wgt, jstar[..., None], 1.0, axis=-1)
@@ -103,7 +104,7 @@ def wta_loss(out: np.ndarray, tgt: np.ndarray, valid: np.ndarray):
     wgt = wgt * valid[..., None] / nv
     live = e < TRUNC
     loss = float((wgt * np.minimum(e, TRUNC)).sum())
-    dout = ((wgt * live)[..., None] * np.sign(diff) * OUT_SCALE).reshape(out.shape)
+    dout = ((wgt * live)[..., None] * np.sign(diff) * OUT_SCALE).sum(axis=-3).reshape(out.shape)
     return loss, dout
 
 
@@ -122,30 +123,23 @@ def backward(acts, out_grad, params, exact: bool = False):
 
 
 def targets_from_nnf(nnf: np.ndarray, H: int, W: int, Hb: int, Wb: int, psize: int):
-    """Per-low-resolution-pixel target offsets [h4, w4, 2] (dx, dy) in pixels and validity: the
-    per-coordinate median (mean of the 8th and 9th of 16) over the 4x4 block of A pixels whose
-    patches are centred in the block; A pixels whose patch would leave the image are skipped."""
+    """Per-low-resolution-pixel sub-targets [h4, w4, 16, 2] (dx, dy) in pixels and validity
+    [h4, w4, 16]: the offsets of the 16 A patches centred in the 4x4 block (row-major in the
+    block); patches that would leave the image are invalid (offset 0)."""
     n_cols, n_rows = W - psize + 1, H - psize + 1
     ncb = Wb - psize + 1
     h4, w4 = H // 4, W // 4
-    tgt = np.zeros((h4, w4, 2), np.float32)
-    valid = np.zeros((h4, w4), bool)
+    tgt = np.zeros((h4, w4, 16, 2), np.float32)
+    valid = np.zeros((h4, w4, 16), bool)
     half = psize // 2
     for i in range(h4):
         for j in range(w4):
-            dxs, dys = [], []
-            for u in range(4):
-                for v in range(4):
-                    y, x = 4 * i + u - half, 4 * j + v - half
-                    if 0 <= y < n_rows and 0 <= x < n_cols:
-                        bidx = int(nnf[y * n_cols + x])
-                        by, bx = divmod(bidx, ncb)
-                        dxs.append(bx - x)
-                        dys.append(by - y)
-            if len(dxs) == 16:
-                sx, sy = np.sort(dxs), np.sort(dys)
-                tgt[i, j] = (0.5 * (sx[7] + sx[8]), 0.5 * (sy[7] + sy[8]))
-                valid[i, j] = True
+            for u in range(16):
+                y, x = 4 * i + u // 4 - half, 4 * j + u % 4 - half
+                if 0 <= y < n_rows and 0 <= x < n_cols:
+                    by, bx = divmod(int(nnf[y * n_cols + x]), ncb)
+                    tgt[i, j, u] = (bx - x, by - y)
+                    valid[i, j, u] = True
     return tgt, valid
 
 

@@ -24,7 +24,7 @@ def test_subspace_pca_captures_leading_variance(gpu_lib, oracle_mod, golden, nam
     z = golden(name)
     k, psize, d, n_subset, leaf, prop, sel, seed = (int(v) for v in z["params"])
     m = ANNFieldPropKDTreeGB300(n_neighbors=k, psize=psize, dim_reduced=d, n_subset=n_subset, leaf_size=leaf,
-                                seed=seed, verbose=0, form="parallel", pca_solver="subspace", pca_iters=10)
+                                seed=seed, verbose=0, form="parallel", pca_solver="subspace")
     m.fit(z["a"], z["b"])
     V = m.components_.cpu().numpy()
     assert np.array_equal(m.mean_.cpu().numpy(), z["mean"])
@@ -128,9 +128,12 @@ def test_project_bf16_matches_bf16_components(gpu_lib, oracle_mod, golden, name)
     for img in (z["a"], z["b"]):
         h, w, c = img.shape
         out = torch.empty(((h - psize + 1) * (w - psize + 1), comps.shape[0]), dtype=torch.float32, device=dev)
-        _lib.Handle(0).call("annf_project_bf16", ptr(torch.from_numpy(img).to(dev)), h, w, c, psize,
-                            ptr(torch.from_numpy(comps).to(dev)), ptr(torch.from_numpy(mean).to(dev)), comps.shape[0],
-                            ptr(out), stream_ptr(dev))
+        # every argument tensor is held by a name until the call returns (a temporary's memory
+        # could be handed to the next temporary by the caching allocator before the kernel runs)
+        img_d, comps_d, mean_d = (torch.from_numpy(t).to(dev) for t in (img, comps, mean))
+        _lib.Handle(0).call("annf_project_bf16", ptr(img_d), h, w, c, psize, ptr(comps_d), ptr(mean_d),
+                            comps.shape[0], ptr(out), stream_ptr(dev))
+        torch.cuda.synchronize()
         cb = C.bf16_round(comps.astype(np.float32)).astype(np.float64)
         X = oracle_mod.extract_patches(img, psize).astype(np.float64)
         want = X @ cb.T - cb @ mean

@@ -37,8 +37,8 @@ def test_conv3x3_backward_matches_finite_differences():
 def test_wta_loss_gradient_matches_finite_differences():
     rng = np.random.default_rng(1)
     out = rng.standard_normal((1, 3, 4, 8)).astype(np.float64)
-    tgt = rng.standard_normal((1, 3, 4, 2)) * 10
-    valid = rng.random((1, 3, 4)) > 0.2
+    tgt = rng.standard_normal((1, 3, 4, 16, 2)) * 10
+    valid = rng.random((1, 3, 4, 16)) > 0.2
     loss, dout = C.wta_loss(out, tgt, valid)
     eps = 1e-7
     for idx in [(0, 0, 0, 0), (0, 1, 2, 5), (0, 2, 3, 7)]:
@@ -57,8 +57,8 @@ def test_full_backward_matches_finite_differences_without_rounding():
         params.append(((rng.standard_normal((co, 3, 3, ci)) * np.sqrt(2.0 / (9 * ci))),
                        rng.standard_normal(co) * 0.1))
     x0 = rng.standard_normal((1, 6, 5, 8))
-    tgt = rng.standard_normal((1, 6, 5, 2)) * 8
-    valid = np.ones((1, 6, 5), bool)
+    tgt = rng.standard_normal((1, 6, 5, 16, 2)) * 8
+    valid = np.ones((1, 6, 5, 16), bool)
     def loss_of(ps):
         acts, out = C.forward(x0, ps, exact=True)
         return C.wta_loss(out, tgt, valid)[0]
@@ -86,7 +86,7 @@ def test_targets_and_proposals_on_a_pure_shift():
     nnf = (by * n_cols + bx).astype(np.int32)
     tgt, valid = C.targets_from_nnf(nnf, H, W, H, W, p)
     assert valid[2:5, 2:5].all()
-    assert np.allclose(tgt[3, 3], (-3, 2))
+    assert np.allclose(tgt[3, 3], np.tile([-3, 2], (16, 1)))
     out = np.zeros((H // 4, W // 4, 8), np.float32)
     out[..., 0::2] = -3 / 16.0
     out[..., 1::2] = 2 / 16.0
