@@ -138,9 +138,12 @@ class BatchNNF:
         torch.cuda.current_stream(self.dev).wait_stream(side)
         torch.cuda.synchronize(self.dev)
         self.graph = torch.cuda.CUDAGraph()
+        from . import _lib
+        before = _lib.launch_count()
         with torch.cuda.graph(self.graph, capture_error_mode="relaxed"):
             self.outputs = [m.fit(A, B, sync=False) for m, (A, B) in zip(self.models, self.inputs)]
         torch.cuda.synchronize(self.dev)
+        self.kernels_per_launch = _lib.launch_count() - before  # this library's kernels in the graph
         return self
 
     def run(self):

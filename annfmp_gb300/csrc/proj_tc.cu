@@ -123,14 +123,16 @@ __global__ void __launch_bounds__(kPjThreads) project_tc_kernel(const uint8_t* _
   for (long long t = blockIdx.x; t < ntiles; t += gridDim.x) {
     const int y = (int)(t / tiles_x), x0 = (int)(t - (long long)y * tiles_x) * 128;
     const int np = min(128, ncols - x0);
-    // stage the psize image rows as aligned words; byte b of row r sits at sI[r*sw + s0 + b]
+    // stage the psize image rows as aligned words; byte b of row r sits at sI[r*sw + s0(r) + b] with
+    // s0(r) = (start of row r) mod 4 (rows need not start 4-byte aligned: W * C may be odd)
     const long long row0 = ((long long)y * W + x0) * C;
-    const int s0 = (int)(row0 & 3);
+    const long long pitch = (long long)W * C;
     const int span = (np + psize - 1) * C;
-    const int nw = (s0 + span + 3) >> 2;
+    const int nw = (3 + span + 3) >> 2;  // words per staged row, enough for any shift
     for (int e = tid; e < psize * nw; e += kPjThreads) {
       const int r = e / nw, wi = e - r * nw;
-      const long long a = row0 + (long long)r * W * C - s0 + 4LL * wi;  // 4-byte aligned
+      const long long rs0 = row0 + (long long)r * pitch;
+      const long long a = (rs0 & ~3LL) + 4LL * wi;  // 4-byte aligned
       uint32_t v;
       if (a + 4 <= nbytes) {
         v = __ldg(reinterpret_cast<const uint32_t*>(img + a));
@@ -148,7 +150,7 @@ __global__ void __launch_bounds__(kPjThreads) project_tc_kernel(const uint8_t* _
       const int r = g / gpr, e0 = (g - r * gpr) * 8;
       uint4 w = make_uint4(0u, 0u, 0u, 0u);
       if (r < psize && row < np) {
-        const int off = r * sw + s0 + row * C + e0;
+        const int off = r * sw + (int)((row0 + (long long)r * pitch) & 3) + row * C + e0;
         const uint32_t* wp = reinterpret_cast<const uint32_t*>(sI + (off & ~3));
         const int sh = (off & 3) * 8;
         const uint32_t q0 = wp[0], q1 = wp[1], q2 = wp[2];

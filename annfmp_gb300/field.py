@@ -163,6 +163,17 @@ class ANNFieldPropKDTreeGB300:
         ev = _Marks(sync)
         ev["t0"].record()
 
+        # offset proposals depend only on the images: computed on a side stream, overlapping the PCA
+        # fit (whose eigensolver occupies one SM) and the projection; joined before the candidates
+        prop, side = None, None
+        if self.form != "plain" and self.proposal is not None:
+            main = torch.cuda.current_stream(dev)
+            side = torch.cuda.Stream(dev) if getattr(self, "_side", None) is None else self._side
+            self._side = side
+            side.wait_stream(main)
+            with torch.cuda.stream(side):
+                prop = self.proposal.propose(A, B, p)
+
         # (1) PCA fit on the sampled subset (annfmp/openmp/base.py:168-191)
         m = int(self.n_subset / 2)
         pos_a = _SUBSETS.get(self._n_rows, self._n_cols, m, self.seed, dev)
@@ -219,9 +230,10 @@ class ANNFieldPropKDTreeGB300:
                    int(bool(self.select_best_nn)), tree._final_max_leaves(), ptr(self.knn_indices_),
                    ptr(self.nn_distances_), st)
         else:
-            prop = None
-            if self.proposal is not None:
-                prop = self.proposal.propose(A, B, p)
+            if side is not None:
+                torch.cuda.current_stream(dev).wait_stream(side)
+                if prop is not None:
+                    prop.record_stream(torch.cuda.current_stream(dev))
             n_prop = 0 if prop is None else int(prop.shape[1])
             lp = self.leaf_precision or "bf16"
             if lp not in ("bf16", "fp16", "fp32"):

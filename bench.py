@@ -438,6 +438,9 @@ def run_graph_workload(args, name, rank, world, local_rank):
     for _ in range(max(args.warmup, 1)):
         one_pass()
     torch.cuda.synchronize(dev)
+    # kernels per timed step: graph replays launch the kernels captured in them
+    per_step = sum(groups[0 if (name == "batch" or len(ch) == cfg["per_graph"]) else -1].kernels_per_launch
+                   for ch in feeds)
     launches0 = _lib.launch_count()
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     with ClockSampler(dev.index) as clocks:
@@ -478,7 +481,8 @@ def run_graph_workload(args, name, rank, world, local_rank):
                    "form": "parallel" + ("+learned" if name == "stream" and learned_available() else ""),
                    "l2": "inputs of the whole pass exceed L2"},
         "distance_error_mean_sampled_pairs": errs, "prepare_s": t_prep,
-        "gpu_launches": int(_lib.launch_count() - launches0), "clocks": clocks.summary(),
+        "gpu_launches": int(_lib.launch_count() - launches0) + per_step * args.steps,
+        "graph_launches_per_step": len(feeds), "clocks": clocks.summary(),
     }
     print(json.dumps(line), flush=True)
 
@@ -492,7 +496,7 @@ def main():
     ap.add_argument("--workload", default="large", choices=sorted(WORKLOADS) + sorted(GRAPH_WORKLOADS))
     ap.add_argument("--form", default="learned", choices=["plain", "parallel", "learned"],
                     help="plain: the reference's method; parallel: BF16 tensor-core form; learned: + proposals")
-    ap.add_argument("--iters", type=int, default=4, help="propagation passes of the parallel forms")
+    ap.add_argument("--iters", type=int, default=3, help="propagation passes of the parallel forms")
     ap.add_argument("--no-compare", action="store_true", help="time only --form (not the other forms)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()

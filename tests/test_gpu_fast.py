@@ -140,3 +140,28 @@ def test_project_bf16_matches_bf16_components(gpu_lib, oracle_mod, golden, name)
         scale = X @ np.abs(cb).T + np.abs(cb) @ np.abs(mean)
         got = out.cpu().numpy()
         assert np.all(np.abs(got - want) <= 2e-5 * scale + 1e-6), np.abs(got - want).max()
+
+
+@pytest.mark.parametrize("h,w,psize", [(37, 53, 7), (41, 190, 9), (29, 133, 5)])
+def test_project_bf16_odd_pitch(gpu_lib, oracle_mod, h, w, psize):
+    """Rows whose byte pitch is not a multiple of 4 (odd widths) and tiles narrower than 128."""
+    import torch
+    from annfmp_gb300 import _lib
+    from annfmp_gb300._torch import ptr, stream_ptr
+    from oracle import cnn as C
+    rng = np.random.default_rng(h * w)
+    img = rng.integers(0, 256, (h, w, 3), dtype=np.uint8)
+    P = psize * psize * 3
+    comps = np.linalg.qr(rng.standard_normal((P, 12)))[0].T.copy()
+    mean = rng.random(P) * 255
+    dev = torch.device("cuda", 0)
+    img_d, comps_d, mean_d = (torch.from_numpy(t).to(dev) for t in (img, comps, mean))
+    out = torch.empty(((h - psize + 1) * (w - psize + 1), 12), dtype=torch.float32, device=dev)
+    _lib.Handle(0).call("annf_project_bf16", ptr(img_d), h, w, 3, psize, ptr(comps_d), ptr(mean_d), 12, ptr(out),
+                        stream_ptr(dev))
+    torch.cuda.synchronize()
+    cb = C.bf16_round(comps.astype(np.float32)).astype(np.float64)
+    X = oracle_mod.extract_patches(img, psize).astype(np.float64)
+    want = X @ cb.T - cb @ mean
+    scale = X @ np.abs(cb).T + np.abs(cb) @ np.abs(mean)
+    assert np.all(np.abs(out.cpu().numpy() - want) <= 2e-5 * scale + 1e-5)
