@@ -81,6 +81,8 @@ SIGNATURES = {
     "annf_cnn_input": (_i, [_vp, _vp, _vp, _i, _i, _vp, _vp]),
     "annf_cnn_prep_weights": (_i, [_vp, _vp, _i, _i, _vp, _vp, _vp]),
     "annf_cnn_conv_forward": (_i, [_vp, _vp, _i, _i, _i, _i, _i, _vp, _vp, _i, _vp, _vp]),
+    "annf_cnn_prep_weights_tc": (_i, [_vp, _vp, _i, _i, _vp, _vp]),
+    "annf_cnn_conv_forward_tc": (_i, [_vp, _vp, _i, _i, _i, _i, _i, _vp, _vp, _i, _vp, _vp]),
     "annf_cnn_conv_backward_data": (_i, [_vp, _vp, _vp, _i, _i, _i, _i, _i, _vp, _vp, _vp]),
     "annf_cnn_conv_backward_weights": (_i, [_vp, _vp, _vp, _vp, _i, _i, _i, _i, _i, _vp, _vp, _vp]),
     "annf_cnn_wta_loss": (_i, [_vp, _vp, _vp, _vp, ctypes.c_longlong, ctypes.c_float, _vp, _vp, _vp]),

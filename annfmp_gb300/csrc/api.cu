@@ -36,6 +36,9 @@ int cnn_input(const uint8_t* A, const uint8_t* B, int H, int W, void* X, cudaStr
 int cnn_prep_weights(const float* W, int co, int ci, float* wf, float* wb, cudaStream_t st);
 int cnn_conv_forward(const void* X, int nimg, int h, int w, int ci, int co, const float* wf, const float* bias,
                      int relu, void* Y, unsigned* status, cudaStream_t st);
+int cnn_prep_weights_tc(const float* W, int co, int ci, uint16_t* wt, cudaStream_t st);
+int cnn_conv_forward_tc(const void* X, int nimg, int h, int w, int ci, int co, const uint16_t* wt, const float* bias,
+                        int relu, void* Y, unsigned* status, cudaStream_t st);
 int cnn_conv_backward_data(const float* G, const void* mask, int nimg, int h, int w, int co, int ci, const float* wb,
                            float* dX, unsigned* status, cudaStream_t st);
 int cnn_conv_backward_weights(const void* X, const float* G, const void* mask, int nimg, int h, int w, int ci, int co,
@@ -407,6 +410,21 @@ int annf_cnn_conv_forward(annf_handle* h, const void* x, int nimg, int hgt, int 
   ANNF_CNN_DIMS(nimg, hgt, wid);
   return cnn_conv_forward(x, nimg, hgt, wid, ci, co, w_fwd, bias, relu, y, h->status.as<unsigned>(),
                           static_cast<cudaStream_t>(stream));
+}
+
+int annf_cnn_prep_weights_tc(annf_handle* h, const float* w, int co, int ci, uint16_t* w_tc, void* stream) {
+  ANNF_API_HANDLE(h);
+  ANNF_REQUIRE(w && w_tc, "annf_cnn_prep_weights_tc: NULL argument");
+  return cnn_prep_weights_tc(w, co, ci, w_tc, static_cast<cudaStream_t>(stream));
+}
+
+int annf_cnn_conv_forward_tc(annf_handle* h, const void* x, int nimg, int hgt, int wid, int ci, int co,
+                             const uint16_t* w_tc, const float* bias, int relu, void* y, void* stream) {
+  ANNF_API_HANDLE(h);
+  ANNF_REQUIRE(x && w_tc && bias && y, "annf_cnn_conv_forward_tc: NULL argument");
+  ANNF_CNN_DIMS(nimg, hgt, wid);
+  return cnn_conv_forward_tc(x, nimg, hgt, wid, ci, co, w_tc, bias, relu, y, h->status.as<unsigned>(),
+                             static_cast<cudaStream_t>(stream));
 }
 
 int annf_cnn_conv_backward_data(annf_handle* h, const float* g, const void* mask, int nimg, int hgt, int wid, int co,

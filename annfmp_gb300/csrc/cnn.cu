@@ -22,6 +22,7 @@
 
 #include "common.cuh"
 #include "handle.cuh"
+#include "tc.cuh"
 
 namespace annf {
 
@@ -338,6 +339,173 @@ __global__ void cnn_proposals_kernel(const float* __restrict__ out, int h4, int 
 }
 
 // ---------------------------------------------------------------------------------------------
+// forward convolution on the tensor cores (inference and training forward): an implicit GEMM per
+// tile of 128 consecutive pixels of one row, M = 128 pixels, N = Cout padded to 16/32, K = taps x
+// Cin in the weights' own order (k = (ky*3 + kx)*Cin + ci). The three input rows are staged in
+// shared memory; for Cin = 32 the A tile is built one kernel row (ky) at a time (K = 96, three
+// accumulating rounds of 6 MMAs), for Cin = 8 all 9 taps at once (K = 72 padded to 80). FP32 TMEM
+// accumulator; epilogue adds the bias, applies the ReLU and stores BF16 (or FP32 for the last layer).
+// ---------------------------------------------------------------------------------------------
+constexpr long long kConvWaitCycles = 2000000000LL;
+
+__device__ __forceinline__ bool conv_wait(uint64_t* mbar, uint32_t phase) {
+  const long long t0 = clock64();
+  while (!tc::mbar_try_wait(mbar, phase)) {
+    if (clock64() - t0 > kConvWaitCycles) return false;
+  }
+  return true;
+}
+
+// W [co][9][ci] FP32 -> wt [cop][kpad] BF16 bits, zero padded
+__global__ void cnn_prep_weights_tc_kernel(const float* __restrict__ W, int co_n, int ci_n, int cop, int kpad,
+                                           uint16_t* __restrict__ wt) {
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < cop * kpad; e += gridDim.x * blockDim.x) {
+    const int co = e / kpad, k = e - co * kpad;
+    const float v = (co < co_n && k < 9 * ci_n) ? W[(size_t)co * 9 * ci_n + k] : 0.f;
+    __nv_bfloat16 b = __float2bfloat16_rn(v);
+    wt[e] = *reinterpret_cast<uint16_t*>(&b);
+  }
+}
+
+template <int CI, int COP, int MODE>  // MODE 0: bias + ReLU, BF16 out; MODE 1: bias, FP32 out
+__global__ void __launch_bounds__(128) cnn_conv_tc_kernel(const __nv_bfloat16* __restrict__ X, int nimg, int h, int w,
+                                                          const uint16_t* __restrict__ wt, const float* __restrict__ bias,
+                                                          int co_n, void* __restrict__ out, unsigned* status) {
+  constexpr int KPAD = CI == 32 ? 288 : 80;           // full K (B tile)
+  constexpr int KR = CI == 32 ? 96 : 80;              // K of one round (A tile)
+  constexpr int ROUNDS = CI == 32 ? 3 : 1;
+  constexpr int SPIX = 130;                           // staged pixels per input row
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  unsigned char* p = smem_raw;
+  unsigned char* sA = p;
+  p += 128 * KR * 2;
+  unsigned char* sB = p;
+  p += COP * KPAD * 2;
+  __nv_bfloat16* sIn = reinterpret_cast<__nv_bfloat16*>(p);  // [3][SPIX][CI]
+  p += 3 * SPIX * CI * 2;
+  p = reinterpret_cast<unsigned char*>(((uintptr_t)p + 15) & ~uintptr_t(15));
+  uint64_t* mbar = reinterpret_cast<uint64_t*>(p);
+  p += 8;
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(p);
+  p += 8;
+  int* sflag = reinterpret_cast<int*>(p);
+  p += 8;
+  if (smem_overrun(smem_raw, p, status)) return;
+  const int tid = threadIdx.x, warp = tid >> 5;
+  if (warp == 0) {
+    tc::tmem_alloc(tslot, 32);
+    tc::tmem_relinquish();
+  }
+  if (tid == 0) {
+    tc::mbar_init(mbar, 1);
+    tc::mbar_fence_init();
+    sflag[0] = 0;
+  }
+  for (int e = tid; e < COP * (KPAD / 8); e += 128) {  // weights tile (core layout)
+    const int r = e / (KPAD / 8), k8 = (e - r * (KPAD / 8)) * 8;
+    *reinterpret_cast<uint4*>(sB + tc::core_offset(r, k8, KPAD)) =
+        *reinterpret_cast<const uint4*>(wt + (size_t)r * KPAD + k8);
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = *tslot;
+  const uint32_t idesc = tc::idesc_bf16(128, COP);
+  const int tiles_x = (w + 127) / 128;
+  const long long ntiles = (long long)nimg * h * tiles_x;
+  uint32_t phase = 0;
+  bool aborted = false;
+  for (long long t = blockIdx.x; t < ntiles && !aborted; t += gridDim.x) {
+    const int n = (int)(t / ((long long)h * tiles_x));
+    const int rem = (int)(t - (long long)n * h * tiles_x);
+    const int y = rem / tiles_x, x0 = (rem - y * tiles_x) * 128;
+    // stage input rows y-1..y+1, pixels x0-1..x0+128 (zero outside the image), 8 channels per uint4
+    for (int e = tid; e < 3 * SPIX * (CI / 8); e += 128) {
+      const int c8 = e % (CI / 8), q = e / (CI / 8);
+      const int ry = q / SPIX, px = q - ry * SPIX;
+      const int yy = y + ry - 1, xx = x0 + px - 1;
+      uint4 v = make_uint4(0u, 0u, 0u, 0u);
+      if (yy >= 0 && yy < h && xx >= 0 && xx < w)
+        v = *reinterpret_cast<const uint4*>(X + (((size_t)n * h + yy) * w + xx) * CI + c8 * 8);
+      *reinterpret_cast<uint4*>(sIn + (size_t)q * CI + c8 * 8) = v;
+    }
+    __syncthreads();
+    for (int round = 0; round < ROUNDS; ++round) {
+      // A tile of this round: pixel tid, K = taps of kernel row `round` (CI 32) or all taps (CI 8)
+      for (int g = 0; g < KR / 8; ++g) {
+        uint4 v = make_uint4(0u, 0u, 0u, 0u);
+        int ky, kx, c8;
+        if (CI == 32) {
+          ky = round;
+          kx = g / 4;
+          c8 = g % 4;
+        } else {
+          ky = g / 3;
+          kx = g % 3;
+          c8 = 0;
+        }
+        if (ky < 3) v = *reinterpret_cast<const uint4*>(sIn + ((size_t)ky * SPIX + tid + kx) * CI + c8 * 8);
+        *reinterpret_cast<uint4*>(sA + tc::core_offset(tid, g * 8, KR)) = v;
+      }
+      tc::fence_async_smem();
+      tc::fence_before_sync();
+      __syncthreads();
+      if (tid == 0) {
+        tc::fence_after_sync();
+#pragma unroll
+        for (int kk = 0; kk < KR / 16; ++kk)
+          tc::mma_bf16(tmem, tc::sdesc(sA + kk * 256, 128, (KR / 8) * 128),
+                       tc::sdesc(sB + (round * KR / 8) * 128 + kk * 256, 128, (KPAD / 8) * 128), idesc,
+                       (round > 0 || kk > 0) ? 1u : 0u);
+        tc::mma_commit(mbar);
+      }
+      if (!conv_wait(mbar, phase)) sflag[0] = 1;
+      phase ^= 1u;
+      __syncthreads();
+      if (sflag[0]) {
+        aborted = true;
+        break;
+      }
+      tc::fence_after_sync();
+    }
+    if (aborted) break;
+    // epilogue: thread tid = pixel x0 + tid = TMEM lane tid
+    const int x = x0 + tid;
+    const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
+#pragma unroll
+    for (int c0 = 0; c0 < COP; c0 += 16) {
+      uint32_t r[16];
+      tc::tmem_ld16(trow + (uint32_t)c0, r);
+      tc::tmem_wait_ld();
+      if (x < w) {
+        const size_t base = (((size_t)n * h + y) * w + x) * co_n;
+#pragma unroll
+        for (int j = 0; j < 16; j += 2) {
+          const int c = c0 + j;
+          if (c >= co_n) break;
+          const float a0 = __uint_as_float(r[j]) + bias[c], a1 = __uint_as_float(r[j + 1]) + bias[c + 1];
+          if (MODE == 0) {
+            *reinterpret_cast<__nv_bfloat162*>(static_cast<__nv_bfloat16*>(out) + base + c) =
+                __floats2bfloat162_rn(fmaxf(a0, 0.f), fmaxf(a1, 0.f));
+          } else {
+            *reinterpret_cast<float2*>(static_cast<float*>(out) + base + c) = make_float2(a0, a1);
+          }
+        }
+      }
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+  }
+  if (aborted) {
+    if (tid == 0) atomicOr(status, DEV_TC_TIMEOUT);
+    conv_wait(mbar, phase ^ 1u);
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) tc::tmem_dealloc(tmem, 32);
+}
+
+// ---------------------------------------------------------------------------------------------
 // host wrappers
 // ---------------------------------------------------------------------------------------------
 static int grid_for(long long n, int block) { return (int)std::max(1LL, std::min<long long>((n + block - 1) / block, 16LL * num_sms())); }
@@ -377,6 +545,39 @@ int cnn_conv_forward(const void* X, int nimg, int h, int w, int ci, int co, cons
   if (ci == 32 && co == 32 && relu) return launch_conv<32, 32, __nv_bfloat16, false, 0>(x, nullptr, nimg, h, w, wf, bias, Y, status, st);
   if (ci == 32 && co == 8 && !relu) return launch_conv<32, 8, __nv_bfloat16, false, 1>(x, nullptr, nimg, h, w, wf, bias, Y, status, st);
   set_error("annf_cnn_conv_forward: unsupported layer shape");
+  return ANNF_ERR_UNSUPPORTED;
+}
+
+int cnn_prep_weights_tc(const float* W, int co, int ci, uint16_t* wt, cudaStream_t st) {
+  ANNF_REQUIRE((ci == 8 || ci == 32) && (co == 8 || co == 32), "annf_cnn_prep_weights_tc: unsupported layer shape");
+  const int cop = co <= 16 ? 16 : 32, kpad = ci == 32 ? 288 : 80;
+  cnn_prep_weights_tc_kernel<<<grid_for((long long)cop * kpad, 256), 256, 0, st>>>(W, co, ci, cop, kpad, wt);
+  ANNF_CHECK_LAUNCH();
+  return ANNF_OK;
+}
+
+template <int CI, int COP, int MODE>
+static int launch_conv_tc(const __nv_bfloat16* x, int nimg, int h, int w, const uint16_t* wt, const float* bias,
+                          int co, void* y, unsigned* status, cudaStream_t st) {
+  constexpr int KPAD = CI == 32 ? 288 : 80, KR = CI == 32 ? 96 : 80;
+  const size_t smem = (size_t)128 * KR * 2 + (size_t)COP * KPAD * 2 + (size_t)3 * 130 * CI * 2 + 16 + 24 + 64;
+  ANNF_CUDA_TRY(cudaFuncSetAttribute(cnn_conv_tc_kernel<CI, COP, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)smem));
+  const long long tiles = (long long)nimg * h * ((w + 127) / 128);
+  const int grid = (int)std::max(1LL, std::min<long long>(tiles, 4LL * num_sms()));
+  cnn_conv_tc_kernel<CI, COP, MODE><<<grid, 128, smem, st>>>(x, nimg, h, w, wt, bias, co, y, status);
+  ANNF_CHECK_LAUNCH();
+  return ANNF_OK;
+}
+
+// forward convolution on the tensor cores, same shapes and outputs as cnn_conv_forward
+int cnn_conv_forward_tc(const void* X, int nimg, int h, int w, int ci, int co, const uint16_t* wt, const float* bias,
+                        int relu, void* Y, unsigned* status, cudaStream_t st) {
+  const __nv_bfloat16* x = static_cast<const __nv_bfloat16*>(X);
+  if (ci == 8 && co == 32 && relu) return launch_conv_tc<8, 32, 0>(x, nimg, h, w, wt, bias, co, Y, status, st);
+  if (ci == 32 && co == 32 && relu) return launch_conv_tc<32, 32, 0>(x, nimg, h, w, wt, bias, co, Y, status, st);
+  if (ci == 32 && co == 8 && !relu) return launch_conv_tc<32, 16, 1>(x, nimg, h, w, wt, bias, co, Y, status, st);
+  set_error("annf_cnn_conv_forward_tc: unsupported layer shape");
   return ANNF_ERR_UNSUPPORTED;
 }
 

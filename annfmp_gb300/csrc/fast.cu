@@ -124,9 +124,8 @@ __global__ void __launch_bounds__(256) raw_nn_kernel(Img A, Img B, const int* __
 // parallel NNF: initial choice among candidates, then propagation / random-search passes
 // ---------------------------------------------------------------------------------------------
 struct Match {
-  int* idx;      // [nA] best B index
-  int* ssd;      // [nA] its exact raw SSD
-  uint8_t* chg;  // [nA] 1 if idx differs from the previous state (all 1 after the candidates)
+  int* idx;  // [nA] best B index
+  int* ssd;  // [nA] its exact raw SSD
 };
 
 __device__ __forceinline__ uint32_t hash3(uint32_t a, uint32_t b, uint32_t c) {
@@ -159,13 +158,11 @@ __global__ void fast_init_kernel(Img A, Img B, int nA, int K, const int* __restr
     }
     out.idx[i] = best;
     out.ssd[i] = bs;
-    out.chg[i] = 1;
   }
 }
 
 // one pass: the four neighbours' matches at distance 'jump', shifted to this pixel, and 'nrand'
-// random offsets around the current match within 'radius'. A neighbour whose match did not change
-// in the previous pass offers the candidate that pass already tried, and is skipped.
+// random offsets around the current match within 'radius'
 __global__ void fast_prop_kernel(Img A, Img B, int nA, int jump, int radius, int nrand, uint32_t seed, Match in,
                                  Match out) {
   const int nb_rows = B.h - B.psize + 1, na_rows = nA / A.ncols;
@@ -188,7 +185,6 @@ __global__ void fast_prop_kernel(Img A, Img B, int nA, int jump, int radius, int
     for (int t = 0; t < 4; ++t) {
       const int ny = y + dy[t] * jump, nx = x + dx[t] * jump;
       if (ny < 0 || nx < 0 || ny >= na_rows || nx >= A.ncols) continue;
-      if (!in.chg[ny * A.ncols + nx]) continue;
       const int nb = in.idx[ny * A.ncols + nx];
       if (nb < 0) continue;
       const int nby = nb / B.ncols, nbx = nb - nby * B.ncols;
@@ -199,7 +195,6 @@ __global__ void fast_prop_kernel(Img A, Img B, int nA, int jump, int radius, int
       const int ox = (int)(r % (2 * radius + 1)) - radius, oy = (int)((r >> 16) % (2 * radius + 1)) - radius;
       consider(b0y + oy, b0x + ox);
     }
-    out.chg[i] = best != in.idx[i] ? 1 : 0;
     out.idx[i] = best;
     out.ssd[i] = bs;
   }
@@ -305,7 +300,6 @@ __global__ void __launch_bounds__(256, 2) fast_init_t_kernel(Img A, Img B, int n
     }
     out.idx[i] = best;
     out.ssd[i] = bs;
-    out.chg[i] = 1;
   }
 }
 
@@ -334,7 +328,6 @@ __global__ void __launch_bounds__(256, 2) fast_prop_t_kernel(Img A, Img B, int n
     for (int t = 0; t < 4; ++t) {
       const int ny = y + dy[t] * jump, nx = x + dx[t] * jump;
       if (ny < 0 || nx < 0 || ny >= na_rows || nx >= A.ncols) continue;
-      if (!in.chg[ny * A.ncols + nx]) continue;
       const int nb = in.idx[ny * A.ncols + nx];
       if (nb < 0) continue;
       const int nby = nb / B.ncols, nbx = nb - nby * B.ncols;
@@ -345,7 +338,6 @@ __global__ void __launch_bounds__(256, 2) fast_prop_t_kernel(Img A, Img B, int n
       const int ox = (int)(r % (2 * radius + 1)) - radius, oy = (int)((r >> 16) % (2 * radius + 1)) - radius;
       consider(b0y + oy, b0x + ox);
     }
-    out.chg[i] = best != in.idx[i] ? 1 : 0;
     out.idx[i] = best;
     out.ssd[i] = bs;
   }
@@ -357,10 +349,9 @@ int fast_search(annf_handle* h, const uint8_t* img_a, int ha, int wa, const uint
   Img A{img_a, ha, wa, c, psize, wa - psize + 1, (long long)ha * wa * c};
   Img B{img_b, hb, wb, c, psize, wb - psize + 1, (long long)hb * wb * c};
   const int nA = (ha - psize + 1) * A.ncols;
-  ANNF_ENSURE(h->fast_buf, (size_t)4 * nA * sizeof(int) + 2 * (size_t)nA + 16);
+  ANNF_ENSURE(h->fast_buf, (size_t)4 * nA * sizeof(int));
   int* base = h->fast_buf.as<int>();
-  uint8_t* flags = reinterpret_cast<uint8_t*>(base + 4 * (size_t)nA);
-  Match m0{base, base + nA, flags}, m1{base + 2 * (size_t)nA, base + 3 * (size_t)nA, flags + nA};
+  Match m0{base, base + nA}, m1{base + 2 * (size_t)nA, base + 3 * (size_t)nA};
   const int blocks = (int)std::min<long long>(ceil_div(nA, 256), 32LL * num_sms());
   // shape-specialised kernels for the common patches, the generic ones otherwise
   const int shape = psize * 100 + psize * c;

@@ -72,6 +72,9 @@ class ProposalNet:
             self.b.append(torch.from_numpy(np.asarray(arrs[f"b{li}"], np.float32).copy()).to(self.dev))
         self.wf = [torch.empty(9 * ci * co, dtype=torch.float32, device=self.dev) for ci, co in LAYERS]
         self.wb = [torch.empty(9 * ci * co, dtype=torch.float32, device=self.dev) for ci, co in LAYERS]
+        self.wt = [torch.empty(((co + 15) // 16 * 16) * (288 if ci == 32 else 80), dtype=torch.int16, device=self.dev)
+                   for ci, co in LAYERS]
+        self.tensor_cores = True  # forward convolutions on tcgen05 (False: the CUDA-core kernels)
         self._dirty = True
 
     @classmethod
@@ -103,6 +106,7 @@ class ProposalNet:
         for li, (ci, co) in enumerate(LAYERS):
             self.h.call("annf_cnn_prep_weights", ptr(self.W[li]), co, ci, ptr(self.wf[li]), ptr(self.wb[li]),
                         self._stream())
+            self.h.call("annf_cnn_prep_weights_tc", ptr(self.W[li]), co, ci, ptr(self.wt[li]), self._stream())
         self._dirty = False
 
     # -- forward ----------------------------------------------------------------------------------
@@ -123,8 +127,12 @@ class ProposalNet:
         for li, (ci, co) in enumerate(LAYERS):
             last = li == len(LAYERS) - 1
             y = torch.empty((n, hh, ww, co), dtype=torch.float32 if last else torch.bfloat16, device=self.dev)
-            self.h.call("annf_cnn_conv_forward", ptr(x), n, hh, ww, ci, co, ptr(self.wf[li]), ptr(self.b[li]),
-                        0 if last else 1, ptr(y), self._stream())
+            if self.tensor_cores:
+                self.h.call("annf_cnn_conv_forward_tc", ptr(x), n, hh, ww, ci, co, ptr(self.wt[li]), ptr(self.b[li]),
+                            0 if last else 1, ptr(y), self._stream())
+            else:
+                self.h.call("annf_cnn_conv_forward", ptr(x), n, hh, ww, ci, co, ptr(self.wf[li]), ptr(self.b[li]),
+                            0 if last else 1, ptr(y), self._stream())
             if not last:
                 acts.append(y)
             x = y

@@ -240,6 +240,24 @@ def config_of(w, args):
 # ---------------------------------------------------------------------------------------------
 # GPU arm
 # ---------------------------------------------------------------------------------------------
+def reduce_max(x: float, world: int, device=None) -> float:
+    """The slowest rank's value (max over ranks; a no-op for one rank). Works with NCCL on CUDA
+    tensors and with gloo on CPU tensors."""
+    if world <= 1:
+        return float(x)
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device if device is not None else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_value(units_per_rank: int, ms: float, world: int) -> float:
+    """Whole-job throughput of `world` replicas that each processed units_per_rank in the slowest
+    rank's time ms (weak scaling, no data-path collective)."""
+    return world * units_per_rank / (ms / 1e3)
+
+
 def learned_available():
     from annfmp_gb300.proposal import DEFAULT_WEIGHTS
     return os.path.exists(DEFAULT_WEIGHTS)
@@ -319,11 +337,8 @@ def run_gpu(args, w, rank, world, local_rank):
         t_wall = time.perf_counter() - t_wall0
     launches = _lib.launch_count() - launches0
     h.profile(False)
-    ms = sum(s.elapsed_time(e) for s, e in ev) / args.steps
+    ms = reduce_max(sum(s.elapsed_time(e) for s, e in ev) / args.steps, world, dev)
     if world > 1:
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
         dist.barrier()
 
     # end to end through the public API: pinned host images in, host NNF out
@@ -337,11 +352,7 @@ def run_gpu(args, w, rank, world, local_rank):
         nn = model.fit(a_pin, b_pin)
         nn_host = nn.cpu()
         e2e_times.append(time.perf_counter() - t0)
-    e2e_s = float(np.median(e2e_times))
-    if world > 1:
-        t = torch.tensor([e2e_s], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = reduce_max(float(np.median(e2e_times)), world, dev)
 
     if rank != 0:
         return
@@ -366,12 +377,13 @@ def run_gpu(args, w, rank, world, local_rank):
             forms[f] = {"ms_per_step": fms, "value": n_a / (fms / 1e3), "distance_error": fq}
     achieved = by / (kernel_stages[dom] / 1e3) / 1e9
     traffic = load_traffic().get(f"{args.workload}:{args.form}:{dom}")
-    value = world * n_a / (ms / 1e3)
+    value = replica_value(n_a, ms, world)
     line = {
         "metric": "query patches/s", "value": value, "unit": "query patches/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": config_of(w, args),
-        "e2e": {"value": world * n_a / e2e_s, "unit": "query patches/s", "h2d_bytes_per_step": int(a.nbytes + b.nbytes),
+        "e2e": {"value": replica_value(n_a, e2e_s * 1e3, world), "unit": "query patches/s",
+                "h2d_bytes_per_step": int(a.nbytes + b.nbytes),
                 "d2h_bytes_per_step": int(nn_host.numel() * nn_host.element_size())},
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
@@ -449,7 +461,7 @@ def run_graph_workload(args, name, rank, world, local_rank):
             one_pass()
             ev[i][1].record()
         torch.cuda.synchronize(dev)
-    ms = sum(a.elapsed_time(b) for a, b in ev) / args.steps
+    ms = reduce_max(sum(a.elapsed_time(b) for a, b in ev) / args.steps, world, dev)
     # a sample of pairs checked against the exact raw-patch nearest neighbour
     from annfmp_gb300 import metrics
     errs = []
@@ -473,9 +485,9 @@ def run_graph_workload(args, name, rank, world, local_rank):
         return
     settings = sorted(set(tuple(x) for g in groups for x in g.settings()))
     line = {
-        "metric": "query patches/s", "value": world * n_a / (ms / 1e3), "unit": "query patches/s", "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": cfg["precision"], "data": "synthetic (generated on the GPU)",
+        "metric": "query patches/s", "value": replica_value(n_a, ms, world), "unit": "query patches/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": cfg["precision"], "data": "synthetic (generated on the GPU)",
         "config": {"workload": name, "pairs": len(pairs), "psize": p, "dim_reduced": cfg["dim_reduced"],
                    "k": cfg["n_neighbors"], "leaf_iters_chosen": settings, "graphs_per_step": len(feeds),
                    "form": "parallel" + ("+learned" if name == "stream" and learned_available() else ""),

@@ -204,6 +204,11 @@ int annf_cnn_prep_weights(annf_handle* h, const float* w, int co, int ci, float*
  * {(8,32), (32,32), (32,8)}. */
 int annf_cnn_conv_forward(annf_handle* h, const void* x, int nimg, int hgt, int wid, int ci, int co,
                           const float* w_fwd, const float* bias, int relu, void* y, void* stream);
+/* The same forward convolution on the tensor cores (tcgen05 implicit GEMM, M = 128 pixels,
+ * K = 9 x ci): w_tc [co padded to 16/32][9*ci padded to 16] BF16 from annf_cnn_prep_weights_tc. */
+int annf_cnn_prep_weights_tc(annf_handle* h, const float* w, int co, int ci, uint16_t* w_tc, void* stream);
+int annf_cnn_conv_forward_tc(annf_handle* h, const void* x, int nimg, int hgt, int wid, int ci, int co,
+                             const uint16_t* w_tc, const float* bias, int relu, void* y, void* stream);
 /* dx [nimg,hgt,wid,ci] FP32 = input gradient for upstream g [.., co] FP32, g multiplied by
  * (mask > 0) when mask (BF16 [.., co], the layer's ReLU output) is given. */
 int annf_cnn_conv_backward_data(annf_handle* h, const float* g, const void* mask, int nimg, int hgt, int wid, int co,

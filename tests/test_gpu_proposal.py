@@ -35,7 +35,8 @@ def test_cnn_input_matches_oracle(gpu_lib):
     assert np.array_equal(_bf16_np(x), C.net_input(a, b))
 
 
-def test_cnn_forward_backward_match_oracle(gpu_lib):
+@pytest.mark.parametrize("tensor_cores", [True, False])
+def test_cnn_forward_backward_match_oracle(gpu_lib, tensor_cores):
     """Layer by layer, each GPU layer equals the oracle fed the GPU's own stored input (BF16
     outputs within 1 BF16 ulp); loss, output gradient and all weight/bias gradients match the
     oracle's within FP32 summation-order tolerance."""
@@ -46,6 +47,7 @@ def test_cnn_forward_backward_match_oracle(gpu_lib):
     x0 = C.bf16_round((rng.standard_normal((N, h, w, 8)) * 0.8).astype(np.float32))
     x0[..., 6:] = 0
     net = _net()
+    net.tensor_cores = tensor_cores
     X = torch.from_numpy(x0).to(torch.bfloat16).cuda()
     out, acts = net.forward(X, keep=True)
     params = [(W.cpu().numpy(), b.cpu().numpy()) for W, b in zip(net.W, net.b)]
