@@ -94,6 +94,7 @@ SIGNATURES = {
     "annf_profile_enable": (_i, [_vp, _i]),
     "annf_profile_read": (_i, [_vp, _vp, _i, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_char_p)]),
     "annf_launch_count": (_ll, []),
+    "annf_buffer_epoch": (_ll, []),
 }
 
 _lock = threading.Lock()
@@ -122,6 +123,12 @@ def load(path: str | None = None):
 def launch_count() -> int:
     """Kernels launched by libannf_gb300.so in this process so far."""
     return int(load().annf_launch_count())
+
+
+def buffer_epoch() -> int:
+    """Reallocations of the library's device scratch buffers in this process so far (a captured
+    graph is valid while this is unchanged)."""
+    return int(load().annf_buffer_epoch())
 
 
 def check(status: int) -> None:

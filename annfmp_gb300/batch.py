@@ -64,7 +64,7 @@ class Autotuner:
                 continue
             for it in self.ITERS:
                 m = ANNFieldPropKDTreeGB300(form="parallel", iters=it, leaf_size=leaf, proposal=proposal,
-                                            leaf_precision=leaf_precision, verbose=0, **base_kw)
+                                            leaf_precision=leaf_precision, verbose=0, graph=False, **base_kw)
                 nn = m.fit(A, B)
                 torch.cuda.synchronize()
                 t0 = time.perf_counter()
@@ -125,7 +125,7 @@ class BatchNNF:
             kw, leaf, it = self._params(A, B)
             self.models.append(ANNFieldPropKDTreeGB300(form="parallel", iters=it, leaf_size=leaf,
                                                        proposal=self.proposal, leaf_precision=self.leaf_precision,
-                                                       verbose=0, **kw))
+                                                       verbose=0, graph=False, **kw))
         # one plain run per pair: validates it and sizes every device buffer
         for m, (A, B) in zip(self.models, self.inputs):
             m.fit(A, B)

@@ -15,6 +15,9 @@ void set_error(const std::string& msg) { g_last_error = msg; }
 static std::atomic<long long> g_launches{0};
 void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 
+static std::atomic<long long> g_reallocs{0};
+void count_realloc() { g_reallocs.fetch_add(1, std::memory_order_relaxed); }
+
 // implemented in tree_build.cu / search.cu / pca.cu
 int build_tree(annf_handle* h, const void* points, int n, int d, int real_type, int depth, int splitting,
                cudaStream_t st);
@@ -477,6 +480,8 @@ int annf_cnn_proposals(annf_handle* h, const float* out, int h4, int w4, int ha,
 }
 
 long long annf_launch_count(void) { return g_launches.load(std::memory_order_relaxed); }
+
+long long annf_buffer_epoch(void) { return g_reallocs.load(std::memory_order_relaxed); }
 
 int annf_profile_enable(annf_handle* h, int on) {
   ANNF_API_HANDLE(h);

@@ -224,19 +224,16 @@ __device__ __forceinline__ void row_words(const uint8_t* __restrict__ img, long 
     const uint4 q1 = __ldg(reinterpret_cast<const uint4*>(img + c0 + 16));
     const uint4 q2 = __ldg(reinterpret_cast<const uint4*>(img + c0 + 32));
     const unsigned x[13] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w, q2.x, q2.y, q2.z, q2.w, 0u};
-    const int sh = (s & 3) * 8;
-    switch (s >> 2) {
-#define ANNF_ROWW_CASE(Q)                                                                  \
-  case Q:                                                                                  \
-    _Pragma("unroll") for (int j = 0; j < NW; ++j) w[j] = __funnelshift_r(x[j + Q], x[j + Q + 1], sh); \
-    break;
-      ANNF_ROWW_CASE(0)
-      ANNF_ROWW_CASE(1)
-      ANNF_ROWW_CASE(2)
-      default:
-        ANNF_ROWW_CASE(3)
-#undef ANNF_ROWW_CASE
-    }
+    // w[j] = bytes s + 4j .. s + 4j + 3: pick the word pair (s >> 2) + j in two branch-free steps
+    // (lanes of a warp have different alignments), then shift
+    const int q = s >> 2, sh = (s & 3) * 8;
+    unsigned y2[NW + 2], y1[NW + 1];
+#pragma unroll
+    for (int k = 0; k < NW + 2; ++k) y2[k] = (q & 2) ? x[k + 2] : x[k];
+#pragma unroll
+    for (int k = 0; k < NW + 1; ++k) y1[k] = (q & 1) ? y2[k + 1] : y2[k];
+#pragma unroll
+    for (int j = 0; j < NW; ++j) w[j] = __funnelshift_r(y1[j], y1[j + 1], sh);
   } else {  // the last bytes of the image: byte loads, all in bounds
 #pragma unroll
     for (int j = 0; j < NW; ++j) {
@@ -250,93 +247,138 @@ __device__ __forceinline__ void row_words(const uint8_t* __restrict__ img, long 
   if (RL % 4) w[NW - 1] &= (1u << (8 * (RL % 4))) - 1u;
 }
 
-template <int PS, int RL>
-__device__ __forceinline__ void load_patch(const Img& I, int y, int x, unsigned (&w)[PS][(RL + 3) / 4]) {
-#pragma unroll
-  for (int r = 0; r < PS; ++r) row_words<RL>(I.p, ((long long)(y + r) * I.w + x) * I.c, I.bytes, w[r]);
-}
-
-// exact SSD of the cached A patch against B patch (by, bx); stops (returning a value > limit) as
-// soon as the partial sum exceeds limit
-template <int PS, int RL>
-__device__ __forceinline__ int ssd_limit(const unsigned (&aw)[PS][(RL + 3) / 4], const Img& B, int by, int bx,
-                                         int limit) {
+// exact SSDs of G candidate B patches (top-left rows cy, columns cx; cy < 0 marks an empty slot)
+// against the A patch (y, x). Row by row, the loads of every live candidate are issued together;
+// a candidate stops once its partial sum exceeds limit (its value is then > limit, so it cannot
+// beat a match of distance limit).
+template <int PS, int RL, int G>
+__device__ __forceinline__ void ssd_group(const Img& A, int y, int x, const Img& B, const int (&cy)[G],
+                                          const int (&cx)[G], int limit, int (&out)[G]) {
   constexpr int NW = (RL + 3) / 4;
-  unsigned s = 0;
+  unsigned s[G];
+  bool live[G];
 #pragma unroll
-  for (int r = 0; r < PS; ++r) {
-    unsigned bw[NW];
-    row_words<RL>(B.p, ((long long)(by + r) * B.w + bx) * B.c, B.bytes, bw);
-#pragma unroll
-    for (int j = 0; j < NW; ++j) {
-      const unsigned x = __vabsdiffu4(aw[r][j], bw[j]);
-      s = __dp4a(x, x, s);
-    }
-    if ((int)s > limit) return (int)s;
+  for (int g = 0; g < G; ++g) {
+    s[g] = 0;
+    live[g] = cy[g] >= 0;
   }
-  return (int)s;
+#pragma unroll 1
+  for (int r = 0; r < PS; ++r) {
+    bool any = false;
+#pragma unroll
+    for (int g = 0; g < G; ++g) any |= live[g];
+    if (!any) break;
+    unsigned aw[NW];
+    row_words<RL>(A.p, ((long long)(y + r) * A.w + x) * A.c, A.bytes, aw);
+    unsigned bw[G][NW];
+#pragma unroll
+    for (int g = 0; g < G; ++g)
+      if (live[g]) row_words<RL>(B.p, ((long long)(cy[g] + r) * B.w + cx[g]) * B.c, B.bytes, bw[g]);
+#pragma unroll
+    for (int g = 0; g < G; ++g) {
+      if (!live[g]) continue;
+#pragma unroll
+      for (int j = 0; j < NW; ++j) {
+        const unsigned dd = __vabsdiffu4(aw[j], bw[g][j]);
+        s[g] = __dp4a(dd, dd, s[g]);
+      }
+      if ((int)s[g] > limit) live[g] = false;
+    }
+  }
+#pragma unroll
+  for (int g = 0; g < G; ++g) out[g] = cy[g] < 0 ? 0x7fffffff : (int)s[g];
 }
 
+// the lexicographic minimum of (distance, index): the order-independent result of trying the
+// candidates one by one with "s < bs || (s == bs && b < best)"
+template <int G>
+__device__ __forceinline__ void take_best(const int (&cy)[G], const int (&cx)[G], const int (&ssd)[G], int ncols,
+                                          int& best, int& bs) {
+#pragma unroll
+  for (int g = 0; g < G; ++g) {
+    if (cy[g] < 0) continue;
+    const int b = cy[g] * ncols + cx[g];
+    if (ssd[g] < bs || (ssd[g] == bs && b < best)) {
+      bs = ssd[g];
+      best = b;
+    }
+  }
+}
+
+constexpr int kGroup = 4;  // candidates evaluated together
+
 template <int PS, int RL>
-__global__ void __launch_bounds__(256, 2) fast_init_t_kernel(Img A, Img B, int nA, int K, const int* __restrict__ nat_pos,
+__global__ void __launch_bounds__(256, 3) fast_init_t_kernel(Img A, Img B, int nA, int K, const int* __restrict__ nat_pos,
                                                           const int* __restrict__ perm, const int* __restrict__ prop,
                                                           int n_prop, Match out) {
   const int nb_rows = B.h - B.psize + 1;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nA; i += gridDim.x * blockDim.x) {
     const int y = i / A.ncols, x = i - y * A.ncols;
-    unsigned aw[PS][(RL + 3) / 4];
-    load_patch<PS, RL>(A, y, x, aw);
     int best = -1, bs = 0x7fffffff;
-    for (int j = 0; j < K + n_prop; ++j) {
-      int b = j < K ? __ldg(perm + __ldg(nat_pos + (long long)i * K + j)) : __ldg(prop + (long long)i * n_prop + (j - K));
-      if (b < 0 || b == best) continue;
-      const int by = b / B.ncols, bx = b - by * B.ncols;
-      if (by >= nb_rows) continue;
-      const int s = ssd_limit<PS, RL>(aw, B, by, bx, bs);
-      if (s < bs || (s == bs && b < best)) {
-        bs = s;
-        best = b;
+    for (int j0 = 0; j0 < K + n_prop; j0 += kGroup) {
+      int cy[kGroup], cx[kGroup], ssd[kGroup];
+#pragma unroll
+      for (int g = 0; g < kGroup; ++g) {
+        const int j = j0 + g;
+        cy[g] = -1;
+        cx[g] = 0;
+        if (j >= K + n_prop) continue;
+        const int b = j < K ? __ldg(perm + __ldg(nat_pos + (long long)i * K + j))
+                            : __ldg(prop + (long long)i * n_prop + (j - K));
+        if (b < 0) continue;
+        const int by = b / B.ncols;
+        if (by >= nb_rows) continue;
+        cy[g] = by;
+        cx[g] = b - by * B.ncols;
       }
+      ssd_group<PS, RL, kGroup>(A, y, x, B, cy, cx, bs, ssd);
+      take_best<kGroup>(cy, cx, ssd, B.ncols, best, bs);
     }
     out.idx[i] = best;
     out.ssd[i] = bs;
   }
 }
 
+// one pass: the four neighbours' matches at distance 'jump', shifted to this pixel (one group),
+// then 'nrand' random offsets around the pass's starting match within 'radius' (groups of four)
 template <int PS, int RL>
-__global__ void __launch_bounds__(256, 2) fast_prop_t_kernel(Img A, Img B, int nA, int jump, int radius, int nrand,
+__global__ void __launch_bounds__(256, 3) fast_prop_t_kernel(Img A, Img B, int nA, int jump, int radius, int nrand,
                                                           uint32_t seed, Match in, Match out) {
   const int nb_rows = B.h - B.psize + 1, na_rows = nA / A.ncols;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nA; i += gridDim.x * blockDim.x) {
     const int y = i / A.ncols, x = i - y * A.ncols;
     int best = in.idx[i], bs = in.ssd[i];
     const int b0y = best / B.ncols, b0x = best - b0y * B.ncols;
-    unsigned aw[PS][(RL + 3) / 4];
-    load_patch<PS, RL>(A, y, x, aw);
-    auto consider = [&](int by, int bx) {
-      if (by < 0 || bx < 0 || by >= nb_rows || bx >= B.ncols) return;
-      const int b = by * B.ncols + bx;
-      if (b == best) return;
-      const int s = ssd_limit<PS, RL>(aw, B, by, bx, bs);
-      if (s < bs || (s == bs && b < best)) {
-        bs = s;
-        best = b;
-      }
-    };
-    const int dy[4] = {-1, 1, 0, 0}, dx[4] = {0, 0, -1, 1};
+    const int ngroups = 1 + (radius > 0 ? (nrand + kGroup - 1) / kGroup : 0);
+    for (int grp = 0; grp < ngroups; ++grp) {  // one evaluation site keeps the registers down
+      int cy[kGroup], cx[kGroup], ssd[kGroup];
 #pragma unroll
-    for (int t = 0; t < 4; ++t) {
-      const int ny = y + dy[t] * jump, nx = x + dx[t] * jump;
-      if (ny < 0 || nx < 0 || ny >= na_rows || nx >= A.ncols) continue;
-      const int nb = in.idx[ny * A.ncols + nx];
-      if (nb < 0) continue;
-      const int nby = nb / B.ncols, nbx = nb - nby * B.ncols;
-      consider(nby - dy[t] * jump, nbx - dx[t] * jump);
-    }
-    for (int t = 0; t < nrand && radius > 0; ++t) {
-      const uint32_t r = hash3(seed, (uint32_t)i, (uint32_t)t);
-      const int ox = (int)(r % (2 * radius + 1)) - radius, oy = (int)((r >> 16) % (2 * radius + 1)) - radius;
-      consider(b0y + oy, b0x + ox);
+      for (int g = 0; g < kGroup; ++g) {
+        cy[g] = -1;
+        cx[g] = 0;
+        int by, bx;
+        if (grp == 0) {
+          const int ddy = g == 0 ? -1 : g == 1 ? 1 : 0, ddx = g == 2 ? -1 : g == 3 ? 1 : 0;
+          const int ny = y + ddy * jump, nx = x + ddx * jump;
+          if (ny < 0 || nx < 0 || ny >= na_rows || nx >= A.ncols) continue;
+          const int nb = in.idx[ny * A.ncols + nx];
+          if (nb < 0) continue;
+          const int nby = nb / B.ncols;
+          by = nby - ddy * jump;
+          bx = nb - nby * B.ncols - ddx * jump;
+        } else {
+          const int t = (grp - 1) * kGroup + g;
+          if (t >= nrand) continue;
+          const uint32_t r = hash3(seed, (uint32_t)i, (uint32_t)t);
+          by = b0y + (int)((r >> 16) % (2 * radius + 1)) - radius;
+          bx = b0x + (int)(r % (2 * radius + 1)) - radius;
+        }
+        if (by < 0 || bx < 0 || by >= nb_rows || bx >= B.ncols || by * B.ncols + bx == best) continue;
+        cy[g] = by;
+        cx[g] = bx;
+      }
+      ssd_group<PS, RL, kGroup>(A, y, x, B, cy, cx, bs, ssd);
+      take_best<kGroup>(cy, cx, ssd, B.ncols, best, bs);
     }
     out.idx[i] = best;
     out.ssd[i] = bs;

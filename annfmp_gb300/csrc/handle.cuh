@@ -11,13 +11,21 @@ struct cusolverDnContext;
 
 namespace annf {
 
+// counts replacements (free + larger allocation) of every DevBuf in the process: a captured CUDA
+// graph holds the buffers' addresses, and stays valid only while this count is unchanged (a first
+// allocation moves nothing and is not counted)
+void count_realloc();
+
 // grow-only device allocation
 struct DevBuf {
   void* p = nullptr;
   size_t bytes = 0;
   int ensure(size_t need) {
     if (need <= bytes) return ANNF_OK;
-    if (p) cudaFree(p);
+    if (p) {
+      count_realloc();
+      cudaFree(p);
+    }
     p = nullptr;
     bytes = 0;
     size_t sz = need < 256 ? 256 : need;

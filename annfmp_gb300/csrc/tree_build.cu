@@ -404,9 +404,117 @@ __global__ void leaf_box_kernel(int L, int d, const T* __restrict__ pts, const i
 
 // ---------------------------------------------------------------------------------------------
 // shared-memory subtree finisher: one CTA per segment of level t0, levels t0..depth-1
+//
+// Staged points use an odd row stride (d | 1), so that lanes reading one coordinate of different
+// rows fall in different banks. While a level has fewer segments than warps, a segment is shared
+// by G = warps / segments warps: each takes a contiguous chunk of the segment's positions; their
+// bounding-box partials, histogram counts and "<" counts are combined in shared memory, so the
+// result is the one a single warp walking the segment in order produces. From the level with one
+// segment per warp on, each warp splits its segments alone.
 // ---------------------------------------------------------------------------------------------
 constexpr int kSubThreads = 256;
 constexpr int kSubWarps = kSubThreads / 32;
+
+__host__ __device__ __forceinline__ int sub_stride(int d) { return d | 1; }
+
+// radix-select step of one warp: from the 256-bin histogram of the keys that match the prefix,
+// the bin holding rank 'rank' and the number of keys in lower bins
+__device__ __forceinline__ void select_bin(const unsigned* hist, int lane, int rank, int& bin, int& before) {
+  int c[8], tot = 0;
+#pragma unroll
+  for (int z = 0; z < 8; ++z) {
+    c[z] = (int)hist[8 * lane + z];  // lane owns bins [8*lane, 8*lane+8)
+    tot += c[z];
+  }
+  int inc = tot;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    int x = __shfl_up_sync(0xffffffffu, inc, o);
+    if (lane >= o) inc += x;
+  }
+  const int ex = inc - tot;
+  const unsigned own = __ballot_sync(0xffffffffu, ex <= rank && rank < inc);
+  const int src = __ffs(own) - 1;
+  bin = 0;
+  before = 0;
+  if (lane == src) {
+    int run = ex;
+#pragma unroll
+    for (int z = 0; z < 8; ++z) {
+      if (run <= rank && rank < run + c[z]) {
+        bin = 8 * lane + z;
+        before = run;
+      }
+      run += c[z];
+    }
+  }
+  bin = __shfl_sync(0xffffffffu, bin, src);
+  before = __shfl_sync(0xffffffffu, before, src);
+}
+
+// histogram of the keys in [ca, cb) that match prefix under hmask, by one warp (aggregated atomics)
+template <typename K>
+__device__ __forceinline__ void warp_hist(const K* skey, int ca, int cb, int lane, K prefix, K hmask, int shift,
+                                          unsigned* hist) {
+  for (int base = ca; base < cb; base += 32) {
+    const int i = base + lane;
+    unsigned bin = 256u;
+    if (i < cb) {
+      const K k = skey[i];
+      if (((k ^ prefix) & hmask) == 0) bin = (unsigned)(k >> shift) & 255u;
+    }
+    const unsigned peers = __match_any_sync(0xffffffffu, bin);
+    if (bin != 256u && lane == __ffs(peers) - 1) atomicAdd(&hist[bin], (unsigned)__popc(peers));
+  }
+}
+
+// stable partition of positions [ca, cb) by key < pivot: "<" forward from a + ltb, ">=" backward
+// from b - 1 - geb (cur -> nxt)
+template <typename K>
+__device__ __forceinline__ void warp_partition(const K* skey, const uint16_t* cur, uint16_t* nxt, int ca, int cb,
+                                               int a, int b, int lane, K pivot, int ltb, int geb) {
+  for (int base = ca; base < cb; base += 32) {
+    const int i = base + lane;
+    const bool valid = i < cb;
+    const K k = valid ? skey[i] : (K)0;
+    const bool lt = valid && (k < pivot), ge = valid && !(k < pivot);
+    const unsigned mlt = __ballot_sync(0xffffffffu, lt), mge = __ballot_sync(0xffffffffu, ge);
+    const unsigned below = (1u << lane) - 1u;
+    if (lt) nxt[a + ltb + __popc(mlt & below)] = cur[i];
+    if (ge) nxt[b - 1 - (geb + __popc(mge & below))] = cur[i];
+    ltb += __popc(mlt);
+    geb += __popc(mge);
+  }
+}
+
+// forward swap pass of the elements equal to the pivot over the ">=" block [a + nlt, b), then the
+// node's axis and split value (one warp)
+template <typename T, typename K>
+__device__ __forceinline__ void warp_finish_split(const T* spts, int ds, uint16_t* nxt, int a, int b, int nlt,
+                                                  int half, int axis, K pivot, int lane, int node,
+                                                  int* __restrict__ node_axis, T* __restrict__ node_split) {
+  int w = a + nlt;
+  for (int base = a + nlt; base < b; base += 32) {
+    const int i = base + lane;
+    const bool eq = i < b && ord_key(spts[(size_t)nxt[i] * ds + axis]) == pivot;
+    unsigned msk = __ballot_sync(0xffffffffu, eq);
+    while (msk) {
+      const int p = base + __ffs(msk) - 1;
+      msk &= msk - 1;
+      if (lane == 0 && p != w) {
+        uint16_t tmp = nxt[p];
+        nxt[p] = nxt[w];
+        nxt[w] = tmp;
+      }
+      ++w;
+      __syncwarp();
+    }
+  }
+  if (lane == 0) {
+    node_axis[node] = axis;
+    node_split[node] = spts[(size_t)nxt[a + half] * ds + axis];
+  }
+}
 
 template <typename T>
 __global__ void __launch_bounds__(kSubThreads) subtree_kernel(
@@ -415,11 +523,20 @@ __global__ void __launch_bounds__(kSubThreads) subtree_kernel(
     int* __restrict__ node_axis, T* __restrict__ node_split, int* __restrict__ leaf_begin,
     int* __restrict__ point_leaf, unsigned* status) {
   using K = typename key_of<T>::type;
+  constexpr int kBits = 8 * sizeof(K);
+  const int ds = sub_stride(d);
   extern __shared__ __align__(16) unsigned char smem[];
-  T* spts = reinterpret_cast<T*>(smem);
-  K* skey = reinterpret_cast<K*>(spts + (size_t)smax * d);
-  int* sperm = reinterpret_cast<int*>(skey + smax);
-  unsigned* shist = reinterpret_cast<unsigned*>(sperm + smax);
+  T* spts = reinterpret_cast<T*>(smem);                         // [smax][ds]
+  T* spmn = spts + (size_t)smax * ds;                           // [warps][d] bounding-box partials
+  T* spmx = spmn + (size_t)kSubWarps * d;
+  K* skey = reinterpret_cast<K*>(spmx + (size_t)kSubWarps * d);  // [smax]
+  K* sprefix = skey + smax;                                     // [warps] per-group select state
+  int* sperm = reinterpret_cast<int*>(sprefix + kSubWarps);     // [smax]
+  int* saxis = sperm + smax;
+  int* srank = saxis + kSubWarps;
+  int* snlt = srank + kSubWarps;
+  int* scnt = snlt + kSubWarps;
+  unsigned* shist = reinterpret_cast<unsigned*>(scnt + kSubWarps);  // [warps][256]
   uint16_t* sidx0 = reinterpret_cast<uint16_t*>(shist + kSubWarps * 256);
   uint16_t* sidx1 = sidx0 + smax;
   if (smem_overrun(smem, sidx1 + smax, status)) return;
@@ -430,7 +547,10 @@ __global__ void __launch_bounds__(kSubThreads) subtree_kernel(
   const int cnt = hi - lo;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 
-  for (long long e = threadIdx.x; e < (long long)cnt * d; e += blockDim.x) spts[e] = pts_in[(long long)lo * d + e];
+  for (long long e = threadIdx.x; e < (long long)cnt * d; e += blockDim.x) {
+    const int r = (int)(e / d), c = (int)(e - (long long)r * d);
+    spts[(size_t)r * ds + c] = pts_in[(long long)lo * d + e];
+  }
   for (int i = threadIdx.x; i < cnt; i += blockDim.x) {
     sperm[i] = perm_in[lo + i];
     sidx0[i] = (uint16_t)i;
@@ -439,132 +559,155 @@ __global__ void __launch_bounds__(kSubThreads) subtree_kernel(
 
   uint16_t* cur = sidx0;
   uint16_t* nxt = sidx1;
-  unsigned* hist = shist + warp * 256;
-  constexpr int kBits = 8 * sizeof(K);
 
   for (int l = t0; l < depth; ++l) {
     const int nsub = 1 << (l - t0);
-    for (int u = warp; u < nsub; u += kSubWarps) {
-      int a, b;
-      seg_range(cnt, l - t0, u, a, b);
-      const int m = b - a, half = m / 2;
-      // --- widest axis (or cyclic) ---
-      T best = 0;
-      int axis = splitting == 0 ? l % d : 0;
-      for (int j = 0; splitting != 0 && j < d; ++j) {
-        T mn = real_traits<T>::big(), mx = -real_traits<T>::big();
-        for (int i = a + lane; i < b; i += 32) {
-          T v = spts[(size_t)cur[i] * d + j];
-          mn = v < mn ? v : mn;
-          mx = v > mx ? v : mx;
-        }
-#pragma unroll
-        for (int o = 16; o; o >>= 1) {
-          T omn = __shfl_xor_sync(0xffffffffu, mn, o), omx = __shfl_xor_sync(0xffffffffu, mx, o);
-          mn = omn < mn ? omn : mn;
-          mx = omx > mx ? omx : mx;
-        }
-        T w = real_traits<T>::sub(mx, mn);
-        if (w > best) {
-          best = w;
-          axis = j;
-        }
-      }
-      // --- keys + radix select of rank 'half' ---
-      for (int i = a + lane; i < b; i += 32) skey[i] = ord_key(spts[(size_t)cur[i] * d + axis]);
-      K prefix = 0;
-      int rank = half, nlt = 0;
-      for (int shift = kBits - 8; shift >= 0; shift -= 8) {
-        for (int z = lane; z < 256; z += 32) hist[z] = 0;
-        __syncwarp();
-        const K hmask = (shift + 8 >= kBits) ? (K)0 : (~(K)0 << (shift + 8));
-        for (int base = a; base < b; base += 32) {
-          const int i = base + lane;
-          unsigned bin = 256u;
-          if (i < b) {
-            const K k = skey[i];
-            if (((k ^ prefix) & hmask) == 0) bin = (unsigned)(k >> shift) & 255u;
+    if (nsub >= kSubWarps) {
+      // ---- one warp per segment ----
+      unsigned* hist = shist + warp * 256;
+      for (int u = warp; u < nsub; u += kSubWarps) {
+        int a, b;
+        seg_range(cnt, l - t0, u, a, b);
+        const int half = (b - a) / 2;
+        T best = 0;
+        int axis = splitting == 0 ? l % d : 0;
+        for (int j = 0; splitting != 0 && j < d; ++j) {
+          T mn = real_traits<T>::big(), mx = -real_traits<T>::big();
+          for (int i = a + lane; i < b; i += 32) {
+            const T v = spts[(size_t)cur[i] * ds + j];
+            mn = v < mn ? v : mn;
+            mx = v > mx ? v : mx;
           }
-          const unsigned peers = __match_any_sync(0xffffffffu, bin);
-          if (bin != 256u && lane == __ffs(peers) - 1) atomicAdd(&hist[bin], (unsigned)__popc(peers));
-        }
-        __syncwarp();
-        // lane owns bins [8*lane, 8*lane+8)
-        int c[8], tot = 0;
 #pragma unroll
-        for (int z = 0; z < 8; ++z) {
-          c[z] = (int)hist[8 * lane + z];
-          tot += c[z];
-        }
-        int inc = tot;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-          int x = __shfl_up_sync(0xffffffffu, inc, o);
-          if (lane >= o) inc += x;
-        }
-        int ex = inc - tot;
-        unsigned own = __ballot_sync(0xffffffffu, ex <= rank && rank < inc);
-        int src = __ffs(own) - 1;
-        int bin = 0, before = 0;
-        if (lane == src) {
-          int run = ex;
-#pragma unroll
-          for (int z = 0; z < 8; ++z) {
-            if (run <= rank && rank < run + c[z]) {
-              bin = 8 * lane + z;
-              before = run;
-            }
-            run += c[z];
+          for (int o = 16; o; o >>= 1) {
+            const T omn = __shfl_xor_sync(0xffffffffu, mn, o), omx = __shfl_xor_sync(0xffffffffu, mx, o);
+            mn = omn < mn ? omn : mn;
+            mx = omx > mx ? omx : mx;
+          }
+          const T wd = real_traits<T>::sub(mx, mn);
+          if (wd > best) {
+            best = wd;
+            axis = j;
           }
         }
-        bin = __shfl_sync(0xffffffffu, bin, src);
-        before = __shfl_sync(0xffffffffu, before, src);
-        prefix |= ((K)bin) << shift;
-        nlt += before;
-        rank -= before;
-        __syncwarp();
-      }
-      const K pivot = prefix;
-      // --- stable partition: "<" forward, ">=" from the back ---
-      int ltb = 0, geb = 0;
-      for (int base = a; base < b; base += 32) {
-        const int i = base + lane;
-        const bool valid = i < b;
-        const K k = valid ? skey[i] : (K)0;
-        const bool lt = valid && (k < pivot), ge = valid && !(k < pivot);
-        const unsigned mlt = __ballot_sync(0xffffffffu, lt), mge = __ballot_sync(0xffffffffu, ge);
-        const unsigned below = (1u << lane) - 1u;
-        if (lt) nxt[a + ltb + __popc(mlt & below)] = cur[i];
-        if (ge) nxt[b - 1 - (geb + __popc(mge & below))] = cur[i];
-        ltb += __popc(mlt);
-        geb += __popc(mge);
-      }
-      __syncwarp();
-      // --- forward swap pass of the equal elements over the ">=" block ---
-      int w = a + nlt;
-      for (int base = a + nlt; base < b; base += 32) {
-        const int i = base + lane;
-        const bool eq = i < b && ord_key(spts[(size_t)nxt[i] * d + axis]) == pivot;
-        unsigned msk = __ballot_sync(0xffffffffu, eq);
-        while (msk) {
-          const int p = base + __ffs(msk) - 1;
-          msk &= msk - 1;
-          if (lane == 0 && p != w) {
-            uint16_t tmp = nxt[p];
-            nxt[p] = nxt[w];
-            nxt[w] = tmp;
-          }
-          ++w;
+        for (int i = a + lane; i < b; i += 32) skey[i] = ord_key(spts[(size_t)cur[i] * ds + axis]);
+        K prefix = 0;
+        int rank = half, nlt = 0;
+        for (int shift = kBits - 8; shift >= 0; shift -= 8) {
+          for (int z = lane; z < 256; z += 32) hist[z] = 0;
+          __syncwarp();
+          const K hmask = (shift + 8 >= kBits) ? (K)0 : (~(K)0 << (shift + 8));
+          warp_hist<K>(skey, a, b, lane, prefix, hmask, shift, hist);
+          __syncwarp();
+          int bin, before;
+          select_bin(hist, lane, rank, bin, before);
+          prefix |= ((K)bin) << shift;
+          nlt += before;
+          rank -= before;
           __syncwarp();
         }
+        warp_partition<K>(skey, cur, nxt, a, b, a, b, lane, prefix, 0, 0);
+        __syncwarp();
+        warp_finish_split<T, K>(spts, ds, nxt, a, b, nlt, half, axis, prefix, lane,
+                                (1 << l) - 1 + (s << (l - t0)) + u, node_axis, node_split);
       }
-      if (lane == 0) {
-        const int node = (1 << l) - 1 + (s << (l - t0)) + u;
-        node_axis[node] = axis;
-        node_split[node] = spts[(size_t)nxt[a + half] * d + axis];
+    } else {
+      // ---- G warps per segment, each on a contiguous chunk ----
+      const int G = kSubWarps / nsub;
+      const int u = warp / G, gw = warp - u * G, w0 = u * G;
+      int a, b;
+      seg_range(cnt, l - t0, u, a, b);
+      const int half = (b - a) / 2;
+      const int cs = (((b - a) + G - 1) / G + 31) & ~31;
+      const int ca = min(b, a + gw * cs), cb = min(b, ca + cs);
+      if (splitting != 0) {
+        for (int j = 0; j < d; ++j) {
+          T mn = real_traits<T>::big(), mx = -real_traits<T>::big();
+          for (int i = ca + lane; i < cb; i += 32) {
+            const T v = spts[(size_t)cur[i] * ds + j];
+            mn = v < mn ? v : mn;
+            mx = v > mx ? v : mx;
+          }
+#pragma unroll
+          for (int o = 16; o; o >>= 1) {
+            const T omn = __shfl_xor_sync(0xffffffffu, mn, o), omx = __shfl_xor_sync(0xffffffffu, mx, o);
+            mn = omn < mn ? omn : mn;
+            mx = omx > mx ? omx : mx;
+          }
+          if (lane == 0) {
+            spmn[warp * d + j] = mn;
+            spmx[warp * d + j] = mx;
+          }
+        }
       }
-      // positions of this sub-segment that were not rewritten keep nothing stale: every position
-      // in [a,b) was written by the partition above
+      // the group's two histogram buffers, used by alternate digit passes
+      unsigned* ghist = shist + u * 512;
+      for (int z = gw * 32 + lane; z < 512; z += G * 32) ghist[z] = 0;
+      __syncthreads();
+      if (gw == 0 && lane == 0) {
+        T best = 0;
+        int axis = splitting == 0 ? l % d : 0;
+        for (int j = 0; splitting != 0 && j < d; ++j) {
+          T mn = spmn[w0 * d + j], mx = spmx[w0 * d + j];
+          for (int g = 1; g < G; ++g) {
+            const T omn = spmn[(w0 + g) * d + j], omx = spmx[(w0 + g) * d + j];
+            mn = omn < mn ? omn : mn;
+            mx = omx > mx ? omx : mx;
+          }
+          const T wd = real_traits<T>::sub(mx, mn);
+          if (wd > best) {
+            best = wd;
+            axis = j;
+          }
+        }
+        saxis[u] = axis;
+        sprefix[u] = 0;
+        srank[u] = half;
+        snlt[u] = 0;
+      }
+      __syncthreads();
+      const int axis = saxis[u];
+      for (int i = ca + lane; i < cb; i += 32) skey[i] = ord_key(spts[(size_t)cur[i] * ds + axis]);
+      int pass = 0;
+      for (int shift = kBits - 8; shift >= 0; shift -= 8, ++pass) {
+        unsigned* hist = ghist + (pass & 1) * 256;
+        const K hmask = (shift + 8 >= kBits) ? (K)0 : (~(K)0 << (shift + 8));
+        warp_hist<K>(skey, ca, cb, lane, sprefix[u], hmask, shift, hist);
+        __syncthreads();
+        if (gw == 0) {
+          int bin, before;
+          select_bin(hist, lane, srank[u], bin, before);
+          __syncwarp();
+          if (lane == 0) {
+            sprefix[u] |= ((K)bin) << shift;
+            snlt[u] += before;
+            srank[u] -= before;
+          }
+        }
+        // the other buffer was read two passes ago: clear it for the next pass
+        unsigned* other = ghist + ((pass + 1) & 1) * 256;
+        for (int z = gw * 32 + lane; z < 256; z += G * 32) other[z] = 0;
+        __syncthreads();
+      }
+      const K pivot = sprefix[u];
+      int clt = 0;
+      for (int base = ca; base < cb; base += 32) {
+        const int i = base + lane;
+        clt += __popc(__ballot_sync(0xffffffffu, i < cb && skey[i] < pivot));
+      }
+      if (lane == 0) scnt[warp] = clt;
+      __syncthreads();
+      int ltb = 0, geb = 0;
+      for (int g = 0; g < gw; ++g) {
+        const int ga = min(b, a + g * cs), gb = min(b, ga + cs);
+        ltb += scnt[w0 + g];
+        geb += (gb - ga) - scnt[w0 + g];
+      }
+      warp_partition<K>(skey, cur, nxt, ca, cb, a, b, lane, pivot, ltb, geb);
+      __syncthreads();
+      if (gw == 0)
+        warp_finish_split<T, K>(spts, ds, nxt, a, b, snlt[u], half, axis, pivot, lane,
+                                (1 << l) - 1 + (s << (l - t0)) + u, node_axis, node_split);
     }
     __syncthreads();
     uint16_t* tmp = cur;
@@ -585,7 +728,7 @@ __global__ void __launch_bounds__(kSubThreads) subtree_kernel(
   }
   for (long long e = threadIdx.x; e < (long long)cnt * d; e += blockDim.x) {
     const int r = (int)(e / d), c = (int)(e - (long long)r * d);
-    pts_out[(long long)(lo + r) * d + c] = spts[(size_t)cur[r] * d + c];
+    pts_out[(long long)(lo + r) * d + c] = spts[(size_t)cur[r] * ds + c];
   }
   for (int i = threadIdx.x; i < cnt; i += blockDim.x) perm_out[lo + i] = sperm[cur[i]];
 }
@@ -593,7 +736,8 @@ __global__ void __launch_bounds__(kSubThreads) subtree_kernel(
 template <typename T>
 static size_t subtree_smem(int smax, int d) {
   using K = typename key_of<T>::type;
-  return (size_t)smax * d * sizeof(T) + (size_t)smax * sizeof(K) + (size_t)smax * sizeof(int) +
+  return (size_t)smax * sub_stride(d) * sizeof(T) + 2 * (size_t)kSubWarps * d * sizeof(T) +
+         (size_t)(smax + kSubWarps) * sizeof(K) + (size_t)(smax + 4 * kSubWarps) * sizeof(int) +
          kSubWarps * 256 * sizeof(unsigned) + 2 * (size_t)smax * sizeof(uint16_t);
 }
 

@@ -78,7 +78,7 @@ class ANNFieldPropKDTreeGB300:
     def __init__(self, n_neighbors=3, psize=8, dim_reduced=5, n_subset=1000, leaf_size=64, n_jobs=-1,
                  propagate=True, select_best_nn=True, float_type="float", verbose=1, seed=0, device=0,
                  form="plain", iters=4, proposal=None, pca_solver=None, pca_iters=6, leaf_precision=None,
-                 projection=None, search=(2, 8)):
+                 projection=None, search=(2, 8), graph="auto"):
         """Reference parameters, plus: ``form`` "plain" (the reference's row-sequential method,
         the drop-in) or "parallel" (natural-leaf candidates + proposals + parallel propagation,
         every candidate checked by exact raw-patch distance); ``iters`` propagation passes of the
@@ -91,7 +91,13 @@ class ANNFieldPropKDTreeGB300:
         exact FP32 re-rank of the survivors of a proven BF16 error bound; the default) or "fp32";
         ``projection`` "exact" (the FP64 result rounded once, the reference's) or "bf16" (BF16
         components on the tensor cores, FP32 sums); None picks "exact" for the plain form, "bf16"
-        otherwise when the shapes allow it."""
+        otherwise when the shapes allow it; ``graph``: repeated fits with unchanged shapes and
+        parameters replay one captured CUDA graph of the whole NNF ("auto": the parallel form;
+        False: never; the plain form is never captured, its cuSOLVER eigensolver sizes its
+        workspace on the host)."""
+        self.graph = graph
+        self._graph = None       # captured state: key, epoch, graph, static inputs, outputs
+        self._graph_seen = None  # key of the last eager fit (capture happens on the second call)
         self.leaf_precision = leaf_precision
         self.projection = projection
         self.search = search  # parallel form: (random offsets per pass, initial search radius)
@@ -124,7 +130,100 @@ class ANNFieldPropKDTreeGB300:
         """image_a and image_b have shape (h, w, c), uint8 (numpy or torch). sync=False (device
         tensors only) enqueues the whole NNF on the current stream without any host
         synchronisation, timing or status check, so that it can be captured into a CUDA graph; the
-        returned tensor is filled when the stream reaches it."""
+        returned tensor is filled when the stream reaches it.
+
+        With graphs enabled, the first fit of a (shapes, parameters) combination runs eagerly
+        (sizing every device buffer), the second captures the NNF into a CUDA graph with static
+        input images, and later fits copy the inputs in and replay it: one launch per NNF. The
+        graph is dropped when the shapes or parameters change or when any of the library's
+        device buffers has been reallocated since the capture."""
+        if sync and self._graph_wanted():
+            return self._fit_graph(image_a, image_b)
+        return self._fit(image_a, image_b, sync)
+
+    # -- CUDA graph replay --------------------------------------------------------------------------
+    def _graph_wanted(self):
+        if self.graph == "auto":
+            return self.form != "plain"
+        if self.graph and self.form == "plain":
+            raise ValueError("the plain form cannot be captured into a CUDA graph (its eigensolver sizes "
+                             "its workspace on the host)")
+        return bool(self.graph)
+
+    def _graph_key(self, image_a, image_b, dev):
+        shape = lambda x: tuple(x.shape) if hasattr(x, "shape") else tuple(numpy.asarray(x).shape)  # noqa: E731
+        return (shape(image_a), shape(image_b), str(dev), self.form, self.n_neighbors, self.psize,
+                self.dim_reduced, self.n_subset, self.leaf_size, self.iters, self.seed, self.float_type,
+                self.leaf_precision, self.projection, tuple(self.search), self.pca_solver, self.pca_iters,
+                id(self.proposal), bool(self.propagate), bool(self.select_best_nn))
+
+    # attributes a fit leaves behind; a replay points them back at the graph's tensors
+    _FIT_ATTRS = ("components_", "mean_", "patches_a_reduced_", "patches_b_reduced_", "nn_distances_",
+                  "_subset_pos", "_n_rows", "_n_cols", "kdtree", "_A", "_B")
+
+    def _capture(self, image_a, image_b, key, dev):
+        from ._torch import to_device as _to
+        A_s = _to(image_a, torch.uint8, dev).clone()
+        B_s = _to(image_b, torch.uint8, dev).clone()
+        epoch = _lib.buffer_epoch()
+        cur = torch.cuda.current_stream(dev)
+        warm = torch.cuda.Stream(dev)
+        warm.wait_stream(cur)
+        with torch.cuda.stream(warm):  # warm the capture on a side stream (torch's recommendation)
+            self._fit(A_s, B_s, sync=False)
+        cur.wait_stream(warm)
+        torch.cuda.synchronize(dev)
+        g = torch.cuda.CUDAGraph()
+        launches = _lib.launch_count()
+        with torch.cuda.graph(g, capture_error_mode="relaxed"):
+            nn = self._fit(A_s, B_s, sync=False)
+        torch.cuda.synchronize(dev)
+        launches = _lib.launch_count() - launches
+        if _lib.buffer_epoch() != epoch:  # a buffer grew during the capture: its nodes are stale
+            return None
+        attrs = {a: getattr(self, a) for a in self._FIT_ATTRS if hasattr(self, a)}
+        return {"key": key, "epoch": epoch, "graph": g, "A": A_s, "B": B_s, "nn": nn, "attrs": attrs,
+                "tree_X": self._tree.X, "kernels": launches}
+
+    def _fit_graph(self, image_a, image_b):
+        dev = require_cuda(self.device)
+        key = self._graph_key(image_a, image_b, dev)
+        g = self._graph
+        if g is not None and (g["key"] != key or g["epoch"] != _lib.buffer_epoch()):
+            self._graph = g = None
+        if g is None:
+            if self._graph_seen != key:  # first fit of this combination: eager, sizes every buffer
+                nn = self._fit(image_a, image_b, True)
+                self._graph_seen = key
+                return nn
+            self._graph = g = self._capture(image_a, image_b, key, dev)
+            if g is None:
+                self._graph_seen = None
+                return self._fit(image_a, image_b, True)
+        numpy_io = is_numpy(image_a)
+        self.image_a = image_a
+        self.image_b = image_b
+        for src, dst in ((image_a, g["A"]), (image_b, g["B"])):
+            if isinstance(src, torch.Tensor):
+                dst.copy_(src.reshape(dst.shape), non_blocking=True)
+            else:
+                dst.copy_(torch.from_numpy(numpy.ascontiguousarray(src, dtype=numpy.uint8)).reshape(dst.shape))
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        g["graph"].replay()
+        e1.record()
+        for a, v in g["attrs"].items():
+            setattr(self, a, v)
+        self._tree.X = g["tree_X"]
+        self._tree.check_device()  # synchronises and raises if a kernel's bounds check tripped
+        self._timers = collections.OrderedDict(graph=e0.elapsed_time(e1) / 1e3)
+        if self.verbose > 0:
+            print("Graph replay (whole NNF):\t{}".format(self._timers["graph"]))
+        if numpy_io:
+            return g["nn"].cpu().numpy()
+        return g["nn"].clone()
+
+    def _fit(self, image_a, image_b, sync):
         numpy.random.seed(self.seed)  # annfmp/openmp/base.py:60
         dev = require_cuda(self.device)
         real = self._get_torch_float_type()
@@ -178,6 +277,7 @@ class ANNFieldPropKDTreeGB300:
         m = int(self.n_subset / 2)
         pos_a = _SUBSETS.get(self._n_rows, self._n_cols, m, self.seed, dev)
         pos_b = _SUBSETS.get(hb - p + 1, wb - p + 1, m, self.seed + 1, dev)
+        self._subset_pos = (pos_a, pos_b)  # kept alive while a captured graph reads them
         self.components_ = torch.empty((d, P), dtype=torch.float64, device=dev)
         self.mean_ = torch.empty(P, dtype=torch.float64, device=dev)
         if self.form not in self.FORMS:

@@ -143,8 +143,8 @@ def stage_bytes(stage, w, n_a, n_b, depth, n_cols, it=1):
         return n_a * (k * 2 * P + 4 * k + 8)
     if stage == "first_row":  # every point once per 128-query tile
         return -(-n_cols // 128) * n_b * 4 * d + n_cols * 4 * d
-    if stage == "project":
-        return (w["size"] ** 2) * 3 + n_b * 4 * d
+    if stage == "project":  # both images: pixels in, reduced patches out
+        return 2 * ((w["size"] ** 2) * 3 + n_b * 4 * d)
     return None
 
 
@@ -263,11 +263,12 @@ def learned_available():
     return os.path.exists(DEFAULT_WEIGHTS)
 
 
-def make_model(form, args, prm, local_rank):
+def make_model(form, args, prm, local_rank, graph="auto"):
     """plain: the reference's method; parallel: subspace PCA, BF16 tensor-core projection and leaf
-    tiles, parallel propagation; learned: parallel + the trained offset-proposal network."""
+    tiles, parallel propagation; learned: parallel + the trained offset-proposal network. The
+    parallel forms replay a captured CUDA graph from their third fit on (graph="auto")."""
     from annfmp_gb300 import ANNFieldPropKDTreeGB300
-    kw = dict(verbose=0, device=local_rank, **prm)
+    kw = dict(verbose=0, device=local_rank, graph=graph, **prm)
     if form == "plain":
         return ANNFieldPropKDTreeGB300(**kw)
     proposal = None
@@ -315,10 +316,7 @@ def run_gpu(args, w, rank, world, local_rank):
     for _ in range(args.warmup):
         model.fit(A, B)
     torch.cuda.synchronize(dev)
-    h = model.kdtree.handle
-    h.profile(True)
-    h.profile_read(torch.cuda.current_stream(dev).cuda_stream)
-    stages = {}
+    graphed = getattr(model, "_graph", None) is not None
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     if world > 1:
         dist.barrier()
@@ -331,13 +329,29 @@ def run_gpu(args, w, rank, world, local_rank):
             ev[i][0].record()
             nn_dev = model.fit(A, B)
             ev[i][1].record()
-            for name, ms in h.profile_read(torch.cuda.current_stream(dev).cuda_stream):
-                stages.setdefault(name, []).append(ms)
         torch.cuda.synchronize(dev)
         t_wall = time.perf_counter() - t_wall0
     launches = _lib.launch_count() - launches0
-    h.profile(False)
+    if graphed:  # a replay launches the kernels the capture recorded
+        launches = args.steps * model._graph["kernels"]
     ms = reduce_max(sum(s.elapsed_time(e) for s, e in ev) / args.steps, world, dev)
+
+    # per-stage kernel times: the same form run eagerly with the library's stage marks
+    pm = make_model(args.form, args, prm, local_rank, graph=False) if graphed else model
+    pm.fit(A, B)
+    h = pm.kdtree.handle
+    h.profile(True)
+    h.profile_read(torch.cuda.current_stream(dev).cuda_stream)
+    stages = {}
+    for i in range(max(2, min(args.steps, 4))):
+        flush.fill_(float(i))
+        pm.fit(A, B)
+        step = {}  # a stage that repeats within a fit (per image, per tree level) adds up
+        for name, sms in h.profile_read(torch.cuda.current_stream(dev).cuda_stream):
+            step[name] = step.get(name, 0.0) + sms
+        for name, sms in step.items():
+            stages.setdefault(name, []).append(sms)
+    h.profile(False)
     if world > 1:
         dist.barrier()
 
@@ -358,7 +372,7 @@ def run_gpu(args, w, rank, world, local_rank):
         return
     stage_ms = {k: float(np.mean(v)) for k, v in stages.items()}
     kernel_stages = {k: v for k, v in stage_ms.items() if not k.endswith(":begin")}
-    depth = model.kdtree.final_tree_depth_
+    depth = pm.kdtree.final_tree_depth_
     peak, peak_kind = load_peaks()
     sb = lambda k: stage_bytes(k, w, n_a, n_b, depth, n_cols, args.iters)  # noqa: E731
     dom = max((k for k in kernel_stages if sb(k)), key=lambda k: kernel_stages[k])
@@ -381,7 +395,8 @@ def run_gpu(args, w, rank, world, local_rank):
     line = {
         "metric": "query patches/s", "value": value, "unit": "query patches/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": config_of(w, args),
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": dict(config_of(w, args), execution="one CUDA graph replay per NNF" if graphed else "eager"),
         "e2e": {"value": replica_value(n_a, e2e_s * 1e3, world), "unit": "query patches/s",
                 "h2d_bytes_per_step": int(a.nbytes + b.nbytes),
                 "d2h_bytes_per_step": int(nn_host.numel() * nn_host.element_size())},

@@ -248,6 +248,13 @@ int annf_profile_enable(annf_handle* h, int on);
 int annf_profile_read(annf_handle* h, void* stream, int cap, float* ms, const char** names);
 long long annf_launch_count(void);
 
+/* Graph capture support (no counterpart in the reference). Handles keep grow-only device scratch
+ * buffers; a CUDA graph captured around library calls holds their addresses. annf_buffer_epoch
+ * returns how many times any handle in the process has replaced a buffer by a larger one (first
+ * allocations are not counted): a graph captured at epoch e may be replayed only while
+ * annf_buffer_epoch() == e. */
+long long annf_buffer_epoch(void);
+
 #ifdef __cplusplus
 }
 #endif
