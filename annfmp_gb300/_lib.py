@@ -77,7 +77,7 @@ SIGNATURES = {
                                _vp]),
     "annf_tc_tile": (_i, [_vp, _vp, _vp, _i, _i, _vp, _vp]),
     "annf_natural_knn": (_i, [_vp, _vp, ctypes.c_longlong, _i, _i, _vp, _vp]),
-    "annf_project_bf16": (_i, [_vp, _vp, _i, _i, _i, _i, _vp, _vp, _i, _vp, _vp]),
+    "annf_project_f16": (_i, [_vp, _vp, _i, _i, _i, _i, _vp, _vp, _i, _vp, _vp]),
     "annf_cnn_input": (_i, [_vp, _vp, _vp, _i, _i, _vp, _vp]),
     "annf_cnn_prep_weights": (_i, [_vp, _vp, _i, _i, _vp, _vp, _vp]),
     "annf_cnn_conv_forward": (_i, [_vp, _vp, _i, _i, _i, _i, _i, _vp, _vp, _i, _vp, _vp]),

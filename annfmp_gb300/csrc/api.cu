@@ -349,13 +349,13 @@ int annf_raw_nn(annf_handle* h, const uint8_t* img_a, int ha, int wa, const uint
                 static_cast<cudaStream_t>(stream));
 }
 
-int annf_project_bf16(annf_handle* h, const uint8_t* img, int hgt, int wid, int channels, int psize,
+int annf_project_f16(annf_handle* h, const uint8_t* img, int hgt, int wid, int channels, int psize,
                       const double* components, const double* mean, int n_components, float* out, void* stream) {
   ANNF_API_HANDLE(h);
-  ANNF_REQUIRE(img && components && mean && out, "annf_project_bf16: NULL argument");
-  ANNF_REQUIRE(channels >= 1 && psize >= 1 && psize <= hgt && psize <= wid, "annf_project_bf16: bad geometry");
+  ANNF_REQUIRE(img && components && mean && out, "annf_project_f16: NULL argument");
+  ANNF_REQUIRE(channels >= 1 && psize >= 1 && psize <= hgt && psize <= wid, "annf_project_f16: bad geometry");
   if (!project_tc_supported(psize, channels, n_components)) {
-    set_error("annf_project_bf16: needs psize*psize*channels <= 256 and n_components <= 32");
+    set_error("annf_project_f16: needs psize*psize*channels <= 256 and n_components <= 32");
     return ANNF_ERR_UNSUPPORTED;
   }
   return project_tc(h, img, hgt, wid, channels, psize, components, mean, n_components, out,

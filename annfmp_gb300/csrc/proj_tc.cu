@@ -1,16 +1,17 @@
 // proj_tc.cu -- patch extraction fused with the PCA projection on the tensor cores (sm_103a).
 //
-// For the approximate NNF forms: every psize x psize x c patch of an image times the BF16-rounded
+// For the approximate NNF forms: every psize x psize x c patch of an image times the FP16-rounded
 // components, FP32 accumulation, minus the projected mean. One tile = 128 consecutive patches of one
 // row: the psize image rows they cover are staged in shared memory (aligned 32-bit loads), each thread
-// pair expands one patch into the K-major BF16 A tile (core-matrix layout; K runs over the patch
+// pair expands one patch into the K-major FP16 A tile (core-matrix layout; K runs over the patch
 // rows, each padded to a multiple of 8 bytes so that a group of 8 is 8 consecutive image bytes, and
-// the components are permuted to match), and tcgen05.mma
+// the components are permuted to match), and tcgen05.mma kind::f16
 // (M = 128, N = components rounded up to 16) accumulates in TMEM; the epilogue reads TMEM, subtracts
-// the mean term and writes FP32 reduced patches. Pixel values 0..255 are exact in BF16 and every
-// product is exact in FP32, so the only rounding beyond FP32 summation is that of the components.
+// the mean term and writes FP32 reduced patches. Pixel values 0..255 are exact in FP16 and every
+// product is exact in FP32, so the only rounding beyond FP32 summation is that of the components
+// (FP16: 11 significant bits).
 // The exact projection (pca.cu) remains the drop-in path.
-#include <cuda_bf16.h>
+#include <cuda_fp16.h>
 
 #include <algorithm>
 
@@ -33,9 +34,9 @@ __device__ __forceinline__ bool pj_wait(uint64_t* mbar, uint32_t phase) {
   return true;
 }
 
-// B operand [npad][kpad] BF16 row-major, K in the tile's order (patch row r occupies
+// B operand [npad][kpad] FP16 row-major, K in the tile's order (patch row r occupies
 // [r*rs, r*rs + psize*C) with rs = psize*C rounded up to 8; padding zero), and the FP32 mean term
-// m_j = sum_k bf16(c_jk) mean_k
+// m_j = sum_k f16(c_jk) mean_k
 __global__ void pj_prep_kernel(const double* __restrict__ comps, const double* __restrict__ mean, int d, int P,
                                int rowlen, int rs, int npad, int kpad, uint16_t* __restrict__ bmat,
                                float* __restrict__ mterm) {
@@ -44,28 +45,68 @@ __global__ void pj_prep_kernel(const double* __restrict__ comps, const double* _
     const int r = k / rs, el = k - r * rs;
     const int src = r * rowlen + el;
     const float v = (j < d && el < rowlen && src < P) ? (float)comps[(size_t)j * P + src] : 0.f;
-    __nv_bfloat16 b = __float2bfloat16_rn(v);
-    bmat[e] = *reinterpret_cast<uint16_t*>(&b);
+    bmat[e] = __half_as_ushort(__float2half_rn(v));
   }
   if (blockIdx.x == 0) {
     for (int j = threadIdx.x; j < d; j += blockDim.x) {
       double s = 0.0;
       for (int k = 0; k < P; ++k)
-        s += (double)__bfloat162float(__float2bfloat16_rn((float)comps[(size_t)j * P + k])) * mean[k];
+        s += (double)__half2float(__float2half_rn((float)comps[(size_t)j * P + k])) * mean[k];
       mterm[j] = (float)s;
     }
   }
 }
 
-// eight BF16 values of eight consecutive bytes (two words), bytes at or beyond `valid` zeroed
-__device__ __forceinline__ uint4 bytes_to_bf16x8(uint32_t w0, uint32_t w1, int valid) {
-  uint32_t v[8];
+// eight FP16 values of eight consecutive bytes (w0 = bytes 0..3, w1 = bytes 4..7): a byte permute
+// pairs each byte b with the byte 0x64, giving the half 1024 + b (bits 0x64bb, exact: 1024 + b <
+// 2048), and one packed subtraction of 1024 leaves b exactly. Bytes past the patch row meet zero
+// components in the B tile, so they need no masking.
+__device__ __forceinline__ uint4 bytes_to_f16x8(uint32_t w0, uint32_t w1) {
+  constexpr uint32_t kMagic = 0x64646464u;
+  const __half2 k1024 = __halves2half2(__ushort_as_half((unsigned short)0x6400), __ushort_as_half((unsigned short)0x6400));
+  const uint32_t p[4] = {__byte_perm(w0, kMagic, 0x4140), __byte_perm(w0, kMagic, 0x4342),
+                         __byte_perm(w1, kMagic, 0x4140), __byte_perm(w1, kMagic, 0x4342)};
+  uint32_t o[4];
 #pragma unroll
-  for (int u = 0; u < 8; ++u) {
-    const uint32_t b = ((u < 4 ? w0 : w1) >> (8 * (u & 3))) & 0xFFu;
-    v[u] = u < valid ? (__float_as_uint(__uint2float_rn(b)) >> 16) : 0u;  // exact: b < 256
+  for (int u = 0; u < 4; ++u) {
+    const __half2 h = __hsub2(*reinterpret_cast<const __half2*>(&p[u]), k1024);
+    o[u] = *reinterpret_cast<const uint32_t*>(&h);
   }
-  return make_uint4(v[0] | (v[1] << 16), v[2] | (v[3] << 16), v[4] | (v[5] << 16), v[6] | (v[7] << 16));
+  return make_uint4(o[0], o[1], o[2], o[3]);
+}
+
+// 4-byte asynchronous global -> shared copy (both addresses 4-byte aligned), and its group fences
+__device__ __forceinline__ void cp_async4(void* sdst, const void* gsrc) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(tc::smem_addr(sdst)), "l"(gsrc) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
+// stage the psize image rows of tile t as aligned words: byte b of row r sits at
+// sI[r*sw + s0(r) + b] with s0(r) = (start of row r) mod 4 (rows need not start 4-byte aligned: W * C
+// may be odd). Interior words are copied asynchronously; the image's last bytes synchronously.
+__device__ __forceinline__ void pj_stage(const uint8_t* __restrict__ img, long long t, int tiles_x, int ncols, int W,
+                                         int C, int psize, long long nbytes, int sw, uint8_t* sI) {
+  const int y = (int)(t / tiles_x), x0 = (int)(t - (long long)y * tiles_x) * 128;
+  const int np = min(128, ncols - x0);
+  const long long row0 = ((long long)y * W + x0) * C;
+  const long long pitch = (long long)W * C;
+  const int span = (np + psize - 1) * C;
+  const int nw = (3 + span + 3) >> 2;  // words per staged row, enough for any shift
+  for (int e = threadIdx.x; e < psize * nw; e += kPjThreads) {
+    const int r = e / nw, wi = e - r * nw;
+    const long long a = ((row0 + (long long)r * pitch) & ~3LL) + 4LL * wi;  // 4-byte aligned
+    uint8_t* dst = sI + r * sw + 4 * wi;
+    if (a + 4 <= nbytes) {
+      cp_async4(dst, img + a);
+    } else {
+      uint32_t v = 0;
+      for (int u = 0; u < 4; ++u)
+        if (a + u < nbytes) v |= (uint32_t)__ldg(img + a + u) << (8 * u);
+      *reinterpret_cast<uint32_t*>(dst) = v;
+    }
+  }
 }
 
 template <int NPAD>
@@ -86,7 +127,9 @@ __global__ void __launch_bounds__(kPjThreads) project_tc_kernel(const uint8_t* _
   p += (size_t)128 * kpad * 2;
   unsigned char* sB = p;
   p += (size_t)NPAD * kpad * 2;
-  uint8_t* sI = p;
+  uint8_t* sI0 = p;  // staged rows, double buffered: the next tile's rows arrive during this tile
+  p += (size_t)psize * sw;
+  uint8_t* sI1 = p;
   p += (size_t)psize * sw;
   p = reinterpret_cast<unsigned char*>(((uintptr_t)p + 15) & ~uintptr_t(15));
   uint64_t* mbar = reinterpret_cast<uint64_t*>(p);
@@ -116,33 +159,24 @@ __global__ void __launch_bounds__(kPjThreads) project_tc_kernel(const uint8_t* _
   __syncthreads();
   tc::fence_after_sync();
   const uint32_t tmem = *tslot;
-  const uint32_t idesc = tc::idesc_bf16(128, NPAD);
+  const uint32_t idesc = tc::idesc_f16(128, NPAD);
   const int row = tid & 127, half = tid >> 7;  // patch row of the tile; K half (expansion) / column half
   const int ngrp = kpad / 8, gpr = rs / 8;     // K groups in all / per patch row
   uint32_t phase = 0;
-  for (long long t = blockIdx.x; t < ntiles; t += gridDim.x) {
+  if (blockIdx.x < ntiles) pj_stage(img, blockIdx.x, tiles_x, ncols, W, C, psize, nbytes, sw, sI0);
+  cp_async_commit();
+  int buf = 0;
+  for (long long t = blockIdx.x; t < ntiles; t += gridDim.x, buf ^= 1) {
     const int y = (int)(t / tiles_x), x0 = (int)(t - (long long)y * tiles_x) * 128;
     const int np = min(128, ncols - x0);
-    // stage the psize image rows as aligned words; byte b of row r sits at sI[r*sw + s0(r) + b] with
-    // s0(r) = (start of row r) mod 4 (rows need not start 4-byte aligned: W * C may be odd)
     const long long row0 = ((long long)y * W + x0) * C;
     const long long pitch = (long long)W * C;
-    const int span = (np + psize - 1) * C;
-    const int nw = (3 + span + 3) >> 2;  // words per staged row, enough for any shift
-    for (int e = tid; e < psize * nw; e += kPjThreads) {
-      const int r = e / nw, wi = e - r * nw;
-      const long long rs0 = row0 + (long long)r * pitch;
-      const long long a = (rs0 & ~3LL) + 4LL * wi;  // 4-byte aligned
-      uint32_t v;
-      if (a + 4 <= nbytes) {
-        v = __ldg(reinterpret_cast<const uint32_t*>(img + a));
-      } else {  // the image's last bytes
-        v = 0;
-        for (int u = 0; u < 4; ++u)
-          if (a + u < nbytes) v |= (uint32_t)__ldg(img + a + u) << (8 * u);
-      }
-      *reinterpret_cast<uint32_t*>(sI + r * sw + 4 * wi) = v;
-    }
+    uint8_t* sI = buf ? sI1 : sI0;
+    // the next tile's rows go to the other buffer (last read by the previous tile's expansion,
+    // which every thread finished before the barrier that precedes its MMA)
+    if (t + gridDim.x < ntiles) pj_stage(img, t + gridDim.x, tiles_x, ncols, W, C, psize, nbytes, sw, buf ? sI0 : sI1);
+    cp_async_commit();
+    cp_async_wait<1>();  // this tile's copies (all but the group just committed)
     __syncthreads();
     // expand: group g of patch `row` = bytes [e0, e0 + 8) of its patch row r (zero beyond rowlen)
     const int g0 = half ? ngrp / 2 : 0, g1 = half ? ngrp : ngrp / 2;
@@ -154,7 +188,7 @@ __global__ void __launch_bounds__(kPjThreads) project_tc_kernel(const uint8_t* _
         const uint32_t* wp = reinterpret_cast<const uint32_t*>(sI + (off & ~3));
         const int sh = (off & 3) * 8;
         const uint32_t q0 = wp[0], q1 = wp[1], q2 = wp[2];
-        w = bytes_to_bf16x8(__funnelshift_r(q0, q1, sh), __funnelshift_r(q1, q2, sh), rowlen - e0);
+        w = bytes_to_f16x8(__funnelshift_r(q0, q1, sh), __funnelshift_r(q1, q2, sh));
       }
       *reinterpret_cast<uint4*>(sA + tc::core_offset(row, g * 8, kpad)) = w;
     }
@@ -189,14 +223,23 @@ __global__ void __launch_bounds__(kPjThreads) project_tc_kernel(const uint8_t* _
       tc::tmem_wait_ld();
       if (lane_row < np) {
         float* dst = out + ((size_t)y * ncols + x0 + lane_row) * d;
+        if (d == NPAD) {  // whole 16-byte groups (rows of d floats are 16-byte aligned)
 #pragma unroll
-        for (int j = 0; j < HC; ++j)
-          if (c0 + j < d) dst[c0 + j] = __uint_as_float(r[j]) - mterm[c0 + j];
+          for (int j = 0; j < HC; j += 4)
+            *reinterpret_cast<float4*>(dst + c0 + j) =
+                make_float4(__uint_as_float(r[j]) - mterm[c0 + j], __uint_as_float(r[j + 1]) - mterm[c0 + j + 1],
+                            __uint_as_float(r[j + 2]) - mterm[c0 + j + 2], __uint_as_float(r[j + 3]) - mterm[c0 + j + 3]);
+        } else {
+#pragma unroll
+          for (int j = 0; j < HC; ++j)
+            if (c0 + j < d) dst[c0 + j] = __uint_as_float(r[j]) - mterm[c0 + j];
+        }
       }
     }
     tc::fence_before_sync();
     __syncthreads();
   }
+  cp_async_wait<0>();  // no copy may still target this CTA's shared memory when it exits
   if (sflag[0]) {
     if (tid == 0) atomicOr(status, DEV_TC_TIMEOUT);
     pj_wait(mbar, phase ^ 1u);
@@ -213,7 +256,7 @@ bool project_tc_supported(int psize, int c, int ncomp) {
 
 int project_tc(annf_handle* h, const uint8_t* img, int H, int W, int c, int psize, const double* comps,
                const double* mean, int ncomp, float* out, cudaStream_t st) {
-  ANNF_REQUIRE(project_tc_supported(psize, c, ncomp), "annf_project_bf16: patch or components too large");
+  ANNF_REQUIRE(project_tc_supported(psize, c, ncomp), "annf_project_f16: patch or components too large");
   const int P = psize * psize * c;
   const int rowlen = psize * c, rs = (rowlen + 7) & ~7;
   const int kpad = (psize * rs + 15) / 16 * 16;
@@ -226,8 +269,8 @@ int project_tc(annf_handle* h, const uint8_t* img, int H, int W, int c, int psiz
                                                                                          rs, npad, kpad, bmat, mterm);
   ANNF_CHECK_LAUNCH();
   const int sw = (((128 + psize - 1) * c + 3 + 16) + 15) & ~15;
-  const size_t smem = (size_t)128 * kpad * 2 + (size_t)npad * kpad * 2 + (size_t)psize * sw + 16 + 24 + 64;
-  ANNF_REQUIRE(smem <= 227 * 1024, "annf_project_bf16: tile too large for shared memory");
+  const size_t smem = (size_t)128 * kpad * 2 + (size_t)npad * kpad * 2 + 2 * (size_t)psize * sw + 16 + 24 + 64;
+  ANNF_REQUIRE(smem <= 227 * 1024, "annf_project_f16: tile too large for shared memory");
   const long long ntiles = (long long)((W - psize + 1 + 127) / 128) * (H - psize + 1);
   // TMEM: 32 columns per CTA, so any residency fits; two CTAs per SM by shared memory at P = 243
   const int grid = (int)std::max(1LL, std::min<long long>(ntiles, 4LL * num_sms()));

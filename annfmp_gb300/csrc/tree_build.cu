@@ -24,6 +24,7 @@
 namespace annf {
 
 constexpr int kChunk = 2048;     // positions per CTA in the global levels
+constexpr int kMaxFusedD = 128;  // dimensions for which the scatter also computes the children's boxes
 constexpr int kThreads = 256;
 constexpr int kItems = kChunk / kThreads;
 
@@ -95,9 +96,17 @@ __global__ void bbox_kernel(int n, int d, int t, int B, const T* __restrict__ pt
 template <typename T>
 __global__ void axis_kernel(int n, int d, int t, int S, int splitting, const typename key_of<T>::type* gmin,
                             const typename key_of<T>::type* gmax, int* axis,
-                            typename key_of<T>::type* prefix, int* rank, int* nlt) {
+                            typename key_of<T>::type* prefix, int* rank, int* nlt,
+                            typename key_of<T>::type* cmin, typename key_of<T>::type* cmax) {
+  using K = typename key_of<T>::type;
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= S) return;
+  if (cmin != nullptr) {  // the children's boxes, filled by this level's scatter: start empty
+    for (int j = 0; j < 2 * d; ++j) {
+      cmin[(long long)2 * s * d + j] = key_max<K>();
+      cmax[(long long)2 * s * d + j] = (K)0;
+    }
+  }
   int lo, hi;
   seg_range(n, t, s, lo, hi);
   T best = 0;
@@ -244,9 +253,11 @@ __global__ void __launch_bounds__(kThreads) scatter_kernel(
     const typename key_of<T>::type* __restrict__ pivot, const int* __restrict__ nlt,
     const int* __restrict__ neq, const int* __restrict__ blk_lt, const int* __restrict__ blk_eq,
     const T* __restrict__ pts_in, const int* __restrict__ perm_in, T* __restrict__ pts_out,
-    int* __restrict__ perm_out, int* __restrict__ eqpos) {
+    int* __restrict__ perm_out, int* __restrict__ eqpos, typename key_of<T>::type* cmin,
+    typename key_of<T>::type* cmax) {
   using K = typename key_of<T>::type;
   __shared__ int sdst[kChunk];
+  __shared__ unsigned char sside[kChunk];  // child of each element: 0 left, 1 right
   const int s = blockIdx.x / B, bb = blockIdx.x % B;
   int lo, hi;
   seg_range(n, t, s, lo, hi);
@@ -287,23 +298,30 @@ __global__ void __launch_bounds__(kThreads) scatter_kernel(
   int lt_before = sum_lt + elt;
   int eq_before = sum_eq + eeq;
   const int seg_neq = neq[s];
+  // after the fix-up the left child holds the "<" elements and the first (half - nlt) equal
+  // elements of the ">=" block, i.e. the equal elements of input rank >= neq - (half - nlt)
+  const int eq_left_from = seg_neq - ((hi - lo) / 2 - nlt[s]);
 #pragma unroll
   for (int q = 0; q < kItems; ++q) {
     int i = base + q;
     if (i < m) {
       int r = (c0 - lo) + i;  // rank of the element in its segment (input order)
       int dst;
+      unsigned char side = 1;
       if ((flt >> q) & 1u) {
         dst = lo + lt_before;
         ++lt_before;
+        side = 0;
       } else {
         dst = hi - 1 - (r - lt_before);  // ">=" elements fill from the back
         if ((feq >> q) & 1u) {
           eqpos[lo + (seg_neq - 1 - eq_before)] = dst;  // ascending position order
+          side = eq_before >= eq_left_from ? 0 : 1;
           ++eq_before;
         }
       }
       sdst[i] = dst;
+      sside[i] = side;
     }
   }
   __syncthreads();
@@ -312,9 +330,71 @@ __global__ void __launch_bounds__(kThreads) scatter_kernel(
     const int w = d >> 2;  // float4 words per row
     const float4* src = reinterpret_cast<const float4*>(pts_in) + (long long)c0 * w;
     float4* dst4 = reinterpret_cast<float4*>(pts_out);
-    for (int e = threadIdx.x; e < m * w; e += blockDim.x) {
-      const int r = e / w, c = e - r * w;
-      dst4[(long long)sdst[r] * w + c] = src[e];
+    if (cmin == nullptr) {
+      for (int e = threadIdx.x; e < m * w; e += blockDim.x) {
+        const int r = e / w, c = e - r * w;
+        dst4[(long long)sdst[r] * w + c] = src[e];
+      }
+    } else {
+      // the children's bounding boxes on the way: a thread always handles word c = tid mod w
+      // (w divides the block), keeping the order keys of its four coordinates per child
+      K mn[2][4], mx[2][4];
+#pragma unroll
+      for (int u = 0; u < 2; ++u)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          mn[u][j] = key_max<K>();
+          mx[u][j] = (K)0;
+        }
+      for (int e = threadIdx.x; e < m * w; e += blockDim.x) {
+        const int r = e / w, c = e - r * w;
+        const float4 v = src[e];
+        dst4[(long long)sdst[r] * w + c] = v;
+        const K kv[4] = {(K)ord_key(v.x), (K)ord_key(v.y), (K)ord_key(v.z), (K)ord_key(v.w)};
+        const bool rt = sside[r] != 0;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          if (rt) {
+            mn[1][j] = kv[j] < mn[1][j] ? kv[j] : mn[1][j];
+            mx[1][j] = kv[j] > mx[1][j] ? kv[j] : mx[1][j];
+          } else {
+            mn[0][j] = kv[j] < mn[0][j] ? kv[j] : mn[0][j];
+            mx[0][j] = kv[j] > mx[0][j] ? kv[j] : mx[0][j];
+          }
+        }
+      }
+      // lanes of a warp with the same word: xor offsets w, 2w, ..., 16
+      for (int o = w; o < 32; o <<= 1) {
+#pragma unroll
+        for (int u = 0; u < 2; ++u)
+#pragma unroll
+          for (int j = 0; j < 4; ++j) {
+            const K a = __shfl_xor_sync(0xffffffffu, mn[u][j], o), b = __shfl_xor_sync(0xffffffffu, mx[u][j], o);
+            mn[u][j] = a < mn[u][j] ? a : mn[u][j];
+            mx[u][j] = b > mx[u][j] ? b : mx[u][j];
+          }
+      }
+      __shared__ K sbmn[2 * kMaxFusedD], sbmx[2 * kMaxFusedD];
+      for (int j = threadIdx.x; j < 2 * d; j += blockDim.x) {
+        sbmn[j] = key_max<K>();
+        sbmx[j] = (K)0;
+      }
+      __syncthreads();
+      const int lane = threadIdx.x & 31;
+      if (lane < w) {
+#pragma unroll
+        for (int u = 0; u < 2; ++u)
+#pragma unroll
+          for (int j = 0; j < 4; ++j) {
+            if (mn[u][j] != key_max<K>()) atomicMin(&sbmn[u * d + 4 * lane + j], mn[u][j]);
+            if (mx[u][j] != (K)0) atomicMax(&sbmx[u * d + 4 * lane + j], mx[u][j]);
+          }
+      }
+      __syncthreads();
+      for (int j = threadIdx.x; j < 2 * d; j += blockDim.x) {
+        if (sbmn[j] != key_max<K>()) atomicMin(&cmin[(long long)2 * s * d + j], sbmn[j]);
+        if (sbmx[j] != (K)0) atomicMax(&cmax[(long long)2 * s * d + j], sbmx[j]);
+      }
     }
   } else {
     for (int e = threadIdx.x; e < m * d; e += blockDim.x) {
@@ -323,7 +403,6 @@ __global__ void __launch_bounds__(kThreads) scatter_kernel(
     }
   }
   for (int i = threadIdx.x; i < m; i += blockDim.x) perm_out[sdst[i]] = perm_in[c0 + i];
-  (void)nlt;
 }
 
 // one warp per segment: the reference's forward swap pass over the equal elements, then the node
@@ -775,6 +854,20 @@ static int build_impl(annf_handle* h, const T* points, int n, int d, int depth, 
 
   const int smax = subtree_capacity<T>(d);
   const size_t sub_smem = subtree_smem<T>(smax, d);
+  // global levels run while a segment exceeds the finisher's capacity; their bounding boxes live
+  // in two halves of bmin / bmax (this level's, the children's)
+  int tg = 0;
+  while (tg < depth && ((long long)n + (1LL << tg) - 1) / (1LL << tg) > smax) ++tg;
+  const long long cap = 1LL << tg;  // segments of the deepest level that needs a box
+  // from level 1 on the scatter computes the children's boxes when a row is whole float4 words, a
+  // power of two of them (a thread then always handles the same word)
+  const bool fused = sizeof(T) == 4 && (d & 3) == 0 && d <= kMaxFusedD && ((d >> 2) & ((d >> 2) - 1)) == 0;
+  if (tg > 0) {
+    ANNF_ENSURE(h->bmin, (size_t)2 * cap * d * sizeof(K));
+    ANNF_ENSURE(h->bmax, (size_t)2 * cap * d * sizeof(K));
+    ANNF_ENSURE(h->hist, (size_t)(cap / 2) * 256 * sizeof(unsigned));
+    ANNF_CUDA_TRY(cudaMemsetAsync(h->hist.p, 0, (size_t)(cap / 2) * 256 * sizeof(unsigned), st));  // picks re-zero it
+  }
   bool finished = false;
   for (int t = 0; t < depth; ++t) {
     const int S = 1 << t;
@@ -797,29 +890,30 @@ static int build_impl(annf_handle* h, const T* points, int n, int d, int depth, 
       set_error("tree too large for the level kernels");
       return ANNF_ERR_UNSUPPORTED;
     }
-    ANNF_ENSURE(h->bmin, (size_t)S * d * sizeof(K));
-    ANNF_ENSURE(h->bmax, (size_t)S * d * sizeof(K));
     ANNF_ENSURE(h->axis, (size_t)S * sizeof(int));
     ANNF_ENSURE(h->sel_prefix, (size_t)S * sizeof(K));
     ANNF_ENSURE(h->sel_rank, (size_t)S * sizeof(int));
     ANNF_ENSURE(h->sel_nlt, (size_t)S * sizeof(int));
     ANNF_ENSURE(h->sel_neq, (size_t)S * sizeof(int));
-    ANNF_ENSURE(h->hist, (size_t)S * 256 * sizeof(unsigned));
     ANNF_ENSURE(h->blk_lt, (size_t)nblk * sizeof(int));
     ANNF_ENSURE(h->blk_eq, (size_t)nblk * sizeof(int));
-    K* gmin = h->bmin.as<K>();
-    K* gmax = h->bmax.as<K>();
-    const int fb = std::min(ceil_div((long long)S * d, 256), 4096);
-    fill_keys_kernel<K><<<fb, 256, 0, st>>>(gmin, (long long)S * d, ~(K)0);
-    ANNF_CHECK_LAUNCH();
-    fill_keys_kernel<K><<<fb, 256, 0, st>>>(gmax, (long long)S * d, (K)0);
-    ANNF_CHECK_LAUNCH();
-    ANNF_CUDA_TRY(cudaMemsetAsync(h->hist.p, 0, (size_t)S * 256 * sizeof(unsigned), st));
-    bbox_kernel<T><<<(unsigned)nblk, kThreads, 0, st>>>(n, d, t, B, cur_pts, gmin, gmax);
-    ANNF_CHECK_LAUNCH();
+    K* gmin = h->bmin.as<K>() + (size_t)(t & 1) * cap * d;
+    K* gmax = h->bmax.as<K>() + (size_t)(t & 1) * cap * d;
+    // the children's boxes, when the next level is a global one and the scatter can compute them
+    K* cmin = (fused && t + 1 < tg) ? h->bmin.as<K>() + (size_t)((t + 1) & 1) * cap * d : nullptr;
+    K* cmax = (fused && t + 1 < tg) ? h->bmax.as<K>() + (size_t)((t + 1) & 1) * cap * d : nullptr;
+    if (t == 0 || !fused) {
+      const int fb = std::min(ceil_div((long long)S * d, 256), 4096);
+      fill_keys_kernel<K><<<fb, 256, 0, st>>>(gmin, (long long)S * d, ~(K)0);
+      ANNF_CHECK_LAUNCH();
+      fill_keys_kernel<K><<<fb, 256, 0, st>>>(gmax, (long long)S * d, (K)0);
+      ANNF_CHECK_LAUNCH();
+      bbox_kernel<T><<<(unsigned)nblk, kThreads, 0, st>>>(n, d, t, B, cur_pts, gmin, gmax);
+      ANNF_CHECK_LAUNCH();
+    }
     axis_kernel<T><<<ceil_div(S, 128), 128, 0, st>>>(n, d, t, S, splitting, gmin, gmax, h->axis.as<int>(),
                                                    h->sel_prefix.as<K>(), h->sel_rank.as<int>(),
-                                                   h->sel_nlt.as<int>());
+                                                   h->sel_nlt.as<int>(), cmin, cmax);
     ANNF_CHECK_LAUNCH();
     constexpr int kBits = 8 * sizeof(K);
     for (int shift = kBits - 8; shift >= 0; shift -= 8) {
@@ -835,7 +929,8 @@ static int build_impl(annf_handle* h, const T* points, int n, int d, int depth, 
     ANNF_CHECK_LAUNCH();
     scatter_kernel<T><<<(unsigned)nblk, kThreads, 0, st>>>(
         n, d, t, B, h->keys.as<K>(), h->sel_prefix.as<K>(), h->sel_nlt.as<int>(), h->sel_neq.as<int>(),
-        h->blk_lt.as<int>(), h->blk_eq.as<int>(), cur_pts, cur_perm, alt_pts, alt_perm, h->eqpos.as<int>());
+        h->blk_lt.as<int>(), h->blk_eq.as<int>(), cur_pts, cur_perm, alt_pts, alt_perm, h->eqpos.as<int>(), cmin,
+        cmax);
     ANNF_CHECK_LAUNCH();
     fixup_kernel<T><<<ceil_div((long long)S * 32, 256), 256, 0, st>>>(
         n, d, t, S, h->axis.as<int>(), h->sel_nlt.as<int>(), h->sel_neq.as<int>(), h->eqpos.as<int>(),

@@ -89,8 +89,8 @@ class ANNFieldPropKDTreeGB300:
         an FP64 Rayleigh-Ritz step); None picks "exact" for the plain form, "subspace" otherwise;
         ``leaf_precision`` of the parallel form's natural-leaf distances: "bf16" (tensor-core tiles,
         exact FP32 re-rank of the survivors of a proven BF16 error bound; the default) or "fp32";
-        ``projection`` "exact" (the FP64 result rounded once, the reference's) or "bf16" (BF16
-        components on the tensor cores, FP32 sums); None picks "exact" for the plain form, "bf16"
+        ``projection`` "exact" (the FP64 result rounded once, the reference's) or "fp16" (FP16
+        components on the tensor cores, FP32 sums); None picks "exact" for the plain form, "fp16"
         otherwise when the shapes allow it; ``graph``: repeated fits with unchanged shapes and
         parameters replay one captured CUDA graph of the whole NNF ("auto": the parallel form;
         False: never; the plain form is never captured, its cuSOLVER eigensolver sizes its
@@ -298,12 +298,12 @@ class ANNFieldPropKDTreeGB300:
         self.patches_b_reduced_ = torch.empty((n_b, d), dtype=real, device=dev)
         proj = self.projection
         if proj is None:
-            proj = "bf16" if (self.form != "plain" and real == torch.float32 and p * p * c <= 256 and d <= 32) else "exact"
-        if proj == "bf16":
+            proj = "fp16" if (self.form != "plain" and real == torch.float32 and p * p * c <= 256 and d <= 32) else "exact"
+        if proj == "fp16":
             if real != torch.float32:
-                raise ValueError("the BF16 projection needs float_type='float'")
+                raise ValueError("the FP16 projection needs float_type='float'")
             for img, hh, ww, dst in ((A, ha, wa, self.patches_a_reduced_), (B, hb, wb, self.patches_b_reduced_)):
-                h.call("annf_project_bf16", ptr(img), hh, ww, c, p, ptr(self.components_), ptr(self.mean_), d,
+                h.call("annf_project_f16", ptr(img), hh, ww, c, p, ptr(self.components_), ptr(self.mean_), d,
                        ptr(dst), st)
         elif proj == "exact":
             h.call("annf_project", ptr(A), ha, wa, c, p, ptr(self.components_), ptr(self.mean_), d, real_type,
@@ -311,7 +311,7 @@ class ANNFieldPropKDTreeGB300:
             h.call("annf_project", ptr(B), hb, wb, c, p, ptr(self.components_), ptr(self.mean_), d, real_type,
                    ptr(self.patches_b_reduced_), st)
         else:
-            raise ValueError("projection must be 'exact' or 'bf16'")
+            raise ValueError("projection must be 'exact' or 'fp16'")
         ev["t2"].record()
 
         # (4) k-d tree over B (annfmp/openmp/base.py:95-103)

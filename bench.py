@@ -337,7 +337,7 @@ def run_gpu(args, w, rank, world, local_rank):
     ms = reduce_max(sum(s.elapsed_time(e) for s, e in ev) / args.steps, world, dev)
 
     # per-stage kernel times: the same form run eagerly with the library's stage marks
-    pm = make_model(args.form, args, prm, local_rank, graph=False) if graphed else model
+    pm = make_model(args.form, args, prm, local_rank, graph=False)
     pm.fit(A, B)
     h = pm.kdtree.handle
     h.profile(True)

@@ -148,11 +148,11 @@ int annf_project(annf_handle* h, const uint8_t* img, int hgt, int wid, int chann
                  void* out, void* stream);
 
 /* Approximate counterpart of annf_project for the approximate NNF forms (no reference
- * counterpart): the same patches times the components rounded to BF16, FP32 accumulation on the
+ * counterpart): the same patches times the components rounded to FP16, FP32 accumulation on the
  * tensor cores (tcgen05), minus the projected mean; out FP32 [(h-psize+1)*(w-psize+1)*n_components].
  * Needs psize*psize*channels <= 256 and n_components <= 32 (else ANNF_ERR_UNSUPPORTED). */
-int annf_project_bf16(annf_handle* h, const uint8_t* img, int hgt, int wid, int channels, int psize,
-                      const double* components, const double* mean, int n_components, float* out, void* stream);
+int annf_project_f16(annf_handle* h, const uint8_t* img, int hgt, int wid, int channels, int psize,
+                     const double* components, const double* mean, int n_components, float* out, void* stream);
 
 /* The parallel NNF form (an addition beside the reference's row-sequential method, which has no
  * counterpart for it): every pixel's natural-leaf k-list (leaf_precision ANNF_LEAF_EXACT: FP32

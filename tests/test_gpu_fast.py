@@ -111,16 +111,15 @@ def test_natural_knn_bf16_vs_fp32(gpu_lib, n, d, leaf, k, quant):
 
 
 # ---------------------------------------------------------------------------------------------
-# BF16 tensor-core projection vs the same arithmetic in float64
+# FP16 tensor-core projection vs the same arithmetic in float64
 # ---------------------------------------------------------------------------------------------
 @pytest.mark.parametrize("name", PIPES)
-def test_project_bf16_matches_bf16_components(gpu_lib, oracle_mod, golden, name):
-    """out = patches . bf16(components)^T - bf16(components) . mean: pixel values and BF16
+def test_project_f16_matches_f16_components(gpu_lib, oracle_mod, golden, name):
+    """out = patches . f16(components)^T - f16(components) . mean: pixel values and FP16
     products are exact, so only FP32 summation order separates the GPU from float64."""
     import torch
     from annfmp_gb300 import _lib
     from annfmp_gb300._torch import ptr, stream_ptr
-    from oracle import cnn as C
     z = golden(name)
     psize = int(z["params"][1])
     comps, mean = np.ascontiguousarray(z["components"]), z["mean"]
@@ -131,10 +130,10 @@ def test_project_bf16_matches_bf16_components(gpu_lib, oracle_mod, golden, name)
         # every argument tensor is held by a name until the call returns (a temporary's memory
         # could be handed to the next temporary by the caching allocator before the kernel runs)
         img_d, comps_d, mean_d = (torch.from_numpy(t).to(dev) for t in (img, comps, mean))
-        _lib.Handle(0).call("annf_project_bf16", ptr(img_d), h, w, c, psize, ptr(comps_d), ptr(mean_d),
+        _lib.Handle(0).call("annf_project_f16", ptr(img_d), h, w, c, psize, ptr(comps_d), ptr(mean_d),
                             comps.shape[0], ptr(out), stream_ptr(dev))
         torch.cuda.synchronize()
-        cb = C.bf16_round(comps.astype(np.float32)).astype(np.float64)
+        cb = comps.astype(np.float32).astype(np.float16).astype(np.float64)
         X = oracle_mod.extract_patches(img, psize).astype(np.float64)
         want = X @ cb.T - cb @ mean
         scale = X @ np.abs(cb).T + np.abs(cb) @ np.abs(mean)
@@ -143,12 +142,11 @@ def test_project_bf16_matches_bf16_components(gpu_lib, oracle_mod, golden, name)
 
 
 @pytest.mark.parametrize("h,w,psize", [(37, 53, 7), (41, 190, 9), (29, 133, 5)])
-def test_project_bf16_odd_pitch(gpu_lib, oracle_mod, h, w, psize):
+def test_project_f16_odd_pitch(gpu_lib, oracle_mod, h, w, psize):
     """Rows whose byte pitch is not a multiple of 4 (odd widths) and tiles narrower than 128."""
     import torch
     from annfmp_gb300 import _lib
     from annfmp_gb300._torch import ptr, stream_ptr
-    from oracle import cnn as C
     rng = np.random.default_rng(h * w)
     img = rng.integers(0, 256, (h, w, 3), dtype=np.uint8)
     P = psize * psize * 3
@@ -157,10 +155,10 @@ def test_project_bf16_odd_pitch(gpu_lib, oracle_mod, h, w, psize):
     dev = torch.device("cuda", 0)
     img_d, comps_d, mean_d = (torch.from_numpy(t).to(dev) for t in (img, comps, mean))
     out = torch.empty(((h - psize + 1) * (w - psize + 1), 12), dtype=torch.float32, device=dev)
-    _lib.Handle(0).call("annf_project_bf16", ptr(img_d), h, w, 3, psize, ptr(comps_d), ptr(mean_d), 12, ptr(out),
+    _lib.Handle(0).call("annf_project_f16", ptr(img_d), h, w, 3, psize, ptr(comps_d), ptr(mean_d), 12, ptr(out),
                         stream_ptr(dev))
     torch.cuda.synchronize()
-    cb = C.bf16_round(comps.astype(np.float32)).astype(np.float64)
+    cb = comps.astype(np.float32).astype(np.float16).astype(np.float64)
     X = oracle_mod.extract_patches(img, psize).astype(np.float64)
     want = X @ cb.T - cb @ mean
     scale = X @ np.abs(cb).T + np.abs(cb) @ np.abs(mean)
