@@ -626,9 +626,35 @@ __global__ void __launch_bounds__(kSubThreads) subtree_kernel(
   const int cnt = hi - lo;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 
-  for (long long e = threadIdx.x; e < (long long)cnt * d; e += blockDim.x) {
-    const int r = (int)(e / d), c = (int)(e - (long long)r * d);
-    spts[(size_t)r * ds + c] = pts_in[(long long)lo * d + e];
+  if (sizeof(T) == 4 && (d & 3) == 0) {
+    // 16-byte loads, eight in flight per thread, spread to the padded rows
+    const float4* src = reinterpret_cast<const float4*>(pts_in + (long long)lo * d);
+    const int nq = cnt * d / 4, qpr = d / 4;
+    for (int e0 = threadIdx.x; e0 < nq; e0 += 8 * kSubThreads) {
+      float4 v[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int e = e0 + u * kSubThreads;
+        if (e < nq) v[u] = __ldg(src + e);
+      }
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int e = e0 + u * kSubThreads;
+        if (e < nq) {
+          const int r = e / qpr, c = (e - r * qpr) * 4;
+          float* dst = reinterpret_cast<float*>(spts) + (size_t)r * ds + c;
+          dst[0] = v[u].x;
+          dst[1] = v[u].y;
+          dst[2] = v[u].z;
+          dst[3] = v[u].w;
+        }
+      }
+    }
+  } else {
+    for (long long e = threadIdx.x; e < (long long)cnt * d; e += blockDim.x) {
+      const int r = (int)(e / d), c = (int)(e - (long long)r * d);
+      spts[(size_t)r * ds + c] = pts_in[(long long)lo * d + e];
+    }
   }
   for (int i = threadIdx.x; i < cnt; i += blockDim.x) {
     sperm[i] = perm_in[lo + i];
@@ -723,26 +749,47 @@ __global__ void __launch_bounds__(kSubThreads) subtree_kernel(
       unsigned* ghist = shist + u * 512;
       for (int z = gw * 32 + lane; z < 512; z += G * 32) ghist[z] = 0;
       __syncthreads();
-      if (gw == 0 && lane == 0) {
+      if (gw == 0) {
+        // lanes take dimensions (lane, lane + 32, ...): the widest, first on ties, as one scan
         T best = 0;
         int axis = splitting == 0 ? l % d : 0;
-        for (int j = 0; splitting != 0 && j < d; ++j) {
-          T mn = spmn[w0 * d + j], mx = spmx[w0 * d + j];
-          for (int g = 1; g < G; ++g) {
-            const T omn = spmn[(w0 + g) * d + j], omx = spmx[(w0 + g) * d + j];
-            mn = omn < mn ? omn : mn;
-            mx = omx > mx ? omx : mx;
-          }
-          const T wd = real_traits<T>::sub(mx, mn);
-          if (wd > best) {
-            best = wd;
-            axis = j;
+        if (splitting != 0) {
+          for (int j0 = 0; j0 < d; j0 += 32) {
+            const int j = j0 + lane;
+            T wd = -real_traits<T>::big();
+            if (j < d) {
+              T mn = spmn[w0 * d + j], mx = spmx[w0 * d + j];
+              for (int g = 1; g < G; ++g) {
+                const T omn = spmn[(w0 + g) * d + j], omx = spmx[(w0 + g) * d + j];
+                mn = omn < mn ? omn : mn;
+                mx = omx > mx ? omx : mx;
+              }
+              wd = real_traits<T>::sub(mx, mn);
+            }
+            // the chunk's widest (lowest dimension on ties), then the serial rule across chunks
+            T bw = wd;
+            int bj = j;
+#pragma unroll
+            for (int o = 16; o; o >>= 1) {
+              const T ow = __shfl_xor_sync(0xffffffffu, bw, o);
+              const int oj = __shfl_xor_sync(0xffffffffu, bj, o);
+              if (ow > bw || (ow == bw && oj < bj)) {
+                bw = ow;
+                bj = oj;
+              }
+            }
+            if (bw > best) {
+              best = bw;
+              axis = bj;
+            }
           }
         }
-        saxis[u] = axis;
-        sprefix[u] = 0;
-        srank[u] = half;
-        snlt[u] = 0;
+        if (lane == 0) {
+          saxis[u] = axis;
+          sprefix[u] = 0;
+          srank[u] = half;
+          snlt[u] = 0;
+        }
       }
       __syncthreads();
       const int axis = saxis[u];
@@ -805,9 +852,19 @@ __global__ void __launch_bounds__(kSubThreads) subtree_kernel(
     }
     for (int i = a + lane; i < b; i += 32) point_leaf[sperm[cur[i]]] = leaf;
   }
-  for (long long e = threadIdx.x; e < (long long)cnt * d; e += blockDim.x) {
-    const int r = (int)(e / d), c = (int)(e - (long long)r * d);
-    pts_out[(long long)(lo + r) * d + c] = spts[(size_t)cur[r] * ds + c];
+  if (sizeof(T) == 4 && (d & 3) == 0) {
+    float4* dst = reinterpret_cast<float4*>(pts_out + (long long)lo * d);
+    const int nq = cnt * d / 4, qpr = d / 4;
+    for (int e = threadIdx.x; e < nq; e += kSubThreads) {
+      const int r = e / qpr, c = (e - r * qpr) * 4;
+      const float* sp = reinterpret_cast<const float*>(spts) + (size_t)cur[r] * ds + c;
+      dst[e] = make_float4(sp[0], sp[1], sp[2], sp[3]);
+    }
+  } else {
+    for (long long e = threadIdx.x; e < (long long)cnt * d; e += blockDim.x) {
+      const int r = (int)(e / d), c = (int)(e - (long long)r * d);
+      pts_out[(long long)(lo + r) * d + c] = spts[(size_t)cur[r] * ds + c];
+    }
   }
   for (int i = threadIdx.x; i < cnt; i += blockDim.x) perm_out[lo + i] = sperm[cur[i]];
 }
