@@ -185,6 +185,7 @@ static int check_k(const annf_handle* h, int k, long long max_leaves) {
 int annf_kneighbors(annf_handle* h, const void* queries, int nq, int k, long long max_leaves, void* distances,
                     int* indices, void* stream) {
   ANNF_API_HANDLE(h);
+  ANNF_REQUIRE(ANNF_ALIGNED(queries, 16), "annf_kneighbors: queries must be 16-byte aligned");
   int rc = check_k(h, k, max_leaves);
   if (rc != ANNF_OK) return rc;
   ANNF_REQUIRE(nq >= 0, "annf_kneighbors: nq < 0");
@@ -207,6 +208,8 @@ int annf_process_rows(annf_handle* h, int* final_idx, const uint8_t* patches_a, 
                       int n_b, int P, const void* ared, int n_rows, int n_cols, int k, int propagate,
                       int select_best, long long max_leaves, int* knn_out, float* dist_out, void* stream) {
   ANNF_API_HANDLE(h);
+  ANNF_REQUIRE(ANNF_ALIGNED(patches_a, 4) && ANNF_ALIGNED(patches_b, 4) && ANNF_ALIGNED(ared, 16),
+               "annf_process_rows: patch arrays must be 4-byte and reduced patches 16-byte aligned");
   int rc = rows_common_checks(h, final_idx, ared, n_rows, n_cols, k, max_leaves);
   if (rc != ANNF_OK) return rc;
   if (select_best) {
@@ -214,7 +217,7 @@ int annf_process_rows(annf_handle* h, int* final_idx, const uint8_t* patches_a, 
     ANNF_REQUIRE(n_a == n_rows * n_cols, "annf_process_rows: patches_a must have n_rows*n_cols rows");
     ANNF_REQUIRE(n_b == h->n, "annf_process_rows: patches_b must have one row per tree point");
   }
-  PatchSrc A{patches_a, 0, P, 1, 0, false}, B{patches_b, 0, P, 1, 0, false};
+  PatchSrc A{patches_a, 0, P, 1, 0, false, (long long)n_a * P}, B{patches_b, 0, P, 1, 0, false, (long long)n_b * P};
   return process_rows_generic(h, final_idx, A, B, ared, n_rows, n_cols, k, propagate, select_best, max_leaves,
                               knn_out, dist_out, static_cast<cudaStream_t>(stream));
 }
@@ -224,6 +227,8 @@ int annf_process_rows_img(annf_handle* h, int* final_idx, const uint8_t* img_a, 
                           int propagate, int select_best, long long max_leaves, int* knn_out, float* dist_out,
                           void* stream) {
   ANNF_API_HANDLE(h);
+  ANNF_REQUIRE(ANNF_ALIGNED(img_a, 4) && ANNF_ALIGNED(img_b, 4) && ANNF_ALIGNED(ared, 16),
+               "annf_process_rows_img: images must be 4-byte and reduced patches 16-byte aligned");
   int rc = rows_common_checks(h, final_idx, ared, n_rows, n_cols, k, max_leaves);
   if (rc != ANNF_OK) return rc;
   if (select_best) {
@@ -233,8 +238,8 @@ int annf_process_rows_img(annf_handle* h, int* final_idx, const uint8_t* img_a, 
     ANNF_REQUIRE((long long)(hb - psize + 1) * (wb - psize + 1) == h->n,
                  "annf_process_rows_img: the tree must hold every patch of image B");
   }
-  PatchSrc A{img_a, wa, channels, psize, wa - psize + 1, true};
-  PatchSrc B{img_b, wb, channels, psize, wb - psize + 1, true};
+  PatchSrc A{img_a, wa, channels, psize, wa - psize + 1, true, (long long)ha * wa * channels};
+  PatchSrc B{img_b, wb, channels, psize, wb - psize + 1, true, (long long)hb * wb * channels};
   return process_rows_generic(h, final_idx, A, B, ared, n_rows, n_cols, k, propagate, select_best, max_leaves,
                               knn_out, dist_out, static_cast<cudaStream_t>(stream));
 }
@@ -294,6 +299,7 @@ int annf_device_status(annf_handle* h, void* stream, unsigned* bits_out) {
 int annf_kneighbors_noalloc(annf_handle* h, const void* queries, int nq, int k, long long max_leaves, void* distances,
                             int* indices, void* stream) {
   ANNF_API_HANDLE(h);
+  ANNF_REQUIRE(ANNF_ALIGNED(queries, 16), "annf_kneighbors_noalloc: queries must be 16-byte aligned");
   int rc = check_k(h, k, max_leaves);
   if (rc != ANNF_OK) return rc;
   ANNF_REQUIRE(nq >= 0, "annf_kneighbors_noalloc: nq < 0");
@@ -307,6 +313,8 @@ int annf_parallel_nnf(annf_handle* h, int* final_idx, const uint8_t* img_a, int 
                       int n_prop, int iters, unsigned seed, int leaf_precision, int rand_samples, int radius0,
                       float* dist_out, void* stream) {
   ANNF_API_HANDLE(h);
+  ANNF_REQUIRE(ANNF_ALIGNED(img_a, 16) && ANNF_ALIGNED(img_b, 16) && ANNF_ALIGNED(ared, 16),
+               "annf_parallel_nnf: images and reduced patches must be 16-byte aligned");
   int rc = check_k(h, k, 2147483640);
   if (rc != ANNF_OK) return rc;
   ANNF_REQUIRE(final_idx && img_a && img_b && ared, "annf_parallel_nnf: NULL argument");
@@ -341,6 +349,7 @@ int annf_parallel_nnf(annf_handle* h, int* final_idx, const uint8_t* img_a, int 
 int annf_raw_nn(annf_handle* h, const uint8_t* img_a, int ha, int wa, const uint8_t* img_b, int hb, int wb,
                 int channels, int psize, const int* query_pixels, int nq, unsigned long long* best, void* stream) {
   ANNF_API_HANDLE(h);
+  ANNF_REQUIRE(ANNF_ALIGNED(img_a, 4) && ANNF_ALIGNED(img_b, 4), "annf_raw_nn: images must be 4-byte aligned");
   ANNF_REQUIRE(img_a && img_b && (nq == 0 || (query_pixels && best)), "annf_raw_nn: NULL argument");
   ANNF_REQUIRE(channels >= 1 && psize >= 1 && psize <= ha && psize <= wa && psize <= hb && psize <= wb,
                "annf_raw_nn: bad geometry");
@@ -352,6 +361,7 @@ int annf_raw_nn(annf_handle* h, const uint8_t* img_a, int ha, int wa, const uint
 int annf_project_f16(annf_handle* h, const uint8_t* img, int hgt, int wid, int channels, int psize,
                       const double* components, const double* mean, int n_components, float* out, void* stream) {
   ANNF_API_HANDLE(h);
+  ANNF_REQUIRE(ANNF_ALIGNED(img, 4), "annf_project_f16: the image must be 4-byte aligned");
   ANNF_REQUIRE(img && components && mean && out, "annf_project_f16: NULL argument");
   ANNF_REQUIRE(channels >= 1 && psize >= 1 && psize <= hgt && psize <= wid, "annf_project_f16: bad geometry");
   if (!project_tc_supported(psize, channels, n_components)) {
@@ -365,6 +375,7 @@ int annf_project_f16(annf_handle* h, const uint8_t* img, int hgt, int wid, int c
 int annf_natural_knn(annf_handle* h, const void* queries, long long nq, int k, int leaf_precision, int* out_pos,
                      void* stream) {
   ANNF_API_HANDLE(h);
+  ANNF_REQUIRE(ANNF_ALIGNED(queries, 16), "annf_natural_knn: queries must be 16-byte aligned");
   int rc = check_k(h, k, 2147483640);
   if (rc != ANNF_OK) return rc;
   ANNF_REQUIRE(nq >= 0, "annf_natural_knn: nq < 0");
@@ -385,6 +396,7 @@ int annf_natural_knn(annf_handle* h, const void* queries, long long nq, int k, i
 
 int annf_tc_tile(annf_handle* h, const uint16_t* a, const uint16_t* b, int n, int kdim, float* d, void* stream) {
   ANNF_API_HANDLE(h);
+  ANNF_REQUIRE(ANNF_ALIGNED(a, 16) && ANNF_ALIGNED(b, 16), "annf_tc_tile: a and b must be 16-byte aligned");
   ANNF_REQUIRE(a && b && d, "annf_tc_tile: NULL argument");
   return tc_tile(a, b, n, kdim, d, h->status.as<unsigned>(), static_cast<cudaStream_t>(stream));
 }
@@ -424,6 +436,7 @@ int annf_cnn_prep_weights_tc(annf_handle* h, const float* w, int co, int ci, uin
 int annf_cnn_conv_forward_tc(annf_handle* h, const void* x, int nimg, int hgt, int wid, int ci, int co,
                              const uint16_t* w_tc, const float* bias, int relu, void* y, void* stream) {
   ANNF_API_HANDLE(h);
+  ANNF_REQUIRE(ANNF_ALIGNED(x, 16) && ANNF_ALIGNED(w_tc, 16), "annf_cnn_conv_forward_tc: x and w_tc must be 16-byte aligned");
   ANNF_REQUIRE(x && w_tc && bias && y, "annf_cnn_conv_forward_tc: NULL argument");
   ANNF_CNN_DIMS(nimg, hgt, wid);
   return cnn_conv_forward_tc(x, nimg, hgt, wid, ci, co, w_tc, bias, relu, y, h->status.as<unsigned>(),

@@ -38,6 +38,10 @@ void count_launch();
     }                                                                                        \
   } while (0)
 
+// device buffers that kernels read with 4- or 16-byte loads must start on such a boundary
+// (cudaMalloc and torch return 256-byte aligned memory)
+#define ANNF_ALIGNED(ptr, a) ((reinterpret_cast<uintptr_t>(ptr) & ((uintptr_t)(a) - 1)) == 0)
+
 #define ANNF_REQUIRE(cond, msg)                                                              \
   do {                                                                                       \
     if (!(cond)) {                                                                           \
@@ -178,6 +182,7 @@ struct PatchSrc {
   const uint8_t* img;  // image (HxWxC) or patch array ([n*P])
   int w, c, psize, ncols;
   bool is_img;
+  long long bytes;     // size of the buffer: no load reaches past it
   __device__ __forceinline__ const uint8_t* row(long long idx, int r) const {
     if (is_img) {
       const long long y = idx / ncols, x = idx - y * ncols;
@@ -186,6 +191,22 @@ struct PatchSrc {
     return img + idx * (long long)psize * psize * c + (long long)r * psize * c;
   }
 };
+
+// bytes [off, off + 4) of a buffer of nbytes bytes (4-byte aligned base), through aligned 32-bit
+// loads; within 8 bytes of the end, byte loads (bytes at or past nbytes read as zero)
+__device__ __forceinline__ unsigned load_word_bounded(const uint8_t* base, long long off, long long nbytes) {
+  const long long a = off & ~3LL;
+  const int sh = (int)(off & 3) * 8;
+  if (a + 8 <= nbytes) {
+    const unsigned* w = reinterpret_cast<const unsigned*>(base + a);
+    const unsigned lo = __ldg(w);
+    return sh ? __funnelshift_r(lo, __ldg(w + 1), sh) : lo;
+  }
+  unsigned v = 0;
+  for (int u = 0; u < 4; ++u)
+    if (off + u < nbytes) v |= (unsigned)__ldg(base + off + u) << (8 * u);
+  return v;
+}
 
 inline int ceil_div(long long a, long long b) { return (int)((a + b - 1) / b); }
 

@@ -19,18 +19,13 @@ int num_sms();
 // ---------------------------------------------------------------------------------------------
 // exact integer SSD between two psize x psize x c patches of two images (rows padded reads)
 // ---------------------------------------------------------------------------------------------
-__device__ __forceinline__ unsigned ldw_at(const uint8_t* base, long long off) {
-  const unsigned* w = reinterpret_cast<const unsigned*>(base + (off & ~3LL));
-  const int sh = (int)(off & 3) * 8;
-  const unsigned lo = __ldg(w);
-  return sh ? __funnelshift_r(lo, __ldg(w + 1), sh) : lo;
-}
-
 struct Img {
   const uint8_t* p;
   int h, w, c, psize, ncols;  // ncols = w - psize + 1
   long long bytes;            // h * w * c
 };
+
+__device__ __forceinline__ unsigned ldw_at(const Img& I, long long off) { return load_word_bounded(I.p, off, I.bytes); }
 
 __device__ __forceinline__ int patch_ssd(const Img& A, int ay, int ax, const Img& B, int by, int bx) {
   const int rowlen = A.psize * A.c;
@@ -39,7 +34,7 @@ __device__ __forceinline__ int patch_ssd(const Img& A, int ay, int ax, const Img
     const long long ao = ((long long)(ay + r) * A.w + ax) * A.c, bo = ((long long)(by + r) * B.w + bx) * B.c;
     int e = 0;
     for (; e + 4 <= rowlen; e += 4) {
-      const unsigned x = __vabsdiffu4(ldw_at(A.p, ao + e), ldw_at(B.p, bo + e));
+      const unsigned x = __vabsdiffu4(ldw_at(A, ao + e), ldw_at(B, bo + e));
       s = (int)__dp4a(x, x, (unsigned)s);
     }
     for (; e < rowlen; ++e) {
@@ -75,7 +70,7 @@ __global__ void __launch_bounds__(256) raw_nn_kernel(Img A, Img B, const int* __
       const int r = w / wpr, wi = w - r * wpr;
       const long long off = ((long long)(y + r) * A.w + x) * A.c + wi * 4;
       const int valid = min(4, rowlen - wi * 4);
-      v = ldw_at(A.p, off);
+      v = ldw_at(A, off);
       if (valid < 4) v &= (1u << (8 * valid)) - 1u;
     }
     sq[qi][w] = v;
@@ -96,7 +91,7 @@ __global__ void __launch_bounds__(256) raw_nn_kernel(Img A, Img B, const int* __
       if (NW == 0 && w >= nw) break;
       const int r = w / wpr, wi = w - r * wpr;
       const int valid = min(4, rowlen - wi * 4);
-      unsigned v = ldw_at(B.p, ((long long)(by + r) * B.w + bx) * B.c + wi * 4);
+      unsigned v = ldw_at(B, ((long long)(by + r) * B.w + bx) * B.c + wi * 4);
       if (valid < 4) v &= (1u << (8 * valid)) - 1u;
       bw[w] = v;
     }

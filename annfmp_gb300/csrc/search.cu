@@ -915,22 +915,14 @@ __global__ void __launch_bounds__(128, 1) chain_sel_kernel(TreeView<float> tv, c
 // ---------------------------------------------------------------------------------------------
 // tree positions -> original indices, and the raw-patch re-rank (base.c:309-353, 362-374)
 // ---------------------------------------------------------------------------------------------
-// bytes [off, off+4) of a byte stream read through aligned 32-bit loads
-__device__ __forceinline__ unsigned load_word_at(const uint8_t* base, long long off) {
-  const unsigned* w = reinterpret_cast<const unsigned*>(base + (off & ~3LL));
-  const int sh = (int)(off & 3) * 8;
-  const unsigned lo = __ldg(w);
-  if (!sh) return lo;
-  return __funnelshift_r(lo, __ldg(w + 1), sh);
-}
-
-// sum over a row of n bytes of (a-b)^2, exact in int
-__device__ __forceinline__ int row_ssd(const uint8_t* abase, long long aoff, const uint8_t* bbase, long long boff,
-                                       int n) {
+// sum over a row of n bytes of (a-b)^2, exact in int (abytes / bbytes: the buffers' sizes)
+__device__ __forceinline__ int row_ssd(const uint8_t* abase, long long aoff, long long abytes, const uint8_t* bbase,
+                                       long long boff, long long bbytes, int n) {
   int s = 0;
   int e = 0;
   for (; e + 4 <= n; e += 4) {
-    const unsigned x = __vabsdiffu4(load_word_at(abase, aoff + e), load_word_at(bbase, boff + e));
+    const unsigned x =
+        __vabsdiffu4(load_word_bounded(abase, aoff + e, abytes), load_word_bounded(bbase, boff + e, bbytes));
     s = (int)__dp4a(x, x, (unsigned)s);
   }
   for (; e < n; ++e) {
@@ -948,7 +940,7 @@ __device__ __forceinline__ T patch_dist(const PatchSrc& A, long long ia, const P
     long long acc = 0;  // every partial sum is exact in the reference's accumulator
     for (int r = 0; r < A.psize; ++r) {
       const long long ao = A.row(ia, r) - A.img, bo = B.row(ib, r) - B.img;
-      acc += row_ssd(A.img, ao, B.img, bo, rowlen);
+      acc += row_ssd(A.img, ao, A.bytes, B.img, bo, B.bytes, rowlen);
     }
     return real_traits<T>::sqrt_((T)acc);
   } else {  // large patches: replay the reference's rounding of the running sum

@@ -6,7 +6,11 @@
  * array data are DEVICE pointers unless a parameter says "host"; the caller owns every input and
  * output buffer. A handle owns the device tree and its scratch memory and frees them in
  * annf_destroy. Calls are asynchronous on the given CUDA stream (NULL = legacy default stream);
- * a handle must not be used from two host threads at once.
+ * a handle must not be used from two host threads at once. Images and patch arrays must start on a
+ * 4-byte boundary, reduced-patch / query arrays on a 16-byte boundary, and the images of
+ * annf_parallel_nnf on a 16-byte boundary (cudaMalloc returns 256-byte aligned memory); a call
+ * whose pointers are not aligned returns ANNF_ERR_INVALID. No kernel reads past the end of a
+ * buffer.
  *
  * Every function returns ANNF_OK (0) or a negative status; annf_last_error() then describes the
  * failure (thread-local). The reference prints and calls exit() instead
