@@ -127,7 +127,7 @@ class ClockSampler:
 # ---------------------------------------------------------------------------------------------
 # algorithmic bytes per launch of each stage ("roofline")
 # ---------------------------------------------------------------------------------------------
-def stage_bytes(stage, w, n_a, n_b, depth, n_cols, it=1):
+def stage_bytes(stage, w, n_a, n_b, depth, n_cols, it=1, nrand=1, n_prop=0):
     d, k, P = w["dim_reduced"], w["n_neighbors"], w["psize"] ** 2 * 3
     ppl = n_b / float(1 << depth)
     rows_q = n_a - n_cols
@@ -135,10 +135,10 @@ def stage_bytes(stage, w, n_a, n_b, depth, n_cols, it=1):
         return rows_q * (4 * d + k * ppl * 4 * d + 8 * k + 12 * k + 4 * k)
     if stage == "natural_knn":  # query + node path + natural leaf + list out
         return n_a * (4 * d + 8 * depth + ppl * 4 * d + 4 * k)
-    if stage == "fast_init":  # k candidate positions + A patch + k B patches + match out
-        return n_a * (4 * k + (k + 1) * P + 8)
-    if stage == "fast_propagate":  # per pass: match in/out, 4 neighbour matches, A patch, 6 B patches
-        return n_a * (8 + 16 + 7 * P + 8) * max(it, 1)
+    if stage == "fast_init":  # k candidate positions + proposals + A patch + k + n_prop B patches + match out
+        return n_a * (4 * k + 4 * n_prop + (k + n_prop + 1) * P + 8)
+    if stage == "fast_propagate":  # per pass: match in/out, 4 neighbour matches, A patch, 4 + nrand B patches
+        return n_a * (8 + 16 + (5 + nrand) * P + 8) * max(it, 1)
     if stage == "select_best":  # k A/B patch pairs + list in + index/distance out
         return n_a * (k * 2 * P + 4 * k + 8)
     if stage == "first_row":  # every point once per 128-query tile
@@ -374,7 +374,8 @@ def run_gpu(args, w, rank, world, local_rank):
     kernel_stages = {k: v for k, v in stage_ms.items() if not k.endswith(":begin")}
     depth = pm.kdtree.final_tree_depth_
     peak, peak_kind = load_peaks()
-    sb = lambda k: stage_bytes(k, w, n_a, n_b, depth, n_cols, args.iters)  # noqa: E731
+    n_prop = 4 if getattr(pm, "proposal", None) is not None else 0
+    sb = lambda k: stage_bytes(k, w, n_a, n_b, depth, n_cols, args.iters, pm.search[0], n_prop)  # noqa: E731
     dom = max((k for k in kernel_stages if sb(k)), key=lambda k: kernel_stages[k])
     by = sb(dom)
     # distance error of the last timed NNF against the exact raw-patch nearest neighbour
