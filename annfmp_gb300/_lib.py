@@ -52,6 +52,7 @@ class TreeView(ctypes.Structure):
         ("n_leaves", ctypes.c_int),
         ("points", ctypes.c_void_p), ("perm", ctypes.c_void_p), ("node_axis", ctypes.c_void_p),
         ("node_split", ctypes.c_void_p), ("leaf_begin", ctypes.c_void_p), ("point_leaf", ctypes.c_void_p),
+        ("leaf_box", ctypes.c_void_p),
     ]
 
 
@@ -75,6 +76,9 @@ SIGNATURES = {
     "annf_device_status": (_i, [_vp, _vp, ctypes.POINTER(_u)]),
     "annf_parallel_nnf": (_i, [_vp, _vp, _vp, _i, _i, _vp, _i, _i, _i, _i, _vp, _i, _vp, _i, _i, _u, _i, _i, _i, _vp,
                                _vp]),
+    "annf_parallel_nnf_seeded": (_i, [_vp, _vp, _vp, _i, _i, _vp, _i, _i, _i, _i, _vp, _i, _vp, _i, _u, _i, _i, _i,
+                                      _vp, _vp]),
+    "annf_seed_matches": (_i, [_vp, _vp, _i, _i, _vp, _i, _i, _i, _i, _vp, _i, _vp, _vp]),
     "annf_tc_tile": (_i, [_vp, _vp, _vp, _i, _i, _vp, _vp]),
     "annf_natural_knn": (_i, [_vp, _vp, ctypes.c_longlong, _i, _i, _vp, _vp]),
     "annf_project_f16": (_i, [_vp, _vp, _i, _i, _i, _i, _vp, _vp, _i, _vp, _vp]),

@@ -30,8 +30,10 @@ int kneighbors_noalloc(annf_handle* h, const void* Q, int nq, int K, long long m
                        cudaStream_t st);
 int natural_knn_all(annf_handle* h, const void* Q, long long nq, int K, int* out_pos, cudaStream_t st);
 int fast_search(annf_handle* h, const uint8_t* img_a, int ha, int wa, const uint8_t* img_b, int hb, int wb, int c,
-                int psize, int K, const int* nat_pos, const int* prop, int n_prop, int iters, uint32_t seed,
-                int rand_samples, int radius0, int* final_idx, float* dist_out, cudaStream_t st);
+                int psize, int K, const int* nat_pos, const int* prop, int n_prop, const int* seed_match, int iters,
+                uint32_t seed, int rand_samples, int radius0, int* final_idx, float* dist_out, cudaStream_t st);
+int seed_matches(const uint8_t* img_a, int ha, int wa, const uint8_t* img_b, int hb, int wb, int c, int psize,
+                 const int* cand, int n_cand, int* seed_out, cudaStream_t st);
 bool leaf_tc_supported(const annf_handle* h, int K);
 int natural_knn_tc(annf_handle* h, const float* Q, long long nq, int K, int prec, int* out_pos, cudaStream_t st);
 int tc_tile(const uint16_t* A, const uint16_t* B, int N, int K, float* D, unsigned* status, cudaStream_t st);
@@ -159,6 +161,7 @@ int annf_tree_get(const annf_handle* h, annf_tree_view* out) {
   out->node_split = h->node_split.p;
   out->leaf_begin = h->leaf_begin.as<int>();
   out->point_leaf = h->point_leaf.as<int>();
+  out->leaf_box = h->leaf_box.p;
   return ANNF_OK;
 }
 
@@ -308,11 +311,10 @@ int annf_kneighbors_noalloc(annf_handle* h, const void* queries, int nq, int k, 
   return kneighbors_noalloc(h, queries, nq, k, max_leaves, distances, indices, static_cast<cudaStream_t>(stream));
 }
 
-int annf_parallel_nnf(annf_handle* h, int* final_idx, const uint8_t* img_a, int ha, int wa, const uint8_t* img_b,
-                      int hb, int wb, int channels, int psize, const void* ared, int k, const int* proposals,
-                      int n_prop, int iters, unsigned seed, int leaf_precision, int rand_samples, int radius0,
-                      float* dist_out, void* stream) {
-  ANNF_API_HANDLE(h);
+static int parallel_nnf_impl(annf_handle* h, int* final_idx, const uint8_t* img_a, int ha, int wa,
+                             const uint8_t* img_b, int hb, int wb, int channels, int psize, const void* ared, int k,
+                             const int* proposals, int n_prop, const int* seed_match, int iters, unsigned seed,
+                             int leaf_precision, int rand_samples, int radius0, float* dist_out, void* stream) {
   ANNF_REQUIRE(ANNF_ALIGNED(img_a, 16) && ANNF_ALIGNED(img_b, 16) && ANNF_ALIGNED(ared, 16),
                "annf_parallel_nnf: images and reduced patches must be 16-byte aligned");
   int rc = check_k(h, k, 2147483640);
@@ -343,7 +345,37 @@ int annf_parallel_nnf(annf_handle* h, int* final_idx, const uint8_t* img_a, int 
   if (rc != ANNF_OK) return rc;
   prof_mark(h, "natural_knn", st);
   return fast_search(h, img_a, ha, wa, img_b, hb, wb, channels, psize, k, h->fast_nat.as<int>(), proposals, n_prop,
-                     iters, seed, rand_samples, radius0, final_idx, dist_out, st);
+                     seed_match, iters, seed, rand_samples, radius0, final_idx, dist_out, st);
+}
+
+int annf_parallel_nnf(annf_handle* h, int* final_idx, const uint8_t* img_a, int ha, int wa, const uint8_t* img_b,
+                      int hb, int wb, int channels, int psize, const void* ared, int k, const int* proposals,
+                      int n_prop, int iters, unsigned seed, int leaf_precision, int rand_samples, int radius0,
+                      float* dist_out, void* stream) {
+  ANNF_API_HANDLE(h);
+  return parallel_nnf_impl(h, final_idx, img_a, ha, wa, img_b, hb, wb, channels, psize, ared, k, proposals, n_prop,
+                           nullptr, iters, seed, leaf_precision, rand_samples, radius0, dist_out, stream);
+}
+
+int annf_parallel_nnf_seeded(annf_handle* h, int* final_idx, const uint8_t* img_a, int ha, int wa,
+                             const uint8_t* img_b, int hb, int wb, int channels, int psize, const void* ared, int k,
+                             const int* seed_match, int iters, unsigned seed, int leaf_precision, int rand_samples,
+                             int radius0, float* dist_out, void* stream) {
+  ANNF_API_HANDLE(h);
+  ANNF_REQUIRE(seed_match, "annf_parallel_nnf_seeded: NULL seed");
+  return parallel_nnf_impl(h, final_idx, img_a, ha, wa, img_b, hb, wb, channels, psize, ared, k, nullptr, 0,
+                           seed_match, iters, seed, leaf_precision, rand_samples, radius0, dist_out, stream);
+}
+
+int annf_seed_matches(annf_handle* h, const uint8_t* img_a, int ha, int wa, const uint8_t* img_b, int hb, int wb,
+                      int channels, int psize, const int* candidates, int n_cand, int* seed_out, void* stream) {
+  ANNF_API_HANDLE(h);
+  ANNF_REQUIRE(img_a && img_b && seed_out && (n_cand == 0 || candidates), "annf_seed_matches: NULL argument");
+  ANNF_REQUIRE(ANNF_ALIGNED(img_a, 16) && ANNF_ALIGNED(img_b, 16), "annf_seed_matches: images must be 16-byte aligned");
+  ANNF_REQUIRE(channels >= 1 && psize >= 1 && psize <= ha && psize <= wa && psize <= hb && psize <= wb && n_cand >= 0,
+               "annf_seed_matches: bad geometry");
+  return seed_matches(img_a, ha, wa, img_b, hb, wb, channels, psize, candidates, n_cand, seed_out,
+                      static_cast<cudaStream_t>(stream));
 }
 
 int annf_raw_nn(annf_handle* h, const uint8_t* img_a, int ha, int wa, const uint8_t* img_b, int hb, int wb,

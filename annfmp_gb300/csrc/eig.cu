@@ -42,97 +42,141 @@ __device__ __forceinline__ uint32_t mix32(uint32_t x) {
   return x;
 }
 
-// Orthonormalise the b columns of Z (column-major [b][P], shared memory) in place by Cholesky-QR
-// after scaling every column to unit norm: in subspace iteration Z = C Q has nearly orthogonal
-// columns, so the scaled Gram matrix is close to the identity and FP32 Cholesky is stable. G and
-// Rinv are b x b shared scratch. A column whose pivot vanishes is replaced by a basis vector.
-__device__ void cholqr_columns(float* Z, int P, int b, float* G) {
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-  for (int j = warp; j < b; j += nw) {  // unit columns
-    float* z = Z + (size_t)j * P;
+// Orthonormalise the B columns of Z ([P][B] row-major, shared memory) by Cholesky-QR, writing Q
+// ([P][B]): every column is scaled to unit norm first (in subspace iteration Z = C Q has nearly
+// orthogonal columns, so the scaled Gram matrix is close to the identity and FP32 Cholesky is
+// stable), R^-1 is formed explicitly by one warp, and Q = Z D R^-1 is a small product that all
+// threads share (no per-row dependent chains). A column whose norm vanishes is replaced by a
+// basis vector. G, Ri: B x B shared scratch; d: B shared column scales.
+template <int B>
+__device__ void cholqr_rows(float* Z, float* Q, int P, float* G, float* Ri, float* d) {
+  const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5;
+  // column norms; vanishing columns become basis vectors
+  for (int j = warp; j < B; j += nt >> 5) {
     float sq = 0.f;
-    for (int i = lane; i < P; i += 32) sq = fmaf(z[i], z[i], sq);
+    for (int i = lane; i < P; i += 32) sq = fmaf(Z[i * B + j], Z[i * B + j], sq);
     sq = warp_sum_f(sq);
-    const float inv = sq > 1e-30f ? rsqrtf(sq) : 0.f;
-    for (int i = lane; i < P; i += 32) z[i] = inv > 0.f ? z[i] * inv : (i == (j * 7 + 3) % P ? 1.f : 0.f);
+    if (!(sq > 1e-30f)) {
+      for (int i = lane; i < P; i += 32) Z[i * B + j] = i == (j * 7 + 3) % P ? 1.f : 0.f;
+      sq = 1.f;
+    }
+    if (lane == 0) d[j] = rsqrtf(sq);
   }
   __syncthreads();
-  for (int e = warp; e < b * b; e += nw) {  // Gram matrix (upper triangle), one warp per entry
-    const int r = e / b, c = e - r * b;
+  // scaled Gram matrix (upper triangle), one thread per entry
+  for (int e = tid; e < B * B; e += nt) {
+    const int r = e / B, c = e - r * B;
     if (c < r) continue;
-    const float* zr = Z + (size_t)r * P;
-    const float* zc = Z + (size_t)c * P;
-    float s = 0.f;
-    for (int i = lane; i < P; i += 32) s = fmaf(zr[i], zc[i], s);
-    s = warp_sum_f(s);
-    if (lane == 0) G[r * b + c] = s;
+    float g = 0.f;
+    for (int i = 0; i < P; ++i) g = fmaf(Z[i * B + r], Z[i * B + c], g);
+    G[e] = g * d[r] * d[c];
   }
   __syncthreads();
-  if (warp == 0) {  // Cholesky G = R^T R (upper R in place), lanes over columns
-    for (int k = 0; k < b; ++k) {
-      float piv = G[k * b + k];
+  if (warp == 0) {
+    // Cholesky G = R^T R (upper R in place), lanes over columns
+    for (int k = 0; k < B; ++k) {
+      const float piv = G[k * B + k];
       const float r = piv > 1e-12f ? sqrtf(piv) : 0.f;
       __syncwarp();
-      for (int j = k + lane; j < b; j += 32) G[k * b + j] = r > 0.f ? (j == k ? r : G[k * b + j] / r) : (j == k ? 1.f : 0.f);
+      for (int j = k + lane; j < B; j += 32) G[k * B + j] = r > 0.f ? (j == k ? r : G[k * B + j] / r) : (j == k ? 1.f : 0.f);
       __syncwarp();
-      for (int j = k + 1 + lane; j < b; j += 32) {
-        const float rkj = G[k * b + j];
-        for (int i = k + 1; i <= j; ++i) G[i * b + j] = fmaf(-G[k * b + i], rkj, G[i * b + j]);
+      for (int j = k + 1 + lane; j < B; j += 32) {
+        const float rkj = G[k * B + j];
+        for (int i = k + 1; i <= j; ++i) G[i * B + j] = fmaf(-G[k * B + i], rkj, G[i * B + j]);
       }
       __syncwarp();
     }
+    // R^-1 (upper), lanes over columns: back substitution of R x = e_j
+    for (int j = lane; j < B; j += 32) {
+      for (int i = B - 1; i >= 0; --i) {
+        float v = i == j ? 1.f : 0.f;
+        if (i > j) {
+          Ri[i * B + j] = 0.f;
+          continue;
+        }
+        for (int t = i + 1; t <= j; ++t) v = fmaf(-G[i * B + t], Ri[t * B + j], v);
+        Ri[i * B + j] = v / G[i * B + i];
+      }
+    }
   }
   __syncthreads();
-  for (int i = threadIdx.x; i < P; i += blockDim.x) {  // each row: q R = z (forward substitution)
-    for (int j = 0; j < b; ++j) {
-      float v = Z[(size_t)j * P + i];
-      for (int t = 0; t < j; ++t) v = fmaf(-Z[(size_t)t * P + i], G[t * b + j], v);
-      Z[(size_t)j * P + i] = v / G[j * b + j];
-    }
+  // Q = Z D R^-1 (R^-1 upper: column j uses t <= j)
+  for (int e = tid; e < P * B; e += nt) {
+    const int i = e / B, j = e - i * B;
+    float q = 0.f;
+    for (int t = 0; t <= j; ++t) q = fmaf(Z[i * B + t] * d[t], Ri[t * B + j], q);
+    Q[e] = q;
   }
   __syncthreads();
 }
 
-// step 1: one CTA. C32 is scratch [P*P]; Qout [b][P] FP32.
-__global__ void __launch_bounds__(kSubThreads) subspace_iter_kernel(const double* __restrict__ C, int P, int b,
+// step 1: one CTA. Z = C Q in FP32 with C (FP32 copy C32, global) read once per step: item
+// (i, s) accumulates row i over the s-th of KS slices of k into registers, the KS partial rows
+// are summed in a fixed order (deterministic), then Cholesky-QR. Qout [B][P] FP32.
+template <int B>
+__global__ void __launch_bounds__(kSubThreads) subspace_iter_kernel(const double* __restrict__ C, int P, int KS,
                                                                     int iters, float* C32, float* __restrict__ Qout,
                                                                     unsigned* status) {
   extern __shared__ __align__(16) float sm[];
-  float* Q = sm;
-  float* Z = sm + (size_t)b * P;
-  float* G = Z + (size_t)b * P;  // [b][b]
-  if (smem_overrun(sm, G + (size_t)b * b, status)) return;
-  for (long long e = threadIdx.x; e < (long long)P * P; e += blockDim.x) C32[e] = (float)C[e];
-  for (int e = threadIdx.x; e < b * P; e += blockDim.x)
-    Q[e] = (float)(mix32((uint32_t)e * 2654435761u + 12345u) >> 8) * (1.0f / 16777216.0f) - 0.5f;
+  float* Q = sm;                        // [P][B]
+  float* Z = Q + (size_t)P * B;         // [P][B]
+  float* part = Z + (size_t)P * B;      // [KS][P][B]
+  float* G = part + (size_t)KS * P * B;  // [B][B]
+  float* Ri = G + B * B;                 // [B][B]
+  float* dsc = Ri + B * B;               // [B]
+  if (smem_overrun(sm, dsc + B, status)) return;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  for (long long e = tid; e < (long long)P * P; e += nt) C32[e] = (float)C[e];
+  for (int e = tid; e < B * P; e += nt) {
+    const int i = e / B, j = e - i * B;
+    Z[e] = (float)(mix32((uint32_t)(j * P + i) * 2654435761u + 12345u) >> 8) * (1.0f / 16777216.0f) - 0.5f;
+  }
   __syncthreads();
-  cholqr_columns(Q, P, b, G);
-  const int groups = b >> 3;
+  cholqr_rows<B>(Z, Q, P, G, Ri, dsc);
+  const int kper = (P + KS - 1) / KS;
   for (int it = 0; it < iters; ++it) {
-    // Z = C Q (C symmetric: row i of C read as column i, coalesced across i)
-    for (int item = threadIdx.x; item < groups * P; item += blockDim.x) {
-      const int g = item / P, i = item - g * P;
-      float acc[8];
+    __threadfence_block();
+    for (int item = tid; item < P * KS; item += nt) {
+      const int s = item / P, i = item - s * P;  // consecutive threads: consecutive rows i
+      const int k0 = s * kper, k1 = min(P, k0 + kper);
+      float acc[B];
 #pragma unroll
-      for (int c = 0; c < 8; ++c) acc[c] = 0.f;
-      const float* q = Q + (size_t)(g * 8) * P;
-#pragma unroll 8
-      for (int k = 0; k < P; ++k) {
-        const float cv = C32[(size_t)k * P + i];
+      for (int c = 0; c < B; ++c) acc[c] = 0.f;
+#pragma unroll 4
+      for (int k = k0; k < k1; ++k) {
+        const float cv = __ldcg(C32 + (size_t)k * P + i);  // C symmetric: row k read along i
+        const float4* q4 = reinterpret_cast<const float4*>(Q + (size_t)k * B);
 #pragma unroll
-        for (int c = 0; c < 8; ++c) acc[c] = fmaf(cv, q[(size_t)c * P + k], acc[c]);
+        for (int c4 = 0; c4 < B / 4; ++c4) {
+          const float4 q = q4[c4];
+          acc[4 * c4] = fmaf(cv, q.x, acc[4 * c4]);
+          acc[4 * c4 + 1] = fmaf(cv, q.y, acc[4 * c4 + 1]);
+          acc[4 * c4 + 2] = fmaf(cv, q.z, acc[4 * c4 + 2]);
+          acc[4 * c4 + 3] = fmaf(cv, q.w, acc[4 * c4 + 3]);
+        }
       }
+      float4* dst = reinterpret_cast<float4*>(part + ((size_t)s * P + i) * B);
 #pragma unroll
-      for (int c = 0; c < 8; ++c) Z[(size_t)(g * 8 + c) * P + i] = acc[c];
+      for (int c4 = 0; c4 < B / 4; ++c4)
+        dst[c4] = make_float4(acc[4 * c4], acc[4 * c4 + 1], acc[4 * c4 + 2], acc[4 * c4 + 3]);
     }
     __syncthreads();
-    cholqr_columns(Z, P, b, G);
-    float* t = Q;
-    Q = Z;
-    Z = t;
+    for (int e = tid; e < P * B; e += nt) {
+      float z = part[e];
+      for (int s = 1; s < KS; ++s) z += part[(size_t)s * P * B + e];
+      Z[e] = z;
+    }
+    __syncthreads();
+    cholqr_rows<B>(Z, Q, P, G, Ri, dsc);
   }
-  cholqr_columns(Q, P, b, G);  // second pass: orthogonal to working precision
-  for (int e = threadIdx.x; e < b * P; e += blockDim.x) Qout[e] = Q[e];
+  // second pass: orthogonal to working precision
+  for (int e = tid; e < P * B; e += nt) Z[e] = Q[e];
+  __syncthreads();
+  cholqr_rows<B>(Z, Q, P, G, Ri, dsc);
+  for (int e = tid; e < B * P; e += nt) {
+    const int j = e / P, i = e - j * P;
+    Qout[e] = Q[i * B + j];
+  }
 }
 
 // step 2a: W[j][i] = sum_k C[i][k] Q[j][k] in FP64, one warp per (j, i)
@@ -171,8 +215,107 @@ __global__ void rr_gram_kernel(int P, int b, const float* __restrict__ Q, const 
   if (lane == 0) (which == 0 ? G : T)[e] = s;
 }
 
+// Cyclic Jacobi on the symmetric m x m matrix T (row-major, shared), accumulating rotations into
+// V (T <- J^T T J, V <- V J), round-robin ordering: each round rotates M/2 disjoint pairs at once
+// (M = m rounded up to even; a pair with the phantom index M-1 >= m is skipped). Rotation angles
+// are computed by one thread per pair from the matrix before the round, then all row updates,
+// then all column updates (disjoint rotations commute). Sweeps stop once the off-diagonal square
+// sum is at most tol times the total. FP64: the rotation's tangent is computed in FP32 and cos by
+// Newton steps on rsqrt (exactly orthogonal in FP64; an FP32 angle leaves ~1e-7 of apq, removed
+// by the next sweep), so the loop has no FP64 division or square root.
+template <typename R>
+__device__ void jacobi_sweeps(R* T, R* V, int m, int max_sweeps, double tol, double* s_cs, double* s_sn, int* s_p,
+                              int* s_q, double* s_off, double* s_tot) {
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const int M = (m + 1) & ~1, half = M / 2;
+  for (int sweep = 0; sweep < max_sweeps && m > 1; ++sweep) {
+    if (tid < 32) {
+      double off = 0.0, tot = 0.0;
+      for (int e = tid; e < m * m; e += 32) {
+        const double v = (double)T[e] * (double)T[e];
+        tot += v;
+        if (e / m != e % m) off += v;
+      }
+      off = warp_sum_d(off);
+      tot = warp_sum_d(tot);
+      if (tid == 0) {
+        *s_off = off;
+        *s_tot = tot;
+      }
+    }
+    __syncthreads();
+    if (!(*s_off > tol * *s_tot)) break;
+    for (int round = 0; round < M - 1; ++round) {
+      if (tid < half) {
+        auto player = [&](int j) { return j == 0 ? 0 : 1 + (j - 1 + round) % (M - 1); };
+        int p = player(tid), q = player(M - 1 - tid);
+        if (p > q) {
+          const int t = p;
+          p = q;
+          q = t;
+        }
+        double cs = 1.0, sn = 0.0;
+        if (q < m) {
+          const R apq = T[p * m + q], app = T[p * m + p], aqq = T[q * m + q];
+          if (sizeof(R) == 8) {
+            if (fabs((double)apq) > 1e-300 && fabs((double)apq) * fabs((double)apq) > 1e-30 * fabs((double)app * aqq)) {
+              const float theta = (float)(((double)aqq - app) / (2.0 * apq));
+              const float tf = (theta >= 0.f ? 1.f : -1.f) / (fabsf(theta) + sqrtf(fmaf(theta, theta, 1.f)));
+              const double t = (double)tf, x = fma(t, t, 1.0);
+              double y = (double)rsqrtf((float)x);
+              y = y * fma(-0.5 * x, y * y, 1.5);
+              y = y * fma(-0.5 * x, y * y, 1.5);
+              cs = y;
+              sn = t * y;
+            }
+          } else {
+            const float fa = (float)apq;
+            if (fabsf(fa) > 1e-30f && fabsf(fa) * fabsf(fa) > 1e-14f * fabsf((float)app * (float)aqq)) {
+              const float theta = ((float)aqq - (float)app) / (2.f * fa);
+              const float t = (theta >= 0.f ? 1.f : -1.f) / (fabsf(theta) + sqrtf(fmaf(theta, theta, 1.f)));
+              const float c = rsqrtf(fmaf(t, t, 1.f));
+              cs = c;
+              sn = t * c;
+            }
+          }
+        }
+        s_p[tid] = p;
+        s_q[tid] = q < m ? q : -1;
+        s_cs[tid] = cs;
+        s_sn[tid] = sn;
+      }
+      __syncthreads();
+      for (int e = tid; e < half * m; e += nt) {  // rows p, q
+        const int i = e / m, k = e - i * m;
+        const int p = s_p[i], q = s_q[i];
+        if (q < 0 || s_sn[i] == 0.0) continue;
+        const R cs = (R)s_cs[i], sn = (R)s_sn[i];
+        const R tp = T[p * m + k], tq = T[q * m + k];
+        T[p * m + k] = cs * tp - sn * tq;
+        T[q * m + k] = sn * tp + cs * tq;
+      }
+      __syncthreads();
+      for (int e = tid; e < half * m; e += nt) {  // columns p, q and the eigenvectors
+        const int i = e / m, k = e - i * m;
+        const int p = s_p[i], q = s_q[i];
+        if (q < 0 || s_sn[i] == 0.0) continue;
+        const R cs = (R)s_cs[i], sn = (R)s_sn[i];
+        const R tp = T[k * m + p], tq = T[k * m + q];
+        T[k * m + p] = cs * tp - sn * tq;
+        T[k * m + q] = sn * tp + cs * tq;
+        const R vp = V[k * m + p], vq = V[k * m + q];
+        V[k * m + p] = cs * vp - sn * vq;
+        V[k * m + q] = sn * vp + cs * vq;
+      }
+      __syncthreads();
+    }
+  }
+}
+
 // step 3: one CTA, FP64. Writes X [ncomp][b] (coefficients of each component in the Q basis).
-__global__ void __launch_bounds__(256) rr_solve_kernel(int b, int ncomp, const double* __restrict__ Gg,
+constexpr int kRrThreads = 256;  // rr_solve_kernel's block: its register arrays assume it
+
+__global__ void __launch_bounds__(kRrThreads) rr_solve_kernel(int b, int ncomp, const double* __restrict__ Gg,
                                                        const double* __restrict__ Tg, double* __restrict__ Xout,
                                                        double* __restrict__ lambda_out) {
   __shared__ double G[kMaxBlock * kMaxBlock], T[kMaxBlock * kMaxBlock], V[kMaxBlock * kMaxBlock];
@@ -258,88 +401,94 @@ __global__ void __launch_bounds__(256) rr_solve_kernel(int b, int ncomp, const d
   __syncthreads();
   for (int e = tid; e < m * m; e += nt) V[e] = (e / m == e % m) ? 1.0 : 0.0;
   __syncthreads();
-  // parallel Jacobi, round-robin ordering: each round rotates M/2 disjoint pairs at once (M = m
-  // rounded up to even; a pair with the phantom index M-1 >= m is skipped). Rotation angles are
-  // computed by one thread per pair from the matrix before the round, then all row updates, then
-  // all column updates (disjoint rotations commute).
+  // Jacobi in two precisions. FP32 sweeps (cheap on this part) bring T to diagonal within FP32
+  // rounding; one Newton-Schulz step makes their eigenvectors orthonormal in FP64; M = V^T T V is
+  // then diagonal to ~1e-7 of its norm, and FP64 sweeps on M (quadratic convergence: one or two)
+  // finish the small eigenproblem in FP64, accumulating into V.
   __shared__ double s_cs[kMaxBlock / 2], s_sn[kMaxBlock / 2];
   __shared__ int s_p[kMaxBlock / 2], s_q[kMaxBlock / 2];
-  const int M = (m + 1) & ~1, half = M / 2;
-  for (int sweep = 0; sweep < 12 && m > 1; ++sweep) {
-    if (tid < 32) {
-      double off = 0.0, tot = 0.0;
-      for (int e = tid; e < m * m; e += 32) {
-        const double v = T[e] * T[e];
-        tot += v;
-        if (e / m != e % m) off += v;
-      }
-      off = warp_sum_d(off);
-      tot = warp_sum_d(tot);
-      if (tid == 0) {
-        s_off = off;
-        s_tot = tot;
+  float* V32 = reinterpret_cast<float*>(V);  // FP32 phase: V32 and T32 share V's storage
+  float* T32 = V32 + kMaxBlock * kMaxBlock;
+  for (int e = tid; e < m * m; e += nt) {
+    T32[e] = (float)T[e];
+    V32[e] = (e / m == e % m) ? 1.f : 0.f;
+  }
+  __syncthreads();
+  jacobi_sweeps<float>(T32, V32, m, 16, 1e-12, s_cs, s_sn, s_p, s_q, &s_off, &s_tot);
+  {  // V (FP64) <- V32: through registers, the two share storage
+    double v[(kMaxBlock * kMaxBlock + kRrThreads - 1) / kRrThreads];
+    int u = 0;
+    for (int e = tid; e < m * m; e += nt) v[u++] = (double)V32[e];
+    __syncthreads();
+    u = 0;
+    for (int e = tid; e < m * m; e += nt) V[e] = v[u++];
+  }
+  __syncthreads();
+  // Newton-Schulz: V <- V (3 I - V^T V) / 2, with T as scratch (T itself waits in registers;
+  // G holds R~ for the back-substitution at the end). The register arrays hold a thread's share
+  // of the m x m entries: at most kMaxBlock^2 / 256 with the 256-thread launch.
+  {
+    double tsave[(kMaxBlock * kMaxBlock + kRrThreads - 1) / kRrThreads];
+    int u = 0;
+    for (int e = tid; e < m * m; e += nt) tsave[u++] = T[e];
+    __syncthreads();
+    for (int e = tid; e < m * m; e += nt) {  // T <- W = V^T V
+      const int i = e / m, j = e - i * m;
+      double w = 0.0;
+      for (int k = 0; k < m; ++k) w = fma(V[k * m + i], V[k * m + j], w);
+      T[e] = (i == j ? 1.5 : 0.0) - 0.5 * w;
+    }
+    __syncthreads();
+    double vn[(kMaxBlock * kMaxBlock + kRrThreads - 1) / kRrThreads];
+    u = 0;
+    for (int e = tid; e < m * m; e += nt) {  // V (1.5 I - 0.5 W)
+      const int i = e / m, j = e - i * m;
+      double a = 0.0;
+      for (int k = 0; k < m; ++k) a = fma(V[i * m + k], T[k * m + j], a);
+      vn[u++] = a;
+    }
+    __syncthreads();
+    u = 0;
+    for (int e = tid; e < m * m; e += nt) {
+      V[e] = vn[u];
+      T[e] = tsave[u];
+      ++u;
+    }
+    __syncthreads();
+    // M = V^T T V: first Y = T V (into registers), then M = V^T Y
+    u = 0;
+    for (int e = tid; e < m * m; e += nt) {
+      const int i = e / m, j = e - i * m;
+      double a = 0.0;
+      for (int k = 0; k < m; ++k) a = fma(T[i * m + k], V[k * m + j], a);
+      vn[u++] = a;
+    }
+    __syncthreads();
+    u = 0;
+    for (int e = tid; e < m * m; e += nt) T[e] = vn[u++];  // T <- Y
+    __syncthreads();
+    u = 0;
+    for (int e = tid; e < m * m; e += nt) {
+      const int i = e / m, j = e - i * m;
+      double a = 0.0;
+      for (int k = 0; k < m; ++k) a = fma(V[k * m + i], T[k * m + j], a);
+      vn[u++] = a;
+    }
+    __syncthreads();
+    u = 0;
+    for (int e = tid; e < m * m; e += nt) T[e] = vn[u++];
+    __syncthreads();
+    for (int e = tid; e < m * m; e += nt) {  // symmetrise M
+      const int i = e / m, j = e - i * m;
+      if (i < j) {
+        const double a = 0.5 * (T[i * m + j] + T[j * m + i]);
+        T[i * m + j] = a;
+        T[j * m + i] = a;
       }
     }
     __syncthreads();
-    if (!(s_off > 1e-20 * s_tot)) break;
-    for (int round = 0; round < M - 1; ++round) {
-      if (tid < half) {
-        auto player = [&](int j) { return j == 0 ? 0 : 1 + (j - 1 + round) % (M - 1); };
-        int p = player(tid), q = player(M - 1 - tid);
-        if (p > q) {
-          const int t = p;
-          p = q;
-          q = t;
-        }
-        double cs = 1.0, sn = 0.0;
-        if (q < m) {
-          const double apq = T[p * m + q];
-          const double app = T[p * m + p], aqq = T[q * m + q];
-          if (fabs(apq) > 1e-300 && fabs(apq) * fabs(apq) > 1e-30 * fabs(app * aqq)) {
-            // tangent of the rotation angle in FP32 (the rotation stays exactly orthogonal in FP64;
-            // an FP32 angle leaves ~1e-7 of apq, removed by the next sweep), cos by one FP64
-            // Newton step on rsqrt, so the loop has no FP64 division or square root
-            const float theta = (float)((aqq - app) / (2.0 * apq));
-            const float tf = (theta >= 0.f ? 1.f : -1.f) / (fabsf(theta) + sqrtf(fmaf(theta, theta, 1.f)));
-            const double t = (double)tf, x = fma(t, t, 1.0);
-            double y = (double)rsqrtf((float)x);
-            y = y * fma(-0.5 * x, y * y, 1.5);
-            y = y * fma(-0.5 * x, y * y, 1.5);
-            cs = y;
-            sn = t * y;
-          }
-        }
-        s_p[tid] = p;
-        s_q[tid] = q < m ? q : -1;
-        s_cs[tid] = cs;
-        s_sn[tid] = sn;
-      }
-      __syncthreads();
-      for (int e = tid; e < half * m; e += nt) {  // rows p, q
-        const int i = e / m, k = e - i * m;
-        const int p = s_p[i], q = s_q[i];
-        if (q < 0 || s_sn[i] == 0.0) continue;
-        const double cs = s_cs[i], sn = s_sn[i];
-        const double tp = T[p * m + k], tq = T[q * m + k];
-        T[p * m + k] = cs * tp - sn * tq;
-        T[q * m + k] = sn * tp + cs * tq;
-      }
-      __syncthreads();
-      for (int e = tid; e < half * m; e += nt) {  // columns p, q and the eigenvectors
-        const int i = e / m, k = e - i * m;
-        const int p = s_p[i], q = s_q[i];
-        if (q < 0 || s_sn[i] == 0.0) continue;
-        const double cs = s_cs[i], sn = s_sn[i];
-        const double tp = T[k * m + p], tq = T[k * m + q];
-        T[k * m + p] = cs * tp - sn * tq;
-        T[k * m + q] = sn * tp + cs * tq;
-        const double vp = V[k * m + p], vq = V[k * m + q];
-        V[k * m + p] = cs * vp - sn * vq;
-        V[k * m + q] = sn * vp + cs * vq;
-      }
-      __syncthreads();
-    }
   }
+  jacobi_sweeps<double>(T, V, m, 8, 1e-20, s_cs, s_sn, s_p, s_q, &s_off, &s_tot);
   for (int i = tid; i < m; i += nt) lam[i] = T[i * m + i];
   __syncthreads();
   // decreasing Ritz value (stable on ties)
@@ -419,8 +568,12 @@ int subspace_block(int P, int ncomp) {
 int eig_top_subspace(annf_handle* h, const double* C, int P, int ncomp, int iters, double* comps, cudaStream_t st) {
   const int b = subspace_block(P, ncomp);
   ANNF_REQUIRE(b > 0, "subspace eigensolver: unsupported size");
-  const size_t smem = ((size_t)2 * b * P + (size_t)b * b) * sizeof(float);
-  ANNF_REQUIRE(smem <= 200 * 1024, "subspace eigensolver: block too large for shared memory");
+  // k slices of the C Q product: as many as the threads and shared memory allow (at most 4)
+  const size_t fixed = ((size_t)2 * b * P + 2 * (size_t)b * b + b) * sizeof(float);
+  int KS = std::max(1, std::min(4, kSubThreads / std::max(P, 1)));
+  while (KS > 1 && fixed + (size_t)KS * P * b * sizeof(float) > 220 * 1024) --KS;
+  const size_t smem = fixed + (size_t)KS * P * b * sizeof(float);
+  ANNF_REQUIRE(smem <= 220 * 1024, "subspace eigensolver: block too large for shared memory");
   const size_t f32_bytes = ((size_t)P * P + (size_t)b * P) * sizeof(float);
   const size_t f64_bytes = ((size_t)b * P + 2 * (size_t)b * b + (size_t)ncomp * b) * sizeof(double);
   ANNF_ENSURE(h->eig_ws, f64_bytes + f32_bytes + 256);
@@ -430,14 +583,29 @@ int eig_top_subspace(annf_handle* h, const double* C, int P, int ncomp, int iter
   double* X = T + (size_t)b * b;
   float* C32 = reinterpret_cast<float*>(X + (size_t)ncomp * b);
   float* Q = C32 + (size_t)P * P;
-  ANNF_CUDA_TRY(cudaFuncSetAttribute(subspace_iter_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  subspace_iter_kernel<<<1, kSubThreads, smem, st>>>(C, P, b, iters, C32, Q, h->status.as<unsigned>());
+  switch (b) {
+#define ANNF_SUBSPACE(BB)                                                                                    \
+  case BB:                                                                                                   \
+    ANNF_CUDA_TRY(cudaFuncSetAttribute(subspace_iter_kernel<BB>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                                       (int)smem));                                                          \
+    subspace_iter_kernel<BB><<<1, kSubThreads, smem, st>>>(C, P, KS, iters, C32, Q, h->status.as<unsigned>());  \
+    break;
+    ANNF_SUBSPACE(8)
+    ANNF_SUBSPACE(16)
+    ANNF_SUBSPACE(24)
+    ANNF_SUBSPACE(32)
+    ANNF_SUBSPACE(40)
+#undef ANNF_SUBSPACE
+    default:
+      set_error("subspace eigensolver: unsupported block");
+      return ANNF_ERR_UNSUPPORTED;
+  }
   ANNF_CHECK_LAUNCH();
   rr_cq_kernel<<<ceil_div((long long)b * P * 32, 256), 256, 0, st>>>(C, P, b, Q, W);
   ANNF_CHECK_LAUNCH();
   rr_gram_kernel<<<ceil_div(2LL * b * b * 32, 256), 256, 0, st>>>(P, b, Q, W, G, T);
   ANNF_CHECK_LAUNCH();
-  rr_solve_kernel<<<1, 256, 0, st>>>(b, ncomp, G, T, X, nullptr);
+  rr_solve_kernel<<<1, kRrThreads, 0, st>>>(b, ncomp, G, T, X, nullptr);
   ANNF_CHECK_LAUNCH();
   rr_comps_kernel<<<ncomp, 256, 0, st>>>(P, b, Q, X, comps);
   ANNF_CHECK_LAUNCH();

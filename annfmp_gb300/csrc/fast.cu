@@ -135,11 +135,12 @@ __device__ __forceinline__ uint32_t hash3(uint32_t a, uint32_t b, uint32_t c) {
 
 // candidates: k natural-leaf neighbours (tree positions -> B indices) and n_prop proposals
 __global__ void fast_init_kernel(Img A, Img B, int nA, int K, const int* __restrict__ nat_pos,
-                                 const int* __restrict__ perm, const int* __restrict__ prop, int n_prop, Match out) {
+                                 const int* __restrict__ perm, const int* __restrict__ prop, int n_prop,
+                                 const int* __restrict__ seed, Match out) {
   const int nb_rows = B.h - B.psize + 1;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nA; i += gridDim.x * blockDim.x) {
     const int y = i / A.ncols, x = i - y * A.ncols;
-    int best = -1, bs = 0x7fffffff;
+    int best = seed ? seed[i] : -1, bs = seed ? seed[nA + i] : 0x7fffffff;
     for (int j = 0; j < K + n_prop; ++j) {
       int b = j < K ? __ldg(perm + __ldg(nat_pos + (long long)i * K + j)) : __ldg(prop + (long long)i * n_prop + (j - K));
       if (b < 0) continue;
@@ -302,14 +303,16 @@ __device__ __forceinline__ void take_best(const int (&cy)[G], const int (&cx)[G]
 
 constexpr int kGroup = 4;  // candidates evaluated together
 
+// seed (optional, [2 nA]: B index, then SSD): a match to start from, e.g. the best proposal found
+// earlier; the result is the lexicographic minimum over the seed and the candidates either way
 template <int PS, int RL>
 __global__ void __launch_bounds__(256, 3) fast_init_t_kernel(Img A, Img B, int nA, int K, const int* __restrict__ nat_pos,
                                                           const int* __restrict__ perm, const int* __restrict__ prop,
-                                                          int n_prop, Match out) {
+                                                          int n_prop, const int* __restrict__ seed, Match out) {
   const int nb_rows = B.h - B.psize + 1;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nA; i += gridDim.x * blockDim.x) {
     const int y = i / A.ncols, x = i - y * A.ncols;
-    int best = -1, bs = 0x7fffffff;
+    int best = seed ? seed[i] : -1, bs = seed ? seed[nA + i] : 0x7fffffff;
     for (int j0 = 0; j0 < K + n_prop; j0 += kGroup) {
       int cy[kGroup], cx[kGroup], ssd[kGroup];
 #pragma unroll
@@ -380,9 +383,29 @@ __global__ void __launch_bounds__(256, 3) fast_prop_t_kernel(Img A, Img B, int n
   }
 }
 
+// best of n_cand candidate B indices per A pixel by exact raw SSD (cand [nA][n_cand], -1 = none),
+// as a match array seed_out [2 nA] (index, then SSD; -1 / INT_MAX where no candidate is valid)
+int seed_matches(const uint8_t* img_a, int ha, int wa, const uint8_t* img_b, int hb, int wb, int c, int psize,
+                 const int* cand, int n_cand, int* seed_out, cudaStream_t st) {
+  Img A{img_a, ha, wa, c, psize, wa - psize + 1, (long long)ha * wa * c};
+  Img B{img_b, hb, wb, c, psize, wb - psize + 1, (long long)hb * wb * c};
+  const int nA = (ha - psize + 1) * A.ncols;
+  const Match out{seed_out, seed_out + nA};
+  const int blocks = (int)std::min<long long>(ceil_div(nA, 256), 32LL * num_sms());
+  switch (psize * 100 + psize * c) {
+    case 927: fast_init_t_kernel<9, 27><<<blocks, 256, 0, st>>>(A, B, nA, 0, nullptr, nullptr, cand, n_cand, nullptr, out); break;
+    case 721: fast_init_t_kernel<7, 21><<<blocks, 256, 0, st>>>(A, B, nA, 0, nullptr, nullptr, cand, n_cand, nullptr, out); break;
+    case 515: fast_init_t_kernel<5, 15><<<blocks, 256, 0, st>>>(A, B, nA, 0, nullptr, nullptr, cand, n_cand, nullptr, out); break;
+    case 1133: fast_init_t_kernel<11, 33><<<blocks, 256, 0, st>>>(A, B, nA, 0, nullptr, nullptr, cand, n_cand, nullptr, out); break;
+    default: fast_init_kernel<<<blocks, 256, 0, st>>>(A, B, nA, 0, nullptr, nullptr, cand, n_cand, nullptr, out);
+  }
+  ANNF_CHECK_LAUNCH();
+  return ANNF_OK;
+}
+
 int fast_search(annf_handle* h, const uint8_t* img_a, int ha, int wa, const uint8_t* img_b, int hb, int wb, int c,
-                int psize, int K, const int* nat_pos, const int* prop, int n_prop, int iters, uint32_t seed,
-                int rand_samples, int radius0, int* final_idx, float* dist_out, cudaStream_t st) {
+                int psize, int K, const int* nat_pos, const int* prop, int n_prop, const int* seed_match, int iters,
+                uint32_t seed, int rand_samples, int radius0, int* final_idx, float* dist_out, cudaStream_t st) {
   Img A{img_a, ha, wa, c, psize, wa - psize + 1, (long long)ha * wa * c};
   Img B{img_b, hb, wb, c, psize, wb - psize + 1, (long long)hb * wb * c};
   const int nA = (ha - psize + 1) * A.ncols;
@@ -393,7 +416,7 @@ int fast_search(annf_handle* h, const uint8_t* img_a, int ha, int wa, const uint
   // shape-specialised kernels for the common patches, the generic ones otherwise
   const int shape = psize * 100 + psize * c;
   const bool special = shape == 927 || shape == 721 || shape == 515 || shape == 1133;
-#define ANNF_FAST_INIT(PS, RL) fast_init_t_kernel<PS, RL><<<blocks, 256, 0, st>>>(A, B, nA, K, nat_pos, h->perm.as<int>(), prop, n_prop, m0)
+#define ANNF_FAST_INIT(PS, RL) fast_init_t_kernel<PS, RL><<<blocks, 256, 0, st>>>(A, B, nA, K, nat_pos, h->perm.as<int>(), prop, n_prop, seed_match, m0)
 #define ANNF_FAST_PROP(PS, RL, ...) fast_prop_t_kernel<PS, RL><<<blocks, 256, 0, st>>>(__VA_ARGS__)
   switch (shape) {
     case 927: ANNF_FAST_INIT(9, 27); break;
@@ -401,7 +424,7 @@ int fast_search(annf_handle* h, const uint8_t* img_a, int ha, int wa, const uint
     case 515: ANNF_FAST_INIT(5, 15); break;
     case 1133: ANNF_FAST_INIT(11, 33); break;
     default:
-      fast_init_kernel<<<blocks, 256, 0, st>>>(A, B, nA, K, nat_pos, h->perm.as<int>(), prop, n_prop, m0);
+      fast_init_kernel<<<blocks, 256, 0, st>>>(A, B, nA, K, nat_pos, h->perm.as<int>(), prop, n_prop, seed_match, m0);
   }
   ANNF_CHECK_LAUNCH();
   prof_mark(h, "fast_init", st);

@@ -137,6 +137,12 @@ __global__ void __launch_bounds__(1024) leaf_scan_kernel(const int* __restrict__
   block_exclusive_scan(cnt, L, true, choff, nullptr);
 }
 
+// work item -> leaf: leaf l owns items choff[l] .. choff[l+1]-1 (one per 128 of its queries)
+__global__ void item_leaf_kernel(const int* __restrict__ choff, int L, int* __restrict__ item_leaf) {
+  for (int l = blockIdx.x * blockDim.x + threadIdx.x; l < L; l += gridDim.x * blockDim.x)
+    for (int c = choff[l]; c < choff[l + 1]; ++c) item_leaf[c] = l;
+}
+
 __global__ void qscatter_kernel(const int* __restrict__ qleaf, long long nq, int* __restrict__ cursor,
                                 int* __restrict__ qorder) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < nq; i += (long long)gridDim.x * blockDim.x)
@@ -192,11 +198,11 @@ struct TcLeafArgs {
   const int* qoff;    // [L+1] queries of leaf l: qorder[qoff[l] .. qoff[l+1])
   const int* qorder;  // [nq]
   const int* choff;   // [L+1] work items (128-query chunks) of leaf l: choff[l] .. choff[l+1]-1
+  const int* item_leaf;  // [choff[L]] leaf of each work item
   int K;              // neighbours written per query (<= KM)
   int npad;           // point rows staged per leaf (multiple of 16, >= largest leaf, <= 256)
   int ncols;          // TMEM columns allocated (power of two >= max(32, npad))
   int* out_pos;       // [nq*K] tree positions
-  int* work;          // leaf counter (zeroed before launch)
 };
 
 template <int KM, int KPAD, int PREC>
@@ -249,20 +255,13 @@ __global__ void __launch_bounds__(kTcThreads) leaf_tc_kernel(TcLeafArgs a) {
 
   const int total = __ldg(a.choff + L);
   int staged = -1;  // leaf whose points are in shared memory
-  for (;;) {
-    __syncthreads();  // every thread has read the previous work item
-    if (tid == 0) sflag[0] = atomicAdd(a.work, 1);
-    __syncthreads();
-    const int w = sflag[0];
-    if (w >= total) break;
-    // leaf of work item w: the last l with choff[l] <= w (leaves without queries have no items)
-    int lo = 0, hi = L;
-    while (hi - lo > 1) {
-      const int mid = (lo + hi) >> 1;
-      if (__ldg(a.choff + mid) <= w) lo = mid;
-      else hi = mid;
-    }
-    const int l = lo;
+  // work items in a fixed round robin (items are at most 128 queries of one leaf, so they cost
+  // about the same); the next item's leaf is read one item ahead
+  int l_next = (int)blockIdx.x < total ? __ldg(a.item_leaf + blockIdx.x) : 0;
+  for (int w = blockIdx.x; w < total; w += gridDim.x) {
+    __syncthreads();  // every thread has finished the previous work item
+    const int l = l_next;
+    if (w + (int)gridDim.x < total) l_next = __ldg(a.item_leaf + w + gridDim.x);
     const int qlb = __ldg(a.qoff + l), qle = __ldg(a.qoff + l + 1);
     const int qb = qlb + (w - __ldg(a.choff + l)) * kTcThreads, qe = min(qle, qb + kTcThreads);
     const int pb = __ldg(tv.leaf_begin + l);
@@ -531,8 +530,9 @@ int natural_knn_tc(annf_handle* h, const float* Q, long long nq, int K, int prec
   tv.point_leaf = h->point_leaf.as<int>();
   tv.status = h->status.as<unsigned>();
   tv.leaf_box = h->leaf_box.as<float>();
-  // scratch: qleaf[nq], qorder[nq], cnt[L], off[L+1], cursor[L], choff[L+1], work counter
-  const size_t need = ((size_t)2 * nq + 4 * (size_t)L + 16) * sizeof(int);
+  // scratch: qleaf[nq], qorder[nq], cnt[L], off[L+1], cursor[L], choff[L+1], item_leaf[items]
+  // (items <= L + nq / 128: each leaf's queries in chunks of 128)
+  const size_t need = ((size_t)2 * nq + 4 * (size_t)L + 16 + (size_t)L + (size_t)nq / kTcThreads + 1) * sizeof(int);
   ANNF_ENSURE(h->tc_buf, need);
   int* qleaf = h->tc_buf.as<int>();
   int* qorder = qleaf + nq;
@@ -540,9 +540,8 @@ int natural_knn_tc(annf_handle* h, const float* Q, long long nq, int K, int prec
   int* off = cnt + L;
   int* cursor = off + L + 1;
   int* choff = cursor + L;
-  int* work = choff + L + 1;
+  int* item_leaf = choff + L + 1;
   ANNF_CUDA_TRY(cudaMemsetAsync(cnt, 0, (size_t)L * sizeof(int), st));
-  ANNF_CUDA_TRY(cudaMemsetAsync(work, 0, sizeof(int), st));
   const size_t ncs = NodeCache<float>::bytes(h->depth);
   ANNF_CUDA_TRY(cudaFuncSetAttribute(qleaf_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ncs));
   const int blocks = (int)std::min<long long>(ceil_div(nq, 256), 8LL * num_sms());
@@ -551,6 +550,8 @@ int natural_knn_tc(annf_handle* h, const float* Q, long long nq, int K, int prec
   leaf_scan_kernel<<<1, 1024, 0, st>>>(cnt, L, off, cursor, choff);
   ANNF_CHECK_LAUNCH();
   qscatter_kernel<<<blocks, 256, 0, st>>>(qleaf, nq, cursor, qorder);
+  ANNF_CHECK_LAUNCH();
+  item_leaf_kernel<<<ceil_div(L, 256), 256, 0, st>>>(choff, L, item_leaf);
   ANNF_CHECK_LAUNCH();
   prof_mark(h, "tc_group", st);
 
@@ -564,7 +565,7 @@ int natural_knn_tc(annf_handle* h, const float* Q, long long nq, int K, int prec
   args.npad = (h->max_leaf + 15) / 16 * 16;
   args.ncols = std::max(32, next_pow2(args.npad));
   args.out_pos = out_pos;
-  args.work = work;
+  args.item_leaf = item_leaf;
   const int kpad = h->d <= 16 ? 16 : 32;
   const int kt = (prec == 0 ? 3 : 1) * kpad;  // K extent of the tiles (BF16 hi/lo split: 3 terms)
   const size_t carve = (size_t)kTcThreads * kt * 2 + (size_t)args.npad * kt * 2 + (size_t)args.npad * kpad * 4 +

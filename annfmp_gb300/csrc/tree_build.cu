@@ -600,7 +600,7 @@ __global__ void __launch_bounds__(kSubThreads) subtree_kernel(
     int n, int d, int depth, int t0, int smax, int splitting, const T* __restrict__ pts_in,
     const int* __restrict__ perm_in, T* __restrict__ pts_out, int* __restrict__ perm_out,
     int* __restrict__ node_axis, T* __restrict__ node_split, int* __restrict__ leaf_begin,
-    int* __restrict__ point_leaf, unsigned* status) {
+    int* __restrict__ point_leaf, T* __restrict__ leaf_box, unsigned* status) {
   using K = typename key_of<T>::type;
   constexpr int kBits = 8 * sizeof(K);
   const int ds = sub_stride(d);
@@ -851,6 +851,25 @@ __global__ void __launch_bounds__(kSubThreads) subtree_kernel(
       if (leaf == (1 << depth) - 1) leaf_begin[leaf + 1] = n;
     }
     for (int i = a + lane; i < b; i += 32) point_leaf[sperm[cur[i]]] = leaf;
+    // the leaf's bounding box, lanes and reduction as leaf_box_kernel (bit-identical)
+    for (int j = 0; j < d; ++j) {
+      T mn = real_traits<T>::big(), mx = -real_traits<T>::big();
+      for (int i = a + lane; i < b; i += 32) {
+        const T v = spts[(size_t)cur[i] * ds + j];
+        mn = v < mn ? v : mn;
+        mx = v > mx ? v : mx;
+      }
+#pragma unroll
+      for (int o = 16; o; o >>= 1) {
+        const T oa = __shfl_xor_sync(0xffffffffu, mn, o), ob = __shfl_xor_sync(0xffffffffu, mx, o);
+        mn = oa < mn ? oa : mn;
+        mx = ob > mx ? ob : mx;
+      }
+      if (lane == 0) {
+        leaf_box[((long long)leaf * 2) * d + j] = mn;
+        leaf_box[((long long)leaf * 2 + 1) * d + j] = mx;
+      }
+    }
   }
   if (sizeof(T) == 4 && (d & 3) == 0) {
     float4* dst = reinterpret_cast<float4*>(pts_out + (long long)lo * d);
@@ -925,6 +944,7 @@ static int build_impl(annf_handle* h, const T* points, int n, int d, int depth, 
     ANNF_ENSURE(h->hist, (size_t)(cap / 2) * 256 * sizeof(unsigned));
     ANNF_CUDA_TRY(cudaMemsetAsync(h->hist.p, 0, (size_t)(cap / 2) * 256 * sizeof(unsigned), st));  // picks re-zero it
   }
+  ANNF_ENSURE(h->leaf_box, (size_t)2 * L * d * sizeof(T));
   bool finished = false;
   for (int t = 0; t < depth; ++t) {
     const int S = 1 << t;
@@ -933,7 +953,8 @@ static int build_impl(annf_handle* h, const T* points, int n, int d, int depth, 
       ANNF_CUDA_TRY(cudaFuncSetAttribute(subtree_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sub_smem));
       subtree_kernel<T><<<S, kSubThreads, sub_smem, st>>>(
           n, d, depth, t, smax, splitting, cur_pts, cur_perm, alt_pts, alt_perm, h->node_axis.as<int>(),
-          h->node_split.as<T>(), h->leaf_begin.as<int>(), h->point_leaf.as<int>(), h->status.as<unsigned>());
+          h->node_split.as<T>(), h->leaf_begin.as<int>(), h->point_leaf.as<int>(), h->leaf_box.as<T>(),
+          h->status.as<unsigned>());
       ANNF_CHECK_LAUNCH();
       std::swap(cur_pts, alt_pts);
       std::swap(cur_perm, alt_perm);
@@ -1008,11 +1029,13 @@ static int build_impl(annf_handle* h, const T* points, int n, int d, int depth, 
   // the final arrays live in h->pts / h->perm
   if (cur_pts != h->pts.as<T>()) std::swap(h->pts, h->pts_tmp);
   if (cur_perm != h->perm.as<int>()) std::swap(h->perm, h->perm_tmp);
-  // per-leaf bounding boxes: lower bounds for the exact search
-  ANNF_ENSURE(h->leaf_box, (size_t)2 * L * d * sizeof(T));
-  leaf_box_kernel<T><<<ceil_div((long long)L * 32, 256), 256, 0, st>>>(L, d, h->pts.as<T>(), h->leaf_begin.as<int>(),
-                                                                     h->leaf_box.as<T>());
-  ANNF_CHECK_LAUNCH();
+  // per-leaf bounding boxes: lower bounds for the exact search (the finisher computed them when
+  // it built the leaves)
+  if (!finished) {
+    leaf_box_kernel<T><<<ceil_div((long long)L * 32, 256), 256, 0, st>>>(L, d, h->pts.as<T>(), h->leaf_begin.as<int>(),
+                                                                       h->leaf_box.as<T>());
+    ANNF_CHECK_LAUNCH();
+  }
   prof_mark(h, "build_leafbox", st);
   const int maxleaf = (int)(((long long)n + L - 1) / L);
   int bits = 1;

@@ -264,7 +264,7 @@ class ANNFieldPropKDTreeGB300:
 
         # offset proposals depend only on the images: computed on a side stream, overlapping the PCA
         # fit (whose eigensolver occupies one SM) and the projection; joined before the candidates
-        prop, side = None, None
+        prop, side, seeded = None, None, False
         if self.form != "plain" and self.proposal is not None:
             main = torch.cuda.current_stream(dev)
             side = torch.cuda.Stream(dev) if getattr(self, "_side", None) is None else self._side
@@ -292,6 +292,14 @@ class ANNFieldPropKDTreeGB300:
         else:
             raise ValueError("pca_solver must be 'exact' or 'subspace'")
         ev["t1"].record()
+
+        # the proposals' exact distances need no tree: their best match is found on the side
+        # stream while the projection and the tree build (bandwidth-bound) run here
+        if prop is not None and hasattr(self.proposal, "seed"):
+            side.wait_stream(torch.cuda.current_stream(dev))
+            with torch.cuda.stream(side):
+                prop = self.proposal.seed(A, B, p, prop)
+            seeded = True
 
         # (2)+(3) patches projected straight from the images (annfmp/openmp/base.py:152-166, 193-200)
         self.patches_a_reduced_ = torch.empty((n_a, d), dtype=real, device=dev)
@@ -334,16 +342,22 @@ class ANNFieldPropKDTreeGB300:
                 torch.cuda.current_stream(dev).wait_stream(side)
                 if prop is not None:
                     prop.record_stream(torch.cuda.current_stream(dev))
-            n_prop = 0 if prop is None else int(prop.shape[1])
             lp = self.leaf_precision or "bf16"
             if lp not in ("bf16", "fp16", "fp32"):
                 raise ValueError("leaf_precision must be 'bf16', 'fp16' or 'fp32'")
             if lp != "fp32" and real != torch.float32:
                 raise ValueError("tensor-core leaf distances need float_type='float'")
-            h.call("annf_parallel_nnf", ptr(nn), ptr(A), ha, wa, ptr(B), hb, wb, c, p,
-                   ptr(self.patches_a_reduced_), k, ptr(prop), n_prop, int(self.iters), int(self.seed) & 0xFFFFFFFF,
-                   {"bf16": _lib.ANNF_LEAF_BF16, "fp16": _lib.ANNF_LEAF_FP16, "fp32": _lib.ANNF_LEAF_EXACT}[lp],
-                   int(self.search[0]), int(self.search[1]), ptr(self.nn_distances_), st)
+            lpc = {"bf16": _lib.ANNF_LEAF_BF16, "fp16": _lib.ANNF_LEAF_FP16, "fp32": _lib.ANNF_LEAF_EXACT}[lp]
+            if seeded:  # the proposals' best match, found on the side stream
+                h.call("annf_parallel_nnf_seeded", ptr(nn), ptr(A), ha, wa, ptr(B), hb, wb, c, p,
+                       ptr(self.patches_a_reduced_), k, ptr(prop), int(self.iters), int(self.seed) & 0xFFFFFFFF, lpc,
+                       int(self.search[0]), int(self.search[1]), ptr(self.nn_distances_), st)
+            else:
+                n_prop = 0 if prop is None else int(prop.shape[1])
+                h.call("annf_parallel_nnf", ptr(nn), ptr(A), ha, wa, ptr(B), hb, wb, c, p,
+                       ptr(self.patches_a_reduced_), k, ptr(prop), n_prop, int(self.iters),
+                       int(self.seed) & 0xFFFFFFFF, lpc, int(self.search[0]), int(self.search[1]),
+                       ptr(self.nn_distances_), st)
         ev["t4"].record()
         self.kdtree = tree
         self._A, self._B = A, B

@@ -176,7 +176,8 @@ class KDTree(object):
     def tree_arrays(self) -> dict:
         """Copies of the device tree arrays, in the reference's layout terms:
         points (tree order), perm (tree position -> original index), node_axis, node_split,
-        leaves (2 ints per leaf: begin, end), point_leaf (original index -> leaf)."""
+        leaves (2 ints per leaf: begin, end), point_leaf (original index -> leaf), leaf_box
+        ([leaves, 2, d]: per leaf the minimum, then the maximum, of each coordinate)."""
         tv = self.handle.tree_view()
         torch.cuda.current_stream(self._dev).synchronize()
         real = np.float32 if tv.real_type == _lib.ANNF_REAL_F32 else np.float64
@@ -193,7 +194,8 @@ class KDTree(object):
                     node_axis=fetch(tv.node_axis, max(L - 1, 0), np.int32),
                     node_split=fetch(tv.node_split, max(L - 1, 0), real),
                     leaves=np.stack([lb[:-1], lb[1:]], axis=1).reshape(-1).astype(np.int32),
-                    point_leaf=fetch(tv.point_leaf, tv.n, np.int32))
+                    point_leaf=fetch(tv.point_leaf, tv.n, np.int32),
+                    leaf_box=fetch(tv.leaf_box, 2 * L * tv.d, real).reshape(L, 2, tv.d))
 
     def __repr__(self):
         return str(self.get_params())

@@ -156,6 +156,20 @@ class ProposalNet:
                     self._stream())
         return props
 
+    def seed(self, A, B, psize: int, props: torch.Tensor) -> torch.Tensor:
+        """int32 [2, n_A] match array: the best of each A patch's proposals by exact raw SSD (B
+        index, then SSD; -1 / INT32_MAX where none is valid). Needs no tree, so it can run beside
+        the PCA fit and the tree build (on the caller's current stream)."""
+        A = to_device(A, torch.uint8, self.dev)
+        B = to_device(B, torch.uint8, self.dev)
+        H, W = A.shape[0], A.shape[1]
+        c = A.shape[2] if A.dim() == 3 else 1
+        n_a = (H - psize + 1) * (W - psize + 1)
+        out = torch.empty((2, n_a), dtype=torch.int32, device=self.dev)
+        self.h.call("annf_seed_matches", ptr(A), H, W, ptr(B), B.shape[0], B.shape[1], c, int(psize), ptr(props),
+                    int(props.shape[1]), ptr(out), self._stream())
+        return out
+
     # -- backward ---------------------------------------------------------------------------------
     def backward(self, acts, dout):
         """Gradients [(dW [co,3,3,ci], db [co]), ...] of every layer for dL/d out = dout."""

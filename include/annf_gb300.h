@@ -60,6 +60,8 @@ typedef struct {
   const void* node_split;  /* [2^depth-1] (reference nodes[].splitting_value) */
   const int* leaf_begin;   /* [2^depth+1]; leaf l = [leaf_begin[l], leaf_begin[l+1]) (reference leaves[]) */
   const int* point_leaf;   /* [n] original index -> leaf (reference points_leaf_indices) */
+  const void* leaf_box;    /* [2^depth][2][d]: per leaf the min, then the max, of each coordinate
+                              (no reference counterpart: lower bounds of the exact search) */
 } annf_tree_view;
 
 int annf_version(void);
@@ -171,6 +173,24 @@ int annf_parallel_nnf(annf_handle* h, int* final_idx, const uint8_t* img_a, int 
                       const uint8_t* img_b, int hb, int wb, int channels, int psize, const void* ared,
                       int k, const int* proposals, int n_prop, int iters, unsigned seed,
                       int leaf_precision, int rand_samples, int radius0, float* dist_out, void* stream);
+
+/* Best of n_cand candidate B patches per A pixel (candidates [n_rows*n_cols*n_cand] B indices, -1 =
+ * none) by exact integer raw-patch SSD, as a match array seed_out [2*n_rows*n_cols]: the B index
+ * (-1 if no candidate is valid), then the SSD (INT32_MAX if none); ties go to the smaller index.
+ * Needs no tree: the caller can run it on a second stream while the PCA fit and the tree run (the
+ * learned proposals' candidates are known before them). No reference counterpart. */
+int annf_seed_matches(annf_handle* h, const uint8_t* img_a, int ha, int wa, const uint8_t* img_b, int hb,
+                      int wb, int channels, int psize, const int* candidates, int n_cand, int* seed_out,
+                      void* stream);
+
+/* annf_parallel_nnf starting from a seed match (annf_seed_matches' output) instead of proposals:
+ * the initial choice is the best of the seed and the natural-leaf k-list, which equals
+ * annf_parallel_nnf with the seed's candidates as proposals. No reference counterpart. */
+int annf_parallel_nnf_seeded(annf_handle* h, int* final_idx, const uint8_t* img_a, int ha, int wa,
+                             const uint8_t* img_b, int hb, int wb, int channels, int psize,
+                             const void* ared, int k, const int* seed_match, int iters, unsigned seed,
+                             int leaf_precision, int rand_samples, int radius0, float* dist_out,
+                             void* stream);
 
 /* Exact raw-patch nearest neighbour (integer SSD over all B patches) of nq sampled A pixels
  * (query_pixels: row-major patch indices). best[i] = ssd << 32 | B index (smallest index on

@@ -28,6 +28,17 @@ def assert_tree_equal(arrs, perm, node_axis, node_split, leaf_bounds, point_leaf
     assert np.array_equal(_bits(arrs["node_split"]), _bits(node_split)), tag
     assert np.array_equal(arrs["leaves"], leaf_bounds), tag
     assert np.array_equal(arrs["point_leaf"], point_leaf), tag
+    # per-leaf bounding boxes (the exact search's lower bounds): min / max of each coordinate
+    pts = X[perm]
+    big = np.finfo(X.dtype).max
+    lb = np.asarray(leaf_bounds).reshape(-1, 2)
+    box = arrs["leaf_box"]
+    for leaf, (b0, b1) in enumerate(lb):
+        if b1 > b0:
+            want_lo, want_hi = pts[b0:b1].min(axis=0), pts[b0:b1].max(axis=0)
+        else:
+            want_lo, want_hi = np.full(X.shape[1], big, X.dtype), np.full(X.shape[1], -big, X.dtype)
+        assert np.array_equal(box[leaf, 0], want_lo) and np.array_equal(box[leaf, 1], want_hi), (tag, leaf)
 
 
 # ---------------------------------------------------------------------------------------------

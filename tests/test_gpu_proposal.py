@@ -147,3 +147,49 @@ def test_trained_proposals_gain(gpu_lib):
         e0 = metrics.distance_ratio_error(a, b, nn0, 7, n_samples=4096, seed=11)
         e1 = metrics.distance_ratio_error(a, b, nn1, 7, n_samples=4096, seed=11)
         assert e1["mean"] < e0["mean"], (iters, e1, e0)
+
+
+class _ProposalsOnly:
+    """A proposal source without a seed method: the NNF then takes the proposals themselves."""
+
+    def __init__(self, net):
+        self.net = net
+
+    def propose(self, A, B, psize):
+        return self.net.propose(A, B, psize)
+
+
+def test_seeded_start_equals_proposals_in_init(gpu_lib):
+    """The proposals' best match found beside the PCA fit (annf_seed_matches) and handed to the
+    NNF (annf_parallel_nnf_seeded) gives the NNF of the proposals passed in (annf_parallel_nnf):
+    the initial choice is the lexicographic minimum of (distance, index) over the same set."""
+    import numpy as np
+    import torch
+    from annfmp_gb300 import ANNFieldPropKDTreeGB300, gen
+    from annfmp_gb300._torch import ptr, stream_ptr
+    from annfmp_gb300.proposal import ProposalNet
+    net = ProposalNet()  # untrained weights: proposals of any quality must give the same NNF
+    for seed, size in ((5, 160), (6, 203)):
+        a, b = gen.pair_flow(seed, size, magnitude=6.0, sigma=24.0)
+        kw = dict(n_neighbors=4, psize=7, dim_reduced=8, n_subset=3000, leaf_size=32, seed=0, verbose=0,
+                  form="parallel", iters=2, graph=False)
+        m1 = ANNFieldPropKDTreeGB300(proposal=net, **kw)
+        nn1 = m1.fit(a, b)
+        m2 = ANNFieldPropKDTreeGB300(proposal=_ProposalsOnly(net), **kw)
+        nn2 = m2.fit(a, b)
+        assert np.array_equal(nn1, nn2)
+        assert torch.equal(m1.nn_distances_, m2.nn_distances_)
+    # the seed itself: each pixel's best proposal by exact SSD (checked against the oracle's SSDs)
+    from oracle import oracle as O
+    A, B = torch.from_numpy(a).cuda(), torch.from_numpy(b).cuda()
+    props = net.propose(A, B, 7)
+    seed = net.seed(A, B, 7, props).cpu().numpy()
+    P = props.cpu().numpy().astype(np.int64)
+    pa, pb = O.extract_patches(a, 7).astype(np.int64), O.extract_patches(b, 7).astype(np.int64)
+    ssd = np.stack([((pa - pb[np.maximum(P[:, j], 0)]) ** 2).sum(axis=1) for j in range(P.shape[1])], axis=1)
+    none = np.int64(1) << 40  # above any SSD
+    ssd[P < 0] = none
+    mins = ssd.min(axis=1)
+    best = np.where(ssd == mins[:, None], P, np.iinfo(np.int64).max).min(axis=1)  # smaller index on ties
+    assert np.array_equal(seed[0], np.where(mins == none, -1, best))
+    assert np.array_equal(seed[1][seed[0] >= 0], mins[seed[0] >= 0])
