@@ -28,6 +28,7 @@ ANNF_SPLIT_LONGEST = 1
 ANNF_LEAF_EXACT = 0
 ANNF_LEAF_BF16 = 1
 ANNF_LEAF_FP16 = 2
+ANNF_LEAF_FP8 = 3
 
 
 class AnnfError(RuntimeError):

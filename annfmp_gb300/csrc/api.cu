@@ -311,6 +311,11 @@ int annf_kneighbors_noalloc(annf_handle* h, const void* queries, int nq, int k, 
   return kneighbors_noalloc(h, queries, nq, k, max_leaves, distances, indices, static_cast<cudaStream_t>(stream));
 }
 
+// tensor-core tile precision of natural_knn_tc: 0 BF16 split, 1 FP16, 2 FP8 (E4M3) split
+static int leaf_tc_prec(int leaf_precision) {
+  return leaf_precision == ANNF_LEAF_FP16 ? 1 : leaf_precision == ANNF_LEAF_FP8 ? 2 : 0;
+}
+
 static int parallel_nnf_impl(annf_handle* h, int* final_idx, const uint8_t* img_a, int ha, int wa,
                              const uint8_t* img_b, int hb, int wb, int channels, int psize, const void* ared, int k,
                              const int* proposals, int n_prop, const int* seed_match, int iters, unsigned seed,
@@ -332,13 +337,13 @@ static int parallel_nnf_impl(annf_handle* h, int* final_idx, const uint8_t* img_
   const long long nA = (long long)(ha - psize + 1) * (wa - psize + 1);
   ANNF_ENSURE(h->fast_nat, (size_t)nA * k * sizeof(int));
   ANNF_REQUIRE(leaf_precision == ANNF_LEAF_EXACT || leaf_precision == ANNF_LEAF_BF16 ||
-                   leaf_precision == ANNF_LEAF_FP16,
+                   leaf_precision == ANNF_LEAF_FP16 || leaf_precision == ANNF_LEAF_FP8,
                "annf_parallel_nnf: bad leaf_precision");
   ANNF_REQUIRE(leaf_precision == ANNF_LEAF_EXACT || leaf_tc_supported(h, k),
                "annf_parallel_nnf: tensor-core leaf distances need FP32 points, d <= 32, leaves <= 256, k <= 32");
   prof_mark(h, "parallel:begin", st);
   if (leaf_precision != ANNF_LEAF_EXACT)
-    rc = natural_knn_tc(h, static_cast<const float*>(ared), nA, k, leaf_precision == ANNF_LEAF_FP16 ? 1 : 0,
+    rc = natural_knn_tc(h, static_cast<const float*>(ared), nA, k, leaf_tc_prec(leaf_precision),
                         h->fast_nat.as<int>(), st);
   else
     rc = natural_knn_all(h, ared, nA, k, h->fast_nat.as<int>(), st);
@@ -414,13 +419,13 @@ int annf_natural_knn(annf_handle* h, const void* queries, long long nq, int k, i
   if (nq == 0) return ANNF_OK;
   ANNF_REQUIRE(queries && out_pos, "annf_natural_knn: NULL argument");
   ANNF_REQUIRE(leaf_precision == ANNF_LEAF_EXACT || leaf_precision == ANNF_LEAF_BF16 ||
-                   leaf_precision == ANNF_LEAF_FP16,
+                   leaf_precision == ANNF_LEAF_FP16 || leaf_precision == ANNF_LEAF_FP8,
                "annf_natural_knn: bad leaf_precision");
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   if (leaf_precision != ANNF_LEAF_EXACT) {
     ANNF_REQUIRE(leaf_tc_supported(h, k), "annf_natural_knn: tensor-core leaf distances need FP32 points, "
                                           "d <= 32, leaves <= 256, k <= 32");
-    return natural_knn_tc(h, static_cast<const float*>(queries), nq, k, leaf_precision == ANNF_LEAF_FP16 ? 1 : 0,
+    return natural_knn_tc(h, static_cast<const float*>(queries), nq, k, leaf_tc_prec(leaf_precision),
                           out_pos, st);
   }
   return natural_knn_all(h, queries, nq, k, out_pos, st);

@@ -11,6 +11,7 @@
 // cancellation that |a|^2 + |b|^2 - 2 a.b suffers on uncentred reduced coordinates.
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
+#include <cuda_fp8.h>
 
 #include <algorithm>
 
@@ -34,7 +35,9 @@ constexpr long long kTcWaitCycles = 2000000000LL;  // ~1 s at 2 GHz: bound of ev
 template <int PREC> struct TcPrec;
 template <> struct TcPrec<0> {
   static constexpr int kSplit = 3;
+  static constexpr int kES = 2;  // bytes per element
   static constexpr float kDot = 5.0e-5f;  // > 3 * 2^-16 + 2^-20 = 4.67e-5
+  static constexpr float kAbs = 0.f;
   __device__ static void split(float x, float& hi, float& lo) {
     hi = __bfloat162float(__float2bfloat16_rn(x));
     lo = __bfloat162float(__float2bfloat16_rn(x - hi));
@@ -47,7 +50,9 @@ template <> struct TcPrec<0> {
 };
 template <> struct TcPrec<1> {
   static constexpr int kSplit = 1;
+  static constexpr int kES = 2;
   static constexpr float kDot = 1.0e-3f;  // > 2^-10 + 2^-20 = 9.77e-4 (centred values far below 65504)
+  static constexpr float kAbs = 0.f;
   __device__ static void split(float x, float& hi, float& lo) {
     hi = __half2float(__float2half_rn(x));
     lo = 0.f;
@@ -58,6 +63,36 @@ template <> struct TcPrec<1> {
   }
   __host__ __device__ static constexpr uint32_t idesc(int M, int N) { return tc::idesc_f16(M, N); }
 };
+
+// FP8 (E4M3) hi/lo split of values scaled by a power of two into [-256, 256] (|x| < 256 once
+// scaled; the largest E4M3 value is 448). Per element, hi + lo represents v within 2^-8 |v| +
+// 2^-10 (lo's relative rounding 2^-4 of |v - hi| <= 2^-4 |v|, or half the subnormal step 2^-9);
+// the tiles [hi|lo|hi] . [hi|hi|lo] drop lo.lo (<= 2^-8 |a||b| + small), every product is exact
+// in FP32, and the FP32 accumulation is charged 1e-3 (a margin far above 64 roundings at 2^-24,
+// which also covers an accumulator narrower than FP32). In the scaled units:
+//   |dot - a.b| <= kDot |a||b| + kAbs sqrt(d) (|a| + |b|) + kConst d.
+template <> struct TcPrec<2> {
+  static constexpr int kSplit = 3;
+  static constexpr int kES = 1;
+  static constexpr float kDot = 1.3e-2f;   // > 2^-7 + 2^-8 + 2^-16 + 1e-3 = 1.273e-2
+  static constexpr float kAbs = 1.1e-3f;   // > 2^-10 + 2^-14 + 2^-18 = 1.04e-3
+  static constexpr float kConst = 2.1e-6f;  // > 2 * 2^-20 per dimension
+  __device__ static uint8_t q8(float v) { return (uint8_t)__nv_cvt_float_to_fp8(v, __NV_SATFINITE, __NV_E4M3); }
+  __device__ static float f8(uint8_t b) {
+    return __half2float(__half(__nv_cvt_fp8_to_halfraw((__nv_fp8_storage_t)b, __NV_E4M3)));
+  }
+  __host__ __device__ static constexpr uint32_t idesc(int M, int N) { return tc::idesc_f16(M, N); }
+};
+
+// power-of-two scale that maps a magnitude m > 0 into [128, 256) (1 for m == 0)
+__device__ __forceinline__ float pow2_scale_256(float m) { return m > 0.f ? ldexpf(1.f, 7 - ilogbf(m)) : 1.f; }
+
+// byte offset of element byte kb of row r in a K-major no-swizzle core-matrix tile whose rows are
+// RB bytes (core matrix: 8 rows x 16 bytes; LBO 128 along K, SBO (RB / 16) * 128 along rows)
+template <int RB>
+__device__ __forceinline__ int core_off_b(int r, int kb) {
+  return ((r >> 3) * (RB >> 4) + (kb >> 4)) * 128 + (r & 7) * 16 + (kb & 15);
+}
 
 __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
   __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
@@ -208,21 +243,22 @@ struct TcLeafArgs {
 template <int KM, int KPAD, int PREC>
 __global__ void __launch_bounds__(kTcThreads) leaf_tc_kernel(TcLeafArgs a) {
   using PR = TcPrec<PREC>;
-  constexpr int KT = PR::kSplit * KPAD;  // K extent of the tiles
+  constexpr int KT = PR::kSplit * KPAD;  // K extent of the tiles (elements)
+  constexpr int RB = (KT * PR::kES + 31) / 32 * 32;  // tile row bytes: whole MMA K steps (32 bytes)
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   const TreeView<float>& tv = a.tv;
   const int d = tv.d, L = 1 << tv.depth, npad = a.npad, K = a.K;
   // carve: A tile, B tile (core-matrix layouts), FP32 leaf points, norms, centre, barrier, TMEM slot
   unsigned char* p = smem_raw;
   unsigned char* sA = p;
-  p += kTcThreads * KT * 2;
+  p += kTcThreads * RB;
   unsigned char* sB = p;
-  p += (size_t)npad * KT * 2;
+  p += (size_t)npad * RB;
   float* sP = reinterpret_cast<float*>(p);  // [npad][KPAD] FP32 leaf points (zero padded)
   p += (size_t)npad * KPAD * 4;
   float* sN = reinterpret_cast<float*>(p);
   p += (size_t)npad * 4;
-  float* sC = reinterpret_cast<float*>(p);  // [KPAD] centre, then [KPAD] = R
+  float* sC = reinterpret_cast<float*>(p);  // [KPAD] centre, then [KPAD] = R, [KPAD+1] = FP8 point scale
   p += (KPAD + 4) * 4;
   p = reinterpret_cast<unsigned char*>(((uintptr_t)p + 15) & ~uintptr_t(15));
   uint64_t* mbar = reinterpret_cast<uint64_t*>(p);
@@ -274,7 +310,7 @@ __global__ void __launch_bounds__(kTcThreads) leaf_tc_kernel(TcLeafArgs a) {
     staged = l;
     // centre (box midpoint) and half-diagonal R of the leaf box
     if (tid < 32) {
-      float r2 = 0.f;
+      float r2 = 0.f, emax = 0.f;
       for (int j = tid; j < KPAD; j += 32) {
         float c = 0.f;
         if (j < d) {
@@ -282,12 +318,21 @@ __global__ void __launch_bounds__(kTcThreads) leaf_tc_kernel(TcLeafArgs a) {
           c = 0.5f * (lo + hi);
           const float e = 0.5f * (hi - lo);
           r2 = fmaf(e, e, r2);
+          emax = fmaxf(emax, e);
         }
         sC[j] = c;
       }
 #pragma unroll
-      for (int o = 16; o; o >>= 1) r2 += __shfl_xor_sync(0xffffffffu, r2, o);
-      if (tid == 0) sC[KPAD] = sqrtf(r2) * 1.000001f + 1e-30f;
+      for (int o = 16; o; o >>= 1) {
+        r2 += __shfl_xor_sync(0xffffffffu, r2, o);
+        emax = fmaxf(emax, __shfl_xor_sync(0xffffffffu, emax, o));
+      }
+      if (tid == 0) {
+        sC[KPAD] = sqrtf(r2) * 1.000001f + 1e-30f;
+        // FP8: every centred coordinate is within the largest half extent (plus the centre's
+        // rounding, far inside the E4M3 range above 256)
+        sC[KPAD + 1] = pow2_scale_256(emax);
+      }
     }
     __syncthreads();
     // the leaf's points: FP32 copy, BF16 centred tile, BF16 norms
@@ -312,31 +357,62 @@ __global__ void __launch_bounds__(kTcThreads) leaf_tc_kernel(TcLeafArgs a) {
         for (int j = 0; j < KPAD; ++j) f[j] = (r < np && j < d) ? __ldg(src + j) : 0.f;
       }
       float nrm = 0.f;
+      if constexpr (PREC != 2) {
 #pragma unroll
-      for (int k8 = 0; k8 < KPAD; k8 += 8) {
-        float hi[8], lo[8];
+        for (int k8 = 0; k8 < KPAD; k8 += 8) {
+          float hi[8], lo[8];
 #pragma unroll
-        for (int u = 0; u < 8; ++u) {
-          const int j = k8 + u;
-          const float x = (r < np && j < d) ? f[j] - sC[j] : 0.f;
-          nrm = fmaf(x, x, nrm);
-          PR::split(x, hi[u], lo[u]);
+          for (int u = 0; u < 8; ++u) {
+            const int j = k8 + u;
+            const float x = (r < np && j < d) ? f[j] - sC[j] : 0.f;
+            nrm = fmaf(x, x, nrm);
+            PR::split(x, hi[u], lo[u]);
+          }
+          uint4 wh, wl;
+          wh.x = PR::pack(hi[0], hi[1]);
+          wh.y = PR::pack(hi[2], hi[3]);
+          wh.z = PR::pack(hi[4], hi[5]);
+          wh.w = PR::pack(hi[6], hi[7]);
+          wl.x = PR::pack(lo[0], lo[1]);
+          wl.y = PR::pack(lo[2], lo[3]);
+          wl.z = PR::pack(lo[4], lo[5]);
+          wl.w = PR::pack(lo[6], lo[7]);
+          // B row: [hi | hi | lo] against A row [hi | lo | hi]
+          *reinterpret_cast<uint4*>(sB + tc::core_offset(r, k8, KT)) = wh;
+          if constexpr (PR::kSplit == 3) {
+            *reinterpret_cast<uint4*>(sB + tc::core_offset(r, KPAD + k8, KT)) = wh;
+            *reinterpret_cast<uint4*>(sB + tc::core_offset(r, 2 * KPAD + k8, KT)) = wl;
+          }
         }
-        uint4 wh, wl;
-        wh.x = PR::pack(hi[0], hi[1]);
-        wh.y = PR::pack(hi[2], hi[3]);
-        wh.z = PR::pack(hi[4], hi[5]);
-        wh.w = PR::pack(hi[6], hi[7]);
-        wl.x = PR::pack(lo[0], lo[1]);
-        wl.y = PR::pack(lo[2], lo[3]);
-        wl.z = PR::pack(lo[4], lo[5]);
-        wl.w = PR::pack(lo[6], lo[7]);
-        // B row: [hi | hi | lo] against A row [hi | lo | hi]
-        *reinterpret_cast<uint4*>(sB + tc::core_offset(r, k8, KT)) = wh;
-        if constexpr (PR::kSplit == 3) {
-          *reinterpret_cast<uint4*>(sB + tc::core_offset(r, KPAD + k8, KT)) = wh;
-          *reinterpret_cast<uint4*>(sB + tc::core_offset(r, 2 * KPAD + k8, KT)) = wl;
+      } else {  // FP8: [hi | hi | lo] of the scaled centred point, zero bytes up to RB
+        const float sb = sC[KPAD + 1];
+        uint32_t hw[KPAD / 4], lw[KPAD / 4];
+#pragma unroll
+        for (int j4 = 0; j4 < KPAD / 4; ++j4) {
+          uint32_t h4 = 0, l4 = 0;
+#pragma unroll
+          for (int u = 0; u < 4; ++u) {
+            const int j = 4 * j4 + u;
+            const float x = (r < np && j < d) ? f[j] - sC[j] : 0.f;
+            nrm = fmaf(x, x, nrm);
+            const float v = x * sb;
+            const uint8_t h = PR::q8(v), lq = PR::q8(v - PR::f8(h));
+            h4 |= (uint32_t)h << (8 * u);
+            l4 |= (uint32_t)lq << (8 * u);
+          }
+          hw[j4] = h4;
+          lw[j4] = l4;
         }
+#pragma unroll
+        for (int c16 = 0; c16 < KPAD / 16; ++c16) {
+          const uint4 H = make_uint4(hw[4 * c16], hw[4 * c16 + 1], hw[4 * c16 + 2], hw[4 * c16 + 3]);
+          const uint4 Lw = make_uint4(lw[4 * c16], lw[4 * c16 + 1], lw[4 * c16 + 2], lw[4 * c16 + 3]);
+          *reinterpret_cast<uint4*>(sB + core_off_b<RB>(r, 16 * c16)) = H;
+          *reinterpret_cast<uint4*>(sB + core_off_b<RB>(r, KPAD + 16 * c16)) = H;
+          *reinterpret_cast<uint4*>(sB + core_off_b<RB>(r, 2 * KPAD + 16 * c16)) = Lw;
+        }
+#pragma unroll
+        for (int kb = 3 * KPAD; kb < RB; kb += 16) *reinterpret_cast<uint4*>(sB + core_off_b<RB>(r, kb)) = make_uint4(0u, 0u, 0u, 0u);
       }
 #pragma unroll
       for (int j = 0; j < KPAD; j += 4)
@@ -366,31 +442,67 @@ __global__ void __launch_bounds__(kTcThreads) leaf_tc_kernel(TcLeafArgs a) {
 #pragma unroll
         for (int j = 0; j < KPAD; ++j) qf[j] = (qi >= 0 && j < d) ? __ldg(a.Q + (size_t)qi * d + j) : 0.f;
       }
-      float ac2 = 0.f, amax = 0.f;
+      float ac2 = 0.f, amax = 0.f, sa = 1.f;
+      if constexpr (PREC != 2) {
 #pragma unroll
-      for (int k8 = 0; k8 < KPAD; k8 += 8) {
-        float hi[8], lo[8];
+        for (int k8 = 0; k8 < KPAD; k8 += 8) {
+          float hi[8], lo[8];
 #pragma unroll
-        for (int u = 0; u < 8; ++u) {
-          const float t = (qi >= 0 && k8 + u < d) ? qf[k8 + u] - sC[k8 + u] : 0.f;
-          ac2 = fmaf(t, t, ac2);
-          amax = fmaxf(amax, fabsf(t));
-          PR::split(t, hi[u], lo[u]);
+          for (int u = 0; u < 8; ++u) {
+            const float t = (qi >= 0 && k8 + u < d) ? qf[k8 + u] - sC[k8 + u] : 0.f;
+            ac2 = fmaf(t, t, ac2);
+            amax = fmaxf(amax, fabsf(t));
+            PR::split(t, hi[u], lo[u]);
+          }
+          uint4 wh, wl;
+          wh.x = PR::pack(hi[0], hi[1]);
+          wh.y = PR::pack(hi[2], hi[3]);
+          wh.z = PR::pack(hi[4], hi[5]);
+          wh.w = PR::pack(hi[6], hi[7]);
+          wl.x = PR::pack(lo[0], lo[1]);
+          wl.y = PR::pack(lo[2], lo[3]);
+          wl.z = PR::pack(lo[4], lo[5]);
+          wl.w = PR::pack(lo[6], lo[7]);
+          *reinterpret_cast<uint4*>(sA + tc::core_offset(tid, k8, KT)) = wh;
+          if constexpr (PR::kSplit == 3) {
+            *reinterpret_cast<uint4*>(sA + tc::core_offset(tid, KPAD + k8, KT)) = wl;
+            *reinterpret_cast<uint4*>(sA + tc::core_offset(tid, 2 * KPAD + k8, KT)) = wh;
+          }
         }
-        uint4 wh, wl;
-        wh.x = PR::pack(hi[0], hi[1]);
-        wh.y = PR::pack(hi[2], hi[3]);
-        wh.z = PR::pack(hi[4], hi[5]);
-        wh.w = PR::pack(hi[6], hi[7]);
-        wl.x = PR::pack(lo[0], lo[1]);
-        wl.y = PR::pack(lo[2], lo[3]);
-        wl.z = PR::pack(lo[4], lo[5]);
-        wl.w = PR::pack(lo[6], lo[7]);
-        *reinterpret_cast<uint4*>(sA + tc::core_offset(tid, k8, KT)) = wh;
-        if constexpr (PR::kSplit == 3) {
-          *reinterpret_cast<uint4*>(sA + tc::core_offset(tid, KPAD + k8, KT)) = wl;
-          *reinterpret_cast<uint4*>(sA + tc::core_offset(tid, 2 * KPAD + k8, KT)) = wh;
+      } else {  // FP8: [hi | lo | hi] of the scaled centred query, zero bytes up to RB
+        float tq[KPAD];
+#pragma unroll
+        for (int u = 0; u < KPAD; ++u) {
+          tq[u] = (qi >= 0 && u < d) ? qf[u] - sC[u] : 0.f;
+          ac2 = fmaf(tq[u], tq[u], ac2);
+          amax = fmaxf(amax, fabsf(tq[u]));
         }
+        sa = pow2_scale_256(amax);
+        uint32_t hw[KPAD / 4], lw[KPAD / 4];
+#pragma unroll
+        for (int j4 = 0; j4 < KPAD / 4; ++j4) {
+          uint32_t h4 = 0, l4 = 0;
+#pragma unroll
+          for (int u = 0; u < 4; ++u) {
+            const float v = tq[4 * j4 + u] * sa;
+            const uint8_t h = PR::q8(v), lq = PR::q8(v - PR::f8(h));
+            h4 |= (uint32_t)h << (8 * u);
+            l4 |= (uint32_t)lq << (8 * u);
+          }
+          hw[j4] = h4;
+          lw[j4] = l4;
+        }
+#pragma unroll
+        for (int c16 = 0; c16 < KPAD / 16; ++c16) {
+          const uint4 H = make_uint4(hw[4 * c16], hw[4 * c16 + 1], hw[4 * c16 + 2], hw[4 * c16 + 3]);
+          const uint4 Lw = make_uint4(lw[4 * c16], lw[4 * c16 + 1], lw[4 * c16 + 2], lw[4 * c16 + 3]);
+          *reinterpret_cast<uint4*>(sA + core_off_b<RB>(tid, 16 * c16)) = H;
+          *reinterpret_cast<uint4*>(sA + core_off_b<RB>(tid, KPAD + 16 * c16)) = Lw;
+          *reinterpret_cast<uint4*>(sA + core_off_b<RB>(tid, 2 * KPAD + 16 * c16)) = H;
+        }
+#pragma unroll
+        for (int kb = 3 * KPAD; kb < RB; kb += 16)
+          *reinterpret_cast<uint4*>(sA + core_off_b<RB>(tid, kb)) = make_uint4(0u, 0u, 0u, 0u);
       }
       tc::fence_async_smem();
       tc::fence_before_sync();
@@ -398,10 +510,13 @@ __global__ void __launch_bounds__(kTcThreads) leaf_tc_kernel(TcLeafArgs a) {
       if (tid == 0) {
         tc::fence_after_sync();
 #pragma unroll
-        for (int kk = 0; kk < KT / 16; ++kk) {
-          const uint64_t ad = tc::sdesc(sA + kk * 256, 128, (KT / 8) * 128);
-          const uint64_t bd = tc::sdesc(sB + kk * 256, 128, (KT / 8) * 128);
-          tc::mma_bf16(tmem, ad, bd, idesc, kk > 0 ? 1u : 0u);
+        for (int kk = 0; kk < RB / 32; ++kk) {  // one MMA per 32 bytes of K
+          const uint64_t ad = tc::sdesc(sA + kk * 256, 128, (RB / 16) * 128);
+          const uint64_t bd = tc::sdesc(sB + kk * 256, 128, (RB / 16) * 128);
+          if constexpr (PREC == 2)
+            tc::mma_f8(tmem, ad, bd, idesc, kk > 0 ? 1u : 0u);
+          else
+            tc::mma_bf16(tmem, ad, bd, idesc, kk > 0 ? 1u : 0u);
         }
         tc::mma_commit(mbar);
       }
@@ -413,6 +528,8 @@ __global__ void __launch_bounds__(kTcThreads) leaf_tc_kernel(TcLeafArgs a) {
         break;
       }
       tc::fence_after_sync();
+      // the tile holds dot products of scaled vectors (FP8: powers of two, exact to undo)
+      const float dsc = PREC == 2 ? -2.f / (sa * sC[KPAD + 1]) : -2.f;
       // pass 1: the KM smallest estimates (padding columns carry sN = FLT_MAX)
       float ev[KM];
 #pragma unroll
@@ -422,7 +539,7 @@ __global__ void __launch_bounds__(kTcThreads) leaf_tc_kernel(TcLeafArgs a) {
         tc::tmem_ld16(trow + (uint32_t)c0, r);
         tc::tmem_wait_ld();
 #pragma unroll
-        for (int j = 0; j < 16; ++j) smallest_insert<KM>(ev, fmaf(-2.f, __uint_as_float(r[j]), sN[c0 + j]));
+        for (int j = 0; j < 16; ++j) smallest_insert<KM>(ev, fmaf(dsc, __uint_as_float(r[j]), sN[c0 + j]));
       }
       // band: est_j <= est_(k) + 2 delta, delta = 2 kDot |a-c| R + FP32 slack
       float evk = FLT_MAX;
@@ -430,7 +547,11 @@ __global__ void __launch_bounds__(kTcThreads) leaf_tc_kernel(TcLeafArgs a) {
       for (int j = 0; j < KM; ++j)
         if (j == K - 1) evk = ev[j];
       const float acn = sqrtf(ac2) * 1.000001f;
-      const float delta = 2.f * PR::kDot * acn * R + 4e-6f * (ac2 + R * R + fabsf(evk));
+      float delta = 2.f * PR::kDot * acn * R + 4e-6f * (ac2 + R * R + fabsf(evk));
+      if constexpr (PREC == 2) {  // FP8: the subnormal-step terms, back in unscaled units
+        const float sb = sC[KPAD + 1];
+        delta += 2.f * (PR::kAbs * sqrtf((float)d) * (acn / sb + R / sa) + PR::kConst * (float)d / (sa * sb));
+      }
       // FP16 cannot hold centred values beyond its range: such queries and leaves take every point
       const bool unsafe = PREC == 1 && (amax > 60000.f || R > 60000.f);
       const float tau = (evk >= FLT_MAX || unsafe) ? FLT_MAX : evk + 2.f * delta;
@@ -450,7 +571,7 @@ __global__ void __launch_bounds__(kTcThreads) leaf_tc_kernel(TcLeafArgs a) {
           unsigned pass = 0;
 #pragma unroll
           for (int j = 0; j < 16; ++j) {
-            const float est = fmaf(-2.f, __uint_as_float(r[j]), sN[c0 + j]);
+            const float est = fmaf(dsc, __uint_as_float(r[j]), sN[c0 + j]);
             pass |= (c0 + j < np && (est <= tau || tau == FLT_MAX)) ? (1u << j) : 0u;
           }
           while (pass) {
@@ -567,8 +688,10 @@ int natural_knn_tc(annf_handle* h, const float* Q, long long nq, int K, int prec
   args.out_pos = out_pos;
   args.item_leaf = item_leaf;
   const int kpad = h->d <= 16 ? 16 : 32;
-  const int kt = (prec == 0 ? 3 : 1) * kpad;  // K extent of the tiles (BF16 hi/lo split: 3 terms)
-  const size_t carve = (size_t)kTcThreads * kt * 2 + (size_t)args.npad * kt * 2 + (size_t)args.npad * kpad * 4 +
+  // tile row bytes: K extent (BF16 / FP8 hi-lo splits: 3 terms) times the element size, in whole
+  // 32-byte MMA K steps (the kernel's RB)
+  const int rb = ((prec == 1 ? 1 : 3) * kpad * (prec == 2 ? 1 : 2) + 31) / 32 * 32;
+  const size_t carve = (size_t)kTcThreads * rb + (size_t)args.npad * rb + (size_t)args.npad * kpad * 4 +
                        (size_t)args.npad * 4 + (kpad + 4) * 4 + 16 + 24 + 64;
   // at most 512 / ncols CTAs may hold TMEM on one SM: pad the shared memory so no more fit
   const int per_sm = std::max(1, 512 / args.ncols);
@@ -583,8 +706,10 @@ int natural_knn_tc(annf_handle* h, const float* Q, long long nq, int K, int prec
   case KMV:                                                                                            \
     if (prec == 0)                                                                                     \
       rc = kpad == 16 ? launch_leaf_tc<KMV, 16, 0>(args, smem, grid, st) : launch_leaf_tc<KMV, 32, 0>(args, smem, grid, st); \
-    else                                                                                               \
+    else if (prec == 1)                                                                                \
       rc = kpad == 16 ? launch_leaf_tc<KMV, 16, 1>(args, smem, grid, st) : launch_leaf_tc<KMV, 32, 1>(args, smem, grid, st); \
+    else                                                                                               \
+      rc = kpad == 16 ? launch_leaf_tc<KMV, 16, 2>(args, smem, grid, st) : launch_leaf_tc<KMV, 32, 2>(args, smem, grid, st); \
     break;
   switch (km) {
     ANNF_TC_LAUNCH(1)

@@ -343,11 +343,12 @@ class ANNFieldPropKDTreeGB300:
                 if prop is not None:
                     prop.record_stream(torch.cuda.current_stream(dev))
             lp = self.leaf_precision or "bf16"
-            if lp not in ("bf16", "fp16", "fp32"):
-                raise ValueError("leaf_precision must be 'bf16', 'fp16' or 'fp32'")
+            if lp not in ("bf16", "fp16", "fp8", "fp32"):
+                raise ValueError("leaf_precision must be 'bf16', 'fp16', 'fp8' or 'fp32'")
             if lp != "fp32" and real != torch.float32:
                 raise ValueError("tensor-core leaf distances need float_type='float'")
-            lpc = {"bf16": _lib.ANNF_LEAF_BF16, "fp16": _lib.ANNF_LEAF_FP16, "fp32": _lib.ANNF_LEAF_EXACT}[lp]
+            lpc = {"bf16": _lib.ANNF_LEAF_BF16, "fp16": _lib.ANNF_LEAF_FP16, "fp8": _lib.ANNF_LEAF_FP8,
+                   "fp32": _lib.ANNF_LEAF_EXACT}[lp]
             if seeded:  # the proposals' best match, found on the side stream
                 h.call("annf_parallel_nnf_seeded", ptr(nn), ptr(A), ha, wa, ptr(B), hb, wb, c, p,
                        ptr(self.patches_a_reduced_), k, ptr(prop), int(self.iters), int(self.seed) & 0xFFFFFFFF, lpc,

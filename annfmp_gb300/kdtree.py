@@ -127,7 +127,8 @@ class KDTree(object):
         numpy_out = is_numpy(X)
         Q = to_device(X, self._torch_dtype(), self._dev)
         k = int(n_neighbors or self.n_neighbors)
-        prec = {"fp32": _lib.ANNF_LEAF_EXACT, "bf16": _lib.ANNF_LEAF_BF16, "fp16": _lib.ANNF_LEAF_FP16}[leaf_precision]
+        prec = {"fp32": _lib.ANNF_LEAF_EXACT, "bf16": _lib.ANNF_LEAF_BF16, "fp16": _lib.ANNF_LEAF_FP16,
+                "fp8": _lib.ANNF_LEAF_FP8}[leaf_precision]
         pos = torch.empty((Q.shape[0], k), dtype=torch.int32, device=self._dev)
         self.handle.call("annf_natural_knn", ptr(Q), Q.shape[0], k, prec, ptr(pos), stream_ptr(self._dev))
         tv = self.handle.tree_view()

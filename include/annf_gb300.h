@@ -46,6 +46,7 @@ extern "C" {
 #define ANNF_LEAF_EXACT 0 /* FP32/FP64 with the reference's summation order */
 #define ANNF_LEAF_BF16 1  /* BF16 tensor-core tiles (FP32 accumulate) + exact FP32 re-rank of the survivors */
 #define ANNF_LEAF_FP16 2  /* the same with FP16 tiles (tighter bound, fewer survivors) */
+#define ANNF_LEAF_FP8 3   /* FP8 (E4M3) hi/lo split tiles with power-of-two scales (wider bound, more survivors) */
 
 typedef struct annf_handle annf_handle;
 

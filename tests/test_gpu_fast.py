@@ -82,19 +82,26 @@ def test_tc_tile_random_bf16(gpu_lib):
 # natural-leaf kNN: BF16 tensor-core tiles + FP32 re-rank vs the exact FP32 leaf scan
 # ---------------------------------------------------------------------------------------------
 @pytest.mark.parametrize("n,d,leaf,k,quant", [(60000, 16, 64, 4, 0), (40000, 8, 32, 1, 0), (30000, 6, 8, 3, 0),
-                                              (50000, 24, 64, 8, 0), (20000, 12, 32, 2, 0), (60000, 16, 64, 4, 8)])
+                                              (50000, 24, 64, 8, 0), (20000, 12, 32, 2, 0), (60000, 16, 64, 4, 8),
+                                              (40000, 16, 64, 4, -1)])
 def test_natural_knn_bf16_vs_fp32(gpu_lib, n, d, leaf, k, quant):
-    """The BF16 tiles only filter: every point within the proven BF16 error bound of the k-th best
-    estimate is re-ranked exactly in FP32, so the k-lists equal the FP32 leaf scan's."""
+    """The BF16, FP16 and FP8 tiles only filter: every point within the tiles' proven error bound
+    of the k-th best estimate is re-ranked exactly in FP32, so the k-lists equal the FP32 leaf
+    scan's. quant > 0: a coarse grid (many exact ties); quant < 0: coordinates from 1e-3 to 1e4
+    (FP8's subnormal range)."""
     import torch
     from annfmp_gb300 import KDTree
     rng = np.random.default_rng(n + d)
     # reduced-patch-like data: offset, anisotropic scales
     X = (rng.standard_normal((n, d)) * (300.0 / (1 + np.arange(d))) + 500.0).astype(np.float32)
     Qn = (X[rng.integers(0, n, 8000)] + rng.standard_normal((8000, d)).astype(np.float32) * 3).astype(np.float32)
-    if quant:  # coarse grid: many exactly tied distances
+    if quant > 0:  # coarse grid: many exactly tied distances
         X = (np.round(X / quant) * quant).astype(np.float32)
         Qn = (np.round(Qn / quant) * quant).astype(np.float32)
+    elif quant < 0:  # per-dimension scales over seven decades
+        sc = (10.0 ** np.linspace(-3, 4, d)).astype(np.float32)
+        X = (X * sc / 300.0).astype(np.float32)
+        Qn = (Qn * sc / 300.0).astype(np.float32)
     t = KDTree(n_neighbors=k, leaf_size=leaf, float_type="float", splitting_type="longest").fit(torch.from_numpy(X).cuda())
     Q = torch.from_numpy(Qn).cuda()
     i32 = t.natural_kneighbors(Q, k, "fp32").cpu().numpy()
@@ -103,6 +110,9 @@ def test_natural_knn_bf16_vs_fp32(gpu_lib, n, d, leaf, k, quant):
     assert same.all(), (same.mean(), np.nonzero(~same)[0][:10])
     ih = t.natural_kneighbors(Q, k, "fp16").cpu().numpy()
     assert np.array_equal(ih, i32)
+    i8 = t.natural_kneighbors(Q, k, "fp8").cpu().numpy()
+    same8 = (i8 == i32).all(axis=1)
+    assert same8.all(), (same8.mean(), np.nonzero(~same8)[0][:10])
 
     def d2(idx):
         diff = X[idx].astype(np.float64) - Qn[:, None, :].astype(np.float64)

@@ -35,3 +35,16 @@ def test_parallel_form_quality(gpu_lib):
     err_0 = metrics.distance_ratio_error(a, b, nn_0, 7, n_samples=2048, seed=3)
     assert err_p["mean"] <= err_0["mean"] + 1e-9, (err_p, err_0)
     assert err_p["mean"] < 0.05, err_p
+
+
+@pytest.mark.parametrize("leaf_precision", ["fp8", "fp16"])
+def test_parallel_form_other_leaf_precisions(gpu_lib, leaf_precision):
+    """The natural-leaf k-lists do not depend on the tile precision (exact FP32 re-rank behind each
+    tile's proven bound), so the whole NNF equals the BF16 one."""
+    from annfmp_gb300 import ANNFieldPropKDTreeGB300, gen
+    a, b = gen.pair_flow(12, 176, magnitude=6.0, sigma=24.0)
+    kw = dict(n_neighbors=4, psize=7, dim_reduced=8, n_subset=6000, leaf_size=32, seed=0, verbose=0,
+              form="parallel", iters=2, graph=False)
+    ref = ANNFieldPropKDTreeGB300(leaf_precision="bf16", **kw).fit(a, b)
+    got = ANNFieldPropKDTreeGB300(leaf_precision=leaf_precision, **kw).fit(a, b)
+    assert np.array_equal(ref, got)
