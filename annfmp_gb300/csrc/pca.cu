@@ -394,6 +394,8 @@ __global__ void __launch_bounds__(kPTW * kPTH) project_kernel(const uint8_t* __r
 static int round_up(int a, int b) { return (a + b - 1) / b * b; }
 
 int subspace_block(int P, int ncomp);
+bool gram_tc_supported(int F, int ns_pad);
+int gram_tc(const uint8_t* XT, int F, int ns_pad, unsigned long long* G, unsigned* status, cudaStream_t st);
 int eig_top_subspace(annf_handle* h, const double* C, int P, int ncomp, int iters, double* comps, cudaStream_t st);
 
 int pca_fit(annf_handle* h, const uint8_t* img_a, int ha, int wa, const int* pos_a, int n_a, const uint8_t* img_b,
@@ -407,7 +409,7 @@ int pca_fit(annf_handle* h, const uint8_t* img_a, int ha, int wa, const int* pos
   ANNF_REQUIRE(ncomp >= 1 && ncomp <= P, "annf_pca_fit: n_components out of range");
   ANNF_REQUIRE(P + 1 <= 4096, "annf_pca_fit: patch too large");
   const int F = P + 1;
-  const int ns_pad = round_up(ns, 4);
+  const int ns_pad = round_up(ns, 64);  // whole 64-sample blocks for the tensor-core Gram
   const int nwords = ns_pad / 4;
   ANNF_ENSURE(h->subset_t, (size_t)F * ns_pad);
   ANNF_ENSURE(h->gram, (size_t)F * F * sizeof(unsigned long long));
@@ -427,11 +429,17 @@ int pca_fit(annf_handle* h, const uint8_t* img_a, int ha, int wa, const int* pos
   }
   ANNF_CHECK_LAUNCH();
   ANNF_CUDA_TRY(cudaMemsetAsync(h->gram.p, 0, (size_t)F * F * sizeof(unsigned long long), st));
-  const int tiles = ceil_div(F, kGT);
-  dim3 g(tiles, tiles, ceil_div(nwords, kGramSplitWords));
-  gram_kernel<<<g, 256, 0, st>>>(reinterpret_cast<const unsigned*>(h->subset_t.p), F, nwords,
-                                 h->gram.as<unsigned long long>());
-  ANNF_CHECK_LAUNCH();
+  if (gram_tc_supported(F, ns_pad)) {  // tensor cores, exact (nibble split); same integers
+    const int rc = gram_tc(h->subset_t.as<uint8_t>(), F, ns_pad, h->gram.as<unsigned long long>(),
+                           h->status.as<unsigned>(), st);
+    if (rc != ANNF_OK) return rc;
+  } else {
+    const int tiles = ceil_div(F, kGT);
+    dim3 g(tiles, tiles, ceil_div(nwords, kGramSplitWords));
+    gram_kernel<<<g, 256, 0, st>>>(reinterpret_cast<const unsigned*>(h->subset_t.p), F, nwords,
+                                   h->gram.as<unsigned long long>());
+    ANNF_CHECK_LAUNCH();
+  }
   prof_mark(h, "pca_gram", st);
   cov_finish_kernel<<<std::min(ceil_div((long long)P * P, 256), 1024), 256, 0, st>>>(
       h->gram.as<unsigned long long>(), F, P, h->cov.as<double>(), mean);

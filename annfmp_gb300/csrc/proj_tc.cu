@@ -57,24 +57,6 @@ __global__ void pj_prep_kernel(const double* __restrict__ comps, const double* _
   }
 }
 
-// eight FP16 values of eight consecutive bytes (w0 = bytes 0..3, w1 = bytes 4..7): a byte permute
-// pairs each byte b with the byte 0x64, giving the half 1024 + b (bits 0x64bb, exact: 1024 + b <
-// 2048), and one packed subtraction of 1024 leaves b exactly. Bytes past the patch row meet zero
-// components in the B tile, so they need no masking.
-__device__ __forceinline__ uint4 bytes_to_f16x8(uint32_t w0, uint32_t w1) {
-  constexpr uint32_t kMagic = 0x64646464u;
-  const __half2 k1024 = __halves2half2(__ushort_as_half((unsigned short)0x6400), __ushort_as_half((unsigned short)0x6400));
-  const uint32_t p[4] = {__byte_perm(w0, kMagic, 0x4140), __byte_perm(w0, kMagic, 0x4342),
-                         __byte_perm(w1, kMagic, 0x4140), __byte_perm(w1, kMagic, 0x4342)};
-  uint32_t o[4];
-#pragma unroll
-  for (int u = 0; u < 4; ++u) {
-    const __half2 h = __hsub2(*reinterpret_cast<const __half2*>(&p[u]), k1024);
-    o[u] = *reinterpret_cast<const uint32_t*>(&h);
-  }
-  return make_uint4(o[0], o[1], o[2], o[3]);
-}
-
 // 4-byte asynchronous global -> shared copy (both addresses 4-byte aligned), and its group fences
 __device__ __forceinline__ void cp_async4(void* sdst, const void* gsrc) {
   asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(tc::smem_addr(sdst)), "l"(gsrc) : "memory");
@@ -188,7 +170,7 @@ __global__ void __launch_bounds__(kPjThreads) project_tc_kernel(const uint8_t* _
         const uint32_t* wp = reinterpret_cast<const uint32_t*>(sI + (off & ~3));
         const int sh = (off & 3) * 8;
         const uint32_t q0 = wp[0], q1 = wp[1], q2 = wp[2];
-        w = bytes_to_f16x8(__funnelshift_r(q0, q1, sh), __funnelshift_r(q1, q2, sh));
+        w = tc::bytes_to_f16x8(__funnelshift_r(q0, q1, sh), __funnelshift_r(q1, q2, sh));
       }
       *reinterpret_cast<uint4*>(sA + tc::core_offset(row, g * 8, kpad)) = w;
     }

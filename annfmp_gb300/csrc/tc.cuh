@@ -7,6 +7,8 @@
 // the caller records an error status, frees its TMEM and returns.
 #pragma once
 
+#include <cuda_fp16.h>
+
 #include <stdint.h>
 
 namespace annf {
@@ -130,6 +132,24 @@ __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.
 // 8-row groups outermost: core (r/8, k/8) at ((r/8) * (K/8) + k/8) * 128, row r%8 at 16 B steps
 __host__ __device__ __forceinline__ uint32_t core_offset(int r, int k, int K) {
   return (uint32_t)(((r >> 3) * (K >> 3) + (k >> 3)) * 128 + (r & 7) * 16 + (k & 7) * 2);
+}
+
+// eight FP16 values of eight consecutive bytes (w0 = bytes 0..3, w1 = bytes 4..7): a byte permute
+// pairs each byte b with the byte 0x64, giving the half 1024 + b (bits 0x64bb, exact: 1024 + b <
+// 2048), and one packed subtraction of 1024 leaves b exactly. Bytes past the patch row meet zero
+// components in the B tile, so they need no masking (callers decide what the bytes meet).
+__device__ __forceinline__ uint4 bytes_to_f16x8(uint32_t w0, uint32_t w1) {
+  constexpr uint32_t kMagic = 0x64646464u;
+  const __half2 k1024 = __halves2half2(__ushort_as_half((unsigned short)0x6400), __ushort_as_half((unsigned short)0x6400));
+  const uint32_t p[4] = {__byte_perm(w0, kMagic, 0x4140), __byte_perm(w0, kMagic, 0x4342),
+                         __byte_perm(w1, kMagic, 0x4140), __byte_perm(w1, kMagic, 0x4342)};
+  uint32_t o[4];
+#pragma unroll
+  for (int u = 0; u < 4; ++u) {
+    const __half2 h = __hsub2(*reinterpret_cast<const __half2*>(&p[u]), k1024);
+    o[u] = *reinterpret_cast<const uint32_t*>(&h);
+  }
+  return make_uint4(o[0], o[1], o[2], o[3]);
 }
 
 }  // namespace tc
