@@ -1,11 +1,12 @@
 // gram_tc.cu -- the exact Gram matrix of the PCA subset on the tensor cores (sm_103a).
 //
-// G = X^T X over n uint8 samples of F features (feature-major XT [F][ns_pad], ns_pad a multiple of
-// 64; feature P is the row of ones, so G also holds the column sums and n). Every sample byte x is
+// G = X^T X over n uint8 samples of F features (blocked layout XB [ns_pad / 64][F][64]: per block
+// of 64 samples, each feature's 64 bytes are contiguous; feature P is the row of ones, so G also
+// holds the column sums and n). Every sample byte x is
 // split into nibbles x = 16 h + l. A tile of 128 features of X (FP16, exact: 0..255) times 128
 // features of H and of L (FP16, exact: 0..15) gives XH and XL; every product is at most
 // 255 * 15 = 3825 and an FP32 sum of such integers is exact below 2^24, so a task sums at most
-// 4096 samples (4096 * 3825 < 2^24) in TMEM and adds G = 16 XH + XL to the 64-bit Gram with
+// 4352 samples (4352 * 3825 < 2^24) in TMEM and adds G = 16 XH + XL to the 64-bit Gram with
 // atomics. tcgen05.mma kind::f16, M = N = 128, both accumulators FP32 in TMEM (256 columns), two
 // staging buffers so that the next 64 samples are converted while the tensor cores run.
 // Bit-identical to the integer dp4a Gram (pca.cu), which remains for F > 256.
@@ -23,7 +24,7 @@ int num_sms();
 
 constexpr int kGtThreads = 128;     // thread t <-> feature row t of the tile <-> TMEM lane t
 constexpr int kGtK = 64;            // samples per staged block
-constexpr int kGtChunk = 4096;      // samples per task: 4096 * 255 * 15 < 2^24
+constexpr int kGtChunkMax = 4352;   // samples per task at most: 4352 * 255 * 15 < 2^24
 constexpr int kGtTile = 128 * kGtK * 2;  // bytes of one FP16 operand tile (128 rows x 64 samples)
 constexpr long long kGtWaitCycles = 2000000000LL;
 
@@ -43,7 +44,7 @@ __device__ __forceinline__ void nibbles_f16(uint32_t w0, uint32_t w1, uint4& hi,
 
 // one task: features [128 ha, 128 ha + 128) x [128 hb, 128 hb + 128) over samples [s0, s1)
 __global__ void __launch_bounds__(kGtThreads) gram_tc_kernel(const uint8_t* __restrict__ XT, int F, int ns_pad,
-                                                             int nchunks, int npairs,
+                                                             int chunk_len, int nchunks, int npairs,
                                                              unsigned long long* __restrict__ G, unsigned* status) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char* p = smem_raw;
@@ -93,23 +94,39 @@ __global__ void __launch_bounds__(kGtThreads) gram_tc_kernel(const uint8_t* __re
       ++ha;
     }
     const int hb = ha + rem;
-    const int s0 = chunk * kGtChunk, s1 = min(ns_pad, s0 + kGtChunk);
+    const int s0 = chunk * chunk_len, s1 = min(ns_pad, s0 + chunk_len);
     const int nblk = (s1 - s0) / kGtK;
     const int fa = ha * 128 + tid, fb = hb * 128 + tid;
+    // this thread's two feature rows of a block (64 samples each); the next block's are loaded
+    // while the current one is converted
+    auto load_block = [&](int blk, uint4 (&xa)[4], uint4 (&xb)[4]) {
+      const size_t gb = (size_t)(s0 / kGtK + blk) * F;  // this block's feature rows, 64 bytes each
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        xa[q] = fa < F ? __ldg(reinterpret_cast<const uint4*>(XT + (gb + fa) * kGtK) + q) : make_uint4(0u, 0u, 0u, 0u);
+        xb[q] = ha == hb ? xa[q]
+                         : (fb < F ? __ldg(reinterpret_cast<const uint4*>(XT + (gb + fb) * kGtK) + q)
+                                   : make_uint4(0u, 0u, 0u, 0u));
+      }
+    };
+    // two blocks in flight ahead of the one being converted
+    uint4 na[4], nb[4], n2a[4], n2b[4];
+    if (nblk > 0) load_block(0, na, nb);
+    if (nblk > 1) load_block(1, n2a, n2b);
     for (int blk = 0; blk < nblk; ++blk) {
       const int buf = blk & 1;
-      if (blk >= 2) {  // the MMAs that read this buffer (block blk - 2) are done
-        if (!gt_wait(&mbar[buf], ph[buf])) sflag[0] = 1;
-        ph[buf] ^= 1u;
-      }
-      const int sb = s0 + blk * kGtK;
       uint4 xa[4], xb[4];
 #pragma unroll
       for (int q = 0; q < 4; ++q) {
-        xa[q] = fa < F ? __ldg(reinterpret_cast<const uint4*>(XT + (size_t)fa * ns_pad + sb) + q) : make_uint4(0u, 0u, 0u, 0u);
-        xb[q] = ha == hb ? xa[q]
-                         : (fb < F ? __ldg(reinterpret_cast<const uint4*>(XT + (size_t)fb * ns_pad + sb) + q)
-                                   : make_uint4(0u, 0u, 0u, 0u));
+        xa[q] = na[q];
+        xb[q] = nb[q];
+        na[q] = n2a[q];
+        nb[q] = n2b[q];
+      }
+      if (blk + 2 < nblk) load_block(blk + 2, n2a, n2b);
+      if (blk >= 2) {  // the MMAs that read this buffer (block blk - 2) are done
+        if (!gt_wait(&mbar[buf], ph[buf])) sflag[0] = 1;
+        ph[buf] ^= 1u;
       }
 #pragma unroll
       for (int q = 0; q < 4; ++q) {  // samples 16q .. 16q + 15
@@ -193,12 +210,18 @@ bool gram_tc_supported(int F, int ns_pad) { return F >= 1 && F <= 256 && ns_pad 
 int gram_tc(const uint8_t* XT, int F, int ns_pad, unsigned long long* G, unsigned* status, cudaStream_t st) {
   ANNF_REQUIRE(gram_tc_supported(F, ns_pad), "tensor-core Gram: unsupported shape");
   const int nh = (F + 127) / 128, npairs = nh * (nh + 1) / 2;
-  const int nchunks = (ns_pad + kGtChunk - 1) / kGtChunk;
+  // chunks (whole 64-sample blocks, at most kGtChunkMax) so that all tasks fit one wave of
+  // two CTAs per SM when the samples allow
+  const int slots = std::max(1, (2 * num_sms()) / npairs);
+  int chunk_len = (int)std::min<long long>(kGtChunkMax, ((long long)ns_pad + slots - 1) / slots);
+  chunk_len = std::max(kGtK, (chunk_len + kGtK - 1) / kGtK * kGtK);
+  if (chunk_len > kGtChunkMax) chunk_len = kGtChunkMax / kGtK * kGtK;
+  const int nchunks = (ns_pad + chunk_len - 1) / chunk_len;
   const size_t smem = 6 * (size_t)kGtTile + 16 + 8 + 8 + 64;
   ANNF_CUDA_TRY(cudaFuncSetAttribute(gram_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   const long long ntasks = (long long)npairs * nchunks;
   const int grid = (int)std::max(1LL, std::min<long long>(ntasks, 2LL * num_sms()));  // two per SM by TMEM
-  gram_tc_kernel<<<grid, kGtThreads, smem, st>>>(XT, F, ns_pad, nchunks, npairs, G, status);
+  gram_tc_kernel<<<grid, kGtThreads, smem, st>>>(XT, F, ns_pad, chunk_len, nchunks, npairs, G, status);
   ANNF_CHECK_LAUNCH();
   return ANNF_OK;
 }

@@ -65,13 +65,15 @@ __global__ void gather_subset_kernel(const uint8_t* __restrict__ img_a, int wa, 
   }
 }
 
-// Same layout, built 64 samples per block: whole patch rows are copied from the image into shared
-// memory, then every feature row of XT is written with coalesced stores (for F <= 1024).
+// Same contents, built 64 samples per block: whole patch rows are copied from the image into shared
+// memory, then written with coalesced stores (for F <= 1024). blocked = 0: XT [F][ns_pad];
+// blocked = 1: [ns_pad / 64][F][64] (each block's feature rows are contiguous 64-byte runs, the
+// tensor-core Gram's read order).
 constexpr int kGatherS = 64;
 __global__ void __launch_bounds__(256) gather_subset_tiled_kernel(
     const uint8_t* __restrict__ img_a, int wa, const int* __restrict__ pos_a, int n_a, const uint8_t* __restrict__ img_b,
-    int wb, const int* __restrict__ pos_b, int n_b, int c, int psize, int F, int ns_pad, uint8_t* __restrict__ XT,
-    unsigned* status) {
+    int wb, const int* __restrict__ pos_b, int n_b, int c, int psize, int F, int ns_pad, int blocked,
+    uint8_t* __restrict__ XT, unsigned* status) {
   extern __shared__ __align__(16) uint8_t sp[];  // [kGatherS][F]
   if (smem_overrun(sp, sp + (size_t)kGatherS * F, status)) return;
   const int P = psize * psize * c, rowlen = psize * c, ns = n_a + n_b;
@@ -101,7 +103,10 @@ __global__ void __launch_bounds__(256) gather_subset_tiled_kernel(
     uint8_t v = 0;
     if (f < P) v = sp[(size_t)i * F + f];
     else if (f == P) v = s < ns ? 1 : 0;
-    XT[(long long)f * ns_pad + s] = v;
+    if (blocked)
+      XT[((long long)blockIdx.x * F + f) * kGatherS + i] = v;
+    else
+      XT[(long long)f * ns_pad + s] = v;
   }
 }
 
@@ -417,19 +422,20 @@ int pca_fit(annf_handle* h, const uint8_t* img_a, int ha, int wa, const int* pos
   ANNF_ENSURE(h->eigval, (size_t)P * sizeof(double));
   ANNF_ENSURE(h->solver_info, sizeof(int));
   prof_mark(h, "pca:begin", st);
+  const bool tc_gram = gram_tc_supported(F, ns_pad);  // tensor cores (exact, nibble split)
   if (F <= 1024) {
     const size_t gsm = (size_t)kGatherS * F;
     ANNF_CUDA_TRY(cudaFuncSetAttribute(gather_subset_tiled_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gsm));
     gather_subset_tiled_kernel<<<ceil_div(ns_pad, kGatherS), 256, gsm, st>>>(
-        img_a, wa, pos_a, n_a, img_b, wb, pos_b, n_b, c, psize, F, ns_pad, h->subset_t.as<uint8_t>(),
-        h->status.as<unsigned>());
+        img_a, wa, pos_a, n_a, img_b, wb, pos_b, n_b, c, psize, F, ns_pad, tc_gram ? 1 : 0,
+        h->subset_t.as<uint8_t>(), h->status.as<unsigned>());
   } else {
     gather_subset_kernel<<<std::min(ceil_div((long long)F * ns_pad, 256), 8192), 256, 0, st>>>(
         img_a, wa, pos_a, n_a, img_b, wb, pos_b, n_b, c, psize, F, ns_pad, h->subset_t.as<uint8_t>());
   }
   ANNF_CHECK_LAUNCH();
   ANNF_CUDA_TRY(cudaMemsetAsync(h->gram.p, 0, (size_t)F * F * sizeof(unsigned long long), st));
-  if (gram_tc_supported(F, ns_pad)) {  // tensor cores, exact (nibble split); same integers
+  if (tc_gram) {  // same integers as the dp4a Gram
     const int rc = gram_tc(h->subset_t.as<uint8_t>(), F, ns_pad, h->gram.as<unsigned long long>(),
                            h->status.as<unsigned>(), st);
     if (rc != ANNF_OK) return rc;
