@@ -301,7 +301,51 @@ __device__ __forceinline__ void take_best(const int (&cy)[G], const int (&cx)[G]
   }
 }
 
-constexpr int kGroup = 4;  // candidates evaluated together
+constexpr int kGroup = 4;  // candidates evaluated together (initial choice)
+
+// ssd_group with the A patch already word-aligned in shared memory: word j of patch row r at
+// sa[(r * NW + j) * stride] (one column per thread, so a warp's reads hit 32 banks)
+template <int PS, int RL, int G>
+__device__ __forceinline__ void ssd_group_s(const unsigned* __restrict__ sa, int stride, const Img& B,
+                                            const int (&cy)[G], const int (&cx)[G], int limit, int (&out)[G]) {
+  constexpr int NW = (RL + 3) / 4;
+  unsigned s[G];
+  bool live[G];
+#pragma unroll
+  for (int g = 0; g < G; ++g) {
+    s[g] = 0;
+    live[g] = cy[g] >= 0;
+  }
+#pragma unroll 1
+  for (int r = 0; r < PS; ++r) {
+    bool any = false;
+#pragma unroll
+    for (int g = 0; g < G; ++g) any |= live[g];
+    if (!any) break;
+    unsigned bw[G][NW];
+#pragma unroll
+    for (int g = 0; g < G; ++g)
+      if (live[g]) row_words<RL>(B.p, ((long long)(cy[g] + r) * B.w + cx[g]) * B.c, B.bytes, bw[g]);
+    unsigned aw[NW];
+#pragma unroll
+    for (int j = 0; j < NW; ++j) aw[j] = sa[(r * NW + j) * stride];
+#pragma unroll
+    for (int g = 0; g < G; ++g) {
+      if (!live[g]) continue;
+#pragma unroll
+      for (int j = 0; j < NW; ++j) {
+        const unsigned dd = __vabsdiffu4(aw[j], bw[g][j]);
+        s[g] = __dp4a(dd, dd, s[g]);
+      }
+      if ((int)s[g] > limit) live[g] = false;
+    }
+  }
+#pragma unroll
+  for (int g = 0; g < G; ++g) out[g] = cy[g] < 0 ? 0x7fffffff : (int)s[g];
+}
+
+constexpr int kPropThreads = 256;
+constexpr int kPropGroup = 5;  // a pass's four neighbour candidates and its first random offset
 
 // seed (optional, [2 nA]: B index, then SSD): a match to start from, e.g. the best proposal found
 // earlier; the result is the lexicographic minimum over the seed and the candidates either way
@@ -337,25 +381,39 @@ __global__ void __launch_bounds__(256, 3) fast_init_t_kernel(Img A, Img B, int n
   }
 }
 
-// one pass: the four neighbours' matches at distance 'jump', shifted to this pixel (one group),
-// then 'nrand' random offsets around the pass's starting match within 'radius' (groups of four)
+// one pass: the four neighbours' matches at distance 'jump', shifted to this pixel, and 'nrand'
+// random offsets around the pass's starting match within 'radius', kPropGroup candidates at a
+// time (the neighbours and the first offset together). The pixel's A patch is aligned into shared
+// memory once and read by every group.
 template <int PS, int RL>
-__global__ void __launch_bounds__(256, 3) fast_prop_t_kernel(Img A, Img B, int nA, int jump, int radius, int nrand,
-                                                          uint32_t seed, Match in, Match out) {
+__global__ void __launch_bounds__(kPropThreads, 3) fast_prop_t_kernel(Img A, Img B, int nA, int jump, int radius,
+                                                                   int nrand, uint32_t seed, Match in, Match out) {
+  constexpr int NW = (RL + 3) / 4;
+  constexpr int G = kPropGroup;
+  extern __shared__ unsigned sAw[];  // [PS * NW][kPropThreads]
+  unsigned* myA = sAw + threadIdx.x;
   const int nb_rows = B.h - B.psize + 1, na_rows = nA / A.ncols;
+  const int nr = radius > 0 ? nrand : 0;
+  const int ngroups = 1 + (nr > G - 4 ? (nr - (G - 4) + G - 1) / G : 0);
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nA; i += gridDim.x * blockDim.x) {
     const int y = i / A.ncols, x = i - y * A.ncols;
     int best = in.idx[i], bs = in.ssd[i];
     const int b0y = best / B.ncols, b0x = best - b0y * B.ncols;
-    const int ngroups = 1 + (radius > 0 ? (nrand + kGroup - 1) / kGroup : 0);
-    for (int grp = 0; grp < ngroups; ++grp) {  // one evaluation site keeps the registers down
-      int cy[kGroup], cx[kGroup], ssd[kGroup];
+#pragma unroll 1
+    for (int r = 0; r < PS; ++r) {
+      unsigned w[NW];
+      row_words<RL>(A.p, ((long long)(y + r) * A.w + x) * A.c, A.bytes, w);
 #pragma unroll
-      for (int g = 0; g < kGroup; ++g) {
+      for (int j = 0; j < NW; ++j) myA[(r * NW + j) * kPropThreads] = w[j];
+    }
+    for (int grp = 0; grp < ngroups; ++grp) {
+      int cy[G], cx[G], ssd[G];
+#pragma unroll
+      for (int g = 0; g < G; ++g) {
         cy[g] = -1;
         cx[g] = 0;
         int by, bx;
-        if (grp == 0) {
+        if (grp == 0 && g < 4) {
           const int ddy = g == 0 ? -1 : g == 1 ? 1 : 0, ddx = g == 2 ? -1 : g == 3 ? 1 : 0;
           const int ny = y + ddy * jump, nx = x + ddx * jump;
           if (ny < 0 || nx < 0 || ny >= na_rows || nx >= A.ncols) continue;
@@ -365,18 +423,18 @@ __global__ void __launch_bounds__(256, 3) fast_prop_t_kernel(Img A, Img B, int n
           by = nby - ddy * jump;
           bx = nb - nby * B.ncols - ddx * jump;
         } else {
-          const int t = (grp - 1) * kGroup + g;
-          if (t >= nrand) continue;
-          const uint32_t r = hash3(seed, (uint32_t)i, (uint32_t)t);
-          by = b0y + (int)((r >> 16) % (2 * radius + 1)) - radius;
-          bx = b0x + (int)(r % (2 * radius + 1)) - radius;
+          const int t = grp == 0 ? g - 4 : (G - 4) + (grp - 1) * G + g;
+          if (t >= nr) continue;
+          const uint32_t rr = hash3(seed, (uint32_t)i, (uint32_t)t);
+          by = b0y + (int)((rr >> 16) % (2 * radius + 1)) - radius;
+          bx = b0x + (int)(rr % (2 * radius + 1)) - radius;
         }
         if (by < 0 || bx < 0 || by >= nb_rows || bx >= B.ncols || by * B.ncols + bx == best) continue;
         cy[g] = by;
         cx[g] = bx;
       }
-      ssd_group<PS, RL, kGroup>(A, y, x, B, cy, cx, bs, ssd);
-      take_best<kGroup>(cy, cx, ssd, B.ncols, best, bs);
+      ssd_group_s<PS, RL, G>(myA, kPropThreads, B, cy, cx, bs, ssd);
+      take_best<G>(cy, cx, ssd, B.ncols, best, bs);
     }
     out.idx[i] = best;
     out.ssd[i] = bs;
@@ -417,7 +475,12 @@ int fast_search(annf_handle* h, const uint8_t* img_a, int ha, int wa, const uint
   const int shape = psize * 100 + psize * c;
   const bool special = shape == 927 || shape == 721 || shape == 515 || shape == 1133;
 #define ANNF_FAST_INIT(PS, RL) fast_init_t_kernel<PS, RL><<<blocks, 256, 0, st>>>(A, B, nA, K, nat_pos, h->perm.as<int>(), prop, n_prop, seed_match, m0)
-#define ANNF_FAST_PROP(PS, RL, ...) fast_prop_t_kernel<PS, RL><<<blocks, 256, 0, st>>>(__VA_ARGS__)
+#define ANNF_FAST_PROP(PS, RL, ...)                                                                     \
+  do {                                                                                                  \
+    const size_t sm = (size_t)(PS) * (((RL) + 3) / 4) * kPropThreads * sizeof(unsigned);                \
+    ANNF_CUDA_TRY(cudaFuncSetAttribute(fast_prop_t_kernel<PS, RL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm)); \
+    fast_prop_t_kernel<PS, RL><<<blocks, kPropThreads, sm, st>>>(__VA_ARGS__);                          \
+  } while (0)
   switch (shape) {
     case 927: ANNF_FAST_INIT(9, 27); break;
     case 721: ANNF_FAST_INIT(7, 21); break;
