@@ -132,28 +132,32 @@ __global__ void axis_kernel(int n, int d, int t, int S, int splitting, const typ
   nlt[s] = 0;
 }
 
-// one radix-select pass: histogram of the current digit over the keys that match the prefix found
-// so far. The first pass reads the split axis from the points and writes the keys. Lanes of a warp
-// that hit the same bin (common: a segment's keys share their high digits) add once, together.
+// one radix-select pass: histogram of the current digit (width bits at shift, at most kSelBits)
+// over the keys that match the prefix found so far. The first pass reads the split axis from the
+// points and writes the keys. Lanes of a warp that hit the same bin (common: a segment's keys share
+// their high digits) add once, together.
+constexpr int kSelBits = 11;                 // widest digit: 32-bit keys take three passes (11, 11, 10)
+constexpr int kSelBins = 1 << kSelBits;
 template <typename T>
-__global__ void hist_kernel(int n, int d, int t, int B, int shift, bool extract, const T* __restrict__ pts,
+__global__ void hist_kernel(int n, int d, int t, int B, int shift, int width, bool extract, const T* __restrict__ pts,
                             const int* __restrict__ axis, typename key_of<T>::type* __restrict__ keys,
                             const typename key_of<T>::type* __restrict__ prefix, unsigned* ghist) {
   using K = typename key_of<T>::type;
-  __shared__ unsigned h[256];
+  __shared__ unsigned h[kSelBins];
   const int s = blockIdx.x / B, bb = blockIdx.x % B;
   int lo, hi;
   seg_range(n, t, s, lo, hi);
   const int c0 = lo + bb * kChunk, c1 = min(hi, c0 + kChunk);
-  h[threadIdx.x] = 0;
+  const int nb = 1 << width;
+  for (int z = threadIdx.x; z < nb; z += blockDim.x) h[z] = 0;
   __syncthreads();
   const K pre = prefix[s];
-  const K hmask = (shift + 8 >= (int)(8 * sizeof(K))) ? (K)0 : (~(K)0 << (shift + 8));
+  const K hmask = (shift + width >= (int)(8 * sizeof(K))) ? (K)0 : (~(K)0 << (shift + width));
   const int ax = axis[s];
   const int lane = threadIdx.x & 31;
   for (int base = c0 + (int)(threadIdx.x & ~31u); base < c1; base += blockDim.x) {
     const int i = base + lane;
-    unsigned bin = 256u;
+    unsigned bin = kSelBins;
     if (i < c1) {
       K k;
       if (extract) {
@@ -162,14 +166,16 @@ __global__ void hist_kernel(int n, int d, int t, int B, int shift, bool extract,
       } else {
         k = keys[i];
       }
-      if (((k ^ pre) & hmask) == 0) bin = (unsigned)(k >> shift) & 255u;
+      if (((k ^ pre) & hmask) == 0) bin = (unsigned)(k >> shift) & (unsigned)(nb - 1);
     }
     const unsigned peers = __match_any_sync(0xffffffffu, bin);
-    if (bin != 256u && lane == __ffs(peers) - 1) atomicAdd(&h[bin], (unsigned)__popc(peers));
+    if (bin != (unsigned)kSelBins && lane == __ffs(peers) - 1) atomicAdd(&h[bin], (unsigned)__popc(peers));
   }
   __syncthreads();
-  unsigned v = h[threadIdx.x];
-  if (v) atomicAdd(&ghist[(long long)s * 256 + threadIdx.x], v);
+  for (int z = threadIdx.x; z < nb; z += blockDim.x) {
+    const unsigned v = h[z];
+    if (v) atomicAdd(&ghist[(long long)s * kSelBins + z], v);
+  }
 }
 
 // block-wide exclusive scan of two counters (kThreads threads)
@@ -206,22 +212,37 @@ __device__ __forceinline__ void block_excl_scan2(int a, int b, int& ea, int& eb,
   __syncthreads();
 }
 
+// the bin of the digit that holds rank r (kThreads threads, kSelBins / kThreads bins each, read
+// and cleared for the next pass)
 template <typename K>
 __global__ void pick_kernel(int shift, bool last, unsigned* ghist, K* prefix, int* rank, int* nlt,
                             int* neq) {
+  constexpr int kPer = kSelBins / kThreads;
   const int s = blockIdx.x;
-  unsigned* h = ghist + (long long)s * 256;
-  int c = (int)h[threadIdx.x];
-  h[threadIdx.x] = 0;  // ready for the next pass
+  unsigned* h = ghist + (long long)s * kSelBins;
+  int c[kPer], sum = 0;
+#pragma unroll
+  for (int u = 0; u < kPer; ++u) {
+    c[u] = (int)h[threadIdx.x * kPer + u];
+    h[threadIdx.x * kPer + u] = 0;  // ready for the next pass
+    sum += c[u];
+  }
   int ex, dummy_e, tot, dummy_t;
-  block_excl_scan2(c, 0, ex, dummy_e, tot, dummy_t);
+  block_excl_scan2(sum, 0, ex, dummy_e, tot, dummy_t);
   const int r = rank[s];
   __syncthreads();
-  if (ex <= r && r < ex + c) {
-    prefix[s] |= ((K)threadIdx.x) << shift;
-    rank[s] = r - ex;
-    nlt[s] += ex;
-    if (last) neq[s] = c;
+  if (ex <= r && r < ex + sum) {
+    int run = ex;
+#pragma unroll
+    for (int u = 0; u < kPer; ++u) {
+      if (run <= r && r < run + c[u]) {
+        prefix[s] |= ((K)(threadIdx.x * kPer + u)) << shift;
+        rank[s] = r - run;
+        nlt[s] += run;
+        if (last) neq[s] = c[u];
+      }
+      run += c[u];
+    }
   }
 }
 
@@ -941,8 +962,8 @@ static int build_impl(annf_handle* h, const T* points, int n, int d, int depth, 
   if (tg > 0) {
     ANNF_ENSURE(h->bmin, (size_t)2 * cap * d * sizeof(K));
     ANNF_ENSURE(h->bmax, (size_t)2 * cap * d * sizeof(K));
-    ANNF_ENSURE(h->hist, (size_t)(cap / 2) * 256 * sizeof(unsigned));
-    ANNF_CUDA_TRY(cudaMemsetAsync(h->hist.p, 0, (size_t)(cap / 2) * 256 * sizeof(unsigned), st));  // picks re-zero it
+    ANNF_ENSURE(h->hist, (size_t)(cap / 2) * kSelBins * sizeof(unsigned));
+    ANNF_CUDA_TRY(cudaMemsetAsync(h->hist.p, 0, (size_t)(cap / 2) * kSelBins * sizeof(unsigned), st));  // picks re-zero it
   }
   ANNF_ENSURE(h->leaf_box, (size_t)2 * L * d * sizeof(T));
   bool finished = false;
@@ -994,13 +1015,18 @@ static int build_impl(annf_handle* h, const T* points, int n, int d, int depth, 
                                                    h->sel_nlt.as<int>(), cmin, cmax);
     ANNF_CHECK_LAUNCH();
     constexpr int kBits = 8 * sizeof(K);
-    for (int shift = kBits - 8; shift >= 0; shift -= 8) {
-      hist_kernel<T><<<(unsigned)nblk, 256, 0, st>>>(n, d, t, B, shift, shift == kBits - 8, cur_pts, h->axis.as<int>(),
-                                                     h->keys.as<K>(), h->sel_prefix.as<K>(), h->hist.as<unsigned>());
+    // digits from the top: kSelBits wide, the rest of the key in the last pass
+    for (int hi_bit = kBits; hi_bit > 0;) {
+      const int width = hi_bit >= 2 * kSelBits ? kSelBits : (hi_bit > kSelBits ? hi_bit - hi_bit / 2 : hi_bit);
+      const int shift = hi_bit - width;
+      hist_kernel<T><<<(unsigned)nblk, 256, 0, st>>>(n, d, t, B, shift, width, hi_bit == kBits, cur_pts,
+                                                     h->axis.as<int>(), h->keys.as<K>(), h->sel_prefix.as<K>(),
+                                                     h->hist.as<unsigned>());
       ANNF_CHECK_LAUNCH();
       pick_kernel<K><<<S, 256, 0, st>>>(shift, shift == 0, h->hist.as<unsigned>(), h->sel_prefix.as<K>(),
                                         h->sel_rank.as<int>(), h->sel_nlt.as<int>(), h->sel_neq.as<int>());
       ANNF_CHECK_LAUNCH();
+      hi_bit -= width;
     }
     count_kernel<K><<<(unsigned)nblk, kThreads, 0, st>>>(n, t, B, h->keys.as<K>(), h->sel_prefix.as<K>(),
                                                         h->blk_lt.as<int>(), h->blk_eq.as<int>());
