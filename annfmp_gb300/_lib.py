@@ -100,6 +100,8 @@ SIGNATURES = {
     "annf_profile_read": (_i, [_vp, _vp, _i, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_char_p)]),
     "annf_launch_count": (_ll, []),
     "annf_buffer_epoch": (_ll, []),
+    "annf_pca_covariance": (_i, [_vp, _vp, _i, _i, _vp, _i, _vp, _i, _i, _vp, _i, _i, _i, _vp, _vp]),
+    "annf_pca_components": (_i, [_vp, _i, _i, _i, _vp, _vp]),
 }
 
 _lock = threading.Lock()

@@ -60,6 +60,10 @@ int project_tc(annf_handle* h, const uint8_t* img, int H, int W, int c, int psiz
                const double* mean, int ncomp, float* out, cudaStream_t st);
 int raw_nn(const uint8_t* img_a, int ha, int wa, const uint8_t* img_b, int hb, int wb, int c, int psize,
            const int* qpix, int nq, unsigned long long* best, cudaStream_t st);
+int pca_covariance(annf_handle* h, const uint8_t* img_a, int ha, int wa, const int* pos_a, int n_a,
+                   const uint8_t* img_b, int hb, int wb, const int* pos_b, int n_b, int c, int psize, double* mean,
+                   cudaStream_t st);
+int pca_components(annf_handle* h, int P, int ncomp, int solver, double* comps, cudaStream_t st);
 int pca_fit(annf_handle* h, const uint8_t* img_a, int ha, int wa, const int* pos_a, int n_a, const uint8_t* img_b,
             int hb, int wb, const int* pos_b, int n_b, int c, int psize, int ncomp, double* comps, double* mean,
             int solver, cudaStream_t st);
@@ -271,6 +275,25 @@ int annf_pca_fit_subspace(annf_handle* h, const uint8_t* img_a, int ha, int wa, 
   ANNF_REQUIRE(iters >= 1 && iters <= 100, "annf_pca_fit_subspace: iters out of range");
   return pca_fit(h, img_a, ha, wa, pos_a, n_a, img_b, hb, wb, pos_b, n_b, channels, psize, n_components,
                  components_out, mean_out, iters, static_cast<cudaStream_t>(stream));
+}
+
+int annf_pca_covariance(annf_handle* h, const uint8_t* img_a, int ha, int wa, const int* pos_a, int n_a,
+                        const uint8_t* img_b, int hb, int wb, const int* pos_b, int n_b, int channels, int psize,
+                        double* mean_out, void* stream) {
+  ANNF_API_HANDLE(h);
+  ANNF_REQUIRE(img_a && img_b && mean_out, "annf_pca_covariance: NULL argument");
+  ANNF_REQUIRE((n_a == 0 || pos_a) && (n_b == 0 || pos_b), "annf_pca_covariance: NULL positions");
+  ANNF_REQUIRE(n_a >= 0 && n_b >= 0 && channels >= 1 && psize >= 1, "annf_pca_covariance: bad sizes");
+  ANNF_REQUIRE(psize <= ha && psize <= wa && psize <= hb && psize <= wb, "annf_pca_covariance: patch larger than image");
+  return pca_covariance(h, img_a, ha, wa, pos_a, n_a, img_b, hb, wb, pos_b, n_b, channels, psize, mean_out,
+                        static_cast<cudaStream_t>(stream));
+}
+
+int annf_pca_components(annf_handle* h, int P, int n_components, int iters, double* components_out, void* stream) {
+  ANNF_API_HANDLE(h);
+  ANNF_REQUIRE(components_out, "annf_pca_components: NULL argument");
+  ANNF_REQUIRE(iters >= 0 && iters <= 100, "annf_pca_components: iters out of range");
+  return pca_components(h, P, n_components, iters, components_out, static_cast<cudaStream_t>(stream));
 }
 
 int annf_project(annf_handle* h, const uint8_t* img, int hgt, int wid, int channels, int psize,

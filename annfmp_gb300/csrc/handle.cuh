@@ -69,6 +69,7 @@ struct annf_handle {
   annf::DevBuf fast_buf, fast_nat, tc_buf, pj_buf;
   // ---- pca scratch ----
   annf::DevBuf gram, colsum, subset_t, cov, eigval, digits, meanproj, solver_ws, solver_info, eig_ws;
+  int cov_p = 0;  // size of the covariance held in cov (0: none)
   cusolverDnContext* solver = nullptr;
   // ---- device status word ----
   annf::DevBuf status;

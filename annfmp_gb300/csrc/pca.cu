@@ -403,15 +403,15 @@ bool gram_tc_supported(int F, int ns_pad);
 int gram_tc(const uint8_t* XT, int F, int ns_pad, unsigned long long* G, unsigned* status, cudaStream_t st);
 int eig_top_subspace(annf_handle* h, const double* C, int P, int ncomp, int iters, double* comps, cudaStream_t st);
 
-int pca_fit(annf_handle* h, const uint8_t* img_a, int ha, int wa, const int* pos_a, int n_a, const uint8_t* img_b,
-            int hb, int wb, const int* pos_b, int n_b, int c, int psize, int ncomp, double* comps, double* mean,
-            int solver, cudaStream_t st) {
+// covariance (FP64, in h->cov) and mean of the sampled patches
+int pca_covariance(annf_handle* h, const uint8_t* img_a, int ha, int wa, const int* pos_a, int n_a,
+                   const uint8_t* img_b, int hb, int wb, const int* pos_b, int n_b, int c, int psize, double* mean,
+                   cudaStream_t st) {
   (void)ha;
   (void)hb;
   const int P = psize * psize * c;
   const int ns = n_a + n_b;
   ANNF_REQUIRE(ns >= 2, "annf_pca_fit: need at least two samples");
-  ANNF_REQUIRE(ncomp >= 1 && ncomp <= P, "annf_pca_fit: n_components out of range");
   ANNF_REQUIRE(P + 1 <= 4096, "annf_pca_fit: patch too large");
   const int F = P + 1;
   const int ns_pad = round_up(ns, 64);  // whole 64-sample blocks for the tensor-core Gram
@@ -450,6 +450,15 @@ int pca_fit(annf_handle* h, const uint8_t* img_a, int ha, int wa, const int* pos
   cov_finish_kernel<<<std::min(ceil_div((long long)P * P, 256), 1024), 256, 0, st>>>(
       h->gram.as<unsigned long long>(), F, P, h->cov.as<double>(), mean);
   ANNF_CHECK_LAUNCH();
+  h->cov_p = P;
+  return ANNF_OK;
+}
+
+// the leading ncomp components of the covariance in h->cov (P x P): solver 0 = full FP64 eigh
+// (cuSOLVER), solver > 0 = subspace iteration with that many steps and an FP64 Rayleigh-Ritz step
+int pca_components(annf_handle* h, int P, int ncomp, int solver, double* comps, cudaStream_t st) {
+  ANNF_REQUIRE(h->cov_p == P && P >= 1, "annf_pca_components: no covariance of this size on the handle");
+  ANNF_REQUIRE(ncomp >= 1 && ncomp <= P, "annf_pca_fit: n_components out of range");
   if (solver > 0 && subspace_block(P, ncomp) > 0) {  // leading components only (approximate forms)
     int rc = eig_top_subspace(h, h->cov.as<double>(), P, ncomp, solver, comps, st);
     prof_mark(h, "pca_eigh", st);
@@ -481,10 +490,21 @@ int pca_fit(annf_handle* h, const uint8_t* img_a, int ha, int wa, const int* pos
     set_error("cusolverDnDsyevd failed");
     return ANNF_ERR_SOLVER;
   }
+  h->cov_p = 0;  // syevd left the eigenvectors in its place
   prof_mark(h, "pca_eigh", st);
   flip_kernel<<<ncomp, 256, 0, st>>>(h->cov.as<double>(), P, ncomp, comps);
   ANNF_CHECK_LAUNCH();
   return ANNF_OK;
+}
+
+int pca_fit(annf_handle* h, const uint8_t* img_a, int ha, int wa, const int* pos_a, int n_a, const uint8_t* img_b,
+            int hb, int wb, const int* pos_b, int n_b, int c, int psize, int ncomp, double* comps, double* mean,
+            int solver, cudaStream_t st) {
+  const int P = psize * psize * c;
+  ANNF_REQUIRE(ncomp >= 1 && ncomp <= P, "annf_pca_fit: n_components out of range");
+  int rc = pca_covariance(h, img_a, ha, wa, pos_a, n_a, img_b, hb, wb, pos_b, n_b, c, psize, mean, st);
+  if (rc != ANNF_OK) return rc;
+  return pca_components(h, P, ncomp, solver, comps, st);
 }
 
 #define ANNF_W4_CASES(X) X(8) X(12) X(16) X(20) X(24) X(28) X(32) X(36) X(40) X(44) X(48) X(52) X(56) X(60) X(64)

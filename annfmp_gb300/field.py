@@ -262,16 +262,24 @@ class ANNFieldPropKDTreeGB300:
         ev = _Marks(sync)
         ev["t0"].record()
 
-        # offset proposals depend only on the images: computed on a side stream, overlapping the PCA
-        # fit (whose eigensolver occupies one SM) and the projection; joined before the candidates
+        # offset proposals depend only on the images: computed on a side stream that starts once
+        # the covariance is formed, beside the eigensolver (which keeps one SM busy and leaves the
+        # rest idle); joined before the candidates
         prop, side, seeded = None, None, False
-        if self.form != "plain" and self.proposal is not None:
-            main = torch.cuda.current_stream(dev)
+
+        def start_proposals():
+            nonlocal prop, side, seeded
+            if self.form == "plain" or self.proposal is None:
+                return
             side = torch.cuda.Stream(dev) if getattr(self, "_side", None) is None else self._side
             self._side = side
-            side.wait_stream(main)
+            side.wait_stream(torch.cuda.current_stream(dev))
             with torch.cuda.stream(side):
                 prop = self.proposal.propose(A, B, p)
+                # their exact distances need no tree: the best proposal of each pixel, here too
+                if prop is not None and hasattr(self.proposal, "seed"):
+                    prop = self.proposal.seed(A, B, p, prop)
+                    seeded = True
 
         # (1) PCA fit on the sampled subset (annfmp/openmp/base.py:168-191)
         m = int(self.n_subset / 2)
@@ -287,19 +295,15 @@ class ANNFieldPropKDTreeGB300:
             h.call("annf_pca_fit", ptr(A), ha, wa, ptr(pos_a), pos_a.shape[0], ptr(B), hb, wb, ptr(pos_b),
                    pos_b.shape[0], c, p, d, ptr(self.components_), ptr(self.mean_), st)
         elif solver == "subspace":
-            h.call("annf_pca_fit_subspace", ptr(A), ha, wa, ptr(pos_a), pos_a.shape[0], ptr(B), hb, wb, ptr(pos_b),
-                   pos_b.shape[0], c, p, d, int(self.pca_iters), ptr(self.components_), ptr(self.mean_), st)
+            h.call("annf_pca_covariance", ptr(A), ha, wa, ptr(pos_a), pos_a.shape[0], ptr(B), hb, wb, ptr(pos_b),
+                   pos_b.shape[0], c, p, ptr(self.mean_), st)
+            start_proposals()
+            h.call("annf_pca_components", P, d, int(self.pca_iters), ptr(self.components_), st)
         else:
             raise ValueError("pca_solver must be 'exact' or 'subspace'")
+        if side is None:
+            start_proposals()  # (the exact solver: after the whole fit)
         ev["t1"].record()
-
-        # the proposals' exact distances need no tree: their best match is found on the side
-        # stream while the projection and the tree build (bandwidth-bound) run here
-        if prop is not None and hasattr(self.proposal, "seed"):
-            side.wait_stream(torch.cuda.current_stream(dev))
-            with torch.cuda.stream(side):
-                prop = self.proposal.seed(A, B, p, prop)
-            seeded = True
 
         # (2)+(3) patches projected straight from the images (annfmp/openmp/base.py:152-166, 193-200)
         self.patches_a_reduced_ = torch.empty((n_a, d), dtype=real, device=dev)

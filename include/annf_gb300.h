@@ -146,6 +146,17 @@ int annf_pca_fit_subspace(annf_handle* h, const uint8_t* img_a, int ha, int wa, 
                           int psize, int n_components, int iters, double* components_out,
                           double* mean_out, void* stream);
 
+/* The two halves of annf_pca_fit / annf_pca_fit_subspace, for callers that want work of their own
+ * between them (no reference counterpart): annf_pca_covariance forms the covariance of the sampled
+ * patches (kept on the handle) and writes the mean; annf_pca_components then writes the leading
+ * components (iters 0: full FP64 eigendecomposition; iters > 0: subspace iteration with that many
+ * steps and an FP64 Rayleigh-Ritz step). P = psize * psize * channels. */
+int annf_pca_covariance(annf_handle* h, const uint8_t* img_a, int ha, int wa, const int* pos_a, int n_a,
+                        const uint8_t* img_b, int hb, int wb, const int* pos_b, int n_b, int channels,
+                        int psize, double* mean_out, void* stream);
+int annf_pca_components(annf_handle* h, int P, int n_components, int iters, double* components_out,
+                        void* stream);
+
 /* Project every psize x psize patch of an image onto the components
  * (annfmp/openmp/base.py:193-200: X @ C^T - mean @ C^T in FP64, cast to real_type). The
  * product is evaluated exactly in integer arithmetic on split coefficients, so the result is the
