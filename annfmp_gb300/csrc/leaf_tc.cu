@@ -129,47 +129,64 @@ __global__ void __launch_bounds__(256) qleaf_kernel(TreeView<float> tv, const fl
 }
 
 // exclusive scans of cnt[L] into off[L+1] and cursor[L], and of the 128-query chunk counts into
-// choff[L+1] (one CTA of 1024 threads; the chunk scan is a second pass of the same code)
-__device__ void block_exclusive_scan(const int* __restrict__ cnt, int L, bool chunks, int* __restrict__ off,
-                                     int* __restrict__ cursor) {
-  __shared__ int warp_tot[32];
-  const int per = (L + blockDim.x - 1) / blockDim.x;
-  const int b0 = threadIdx.x * per, b1 = min(L, b0 + per);
-  int s = 0;
-  for (int i = b0; i < b1; ++i) s += chunks ? (cnt[i] + kTcThreads - 1) / kTcThreads : cnt[i];
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  int x = s;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    const int y = __shfl_up_sync(0xffffffffu, x, o);
-    if (lane >= o) x += y;
-  }
-  if (lane == 31) warp_tot[w] = x;
-  __syncthreads();
-  if (w == 0) {
-    int t = warp_tot[lane];
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const int y = __shfl_up_sync(0xffffffffu, t, o);
-      if (lane >= o) t += y;
-    }
-    warp_tot[lane] = t;
-  }
-  __syncthreads();
-  int run = x - s + (w ? warp_tot[w - 1] : 0);
-  for (int i = b0; i < b1; ++i) {
-    off[i] = run;
-    if (cursor) cursor[i] = run;
-    run += chunks ? (cnt[i] + kTcThreads - 1) / kTcThreads : cnt[i];
-  }
-  if (threadIdx.x == blockDim.x - 1) off[L] = run;
-  __syncthreads();
-}
-
+// choff[L+1], together (one CTA of 1024 threads, each over a run of consecutive leaves: its sums
+// with independent, unrolled loads, one block-wide scan of both, then its outputs)
 __global__ void __launch_bounds__(1024) leaf_scan_kernel(const int* __restrict__ cnt, int L, int* __restrict__ off,
                                                          int* __restrict__ cursor, int* __restrict__ choff) {
-  block_exclusive_scan(cnt, L, false, off, cursor);
-  block_exclusive_scan(cnt, L, true, choff, nullptr);
+  __shared__ int warp_tot[2][32];
+  const int per = (L + blockDim.x - 1) / blockDim.x;
+  const int b0 = min(L, (int)threadIdx.x * per), b1 = min(L, b0 + per);
+  int sq = 0, sc = 0;
+#pragma unroll 8
+  for (int i = b0; i < b1; ++i) {
+    const int v = __ldg(cnt + i);
+    sq += v;
+    sc += (v + kTcThreads - 1) / kTcThreads;
+  }
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  int xq = sq, xc = sc;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int yq = __shfl_up_sync(0xffffffffu, xq, o), yc = __shfl_up_sync(0xffffffffu, xc, o);
+    if (lane >= o) {
+      xq += yq;
+      xc += yc;
+    }
+  }
+  if (lane == 31) {
+    warp_tot[0][w] = xq;
+    warp_tot[1][w] = xc;
+  }
+  __syncthreads();
+  if (w == 0) {
+    int tq = lane < (int)(blockDim.x >> 5) ? warp_tot[0][lane] : 0;
+    int tc = lane < (int)(blockDim.x >> 5) ? warp_tot[1][lane] : 0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int yq = __shfl_up_sync(0xffffffffu, tq, o), yc = __shfl_up_sync(0xffffffffu, tc, o);
+      if (lane >= o) {
+        tq += yq;
+        tc += yc;
+      }
+    }
+    warp_tot[0][lane] = tq;
+    warp_tot[1][lane] = tc;
+  }
+  __syncthreads();
+  int rq = xq - sq + (w ? warp_tot[0][w - 1] : 0), rc = xc - sc + (w ? warp_tot[1][w - 1] : 0);
+#pragma unroll 8
+  for (int i = b0; i < b1; ++i) {
+    const int v = __ldg(cnt + i);
+    off[i] = rq;
+    cursor[i] = rq;
+    choff[i] = rc;
+    rq += v;
+    rc += (v + kTcThreads - 1) / kTcThreads;
+  }
+  if (threadIdx.x == blockDim.x - 1) {
+    off[L] = rq;
+    choff[L] = rc;
+  }
 }
 
 // work item -> leaf: leaf l owns items choff[l] .. choff[l+1]-1 (one per 128 of its queries)

@@ -358,32 +358,44 @@ __global__ void __launch_bounds__(kThreads) scatter_kernel(
       }
     } else {
       // the children's bounding boxes on the way: a thread always handles word c = tid mod w
-      // (w divides the block), keeping the order keys of its four coordinates per child
+      // (w divides the block), keeping its four coordinates' minima and maxima per child as
+      // floats (branch-free: the other child's update sees +-inf); order keys only at the end
+      float fmn[2][4], fmx[2][4];
+#pragma unroll
+      for (int u = 0; u < 2; ++u)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          fmn[u][j] = __int_as_float(0x7f800000);
+          fmx[u][j] = -__int_as_float(0x7f800000);
+        }
+      bool has[2] = {false, false};  // (infinite coordinates are valid points: no sentinel test)
+      for (int e = threadIdx.x; e < m * w; e += blockDim.x) {
+        const int r = e / w, c = e - r * w;
+        const float4 v = src[e];
+        dst4[(long long)sdst[r] * w + c] = v;
+        const bool rt = sside[r] != 0;
+        has[0] |= !rt;
+        has[1] |= rt;
+        const float inf = __int_as_float(0x7f800000);
+        const float vv[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          fmn[0][j] = fminf(fmn[0][j], rt ? inf : vv[j]);
+          fmx[0][j] = fmaxf(fmx[0][j], rt ? -inf : vv[j]);
+          fmn[1][j] = fminf(fmn[1][j], rt ? vv[j] : inf);
+          fmx[1][j] = fmaxf(fmx[1][j], rt ? vv[j] : -inf);
+        }
+      }
+      // to order keys (-0 and +0 fold together, so fminf's choice between them does not matter);
+      // a side without elements keeps the neutral keys
       K mn[2][4], mx[2][4];
 #pragma unroll
       for (int u = 0; u < 2; ++u)
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
-          mn[u][j] = key_max<K>();
-          mx[u][j] = (K)0;
+          mn[u][j] = has[u] ? (K)ord_key(fmn[u][j]) : key_max<K>();
+          mx[u][j] = has[u] ? (K)ord_key(fmx[u][j]) : (K)0;
         }
-      for (int e = threadIdx.x; e < m * w; e += blockDim.x) {
-        const int r = e / w, c = e - r * w;
-        const float4 v = src[e];
-        dst4[(long long)sdst[r] * w + c] = v;
-        const K kv[4] = {(K)ord_key(v.x), (K)ord_key(v.y), (K)ord_key(v.z), (K)ord_key(v.w)};
-        const bool rt = sside[r] != 0;
-#pragma unroll
-        for (int j = 0; j < 4; ++j) {
-          if (rt) {
-            mn[1][j] = kv[j] < mn[1][j] ? kv[j] : mn[1][j];
-            mx[1][j] = kv[j] > mx[1][j] ? kv[j] : mx[1][j];
-          } else {
-            mn[0][j] = kv[j] < mn[0][j] ? kv[j] : mn[0][j];
-            mx[0][j] = kv[j] > mx[0][j] ? kv[j] : mx[0][j];
-          }
-        }
-      }
       // lanes of a warp with the same word: xor offsets w, 2w, ..., 16
       for (int o = w; o < 32; o <<= 1) {
 #pragma unroll
