@@ -437,7 +437,7 @@ def run_graph_workload(args, name, rank, world, local_rank):
     if name == "batch":
         pairs = gen.gpu_pairs_uneven(2, 64, device=local_rank)
         t0 = time.perf_counter()
-        groups = [BatchNNF(leaf_size=cfg["leaf"], iters=cfg["iters"], tuner=Autotuner(samples=512, reps=1),
+        groups = [BatchNNF(leaf_size=cfg["leaf"], iters=cfg["iters"], tuner=Autotuner(max_error=0.005, samples=512, reps=1),
                            **kw).prepare(pairs)]
         t_prep = time.perf_counter() - t0
         feeds = [None]
