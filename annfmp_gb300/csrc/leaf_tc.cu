@@ -129,38 +129,33 @@ __global__ void __launch_bounds__(256) qleaf_kernel(TreeView<float> tv, const fl
 }
 
 // exclusive scans of cnt[L] into off[L+1] and cursor[L], and of the 128-query chunk counts into
-// choff[L+1], together (one CTA of 1024 threads, each over a run of consecutive leaves: its sums
-// with independent, unrolled loads, one block-wide scan of both, then its outputs)
-__global__ void __launch_bounds__(1024) leaf_scan_kernel(const int* __restrict__ cnt, int L, int* __restrict__ off,
-                                                         int* __restrict__ cursor, int* __restrict__ choff) {
-  __shared__ int warp_tot[2][32];
-  const int per = (L + blockDim.x - 1) / blockDim.x;
-  const int b0 = min(L, (int)threadIdx.x * per), b1 = min(L, b0 + per);
-  int sq = 0, sc = 0;
-#pragma unroll 8
-  for (int i = b0; i < b1; ++i) {
-    const int v = __ldg(cnt + i);
-    sq += v;
-    sc += (v + kTcThreads - 1) / kTcThreads;
-  }
+// choff[L+1], in two kernels over 1024-leaf tiles: per-tile totals, then each tile's scan from the
+// totals before it (coalesced loads, one block-wide scan of both counts per tile)
+constexpr int kScanTile = 1024;
+
+__device__ __forceinline__ int chunks_of(int v) { return (v + kTcThreads - 1) / kTcThreads; }
+
+// block-wide inclusive scan of two counters (kScanTile threads); *tot_q / *tot_c get the totals
+__device__ __forceinline__ void scan_tile2(int vq, int vc, int& iq, int& ic, int* tot_q, int* tot_c) {
+  __shared__ int wt[2][kScanTile / 32];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  int xq = sq, xc = sc;
+  iq = vq;
+  ic = vc;
 #pragma unroll
   for (int o = 1; o < 32; o <<= 1) {
-    const int yq = __shfl_up_sync(0xffffffffu, xq, o), yc = __shfl_up_sync(0xffffffffu, xc, o);
+    const int yq = __shfl_up_sync(0xffffffffu, iq, o), yc = __shfl_up_sync(0xffffffffu, ic, o);
     if (lane >= o) {
-      xq += yq;
-      xc += yc;
+      iq += yq;
+      ic += yc;
     }
   }
   if (lane == 31) {
-    warp_tot[0][w] = xq;
-    warp_tot[1][w] = xc;
+    wt[0][w] = iq;
+    wt[1][w] = ic;
   }
   __syncthreads();
   if (w == 0) {
-    int tq = lane < (int)(blockDim.x >> 5) ? warp_tot[0][lane] : 0;
-    int tc = lane < (int)(blockDim.x >> 5) ? warp_tot[1][lane] : 0;
+    int tq = wt[0][lane], tc = wt[1][lane];
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
       const int yq = __shfl_up_sync(0xffffffffu, tq, o), yc = __shfl_up_sync(0xffffffffu, tc, o);
@@ -169,23 +164,63 @@ __global__ void __launch_bounds__(1024) leaf_scan_kernel(const int* __restrict__
         tc += yc;
       }
     }
-    warp_tot[0][lane] = tq;
-    warp_tot[1][lane] = tc;
+    wt[0][lane] = tq;
+    wt[1][lane] = tc;
   }
   __syncthreads();
-  int rq = xq - sq + (w ? warp_tot[0][w - 1] : 0), rc = xc - sc + (w ? warp_tot[1][w - 1] : 0);
-#pragma unroll 8
-  for (int i = b0; i < b1; ++i) {
-    const int v = __ldg(cnt + i);
-    off[i] = rq;
-    cursor[i] = rq;
-    choff[i] = rc;
-    rq += v;
-    rc += (v + kTcThreads - 1) / kTcThreads;
+  if (w) {
+    iq += wt[0][w - 1];
+    ic += wt[1][w - 1];
   }
-  if (threadIdx.x == blockDim.x - 1) {
-    off[L] = rq;
-    choff[L] = rc;
+  *tot_q = wt[0][kScanTile / 32 - 1];
+  *tot_c = wt[1][kScanTile / 32 - 1];
+}
+
+__global__ void __launch_bounds__(kScanTile) leaf_tile_sums_kernel(const int* __restrict__ cnt, int L,
+                                                                   int* __restrict__ tile_tot) {
+  const int i = blockIdx.x * kScanTile + threadIdx.x;
+  const int v = i < L ? __ldg(cnt + i) : 0;
+  int iq, ic, tq, tc;
+  scan_tile2(v, chunks_of(v), iq, ic, &tq, &tc);
+  if (threadIdx.x == 0) {
+    tile_tot[2 * blockIdx.x] = tq;
+    tile_tot[2 * blockIdx.x + 1] = tc;
+  }
+}
+
+__global__ void __launch_bounds__(kScanTile) leaf_scan_kernel(const int* __restrict__ cnt, int L,
+                                                              const int* __restrict__ tile_tot, int* __restrict__ off,
+                                                              int* __restrict__ cursor, int* __restrict__ choff) {
+  __shared__ int base[2];
+  if (threadIdx.x < 32) {  // totals of the tiles before this one
+    int bq = 0, bc = 0;
+    for (int t = threadIdx.x; t < (int)blockIdx.x; t += 32) {
+      bq += tile_tot[2 * t];
+      bc += tile_tot[2 * t + 1];
+    }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+      bq += __shfl_xor_sync(0xffffffffu, bq, o);
+      bc += __shfl_xor_sync(0xffffffffu, bc, o);
+    }
+    if (threadIdx.x == 0) {
+      base[0] = bq;
+      base[1] = bc;
+    }
+  }
+  const int i = blockIdx.x * kScanTile + threadIdx.x;
+  const int v = i < L ? __ldg(cnt + i) : 0, vc = chunks_of(v);
+  int iq, ic, tq, tc;
+  scan_tile2(v, vc, iq, ic, &tq, &tc);  // (its barriers also publish base)
+  const int eq = base[0] + iq - v, ec = base[1] + ic - vc;
+  if (i < L) {
+    off[i] = eq;
+    cursor[i] = eq;
+    choff[i] = ec;
+  }
+  if (i == L - 1) {
+    off[L] = eq + v;
+    choff[L] = ec + vc;
   }
 }
 
@@ -670,7 +705,8 @@ int natural_knn_tc(annf_handle* h, const float* Q, long long nq, int K, int prec
   tv.leaf_box = h->leaf_box.as<float>();
   // scratch: qleaf[nq], qorder[nq], cnt[L], off[L+1], cursor[L], choff[L+1], item_leaf[items]
   // (items <= L + nq / 128: each leaf's queries in chunks of 128)
-  const size_t need = ((size_t)2 * nq + 4 * (size_t)L + 16 + (size_t)L + (size_t)nq / kTcThreads + 1) * sizeof(int);
+  const size_t need = ((size_t)2 * nq + 4 * (size_t)L + 16 + (size_t)L + (size_t)nq / kTcThreads + 1 +
+                       2 * (size_t)ceil_div(L, kScanTile) + 2) * sizeof(int);
   ANNF_ENSURE(h->tc_buf, need);
   int* qleaf = h->tc_buf.as<int>();
   int* qorder = qleaf + nq;
@@ -679,13 +715,17 @@ int natural_knn_tc(annf_handle* h, const float* Q, long long nq, int K, int prec
   int* cursor = off + L + 1;
   int* choff = cursor + L;
   int* item_leaf = choff + L + 1;
+  int* tile_tot = item_leaf + (size_t)L + (size_t)nq / kTcThreads + 1;  // [2 * tiles]
   ANNF_CUDA_TRY(cudaMemsetAsync(cnt, 0, (size_t)L * sizeof(int), st));
   const size_t ncs = NodeCache<float>::bytes(h->depth);
   ANNF_CUDA_TRY(cudaFuncSetAttribute(qleaf_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ncs));
   const int blocks = (int)std::min<long long>(ceil_div(nq, 256), 8LL * num_sms());
   qleaf_kernel<<<blocks, 256, ncs, st>>>(tv, Q, nq, qleaf, cnt);
   ANNF_CHECK_LAUNCH();
-  leaf_scan_kernel<<<1, 1024, 0, st>>>(cnt, L, off, cursor, choff);
+  const int tiles = ceil_div(L, kScanTile);
+  leaf_tile_sums_kernel<<<tiles, kScanTile, 0, st>>>(cnt, L, tile_tot);
+  ANNF_CHECK_LAUNCH();
+  leaf_scan_kernel<<<tiles, kScanTile, 0, st>>>(cnt, L, tile_tot, off, cursor, choff);
   ANNF_CHECK_LAUNCH();
   qscatter_kernel<<<blocks, 256, 0, st>>>(qleaf, nq, cursor, qorder);
   ANNF_CHECK_LAUNCH();
