@@ -112,14 +112,18 @@ __device__ __forceinline__ bool mbar_wait_clock(uint64_t* mbar, uint32_t phase) 
 // ---------------------------------------------------------------------------------------------
 // grouping queries by natural leaf
 // ---------------------------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) qleaf_kernel(TreeView<float> tv, const float* __restrict__ Q, long long nq,
-                                                    int* __restrict__ qleaf, int* __restrict__ cnt) {
+// the top kQleafLevels levels of nodes in shared memory (one 1024-thread CTA per SM holds them)
+constexpr int kQleafLevels = 14;
+constexpr int kQleafThreads = 1024;
+__global__ void __launch_bounds__(kQleafThreads) qleaf_kernel(TreeView<float> tv, const float* __restrict__ Q,
+                                                              long long nq, int* __restrict__ qleaf,
+                                                              int* __restrict__ cnt) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   unsigned char* p = smem_raw;
   NodeCache<float> nc;
-  nc.carve(p, tv.depth);
+  nc.carve(p, tv.depth, kQleafLevels);
   if (smem_overrun(smem_raw, p, tv.status)) return;
-  nc.fill(tv);
+  nc.fill(tv, kQleafLevels);
   __syncthreads();
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < nq; i += (long long)gridDim.x * blockDim.x) {
     const int lf = descend(tv, nc, Q + i * tv.d);
@@ -717,10 +721,11 @@ int natural_knn_tc(annf_handle* h, const float* Q, long long nq, int K, int prec
   int* item_leaf = choff + L + 1;
   int* tile_tot = item_leaf + (size_t)L + (size_t)nq / kTcThreads + 1;  // [2 * tiles]
   ANNF_CUDA_TRY(cudaMemsetAsync(cnt, 0, (size_t)L * sizeof(int), st));
-  const size_t ncs = NodeCache<float>::bytes(h->depth);
+  const size_t ncs = NodeCache<float>::bytes(h->depth, kQleafLevels);
   ANNF_CUDA_TRY(cudaFuncSetAttribute(qleaf_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ncs));
   const int blocks = (int)std::min<long long>(ceil_div(nq, 256), 8LL * num_sms());
-  qleaf_kernel<<<blocks, 256, ncs, st>>>(tv, Q, nq, qleaf, cnt);
+  const int qblocks = (int)std::min<long long>(ceil_div(nq, kQleafThreads), num_sms());
+  qleaf_kernel<<<qblocks, kQleafThreads, ncs, st>>>(tv, Q, nq, qleaf, cnt);
   ANNF_CHECK_LAUNCH();
   const int tiles = ceil_div(L, kScanTile);
   leaf_tile_sums_kernel<<<tiles, kScanTile, 0, st>>>(cnt, L, tile_tot);

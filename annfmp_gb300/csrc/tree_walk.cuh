@@ -16,8 +16,8 @@ struct NodeCache {
   int* axis;
   T* split;
   int n;  // cached nodes
-  __device__ void fill(const TreeView<T>& tv) {
-    const int lv = tv.depth < kCacheLevels ? tv.depth : kCacheLevels;
+  __device__ void fill(const TreeView<T>& tv, int levels = kCacheLevels) {
+    const int lv = tv.depth < levels ? tv.depth : levels;
     n = (1 << lv) - 1;
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
       axis[i] = __ldg(tv.node_axis + i);
@@ -33,13 +33,13 @@ struct NodeCache {
       s = __ldg(tv.node_split + node);
     }
   }
-  static size_t bytes(int depth) {
-    const int lv = depth < kCacheLevels ? depth : kCacheLevels;
+  static size_t bytes(int depth, int levels = kCacheLevels) {
+    const int lv = depth < levels ? depth : levels;
     const size_t m = (size_t)(1 << lv);
     return m * sizeof(int) + m * sizeof(T) + 32;
   }
-  __device__ void carve(unsigned char*& p, int depth) {
-    const int lv = depth < kCacheLevels ? depth : kCacheLevels;
+  __device__ void carve(unsigned char*& p, int depth, int levels = kCacheLevels) {
+    const int lv = depth < levels ? depth : levels;
     const int m = 1 << lv;
     axis = reinterpret_cast<int*>(p);
     split = reinterpret_cast<T*>(((uintptr_t)(axis + m) + 7) & ~uintptr_t(7));
