@@ -129,7 +129,8 @@ class ClockSampler:
 
 
 # ---------------------------------------------------------------------------------------------
-# algorithmic bytes per launch of each stage ("roofline")
+# algorithmic bytes of each stage per NNF: the bytes the algorithm touches (served by DRAM, L2 or
+# L1), the numerator of the roofline's achieved bandwidth
 # ---------------------------------------------------------------------------------------------
 def stage_bytes(stage, w, n_a, n_b, depth, n_cols, it=1, nrand=1, n_prop=0):
     d, k, P = w["dim_reduced"], w["n_neighbors"], w["psize"] ** 2 * 3
