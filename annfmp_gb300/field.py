@@ -78,7 +78,7 @@ class ANNFieldPropKDTreeGB300:
     def __init__(self, n_neighbors=3, psize=8, dim_reduced=5, n_subset=1000, leaf_size=64, n_jobs=-1,
                  propagate=True, select_best_nn=True, float_type="float", verbose=1, seed=0, device=0,
                  form="plain", iters=4, proposal=None, pca_solver=None, pca_iters=6, leaf_precision=None,
-                 projection=None, search=(1, 4), graph="auto"):
+                 projection=None, search=(1, 2), graph="auto"):
         """Reference parameters, plus: ``form`` "plain" (the reference's row-sequential method,
         the drop-in) or "parallel" (natural-leaf candidates + proposals + parallel propagation,
         every candidate checked by exact raw-patch distance); ``iters`` propagation passes of the
