@@ -224,6 +224,25 @@ class ANNFieldPropKDTreeGB300:
         return g["nn"].clone()
 
     def _fit(self, image_a, image_b, sync):
+        """With proposals, the NNF's own chain runs on a high-priority stream: the side stream's
+        proposal kernels then fill idle SMs without holding back the eigensolver (a one-CTA kernel
+        that needs a whole SM)."""
+        if self.form == "plain" or self.proposal is None:
+            return self._fit_chain(image_a, image_b, sync)
+        dev = require_cuda(self.device)
+        caller = torch.cuda.current_stream(dev)
+        hp = getattr(self, "_hp", None)
+        if hp is None:
+            hp = self._hp = torch.cuda.Stream(dev, priority=-8)  # clamped to the highest priority
+        hp.wait_stream(caller)
+        with torch.cuda.stream(hp):
+            nn = self._fit_chain(image_a, image_b, sync)
+        caller.wait_stream(hp)
+        if isinstance(nn, torch.Tensor):
+            nn.record_stream(caller)
+        return nn
+
+    def _fit_chain(self, image_a, image_b, sync):
         numpy.random.seed(self.seed)  # annfmp/openmp/base.py:60
         dev = require_cuda(self.device)
         real = self._get_torch_float_type()
