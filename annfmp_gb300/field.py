@@ -330,12 +330,25 @@ class ANNFieldPropKDTreeGB300:
         proj = self.projection
         if proj is None:
             proj = "fp16" if (self.form != "plain" and real == torch.float32 and p * p * c <= 256 and d <= 32) else "exact"
+        a_side = None
         if proj == "fp16":
             if real != torch.float32:
                 raise ValueError("the FP16 projection needs float_type='float'")
-            for img, hh, ww, dst in ((A, ha, wa, self.patches_a_reduced_), (B, hb, wb, self.patches_b_reduced_)):
-                h.call("annf_project_f16", ptr(img), hh, ww, c, p, ptr(self.components_), ptr(self.mean_), d,
-                       ptr(dst), st)
+            h.call("annf_project_f16", ptr(B), hb, wb, c, p, ptr(self.components_), ptr(self.mean_), d,
+                   ptr(self.patches_b_reduced_), st)
+            # A's patches are needed only from the leaf stage on: projected on another stream (with
+            # a handle of its own) while the tree over B is built, whose small per-level kernels
+            # leave SMs idle
+            a_side = self._a_stream if getattr(self, "_a_stream", None) is not None else torch.cuda.Stream(dev)
+            self._a_stream = a_side
+            if getattr(self, "_a_handle", None) is None:
+                self._a_handle = _lib.Handle(dev.index)
+            a_side.wait_stream(torch.cuda.current_stream(dev))
+            with torch.cuda.stream(a_side):
+                self._a_handle.call("annf_project_f16", ptr(A), ha, wa, c, p, ptr(self.components_), ptr(self.mean_),
+                                    d, ptr(self.patches_a_reduced_), stream_ptr(dev))
+            for t in (A, self.components_, self.mean_, self.patches_a_reduced_):
+                t.record_stream(a_side)
         elif proj == "exact":
             h.call("annf_project", ptr(A), ha, wa, c, p, ptr(self.components_), ptr(self.mean_), d, real_type,
                    ptr(self.patches_a_reduced_), st)
@@ -348,6 +361,9 @@ class ANNFieldPropKDTreeGB300:
         # (4) k-d tree over B (annfmp/openmp/base.py:95-103)
         tree.fit(self.patches_b_reduced_)
         ev["t3"].record()
+
+        if a_side is not None:
+            torch.cuda.current_stream(dev).wait_stream(a_side)
 
         # (5) rows (annfmp/openmp/base.py:113-125)
         assert self.leaf_size > self.n_neighbors
