@@ -3,7 +3,9 @@
 // The full FP64 eigendecomposition of the P x P covariance (P = 243 for 9x9x3 patches) costs
 // milliseconds in a library solver, while the NNF only needs the top n_components. This solver:
 //   1. simultaneous (subspace) iteration in FP32 on a block of b >= n_components vectors, one CTA:
-//      Z = C Q, then column-scaled Cholesky-QR, `iters` times (C kept in FP32 in global memory);
+//      Z = C Q, then column-scaled Cholesky-QR, `iters` times (C kept in FP32 in global memory),
+//      from a random block (the first step's Cholesky-QR orthonormalises it); the last step's Q
+//      goes on as is, its loss of orthogonality in FP32 being absorbed by the FP64 Gram below;
 //   2. Rayleigh-Ritz in FP64 on span(Q): W = C Q, G = Q^T Q, T = Q^T W over many CTAs;
 //   3. the b x b generalised problem T y = lambda G y in FP64 on one CTA: Cholesky G = R^T R
 //      (columns with a vanishing pivot are dropped), T~ = R^-T T R^-1, cyclic Jacobi on T~, and
@@ -28,6 +30,12 @@ __device__ __forceinline__ float warp_sum_f(float v) {
   return v;
 }
 __device__ __forceinline__ double warp_sum_d(double v) {
+#pragma unroll
+  for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+template <typename R>
+__device__ __forceinline__ R warp_sum_r(R v) {
 #pragma unroll
   for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   return v;
@@ -112,7 +120,8 @@ __device__ void cholqr_rows(float* Z, float* Q, int P, float* G, float* Ri, floa
 
 // step 1: one CTA. Z = C Q in FP32 with C (FP32 copy C32, global) read once per step: item
 // (i, s) accumulates row i over the s-th of KS slices of k into registers, the KS partial rows
-// are summed in a fixed order (deterministic), then Cholesky-QR. Qout [B][P] FP32.
+// are summed in a fixed order (deterministic), then Cholesky-QR. Qout [B][P] FP32. (Each
+// Cholesky-QR is a chain of dependent steps on one warp, ~33 us at b = 24: it runs once per step.)
 template <int B>
 __global__ void __launch_bounds__(kSubThreads) subspace_iter_kernel(const double* __restrict__ C, int P, int KS,
                                                                     int iters, float* C32, float* __restrict__ Qout,
@@ -129,10 +138,9 @@ __global__ void __launch_bounds__(kSubThreads) subspace_iter_kernel(const double
   for (long long e = tid; e < (long long)P * P; e += nt) C32[e] = (float)C[e];
   for (int e = tid; e < B * P; e += nt) {
     const int i = e / B, j = e - i * B;
-    Z[e] = (float)(mix32((uint32_t)(j * P + i) * 2654435761u + 12345u) >> 8) * (1.0f / 16777216.0f) - 0.5f;
+    Q[e] = (float)(mix32((uint32_t)(j * P + i) * 2654435761u + 12345u) >> 8) * (1.0f / 16777216.0f) - 0.5f;
   }
   __syncthreads();
-  cholqr_rows<B>(Z, Q, P, G, Ri, dsc);
   const int kper = (P + KS - 1) / KS;
   for (int it = 0; it < iters; ++it) {
     __threadfence_block();
@@ -169,10 +177,6 @@ __global__ void __launch_bounds__(kSubThreads) subspace_iter_kernel(const double
     __syncthreads();
     cholqr_rows<B>(Z, Q, P, G, Ri, dsc);
   }
-  // second pass: orthogonal to working precision
-  for (int e = tid; e < P * B; e += nt) Z[e] = Q[e];
-  __syncthreads();
-  cholqr_rows<B>(Z, Q, P, G, Ri, dsc);
   for (int e = tid; e < B * P; e += nt) {
     const int j = e / P, i = e - j * P;
     Qout[e] = Q[i * B + j];
@@ -224,27 +228,27 @@ __global__ void rr_gram_kernel(int P, int b, const float* __restrict__ Q, const 
 // Newton steps on rsqrt (exactly orthogonal in FP64; an FP32 angle leaves ~1e-7 of apq, removed
 // by the next sweep), so the loop has no FP64 division or square root.
 template <typename R>
-__device__ void jacobi_sweeps(R* T, R* V, int m, int max_sweeps, double tol, double* s_cs, double* s_sn, int* s_p,
-                              int* s_q, double* s_off, double* s_tot) {
+__device__ void jacobi_sweeps(R* T, R* V, int m, int max_sweeps, double tol, R* s_cs, R* s_sn, int* s_p, int* s_q,
+                              R* s_off, R* s_tot) {
   const int tid = threadIdx.x, nt = blockDim.x;
   const int M = (m + 1) & ~1, half = M / 2;
   for (int sweep = 0; sweep < max_sweeps && m > 1; ++sweep) {
     if (tid < 32) {
-      double off = 0.0, tot = 0.0;
+      R off = 0, tot = 0;
       for (int e = tid; e < m * m; e += 32) {
-        const double v = (double)T[e] * (double)T[e];
+        const R v = T[e] * T[e];
         tot += v;
         if (e / m != e % m) off += v;
       }
-      off = warp_sum_d(off);
-      tot = warp_sum_d(tot);
+      off = warp_sum_r(off);
+      tot = warp_sum_r(tot);
       if (tid == 0) {
         *s_off = off;
         *s_tot = tot;
       }
     }
     __syncthreads();
-    if (!(*s_off > tol * *s_tot)) break;
+    if (!(*s_off > (R)tol * *s_tot)) break;
     for (int round = 0; round < M - 1; ++round) {
       if (tid < half) {
         auto player = [&](int j) { return j == 0 ? 0 : 1 + (j - 1 + round) % (M - 1); };
@@ -254,7 +258,7 @@ __device__ void jacobi_sweeps(R* T, R* V, int m, int max_sweeps, double tol, dou
           p = q;
           q = t;
         }
-        double cs = 1.0, sn = 0.0;
+        R cs = 1, sn = 0;
         if (q < m) {
           const R apq = T[p * m + q], app = T[p * m + p], aqq = T[q * m + q];
           if (sizeof(R) == 8) {
@@ -288,8 +292,8 @@ __device__ void jacobi_sweeps(R* T, R* V, int m, int max_sweeps, double tol, dou
       for (int e = tid; e < half * m; e += nt) {  // rows p, q
         const int i = e / m, k = e - i * m;
         const int p = s_p[i], q = s_q[i];
-        if (q < 0 || s_sn[i] == 0.0) continue;
-        const R cs = (R)s_cs[i], sn = (R)s_sn[i];
+        if (q < 0 || s_sn[i] == (R)0) continue;
+        const R cs = s_cs[i], sn = s_sn[i];
         const R tp = T[p * m + k], tq = T[q * m + k];
         T[p * m + k] = cs * tp - sn * tq;
         T[q * m + k] = sn * tp + cs * tq;
@@ -298,8 +302,8 @@ __device__ void jacobi_sweeps(R* T, R* V, int m, int max_sweeps, double tol, dou
       for (int e = tid; e < half * m; e += nt) {  // columns p, q and the eigenvectors
         const int i = e / m, k = e - i * m;
         const int p = s_p[i], q = s_q[i];
-        if (q < 0 || s_sn[i] == 0.0) continue;
-        const R cs = (R)s_cs[i], sn = (R)s_sn[i];
+        if (q < 0 || s_sn[i] == (R)0) continue;
+        const R cs = s_cs[i], sn = s_sn[i];
         const R tp = T[k * m + p], tq = T[k * m + q];
         T[k * m + p] = cs * tp - sn * tq;
         T[k * m + q] = sn * tp + cs * tq;
@@ -406,6 +410,7 @@ __global__ void __launch_bounds__(kRrThreads) rr_solve_kernel(int b, int ncomp, 
   // then diagonal to ~1e-7 of its norm, and FP64 sweeps on M (quadratic convergence: one or two)
   // finish the small eigenproblem in FP64, accumulating into V.
   __shared__ double s_cs[kMaxBlock / 2], s_sn[kMaxBlock / 2];
+  __shared__ float f_cs[kMaxBlock / 2], f_sn[kMaxBlock / 2], f_off, f_tot;  // the FP32 sweeps' own scratch
   __shared__ int s_p[kMaxBlock / 2], s_q[kMaxBlock / 2];
   float* V32 = reinterpret_cast<float*>(V);  // FP32 phase: V32 and T32 share V's storage
   float* T32 = V32 + kMaxBlock * kMaxBlock;
@@ -414,7 +419,7 @@ __global__ void __launch_bounds__(kRrThreads) rr_solve_kernel(int b, int ncomp, 
     V32[e] = (e / m == e % m) ? 1.f : 0.f;
   }
   __syncthreads();
-  jacobi_sweeps<float>(T32, V32, m, 16, 1e-12, s_cs, s_sn, s_p, s_q, &s_off, &s_tot);
+  jacobi_sweeps<float>(T32, V32, m, 16, 1e-12, f_cs, f_sn, s_p, s_q, &f_off, &f_tot);
   {  // V (FP64) <- V32: through registers, the two share storage
     double v[(kMaxBlock * kMaxBlock + kRrThreads - 1) / kRrThreads];
     int u = 0;
