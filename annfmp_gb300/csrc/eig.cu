@@ -53,9 +53,9 @@ __device__ __forceinline__ uint32_t mix32(uint32_t x) {
 // Orthonormalise the B columns of Z ([P][B] row-major, shared memory) by Cholesky-QR, writing Q
 // ([P][B]): every column is scaled to unit norm first (in subspace iteration Z = C Q has nearly
 // orthogonal columns, so the scaled Gram matrix is close to the identity and FP32 Cholesky is
-// stable), R^-1 is formed explicitly by one warp, and Q = Z D R^-1 is a small product that all
-// threads share (no per-row dependent chains). A column whose norm vanishes is replaced by a
-// basis vector. G, Ri: B x B shared scratch; d: B shared column scales.
+// stable), R^-1 is formed explicitly by one warp, and Q = Z D R^-1 is a small product (a row per
+// thread). A column whose norm vanishes is replaced by a basis vector. G, Ri: B x B shared
+// scratch; d: B shared column scales. Q's contents on entry are overwritten (used as scratch).
 template <int B>
 __device__ void cholqr_rows(float* Z, float* Q, int P, float* G, float* Ri, float* d) {
   const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5;
@@ -71,12 +71,30 @@ __device__ void cholqr_rows(float* Z, float* Q, int P, float* G, float* Ri, floa
     if (lane == 0) d[j] = rsqrtf(sq);
   }
   __syncthreads();
-  // scaled Gram matrix (upper triangle), one thread per entry
+  // scaled Gram matrix (upper triangle): a thread per entry and part of the rows (three parts
+  // when the rows allow), the partial sums kept in Q (its old contents are dead here) and added
+  // in a fixed order
+  constexpr int kUpper = B * (B + 1) / 2;
+  const int parts = (P >= 3 * B && 3 * kUpper <= nt) ? 3 : 1;
+  const int rows = (P + parts - 1) / parts;
+  for (int e = tid; e < parts * kUpper; e += nt) {
+    const int s = e / kUpper;
+    int r = 0, t = e - s * kUpper;
+    while (t >= B - r) {
+      t -= B - r;
+      ++r;
+    }
+    const int c = r + t;
+    float g = 0.f;
+    const int i1 = min(P, (s + 1) * rows);
+    for (int i = s * rows; i < i1; ++i) g = fmaf(Z[i * B + r], Z[i * B + c], g);
+    Q[s * B * B + r * B + c] = g;
+  }
+  __syncthreads();
   for (int e = tid; e < B * B; e += nt) {
     const int r = e / B, c = e - r * B;
     if (c < r) continue;
-    float g = 0.f;
-    for (int i = 0; i < P; ++i) g = fmaf(Z[i * B + r], Z[i * B + c], g);
+    const float g = parts == 3 ? (Q[e] + Q[B * B + e]) + Q[2 * B * B + e] : Q[e];
     G[e] = g * d[r] * d[c];
   }
   __syncthreads();
@@ -88,32 +106,63 @@ __device__ void cholqr_rows(float* Z, float* Q, int P, float* G, float* Ri, floa
       __syncwarp();
       for (int j = k + lane; j < B; j += 32) G[k * B + j] = r > 0.f ? (j == k ? r : G[k * B + j] / r) : (j == k ? 1.f : 0.f);
       __syncwarp();
+      // row k of R in registers first: the column updates then have no load that waits on an
+      // earlier store
+      float row[B];
+#pragma unroll
+      for (int u = 0; u < B; ++u) row[u] = k + 1 + u < B ? G[k * B + k + 1 + u] : 0.f;
       for (int j = k + 1 + lane; j < B; j += 32) {
         const float rkj = G[k * B + j];
-        for (int i = k + 1; i <= j; ++i) G[i * B + j] = fmaf(-G[k * B + i], rkj, G[i * B + j]);
+#pragma unroll
+        for (int u = 0; u < B - 1; ++u) {
+          const int i = k + 1 + u;
+          if (i <= j) G[i * B + j] = fmaf(-row[u], rkj, G[i * B + j]);
+        }
       }
       __syncwarp();
     }
-    // R^-1 (upper), lanes over columns: back substitution of R x = e_j
+    // R^-1 (upper), lanes over columns: back substitution of R x = e_j with the column in
+    // registers; each sum runs from the oldest entry of x to the newest, so only its last term
+    // waits on the previous step
     for (int j = lane; j < B; j += 32) {
-      for (int i = B - 1; i >= 0; --i) {
+      float x[B];
+#pragma unroll
+      for (int ii = 0; ii < B; ++ii) {
+        const int i = B - 1 - ii;
         float v = i == j ? 1.f : 0.f;
-        if (i > j) {
-          Ri[i * B + j] = 0.f;
-          continue;
-        }
-        for (int t = i + 1; t <= j; ++t) v = fmaf(-G[i * B + t], Ri[t * B + j], v);
-        Ri[i * B + j] = v / G[i * B + i];
+#pragma unroll
+        for (int t = B - 1; t > i; --t) v = fmaf(-G[i * B + t], x[t], v);  // x[t] = 0 beyond j
+        x[i] = i <= j ? v / G[i * B + i] : 0.f;
       }
+#pragma unroll
+      for (int i = 0; i < B; ++i) Ri[i * B + j] = x[i];
     }
   }
   __syncthreads();
-  // Q = Z D R^-1 (R^-1 upper: column j uses t <= j)
-  for (int e = tid; e < P * B; e += nt) {
-    const int i = e / B, j = e - i * B;
-    float q = 0.f;
-    for (int t = 0; t <= j; ++t) q = fmaf(Z[i * B + t] * d[t], Ri[t * B + j], q);
-    Q[e] = q;
+  // Q = Z D R^-1 (R^-1 upper: column j uses t <= j, summed in increasing t)
+  if constexpr (B <= 24) {
+    // a row per thread, its outputs in registers: R^-1 is read as broadcasts, and no lane idles
+    // on a shorter column than its neighbours'
+    for (int i = tid; i < P; i += nt) {
+      float q[B];
+#pragma unroll
+      for (int j = 0; j < B; ++j) q[j] = 0.f;
+#pragma unroll
+      for (int t = 0; t < B; ++t) {
+        const float zt = Z[i * B + t] * d[t];
+#pragma unroll
+        for (int j = t; j < B; ++j) q[j] = fmaf(zt, Ri[t * B + j], q[j]);
+      }
+#pragma unroll
+      for (int j = 0; j < B; ++j) Q[i * B + j] = q[j];
+    }
+  } else {
+    for (int e = tid; e < P * B; e += nt) {
+      const int i = e / B, j = e - i * B;
+      float q = 0.f;
+      for (int t = 0; t <= j; ++t) q = fmaf(Z[i * B + t] * d[t], Ri[t * B + j], q);
+      Q[e] = q;
+    }
   }
   __syncthreads();
 }
