@@ -7,9 +7,10 @@
 //      from a random block (the first step's Cholesky-QR orthonormalises it); the last step's Q
 //      goes on as is, its loss of orthogonality in FP32 being absorbed by the FP64 Gram below;
 //   2. Rayleigh-Ritz in FP64 on span(Q): W = C Q, G = Q^T Q, T = Q^T W over many CTAs;
-//   3. the b x b generalised problem T y = lambda G y in FP64 on one CTA: Cholesky G = R^T R
-//      (columns with a vanishing pivot are dropped), T~ = R^-T T R^-1, cyclic Jacobi on T~, and
-//      coefficients x = R^-1 y;
+//   3. the b x b generalised problem T y = lambda G y in FP64 on one CTA: W = G^-1/2 by a short
+//      binomial series when G is within FP32 rounding of the identity (the usual case; otherwise
+//      Cholesky G = R^T R with W = R^-1, dropping columns with a vanishing pivot), T~ = W^T T W,
+//      cyclic Jacobi on T~, and coefficients x = W y;
 //   4. components = Q x, in decreasing Ritz value, each signed so that its largest |entry| is
 //      positive (the sign convention of the exact solver).
 // The covariance and the small eigenproblem stay in FP64; only the power steps that find the
@@ -367,6 +368,7 @@ __device__ void jacobi_sweeps(R* T, R* V, int m, int max_sweeps, double tol, R* 
 
 // step 3: one CTA, FP64. Writes X [ncomp][b] (coefficients of each component in the Q basis).
 constexpr int kRrThreads = 256;  // rr_solve_kernel's block: its register arrays assume it
+constexpr double kNearIdentity = 2e-5;  // largest |G - I| entry for the series path
 
 __global__ void __launch_bounds__(kRrThreads) rr_solve_kernel(int b, int ncomp, const double* __restrict__ Gg,
                                                        const double* __restrict__ Tg, double* __restrict__ Xout,
@@ -383,69 +385,137 @@ __global__ void __launch_bounds__(kRrThreads) rr_solve_kernel(int b, int ncomp, 
     T[e] = 0.5 * (Tg[i * b + j] + Tg[j * b + i]);
   }
   __syncthreads();
-  // Cholesky G = R^T R in place, right-looking (upper triangle holds R; the trailing block is
-  // updated by all threads); vanishing pivots drop their column
-  __shared__ double s_gmax, s_piv;
-  if (tid == 0) {
-    double gmax = 0.0;
-    for (int i = 0; i < b; ++i) gmax = fmax(gmax, G[i * b + i]);
-    s_gmax = gmax;
-    s_m = 0;
+  // G = Q^T Q is within FP32 rounding of the identity when Q comes out of Cholesky-QR. Then
+  // W = G^-1/2 comes from the binomial series of (I + E)^-1/2, E = G - I, to the E^4 term (with
+  // max |E_ij| <= kNearIdentity the first term left out is below FP64 rounding), T~ = W T W and
+  // x = W y: products that all threads share, in place of a serial Cholesky and triangular
+  // solves. Otherwise (a degenerate block) Cholesky, dropping the columns with vanishing pivots.
+  __shared__ int s_near;
+  if (tid < 32) {
+    double e = 0.0;
+    for (int idx = tid; idx < b * b; idx += 32) e = fmax(e, fabs(G[idx] - (idx / b == idx % b ? 1.0 : 0.0)));
+#pragma unroll
+    for (int o = 16; o; o >>= 1) e = fmax(e, __shfl_xor_sync(0xffffffffu, e, o));
+    if (tid == 0) s_near = e <= kNearIdentity;
   }
   __syncthreads();
-  for (int k = 0; k < b; ++k) {
-    if (tid == 0) {
-      const double piv = G[k * b + k];
-      const bool ok = piv > 1e-10 * s_gmax && piv > 0.0;
-      keep[k] = ok ? s_m++ : -1;
-      s_piv = ok ? sqrt(piv) : 0.0;
+  const bool near_identity = s_near != 0;
+  int m;
+  if (near_identity) {
+    m = b;
+    for (int k = tid; k < b; k += nt) keep[k] = k;
+    constexpr double kC[5] = {1.0, 0.5, 0.375, 0.3125, 0.2734375};  // binom(2n, n) / 4^n
+    // G <- F = I - G; V <- S = c4 I; then S <- c_n I + F S for n = 3, 2, 1, 0 (the last is W)
+    for (int e = tid; e < b * b; e += nt) {
+      const bool dg = e / b == e % b;
+      G[e] = (dg ? 1.0 : 0.0) - G[e];
+      V[e] = dg ? kC[4] : 0.0;
     }
     __syncthreads();
-    const double r = s_piv;
-    for (int j = k + tid; j < b; j += nt) G[k * b + j] = r > 0.0 ? (j == k ? r : G[k * b + j] / r) : 0.0;
+    double acc[(kMaxBlock * kMaxBlock + kRrThreads - 1) / kRrThreads];
+    for (int n = 3; n >= 0; --n) {
+      int u = 0;
+      for (int e = tid; e < b * b; e += nt) {
+        const int i = e / b, j = e - i * b;
+        double a = i == j ? kC[n] : 0.0;
+        for (int k = 0; k < b; ++k) a = fma(G[i * b + k], V[k * b + j], a);
+        acc[u++] = a;
+      }
+      __syncthreads();
+      u = 0;
+      for (int e = tid; e < b * b; e += nt) V[e] = acc[u++];
+      __syncthreads();
+    }
+    for (int e = tid; e < b * b; e += nt) G[e] = V[e];  // G <- W (x = W y at the end)
     __syncthreads();
-    if (r > 0.0) {
-      const int tw = b - k - 1;
-      for (int e = tid; e < tw * tw; e += nt) {
-        const int i = k + 1 + e / tw, j = k + 1 + e % tw;
-        if (j >= i) G[i * b + j] -= G[k * b + i] * G[k * b + j];
+    // T~ = W T W into V (where the other path leaves it): Y = T W, then W Y
+    int u = 0;
+    for (int e = tid; e < b * b; e += nt) {
+      const int i = e / b, j = e - i * b;
+      double a = 0.0;
+      for (int k = 0; k < b; ++k) a = fma(T[i * b + k], G[k * b + j], a);
+      acc[u++] = a;
+    }
+    __syncthreads();
+    u = 0;
+    for (int e = tid; e < b * b; e += nt) V[e] = acc[u++];
+    __syncthreads();
+    u = 0;
+    for (int e = tid; e < b * b; e += nt) {
+      const int i = e / b, j = e - i * b;
+      double a = 0.0;
+      for (int k = 0; k < b; ++k) a = fma(G[k * b + i], V[k * b + j], a);  // W symmetric
+      acc[u++] = a;
+    }
+    __syncthreads();
+    u = 0;
+    for (int e = tid; e < b * b; e += nt) V[e] = acc[u++];
+    __syncthreads();
+  } else {
+    // Cholesky G = R^T R in place, right-looking (upper triangle holds R; the trailing block is
+    // updated by all threads); vanishing pivots drop their column
+    __shared__ double s_gmax, s_piv;
+    if (tid == 0) {
+      double gmax = 0.0;
+      for (int i = 0; i < b; ++i) gmax = fmax(gmax, G[i * b + i]);
+      s_gmax = gmax;
+      s_m = 0;
+    }
+    __syncthreads();
+    for (int k = 0; k < b; ++k) {
+      if (tid == 0) {
+        const double piv = G[k * b + k];
+        const bool ok = piv > 1e-10 * s_gmax && piv > 0.0;
+        keep[k] = ok ? s_m++ : -1;
+        s_piv = ok ? sqrt(piv) : 0.0;
+      }
+      __syncthreads();
+      const double r = s_piv;
+      for (int j = k + tid; j < b; j += nt) G[k * b + j] = r > 0.0 ? (j == k ? r : G[k * b + j] / r) : 0.0;
+      __syncthreads();
+      if (r > 0.0) {
+        const int tw = b - k - 1;
+        for (int e = tid; e < tw * tw; e += nt) {
+          const int i = k + 1 + e / tw, j = k + 1 + e % tw;
+          if (j >= i) G[i * b + j] -= G[k * b + i] * G[k * b + j];
+        }
+      }
+      __syncthreads();
+    }
+    m = s_m;
+    // compact the kept columns: R~ (m x m upper), T (m x m); V <- T restricted
+    // (kept column k maps to keep[k]); reuse V as scratch for the compacted T
+    for (int e = tid; e < b * b; e += nt) {
+      const int i = e / b, j = e - i * b;
+      if (keep[i] >= 0 && keep[j] >= 0) V[keep[i] * m + keep[j]] = T[e];
+    }
+    __syncthreads();
+    for (int e = tid; e < b * b; e += nt) {
+      const int i = e / b, j = e - i * b;
+      if (keep[i] >= 0 && keep[j] >= 0) T[keep[i] * m + keep[j]] = (j >= i) ? G[e] : 0.0;  // T now holds R~
+    }
+    __syncthreads();
+    for (int e = tid; e < m * m; e += nt) G[e] = T[e];  // G = R~ (m x m, upper)
+    __syncthreads();
+    // X = R~^-T Tm : forward substitution per column (R~^T lower)
+    for (int c = tid; c < m; c += nt) {
+      for (int i = 0; i < m; ++i) {
+        double v = V[i * m + c];
+        for (int t = 0; t < i; ++t) v -= G[t * m + i] * T[t * m + c];
+        T[i * m + c] = v / G[i * m + i];
+      }
+    }
+    __syncthreads();
+    // T~ = X R~^-1 : solve T~ R~ = X row by row
+    for (int r = tid; r < m; r += nt) {
+      for (int j = 0; j < m; ++j) {
+        double v = T[r * m + j];
+        for (int t = 0; t < j; ++t) v -= V[r * m + t] * G[t * m + j];
+        V[r * m + j] = v / G[j * m + j];
       }
     }
     __syncthreads();
   }
-  const int m = s_m;
-  // compact the kept columns: R~ (m x m upper), T (m x m); V <- T restricted
-  // (kept column k maps to keep[k]); reuse V as scratch for the compacted T
-  for (int e = tid; e < b * b; e += nt) {
-    const int i = e / b, j = e - i * b;
-    if (keep[i] >= 0 && keep[j] >= 0) V[keep[i] * m + keep[j]] = T[e];
-  }
-  __syncthreads();
-  for (int e = tid; e < b * b; e += nt) {
-    const int i = e / b, j = e - i * b;
-    if (keep[i] >= 0 && keep[j] >= 0) T[keep[i] * m + keep[j]] = (j >= i) ? G[e] : 0.0;  // T now holds R~
-  }
-  __syncthreads();
-  for (int e = tid; e < m * m; e += nt) G[e] = T[e];  // G = R~ (m x m, upper)
-  __syncthreads();
-  // X = R~^-T Tm : forward substitution per column (R~^T lower)
-  for (int c = tid; c < m; c += nt) {
-    for (int i = 0; i < m; ++i) {
-      double v = V[i * m + c];
-      for (int t = 0; t < i; ++t) v -= G[t * m + i] * T[t * m + c];
-      T[i * m + c] = v / G[i * m + i];
-    }
-  }
-  __syncthreads();
-  // T~ = X R~^-1 : solve T~ R~ = X row by row
-  for (int r = tid; r < m; r += nt) {
-    for (int j = 0; j < m; ++j) {
-      double v = T[r * m + j];
-      for (int t = 0; t < j; ++t) v -= V[r * m + t] * G[t * m + j];
-      V[r * m + j] = v / G[j * m + j];
-    }
-  }
-  __syncthreads();
   // symmetrise into T, V = I
   for (int e = tid; e < m * m; e += nt) {
     const int i = e / m, j = e - i * m;
@@ -552,6 +622,18 @@ __global__ void __launch_bounds__(kRrThreads) rr_solve_kernel(int b, int ncomp, 
     order[r] = i;
   }
   __syncthreads();
+  if (near_identity) {  // x = W y for the selected Ritz vectors, a thread per entry
+    for (int e = tid; e < ncomp * b; e += nt) {
+      const int c = e / b, k = e - c * b;
+      const int col = order[c];
+      double a = 0.0;
+      for (int j = 0; j < b; ++j) a = fma(G[k * b + j], V[j * m + col], a);
+      Xout[(size_t)c * b + k] = a;
+    }
+    if (lambda_out)
+      for (int c = tid; c < ncomp; c += nt) lambda_out[c] = lam[order[c]];
+    return;
+  }
   // x = R~^-1 y for the selected Ritz vectors, scattered back to the b kept columns
   for (int c = tid; c < ncomp; c += nt) {
     double* x = Xout + (size_t)c * b;
