@@ -280,7 +280,7 @@ __global__ void rr_gram_kernel(int P, int b, const float* __restrict__ Q, const 
 template <typename R>
 __device__ void jacobi_sweeps(R* T, R* V, int m, int max_sweeps, double tol, R* s_cs, R* s_sn, int* s_p, int* s_q,
                               R* s_off, R* s_tot) {
-  const int tid = threadIdx.x, nt = blockDim.x;
+  const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
   const int M = (m + 1) & ~1, half = M / 2;
   for (int sweep = 0; sweep < max_sweeps && m > 1; ++sweep) {
     if (tid < 32) {
@@ -301,7 +301,10 @@ __device__ void jacobi_sweeps(R* T, R* V, int m, int max_sweeps, double tol, R* 
     if (!(*s_off > (R)tol * *s_tot)) break;
     for (int round = 0; round < M - 1; ++round) {
       if (tid < half) {
-        auto player = [&](int j) { return j == 0 ? 0 : 1 + (j - 1 + round) % (M - 1); };
+        auto player = [&](int j) {  // 1 + (j - 1 + round) mod (M - 1), both terms below M - 1
+          const int x = j - 1 + round;
+          return j == 0 ? 0 : 1 + (x >= M - 1 ? x - (M - 1) : x);
+        };
         int p = player(tid), q = player(M - 1 - tid);
         if (p > q) {
           const int t = p;
@@ -325,8 +328,10 @@ __device__ void jacobi_sweeps(R* T, R* V, int m, int max_sweeps, double tol, R* 
           } else {
             const float fa = (float)apq;
             if (fabsf(fa) > 1e-30f && fabsf(fa) * fabsf(fa) > 1e-14f * fabsf((float)app * (float)aqq)) {
-              const float theta = ((float)aqq - (float)app) / (2.f * fa);
-              const float t = (theta >= 0.f ? 1.f : -1.f) / (fabsf(theta) + sqrtf(fmaf(theta, theta, 1.f)));
+              // approximate quotients are enough here: the rotation stays orthogonal (c, s from
+              // one t), and the FP64 sweeps that follow correct the angles
+              const float theta = __fdividef((float)aqq - (float)app, 2.f * fa);
+              const float t = __fdividef(theta >= 0.f ? 1.f : -1.f, fabsf(theta) + sqrtf(fmaf(theta, theta, 1.f)));
               const float c = rsqrtf(fmaf(t, t, 1.f));
               cs = c;
               sn = t * c;
@@ -339,27 +344,29 @@ __device__ void jacobi_sweeps(R* T, R* V, int m, int max_sweeps, double tol, R* 
         s_sn[tid] = sn;
       }
       __syncthreads();
-      for (int e = tid; e < half * m; e += nt) {  // rows p, q
-        const int i = e / m, k = e - i * m;
+      for (int i = warp; i < half; i += nw) {  // rows p, q: a warp per pair, lanes over the columns
         const int p = s_p[i], q = s_q[i];
-        if (q < 0 || s_sn[i] == (R)0) continue;
         const R cs = s_cs[i], sn = s_sn[i];
-        const R tp = T[p * m + k], tq = T[q * m + k];
-        T[p * m + k] = cs * tp - sn * tq;
-        T[q * m + k] = sn * tp + cs * tq;
+        if (q < 0 || sn == (R)0) continue;
+        for (int k = lane; k < m; k += 32) {
+          const R tp = T[p * m + k], tq = T[q * m + k];
+          T[p * m + k] = cs * tp - sn * tq;
+          T[q * m + k] = sn * tp + cs * tq;
+        }
       }
       __syncthreads();
-      for (int e = tid; e < half * m; e += nt) {  // columns p, q and the eigenvectors
-        const int i = e / m, k = e - i * m;
+      for (int i = warp; i < half; i += nw) {  // columns p, q and the eigenvectors
         const int p = s_p[i], q = s_q[i];
-        if (q < 0 || s_sn[i] == (R)0) continue;
         const R cs = s_cs[i], sn = s_sn[i];
-        const R tp = T[k * m + p], tq = T[k * m + q];
-        T[k * m + p] = cs * tp - sn * tq;
-        T[k * m + q] = sn * tp + cs * tq;
-        const R vp = V[k * m + p], vq = V[k * m + q];
-        V[k * m + p] = cs * vp - sn * vq;
-        V[k * m + q] = sn * vp + cs * vq;
+        if (q < 0 || sn == (R)0) continue;
+        for (int k = lane; k < m; k += 32) {
+          const R tp = T[k * m + p], tq = T[k * m + q];
+          T[k * m + p] = cs * tp - sn * tq;
+          T[k * m + q] = sn * tp + cs * tq;
+          const R vp = V[k * m + p], vq = V[k * m + q];
+          V[k * m + p] = cs * vp - sn * vq;
+          V[k * m + q] = sn * vp + cs * vq;
+        }
       }
       __syncthreads();
     }
