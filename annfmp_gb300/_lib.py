@@ -95,6 +95,7 @@ SIGNATURES = {
                            ctypes.c_float, _i, _vp]),
     "annf_cnn_targets": (_i, [_vp, _vp, _i, _i, _i, _i, _vp, _vp, _vp]),
     "annf_cnn_proposals": (_i, [_vp, _vp, _i, _i, _i, _i, _i, _i, _i, _vp, _vp]),
+    "annf_cnn_proposals_per_pixel": (_i, [_vp, _vp, _i, _i, _i, _i, _i, _i, _i, _i, _vp, _vp]),
     "annf_raw_nn": (_i, [_vp, _vp, _i, _i, _vp, _i, _i, _i, _i, _vp, _i, _vp, _vp]),
     "annf_profile_enable": (_i, [_vp, _i]),
     "annf_profile_read": (_i, [_vp, _vp, _i, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_char_p)]),

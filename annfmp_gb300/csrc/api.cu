@@ -53,7 +53,7 @@ int cnn_wta_loss(const float* out, const float* tgt, const uint8_t* valid, long 
 int cnn_adam(float* p, const float* g, float* m, float* v, int n, float lr, float b1, float b2, float eps, int step,
              cudaStream_t st);
 int cnn_targets(const int* nnf, int H, int W, int Wb, int psize, float* tgt, uint8_t* valid, cudaStream_t st);
-int cnn_proposals(const float* out, int h4, int w4, int H, int W, int Hb, int Wb, int psize, int* props,
+int cnn_proposals(const float* out, int h4, int w4, int H, int W, int Hb, int Wb, int psize, int per_pixel, int* props,
                   cudaStream_t st);
 bool project_tc_supported(int psize, int c, int ncomp);
 int project_tc(annf_handle* h, const uint8_t* img, int H, int W, int c, int psize, const double* comps,
@@ -549,7 +549,17 @@ int annf_cnn_proposals(annf_handle* h, const float* out, int h4, int w4, int ha,
   ANNF_REQUIRE(out && props && h4 >= 1 && w4 >= 1 && psize >= 1 && psize <= ha && psize <= wa && psize <= hb &&
                    psize <= wb,
                "annf_cnn_proposals: bad argument");
-  return cnn_proposals(out, h4, w4, ha, wa, hb, wb, psize, props, static_cast<cudaStream_t>(stream));
+  return cnn_proposals(out, h4, w4, ha, wa, hb, wb, psize, 4, props, static_cast<cudaStream_t>(stream));
+}
+
+int annf_cnn_proposals_per_pixel(annf_handle* h, const float* out, int h4, int w4, int ha, int wa, int hb, int wb,
+                                 int psize, int per_pixel, int* props, void* stream) {
+  ANNF_API_HANDLE(h);
+  ANNF_REQUIRE(out && props && h4 >= 1 && w4 >= 1 && psize >= 1 && psize <= ha && psize <= wa && psize <= hb &&
+                   psize <= wb,
+               "annf_cnn_proposals_per_pixel: bad argument");
+  ANNF_REQUIRE(per_pixel == 1 || per_pixel == 2 || per_pixel == 4, "annf_cnn_proposals_per_pixel: per_pixel must be 1, 2 or 4");
+  return cnn_proposals(out, h4, w4, ha, wa, hb, wb, psize, per_pixel, props, static_cast<cudaStream_t>(stream));
 }
 
 long long annf_launch_count(void) { return g_launches.load(std::memory_order_relaxed); }

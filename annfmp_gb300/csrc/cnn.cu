@@ -321,19 +321,22 @@ __global__ void cnn_targets_kernel(const int* __restrict__ nnf, int H, int W, in
   }
 }
 
+// per_pixel 4: every A patch takes its block's 4 hypotheses; 2: (x + y) even takes 0, 1 and odd 2, 3;
+// 1: patch (y, x) takes hypothesis 2 (y mod 2) + (x mod 2), so each 2 x 2 group verifies all four
 __global__ void cnn_proposals_kernel(const float* __restrict__ out, int h4, int w4, int n_rows, int n_cols, int nrb,
-                                     int ncb, int psize, int* __restrict__ props) {
+                                     int ncb, int psize, int per_pixel, int* __restrict__ props) {
   const long long nA = (long long)n_rows * n_cols;
   const int half = psize / 2;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < nA; i += (long long)gridDim.x * blockDim.x) {
     const int y = (int)(i / n_cols), x = (int)(i - (long long)y * n_cols);
     const int li = min((y + half) >> 2, h4 - 1), lj = min((x + half) >> 2, w4 - 1);
     const float* o = out + ((size_t)li * w4 + lj) * 8;
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
+    const int j0 = per_pixel == 4 ? 0 : per_pixel == 2 ? 2 * ((x + y) & 1) : 2 * (y & 1) + (x & 1);
+    for (int u = 0; u < per_pixel; ++u) {
+      const int j = j0 + u;
       const int by = min(max(y + __float2int_rn(o[2 * j + 1] * kOutScale), 0), nrb - 1);
       const int bx = min(max(x + __float2int_rn(o[2 * j] * kOutScale), 0), ncb - 1);
-      props[i * 4 + j] = by * ncb + bx;
+      props[i * per_pixel + u] = by * ncb + bx;
     }
   }
 }
@@ -651,11 +654,11 @@ int cnn_targets(const int* nnf, int H, int W, int Wb, int psize, float* tgt, uin
   return ANNF_OK;
 }
 
-int cnn_proposals(const float* out, int h4, int w4, int H, int W, int Hb, int Wb, int psize, int* props,
+int cnn_proposals(const float* out, int h4, int w4, int H, int W, int Hb, int Wb, int psize, int per_pixel, int* props,
                   cudaStream_t st) {
   const int n_rows = H - psize + 1, n_cols = W - psize + 1;
   cnn_proposals_kernel<<<grid_for((long long)n_rows * n_cols, 256), 256, 0, st>>>(
-      out, h4, w4, n_rows, n_cols, Hb - psize + 1, Wb - psize + 1, psize, props);
+      out, h4, w4, n_rows, n_cols, Hb - psize + 1, Wb - psize + 1, psize, per_pixel, props);
   ANNF_CHECK_LAUNCH();
   return ANNF_OK;
 }

@@ -379,7 +379,10 @@ def run_gpu(args, w, rank, world, local_rank):
     kernel_stages = {k: v for k, v in stage_ms.items() if not k.endswith(":begin")}
     depth = pm.kdtree.final_tree_depth_
     peak, peak_kind = load_peaks()
-    n_prop = 4 if getattr(pm, "proposal", None) is not None else 0
+    # proposals with a seed method are verified on their own handle beside the PCA fit: the
+    # profiled fast_init then reads one seed match per pixel, not the proposals
+    prop_src = getattr(pm, "proposal", None)
+    n_prop = 0 if prop_src is None or hasattr(prop_src, "seed") else int(getattr(prop_src, "per_pixel", 4))
     sb = lambda k: stage_bytes(k, w, n_a, n_b, depth, n_cols, args.iters, pm.search[0], n_prop)  # noqa: E731
     dom = max((k for k in kernel_stages if sb(k)), key=lambda k: kernel_stages[k])
     by = sb(dom)

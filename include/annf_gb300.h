@@ -271,6 +271,11 @@ int annf_cnn_targets(annf_handle* h, const int* nnf, int ha, int wa, int wb, int
  * the 4 hypotheses of the low-resolution pixel holding its centre, rounded, clamped to B's grid. */
 int annf_cnn_proposals(annf_handle* h, const float* out, int h4, int w4, int ha, int wa, int hb, int wb, int psize,
                        int* props, void* stream);
+/* The same with per_pixel (1, 2 or 4) hypotheses per A patch, props [n_A][per_pixel]: 4 as above;
+ * 2: patches with x + y even take hypotheses 0 and 1, odd ones 2 and 3; 1: patch (y, x) takes
+ * hypothesis 2 (y mod 2) + (x mod 2), so every 2 x 2 group of patches verifies all four. */
+int annf_cnn_proposals_per_pixel(annf_handle* h, const float* out, int h4, int w4, int ha, int wa, int hb, int wb,
+                                 int psize, int per_pixel, int* props, void* stream);
 
 /* Synchronise the stream and report (and clear) the kernels' bounds-check status bits. */
 int annf_device_status(annf_handle* h, void* stream, unsigned* bits_out);

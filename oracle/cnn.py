@@ -143,9 +143,11 @@ def targets_from_nnf(nnf: np.ndarray, H: int, W: int, Hb: int, Wb: int, psize: i
     return tgt, valid
 
 
-def proposals(out: np.ndarray, H: int, W: int, Hb: int, Wb: int, psize: int) -> np.ndarray:
-    """[n_A, 4] B patch indices: A patch (y, x) takes the 4 hypotheses of the low-resolution pixel
-    holding its centre, rounded to the nearest pixel and clamped to B's patch grid."""
+def proposals(out: np.ndarray, H: int, W: int, Hb: int, Wb: int, psize: int, per_pixel: int = 4) -> np.ndarray:
+    """[n_A, per_pixel] B patch indices: A patch (y, x) takes the hypotheses of the low-resolution
+    pixel holding its centre, rounded to the nearest pixel and clamped to B's patch grid; all 4, or
+    with per_pixel 2 hypotheses 0, 1 (x + y even) or 2, 3 (odd), or with per_pixel 1 hypothesis
+    2 (y mod 2) + (x mod 2)."""
     n_cols, n_rows = W - psize + 1, H - psize + 1
     ncb, nrb = Wb - psize + 1, Hb - psize + 1
     h4, w4 = out.shape[0], out.shape[1]
@@ -156,4 +158,9 @@ def proposals(out: np.ndarray, H: int, W: int, Hb: int, Wb: int, psize: int) -> 
     o = out[i, j].astype(np.float32).reshape(-1, 4, 2) * np.float32(OUT_SCALE)
     by = np.clip(y[:, None] + np.rint(o[..., 1]).astype(np.int64), 0, nrb - 1)
     bx = np.clip(x[:, None] + np.rint(o[..., 0]).astype(np.int64), 0, ncb - 1)
-    return (by * ncb + bx).astype(np.int32)
+    full = (by * ncb + bx).astype(np.int32)
+    if per_pixel == 4:
+        return full
+    j0 = 2 * ((x + y) & 1) if per_pixel == 2 else 2 * (y & 1) + (x & 1)
+    cols = j0[:, None] + np.arange(per_pixel)[None, :]
+    return np.take_along_axis(full, cols, axis=1)

@@ -125,6 +125,11 @@ def test_targets_and_proposals_match_oracle(gpu_lib):
     out_d = torch.from_numpy(out).cuda()
     net.h.call("annf_cnn_proposals", ptr(out_d), H // 4, W // 4, H, W, H, W, p, ptr(props), stream_ptr(dev))
     assert np.array_equal(props.cpu().numpy(), C.proposals(out, H, W, H, W, p))
+    for per_pixel in (1, 2, 4):  # a subset of the block's hypotheses per pixel
+        sub = torch.empty((n_rows * n_cols, per_pixel), dtype=torch.int32, device=dev)
+        net.h.call("annf_cnn_proposals_per_pixel", ptr(out_d), H // 4, W // 4, H, W, H, W, p, per_pixel, ptr(sub),
+                   stream_ptr(dev))
+        assert np.array_equal(sub.cpu().numpy(), C.proposals(out, H, W, H, W, p, per_pixel))
 
 
 def test_trained_proposals_gain(gpu_lib):
@@ -138,15 +143,16 @@ def test_trained_proposals_gain(gpu_lib):
     if not os.path.exists(DEFAULT_WEIGHTS):
         pytest.skip("no trained weights")
     a, b = gen.pair_flow(424242, 512)
-    net = ProposalNet.pretrained()
-    for iters in (1, 2):
-        kw = dict(n_neighbors=4, psize=7, dim_reduced=8, n_subset=int(round(0.1 * 506 * 506)), leaf_size=32, seed=0,
-                  verbose=0, form="parallel", iters=iters)
-        nn0 = ANNFieldPropKDTreeGB300(**kw).fit(a, b)
-        nn1 = ANNFieldPropKDTreeGB300(proposal=net, **kw).fit(a, b)
-        e0 = metrics.distance_ratio_error(a, b, nn0, 7, n_samples=4096, seed=11)
-        e1 = metrics.distance_ratio_error(a, b, nn1, 7, n_samples=4096, seed=11)
-        assert e1["mean"] < e0["mean"], (iters, e1, e0)
+    for per_pixel in (1, 4):  # one hypothesis per pixel (the default) and all four
+        net = ProposalNet.pretrained(per_pixel=per_pixel)
+        for iters in (1, 2):
+            kw = dict(n_neighbors=4, psize=7, dim_reduced=8, n_subset=int(round(0.1 * 506 * 506)), leaf_size=32,
+                      seed=0, verbose=0, form="parallel", iters=iters)
+            nn0 = ANNFieldPropKDTreeGB300(**kw).fit(a, b)
+            nn1 = ANNFieldPropKDTreeGB300(proposal=net, **kw).fit(a, b)
+            e0 = metrics.distance_ratio_error(a, b, nn0, 7, n_samples=4096, seed=11)
+            e1 = metrics.distance_ratio_error(a, b, nn1, 7, n_samples=4096, seed=11)
+            assert e1["mean"] < e0["mean"], (per_pixel, iters, e1, e0)
 
 
 class _ProposalsOnly:
@@ -168,8 +174,9 @@ def test_seeded_start_equals_proposals_in_init(gpu_lib):
     from annfmp_gb300 import ANNFieldPropKDTreeGB300, gen
     from annfmp_gb300._torch import ptr, stream_ptr
     from annfmp_gb300.proposal import ProposalNet
-    net = ProposalNet()  # untrained weights: proposals of any quality must give the same NNF
-    for seed, size in ((5, 160), (6, 203)):
+    # untrained weights (proposals of any quality must give the same NNF), one and four per pixel
+    for seed, size, per_pixel in ((5, 160, 1), (6, 203, 4)):
+        net = ProposalNet(per_pixel=per_pixel)
         a, b = gen.pair_flow(seed, size, magnitude=6.0, sigma=24.0)
         kw = dict(n_neighbors=4, psize=7, dim_reduced=8, n_subset=3000, leaf_size=32, seed=0, verbose=0,
                   form="parallel", iters=2, graph=False)
