@@ -231,13 +231,238 @@ __global__ void __launch_bounds__(kPjThreads) project_tc_kernel(const uint8_t* _
   if (warp == 0) tc::tmem_dealloc(tmem, 32);
 }
 
+// ---------------------------------------------------------------------------------------------
+// Row form (images of at most 4 channels): no per-patch expansion. An image row is converted once
+// into FP16 with every pixel padded to 4 channels (8 bytes), so consecutive pixels are 8 bytes
+// apart and every second one 16 bytes: exactly the row pitch of a K-major core matrix. With the
+// A tile's rows taken as the patches x0, x0 + 2, ..., x0 + 254 and the K-adjacent core matrices
+// 16 bytes apart (LBO = 16), the converted row itself is the A operand of filter row r: element
+// (patch i, k) sits at byte 16 i + 2 k, i.e. channel k mod 4 of pixel 2 i + k / 4. A second copy
+// shifted by one pixel gives the odd patches. Each output row is then 2 x psize x KS MMAs
+// (M = 128, N = components padded to 16/32, K = 16 per MMA, KS = 4 psize / 16 rounded up) into two
+// TMEM accumulators, over a ring of the psize converted rows it covers; a CTA walks a strip of 256
+// patches down kPrRows output rows and converts one new image row per output row.
+// ---------------------------------------------------------------------------------------------
+constexpr int kPrThreads = 128;  // one thread per TMEM lane: the even patch 2 i and the odd one 2 i + 1
+constexpr int kPrRows = 8;       // output rows per CTA
+
+__host__ __device__ constexpr int pr_kr(int psize) { return (4 * psize + 15) / 16 * 16; }  // K per filter row
+__host__ __device__ constexpr int pr_pe(int psize) { return 254 + pr_kr(psize) / 4; }      // pixels per copy
+
+// B operand per filter row r: [psize][npad][kr] FP16 row-major, k = 4 s + ch (pixel s of the
+// filter row, channel ch; zero for s >= psize or ch >= C), and the FP32 mean term as pj_prep_kernel
+__global__ void pr_prep_kernel(const double* __restrict__ comps, const double* __restrict__ mean, int d, int P,
+                               int psize, int C, int npad, int kr, uint16_t* __restrict__ bmat,
+                               float* __restrict__ mterm) {
+  const int total = psize * npad * kr;
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
+    const int r = e / (npad * kr), rem = e - r * npad * kr, j = rem / kr, k = rem - j * kr;
+    const int px = k >> 2, ch = k & 3;
+    const float v = (j < d && px < psize && ch < C) ? (float)comps[(size_t)j * P + (r * psize + px) * C + ch] : 0.f;
+    bmat[e] = __half_as_ushort(__float2half_rn(v));
+  }
+  if (blockIdx.x == 0) {
+    for (int j = threadIdx.x; j < d; j += blockDim.x) {
+      double s = 0.0;
+      for (int k = 0; k < P; ++k)
+        s += (double)__half2float(__float2half_rn((float)comps[(size_t)j * P + k])) * mean[k];
+      mterm[j] = (float)s;
+    }
+  }
+}
+
+// image row Y, pixels x0 .. x0 + pe (zero beyond the image) -> the even copy (pixel x0 + q at q)
+// and the odd copy (pixel x0 + 1 + q at q), 4 FP16 channels per pixel
+__device__ __forceinline__ void pr_convert_row(const uint8_t* __restrict__ img, int W, int C, int Y, int x0, int pe,
+                                               uint2* even, uint2* odd) {
+  for (int q = threadIdx.x; q <= pe; q += kPrThreads) {
+    const int X = x0 + q;
+    uint32_t ch[4] = {0u, 0u, 0u, 0u};
+    if (X < W) {
+      const uint8_t* px = img + ((size_t)Y * W + X) * C;
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+        if (u < C) ch[u] = __ldg(px + u);
+    }
+    // a byte b is the FP16 value b: exact, via the integer-to-half conversion
+    const uint32_t lo = (uint32_t)__half_as_ushort(__uint2half_rn(ch[0])) |
+                        ((uint32_t)__half_as_ushort(__uint2half_rn(ch[1])) << 16);
+    const uint32_t hi = (uint32_t)__half_as_ushort(__uint2half_rn(ch[2])) |
+                        ((uint32_t)__half_as_ushort(__uint2half_rn(ch[3])) << 16);
+    const uint2 v = make_uint2(lo, hi);
+    if (q < pe) even[q] = v;
+    if (q >= 1) odd[q - 1] = v;
+  }
+}
+
+template <int NPAD, int KS>
+__global__ void __launch_bounds__(kPrThreads) project_rows_tc_kernel(
+    const uint8_t* __restrict__ img, int H, int W, int C, int psize, int d, const uint16_t* __restrict__ bmat,
+    const float* __restrict__ mterm, float* __restrict__ out, int vec_out, unsigned* status) {
+  constexpr int KR = KS * 16;
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  const int ncols = W - psize + 1, nrows = H - psize + 1;
+  const int pe = 254 + KR / 4;  // pixels per copy (even: 0 .. pe - 1 relative to x0)
+  const int strips = (ncols + 255) / 256;
+  const int strip = blockIdx.x % strips, chunk = blockIdx.x / strips;
+  const int x0 = strip * 256, yb = chunk * kPrRows, ye = min(nrows, yb + kPrRows);
+  unsigned char* p = smem_raw;
+  unsigned char* sB = p;  // [psize] filter rows of NPAD x KR FP16, core layout
+  p += (size_t)psize * NPAD * KR * 2;
+  unsigned char* ring = p;  // [psize slots][even, odd][pe pixels][8 bytes]
+  p += (size_t)psize * 2 * pe * 8;
+  p = reinterpret_cast<unsigned char*>(((uintptr_t)p + 15) & ~uintptr_t(15));
+  uint64_t* mbar = reinterpret_cast<uint64_t*>(p);
+  p += 8;
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(p);
+  p += 8;
+  int* sflag = reinterpret_cast<int*>(p);
+  p += 8;
+  if (smem_overrun(smem_raw, p, status)) return;
+  if (yb >= nrows) return;  // uniform per block
+  const int tid = threadIdx.x, warp = tid >> 5;
+  if (warp == 0) {
+    tc::tmem_alloc(tslot, 2 * NPAD);
+    tc::tmem_relinquish();
+  }
+  if (tid == 0) {
+    tc::mbar_init(mbar, 1);
+    tc::mbar_fence_init();
+    sflag[0] = 0;
+  }
+  for (int e = tid; e < psize * NPAD * (KR / 8); e += kPrThreads) {  // components, core layout per filter row
+    const int r = e / (NPAD * (KR / 8)), rem = e - r * NPAD * (KR / 8);
+    const int n = rem / (KR / 8), k8 = (rem - n * (KR / 8)) * 8;
+    *reinterpret_cast<uint4*>(sB + (size_t)r * NPAD * KR * 2 + tc::core_offset(n, k8, KR)) =
+        *reinterpret_cast<const uint4*>(bmat + ((size_t)r * NPAD + n) * KR + k8);
+  }
+  auto slot_even = [&](int Y) { return reinterpret_cast<uint2*>(ring + (size_t)(2 * (Y % psize)) * pe * 8); };
+  auto slot_odd = [&](int Y) { return reinterpret_cast<uint2*>(ring + (size_t)(2 * (Y % psize) + 1) * pe * 8); };
+  for (int Y = yb; Y < yb + psize - 1; ++Y) pr_convert_row(img, W, C, Y, x0, pe, slot_even(Y), slot_odd(Y));
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = *tslot;
+  const uint32_t idesc = tc::idesc_f16(128, NPAD);
+  uint32_t phase = 0;
+  for (int y = yb; y < ye; ++y) {
+    // the newest image row goes to the slot of row y - 1, whose MMAs finished before the last wait
+    pr_convert_row(img, W, C, y + psize - 1, x0, pe, slot_even(y + psize - 1), slot_odd(y + psize - 1));
+    tc::fence_async_smem();
+    tc::fence_before_sync();
+    __syncthreads();
+    if (tid == 0) {
+      tc::fence_after_sync();
+      for (int half = 0; half < 2; ++half) {
+        for (int r = 0; r < psize; ++r) {
+          const unsigned char* a = reinterpret_cast<const unsigned char*>(half ? slot_odd(y + r) : slot_even(y + r));
+          const unsigned char* b = sB + (size_t)r * NPAD * KR * 2;
+#pragma unroll
+          for (int kk = 0; kk < KS; ++kk)
+            tc::mma_bf16(tmem + (uint32_t)(half * NPAD), tc::sdesc(a + kk * 32, 16, 128),
+                         tc::sdesc(b + kk * 256, 128, (KR / 8) * 128), idesc, (r > 0 || kk > 0) ? 1u : 0u);
+        }
+      }
+      tc::mma_commit(mbar);
+    }
+    if (!pj_wait(mbar, phase)) sflag[0] = 1;
+    phase ^= 1u;
+    __syncthreads();
+    if (sflag[0]) break;
+    tc::fence_after_sync();
+    // epilogue: lane i holds patch x0 + 2 i (columns 0..NPAD) and x0 + 2 i + 1 (NPAD..2 NPAD)
+    {
+      const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16);
+#pragma unroll
+      for (int half = 0; half < 2; ++half) {
+        uint32_t r[NPAD];
+        if constexpr (NPAD == 16) {
+          tc::tmem_ld16(taddr + (uint32_t)(half * NPAD), r);
+        } else {
+          uint32_t(&r0)[16] = *reinterpret_cast<uint32_t(*)[16]>(r);
+          uint32_t(&r1)[16] = *reinterpret_cast<uint32_t(*)[16]>(r + 16);
+          tc::tmem_ld16(taddr + (uint32_t)(half * NPAD), r0);
+          tc::tmem_ld16(taddr + (uint32_t)(half * NPAD + 16), r1);
+        }
+        tc::tmem_wait_ld();
+        const int x = x0 + 2 * tid + half;
+        if (x < ncols) {
+          float* dst = out + ((size_t)y * ncols + x) * d;
+          if (vec_out) {  // d a multiple of 4 and out 16-byte aligned
+#pragma unroll
+            for (int j = 0; j < NPAD; j += 4)
+              if (j < d)
+                *reinterpret_cast<float4*>(dst + j) =
+                    make_float4(__uint_as_float(r[j]) - mterm[j], __uint_as_float(r[j + 1]) - mterm[j + 1],
+                                __uint_as_float(r[j + 2]) - mterm[j + 2], __uint_as_float(r[j + 3]) - mterm[j + 3]);
+          } else {
+#pragma unroll
+            for (int j = 0; j < NPAD; ++j)
+              if (j < d) dst[j] = __uint_as_float(r[j]) - mterm[j];
+          }
+        }
+      }
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+  }
+  if (sflag[0]) {
+    if (tid == 0) atomicOr(status, DEV_TC_TIMEOUT);
+    pj_wait(mbar, phase ^ 1u);
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) tc::tmem_dealloc(tmem, 2 * NPAD);
+}
+
+bool project_rows_supported(int psize, int c, int ncomp) {
+  return psize >= 1 && psize <= 12 && c >= 1 && c <= 4 && ncomp >= 1 && ncomp <= 32;
+}
+
 bool project_tc_supported(int psize, int c, int ncomp) {
   const int rs = (psize * c + 7) & ~7;
   return psize >= 1 && c >= 1 && psize * rs <= 320 && ncomp >= 1 && ncomp <= 32 && (128 + psize - 1) * c <= 4096;
 }
 
+static int project_rows_tc(annf_handle* h, const uint8_t* img, int H, int W, int c, int psize, const double* comps,
+                          const double* mean, int ncomp, float* out, cudaStream_t st) {
+  const int P = psize * psize * c;
+  const int kr = pr_kr(psize), ks = kr / 16, pe = pr_pe(psize);
+  const int npad = ncomp <= 16 ? 16 : 32;
+  const size_t bbytes = (size_t)psize * npad * kr * 2;
+  ANNF_ENSURE(h->pj_buf, bbytes + 64 * sizeof(float) + 256);
+  uint16_t* bmat = h->pj_buf.as<uint16_t>();
+  float* mterm = reinterpret_cast<float*>(reinterpret_cast<unsigned char*>(h->pj_buf.p) + ((bbytes + 255) & ~size_t(255)));
+  prof_mark(h, "project:begin", st);
+  pr_prep_kernel<<<std::max(1, std::min(ceil_div((int)(bbytes / 2), 256), 64)), 256, 0, st>>>(
+      comps, mean, ncomp, P, psize, c, npad, kr, bmat, mterm);
+  ANNF_CHECK_LAUNCH();
+  // with 64 TMEM columns per CTA (npad 32) at most 8 CTAs may share an SM's 512 columns: the
+  // shared memory request keeps any more from being resident
+  const size_t smem = std::max(bbytes + (size_t)psize * 2 * pe * 8 + 16 + 24 + 64, npad == 32 ? (size_t)28 * 1024 : 0);
+  ANNF_REQUIRE(smem <= 227 * 1024, "annf_project_f16: tile too large for shared memory");
+  const int ncols = W - psize + 1, nrows = H - psize + 1;
+  const long long blocks = (long long)((ncols + 255) / 256) * ((nrows + kPrRows - 1) / kPrRows);
+  ANNF_REQUIRE(blocks <= 0x7fffffffLL, "annf_project_f16: image too large");
+  const int vec = (ncomp % 4 == 0 && ((uintptr_t)out & 15) == 0) ? 1 : 0;
+#define ANNF_PR(NP, KS_)                                                                                          \
+  if (npad == NP && ks == KS_) {                                                                                 \
+    ANNF_CUDA_TRY(cudaFuncSetAttribute(project_rows_tc_kernel<NP, KS_>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                                       (int)smem));                                                              \
+    project_rows_tc_kernel<NP, KS_><<<(unsigned)blocks, kPrThreads, smem, st>>>(img, H, W, c, psize, ncomp, bmat,  \
+                                                                               mterm, out, vec,                  \
+                                                                               h->status.as<unsigned>());        \
+  }
+  ANNF_PR(16, 1) ANNF_PR(16, 2) ANNF_PR(16, 3) ANNF_PR(32, 1) ANNF_PR(32, 2) ANNF_PR(32, 3)
+#undef ANNF_PR
+  ANNF_CHECK_LAUNCH();
+  prof_mark(h, "project", st);
+  return ANNF_OK;
+}
+
 int project_tc(annf_handle* h, const uint8_t* img, int H, int W, int c, int psize, const double* comps,
                const double* mean, int ncomp, float* out, cudaStream_t st) {
+  if (project_rows_supported(psize, c, ncomp)) return project_rows_tc(h, img, H, W, c, psize, comps, mean, ncomp, out, st);
   ANNF_REQUIRE(project_tc_supported(psize, c, ncomp), "annf_project_f16: patch or components too large");
   const int P = psize * psize * c;
   const int rowlen = psize * c, rs = (rowlen + 7) & ~7;
