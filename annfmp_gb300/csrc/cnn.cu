@@ -345,8 +345,11 @@ __global__ void cnn_proposals_kernel(const float* __restrict__ out, int h4, int 
 // forward convolution on the tensor cores (inference and training forward): an implicit GEMM per
 // tile of 128 consecutive pixels of one row, M = 128 pixels, N = Cout padded to 16/32, K = taps x
 // Cin in the weights' own order (k = (ky*3 + kx)*Cin + ci). The three input rows are staged in
-// shared memory; for Cin = 32 the A tile is built one kernel row (ky) at a time (K = 96, three
-// accumulating rounds of 6 MMAs), for Cin = 8 all 9 taps at once (K = 72 padded to 80). FP32 TMEM
+// shared memory. For Cin = 32 they are staged as planes of 8 channels (16 bytes per pixel), so the
+// pixels of a plane are 16 bytes apart like the rows of a K-major core matrix: the staged rows are
+// the A operand itself (tap (ky, kx) starts kx pixels into row ky's planes, the next 8 channels
+// one plane further: LBO = the plane size), and a tile is 9 taps x 2 MMAs with no A tile built.
+// For Cin = 8 all 9 taps are expanded into an A tile at once (K = 72 padded to 80). FP32 TMEM
 // accumulator; epilogue adds the bias, applies the ReLU and stores BF16 (or FP32 for the last layer).
 // ---------------------------------------------------------------------------------------------
 constexpr long long kConvWaitCycles = 2000000000LL;
@@ -380,8 +383,8 @@ __global__ void __launch_bounds__(128) cnn_conv_tc_kernel(const __nv_bfloat16* _
   constexpr int SPIX = 130;                           // staged pixels per input row
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char* p = smem_raw;
-  unsigned char* sA = p;
-  p += 128 * KR * 2;
+  unsigned char* sA = p;  // the expanded A tile (Cin = 8 only)
+  if (CI != 32) p += 128 * KR * 2;
   unsigned char* sB = p;
   p += COP * KPAD * 2;
   __nv_bfloat16* sIn = reinterpret_cast<__nv_bfloat16*>(p);  // [3][SPIX][CI]
@@ -430,10 +433,38 @@ __global__ void __launch_bounds__(128) cnn_conv_tc_kernel(const __nv_bfloat16* _
       uint4 v = make_uint4(0u, 0u, 0u, 0u);
       if (yy >= 0 && yy < h && xx >= 0 && xx < w)
         v = *reinterpret_cast<const uint4*>(X + (((size_t)n * h + yy) * w + xx) * CI + c8 * 8);
-      *reinterpret_cast<uint4*>(sIn + (size_t)q * CI + c8 * 8) = v;
+      if (CI == 32)  // plane (row ry, channels 8 c8 .. 8 c8 + 7): SPIX pixels x 16 bytes
+        *reinterpret_cast<uint4*>(sIn + ((size_t)(ry * (CI / 8) + c8) * SPIX + px) * 8) = v;
+      else
+        *reinterpret_cast<uint4*>(sIn + (size_t)q * CI + c8 * 8) = v;
     }
-    __syncthreads();
-    for (int round = 0; round < ROUNDS; ++round) {
+    if constexpr (CI == 32) {
+      tc::fence_async_smem();
+      tc::fence_before_sync();
+      __syncthreads();
+      if (tid == 0) {
+        tc::fence_after_sync();
+        constexpr uint32_t kPlane = SPIX * 16;  // bytes per plane
+        for (int tap = 0; tap < 9; ++tap) {
+          const int ky = tap / 3, kx = tap - ky * 3;
+          const unsigned char* a = reinterpret_cast<const unsigned char*>(sIn) + (size_t)ky * (CI / 8) * kPlane + kx * 16;
+#pragma unroll
+          for (int kk = 0; kk < CI / 16; ++kk)
+            tc::mma_bf16(tmem, tc::sdesc(a + 2 * kk * kPlane, kPlane, 128),
+                         tc::sdesc(sB + ((tap * CI + 16 * kk) / 8) * 128, 128, (KPAD / 8) * 128), idesc,
+                         (tap > 0 || kk > 0) ? 1u : 0u);
+        }
+        tc::mma_commit(mbar);
+      }
+      if (!conv_wait(mbar, phase)) sflag[0] = 1;
+      phase ^= 1u;
+      __syncthreads();
+      if (sflag[0]) aborted = true;
+      tc::fence_after_sync();
+    } else {
+      __syncthreads();
+    }
+    for (int round = 0; round < (CI == 32 ? 0 : ROUNDS); ++round) {
       // A tile of this round: pixel tid, K = taps of kernel row `round` (CI 32) or all taps (CI 8)
       for (int g = 0; g < KR / 8; ++g) {
         uint4 v = make_uint4(0u, 0u, 0u, 0u);
@@ -563,11 +594,13 @@ template <int CI, int COP, int MODE>
 static int launch_conv_tc(const __nv_bfloat16* x, int nimg, int h, int w, const uint16_t* wt, const float* bias,
                           int co, void* y, unsigned* status, cudaStream_t st) {
   constexpr int KPAD = CI == 32 ? 288 : 80, KR = CI == 32 ? 96 : 80;
-  const size_t smem = (size_t)128 * KR * 2 + (size_t)COP * KPAD * 2 + (size_t)3 * 130 * CI * 2 + 16 + 24 + 64;
+  const size_t smem = (CI == 32 ? 0 : (size_t)128 * KR * 2) + (size_t)COP * KPAD * 2 + (size_t)3 * 130 * CI * 2 + 16 + 24 + 64;
   ANNF_CUDA_TRY(cudaFuncSetAttribute(cnn_conv_tc_kernel<CI, COP, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)smem));
   const long long tiles = (long long)nimg * h * ((w + 127) / 128);
-  const int grid = (int)std::max(1LL, std::min<long long>(tiles, 4LL * num_sms()));
+  // two persistent CTAs per SM: in the NNF the network runs on a side stream beside the main
+  // chain, and fewer long-lived CTAs leave it more of the GPU (measured faster than four)
+  const int grid = (int)std::max(1LL, std::min<long long>(tiles, 2LL * num_sms()));
   cnn_conv_tc_kernel<CI, COP, MODE><<<grid, 128, smem, st>>>(x, nimg, h, w, wt, bias, co, y, status);
   ANNF_CHECK_LAUNCH();
   return ANNF_OK;
