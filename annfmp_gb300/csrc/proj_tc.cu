@@ -240,11 +240,12 @@ __global__ void __launch_bounds__(kPjThreads) project_tc_kernel(const uint8_t* _
 // (patch i, k) sits at byte 16 i + 2 k, i.e. channel k mod 4 of pixel 2 i + k / 4. A second copy
 // shifted by one pixel gives the odd patches. Each output row is then 2 x psize x KS MMAs
 // (M = 128, N = components padded to 16/32, K = 16 per MMA, KS = 4 psize / 16 rounded up) into two
-// TMEM accumulators, over a ring of the psize converted rows it covers; a CTA walks a strip of 256
-// patches down kPrRows output rows and converts one new image row per output row.
+// TMEM accumulators, over a ring of psize + 1 converted rows; a CTA walks a strip of 256 patches
+// down kPrRows output rows, converting the next image row into the spare slot while the tensor
+// cores work on the current one.
 // ---------------------------------------------------------------------------------------------
 constexpr int kPrThreads = 128;  // one thread per TMEM lane: the even patch 2 i and the odd one 2 i + 1
-constexpr int kPrRows = 8;       // output rows per CTA
+constexpr int kPrRows = 16;      // output rows per CTA
 
 __host__ __device__ constexpr int pr_kr(int psize) { return (4 * psize + 15) / 16 * 16; }  // K per filter row
 __host__ __device__ constexpr int pr_pe(int psize) { return 254 + pr_kr(psize) / 4; }      // pixels per copy
@@ -261,12 +262,15 @@ __global__ void pr_prep_kernel(const double* __restrict__ comps, const double* _
     const float v = (j < d && px < psize && ch < C) ? (float)comps[(size_t)j * P + (r * psize + px) * C + ch] : 0.f;
     bmat[e] = __half_as_ushort(__float2half_rn(v));
   }
-  if (blockIdx.x == 0) {
-    for (int j = threadIdx.x; j < d; j += blockDim.x) {
+  if (blockIdx.x == 0) {  // a warp per component, lanes over the patch elements
+    const int lane = threadIdx.x & 31;
+    for (int j = threadIdx.x >> 5; j < d; j += blockDim.x >> 5) {
       double s = 0.0;
-      for (int k = 0; k < P; ++k)
+      for (int k = lane; k < P; k += 32)
         s += (double)__half2float(__float2half_rn((float)comps[(size_t)j * P + k])) * mean[k];
-      mterm[j] = (float)s;
+#pragma unroll
+      for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+      if (lane == 0) mterm[j] = (float)s;
     }
   }
 }
@@ -309,8 +313,9 @@ __global__ void __launch_bounds__(kPrThreads) project_rows_tc_kernel(
   unsigned char* p = smem_raw;
   unsigned char* sB = p;  // [psize] filter rows of NPAD x KR FP16, core layout
   p += (size_t)psize * NPAD * KR * 2;
-  unsigned char* ring = p;  // [psize slots][even, odd][pe pixels][8 bytes]
-  p += (size_t)psize * 2 * pe * 8;
+  const int nslot = psize + 1;
+  unsigned char* ring = p;  // [psize + 1 slots][even, odd][pe pixels][8 bytes]
+  p += (size_t)nslot * 2 * pe * 8;
   p = reinterpret_cast<unsigned char*>(((uintptr_t)p + 15) & ~uintptr_t(15));
   uint64_t* mbar = reinterpret_cast<uint64_t*>(p);
   p += 8;
@@ -336,9 +341,10 @@ __global__ void __launch_bounds__(kPrThreads) project_rows_tc_kernel(
     *reinterpret_cast<uint4*>(sB + (size_t)r * NPAD * KR * 2 + tc::core_offset(n, k8, KR)) =
         *reinterpret_cast<const uint4*>(bmat + ((size_t)r * NPAD + n) * KR + k8);
   }
-  auto slot_even = [&](int Y) { return reinterpret_cast<uint2*>(ring + (size_t)(2 * (Y % psize)) * pe * 8); };
-  auto slot_odd = [&](int Y) { return reinterpret_cast<uint2*>(ring + (size_t)(2 * (Y % psize) + 1) * pe * 8); };
-  for (int Y = yb; Y < yb + psize - 1; ++Y) pr_convert_row(img, W, C, Y, x0, pe, slot_even(Y), slot_odd(Y));
+  auto slot_even = [&](int Y) { return reinterpret_cast<uint2*>(ring + (size_t)(2 * (Y % nslot)) * pe * 8); };
+  auto slot_odd = [&](int Y) { return reinterpret_cast<uint2*>(ring + (size_t)(2 * (Y % nslot) + 1) * pe * 8); };
+  for (int Y = yb; Y < yb + psize; ++Y) pr_convert_row(img, W, C, Y, x0, pe, slot_even(Y), slot_odd(Y));
+  tc::fence_async_smem();
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
@@ -346,11 +352,7 @@ __global__ void __launch_bounds__(kPrThreads) project_rows_tc_kernel(
   const uint32_t idesc = tc::idesc_f16(128, NPAD);
   uint32_t phase = 0;
   for (int y = yb; y < ye; ++y) {
-    // the newest image row goes to the slot of row y - 1, whose MMAs finished before the last wait
-    pr_convert_row(img, W, C, y + psize - 1, x0, pe, slot_even(y + psize - 1), slot_odd(y + psize - 1));
-    tc::fence_async_smem();
-    tc::fence_before_sync();
-    __syncthreads();
+    // rows y .. y + psize - 1 are converted (and fenced for the tensor cores) by now
     if (tid == 0) {
       tc::fence_after_sync();
       for (int half = 0; half < 2; ++half) {
@@ -365,8 +367,15 @@ __global__ void __launch_bounds__(kPrThreads) project_rows_tc_kernel(
       }
       tc::mma_commit(mbar);
     }
+    // meanwhile the next output row's newest image row goes to the spare slot (that of row y - 1,
+    // whose MMAs finished before the previous wait)
+    if (y + 1 < ye) {
+      pr_convert_row(img, W, C, y + psize, x0, pe, slot_even(y + psize), slot_odd(y + psize));
+      tc::fence_async_smem();
+    }
     if (!pj_wait(mbar, phase)) sflag[0] = 1;
     phase ^= 1u;
+    tc::fence_before_sync();
     __syncthreads();
     if (sflag[0]) break;
     tc::fence_after_sync();
@@ -439,7 +448,7 @@ static int project_rows_tc(annf_handle* h, const uint8_t* img, int H, int W, int
   ANNF_CHECK_LAUNCH();
   // with 64 TMEM columns per CTA (npad 32) at most 8 CTAs may share an SM's 512 columns: the
   // shared memory request keeps any more from being resident
-  const size_t smem = std::max(bbytes + (size_t)psize * 2 * pe * 8 + 16 + 24 + 64, npad == 32 ? (size_t)28 * 1024 : 0);
+  const size_t smem = std::max(bbytes + (size_t)(psize + 1) * 2 * pe * 8 + 16 + 24 + 64, npad == 32 ? (size_t)28 * 1024 : 0);
   ANNF_REQUIRE(smem <= 227 * 1024, "annf_project_f16: tile too large for shared memory");
   const int ncols = W - psize + 1, nrows = H - psize + 1;
   const long long blocks = (long long)((ncols + 255) / 256) * ((nrows + kPrRows - 1) / kPrRows);
