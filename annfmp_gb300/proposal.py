@@ -6,8 +6,9 @@ B patch indices, which the parallel form verifies with the exact raw-patch dista
 tree candidates (the tree stays the fallback and decides every pixel whose proposals are worse).
 By default (``per_pixel=1``) each A pixel verifies one of its block's four hypotheses, 2 (y mod 2)
 + (x mod 2), so every 2x2 group of pixels tries all four and the propagation passes carry the
-winners to the neighbours: at 2048x2048 this takes 11.30 ms per NNF at 0.365% mean distance error,
-against 11.57 ms at 0.362% when every pixel verifies all four (``per_pixel=4``). The reference has no learned part; its propagation candidates come only from
+winners to the neighbours: at 2048x2048 this measured 11.30 ms per NNF at 0.365% mean distance
+error, against 11.57 ms at 0.362% when every pixel verifies all four (``per_pixel=4``), in the
+same build. The reference has no learned part; its propagation candidates come only from
 the row above (annfmp/openmp/kdtree/src/base.c:255-282).
 
 Network: the pair at 1/4 resolution (6 channels + 2 zero), six 3x3 convolutions 8->32, 32->32 x4,
