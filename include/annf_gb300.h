@@ -168,7 +168,9 @@ int annf_project(annf_handle* h, const uint8_t* img, int hgt, int wid, int chann
 /* Approximate counterpart of annf_project for the approximate NNF forms (no reference
  * counterpart): the same patches times the components rounded to FP16, FP32 accumulation on the
  * tensor cores (tcgen05), minus the projected mean; out FP32 [(h-psize+1)*(w-psize+1)*n_components].
- * Needs psize*psize*channels <= 256 and n_components <= 32 (else ANNF_ERR_UNSUPPORTED). */
+ * Images of 1 to 4 channels are read by the tensor cores from FP16 copies of their rows (no
+ * per-patch expansion); others through an expanded tile. Needs psize*psize*channels <= 256 and
+ * n_components <= 32 (else ANNF_ERR_UNSUPPORTED). */
 int annf_project_f16(annf_handle* h, const uint8_t* img, int hgt, int wid, int channels, int psize,
                      const double* components, const double* mean, int n_components, float* out, void* stream);
 
