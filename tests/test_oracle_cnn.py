@@ -92,3 +92,22 @@ def test_targets_and_proposals_on_a_pure_shift():
     out[..., 1::2] = 2 / 16.0
     props = C.proposals(out, H, W, H, W, p)
     assert np.array_equal(props[:, 0], nnf)
+
+
+def test_proposals_per_pixel_take_their_share_of_the_hypotheses():
+    """per_pixel 1: pixel (y, x) takes hypothesis 2 (y mod 2) + (x mod 2), so each 2x2 group of
+    pixels covers all four; per_pixel 2: hypotheses 0, 1 for x + y even and 2, 3 for odd; every
+    choice is a column of the four-per-pixel proposals."""
+    rng = np.random.default_rng(4)
+    H, W, p = 29, 38, 5
+    n_cols = W - p + 1
+    out = (rng.standard_normal((H // 4, W // 4, 8)) * 0.5).astype(np.float32)
+    full = C.proposals(out, H, W, H, W, p)
+    ys, xs = np.divmod(np.arange(full.shape[0]), n_cols)
+    one = C.proposals(out, H, W, H, W, p, per_pixel=1)
+    assert one.shape == (full.shape[0], 1)
+    assert np.array_equal(one[:, 0], full[np.arange(full.shape[0]), 2 * (ys % 2) + xs % 2])
+    two = C.proposals(out, H, W, H, W, p, per_pixel=2)
+    j0 = 2 * ((xs + ys) % 2)
+    assert np.array_equal(two, np.stack([full[np.arange(full.shape[0]), j0], full[np.arange(full.shape[0]), j0 + 1]], 1))
+    assert np.array_equal(C.proposals(out, H, W, H, W, p, per_pixel=4), full)
