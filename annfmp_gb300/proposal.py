@@ -41,7 +41,7 @@ from ._torch import ptr, require_cuda, stream_ptr, to_device
 LAYERS = [(8, 32), (32, 32), (32, 32), (32, 32), (32, 32), (32, 8)]
 WEIGHTS_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "weights")
 DEFAULT_WEIGHTS = os.path.join(WEIGHTS_DIR, "proposal_flow.npz")
-N_HYP = 4
+N_HYP = 4  # offset hypotheses per low-resolution pixel (the last layer's 8 outputs)
 
 
 class ProposalNet:
@@ -49,7 +49,7 @@ class ProposalNet:
     path to an .npz with w0..w5 [co,3,3,ci] and b0..b5 [co], or a dict of such arrays."""
 
     def __init__(self, weights=None, device=0, seed=0, per_pixel=1):
-        if per_pixel not in (1, 2, 4):
+        if per_pixel not in (1, 2, N_HYP):
             raise ValueError("per_pixel must be 1, 2 or 4")
         self.per_pixel = int(per_pixel)
         self.dev = require_cuda(device)
