@@ -19,6 +19,7 @@
 // and the few that qualify are inserted with a shuffle-shift, so the pruning threshold is always
 // exact.
 #include <algorithm>
+#include <atomic>
 
 #include "common.cuh"
 #include "handle.cuh"
@@ -1261,39 +1262,44 @@ int natural_knn_all(annf_handle* h, const void* Q, long long nq, int K, int* out
 // ---------------------------------------------------------------------------------------------
 // Exact kNN that allocates nothing.
 //
-// Some callers cannot allocate device memory at query time: a query issued while a stream is
-// being captured into a CUDA graph (cudaMalloc is not capturable), a serving process whose device
-// memory was reserved up front, or a caller running under an allocator that forbids growth. They
-// build the tree once (that call allocates), and then query with this variant, whose only scratch
-// -- the natural-leaf seeds of every query -- lives in one fixed array in device memory. The array
-// is statically sized (kNoAllocMaxEntries query*k entries of 12 bytes, 3 MiB), exists on every
-// GPU that loads the library until the process exits, and is shared by all calls: two calls that
-// overlap on the GPU (different streams, no ordering) race on it. Nothing in it needs clearing:
-// every entry a call reads was written earlier in the same call.
+// Some callers cannot allocate device memory at query time: a serving process whose device
+// memory was reserved up front, a host application that owns all device memory through its own
+// pool, or a caller running under an allocator that forbids growth. They build the tree once
+// (that call allocates), and then query with this variant, whose only scratch -- the natural-leaf
+// seeds of every query -- lives in one fixed array in device memory. The array is statically
+// sized for kNoAllocMaxEntries query*k entries of the widest seed (a 16-byte double key and a
+// 4-byte position: 5 MiB), exists on every GPU that loads the library until the process exits,
+// and is shared by all calls: two calls that overlap on the GPU (different streams, no ordering)
+// race on it. Nothing in it needs clearing: every entry a call reads was written earlier in the
+// same call.
 // ---------------------------------------------------------------------------------------------
-constexpr long long kNoAllocMaxEntries = 1LL << 18;  // queries * k per call
-constexpr size_t kNoAllocKeyBytes = (size_t)kNoAllocMaxEntries * 8;
+constexpr long long kNoAllocMaxEntries = 1LL << 18;  // queries * k per call, both real types
+constexpr size_t kNoAllocKeyBytes = (size_t)kNoAllocMaxEntries * sizeof(dkey);
+static_assert(sizeof(dkey) >= sizeof(cand_key<float>::type), "the key region is sized by the widest key");
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocKeyBytes + (size_t)kNoAllocMaxEntries * 4];
 
 // device address of g_noalloc_scratch per device, looked up once (a host-side stand-in, not the
-// symbol itself, must be passed to kernels)
-static unsigned char* g_noalloc_addr[64] = {};
+// symbol itself, must be passed to kernels). Atomic slots: two host threads making their first
+// call on one device both look the address up and store the same value.
+static std::atomic<unsigned char*> g_noalloc_addr[64];
 
 static int noalloc_scratch(int device, unsigned char** out) {
   if (device < 0 || device >= 64) {
     set_error("annf_kneighbors_noalloc: device index out of range");
     return ANNF_ERR_INVALID;
   }
-  if (!g_noalloc_addr[device]) {  // first call on this device (the device is current)
+  unsigned char* addr = g_noalloc_addr[device].load(std::memory_order_acquire);
+  if (!addr) {  // first call on this device (the device is current)
     void* p = nullptr;
     cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (e != cudaSuccess || !p) {
       set_error(std::string("annf_kneighbors_noalloc: cudaGetSymbolAddress: ") + cudaGetErrorString(e));
       return ANNF_ERR_CUDA;
     }
-    g_noalloc_addr[device] = static_cast<unsigned char*>(p);
+    addr = static_cast<unsigned char*>(p);
+    g_noalloc_addr[device].store(addr, std::memory_order_release);
   }
-  *out = g_noalloc_addr[device];
+  *out = addr;
   return ANNF_OK;
 }
 
@@ -1310,6 +1316,7 @@ static int noalloc_typed(annf_handle* h, unsigned char* scratch, const T* Q, int
     ANNF_CHECK_LAUNCH();
     return ANNF_OK;
   }
+  static_assert(sizeof(Kt) * kNoAllocMaxEntries <= kNoAllocKeyBytes, "seed keys overrun their region");
   Kt* seed_key = reinterpret_cast<Kt*>(scratch);
   int* seed_pos = reinterpret_cast<int*>(scratch + kNoAllocKeyBytes);
   int rc = ANNF_OK;

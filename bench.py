@@ -15,9 +15,13 @@ forms on the same pair. e2e = the same through the public API from pinned host i
 NNF. The L2 cache (129 MB) is flushed between timed steps by writing 256 MB.
 
 --impl reference times the CPU path (the oracle: a C restatement of the reference's OpenMP core with
-OpenMP on all host cores, plus the numpy restatement of its PCA) on a bounded sample of the same
-workload: every per-pair stage on the full pair, and the row loop on the first ROWS_SAMPLE rows,
-extrapolated to all rows.
+OpenMP on all host cores, plus the numpy restatement of its PCA): every step is one complete fit
+of the same pair by the reference's plain method (PCA fit, projection of both images, tree, the
+whole row loop with the re-rank); nothing is extrapolated.
+
+With --gpus 1 and no --no-compare, the line also carries "workloads": the 512x512 pair by the
+plain method (patch 7, PCA 8, leaf 32, k 1), the 64 uneven pairs in one graph launch and the
+1920x1080 frame stream, each with its own time and distance error.
 """
 from __future__ import annotations
 
@@ -52,8 +56,17 @@ GRAPH_WORKLOADS = {
     # 8 pairs per graph launch
     "stream": dict(psize=5, dim_reduced=12, n_neighbors=8, leaf=32, iters=2, precision="fp16", per_graph=8),
 }
-ROWS_SAMPLE = 32
 L2_FLUSH_BYTES = 256 << 20
+# the arithmetic each form computes in
+DTYPES = {"plain": "f32", "parallel": "bf16", "learned": "bf16"}
+ARITHMETIC = {
+    "plain": "u8 images; FP64 covariance and eigendecomposition; exact FP32 projection; FP32 tree and "
+             "leaf distances (no FMA, the reference's order); int32 raw-patch re-rank",
+    "parallel": "u8 images; FP64 covariance and Rayleigh-Ritz, FP32 subspace iteration; FP16 tensor-core "
+                "projection (FP32 accumulate); FP32 tree; BF16 hi/lo tensor-core leaf tiles (FP32 accumulate) "
+                "with an exact FP32 re-rank; int32 exact raw-patch SSD for every candidate",
+}
+ARITHMETIC["learned"] = ARITHMETIC["parallel"] + "; BF16 tensor-core proposal network (FP32 accumulate)"
 
 
 def make_pair(w):
@@ -132,14 +145,23 @@ class ClockSampler:
 # algorithmic bytes of each stage per NNF: the bytes the algorithm touches (served by DRAM, L2 or
 # L1), the numerator of the roofline's achieved bandwidth
 # ---------------------------------------------------------------------------------------------
-def stage_bytes(stage, w, n_a, n_b, depth, n_cols, it=1, nrand=1, n_prop=0):
+def stage_bytes(stage, w, n_a, n_b, depth, n_cols, it=1, nrand=1, n_prop=0, count=1):
+    """Algorithmic bytes of one stage per NNF (count = how many times the stage's mark repeats
+    in one fit, e.g. the global tree levels)."""
     d, k, P = w["dim_reduced"], w["n_neighbors"], w["psize"] ** 2 * 3
     ppl = n_b / float(1 << depth)
     rows_q = n_a - n_cols
+    n_sub = int(round(0.1 * n_b))
     if stage == "chain":  # per query: query + k propagated leaves + leaf spans + natural list + k-list out
         return rows_q * (4 * d + k * ppl * 4 * d + 8 * k + 12 * k + 4 * k)
     if stage == "natural_knn":  # query + node path + natural leaf + list out
         return n_a * (4 * d + 8 * depth + ppl * 4 * d + 4 * k)
+    if stage == "natural_leaf":  # query + node path + leaf id out
+        return n_a * (4 * d + 8 * depth + 4)
+    if stage == "next_range":  # per tree position: its row-below position's leaf span
+        return n_b * (4 + 4 + 8)
+    if stage == "tc_group":  # query + node path + leaf id, then the leaf-ordered query list
+        return n_a * (4 * d + 8 * depth + 4 + 8)
     if stage == "fast_init":  # k candidate positions + proposals + A patch + k + n_prop B patches + match out
         return n_a * (4 * k + 4 * n_prop + (k + n_prop + 1) * P + 8)
     if stage == "fast_propagate":  # per pass: match in/out, 4 neighbour matches, A patch, 4 + nrand B patches
@@ -150,6 +172,15 @@ def stage_bytes(stage, w, n_a, n_b, depth, n_cols, it=1, nrand=1, n_prop=0):
         return -(-n_cols // 128) * n_b * 4 * d + n_cols * 4 * d
     if stage == "project":  # both images: pixels in, reduced patches out
         return 2 * ((w["size"] ** 2) * 3 + n_b * 4 * d)
+    if stage == "build_level":  # per global level and point: split coordinate in, key out, two more
+        # digit passes and the count over the keys, the scatter's key, row and index in and out
+        return count * n_b * (4 + 4 + 4 + 4 + 4 + (4 + 4 * d + 4) + (4 * d + 4))
+    if stage == "build_subtree":  # rows and indices in and out once, point leaf out, leaf boxes
+        return n_b * (2 * (4 * d + 4) + 4) + (1 << depth) * 2 * 4 * d
+    if stage == "pca_gram":  # sampled patches gathered from the images, written blocked, read by the Gram
+        return 3 * n_sub * P
+    if stage == "pca_eigh":  # the covariance in, the components out (latency-bound)
+        return 8 * P * P + 8 * d * P
     return None
 
 
@@ -173,38 +204,41 @@ def load_traffic():
 # ---------------------------------------------------------------------------------------------
 # CPU arm (oracle)
 # ---------------------------------------------------------------------------------------------
-def cpu_sample(a, b, w, rows=ROWS_SAMPLE):
-    """Time the oracle on the pair: PCA fit, projection of B and of the sampled A rows, tree,
-    first row + `rows` later rows; returns (seconds extrapolated to the whole pair, detail)."""
+def _transform(O, patches, comps, mean, chunk=262144):
+    """The reference's FP64 projection, in chunks (bounded host memory)."""
+    return np.concatenate([O.pca_transform(patches[i:i + chunk], comps, mean) for i in range(0, len(patches), chunk)])
+
+
+def cpu_full(a, b, w):
+    """Time the oracle's complete plain-method fit of the pair (annfmp/openmp/base.py:53-150):
+    PCA fit, extraction and projection of both images, tree, and the whole row loop (first row,
+    every later row, re-rank). Returns (seconds, per-stage detail, NNF)."""
     from oracle import oracle as O
     prm = params_of(w)
     p = w["psize"]
     n_rows, n_cols = a.shape[0] - p + 1, a.shape[1] - p + 1
-    r = min(rows + 1, n_rows)
     t0 = time.perf_counter()
     comps, mean = O.pca_fit(a, b, p, prm["dim_reduced"], prm["n_subset"], prm["seed"])
     t1 = time.perf_counter()
     pb = O.extract_patches(b, p)
-    bred = np.concatenate([O.pca_transform(pb[i:i + 262144], comps, mean) for i in range(0, len(pb), 262144)])
+    bred = _transform(O, pb, comps, mean)
+    pa = O.extract_patches(a, p)
+    ared = _transform(O, pa, comps, mean)
     t2 = time.perf_counter()
-    pa = O.extract_patches(np.ascontiguousarray(a[: r + p - 1]), p)
-    ared = O.pca_transform(pa, comps, mean)
-    t3 = time.perf_counter()
     tree = O.OracleTree(bred, O.tree_depth(len(bred), prm["leaf_size"]))
+    t3 = time.perf_counter()
+    final, _ = tree.process_rows(ared, pa, pb, n_rows, n_cols, prm["n_neighbors"])
     t4 = time.perf_counter()
-    tree.process_rows(ared[:n_cols], pa[:n_cols], pb, 1, n_cols, prm["n_neighbors"])
-    t5 = time.perf_counter()
-    tree.process_rows(ared, pa, pb, r, n_cols, prm["n_neighbors"])
-    t6 = time.perf_counter()
-    first_row = t5 - t4
-    later = max((t6 - t5) - first_row, 0.0)  # rows 1..r-1 with their re-rank
-    proj_a = (t3 - t2) * n_rows / r
-    rows_all = later * (n_rows - 1) / max(r - 1, 1)
-    total = (t1 - t0) + (t2 - t1) + proj_a + (t4 - t3) + first_row + rows_all
-    det = dict(pca_fit=round(t1 - t0, 3), project_b=round(t2 - t1, 3), project_a=round(proj_a, 3),
-               tree=round(t4 - t3, 3), first_row=round(first_row, 3), rows=round(rows_all, 3),
-               rows_sampled=r - 1)
-    return total, det
+    det = dict(pca_fit=round(t1 - t0, 3), patches_and_projection=round(t2 - t1, 3), tree=round(t3 - t2, 3),
+               rows=round(t4 - t3, 3))
+    return t4 - t0, det, final
+
+
+def cpu_threads():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count()
 
 
 def run_reference(args, w, rank, world):
@@ -214,30 +248,31 @@ def run_reference(args, w, rank, world):
     p = w["psize"]
     n_a = (a.shape[0] - p + 1) * (a.shape[1] - p + 1)
     for _ in range(args.warmup):
-        cpu_sample(a, b, w)
+        cpu_full(a, b, w)
     times = []
     for _ in range(args.steps):
-        t, det = cpu_sample(a, b, w)
+        t, det, _ = cpu_full(a, b, w)
         times.append(t)
     t = float(np.mean(times))
-    cores = os.cpu_count()
+    cores = cpu_threads()
     val = n_a / t
     line = {"metric": "query patches/s", "value": val, "unit": "query patches/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "impl": "reference", "config": config_of(w, args),
+            "impl": "reference", "form": "plain", "config": config_of(w, args),
             "cpu_baseline": {"value": val, "unit": "query patches/s", "cores": cores, "kind": "port",
-                             "sample": f"full-pair PCA fit, projection, tree and first row; {ROWS_SAMPLE} later "
-                                       f"rows timed and extrapolated to all rows (last step: {det})"},
+                             "sample": f"every step one complete plain-method fit of the pair by the oracle (C "
+                                       f"restatement, OpenMP over {cores} threads, numpy PCA): all {n_a} query "
+                                       f"patches, nothing extrapolated (last step: {det})"},
             "e2e": {"value": val, "unit": "query patches/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
 
 def config_of(w, args):
+    """The workload, identical in both arms (the form each arm runs is a key of its own)."""
     prm = params_of(w)
     return {"workload": f"{w['size']}x{w['size']}x3 {w['kind']} pair seed {w['seed']}, patch {w['psize']}x"
                         f"{w['psize']}x3, PCA {w['dim_reduced']}, leaf {w['leaf_size']}, k {w['n_neighbors']}",
-            "form": args.form, "iters": args.iters if args.form != "plain" else None,
             "n_subset": prm["n_subset"], "pairs_per_rank": 1,
             "l2": "flushed between timed steps (256 MB write)", "parallelism": f"replicas x{args.gpus}"}
 
@@ -348,12 +383,16 @@ def run_gpu(args, w, rank, world, local_rank):
     h.profile(True)
     h.profile_read(torch.cuda.current_stream(dev).cuda_stream)
     stages = {}
+    stage_counts = {}
     for i in range(max(2, min(args.steps, 4))):
         flush.fill_(float(i))
         pm.fit(A, B)
         step = {}  # a stage that repeats within a fit (per image, per tree level) adds up
+        counts = {}
         for name, sms in h.profile_read(torch.cuda.current_stream(dev).cuda_stream):
             step[name] = step.get(name, 0.0) + sms
+            counts[name] = counts.get(name, 0) + 1
+        stage_counts = counts
         for name, sms in step.items():
             stages.setdefault(name, []).append(sms)
     h.profile(False)
@@ -383,9 +422,13 @@ def run_gpu(args, w, rank, world, local_rank):
     # profiled fast_init then reads one seed match per pixel, not the proposals
     prop_src = getattr(pm, "proposal", None)
     n_prop = 0 if prop_src is None or hasattr(prop_src, "seed") else int(getattr(prop_src, "per_pixel", 4))
-    sb = lambda k: stage_bytes(k, w, n_a, n_b, depth, n_cols, args.iters, pm.search[0], n_prop)  # noqa: E731
-    dom = max((k for k in kernel_stages if sb(k)), key=lambda k: kernel_stages[k])
-    by = sb(dom)
+    search = getattr(pm, "search", (1, 2))
+
+    def sb(k):
+        return stage_bytes(k, w, n_a, n_b, depth, n_cols, args.iters, search[0], n_prop, stage_counts.get(k, 1))
+    # the dominant stage: the largest of ALL stages (every stage has a byte model)
+    dom = max(kernel_stages, key=lambda k: kernel_stages[k])
+    by = sb(dom) or 0
     # distance error of the last timed NNF against the exact raw-patch nearest neighbour
     from annfmp_gb300 import metrics
     quality = metrics.distance_ratio_error(a, b, nn_dev, p, n_samples=4096, seed=w["seed"] + 7, device=local_rank)
@@ -401,33 +444,91 @@ def run_gpu(args, w, rank, world, local_rank):
     achieved = by / (kernel_stages[dom] / 1e3) / 1e9
     traffic = load_traffic().get(f"{args.workload}:{args.form}:{dom}")
     value = replica_value(n_a, ms, world)
+    roof = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "peak_kind": peak_kind, "algorithmic_bytes": by, "per": "NNF (all launches of the stage)",
+            "traffic": traffic}
+    if traffic:  # what DRAM itself delivered (ncu capture of the same stage), beside the touched bytes
+        roof["dram_achieved"] = traffic / (kernel_stages[dom] / 1e3) / 1e9
+        roof["dram_frac"] = roof["dram_achieved"] / peak
+    if dom in BINDING:
+        roof["binding_unit"], roof["binding_evidence"] = BINDING[dom]
     line = {
         "metric": "query patches/s", "value": value, "unit": "query patches/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": dict(config_of(w, args), execution="one CUDA graph replay per NNF" if graphed else "eager"),
+        "vs_baseline": None, "dtype": DTYPES[args.form], "arithmetic": ARITHMETIC[args.form], "data": "synthetic",
+        "form": args.form, "iters": args.iters if args.form != "plain" else None,
+        "execution": "one CUDA graph replay per NNF" if graphed else "eager",
+        "config": config_of(w, args),
         "e2e": {"value": replica_value(n_a, e2e_s * 1e3, world), "unit": "query patches/s",
                 "h2d_bytes_per_step": int(a.nbytes + b.nbytes),
                 "d2h_bytes_per_step": int(nn_host.numel() * nn_host.element_size())},
         "gpu_launches": int(launches),
-        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "peak_kind": peak_kind, "algorithmic_bytes": by,
-                     "traffic": traffic},
+        "roofline": roof,
+        "roofline_stages": {k: {"ms": v, "algorithmic_bytes": sb(k), "frac": (sb(k) or 0) / (v / 1e3) / 1e9 / peak}
+                            for k, v in sorted(kernel_stages.items(), key=lambda kv: -kv[1])},
         "distance_error": quality,
         "forms": forms,
-        "stages_ms": stage_ms, "wall_ms_per_step": t_wall * 1e3 / args.steps,
+        "stages_ms": stage_ms, "stage_marks_per_fit": stage_counts, "wall_ms_per_step": t_wall * 1e3 / args.steps,
         "clocks": clocks.summary(),
     }
     if world == 1 and not args.no_cpu_baseline:
-        t_cpu, det = cpu_sample(a, b, w)
-        line["cpu_baseline"] = {"value": n_a / t_cpu, "unit": "query patches/s", "cores": os.cpu_count(),
-                                "kind": "port", "sample": f"oracle: full-pair PCA fit, projection, tree, first row; "
-                                                          f"{ROWS_SAMPLE} later rows extrapolated ({det})"}
+        t_cpu, det, _ = cpu_full(a, b, w)
+        line["cpu_baseline"] = {"value": n_a / t_cpu, "unit": "query patches/s", "cores": cpu_threads(),
+                                "kind": "port", "sample": f"one complete plain-method fit of the pair by the oracle "
+                                                          f"(all {n_a} query patches, nothing extrapolated; {det})"}
+    if world == 1 and not args.no_compare:
+        del model, pm
+        torch.cuda.empty_cache()
+        line["workloads"] = other_workloads(args, local_rank, flush)
     print(json.dumps(line), flush=True)
 
 
-def run_graph_workload(args, name, rank, world, local_rank):
-    """Batched pairs under CUDA graphs: value = query patches of all pairs / time of the launches."""
+# where ncu located the binding unit of a stage's main kernel (committed summaries)
+BINDING = {
+    "fast_propagate": ("l1", "profiles/fast_prop_t_kernel_medium_learned.md: L1 throughput 83%, DRAM 1%"),
+    "natural_knn": ("issue (per-query selection and exact re-rank)", "profiles/leaf_tc_kernel_medium_learned.md"),
+    "chain": ("latency (long-scoreboard stalls, leaf re-reads from L2)", "profiles/chain_sel_kernel_medium_plain.md"),
+    "first_row": ("latency (one warp per query, few warps active)", "profiles/exact_scan_kernel_medium_plain.md"),
+}
+
+
+def other_workloads(args, local_rank, flush):
+    """The 512x512 pair by the plain method (with the oracle on the same pair), the 64 uneven
+    pairs in one graph launch and the 1920x1080 frame stream: each timed with its own events
+    and checked for distance error, so one default run records every workload."""
+    from annfmp_gb300 import metrics
+    import torch
+    out = {}
+    w = WORKLOADS["small"]
+    a, b = make_pair(w)
+    prm = params_of(w)
+    p = w["psize"]
+    n_a = (a.shape[0] - p + 1) * (a.shape[1] - p + 1)
+    dev = torch.device("cuda", local_rank)
+    A, B = torch.from_numpy(a).to(dev), torch.from_numpy(b).to(dev)
+    rec = {"config": config_of(w, args)}
+    for f in ("plain", "learned" if learned_available() else "parallel"):
+        fms, fnn = time_form(f, args, prm, local_rank, A, B, flush, max(3, args.steps // 2))
+        rec[f] = {"ms_per_step": fms, "value": n_a / (fms / 1e3),
+                  "distance_error": metrics.distance_ratio_error(a, b, fnn, p, n_samples=4096, seed=w["seed"] + 7,
+                                                                 device=local_rank)}
+        if f == "plain":
+            nn_plain = fnn.cpu().numpy()
+    t_cpu, det, nn_cpu = cpu_full(a, b, w)
+    rec["cpu_oracle"] = {"ms_per_step": t_cpu * 1e3, "value": n_a / t_cpu, "cores": cpu_threads(), "detail": det}
+    rec["plain_nnf_identical_to_oracle"] = float((nn_plain == nn_cpu).mean())
+    out["small"] = rec
+    gargs = argparse.Namespace(**vars(args))
+    gargs.steps = 3
+    for name in ("batch", "stream"):
+        out[name] = run_graph_workload(gargs, name, 0, 1, local_rank, emit=False)
+        torch.cuda.empty_cache()
+    return out
+
+
+def run_graph_workload(args, name, rank, world, local_rank, emit=True):
+    """Batched pairs under CUDA graphs: value = query patches of all pairs / time of the launches.
+    Prints the JSON line (emit) or returns it."""
     import torch
 
     from annfmp_gb300 import _lib, gen
@@ -520,7 +621,9 @@ def run_graph_workload(args, name, rank, world, local_rank):
         "gpu_launches": int(_lib.launch_count() - launches0) + per_step * args.steps,
         "graph_launches_per_step": len(feeds), "clocks": clocks.summary(),
     }
-    print(json.dumps(line), flush=True)
+    if emit:
+        print(json.dumps(line), flush=True)
+    return line
 
 
 def main():

@@ -93,14 +93,17 @@ int annf_kneighbors(annf_handle* h, const void* queries, int nq, int k, long lon
                     void* distances, int* indices, void* stream);
 
 /* No counterpart in the reference. The same exact k nearest neighbours as annf_kneighbors (same
- * results), for callers that must not allocate device memory while they query: work issued under
- * CUDA stream capture (cudaMalloc cannot be captured), serving processes whose device memory is
- * reserved ahead of time, or allocators that refuse to grow. Build the tree first (that allocates);
- * this call then allocates nothing. Its scratch is one static device array shared by all calls,
- * sized for nq * k <= 262144 (3 MiB, held by every GPU that loads the library until exit); larger
+ * results), for callers that must not allocate device memory while they query: serving processes
+ * whose device memory is reserved ahead of time, host applications that own all device memory
+ * through their own pool, or allocators that refuse to grow. Build the tree first (that
+ * allocates); this call then allocates nothing. Its scratch is one static device array shared by
+ * all calls, sized for nq * k <= 262144 for both real types (5 MiB: a 16-byte double seed key and
+ * a 4-byte position per entry, held by every GPU that loads the library until exit); larger
  * requests fail with ANNF_ERR_INVALID. The first call on each device looks the array's device
  * address up (cudaGetSymbolAddress), so make that first call before any stream capture. Calls that
- * overlap on the GPU (unordered streams) race on the shared scratch. */
+ * overlap on the GPU (unordered streams) race on the shared scratch. The unbudgeted search always
+ * scans every leaf box per query (one warp per query), so many queries on a deep tree run slower
+ * here than through annf_kneighbors, which switches to its tiled box scan. */
 int annf_kneighbors_noalloc(annf_handle* h, const void* queries, int nq, int k, long long max_leaves,
                             void* distances, int* indices, void* stream);
 

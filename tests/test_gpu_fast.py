@@ -39,6 +39,40 @@ def test_subspace_pca_captures_leading_variance(gpu_lib, oracle_mod, golden, nam
     assert np.all(V[np.arange(d), j] > 0)
 
 
+def test_subspace_pca_rank_deficient_covariance(gpu_lib, oracle_mod):
+    """A covariance of lower rank than the iteration's block (B = d + max(8, d/2) = 16 vectors for
+    d = 8): images whose pixels are u[x] + v[y] in all three channels give 7x7 patches spanning
+    13 directions, so Cholesky-QR loses columns and Q^T Q is far from the identity. The FP64
+    Rayleigh-Ritz step then takes its Cholesky path, dropping the dependent columns. The
+    components must still be orthonormal, in decreasing Ritz value, and capture the top-d
+    variance of numpy's eigh of the same covariance to the bound the other cases use."""
+    from annfmp_gb300 import ANNFieldPropKDTreeGB300
+    O = oracle_mod
+    rng = np.random.default_rng(17)
+    imgs = []
+    for _ in range(2):
+        u, v = rng.integers(0, 128, 96), rng.integers(0, 128, 96)
+        imgs.append(np.repeat((v[:, None] + u[None, :]).astype(np.uint8)[:, :, None], 3, axis=2))
+    a, b = imgs
+    psize, d, n_subset, seed = 7, 8, 2000, 0
+    C = _covariance(O, a, b, psize, n_subset, seed)
+    assert np.linalg.matrix_rank(C) < d + max(8, d // 2)  # the block is rank-deficient
+    m = ANNFieldPropKDTreeGB300(n_neighbors=1, psize=psize, dim_reduced=d, n_subset=n_subset, leaf_size=16,
+                                seed=seed, verbose=0, form="parallel", pca_solver="subspace")
+    nn = m.fit(a, b)
+    assert nn.shape == (90 * 90,) and nn.min() >= 0 and nn.max() < 90 * 90
+    V = m.components_.cpu().numpy()
+    assert np.all(np.isfinite(V))
+    Xs = np.concatenate([O.subset_patches(a, psize, n_subset // 2, seed),
+                         O.subset_patches(b, psize, n_subset // 2, seed + 1)]).astype(np.float64)
+    assert np.array_equal(m.mean_.cpu().numpy(), Xs.mean(axis=0))
+    assert np.abs(V @ V.T - np.eye(d)).max() < 1e-9
+    w = np.linalg.eigvalsh(C)[::-1]
+    ritz = np.einsum("ij,jk,ik->i", V, C, V)
+    assert np.all(np.diff(ritz) <= 1e-9 * ritz[0])
+    assert ritz.sum() >= w[:d].sum() * (1 - 1e-4), (ritz.sum(), w[:d].sum())
+
+
 # ---------------------------------------------------------------------------------------------
 # tensor cores: one tcgen05 tile against a torch FP32 matmul of the same BF16 values
 # ---------------------------------------------------------------------------------------------

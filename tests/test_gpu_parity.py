@@ -256,6 +256,27 @@ def _relative_excess(a, b, psize, nn_x, nn_y):
     return dx, dy
 
 
+REL_TOL = 1e-5  # a pixel whose NNF entry differs must match as well as the reference's entry, to 1e-5
+
+
+def assert_differing_pixels_close(a, b, psize, nn_gpu, nn_ref, rel=REL_TOL):
+    """Where the two NNFs differ, the raw-patch L2 of the GPU's match is within `rel` (relative)
+    of the reference's: the difference is a tie or a rounding difference, not a worse match.
+    Returns the number of differing pixels."""
+    from annfmp_gb300.metrics import _patch_ssd
+    nn_gpu, nn_ref = np.asarray(nn_gpu), np.asarray(nn_ref)
+    diff = np.nonzero(nn_gpu != nn_ref)[0]
+    if len(diff) == 0:
+        return 0
+    dg = np.sqrt(_patch_ssd(a, b, psize, diff, nn_gpu[diff]).astype(np.float64))
+    dr = np.sqrt(_patch_ssd(a, b, psize, diff, nn_ref[diff]).astype(np.float64))
+    bad = np.abs(dg - dr) > rel * np.maximum(dr, 1e-300)
+    bad &= ~((dg == 0) & (dr == 0))
+    assert not bad.any(), (f"{int(bad.sum())} of {len(diff)} differing pixels beyond {rel} relative distance",
+                           diff[bad][:8], dg[bad][:8], dr[bad][:8])
+    return len(diff)
+
+
 @pytest.mark.parametrize("name", PIPES)
 def test_pipeline_vs_reference(gpu_lib, golden, name):
     """End to end from the images (GPU PCA fit, projection, tree, rows, re-rank) vs the reference's
@@ -268,6 +289,9 @@ def test_pipeline_vs_reference(gpu_lib, golden, name):
     dg, dr = _relative_excess(z["a"], z["b"], psize, nn, z["nn"])
     # the per-pixel distance the GPU reports is the raw-patch L2 of its choice
     assert np.allclose(m.nn_distances_.cpu().numpy(), dg, rtol=1e-6)
+    # every differing pixel: within 1e-5 relative raw-patch distance of the reference's match
+    differ = nn != z["nn"]
+    assert np.all(np.abs(dg[differ] - dr[differ]) <= REL_TOL * dr[differ]), np.nonzero(differ)[0][:8]
 
 
 @pytest.mark.slow
@@ -283,6 +307,95 @@ def test_small_pair_workload_vs_oracle(gpu_lib, oracle_mod):
     nn_o = O.oracle_fit(a, b, n_neighbors=1, psize=7, dim_reduced=8, n_subset=nsub, leaf_size=32, seed=0)
     agree = (nn == nn_o).mean()
     assert agree >= 0.999, agree
+    assert_differing_pixels_close(a, b, 7, nn, nn_o)
+
+
+def _workload_pair(shape):
+    """The image pairs and parameters of the 2048x2048 flow workload (patch 9, PCA 16, leaf 64,
+    k 4) and of one 1920x1080 frame pair of the frame stream (patch 5, PCA 12, leaf 32, k 8);
+    n_subset is 10% of B's patch count, as in the benchmark."""
+    from annfmp_gb300 import gen
+    if shape == "flow2048":
+        a, b = gen.pair_flow(1, 2048)
+        kw = dict(n_neighbors=4, psize=9, dim_reduced=16, leaf_size=64, seed=1)
+    else:
+        a, b = gen.frame_stream(3, 2, 1080, 1920)[:2]
+        kw = dict(n_neighbors=8, psize=5, dim_reduced=12, leaf_size=32, seed=3)
+    p = kw["psize"]
+    kw["n_subset"] = int(round(0.1 * (b.shape[0] - p + 1) * (b.shape[1] - p + 1)))
+    return a, b, kw
+
+
+@pytest.mark.slow
+@pytest.mark.parametrize("shape", ["flow2048", "frame1080"])
+def test_plain_form_at_workload_shape_vs_oracle(gpu_lib, oracle_mod, shape):
+    """The plain form at the benchmark's own shapes (4.16 M and 2.06 M patches, depth 15) against
+    the oracle on the same images. End to end (the GPU fits its own PCA): >= 99.9% identical NNF
+    and every differing pixel within 1e-5 relative raw-patch distance. On the oracle's own reduced
+    arrays: the tree (permutation, split axes and value bits, leaf bounds, point leaves, leaf
+    boxes), the k-lists and the NNF bit for bit."""
+    O = oracle_mod
+    from annfmp_gb300 import ANNFieldPropKDTreeGB300, KDTree
+    a, b, kw = _workload_pair(shape)
+    p, k = kw["psize"], kw["n_neighbors"]
+    r = O.oracle_fit(a, b, return_all=True, **kw)
+    m = ANNFieldPropKDTreeGB300(verbose=0, **kw)
+    nn = m.fit(a, b)
+    agree = float((nn == r["nn"]).mean())
+    assert agree >= 0.999, agree
+    assert_differing_pixels_close(a, b, p, nn, r["nn"])
+    del m
+    ot = r["tree"]
+    kd = KDTree(n_neighbors=k, leaf_size=kw["leaf_size"], splitting_type="longest", float_type="float").fit(r["bred"])
+    assert kd.final_tree_depth_ == ot.depth
+    assert_tree_equal(kd.tree_arrays(), ot.perm, ot.node_axis, ot.node_split, ot.leaf_bounds, ot.point_leaf,
+                      r["bred"], shape)
+    out = np.zeros(r["n_rows"] * r["n_cols"], np.int32)
+    kd.process_rows(out, r["pa"], r["pb"], r["ared"], r["n_rows"], r["n_cols"], k, True, True)
+    assert np.array_equal(kd.knn_indices_.cpu().numpy(), r["knn"])
+    assert np.array_equal(out, r["nn"])
+
+
+# ---------------------------------------------------------------------------------------------
+# natural-leaf kNN (the reference's traversal with max_leaves=1) in every leaf precision
+# ---------------------------------------------------------------------------------------------
+def _reduced_pair(O, kind):
+    """Reduced patches (oracle PCA and FP64 transform) of a flow pair at the 2048x2048 workload's
+    patch settings (patch 9, PCA 16), of a frame pair at the frame stream's (patch 5, PCA 12), or
+    the flow pair's coordinates on a coarse grid (many exactly tied distances)."""
+    from annfmp_gb300 import gen
+    if kind == "frames":
+        a, b = gen.frame_stream(3, 2, 360, 640)[:2]
+        p, d = 5, 12
+    else:
+        a, b = gen.pair_flow(1, 512)
+        p, d = 9, 16
+    nb = (b.shape[0] - p + 1) * (b.shape[1] - p + 1)
+    comps, mean = O.pca_fit(a, b, p, d, int(round(0.1 * nb)), 0)
+    ared = O.pca_transform(O.extract_patches(a, p), comps, mean)
+    bred = O.pca_transform(O.extract_patches(b, p), comps, mean)
+    if kind == "grid":
+        ared = (np.round(ared / 16) * 16).astype(np.float32)
+        bred = (np.round(bred / 16) * 16).astype(np.float32)
+    return ared, bred
+
+
+@pytest.mark.parametrize("kind,leaf,k", [("flow", 64, 4), ("frames", 32, 8), ("grid", 64, 4)])
+def test_natural_knn_all_precisions_vs_oracle(gpu_lib, oracle_mod, kind, leaf, k):
+    """The k-lists of the natural leaf (the reference's query with max_leaves=1, kdtree.c:179-183)
+    from the FP32 leaf scan and from the BF16 / FP16 / FP8 tensor-core tiles with their exact FP32
+    re-rank equal the oracle's, index for index (ties broken in the reference's leaf order)."""
+    O = oracle_mod
+    from annfmp_gb300 import KDTree
+    ared, bred = _reduced_pair(O, kind)
+    depth = O.tree_depth(len(bred), leaf)
+    ot = O.OracleTree(bred, depth)
+    _, want = ot.kneighbors(ared, k, max_leaves=1)
+    kd = KDTree(n_neighbors=k, leaf_size=leaf, splitting_type="longest", float_type="float").fit(bred)
+    for prec in ("fp32", "bf16", "fp16", "fp8"):
+        got = kd.natural_kneighbors(ared, k, prec)
+        same = (got == want).all(axis=1)
+        assert same.all(), (kind, prec, float(same.mean()), np.nonzero(~same)[0][:8])
 
 
 def test_image_and_array_paths_agree(gpu_lib, golden):

@@ -134,3 +134,22 @@ def test_generators_are_seeded():
     a, b = gen.pair_flow(1, 96, sigma=8.0)
     assert a.shape == b.shape == (96, 96, 3)
     assert a.min() == 0 and a.max() == 255
+
+
+def test_mean_patch_l2_is_the_example_score():
+    """metrics.mean_patch_l2 equals the reference example's overall L2 score
+    (examples/simple.py:31-36: float32 patch differences, their L2 norms, the mean), restated
+    here on the oracle's patch arrays; integer SSDs make ours exact, the example's float32
+    norms agree to 1e-6."""
+    from annfmp_gb300 import gen, metrics
+    from oracle import oracle as O
+    O.build_oracle()
+    a, b = gen.pair_small(0, 96)
+    psize = 5
+    n = (96 - psize + 1) ** 2
+    nnf = np.random.default_rng(3).integers(0, n, n).astype(np.int32)
+    nnf[::4] = np.arange(n)[::4]
+    pa, pb = O.extract_patches(a, psize), O.extract_patches(b, psize)
+    diff = pa.astype(np.float32) - pb[nnf].astype(np.float32)
+    score = np.mean(np.linalg.norm(diff, axis=1))
+    assert np.isclose(metrics.mean_patch_l2(a, b, nnf, psize), float(score), rtol=1e-6, atol=0)
