@@ -21,6 +21,7 @@ ANNF_ERR_STATE = -5
 ANNF_ERR_DEVICE = -6
 ANNF_ERR_SOLVER = -7
 
+ANNF_OPT_INT_PROJECTION = 1
 ANNF_REAL_F32 = 0
 ANNF_REAL_F64 = 1
 ANNF_SPLIT_CYCLIC = 0
@@ -75,6 +76,7 @@ SIGNATURES = {
     "annf_pca_fit_subspace": (_i, [_vp, _vp, _i, _i, _vp, _i, _vp, _i, _i, _vp, _i, _i, _i, _i, _i, _vp, _vp, _vp]),
     "annf_project": (_i, [_vp, _vp, _i, _i, _i, _i, _vp, _vp, _i, _i, _vp, _vp]),
     "annf_device_status": (_i, [_vp, _vp, ctypes.POINTER(_u)]),
+    "annf_set_option": (_i, [_vp, _i, _i]),
     "annf_parallel_nnf": (_i, [_vp, _vp, _vp, _i, _i, _vp, _i, _i, _i, _i, _vp, _i, _vp, _i, _i, _u, _i, _i, _i, _vp,
                                _vp]),
     "annf_parallel_nnf_seeded": (_i, [_vp, _vp, _vp, _i, _i, _vp, _i, _i, _i, _i, _vp, _i, _vp, _i, _u, _i, _i, _i,

@@ -307,6 +307,19 @@ int annf_project(annf_handle* h, const uint8_t* img, int hgt, int wid, int chann
                  static_cast<cudaStream_t>(stream));
 }
 
+int annf_set_option(annf_handle* h, int option, int value) {
+  ANNF_API_HANDLE(h);
+  switch (option) {
+    case ANNF_OPT_INT_PROJECTION:
+      ANNF_REQUIRE(value == 0 || value == 1, "annf_set_option: ANNF_OPT_INT_PROJECTION takes 0 or 1");
+      h->opt_int_projection = value;
+      return ANNF_OK;
+    default:
+      set_error("annf_set_option: unknown option " + std::to_string(option));
+      return ANNF_ERR_INVALID;
+  }
+}
+
 int annf_device_status(annf_handle* h, void* stream, unsigned* bits_out) {
   ANNF_API_HANDLE(h);
   unsigned bits = 0;

@@ -64,12 +64,14 @@ struct annf_handle {
   annf::DevBuf bmin, bmax, axis, keys, hist, sel_prefix, sel_rank, sel_nlt, sel_neq, blk_lt, blk_eq,
       off_lt, off_eq, eqpos;
   // ---- query scratch ----
-  annf::DevBuf nat_keys, nat_pos, lists, next_range, part_keys, part_pos;
+  annf::DevBuf nat_keys, nat_pos, lists, next_range, part_keys, part_pos, leaf_marks;
   // ---- parallel form scratch ----
   annf::DevBuf fast_buf, fast_nat, tc_buf, pj_buf;
   // ---- pca scratch ----
   annf::DevBuf gram, colsum, subset_t, cov, eigval, digits, meanproj, solver_ws, solver_info, eig_ws;
   int cov_p = 0;  // size of the covariance held in cov (0: none)
+  // ---- options (annf_set_option) ----
+  int opt_int_projection = 0;  // 1: the exact projection always runs the dp4a kernel
   cusolverDnContext* solver = nullptr;
   // ---- device status word ----
   annf::DevBuf status;

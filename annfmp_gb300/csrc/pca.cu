@@ -18,6 +18,7 @@
 
 #include "common.cuh"
 #include "handle.cuh"
+#include "fixed.cuh"
 
 namespace annf {
 
@@ -218,7 +219,6 @@ constexpr int kSlices = 8;  // signed 7-bit digits per coefficient
 // digits[j][k][word*4 + byte] laid out over the padded patch (row r occupies rw bytes, rw =
 // round_up(psize*c, 4)), total W4 words (multiple of 4). Also scale exponent per component and
 // the FP64 mean term m_j = mean . c_j.
-__device__ __forceinline__ __int128 double_to_fixed(double m, int sh);
 
 __global__ void digits_kernel(const double* __restrict__ comps, const double* __restrict__ mean, int P, int psize,
                               int c, int rw, int W4, int8_t* __restrict__ digits, int* __restrict__ expo,
@@ -269,50 +269,6 @@ __global__ void digits_kernel(const double* __restrict__ comps, const double* __
 }
 
 constexpr int kPTW = 32, kPTH = 4;  // projection tile: 32 x 4 pixels, one thread per pixel
-
-// D * 2^-sh rounded to the nearest float (ties to even), integer arithmetic only
-__device__ __forceinline__ float fixed_to_float(__int128 D, int sh) {
-  if (D == 0) return 0.0f;
-  const bool neg = D < 0;
-  const unsigned __int128 A = neg ? (unsigned __int128)(-D) : (unsigned __int128)D;
-  const unsigned long long hi = (unsigned long long)(A >> 64), lo = (unsigned long long)A;
-  const int p = hi ? 127 - __clzll((long long)hi) : 63 - __clzll((long long)lo);  // top bit
-  unsigned long long mant;
-  int e;
-  if (p <= 23) {
-    mant = lo;
-    e = -sh;
-  } else {
-    const int s = p - 23;
-    const unsigned __int128 q = A >> s;
-    const unsigned __int128 r = A - (q << s);
-    const unsigned __int128 half = (unsigned __int128)1 << (s - 1);
-    mant = (unsigned long long)q;
-    if (r > half || (r == half && (mant & 1ull))) ++mant;  // may reach 2^24: still exact below
-    e = s - sh;
-  }
-  const float f = ldexpf((float)mant, e);
-  return neg ? -f : f;
-}
-
-// m * 2^sh rounded to an integer (m FP64); exact whenever m's last bit weighs at least 2^-sh
-__device__ __forceinline__ __int128 double_to_fixed(double m, int sh) {
-  if (m == 0.0) return 0;
-  int e;
-  const double f = frexp(fabs(m), &e);                          // |m| = f 2^e, f in [0.5, 1)
-  const long long mant = (long long)ldexp(f, 53);                // exact 53-bit integer
-  const int s = e - 53 + sh;                                     // |m| 2^sh = mant 2^s
-  __int128 v;
-  if (s >= 0) {
-    v = (__int128)mant << s;
-  } else if (s > -64) {
-    const long long q = mant >> (-s), r = mant - (q << (-s)), half = 1LL << (-s - 1);
-    v = q + ((r > half || (r == half && (q & 1))) ? 1 : 0);
-  } else {
-    v = 0;
-  }
-  return m < 0 ? -v : v;
-}
 
 __device__ __forceinline__ unsigned load_u32_unaligned_smem(const unsigned* base_words, int byte_off) {
   const int w = byte_off >> 2, sh = (byte_off & 3) * 8;
@@ -402,6 +358,10 @@ int subspace_block(int P, int ncomp);
 bool gram_tc_supported(int F, int ns_pad);
 int gram_tc(const uint8_t* XT, int F, int ns_pad, unsigned long long* G, unsigned* status, cudaStream_t st);
 int eig_top_subspace(annf_handle* h, const double* C, int P, int ncomp, int iters, double* comps, cudaStream_t st);
+bool project_rows_exact_supported(int psize, int c, int ncomp);
+int project_rows_exact(annf_handle* h, const uint8_t* img, int H, int W, int c, int psize, int ncomp,
+                       const int8_t* digits, int rw, int W4, const int* expo, const unsigned long long* mfix,
+                       float* out, cudaStream_t st);
 
 // covariance (FP64, in h->cov) and mean of the sampled patches
 int pca_covariance(annf_handle* h, const uint8_t* img_a, int ha, int wa, const int* pos_a, int n_a,
@@ -526,6 +486,14 @@ int project(annf_handle* h, const uint8_t* img, int H, int W, int c, int psize, 
       (reinterpret_cast<uintptr_t>(expo + ncomp) + 15) & ~uintptr_t(15));
   digits_kernel<<<ncomp, 256, 0, st>>>(comps, mean, P, psize, c, rw, W4, dig, expo, h->meanproj.as<double>(), mfix);
   ANNF_CHECK_LAUNCH();
+  // FP32 output of images with at most 4 channels: the slice sums on the tensor cores (the same
+  // integers, the same single rounding); otherwise, or when asked, the dp4a kernel below
+  if (real_type == ANNF_REAL_F32 && !h->opt_int_projection && project_rows_exact_supported(psize, c, ncomp)) {
+    const int rc = project_rows_exact(h, img, H, W, c, psize, ncomp, dig, rw, W4, expo, mfix, (float*)out, st);
+    if (rc != ANNF_OK) return rc;
+    prof_mark(h, "project", st);
+    return ANNF_OK;
+  }
   const int nrows = H - psize + 1, ncols = W - psize + 1;
   dim3 grid(ceil_div(ncols, kPTW), ceil_div(nrows, kPTH));
   const int reg_rows = kPTH + psize - 1;

@@ -16,6 +16,7 @@
 #include <algorithm>
 
 #include "common.cuh"
+#include "fixed.cuh"
 #include "handle.cuh"
 #include "tc.cuh"
 
@@ -422,6 +423,255 @@ __global__ void __launch_bounds__(kPrThreads) project_rows_tc_kernel(
   tc::fence_before_sync();
   __syncthreads();
   if (warp == 0) tc::tmem_dealloc(tmem, 2 * NPAD);
+}
+
+// ---------------------------------------------------------------------------------------------
+// Exact projection (annf_project) on the tensor cores. pca.cu splits every FP64 coefficient into
+// 8 signed 7-bit digits (c = 2^-E sum_k s_k 2^-7k); the product of a patch with one digit slice
+// is an integer of magnitude below 2^24 (at most 256 products of a pixel <= 255 and a digit
+// <= 64), so FP16 operands with an FP32 accumulator give it exactly, in any summation order. The
+// MMAs are the row form's (converted image rows as the A operand); the B columns of a CTA are the
+// 8 slices of 8 components (column 8 c + k = slice k of component 8 g + c, g = the CTA's component
+// group). The epilogue recombines a component's slices in 128-bit fixed point, subtracts the mean
+// term in the same units and rounds once to FP32: the arithmetic of project_kernel (pca.cu), so
+// the two give the same bits. Eight warps per CTA: warp w reads TMEM lanes 32 (w mod 4) .. + 31
+// for the even patches (w < 4) or the odd ones; two TMEM accumulators, so the MMAs of the next
+// output row run while this row's epilogue reads the other.
+// ---------------------------------------------------------------------------------------------
+constexpr int kPxThreads = 256;
+constexpr int kPxCols = 64;  // B columns per CTA: 8 components x 8 digit slices
+
+// B operand per component group g and filter row r: [groups][psize][64][kr] FP16, k = 4 s + ch as
+// pr_prep_kernel; from digits_kernel's table digits[j][slice][r * rw + s * C + ch] (W4 words per
+// slice); zero past the patch or past the last component
+__global__ void px_prep_kernel(const int8_t* __restrict__ digits, int d, int groups, int psize, int C, int rw, int W4,
+                               int kr, uint16_t* __restrict__ bmat) {
+  const long long total = (long long)groups * psize * kPxCols * kr;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x) {
+    const int k = (int)(e % kr);
+    const long long t = e / kr;
+    const int n = (int)(t % kPxCols);
+    const long long t2 = t / kPxCols;
+    const int r = (int)(t2 % psize), g = (int)(t2 / psize);
+    const int j = 8 * g + (n >> 3), sl = n & 7;
+    const int px = k >> 2, ch = k & 3;
+    int v = 0;
+    if (j < d && px < psize && ch < C) v = digits[((size_t)j * 8 + sl) * W4 * 4 + r * rw + px * C + ch];
+    bmat[e] = __half_as_ushort(__int2half_rn(v));
+  }
+}
+
+// image row Y into the even / odd copies, as pr_convert_row, with kPxThreads threads
+__device__ __forceinline__ void px_convert_row(const uint8_t* __restrict__ img, int W, int C, int Y, int x0, int pe,
+                                               uint2* even, uint2* odd) {
+  for (int q = threadIdx.x; q <= pe; q += kPxThreads) {
+    const int X = x0 + q;
+    uint32_t ch[4] = {0u, 0u, 0u, 0u};
+    if (X < W) {
+      const uint8_t* px = img + ((size_t)Y * W + X) * C;
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+        if (u < C) ch[u] = __ldg(px + u);
+    }
+    const uint32_t lo = (uint32_t)__half_as_ushort(__uint2half_rn(ch[0])) |
+                        ((uint32_t)__half_as_ushort(__uint2half_rn(ch[1])) << 16);
+    const uint32_t hi = (uint32_t)__half_as_ushort(__uint2half_rn(ch[2])) |
+                        ((uint32_t)__half_as_ushort(__uint2half_rn(ch[3])) << 16);
+    const uint2 v = make_uint2(lo, hi);
+    if (q < pe) even[q] = v;
+    if (q >= 1) odd[q - 1] = v;
+  }
+}
+
+template <int KS>
+__global__ void __launch_bounds__(kPxThreads) project_exact_tc_kernel(
+    const uint8_t* __restrict__ img, int H, int W, int C, int psize, int d, int groups,
+    const uint16_t* __restrict__ bmat, const int* __restrict__ expo, const unsigned long long* __restrict__ mfix,
+    float* __restrict__ out, int vec_out, unsigned* status) {
+  constexpr int KR = KS * 16;
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  const int ncols = W - psize + 1, nrows = H - psize + 1;
+  const int pe = 254 + KR / 4;
+  const int strips = (ncols + 255) / 256;
+  const int g = blockIdx.x % groups;  // component group: neighbouring CTAs read the same image rows
+  const int rest = blockIdx.x / groups;
+  const int strip = rest % strips, chunk = rest / strips;
+  const int x0 = strip * 256, yb = chunk * kPrRows, ye = min(nrows, yb + kPrRows);
+  unsigned char* p = smem_raw;
+  unsigned char* sB = p;  // [psize] filter rows of 64 x KR FP16, core layout
+  p += (size_t)psize * kPxCols * KR * 2;
+  const int nslot = psize + 1;
+  unsigned char* ring = p;  // [psize + 1 slots][even, odd][pe pixels][8 bytes]
+  p += (size_t)nslot * 2 * pe * 8;
+  p = reinterpret_cast<unsigned char*>(((uintptr_t)p + 15) & ~uintptr_t(15));
+  uint64_t* mbar = reinterpret_cast<uint64_t*>(p);  // [2]: one per TMEM accumulator
+  p += 16;
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(p);
+  p += 8;
+  int* sflag = reinterpret_cast<int*>(p);
+  p += 8;
+  if (smem_overrun(smem_raw, p, status)) return;
+  if (yb >= nrows) return;  // uniform per block
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  if (warp == 0) {
+    tc::tmem_alloc(tslot, 4 * kPxCols);  // two accumulators x (even, odd) x 64 columns
+    tc::tmem_relinquish();
+  }
+  if (tid == 0) {
+    tc::mbar_init(mbar, 1);
+    tc::mbar_init(mbar + 1, 1);
+    tc::mbar_fence_init();
+    sflag[0] = 0;
+  }
+  const uint16_t* bg = bmat + (size_t)g * psize * kPxCols * KR;
+  for (int e = tid; e < psize * kPxCols * (KR / 8); e += kPxThreads) {
+    const int r = e / (kPxCols * (KR / 8)), rem = e - r * kPxCols * (KR / 8);
+    const int n = rem / (KR / 8), k8 = (rem - n * (KR / 8)) * 8;
+    *reinterpret_cast<uint4*>(sB + (size_t)r * kPxCols * KR * 2 + tc::core_offset(n, k8, KR)) =
+        *reinterpret_cast<const uint4*>(bg + ((size_t)r * kPxCols + n) * KR + k8);
+  }
+  auto slot_even = [&](int Y) { return reinterpret_cast<uint2*>(ring + (size_t)(2 * (Y % nslot)) * pe * 8); };
+  auto slot_odd = [&](int Y) { return reinterpret_cast<uint2*>(ring + (size_t)(2 * (Y % nslot) + 1) * pe * 8); };
+  for (int Y = yb; Y < yb + psize; ++Y) px_convert_row(img, W, C, Y, x0, pe, slot_even(Y), slot_odd(Y));
+  tc::fence_async_smem();
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = *tslot;
+  const uint32_t idesc = tc::idesc_f16(128, kPxCols);
+  // the MMAs of output row y (image rows y .. y + psize - 1) into accumulator buf
+  auto issue = [&](int y, int buf) {
+    for (int half = 0; half < 2; ++half) {
+      for (int r = 0; r < psize; ++r) {
+        const unsigned char* a = reinterpret_cast<const unsigned char*>(half ? slot_odd(y + r) : slot_even(y + r));
+        const unsigned char* b = sB + (size_t)r * kPxCols * KR * 2;
+#pragma unroll
+        for (int kk = 0; kk < KS; ++kk)
+          tc::mma_bf16(tmem + (uint32_t)(buf * 2 * kPxCols + half * kPxCols), tc::sdesc(a + kk * 32, 16, 128),
+                       tc::sdesc(b + kk * 256, 128, (KR / 8) * 128), idesc, (r > 0 || kk > 0) ? 1u : 0u);
+      }
+    }
+    tc::mma_commit(mbar + buf);
+  };
+  uint32_t phase = 0u;    // bit b: the parity to wait for on mbar[b]
+  uint32_t pending = 1u;  // bit b: a commit on mbar[b] not waited for yet
+  if (tid == 0) issue(yb, 0);
+  const int quarter = warp & 3, half = warp >> 2;
+  const int x = x0 + 2 * (quarter * 32 + lane) + half;
+  const bool vec = vec_out && 8 * g + 8 <= d;  // vec_out: d a multiple of 4 and out 16-byte aligned
+  for (int y = yb; y < ye; ++y) {
+    const int buf = (y - yb) & 1;
+    // the image row the next output row adds goes to the slot of row y - 1, whose MMAs were
+    // waited for in the previous iteration (row y's MMAs do not read it)
+    if (y + 1 < ye) {
+      px_convert_row(img, W, C, y + psize, x0, pe, slot_even(y + psize), slot_odd(y + psize));
+      tc::fence_async_smem();
+    }
+    tc::fence_before_sync();
+    __syncthreads();  // the row is converted, and the epilogue of row y - 1 has left accumulator buf ^ 1
+    if (sflag[0]) break;
+    if (y + 1 < ye) {
+      if (tid == 0) {
+        tc::fence_after_sync();
+        issue(y + 1, buf ^ 1);
+      }
+      pending |= 2u >> buf;  // bit buf ^ 1
+    }
+    const bool ok = __all_sync(0xffffffffu, pj_wait(mbar + buf, (phase >> buf) & 1u));
+    phase ^= 1u << buf;
+    pending &= ~(1u << buf);
+    if (!ok) {
+      if (lane == 0) sflag[0] = 1;
+      continue;
+    }
+    tc::fence_after_sync();
+    const uint32_t taddr = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(buf * 2 * kPxCols + half * kPxCols);
+    float res[8];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {  // two components per 16 columns
+      uint32_t r[16];
+      tc::tmem_ld16(taddr + (uint32_t)(16 * q), r);
+      tc::tmem_wait_ld();
+#pragma unroll
+      for (int u = 0; u < 2; ++u) {
+        const int j = 8 * g + 2 * q + u;
+        long long hi = __float2int_rn(__uint_as_float(r[8 * u]));
+        long long lo = __float2int_rn(__uint_as_float(r[8 * u + 4]));
+#pragma unroll
+        for (int k = 1; k < 4; ++k) {
+          hi = hi * 128 + __float2int_rn(__uint_as_float(r[8 * u + k]));
+          lo = lo * 128 + __float2int_rn(__uint_as_float(r[8 * u + 4 + k]));
+        }
+        res[2 * q + u] = 0.f;
+        if (j < d) {
+          const __int128 X = (__int128)hi * ((__int128)1 << 28) + lo;  // sum_k s_k 2^(7 (7 - k))
+          const __int128 M =
+              ((__int128)(long long)__ldg(mfix + 2 * j + 1) << 64) | (unsigned long long)__ldg(mfix + 2 * j);
+          res[2 * q + u] = fixed_to_float(X - M, 49 + __ldg(expo + j));
+        }
+      }
+    }
+    if (x < ncols) {
+      float* dst = out + ((size_t)y * ncols + x) * d + 8 * g;
+      if (vec) {
+        *reinterpret_cast<float4*>(dst) = make_float4(res[0], res[1], res[2], res[3]);
+        *reinterpret_cast<float4*>(dst + 4) = make_float4(res[4], res[5], res[6], res[7]);
+      } else {
+#pragma unroll
+        for (int c = 0; c < 8; ++c)
+          if (8 * g + c < d) dst[c] = res[c];
+      }
+    }
+  }
+  if (sflag[0] && tid == 0) atomicOr(status, DEV_TC_TIMEOUT);
+  // no MMA may still write TMEM when it is freed (after a time-out the next row's may be in flight)
+  for (int b = 0; b < 2; ++b)
+    if ((pending >> b) & 1u) pj_wait(mbar + b, (phase >> b) & 1u);
+  tc::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) tc::tmem_dealloc(tmem, 4 * kPxCols);
+}
+
+static size_t px_smem(int psize) {
+  return (size_t)psize * kPxCols * pr_kr(psize) * 2 + (size_t)(psize + 1) * 2 * pr_pe(psize) * 8 + 16 + 16 + 16 + 64;
+}
+
+bool project_rows_exact_supported(int psize, int c, int ncomp) {
+  return psize >= 1 && psize <= 12 && c >= 1 && c <= 4 && ncomp >= 1 && ncomp <= 32 && px_smem(psize) <= 227 * 1024;
+}
+
+// the exact projection (annf_project) on the tensor cores: digits, expo and mfix as digits_kernel
+// leaves them (8 slices, rw bytes per patch row, W4 words per slice)
+int project_rows_exact(annf_handle* h, const uint8_t* img, int H, int W, int c, int psize, int ncomp,
+                       const int8_t* digits, int rw, int W4, const int* expo, const unsigned long long* mfix,
+                       float* out, cudaStream_t st) {
+  const int kr = pr_kr(psize), ks = kr / 16;
+  const int groups = (ncomp + 7) / 8;
+  const size_t bbytes = (size_t)groups * psize * kPxCols * kr * 2;
+  ANNF_ENSURE(h->pj_buf, bbytes + 256);
+  uint16_t* bmat = h->pj_buf.as<uint16_t>();
+  px_prep_kernel<<<std::max(1, std::min(ceil_div((long long)(bbytes / 2), 256), 256)), 256, 0, st>>>(
+      digits, ncomp, groups, psize, c, rw, W4, kr, bmat);
+  ANNF_CHECK_LAUNCH();
+  // 256 TMEM columns per CTA: the shared memory request keeps at most two CTAs on an SM
+  const size_t smem = std::max(px_smem(psize), (size_t)78 * 1024);
+  ANNF_REQUIRE(smem <= 227 * 1024, "annf_project: tile too large for shared memory");
+  const int ncols = W - psize + 1, nrows = H - psize + 1;
+  const long long blocks = (long long)((ncols + 255) / 256) * ((nrows + kPrRows - 1) / kPrRows) * groups;
+  ANNF_REQUIRE(blocks <= 0x7fffffffLL, "annf_project: image too large");
+  const int vec = (ncomp % 4 == 0 && ((uintptr_t)out & 15) == 0) ? 1 : 0;
+#define ANNF_PX(KS_)                                                                                           \
+  if (ks == KS_) {                                                                                             \
+    ANNF_CUDA_TRY(cudaFuncSetAttribute(project_exact_tc_kernel<KS_>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                                       (int)smem));                                                            \
+    project_exact_tc_kernel<KS_><<<(unsigned)blocks, kPxThreads, smem, st>>>(img, H, W, c, psize, ncomp, groups, \
+                                                                           bmat, expo, mfix, out, vec,         \
+                                                                           h->status.as<unsigned>());          \
+  }
+  ANNF_PX(1) ANNF_PX(2) ANNF_PX(3)
+#undef ANNF_PX
+  ANNF_CHECK_LAUNCH();
+  return ANNF_OK;
 }
 
 bool project_rows_supported(int psize, int c, int ncomp) {

@@ -651,6 +651,156 @@ __global__ void __launch_bounds__(256) exact_scan_kernel(TreeView<T> tv, const T
   }
 }
 
+// ---------------------------------------------------------------------------------------------
+// Exact kNN by marked leaves, for a moderate number of queries (the first row of a pair: 2040
+// queries over 32768 leaves at 2048x2048). A leaf can hold one of a query's exact K nearest only
+// if its box lies within the query's seed distance (the K-th distance inside its natural leaf:
+// the box bound never exceeds the distance of any point inside, in FP32 too, since the bound
+// takes the same rounded steps on smaller differences). So:
+//   1. leaf_mark_kernel: a CTA per (128-query tile, range of leaves) tests the ranges' boxes,
+//      staged in shared memory and read by every thread at once, and writes one bit per
+//      (query, leaf);
+//   2. leaf_chunk_scan_kernel: a warp per (query, chunk of 32*CW leaves) scans the marked leaves
+//      of its chunk with the reference's arithmetic and keeps the chunk's K best keys. Tasks run
+//      chunk-major: warps that run together read the same leaves, which neighbouring pixels of a
+//      row mostly share;
+//   3. exact_merge_kernel: the K smallest keys over a query's chunks.
+// Every key is unique (distance bits, the leaf's depth-first rank for that query, the offset in
+// the leaf), so the K smallest over the marked leaves are the reference's K, found in any order.
+// ---------------------------------------------------------------------------------------------
+constexpr int kMarkThreads = 128;
+constexpr int kMarkStage = 32;       // leaves whose boxes are staged at a time
+constexpr int kChunkCacheLevels = 10;  // node levels the chunk scan keeps in shared memory (8 KB)
+
+template <typename T, int D>
+__global__ void __launch_bounds__(kMarkThreads) leaf_mark_kernel(TreeView<T> tv, const T* __restrict__ Q, int nq,
+                                                                 int K, const typename KeyOps<T>::K* __restrict__ seed_key,
+                                                                 int leaves_per_split, int nwords,
+                                                                 uint32_t* __restrict__ marks) {
+  using Ops = KeyOps<T>;
+  using R = real_traits<T>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int d = D > 0 ? D : tv.d;
+  T* sbox = reinterpret_cast<T*>(smem_raw);  // [kMarkStage][2][d]
+  if (smem_overrun(smem_raw, sbox + kMarkStage * 2 * d, tv.status)) return;
+  const int qi = blockIdx.x * kMarkThreads + threadIdx.x;
+  const bool active = qi < nq;
+  T q[D > 0 ? D : 1];
+  const T* qg = Q + (long long)(active ? qi : 0) * d;
+  if constexpr (D > 0) {
+#pragma unroll
+    for (int j = 0; j < D; ++j) q[j] = qg[j];
+  }
+  const T thr = active ? Ops::dist(seed_key[(long long)qi * K + K - 1]) : T(0);
+  const int nleaves = 1 << tv.depth;
+  const int l0 = blockIdx.y * leaves_per_split, l1 = min(nleaves, l0 + leaves_per_split);
+  for (int s0 = l0; s0 < l1; s0 += kMarkStage) {
+    const int ns = min(kMarkStage, l1 - s0);
+    __syncthreads();
+    for (int e = threadIdx.x; e < ns * 2 * d; e += kMarkThreads) sbox[e] = __ldg(tv.leaf_box + (long long)s0 * 2 * d + e);
+    __syncthreads();
+    uint32_t bits = 0;
+    for (int i = 0; i < ns; ++i) {
+      const T* lo = sbox + i * 2 * d;
+      const T* hi = lo + d;
+      T lb = 0;
+      if constexpr (D > 0) {
+#pragma unroll
+        for (int j = 0; j < D; ++j) {
+          const T g = q[j] < lo[j] ? R::sub(lo[j], q[j]) : (q[j] > hi[j] ? R::sub(q[j], hi[j]) : T(0));
+          lb = R::add(lb, R::mul(g, g));
+        }
+      } else {
+        for (int j = 0; j < d; ++j) {
+          const T qv = qg[j];
+          const T g = qv < lo[j] ? R::sub(lo[j], qv) : (qv > hi[j] ? R::sub(qv, hi[j]) : T(0));
+          lb = R::add(lb, R::mul(g, g));
+        }
+      }
+      bits |= (uint32_t)(!(lb > thr)) << i;
+    }
+    if (active) marks[(long long)qi * nwords + (s0 >> 5)] = bits;
+  }
+}
+
+template <typename T, int D>
+__global__ void __launch_bounds__(256, 3) leaf_chunk_scan_kernel(TreeView<T> tv, const T* __restrict__ Q, int nq, int K,
+                                                              const typename KeyOps<T>::K* __restrict__ seed_key,
+                                                              int nwords, int cw, const uint32_t* __restrict__ marks,
+                                                              typename KeyOps<T>::K* __restrict__ part_key,
+                                                              int* __restrict__ part_pos) {
+  using Ops = KeyOps<T>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  unsigned char* p = smem_raw;
+  NodeCache<T> nc;
+  nc.carve(p, tv.depth, kChunkCacheLevels);
+  const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  T* sq = reinterpret_cast<T*>(p) + wib * kMaxDynD;
+  if (smem_overrun(smem_raw, reinterpret_cast<T*>(p) + (blockDim.x >> 5) * kMaxDynD, tv.status)) return;
+  nc.fill(tv, kChunkCacheLevels);
+  __syncthreads();
+  const int d = tv.d, depth = tv.depth;
+  const int nchunks = (nwords + cw - 1) / cw;
+  const long long ntasks = (long long)nchunks * nq;
+  const long long nw = (long long)gridDim.x * (blockDim.x >> 5);
+  for (long long task = blockIdx.x * (long long)(blockDim.x >> 5) + wib; task < ntasks; task += nw) {
+    const int chunk = (int)(task / nq);
+    const int qi = (int)(task - (long long)chunk * nq);
+    WarpList<T> L;
+    L.init(K, lane);
+    const int w0 = chunk * cw, w1 = min(nwords, w0 + cw);
+    // the chunk's marked words, one per lane
+    const uint32_t myword = (w0 + lane < w1) ? __ldg(marks + (long long)qi * nwords + w0 + lane) : 0u;
+    if (__ballot_sync(kFull, myword != 0u)) {
+      __syncwarp();
+      for (int j = lane; j < d; j += 32) sq[j] = Q[(long long)qi * d + j];
+      __syncwarp();
+      QReg<T, D> qr;
+      if constexpr (D == 0) {
+        qr.v = sq;
+        qr.d = d;
+      } else {
+        qr.load(sq, d);
+      }
+      const T seed = Ops::dist(seed_key[(long long)qi * K + K - 1]);
+      for (int wi = 0; wi < w1 - w0; ++wi) {
+        uint32_t bits = __shfl_sync(kFull, myword, wi);
+        while (bits) {
+          const int leaf = ((w0 + wi) << 5) + __ffs(bits) - 1;
+          bits &= bits - 1;
+          uint32_t rank = 0;  // the leaf's position in this query's depth-first visiting order
+          for (int t = 0; t < depth; ++t) {
+            const int node = (1 << t) - 1 + (leaf >> (depth - t));
+            int ax;
+            T s;
+            nc.get(tv, node, ax, s);
+            rank = (rank << 1) | (uint32_t)(((leaf >> (depth - 1 - t)) & 1) ^ (sq[ax] >= s ? 1 : 0));
+          }
+          const uint32_t hi = rank << tv.leaf_bits;
+          const int beg = __ldg(tv.leaf_begin + leaf), end = __ldg(tv.leaf_begin + leaf + 1);
+          for (int pb = beg; pb < end; pb += 128) {
+            int pp[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) pp[u] = pb + lane + 32 * u;
+            T dd[4];
+            dist4<false>(qr, tv.pts + (long long)min(pp[0], end - 1) * d, tv.pts + (long long)min(pp[1], end - 1) * d,
+                         tv.pts + (long long)min(pp[2], end - 1) * d, tv.pts + (long long)min(pp[3], end - 1) * d, d,
+                         dd);
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+              L.offer(pp[u] < end && !(dd[u] > seed), Ops::make(dd[u], hi | (uint32_t)(pp[u] - beg)), pp[u]);
+          }
+        }
+      }
+    }
+    if (lane < K) {
+      const long long o = ((long long)chunk * nq + qi) * K + lane;
+      part_key[o] = L.key;
+      part_pos[o] = L.pos;
+    }
+  }
+}
+
 // merge the per-split lists: warp per query. mode 0: tree positions to out_pos; mode 1: square
 // rooted distances + original indices (kneighbors)
 template <typename T, int KM>
@@ -794,7 +944,7 @@ __global__ void __launch_bounds__(128, 1) chain_kernel(TreeView<T> tv, const T* 
 // and re-enters with its next slot once extracted, so points met twice are listed twice exactly
 // as the reference's insertion does.
 template <int D, int CPL, int LM>
-__global__ void __launch_bounds__(128, 1) chain_sel_kernel(TreeView<float> tv, const float* __restrict__ Q, int n_rows,
+__global__ void __launch_bounds__(64, 7) chain_sel_kernel(TreeView<float> tv, const float* __restrict__ Q, int n_rows,
                                                             int n_cols, int K, const int2* __restrict__ nat_range,
                                                             const int2* __restrict__ next_range, int* __restrict__ lists) {
   using Ops = KeyOps<float>;
@@ -1071,11 +1221,35 @@ static int exact_box_launch(annf_handle* h, const T* Q, int nq, int K, int mode,
   natural_knn_kernel<T, D, KM><<<(int)std::min<long long>(ceil_div((long long)nq * 32, 256), 64LL * num_sms()), 256, nsm,
                                  st>>>(tv, Q, 0, nq, K, h->nat_pos.as<int>(), h->nat_keys.as<Kt>());
   ANNF_CHECK_LAUNCH();
-  if ((long long)nq * nleaves <= (1LL << 28)) {  // few queries: warp per query over the leaf boxes
-    const size_t ssm = NodeCache<T>::bytes(h->depth) + 8 * kMaxDynD * sizeof(T) + 64;
-    ANNF_CUDA_TRY(cudaFuncSetAttribute(exact_scan_kernel<T, D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ssm));
-    exact_scan_kernel<T, D><<<std::max(1, std::min(ceil_div(nq, 8), 32 * num_sms())), 256, ssm, st>>>(
-        tv, Q, nq, K, h->nat_keys.as<Kt>(), mode, out_pos, out_dist, out_idx);
+  if ((long long)nq * nleaves <= (1LL << 28)) {  // few queries: marked leaves, scanned in chunks
+    if (nq <= 0) return ANNF_OK;
+    const int nwords = ceil_div(nleaves, 32);
+    // chunk width: 2 words (64 leaves), wider when the partial lists would pass 256 MB
+    int cw = 2;
+    while (cw < nwords && (long long)ceil_div(nwords, cw) * nq * K * (long long)(sizeof(Kt) + sizeof(int)) > (256LL << 20))
+      cw *= 2;
+    const int nchunks = ceil_div(nwords, cw);
+    ANNF_ENSURE(h->leaf_marks, (size_t)nq * nwords * sizeof(uint32_t));
+    ANNF_ENSURE(h->part_keys, (size_t)nchunks * nq * K * sizeof(Kt));
+    ANNF_ENSURE(h->part_pos, (size_t)nchunks * nq * K * sizeof(int));
+    const int tiles = ceil_div(nq, kMarkThreads);
+    const int want = std::max(1, (4 * num_sms()) / tiles);
+    const int lps = std::max(32, ceil_div(ceil_div(nleaves, want), 32) * 32);
+    const int nsplit = ceil_div(nleaves, lps);
+    const size_t msm = (size_t)kMarkStage * 2 * h->d * sizeof(T) + 64;
+    ANNF_CUDA_TRY(cudaFuncSetAttribute(leaf_mark_kernel<T, D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)msm));
+    leaf_mark_kernel<T, D><<<dim3(tiles, nsplit), kMarkThreads, msm, st>>>(tv, Q, nq, K, h->nat_keys.as<Kt>(), lps,
+                                                                          nwords, h->leaf_marks.as<uint32_t>());
+    ANNF_CHECK_LAUNCH();
+    const size_t ssm = NodeCache<T>::bytes(h->depth, kChunkCacheLevels) + 8 * kMaxDynD * sizeof(T) + 64;
+    ANNF_CUDA_TRY(cudaFuncSetAttribute(leaf_chunk_scan_kernel<T, D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ssm));
+    const long long ntasks = (long long)nchunks * nq;
+    leaf_chunk_scan_kernel<T, D><<<(int)std::max(1LL, std::min<long long>(ceil_div(ntasks, 8LL), 16LL * num_sms())), 256, ssm, st>>>(
+        tv, Q, nq, K, h->nat_keys.as<Kt>(), nwords, cw, h->leaf_marks.as<uint32_t>(), h->part_keys.as<Kt>(),
+        h->part_pos.as<int>());
+    ANNF_CHECK_LAUNCH();
+    exact_merge_kernel<T, KM><<<ceil_div((long long)nq * 32, 256), 256, 0, st>>>(
+        tv, nq, K, nchunks, h->part_keys.as<Kt>(), h->part_pos.as<int>(), mode, out_pos, out_dist, out_idx);
     ANNF_CHECK_LAUNCH();
     return ANNF_OK;
   }
@@ -1143,8 +1317,12 @@ static int rows_typed(annf_handle* h, const T* ared, int n_rows, int n_cols, int
         const int2* nr = h->nat_pos.as<int2>();
         const int2* xr = h->next_range.as<int2>();
         const bool small_leaf = h->max_leaf <= 64;
+        // two columns per CTA at <= 128 registers: 16 warps per SM, so every column of a 2048-wide
+        // image (2040 warps on 152 SMs) is resident at once -- a column left for a second wave
+        // would double the chain's time
+        const int sblocks = ceil_div((long long)n_cols * 32, 64);
 #define ANNF_CHAIN_SEL(CPLV, LMV) \
-  chain_sel_kernel<D, CPLV, LMV><<<cblocks, 128, 0, st>>>(tv, ared, n_rows, n_cols, K, nr, xr, lists)
+  chain_sel_kernel<D, CPLV, LMV><<<sblocks, 64, 0, st>>>(tv, ared, n_rows, n_cols, K, nr, xr, lists)
         if (K == 1) {
           if (small_leaf) ANNF_CHAIN_SEL(2, 2); else ANNF_CHAIN_SEL(4, 2);
         } else if (K <= 4) {

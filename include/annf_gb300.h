@@ -48,6 +48,11 @@ extern "C" {
 #define ANNF_LEAF_FP16 2  /* the same with FP16 tiles (tighter bound, fewer survivors) */
 #define ANNF_LEAF_FP8 3   /* FP8 (E4M3) hi/lo split tiles with power-of-two scales (wider bound, more survivors) */
 
+/* options (annf_set_option) */
+#define ANNF_OPT_INT_PROJECTION 1 /* 1: annf_project always evaluates the exact integer sums with dp4a
+                                     (default 0: on the tensor cores where the shape allows; the same
+                                     integers, so the same bits) */
+
 typedef struct annf_handle annf_handle;
 
 /* Tree arrays as device pointers (structure-of-arrays form of the reference KD_TREE_RECORD,
@@ -162,11 +167,17 @@ int annf_pca_components(annf_handle* h, int P, int n_components, int iters, doub
 
 /* Project every psize x psize patch of an image onto the components
  * (annfmp/openmp/base.py:193-200: X @ C^T - mean @ C^T in FP64, cast to real_type). The
- * product is evaluated exactly in integer arithmetic on split coefficients, so the result is the
- * FP64 value rounded once. out [(h-psize+1)*(w-psize+1)*n_components], row-major pixels. */
+ * product is evaluated exactly in integer arithmetic on split coefficients (each coefficient as
+ * 8 signed 7-bit digits; the digit sums on the tensor cores for FP32 output of images with at
+ * most 4 channels, else with dp4a), so the result is the FP64 value rounded once.
+ * out [(h-psize+1)*(w-psize+1)*n_components], row-major pixels. */
 int annf_project(annf_handle* h, const uint8_t* img, int hgt, int wid, int channels, int psize,
                  const double* components, const double* mean, int n_components, int real_type,
                  void* out, void* stream);
+
+/* Set a per-handle option (ANNF_OPT_*). No counterpart in the reference: a knob of this
+ * implementation that changes no result. */
+int annf_set_option(annf_handle* h, int option, int value);
 
 /* Approximate counterpart of annf_project for the approximate NNF forms (no reference
  * counterpart): the same patches times the components rounded to FP16, FP32 accumulation on the

@@ -226,6 +226,36 @@ def test_projection_rounds_like_fp64(gpu_lib, oracle_mod, golden, name):
     assert (ulps == 0).mean() >= 0.9999
 
 
+@pytest.mark.parametrize("shape", [(160, 170, 3, 9, 16), (128, 140, 3, 7, 8), (96, 101, 3, 5, 12), (80, 90, 1, 12, 32),
+                                   (70, 77, 4, 3, 5), (64, 66, 2, 6, 20)])
+def test_exact_projection_tensor_cores_equal_dp4a(gpu_lib, shape):
+    """annf_project on the tensor cores (digit-slice sums in FP32 TMEM) and with dp4a (the same
+    sums in int32) give identical bits: every slice sum is an integer below 2^24."""
+    from annfmp_gb300 import _lib
+    from annfmp_gb300._torch import ptr, stream_ptr
+    H, W, C, psize, d = shape
+    rng = np.random.default_rng(H * W + d)
+    dev = torch.device("cuda", 0)
+    P = psize * psize * C
+    comps = rng.standard_normal((d, P))
+    comps /= np.linalg.norm(comps, axis=1, keepdims=True)
+    comps[0, :] = np.abs(comps[0, :])  # a component whose digits are all of one sign
+    img = torch.from_numpy(rng.integers(0, 256, (H, W, C), dtype=np.uint8)).to(dev)
+    img[:8] = 255  # largest products
+    C_ = torch.from_numpy(comps).to(dev)
+    mean = torch.from_numpy(rng.uniform(0, 255, P)).to(dev)
+    outs = []
+    for opt in (0, 1):
+        h = _lib.Handle(0)
+        h.call("annf_set_option", _lib.ANNF_OPT_INT_PROJECTION, opt)
+        out = torch.empty(((H - psize + 1) * (W - psize + 1), d), dtype=torch.float32, device=dev)
+        h.call("annf_project", ptr(img), H, W, C, psize, ptr(C_), ptr(mean), d, _lib.ANNF_REAL_F32, ptr(out),
+               stream_ptr(dev))
+        torch.cuda.synchronize()
+        outs.append(out.cpu().numpy())
+    assert np.array_equal(outs[0].view(np.uint32), outs[1].view(np.uint32))
+
+
 @pytest.mark.parametrize("name", PIPES)
 def test_rows_on_reference_reduced_arrays(gpu_lib, oracle_mod, golden, name):
     """Tree + rows on the reference's reduced patches (numpy FP64 transform of the reference's
