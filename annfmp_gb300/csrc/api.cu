@@ -292,7 +292,7 @@ int annf_pca_covariance(annf_handle* h, const uint8_t* img_a, int ha, int wa, co
 int annf_pca_components(annf_handle* h, int P, int n_components, int iters, double* components_out, void* stream) {
   ANNF_API_HANDLE(h);
   ANNF_REQUIRE(components_out, "annf_pca_components: NULL argument");
-  ANNF_REQUIRE(iters >= 0 && iters <= 100, "annf_pca_components: iters out of range");
+  ANNF_REQUIRE(iters >= -1 && iters <= 100, "annf_pca_components: iters out of range");
   return pca_components(h, P, n_components, iters, components_out, static_cast<cudaStream_t>(stream));
 }
 

@@ -57,6 +57,7 @@ enum : unsigned {
   DEV_LIST_OVERFLOW = 4u,
   DEV_SMEM_CARVE = 8u,  // a kernel's shared-memory carve exceeded its launch allocation
   DEV_TC_TIMEOUT = 16u, // a tensor-core kernel's bounded wait on its MMA ran out
+  DEV_GRID_TIMEOUT = 32u, // a bounded grid-wide barrier gave up waiting for the other CTAs
 };
 
 __device__ __forceinline__ unsigned dyn_smem_size() {

@@ -699,6 +699,280 @@ __global__ void rr_comps_kernel(int P, int b, const float* __restrict__ Q, const
     for (int i = threadIdx.x; i < P; i += blockDim.x) out[i] = -out[i];
 }
 
+// ---------------------------------------------------------------------------------------------
+// Exact-grade leading eigenvectors (the drop-in form): subspace iteration in FP64 on all SMs.
+// A block of b = min(40, P) vectors from a fixed pseudo-random start; kExactSteps times
+//   Z = C Q                      (FP64, every output split over four threads),
+//   G = Z^T Z                    (FP64, a warp per entry),
+//   Q = Z D R^-1                 (D = diag(G)^-1/2, R the Cholesky factor of D G D),
+// then W = C Q, G = Q^T Q, T = Q^T W for the FP64 Rayleigh-Ritz step (rr_solve_kernel, as the
+// approximate form) and the components Q x. Every CTA factors the small scaled Gram matrix in
+// FP32 itself (it is well conditioned: at most ~3e5 in the first steps from a random start, then
+// near 1); Q = Z (D R^-1) is formed in FP64, so the span of Z is kept to FP64 rounding whatever
+// R's accuracy, and the final Rayleigh-Ritz step absorbs Q's departure from orthonormality. A
+// pivot that vanishes drops its column (a covariance of lower rank than the block). The error of
+// component j after s steps shrinks like (lambda_{b+1} / lambda_j)^s: 40 steps reach FP64 accuracy
+// for ratios up to ~0.45 (measured on the workloads' covariances: 0.10 to 0.29, 12 to 24 steps).
+// The phases are separated by a bounded grid barrier; the launch is cooperative, so every CTA is
+// resident and the barrier cannot wait on a CTA that has not started.
+// ---------------------------------------------------------------------------------------------
+constexpr int kExactThreads = 256;
+constexpr int kExactSteps = 40;
+constexpr long long kBarrierPolls = 20000000LL;  // ~1 s of polls at 64 ns: then give up, flag it
+
+__device__ __forceinline__ unsigned ld_volatile_u32(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.volatile.global.u32 %0, [%1];" : "=r"(v) : "l"(p));
+  return v;
+}
+
+// bar[0] counts arrivals, bar[1] is the generation (both zero at launch). Returns false once a
+// wait ran out (the status bit is then set and later barriers do not wait).
+__device__ bool grid_barrier(unsigned* bar, unsigned nblocks, unsigned& gen, unsigned* status) {
+  __shared__ int s_ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    s_ok = 1;
+    const unsigned target = gen + 1;
+    __threadfence();
+    if (atomicAdd(bar, 1u) == nblocks - 1) {
+      atomicExch(bar, 0u);
+      __threadfence();
+      atomicExch(bar + 1, target);
+    } else if (!(ld_volatile_u32(status) & DEV_GRID_TIMEOUT)) {
+      long long polls = 0;
+      while (ld_volatile_u32(bar + 1) != target) {
+        if (++polls > kBarrierPolls) {
+          atomicOr(status, DEV_GRID_TIMEOUT);
+          s_ok = 0;
+          break;
+        }
+        __nanosleep(64);
+      }
+    } else {
+      s_ok = 0;
+    }
+    __threadfence();
+  }
+  gen += 1;
+  __syncthreads();
+  return s_ok != 0;
+}
+
+__device__ __forceinline__ double hash_unit(uint32_t i, uint32_t j) {  // deterministic start in [-1, 1)
+  const uint32_t h = mix32(i * 0x9E3779B1u + mix32(j + 0x632BE5ABu));
+  return (double)h * (2.0 / 4294967296.0) - 1.0;
+}
+
+// Z[i][j] = sum_k C[i][k] Q[k][j] (Q, Z: [P][b] row-major), four threads per output
+__device__ void exact_cq(const double* __restrict__ C, int P, int b, const double* __restrict__ Q, double* __restrict__ Z) {
+  const long long total = (long long)P * b * 4;
+  const long long nthr = (long long)gridDim.x * blockDim.x;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < ((total + 31) / 32) * 32; t += nthr) {
+    const long long o = t >> 2;
+    const int part = (int)(t & 3);
+    double s = 0.0;
+    if (o < (long long)P * b) {
+      const int i = (int)(o / b), j = (int)(o - (long long)i * b);
+      const double* c = C + (size_t)i * P;
+      for (int k = part; k < P; k += 4) s = fma(c[k], Q[(size_t)k * b + j], s);
+    }
+    s += __shfl_xor_sync(0xffffffffu, s, 1);
+    s += __shfl_xor_sync(0xffffffffu, s, 2);
+    if (part == 0 && o < (long long)P * b) Z[o] = s;
+  }
+}
+
+// out[i][j] = out[j][i] = sum_k X[k][i] Y[k][j] (b x b), a warp per upper-triangular entry
+__device__ void exact_gram(int P, int b, const double* __restrict__ X, const double* __restrict__ Y,
+                           double* __restrict__ out) {
+  const int lane = threadIdx.x & 31;
+  const int nent = b * (b + 1) / 2;
+  const int nw = gridDim.x * (blockDim.x >> 5);
+  for (int e = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); e < nent; e += nw) {
+    int i = 0, rem = e;  // entry e -> (i, j), i <= j, rows of the upper triangle in order
+    while (rem >= b - i) {
+      rem -= b - i;
+      ++i;
+    }
+    const int j = i + rem;
+    double s = 0.0;
+    for (int k = lane; k < P; k += 32) s = fma(X[(size_t)k * b + i], Y[(size_t)k * b + j], s);
+    s = warp_sum_d(s);
+    if (lane == 0) {
+      out[i * b + j] = s;
+      out[j * b + i] = s;
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kExactThreads, 1) subspace_exact_kernel(const double* __restrict__ C, int P, int b,
+                                                                          int steps, double* __restrict__ Q,
+                                                                          double* __restrict__ Z,
+                                                                          double* __restrict__ Gw,
+                                                                          double* __restrict__ Gout,
+                                                                          double* __restrict__ Tout, unsigned* bar,
+                                                                          unsigned* status) {
+  __shared__ float sG[kMaxBlock * kMaxBlock];   // scaled Gram, then R (upper)
+  __shared__ float sRi[kMaxBlock * kMaxBlock];  // R^-1 (upper)
+  __shared__ double sM[kMaxBlock * kMaxBlock];  // D R^-1 in FP64
+  __shared__ double sD[kMaxBlock];
+  __shared__ float s_piv;
+  __shared__ int s_keep[kMaxBlock];
+  const int tid = threadIdx.x, nt = blockDim.x;
+  unsigned gen = 0;
+  const long long nthr = (long long)gridDim.x * nt;
+  for (long long o = blockIdx.x * (long long)nt + tid; o < (long long)P * b; o += nthr)
+    Q[o] = hash_unit((uint32_t)(o / b), (uint32_t)(o % b));
+  bool ok = grid_barrier(bar, gridDim.x, gen, status);
+  for (int step = 0; step < steps && ok; ++step) {
+    exact_cq(C, P, b, Q, Z);
+    ok = grid_barrier(bar, gridDim.x, gen, status);
+    if (!ok) break;
+    exact_gram(P, b, Z, Z, Gw);
+    ok = grid_barrier(bar, gridDim.x, gen, status);
+    if (!ok) break;
+    // every CTA: D, the Cholesky factor of D G D (FP32, right-looking), R^-1, M = D R^-1
+    for (int e = tid; e < b; e += nt) {
+      const double g = Gw[e * b + e];
+      sD[e] = g > 0.0 ? 1.0 / sqrt(g) : 0.0;
+    }
+    __syncthreads();
+    for (int e = tid; e < b * b; e += nt) {
+      const int i = e / b, j = e - i * b;
+      sG[e] = (float)(Gw[e] * sD[i] * sD[j]);
+    }
+    __syncthreads();
+    for (int k = 0; k < b; ++k) {
+      if (tid == 0) {
+        const float piv = sG[k * b + k];
+        const bool keep = piv > 1e-7f;  // a column (nearly) in the span of the earlier ones: drop it
+        s_keep[k] = keep;
+        s_piv = keep ? sqrtf(piv) : 0.f;
+      }
+      __syncthreads();
+      const float r = s_piv;
+      for (int j = k + tid; j < b; j += nt) sG[k * b + j] = r > 0.f ? sG[k * b + j] / r : 0.f;
+      __syncthreads();
+      const int tw = b - k - 1;
+      for (int e = tid; e < tw * tw; e += nt) {
+        const int i = k + 1 + e / tw, j = k + 1 + e % tw;
+        if (j >= i) sG[i * b + j] -= sG[k * b + i] * sG[k * b + j];
+      }
+      __syncthreads();
+    }
+    for (int j = tid; j < b; j += nt) {  // column j of R^-1 by back-substitution (dropped pivots: zero)
+      for (int i = b - 1; i >= 0; --i) {
+        float v = i == j ? 1.f : 0.f;
+        if (i > j || !s_keep[i]) {
+          sRi[i * b + j] = 0.f;
+          continue;
+        }
+        for (int k = i + 1; k <= j; ++k) v -= sG[i * b + k] * sRi[k * b + j];
+        sRi[i * b + j] = v / sG[i * b + i];
+      }
+    }
+    __syncthreads();
+    for (int e = tid; e < b * b; e += nt) sM[e] = sD[e / b] * (double)sRi[e];
+    __syncthreads();
+    for (long long o = blockIdx.x * (long long)nt + tid; o < (long long)P * b; o += nthr) {
+      const int i = (int)(o / b), j = (int)(o - (long long)i * b);
+      double s = 0.0;
+      for (int k = 0; k <= j; ++k) s = fma(Z[(size_t)i * b + k], sM[k * b + j], s);
+      Q[o] = s;
+    }
+    ok = grid_barrier(bar, gridDim.x, gen, status);
+  }
+  if (!ok) return;
+  exact_cq(C, P, b, Q, Z);  // W = C Q
+  if (!grid_barrier(bar, gridDim.x, gen, status)) return;
+  exact_gram(P, b, Q, Q, Gout);
+  exact_gram(P, b, Q, Z, Tout);  // Q^T W: symmetric up to rounding (rr_solve_kernel averages it)
+}
+
+// components [ncomp][P] = Q x (Q [P][b] FP64), signed so that the largest |entry| (first on
+// ties) is positive
+__global__ void rr_comps_exact_kernel(int P, int b, const double* __restrict__ Q, const double* __restrict__ X,
+                                      double* __restrict__ comps) {
+  const int c = blockIdx.x;
+  const double* x = X + (size_t)c * b;
+  double* out = comps + (size_t)c * P;
+  __shared__ double sbest[256];
+  __shared__ int sidx[256];
+  double best = -1.0;
+  int bi = 0x7fffffff;
+  for (int i = threadIdx.x; i < P; i += blockDim.x) {
+    double s = 0.0;
+    for (int k = 0; k < b; ++k) s = fma(Q[(size_t)i * b + k], x[k], s);
+    out[i] = s;
+    const double a = fabs(s);
+    if (a > best || (a == best && i < bi)) {
+      best = a;
+      bi = i;
+    }
+  }
+  sbest[threadIdx.x] = best;
+  sidx[threadIdx.x] = bi;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o; o >>= 1) {
+    if ((int)threadIdx.x < o) {
+      const double ob = sbest[threadIdx.x + o];
+      const int oi = sidx[threadIdx.x + o];
+      if (ob > sbest[threadIdx.x] || (ob == sbest[threadIdx.x] && oi < sidx[threadIdx.x])) {
+        sbest[threadIdx.x] = ob;
+        sidx[threadIdx.x] = oi;
+      }
+    }
+    __syncthreads();
+  }
+  const double piv = sidx[0] < P ? out[sidx[0]] : 0.0;
+  __syncthreads();
+  if (piv < 0)
+    for (int i = threadIdx.x; i < P; i += blockDim.x) out[i] = -out[i];
+}
+
+int num_sms();
+
+int exact_block_max() { return kMaxBlock; }
+
+// C [P*P] FP64 covariance (device) -> comps [ncomp*P] FP64, exact-grade (FP64 iteration)
+int eig_top_exact(annf_handle* h, const double* C, int P, int ncomp, double* comps, cudaStream_t st) {
+  const int b = std::min(kMaxBlock, P);
+  ANNF_REQUIRE(ncomp >= 1 && ncomp <= b, "exact subspace eigensolver: n_components above the block size");
+  const size_t f64 = (2 * (size_t)P * b + 3 * (size_t)b * b + (size_t)ncomp * b) * sizeof(double);
+  ANNF_ENSURE(h->eig_ws, f64 + 256);
+  double* Q = h->eig_ws.as<double>();
+  double* Z = Q + (size_t)P * b;
+  double* Gw = Z + (size_t)P * b;
+  double* G = Gw + (size_t)b * b;
+  double* T = G + (size_t)b * b;
+  double* X = T + (size_t)b * b;
+  unsigned* bar = reinterpret_cast<unsigned*>(reinterpret_cast<unsigned char*>(h->eig_ws.p) + ((f64 + 15) & ~size_t(15)));
+  ANNF_CUDA_TRY(cudaMemsetAsync(bar, 0, 2 * sizeof(unsigned), st));
+  int per_sm = 0;
+  ANNF_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, subspace_exact_kernel, kExactThreads, 0));
+  ANNF_REQUIRE(per_sm >= 1, "exact subspace eigensolver: kernel does not fit an SM");
+  const int grid = num_sms();  // one CTA per SM: all resident (cooperative launch)
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(kExactThreads);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  ANNF_CUDA_TRY(cudaLaunchKernelEx(&cfg, subspace_exact_kernel, C, P, b, kExactSteps, Q, Z, Gw, G, T, bar,
+                                   h->status.as<unsigned>()));
+  count_launch();
+  rr_solve_kernel<<<1, kRrThreads, 0, st>>>(b, ncomp, G, T, X, nullptr);
+  ANNF_CHECK_LAUNCH();
+  rr_comps_exact_kernel<<<ncomp, 256, 0, st>>>(P, b, Q, X, comps);
+  ANNF_CHECK_LAUNCH();
+  return ANNF_OK;
+}
+
 // block size for n components: b >= ncomp + max(8, ncomp / 2), a multiple of 8
 int subspace_block(int P, int ncomp) {
   int b = ncomp + std::max(8, ncomp / 2);

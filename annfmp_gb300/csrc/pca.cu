@@ -358,6 +358,8 @@ int subspace_block(int P, int ncomp);
 bool gram_tc_supported(int F, int ns_pad);
 int gram_tc(const uint8_t* XT, int F, int ns_pad, unsigned long long* G, unsigned* status, cudaStream_t st);
 int eig_top_subspace(annf_handle* h, const double* C, int P, int ncomp, int iters, double* comps, cudaStream_t st);
+int eig_top_exact(annf_handle* h, const double* C, int P, int ncomp, double* comps, cudaStream_t st);
+int exact_block_max();
 bool project_rows_exact_supported(int psize, int c, int ncomp);
 int project_rows_exact(annf_handle* h, const uint8_t* img, int H, int W, int c, int psize, int ncomp,
                        const int8_t* digits, int rw, int W4, const int* expo, const unsigned long long* mfix,
@@ -414,13 +416,20 @@ int pca_covariance(annf_handle* h, const uint8_t* img_a, int ha, int wa, const i
   return ANNF_OK;
 }
 
-// the leading ncomp components of the covariance in h->cov (P x P): solver 0 = full FP64 eigh
-// (cuSOLVER), solver > 0 = subspace iteration with that many steps and an FP64 Rayleigh-Ritz step
+// the leading ncomp components of the covariance in h->cov (P x P): solver 0 = FP64 subspace
+// iteration on all SMs with an FP64 Rayleigh-Ritz step (the drop-in form's result; the library
+// solver above 40 components), solver < 0 = full FP64 eigh (cuSOLVER), solver > 0 = FP32
+// subspace iteration with that many steps and an FP64 Rayleigh-Ritz step (approximate forms)
 int pca_components(annf_handle* h, int P, int ncomp, int solver, double* comps, cudaStream_t st) {
   ANNF_REQUIRE(h->cov_p == P && P >= 1, "annf_pca_components: no covariance of this size on the handle");
   ANNF_REQUIRE(ncomp >= 1 && ncomp <= P, "annf_pca_fit: n_components out of range");
   if (solver > 0 && subspace_block(P, ncomp) > 0) {  // leading components only (approximate forms)
     int rc = eig_top_subspace(h, h->cov.as<double>(), P, ncomp, solver, comps, st);
+    prof_mark(h, "pca_eigh", st);
+    return rc;
+  }
+  if (solver == 0 && ncomp <= std::min(exact_block_max(), P)) {
+    int rc = eig_top_exact(h, h->cov.as<double>(), P, ncomp, comps, st);
     prof_mark(h, "pca_eigh", st);
     return rc;
   }

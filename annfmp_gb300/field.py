@@ -84,17 +84,19 @@ class ANNFieldPropKDTreeGB300:
         every candidate checked by exact raw-patch distance); ``iters`` propagation passes of the
         parallel form; ``proposal`` an object with ``propose(A, B, psize) -> int32 [n_A, P]`` B
         indices (e.g. ``annfmp_gb300.proposal.ProposalNet``) feeding the parallel form;
-        ``pca_solver`` "exact" (full FP64 eigendecomposition, the reference's result) or
-        "subspace" (leading components only: FP32 subspace iteration, ``pca_iters`` steps, with
-        an FP64 Rayleigh-Ritz step); None picks "exact" for the plain form, "subspace" otherwise;
+        ``pca_solver`` "exact" (the reference's result: the leading eigenvectors in FP64, by
+        subspace iteration over all SMs and an FP64 Rayleigh-Ritz step), "full" (the full FP64
+        eigendecomposition by cuSOLVER) or "subspace" (FP32 subspace iteration, ``pca_iters``
+        steps, with an FP64 Rayleigh-Ritz step); None picks "exact" for the plain form,
+        "subspace" otherwise;
         ``leaf_precision`` of the parallel form's natural-leaf distances: "bf16" (tensor-core tiles,
         exact FP32 re-rank of the survivors of a proven BF16 error bound; the default) or "fp32";
         ``projection`` "exact" (the FP64 result rounded once, the reference's) or "fp16" (FP16
         components on the tensor cores, FP32 sums); None picks "exact" for the plain form, "fp16"
         otherwise when the shapes allow it; ``graph``: repeated fits with unchanged shapes and
-        parameters replay one captured CUDA graph of the whole NNF ("auto": the parallel form;
-        False: never; the plain form is never captured, its cuSOLVER eigensolver sizes its
-        workspace on the host)."""
+        parameters replay one captured CUDA graph of the whole NNF ("auto": every form; False:
+        never; not with pca_solver "full", whose library solver sizes its workspace on the
+        host)."""
         self.graph = graph
         self._graph = None       # captured state: key, epoch, graph, static inputs, outputs
         self._graph_seen = None  # key of the last eager fit (capture happens on the second call)
@@ -143,10 +145,11 @@ class ANNFieldPropKDTreeGB300:
 
     # -- CUDA graph replay --------------------------------------------------------------------------
     def _graph_wanted(self):
+        full = self.pca_solver == "full"
         if self.graph == "auto":
-            return self.form != "plain"
-        if self.graph and self.form == "plain":
-            raise ValueError("the plain form cannot be captured into a CUDA graph (its eigensolver sizes "
+            return not full
+        if self.graph and full:
+            raise ValueError("pca_solver 'full' cannot be captured into a CUDA graph (its library solver sizes "
                              "its workspace on the host)")
         return bool(self.graph)
 
@@ -310,16 +313,17 @@ class ANNFieldPropKDTreeGB300:
         if self.form not in self.FORMS:
             raise ValueError("form must be one of {}".format(self.FORMS))
         solver = self.pca_solver or ("exact" if self.form == "plain" else "subspace")
-        if solver == "exact":
-            h.call("annf_pca_fit", ptr(A), ha, wa, ptr(pos_a), pos_a.shape[0], ptr(B), hb, wb, ptr(pos_b),
-                   pos_b.shape[0], c, p, d, ptr(self.components_), ptr(self.mean_), st)
+        if solver in ("exact", "full"):
+            h.call("annf_pca_covariance", ptr(A), ha, wa, ptr(pos_a), pos_a.shape[0], ptr(B), hb, wb, ptr(pos_b),
+                   pos_b.shape[0], c, p, ptr(self.mean_), st)
+            h.call("annf_pca_components", P, d, 0 if solver == "exact" else -1, ptr(self.components_), st)
         elif solver == "subspace":
             h.call("annf_pca_covariance", ptr(A), ha, wa, ptr(pos_a), pos_a.shape[0], ptr(B), hb, wb, ptr(pos_b),
                    pos_b.shape[0], c, p, ptr(self.mean_), st)
             start_proposals()
             h.call("annf_pca_components", P, d, int(self.pca_iters), ptr(self.components_), st)
         else:
-            raise ValueError("pca_solver must be 'exact' or 'subspace'")
+            raise ValueError("pca_solver must be 'exact', 'full' or 'subspace'")
         if side is None:
             start_proposals()  # (the exact solver: after the whole fit)
         ev["t1"].record()

@@ -135,8 +135,10 @@ int annf_process_rows_img(annf_handle* h, int* final_idx, const uint8_t* img_a, 
 
 /* PCA fit on sampled patches of both images (annfmp/openmp/base.py:168-191 with scikit-learn's
  * covariance_eigh solver): Gram matrix accumulated exactly, covariance finished in FP64 in the
- * solver's own operation order, FP64 symmetric eigendecomposition on the GPU, components sorted
- * by decreasing eigenvalue with the sign convention "largest |entry| positive".
+ * solver's own operation order, then the leading eigenvectors in FP64 on the GPU (subspace
+ * iteration over all SMs on a block of min(40, P) vectors and an FP64 Rayleigh-Ritz step; the
+ * library's full eigendecomposition beyond 40 components), sorted by decreasing eigenvalue with
+ * the sign convention "largest |entry| positive".
  *   pos_a [n_a*2], pos_b [n_b*2]: (row, col) of the sampled patches (int32, device)
  *   components_out [n_components*P] FP64, mean_out [P] FP64 (device) */
 int annf_pca_fit(annf_handle* h, const uint8_t* img_a, int ha, int wa, const int* pos_a, int n_a,
@@ -157,7 +159,8 @@ int annf_pca_fit_subspace(annf_handle* h, const uint8_t* img_a, int ha, int wa, 
 /* The two halves of annf_pca_fit / annf_pca_fit_subspace, for callers that want work of their own
  * between them (no reference counterpart): annf_pca_covariance forms the covariance of the sampled
  * patches (kept on the handle) and writes the mean; annf_pca_components then writes the leading
- * components (iters 0: full FP64 eigendecomposition; iters > 0: subspace iteration with that many
+ * components (iters 0: the drop-in result, as annf_pca_fit; iters -1: the full FP64
+ * eigendecomposition by the library solver; iters > 0: FP32 subspace iteration with that many
  * steps and an FP64 Rayleigh-Ritz step). P = psize * psize * channels. */
 int annf_pca_covariance(annf_handle* h, const uint8_t* img_a, int ha, int wa, const int* pos_a, int n_a,
                         const uint8_t* img_b, int hb, int wb, const int* pos_b, int n_b, int channels,

@@ -39,6 +39,71 @@ def test_subspace_pca_captures_leading_variance(gpu_lib, oracle_mod, golden, nam
     assert np.all(V[np.arange(d), j] > 0)
 
 
+@pytest.mark.parametrize("name", PIPES)
+def test_exact_solver_matches_numpy_eigh(gpu_lib, oracle_mod, golden, name):
+    """The drop-in PCA's FP64 subspace solver (annf_pca_components iters 0) and the library's full
+    eigendecomposition (iters -1) give the same components as numpy's eigh of the same
+    covariance, to 1e-10, with the same sign convention."""
+    import torch
+    from annfmp_gb300 import _lib
+    from annfmp_gb300._torch import ptr, stream_ptr
+    O = oracle_mod
+    z = golden(name)
+    k, psize, d, n_subset, leaf, prop, sel, seed = (int(v) for v in z["params"])
+    a, b = z["a"], z["b"]
+    C = _covariance(O, a, b, psize, n_subset, seed)
+    w, V = np.linalg.eigh(C)
+    V = V[:, ::-1][:, :d].T
+    j = np.argmax(np.abs(V), axis=1)
+    V = V * np.sign(V[np.arange(d), j])[:, None]
+    dev = torch.device("cuda", 0)
+    m = int(n_subset / 2)
+    pa = O.sample_positions(a.shape[0] - psize + 1, a.shape[1] - psize + 1, m, seed)
+    pb = O.sample_positions(b.shape[0] - psize + 1, b.shape[1] - psize + 1, m, seed + 1)
+    pos_a = torch.from_numpy(np.stack(pa, 1).astype(np.int32)).to(dev)
+    pos_b = torch.from_numpy(np.stack(pb, 1).astype(np.int32)).to(dev)
+    A, B = torch.from_numpy(a).to(dev), torch.from_numpy(b).to(dev)
+    P = psize * psize * a.shape[2]
+    for iters in (0, -1):
+        h = _lib.Handle(0)
+        mean = torch.empty(P, dtype=torch.float64, device=dev)
+        comps = torch.empty((d, P), dtype=torch.float64, device=dev)
+        h.call("annf_pca_covariance", ptr(A), a.shape[0], a.shape[1], ptr(pos_a), m, ptr(B), b.shape[0], b.shape[1],
+               ptr(pos_b), m, a.shape[2], psize, ptr(mean), stream_ptr(dev))
+        h.call("annf_pca_components", P, d, iters, ptr(comps), stream_ptr(dev))
+        got = comps.cpu().numpy()
+        assert np.abs(got - V).max() < 1e-10, (iters, np.abs(got - V).max())
+        assert np.allclose(got, z["components"], rtol=0, atol=1e-10)
+
+
+@pytest.mark.parametrize("psize,d", [(7, 8), (5, 12), (3, 8)])
+def test_exact_solver_rank_deficient_covariance(gpu_lib, oracle_mod, psize, d):
+    """The FP64 subspace solver on covariances of lower rank than its block (images u[x] + v[y]:
+    2 psize - 1 directions): the dependent columns are dropped, and the leading components are
+    orthonormal and capture the variance of numpy's eigh of the same covariance."""
+    from annfmp_gb300 import ANNFieldPropKDTreeGB300
+    O = oracle_mod
+    rng = np.random.default_rng(psize * 10 + d)
+    imgs = []
+    for _ in range(2):
+        u, v = rng.integers(0, 128, 96), rng.integers(0, 128, 96)
+        imgs.append(np.repeat((v[:, None] + u[None, :]).astype(np.uint8)[:, :, None], 3, axis=2))
+    a, b = imgs
+    n_subset = 3000
+    C = _covariance(O, a, b, psize, n_subset, 0)
+    assert np.linalg.matrix_rank(C) < min(40, C.shape[0])
+    m = ANNFieldPropKDTreeGB300(n_neighbors=1, psize=psize, dim_reduced=d, n_subset=n_subset, leaf_size=16, seed=0,
+                                verbose=0, graph=False)
+    m.fit(a, b)
+    Vg = m.components_.cpu().numpy()
+    assert np.all(np.isfinite(Vg))
+    w = np.linalg.eigvalsh(C)[::-1]
+    ritz = np.einsum("ij,jk,ik->i", Vg, C, Vg)
+    r = min(d, int(np.linalg.matrix_rank(C)))
+    assert np.abs(Vg[:r] @ Vg[:r].T - np.eye(r)).max() < 1e-9
+    assert ritz[:r].sum() >= w[:r].sum() * (1 - 1e-10)
+
+
 def test_subspace_pca_rank_deficient_covariance(gpu_lib, oracle_mod):
     """A covariance of lower rank than the iteration's block (B = d + max(8, d/2) = 16 vectors for
     d = 8): images whose pixels are u[x] + v[y] in all three channels give 7x7 patches spanning

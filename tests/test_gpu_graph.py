@@ -78,3 +78,19 @@ def test_graph_dropped_on_shape_change_and_buffer_growth(gpu_lib):
 def _eager_iters(a, b, iters):
     from annfmp_gb300 import ANNFieldPropKDTreeGB300
     return ANNFieldPropKDTreeGB300(form="parallel", iters=iters, graph=False, **KW).fit(a, b)
+
+
+def test_plain_form_graph_replay_equals_eager(gpu_lib):
+    """The plain form (the drop-in) is captured too: its FP64 eigensolver needs no host-side
+    workspace query. Replays on new images give the eager NNF, bit for bit."""
+    from annfmp_gb300 import ANNFieldPropKDTreeGB300, gen
+    kw = dict(KW, n_subset=4000)
+    pairs = [gen.pair_flow(s, 144, magnitude=6.0, sigma=24.0) for s in (41, 42, 43)]
+    refs = [ANNFieldPropKDTreeGB300(graph=False, **kw).fit(a, b) for a, b in pairs]
+    m = ANNFieldPropKDTreeGB300(**kw)  # form "plain", graph "auto"
+    assert np.array_equal(m.fit(*pairs[0]), refs[0]) and m._graph is None
+    assert np.array_equal(m.fit(*pairs[0]), refs[0]) and m._graph is not None
+    graph = m._graph["graph"]
+    for (a, b), ref in zip(pairs[1:], refs[1:]):
+        assert np.array_equal(m.fit(a, b), ref)
+        assert m._graph["graph"] is graph

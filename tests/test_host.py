@@ -61,15 +61,14 @@ def test_no_cuda_device_is_an_error(built_lib):
     assert _lib.load().annf_create(ctypes.byref(h), 0) == _lib.ANNF_ERR_CUDA
 
 
-def test_plain_form_is_never_captured():
-    """graph=True asks for a CUDA graph; the plain form's eigensolver cannot be captured."""
+def test_library_eigensolver_is_never_captured():
+    """graph=True asks for a CUDA graph; the library eigensolver (pca_solver "full") sizes its
+    workspace on the host and cannot be captured (the default FP64 solver can)."""
     from annfmp_gb300 import ANNFieldPropKDTreeGB300
     img = np.zeros((20, 20, 3), np.uint8)
-    with pytest.raises(ValueError, match="plain form"):
-        ANNFieldPropKDTreeGB300(verbose=0, graph=True).fit(img, img)
-    assert ANNFieldPropKDTreeGB300(form="parallel")._graph_wanted()
-    assert not ANNFieldPropKDTreeGB300()._graph_wanted()
-    assert not ANNFieldPropKDTreeGB300(form="parallel", graph=False)._graph_wanted()
+    with pytest.raises(ValueError, match="full"):
+        ANNFieldPropKDTreeGB300(verbose=0, graph=True, pca_solver="full").fit(img, img)
+    assert ANNFieldPropKDTreeGB300(verbose=0)._graph_wanted()
 
 
 def test_missing_library_fails_loudly(tmp_path):
