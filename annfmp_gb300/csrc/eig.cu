@@ -701,15 +701,13 @@ __global__ void rr_comps_kernel(int P, int b, const float* __restrict__ Q, const
 
 // ---------------------------------------------------------------------------------------------
 // Exact-grade leading eigenvectors (the drop-in form): subspace iteration in FP64 on all SMs.
-// A block of b = min(40, P) vectors from a fixed pseudo-random start; kExactSteps times
-//   Z = C Q                      (FP64, every output split over four threads),
-//   G = Z^T Z                    (FP64, a warp per entry),
-//   Q = Z D R^-1                 (D = diag(G)^-1/2, R the Cholesky factor of D G D),
-// then W = C Q, G = Q^T Q, T = Q^T W for the FP64 Rayleigh-Ritz step (rr_solve_kernel, as the
-// approximate form) and the components Q x. Every CTA factors the small scaled Gram matrix in
-// FP32 itself (it is well conditioned: at most ~3e5 in the first steps from a random start, then
-// near 1); Q = Z (D R^-1) is formed in FP64, so the span of Z is kept to FP64 rounding whatever
-// R's accuracy, and the final Rayleigh-Ritz step absorbs Q's departure from orthonormality. A
+// A block of b = min(40, P) vectors from a fixed pseudo-random start; kExactSteps power steps
+// Z <- C Z M, where M (exact_factor) makes Z M nearly orthonormal: D (I + E)^-1/2 to second
+// order once the scaled Gram matrix I + E is near the identity, an FP32 Cholesky factor in the
+// first steps from the random start (condition up to ~3e5). Every CTA forms the small M itself;
+// the products with M are FP64, so the span is kept to FP64 rounding whatever M's accuracy, and
+// the final FP64 Rayleigh-Ritz step (rr_solve_kernel, as the approximate form: G = Q^T Q,
+// T = Q^T C Q) absorbs Q's departure from orthonormality; the components are Q x. A Cholesky
 // pivot that vanishes drops its column (a covariance of lower rank than the block). The error of
 // component j after s steps shrinks like (lambda_{b+1} / lambda_j)^s: 40 steps reach FP64 accuracy
 // for ratios up to ~0.45 (measured on the workloads' covariances: 0.10 to 0.29, 12 to 24 steps).
@@ -717,7 +715,8 @@ __global__ void rr_comps_kernel(int P, int b, const float* __restrict__ Q, const
 // resident and the barrier cannot wait on a CTA that has not started.
 // ---------------------------------------------------------------------------------------------
 constexpr int kExactThreads = 256;
-constexpr int kExactSteps = 40;
+constexpr int kExactSteps = 40;    // power steps in all
+constexpr int kExactSteps32 = 24;  // of which the first run their products with C in FP32
 constexpr long long kBarrierPolls = 20000000LL;  // ~1 s of polls at 64 ns: then give up, flag it
 
 __device__ __forceinline__ unsigned ld_volatile_u32(const unsigned* p) {
@@ -764,28 +763,57 @@ __device__ __forceinline__ double hash_unit(uint32_t i, uint32_t j) {  // determ
   return (double)h * (2.0 / 4294967296.0) - 1.0;
 }
 
-// Z[i][j] = sum_k C[i][k] Q[k][j] (Q, Z: [P][b] row-major), four threads per output
-__device__ void exact_cq(const double* __restrict__ C, int P, int b, const double* __restrict__ Q, double* __restrict__ Z) {
-  const long long total = (long long)P * b * 4;
-  const long long nthr = (long long)gridDim.x * blockDim.x;
-  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < ((total + 31) / 32) * 32; t += nthr) {
-    const long long o = t >> 2;
-    const int part = (int)(t & 3);
-    double s = 0.0;
-    if (o < (long long)P * b) {
-      const int i = (int)(o / b), j = (int)(o - (long long)i * b);
-      const double* c = C + (size_t)i * P;
-      for (int k = part; k < P; k += 4) s = fma(c[k], Q[(size_t)k * b + j], s);
-    }
-    s += __shfl_xor_sync(0xffffffffu, s, 1);
-    s += __shfl_xor_sync(0xffffffffu, s, 2);
-    if (part == 0 && o < (long long)P * b) Z[o] = s;
+// Work split of a [P][b] product over the grid: CTA c owns outputs [c * opb, (c + 1) * opb), each
+// shared by tpo threads (a power of two) that split the sum and meet in shuffles.
+struct ExactSplit {
+  int opb, tpo;
+  __device__ ExactSplit(int P, int b) {
+    opb = (P * b + gridDim.x - 1) / gridDim.x;
+    tpo = 1;
+    while (tpo < 8 && 2 * tpo * opb <= (int)blockDim.x) tpo *= 2;
   }
+};
+
+// stage X [P][b] (FP64, global) into shared memory, 16 bytes per load
+__device__ void exact_stage(const double* __restrict__ X, int n, double* sX) {
+  const int n2 = n >> 1;
+  const double2* x2 = reinterpret_cast<const double2*>(X);
+  double2* s2 = reinterpret_cast<double2*>(sX);
+  for (int e = threadIdx.x; e < n2; e += blockDim.x) s2[e] = x2[e];
+  if ((n & 1) && threadIdx.x == 0) sX[n - 1] = X[n - 1];
 }
 
-// out[i][j] = out[j][i] = sum_k X[k][i] Y[k][j] (b x b), a warp per upper-triangular entry
-__device__ void exact_gram(int P, int b, const double* __restrict__ X, const double* __restrict__ Y,
-                           double* __restrict__ out) {
+// Y[i][j] = sum_k C[i][k] Z[k][j] for this CTA's outputs, Z staged in shared memory; R: the
+// arithmetic (float in the first power steps, double in the last)
+template <typename R>
+__device__ void exact_cq(const double* __restrict__ C, int P, int b, const double* sZ, double* __restrict__ Y) {
+  const ExactSplit sp(P, b);
+  const int slot = threadIdx.x / sp.tpo, part = threadIdx.x - slot * sp.tpo;
+  const long long o = (long long)blockIdx.x * sp.opb + slot;
+  const bool live = slot < sp.opb && o < (long long)P * b;
+  R s = 0;
+  if (live) {  // four independent partial sums: the FMA latency is hidden within the thread
+    const int i = (int)(o / b), j = (int)(o - (long long)i * b);
+    const double* c = C + (size_t)i * P;
+    R a0 = 0, a1 = 0, a2 = 0, a3 = 0;
+    const int st = sp.tpo;
+    int k = part;
+    for (; k + 3 * st < P; k += 4 * st) {
+      a0 = fma((R)__ldg(c + k), (R)sZ[k * b + j], a0);
+      a1 = fma((R)__ldg(c + k + st), (R)sZ[(k + st) * b + j], a1);
+      a2 = fma((R)__ldg(c + k + 2 * st), (R)sZ[(k + 2 * st) * b + j], a2);
+      a3 = fma((R)__ldg(c + k + 3 * st), (R)sZ[(k + 3 * st) * b + j], a3);
+    }
+    for (; k < P; k += st) a0 = fma((R)__ldg(c + k), (R)sZ[k * b + j], a0);
+    s = (a0 + a1) + (a2 + a3);
+  }
+  for (int m = 1; m < sp.tpo; m <<= 1) s += __shfl_xor_sync(0xffffffffu, s, m);
+  if (live && part == 0) Y[o] = (double)s;
+}
+
+// out[i][j] = out[j][i] = sum_k X[k][i] Y[k][j] (b x b), a warp per upper-triangular entry, X and
+// Y in shared memory
+__device__ void exact_gram(int P, int b, const double* sX, const double* sY, double* __restrict__ out) {
   const int lane = threadIdx.x & 31;
   const int nent = b * (b + 1) / 2;
   const int nw = gridDim.x * (blockDim.x >> 5);
@@ -797,7 +825,7 @@ __device__ void exact_gram(int P, int b, const double* __restrict__ X, const dou
     }
     const int j = i + rem;
     double s = 0.0;
-    for (int k = lane; k < P; k += 32) s = fma(X[(size_t)k * b + i], Y[(size_t)k * b + j], s);
+    for (int k = lane; k < P; k += 32) s = fma(sX[k * b + i], sY[k * b + j], s);
     s = warp_sum_d(s);
     if (lane == 0) {
       out[i * b + j] = s;
@@ -806,88 +834,187 @@ __device__ void exact_gram(int P, int b, const double* __restrict__ X, const dou
   }
 }
 
+// The factor that makes Z's columns (nearly) orthonormal, from the Gram matrix G = Z^T Z (FP64,
+// global). Every CTA computes the same factor (same inputs, same thread mapping, same
+// operations). With D = diag(G)^-1/2 and E = D G D - I: when max |E| <= kNsLimit, the full
+// matrix M = D (I - E/2 + 3 E^2 / 8) (the binomial series of (I + E)^-1/2 to second order; returns
+// true); otherwise the upper Cholesky factor R of I + E in FP32 (in sE, columns whose pivot
+// vanishes dropped: their row of R is zero), applied as Z D R^-1 by exact_apply (returns
+// false). The factor's accuracy does not matter: the span of the product is that of Z.
+constexpr float kNsLimit = 0.25f;
+
+__device__ bool exact_factor(const double* __restrict__ Gw, int b, double* sM, double* sD, float* sE, int* s_keep,
+                             unsigned* s_emax) {
+  const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
+  if (tid == 0) *s_emax = 0u;
+  for (int e = tid; e < b; e += nt) {
+    const double g = Gw[e * b + e];
+    sD[e] = g > 0.0 ? 1.0 / sqrt(g) : 0.0;
+  }
+  __syncthreads();
+  float emax = 0.f;
+  for (int i = warp; i < b; i += nw)
+    for (int j = lane; j < b; j += 32) {
+      const bool live = sD[i] > 0.0 && sD[j] > 0.0;
+      const float v = live ? (float)(Gw[i * b + j] * sD[i] * sD[j]) - (i == j ? 1.f : 0.f) : 0.f;
+      sE[i * b + j] = v;
+      emax = fmaxf(emax, fabsf(v));
+    }
+  atomicMax(s_emax, __float_as_uint(emax));  // non-negative floats order like their bits
+  __syncthreads();
+  if (__uint_as_float(*s_emax) <= kNsLimit) {
+    for (int i = warp; i < b; i += nw)
+      for (int j = lane; j < b; j += 32) {
+        float e2 = 0.f;
+        for (int k = 0; k < b; ++k) e2 = fmaf(sE[i * b + k], sE[k * b + j], e2);
+        const float f = (i == j ? 1.f : 0.f) - 0.5f * sE[i * b + j] + 0.375f * e2;
+        sM[i * b + j] = sD[i] * (double)f;
+      }
+    __syncthreads();
+    return true;
+  }
+  // Cholesky of A = I + E, right-looking, one barrier per column: step k reads row k and updates
+  // rows k+1.. (A_ij -= A_ki A_kj / A_kk for k < i <= j, warps over rows, lanes over columns);
+  // row k of R is then row k of A over sqrt(A_kk)
+  for (int e = tid; e < b; e += nt) sE[e * b + e] += 1.f;
+  __syncthreads();
+  for (int k = 0; k < b; ++k) {
+    const float piv = sE[k * b + k];
+    const bool keep = sD[k] > 0.0 && piv > 1e-7f;  // (nearly) in the span of the earlier columns: drop
+    if (tid == 0) s_keep[k] = keep;
+    if (keep) {
+      const float inv = 1.f / piv;
+      for (int i = k + 1 + warp; i < b; i += nw) {
+        const float aki = sE[k * b + i] * inv;
+        for (int j = i + lane; j < b; j += 32) sE[i * b + j] -= aki * sE[k * b + j];
+      }
+    }
+    __syncthreads();
+  }
+  for (int k = warp; k < b; k += nw) {
+    const float piv = sE[k * b + k];
+    const float r = s_keep[k] ? rsqrtf(piv) : 0.f;
+    for (int j = k + lane; j < b; j += 32) sE[k * b + j] *= r;
+  }
+  __syncthreads();
+  return false;
+}
+
+// out = in M (ns) or out = (in D) R^-1 (R in sE), in arithmetic R (float in the first power steps,
+// double in the last); this CTA's rows, a warp per row
+template <typename R>
+__device__ void exact_apply(int P, int b, const double* __restrict__ in, bool ns, const double* sM, const double* sD,
+                            const float* sE, const int* s_keep, double* __restrict__ out) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const int rpb = (P + gridDim.x - 1) / gridDim.x;
+  const int r0 = blockIdx.x * rpb, r1 = min(P, r0 + rpb);
+  for (int i = r0 + warp; i < r1; i += nw) {
+    const double* y = in + (size_t)i * b;
+    double* x = out + (size_t)i * b;
+    const R y0 = lane < b ? (R)y[lane] : R(0), y1 = lane + 32 < b ? (R)y[lane + 32] : R(0);
+    if (ns) {
+      R s0 = 0, s1 = 0, t0 = 0, t1 = 0;  // two chains per output
+      for (int k = 0; k < b; k += 2) {
+        const R yk = __shfl_sync(0xffffffffu, k < 32 ? y0 : y1, k & 31);
+        const bool k1 = k + 1 < b;
+        const R yk1 = __shfl_sync(0xffffffffu, (k + 1) < 32 ? y0 : y1, (k + 1) & 31);
+        if (lane < b) {
+          s0 = fma(yk, (R)sM[k * b + lane], s0);
+          if (k1) t0 = fma(yk1, (R)sM[(k + 1) * b + lane], t0);
+        }
+        if (lane + 32 < b) {
+          s1 = fma(yk, (R)sM[k * b + lane + 32], s1);
+          if (k1) t1 = fma(yk1, (R)sM[(k + 1) * b + lane + 32], t1);
+        }
+      }
+      if (lane < b) x[lane] = (double)(s0 + t0);
+      if (lane + 32 < b) x[lane + 32] = (double)(s1 + t1);
+      continue;
+    }
+    // x R = y D by forward substitution: x_j = (y_j D_j - sum_{k<j} x_k R_kj) / R_jj; lane k
+    // holds x_k (and x_{k+32}), the sum is a warp reduction
+    R x0 = 0, x1 = 0;
+    for (int j = 0; j < b; ++j) {
+      R part = 0;
+      if (lane < j) part = x0 * (R)sE[lane * b + j];
+      if (lane + 32 < j) part = fma(x1, (R)sE[(lane + 32) * b + j], part);
+#pragma unroll
+      for (int o = 16; o; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+      const R yj = __shfl_sync(0xffffffffu, j < 32 ? y0 : y1, j & 31);
+      const R rjj = (R)sE[j * b + j];
+      const R xj = (s_keep[j] && rjj > R(0)) ? (yj * (R)sD[j] - part) / rjj : R(0);
+      if (lane == (j & 31)) {
+        if (j < 32) x0 = xj; else x1 = xj;
+      }
+    }
+    if (lane < b) x[lane] = (double)x0;
+    if (lane + 32 < b) x[lane + 32] = (double)x1;
+  }
+}
+
+// Z_0 = C Q_0; then per step s: Y = C Z_s and G = Z_s^T Z_s (one phase: both read Z_s only,
+// staged in shared memory), M_s from G, Z_{s+1} = Y M_s = C (Z_s M_s). The last step writes
+// Q = Z M (the basis) and W = Y M = C Q instead, and the Rayleigh-Ritz Gram matrices
+// G = Q^T Q, T = Q^T W follow. The first steps32 products with C run in FP32 arithmetic (they
+// only have to find the subspace to FP32 accuracy), the rest in FP64.
 __global__ void __launch_bounds__(kExactThreads, 1) subspace_exact_kernel(const double* __restrict__ C, int P, int b,
-                                                                          int steps, double* __restrict__ Q,
+                                                                          int steps, int steps32,
                                                                           double* __restrict__ Z,
+                                                                          double* __restrict__ Y,
+                                                                          double* __restrict__ Q,
+                                                                          double* __restrict__ W,
                                                                           double* __restrict__ Gw,
                                                                           double* __restrict__ Gout,
                                                                           double* __restrict__ Tout, unsigned* bar,
                                                                           unsigned* status) {
-  __shared__ float sG[kMaxBlock * kMaxBlock];   // scaled Gram, then R (upper)
-  __shared__ float sRi[kMaxBlock * kMaxBlock];  // R^-1 (upper)
-  __shared__ double sM[kMaxBlock * kMaxBlock];  // D R^-1 in FP64
+  __shared__ float sE[kMaxBlock * kMaxBlock];
+  __shared__ double sM[kMaxBlock * kMaxBlock];
   __shared__ double sD[kMaxBlock];
-  __shared__ float s_piv;
   __shared__ int s_keep[kMaxBlock];
+  __shared__ unsigned s_emax;
+  extern __shared__ __align__(16) double dyn[];
+  const size_t pb2 = ((size_t)P * b + 1) & ~size_t(1);  // 16-byte aligned regions
+  double* sZ = dyn;                                      // [P][b]: the block being multiplied
+  double* sRows = dyn + pb2;                             // this CTA's rows for exact_apply, or W
   const int tid = threadIdx.x, nt = blockDim.x;
   unsigned gen = 0;
   const long long nthr = (long long)gridDim.x * nt;
   for (long long o = blockIdx.x * (long long)nt + tid; o < (long long)P * b; o += nthr)
     Q[o] = hash_unit((uint32_t)(o / b), (uint32_t)(o % b));
-  bool ok = grid_barrier(bar, gridDim.x, gen, status);
-  for (int step = 0; step < steps && ok; ++step) {
-    exact_cq(C, P, b, Q, Z);
-    ok = grid_barrier(bar, gridDim.x, gen, status);
-    if (!ok) break;
-    exact_gram(P, b, Z, Z, Gw);
-    ok = grid_barrier(bar, gridDim.x, gen, status);
-    if (!ok) break;
-    // every CTA: D, the Cholesky factor of D G D (FP32, right-looking), R^-1, M = D R^-1
-    for (int e = tid; e < b; e += nt) {
-      const double g = Gw[e * b + e];
-      sD[e] = g > 0.0 ? 1.0 / sqrt(g) : 0.0;
-    }
-    __syncthreads();
-    for (int e = tid; e < b * b; e += nt) {
-      const int i = e / b, j = e - i * b;
-      sG[e] = (float)(Gw[e] * sD[i] * sD[j]);
-    }
-    __syncthreads();
-    for (int k = 0; k < b; ++k) {
-      if (tid == 0) {
-        const float piv = sG[k * b + k];
-        const bool keep = piv > 1e-7f;  // a column (nearly) in the span of the earlier ones: drop it
-        s_keep[k] = keep;
-        s_piv = keep ? sqrtf(piv) : 0.f;
-      }
-      __syncthreads();
-      const float r = s_piv;
-      for (int j = k + tid; j < b; j += nt) sG[k * b + j] = r > 0.f ? sG[k * b + j] / r : 0.f;
-      __syncthreads();
-      const int tw = b - k - 1;
-      for (int e = tid; e < tw * tw; e += nt) {
-        const int i = k + 1 + e / tw, j = k + 1 + e % tw;
-        if (j >= i) sG[i * b + j] -= sG[k * b + i] * sG[k * b + j];
-      }
-      __syncthreads();
-    }
-    for (int j = tid; j < b; j += nt) {  // column j of R^-1 by back-substitution (dropped pivots: zero)
-      for (int i = b - 1; i >= 0; --i) {
-        float v = i == j ? 1.f : 0.f;
-        if (i > j || !s_keep[i]) {
-          sRi[i * b + j] = 0.f;
-          continue;
-        }
-        for (int k = i + 1; k <= j; ++k) v -= sG[i * b + k] * sRi[k * b + j];
-        sRi[i * b + j] = v / sG[i * b + i];
-      }
-    }
-    __syncthreads();
-    for (int e = tid; e < b * b; e += nt) sM[e] = sD[e / b] * (double)sRi[e];
-    __syncthreads();
-    for (long long o = blockIdx.x * (long long)nt + tid; o < (long long)P * b; o += nthr) {
-      const int i = (int)(o / b), j = (int)(o - (long long)i * b);
-      double s = 0.0;
-      for (int k = 0; k <= j; ++k) s = fma(Z[(size_t)i * b + k], sM[k * b + j], s);
-      Q[o] = s;
-    }
-    ok = grid_barrier(bar, gridDim.x, gen, status);
-  }
-  if (!ok) return;
-  exact_cq(C, P, b, Q, Z);  // W = C Q
   if (!grid_barrier(bar, gridDim.x, gen, status)) return;
-  exact_gram(P, b, Q, Q, Gout);
-  exact_gram(P, b, Q, Z, Tout);  // Q^T W: symmetric up to rounding (rr_solve_kernel averages it)
+  exact_stage(Q, P * b, sZ);
+  __syncthreads();
+  exact_cq<float>(C, P, b, sZ, Z);
+  if (!grid_barrier(bar, gridDim.x, gen, status)) return;
+  for (int step = 0; step < steps; ++step) {
+    exact_stage(Z, P * b, sZ);
+    __syncthreads();
+    exact_gram(P, b, sZ, sZ, Gw);
+    if (step < steps32) {
+      exact_cq<float>(C, P, b, sZ, Y);
+    } else {
+      exact_cq<double>(C, P, b, sZ, Y);
+    }
+    if (!grid_barrier(bar, gridDim.x, gen, status)) return;
+    const bool ns = exact_factor(Gw, b, sM, sD, sE, s_keep, &s_emax);
+    if (step + 1 < steps) {
+      if (step < steps32) {
+        exact_apply<float>(P, b, Y, ns, sM, sD, sE, s_keep, Z);
+      } else {
+        exact_apply<double>(P, b, Y, ns, sM, sD, sE, s_keep, Z);
+      }
+    } else {
+      exact_apply<double>(P, b, Z, ns, sM, sD, sE, s_keep, Q);
+      exact_apply<double>(P, b, Y, ns, sM, sD, sE, s_keep, W);
+    }
+    if (!grid_barrier(bar, gridDim.x, gen, status)) return;
+  }
+  exact_stage(Q, P * b, sZ);
+  __syncthreads();
+  exact_gram(P, b, sZ, sZ, Gout);
+  exact_stage(W, P * b, sRows);  // (the rows region has room for a whole block: see the host)
+  __syncthreads();
+  exact_gram(P, b, sZ, sRows, Tout);  // Q^T W: symmetric up to rounding (rr_solve_kernel averages it)
 }
 
 // components [ncomp][P] = Q x (Q [P][b] FP64), signed so that the largest |entry| (first on
@@ -933,38 +1060,50 @@ __global__ void rr_comps_exact_kernel(int P, int b, const double* __restrict__ Q
 
 int num_sms();
 
-int exact_block_max() { return kMaxBlock; }
+// the FP64 subspace solver stages two [P][b] blocks in shared memory
+bool exact_supported(int P, int ncomp) {
+  const int b = std::min(kMaxBlock, P);
+  return ncomp >= 1 && ncomp <= b && 2 * ((size_t)P * b + 2) * sizeof(double) <= 196 * 1024;
+}
 
 // C [P*P] FP64 covariance (device) -> comps [ncomp*P] FP64, exact-grade (FP64 iteration)
 int eig_top_exact(annf_handle* h, const double* C, int P, int ncomp, double* comps, cudaStream_t st) {
   const int b = std::min(kMaxBlock, P);
   ANNF_REQUIRE(ncomp >= 1 && ncomp <= b, "exact subspace eigensolver: n_components above the block size");
-  const size_t f64 = (2 * (size_t)P * b + 3 * (size_t)b * b + (size_t)ncomp * b) * sizeof(double);
+  ANNF_REQUIRE(exact_supported(P, ncomp), "exact subspace eigensolver: unsupported size");
+  const size_t pb2 = ((size_t)P * b + 1) & ~size_t(1);  // every block 16-byte aligned (staged as double2)
+  const size_t f64 = (4 * pb2 + 3 * (size_t)b * b + (size_t)ncomp * b) * sizeof(double);
   ANNF_ENSURE(h->eig_ws, f64 + 256);
   double* Q = h->eig_ws.as<double>();
-  double* Z = Q + (size_t)P * b;
-  double* Gw = Z + (size_t)P * b;
+  double* Z = Q + pb2;
+  double* Y = Z + pb2;
+  double* Wm = Y + pb2;
+  double* Gw = Wm + pb2;
   double* G = Gw + (size_t)b * b;
   double* T = G + (size_t)b * b;
   double* X = T + (size_t)b * b;
   unsigned* bar = reinterpret_cast<unsigned*>(reinterpret_cast<unsigned char*>(h->eig_ws.p) + ((f64 + 15) & ~size_t(15)));
   ANNF_CUDA_TRY(cudaMemsetAsync(bar, 0, 2 * sizeof(unsigned), st));
+  // two staged [P][b] blocks (the block being multiplied; W, or a CTA's rows of Y) in dynamic
+  // shared memory beside the 26 KB of static scratch
+  const size_t smem = 2 * (pb2 + 2) * sizeof(double);
+  ANNF_CUDA_TRY(cudaFuncSetAttribute(subspace_exact_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int per_sm = 0;
-  ANNF_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, subspace_exact_kernel, kExactThreads, 0));
+  ANNF_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, subspace_exact_kernel, kExactThreads, smem));
   ANNF_REQUIRE(per_sm >= 1, "exact subspace eigensolver: kernel does not fit an SM");
   const int grid = num_sms();  // one CTA per SM: all resident (cooperative launch)
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(grid);
   cfg.blockDim = dim3(kExactThreads);
-  cfg.dynamicSmemBytes = 0;
+  cfg.dynamicSmemBytes = smem;
   cfg.stream = st;
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeCooperative;
   attr[0].val.cooperative = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  ANNF_CUDA_TRY(cudaLaunchKernelEx(&cfg, subspace_exact_kernel, C, P, b, kExactSteps, Q, Z, Gw, G, T, bar,
-                                   h->status.as<unsigned>()));
+  ANNF_CUDA_TRY(cudaLaunchKernelEx(&cfg, subspace_exact_kernel, C, P, b, kExactSteps, kExactSteps32, Z, Y, Q, Wm, Gw,
+                                   G, T, bar, h->status.as<unsigned>()));
   count_launch();
   rr_solve_kernel<<<1, kRrThreads, 0, st>>>(b, ncomp, G, T, X, nullptr);
   ANNF_CHECK_LAUNCH();

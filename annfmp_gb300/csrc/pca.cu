@@ -359,7 +359,7 @@ bool gram_tc_supported(int F, int ns_pad);
 int gram_tc(const uint8_t* XT, int F, int ns_pad, unsigned long long* G, unsigned* status, cudaStream_t st);
 int eig_top_subspace(annf_handle* h, const double* C, int P, int ncomp, int iters, double* comps, cudaStream_t st);
 int eig_top_exact(annf_handle* h, const double* C, int P, int ncomp, double* comps, cudaStream_t st);
-int exact_block_max();
+bool exact_supported(int P, int ncomp);
 bool project_rows_exact_supported(int psize, int c, int ncomp);
 int project_rows_exact(annf_handle* h, const uint8_t* img, int H, int W, int c, int psize, int ncomp,
                        const int8_t* digits, int rw, int W4, const int* expo, const unsigned long long* mfix,
@@ -428,7 +428,7 @@ int pca_components(annf_handle* h, int P, int ncomp, int solver, double* comps, 
     prof_mark(h, "pca_eigh", st);
     return rc;
   }
-  if (solver == 0 && ncomp <= std::min(exact_block_max(), P)) {
+  if (solver == 0 && exact_supported(P, ncomp)) {
     int rc = eig_top_exact(h, h->cov.as<double>(), P, ncomp, comps, st);
     prof_mark(h, "pca_eigh", st);
     return rc;
