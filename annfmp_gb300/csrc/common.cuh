@@ -88,6 +88,33 @@ template <> struct real_traits<float> {
   __device__ static float add(float a, float b) { return __fadd_rn(a, b); }
   __device__ static float sqrt_(float a) { return __fsqrt_rn(a); }
 };
+// Two IEEE round-to-nearest FP32 operations in one instruction (sm_100 and later): each half
+// rounds exactly like __fsub_rn / __fmul_rn, so a distance formed with these keeps its bits.
+__device__ __forceinline__ float2 sub2_rn(float2 a, float2 b) {
+  unsigned long long r;
+  asm("sub.rn.f32x2 %0, %1, %2;"
+      : "=l"(r)
+      : "l"(((unsigned long long)__float_as_uint(a.y) << 32) | __float_as_uint(a.x)),
+        "l"(((unsigned long long)__float_as_uint(b.y) << 32) | __float_as_uint(b.x)));
+  return make_float2(__uint_as_float((unsigned)r), __uint_as_float((unsigned)(r >> 32)));
+}
+__device__ __forceinline__ float2 sq2_rn(float2 t) {  // (t.x * t.x, t.y * t.y)
+  unsigned long long r;
+  const unsigned long long v = ((unsigned long long)__float_as_uint(t.y) << 32) | __float_as_uint(t.x);
+  asm("mul.rn.f32x2 %0, %1, %1;" : "=l"(r) : "l"(v));
+  return make_float2(__uint_as_float((unsigned)r), __uint_as_float((unsigned)(r >> 32)));
+}
+// acc + (w.x - q0)^2 + (w.y - q1)^2 + (w.z - q2)^2 + (w.w - q3)^2, summed in that order with
+// every step rounded (the reference's order, no contraction): differences and squares pairwise
+__device__ __forceinline__ float dist_step4(float acc, float4 w, float q0, float q1, float q2, float q3) {
+  const float2 a = sq2_rn(sub2_rn(make_float2(w.x, w.y), make_float2(q0, q1)));
+  const float2 b = sq2_rn(sub2_rn(make_float2(w.z, w.w), make_float2(q2, q3)));
+  acc = __fadd_rn(acc, a.x);
+  acc = __fadd_rn(acc, a.y);
+  acc = __fadd_rn(acc, b.x);
+  return __fadd_rn(acc, b.y);
+}
+
 template <> struct real_traits<double> {
   static constexpr double big() { return DBL_MAX; }
   __device__ static double sub(double a, double b) { return __dsub_rn(a, b); }

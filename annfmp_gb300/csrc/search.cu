@@ -178,14 +178,8 @@ struct QReg {
     if constexpr (sizeof(T) == 4 && D % 4 == 0) {
       const float4* p4 = reinterpret_cast<const float4*>(p);
 #pragma unroll
-      for (int j = 0; j < D / 4; ++j) {
-        const float4 w = __ldg(p4 + j);
-        float t;
-        t = R::sub(w.x, v[4 * j + 0]); acc = R::add(acc, R::mul(t, t));
-        t = R::sub(w.y, v[4 * j + 1]); acc = R::add(acc, R::mul(t, t));
-        t = R::sub(w.z, v[4 * j + 2]); acc = R::add(acc, R::mul(t, t));
-        t = R::sub(w.w, v[4 * j + 3]); acc = R::add(acc, R::mul(t, t));
-      }
+      for (int j = 0; j < D / 4; ++j)
+        acc = dist_step4(acc, __ldg(p4 + j), v[4 * j + 0], v[4 * j + 1], v[4 * j + 2], v[4 * j + 3]);
     } else {
 #pragma unroll
       for (int j = 0; j < D; ++j) {
@@ -233,13 +227,8 @@ __device__ __forceinline__ void dist4(const QReg<T, D>& q, const T* p0, const T*
       for (int u = 0; u < 4; ++u)
         w[u] = kSmem ? reinterpret_cast<const float4*>(p[u])[j] : __ldg(reinterpret_cast<const float4*>(p[u]) + j);
 #pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        float t;
-        t = R::sub(w[u].x, q.v[4 * j + 0]); acc[u] = R::add(acc[u], R::mul(t, t));
-        t = R::sub(w[u].y, q.v[4 * j + 1]); acc[u] = R::add(acc[u], R::mul(t, t));
-        t = R::sub(w[u].z, q.v[4 * j + 2]); acc[u] = R::add(acc[u], R::mul(t, t));
-        t = R::sub(w[u].w, q.v[4 * j + 3]); acc[u] = R::add(acc[u], R::mul(t, t));
-      }
+      for (int u = 0; u < 4; ++u)
+        acc[u] = dist_step4(acc[u], w[u], q.v[4 * j + 0], q.v[4 * j + 1], q.v[4 * j + 2], q.v[4 * j + 3]);
     }
   } else {
     const int dd = D > 0 ? D : d;
@@ -268,13 +257,8 @@ __device__ __forceinline__ void distN(const QReg<T, D>& q, const T* const (&p)[N
 #pragma unroll
       for (int u = 0; u < N; ++u) w[u] = __ldg(reinterpret_cast<const float4*>(p[u]) + j);
 #pragma unroll
-      for (int u = 0; u < N; ++u) {
-        float t;
-        t = R::sub(w[u].x, q.v[4 * j + 0]); acc[u] = R::add(acc[u], R::mul(t, t));
-        t = R::sub(w[u].y, q.v[4 * j + 1]); acc[u] = R::add(acc[u], R::mul(t, t));
-        t = R::sub(w[u].z, q.v[4 * j + 2]); acc[u] = R::add(acc[u], R::mul(t, t));
-        t = R::sub(w[u].w, q.v[4 * j + 3]); acc[u] = R::add(acc[u], R::mul(t, t));
-      }
+      for (int u = 0; u < N; ++u)
+        acc[u] = dist_step4(acc[u], w[u], q.v[4 * j + 0], q.v[4 * j + 1], q.v[4 * j + 2], q.v[4 * j + 3]);
     }
   } else {
 #pragma unroll
