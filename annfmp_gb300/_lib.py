@@ -58,6 +58,15 @@ class TreeView(ctypes.Structure):
     ]
 
 
+class OclTreeView(ctypes.Structure):
+    _fields_ = [
+        ("m", ctypes.c_int), ("d", ctypes.c_int), ("height", ctypes.c_int), ("n_nodes", ctypes.c_int),
+        ("points_per_leaf", ctypes.c_int), ("m_padded", ctypes.c_int),
+        ("points", ctypes.c_void_p), ("indir", ctypes.c_void_p), ("node_dim", ctypes.c_void_p),
+        ("node_val", ctypes.c_void_p), ("node_same_dim_ancestor", ctypes.c_void_p), ("orig2leaf", ctypes.c_void_p),
+    ]
+
+
 # every exported symbol and its signature: (restype, argtypes)
 _vp, _i, _ll, _u = ctypes.c_void_p, ctypes.c_int, ctypes.c_longlong, ctypes.c_uint
 SIGNATURES = {
@@ -77,6 +86,9 @@ SIGNATURES = {
     "annf_project": (_i, [_vp, _vp, _i, _i, _i, _i, _vp, _vp, _i, _i, _vp, _vp]),
     "annf_device_status": (_i, [_vp, _vp, ctypes.POINTER(_u)]),
     "annf_set_option": (_i, [_vp, _i, _i]),
+    "annf_ocl_build_tree": (_i, [_vp, _vp, _i, _i, _i, _vp]),
+    "annf_ocl_tree_get": (_i, [_vp, ctypes.POINTER(OclTreeView)]),
+    "annf_ocl_rows": (_i, [_vp, _vp, _vp, _i, _i, _vp, _i, _i, _i, _i, _vp, _i, _i, _vp, _vp, _vp, _vp]),
     "annf_parallel_nnf": (_i, [_vp, _vp, _vp, _i, _i, _vp, _i, _i, _i, _i, _vp, _i, _vp, _i, _i, _u, _i, _i, _i, _vp,
                                _vp]),
     "annf_parallel_nnf_seeded": (_i, [_vp, _vp, _vp, _i, _i, _vp, _i, _i, _i, _i, _vp, _i, _vp, _i, _u, _i, _i, _i,

@@ -2,12 +2,15 @@
 
 The reference selects its backend with a string in ``fit`` (annfmp/base.py:72-133); the GB300
 backend is one more branch of that switch, with the same constructor parameters.
+``algorithm="openclopt"`` runs the reference GPU backend's algorithm (annfmp/base.py:100-114) on
+this library's kernels (``ANNFieldPropKDTreeOpenCLOPTGB300``).
 """
 from __future__ import annotations
 
 from .field import ANNFieldPropKDTreeGB300
+from .openclopt import ANNFieldPropKDTreeOpenCLOPTGB300
 
-ALGORITHMS = ["gb300"]
+ALGORITHMS = ["gb300", "openclopt"]
 
 
 class ANNField:
@@ -39,6 +42,12 @@ class ANNField:
     def fit(self, image_a, image_b):
         if self.algorithm not in ALGORITHMS:
             raise Exception("Unknown algorithm '{}'!".format(self.algorithm))
+        if self.algorithm == "openclopt":
+            self._model = ANNFieldPropKDTreeOpenCLOPTGB300(
+                n_neighbors=self.n_neighbors, psize=self.psize, dim_reduced=self.dim_reduced,
+                n_subset=self.n_subset, leaf_size=self.leaf_size, n_jobs=self.n_jobs,
+                select_best_nn=self.select_best_nn, verbose=self.verbose, seed=self.seed)
+            return self._model.fit(image_a, image_b)
         self._model = ANNFieldPropKDTreeGB300(
             n_neighbors=self.n_neighbors, psize=self.psize, dim_reduced=self.dim_reduced, n_subset=self.n_subset,
             leaf_size=self.leaf_size, n_jobs=self.n_jobs, propagate=self.propagate,

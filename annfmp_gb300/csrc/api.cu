@@ -35,6 +35,10 @@ int fast_search(annf_handle* h, const uint8_t* img_a, int ha, int wa, const uint
 int seed_matches(const uint8_t* img_a, int ha, int wa, const uint8_t* img_b, int hb, int wb, int c, int psize,
                  const int* cand, int n_cand, int* seed_out, cudaStream_t st);
 bool leaf_tc_supported(const annf_handle* h, int K);
+int ocl_build_tree(annf_handle* h, const float* X, int m, int d, int leaf_size, cudaStream_t st);
+int ocl_rows(annf_handle* h, int* final_idx, const uint8_t* img_a, int ha, int wa, const uint8_t* img_b, int hb,
+             int wb, int ch, int psize, const float* ared, int n_rows, int n_cols, int* knn_out, float* knn_sqdist_out,
+             float* dist_out, cudaStream_t st);
 int natural_knn_tc(annf_handle* h, const float* Q, long long nq, int K, int prec, int* out_pos, cudaStream_t st);
 int tc_tile(const uint16_t* A, const uint16_t* B, int N, int K, float* D, unsigned* status, cudaStream_t st);
 int cnn_input(const uint8_t* A, const uint8_t* B, int H, int W, void* X, cudaStream_t st);
@@ -132,7 +136,9 @@ void annf_destroy(annf_handle* h) {
                     &h->sel_rank, &h->sel_nlt, &h->sel_neq, &h->blk_lt, &h->blk_eq, &h->off_lt, &h->off_eq,
                     &h->eqpos, &h->nat_keys, &h->nat_pos, &h->lists, &h->next_range, &h->part_keys,
                     &h->part_pos, &h->fast_buf, &h->fast_nat, &h->tc_buf, &h->pj_buf, &h->gram, &h->colsum, &h->subset_t, &h->cov, &h->eigval, &h->digits,
-                    &h->meanproj, &h->solver_ws, &h->solver_info, &h->eig_ws, &h->status};
+                    &h->meanproj, &h->solver_ws, &h->solver_info, &h->eig_ws, &h->status, &h->leaf_marks,
+                    &h->ocl_pts, &h->ocl_indir, &h->ocl_indir_tmp, &h->ocl_dims, &h->ocl_vals, &h->ocl_clanc,
+                    &h->ocl_o2l, &h->ocl_keys, &h->ocl_bounds, &h->ocl_sort_ws, &h->ocl_ki, &h->ocl_kd, &h->ocl_nat};
   for (DevBuf* b : bufs) b->release();
   for (int i = 0; i < annf_handle::kMaxMarks; ++i)
     if (h->prof_ev[i]) cudaEventDestroy(h->prof_ev[i]);
@@ -305,6 +311,48 @@ int annf_project(annf_handle* h, const uint8_t* img, int hgt, int wid, int chann
   ANNF_REQUIRE(real_type == ANNF_REAL_F32 || real_type == ANNF_REAL_F64, "annf_project: bad real_type");
   return project(h, img, hgt, wid, channels, psize, components, mean, n_components, real_type, out,
                  static_cast<cudaStream_t>(stream));
+}
+
+int annf_ocl_build_tree(annf_handle* h, const float* points, int n, int d, int leaf_size, void* stream) {
+  ANNF_API_HANDLE(h);
+  ANNF_REQUIRE(points, "annf_ocl_build_tree: NULL points");
+  ANNF_REQUIRE(ANNF_ALIGNED(points, 4), "annf_ocl_build_tree: points must be 4-byte aligned");
+  return ocl_build_tree(h, points, n, d, leaf_size, static_cast<cudaStream_t>(stream));
+}
+
+int annf_ocl_tree_get(const annf_handle* h, annf_ocl_tree_view* out) {
+  if (!h || !out) {
+    set_error("annf_ocl_tree_get: NULL argument");
+    return ANNF_ERR_INVALID;
+  }
+  if (!h->ocl_built) {
+    set_error("annf_ocl_tree_get: no tree has been built");
+    return ANNF_ERR_STATE;
+  }
+  out->m = h->ocl_m;
+  out->d = h->ocl_d;
+  out->height = h->ocl_h;
+  out->n_nodes = h->ocl_q;
+  out->points_per_leaf = h->ocl_ppl;
+  out->m_padded = h->ocl_mp;
+  out->points = h->ocl_pts.as<float>();
+  out->indir = h->ocl_indir.as<int>();
+  out->node_dim = h->ocl_dims.as<int>();
+  out->node_val = h->ocl_vals.as<float>();
+  out->node_same_dim_ancestor = h->ocl_clanc.as<int>();
+  out->orig2leaf = h->ocl_o2l.as<int>();
+  return ANNF_OK;
+}
+
+int annf_ocl_rows(annf_handle* h, int* final_idx, const uint8_t* img_a, int ha, int wa, const uint8_t* img_b, int hb,
+                  int wb, int channels, int psize, const float* ared, int n_rows, int n_cols, int* knn_out,
+                  float* knn_sqdist_out, float* dist_out, void* stream) {
+  ANNF_API_HANDLE(h);
+  ANNF_REQUIRE(final_idx && img_a && img_b && ared, "annf_ocl_rows: NULL argument");
+  ANNF_REQUIRE(channels >= 1 && psize >= 1 && psize <= ha && psize <= wa && psize <= hb && psize <= wb,
+               "annf_ocl_rows: bad geometry");
+  return ocl_rows(h, final_idx, img_a, ha, wa, img_b, hb, wb, channels, psize, ared, n_rows, n_cols, knn_out,
+                  knn_sqdist_out, dist_out, static_cast<cudaStream_t>(stream));
 }
 
 int annf_set_option(annf_handle* h, int option, int value) {

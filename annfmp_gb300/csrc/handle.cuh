@@ -70,6 +70,10 @@ struct annf_handle {
   // ---- pca scratch ----
   annf::DevBuf gram, colsum, subset_t, cov, eigval, digits, meanproj, solver_ws, solver_info, eig_ws;
   int cov_p = 0;  // size of the covariance held in cov (0: none)
+  // ---- openclopt-semantics tree and lists (openclopt.cu) ----
+  int ocl_built = 0, ocl_m = 0, ocl_d = 0, ocl_h = -1, ocl_q = 0, ocl_ppl = 0, ocl_mp = 0;
+  annf::DevBuf ocl_pts, ocl_indir, ocl_indir_tmp, ocl_dims, ocl_vals, ocl_clanc, ocl_o2l, ocl_keys, ocl_bounds,
+      ocl_sort_ws, ocl_ki, ocl_kd, ocl_nat;
   // ---- options (annf_set_option) ----
   int opt_int_projection = 0;  // 1: the exact projection always runs the dp4a kernel
   cusolverDnContext* solver = nullptr;

@@ -178,6 +178,46 @@ int annf_project(annf_handle* h, const uint8_t* img, int hgt, int wid, int chann
                  const double* components, const double* mean, int n_components, int real_type,
                  void* out, void* stream);
 
+/* ---- openclopt semantics: the NNF algorithm of annfmp's GPU backend ---------------------------
+ * (annfmp/openclopt/src/futhark/driverKNN.fut and the files it imports, driven by
+ * annfmp/openclopt/src/base.c:fit_extern, which the
+ * reference runs through Futhark-generated code) as a mode of this library, for comparison with
+ * that backend: K is 8 whatever the caller's n_neighbors; the tree has 2^(height+1) leaves of
+ * exactly points_per_leaf points (the input padded with +inf rows to m_padded), each node split
+ * at the mean of the two middle values of a stable sort of its points by the widest side of its
+ * box (lowest dimension on ties); descent goes left on "<="; the first row is searched exactly by
+ * the backend's incremental-distance traversal; propagated leaves are deduplicated against the
+ * natural leaf, "one row below" clamped to the last row; select best by squared raw-patch
+ * distance. FP32 only. */
+typedef struct {
+  int m, d;                 /* points (before padding), dimension */
+  int height;               /* levels of internal nodes minus one (-1: a single leaf) */
+  int n_nodes;              /* internal nodes: 2^(height+1) - 1 */
+  int points_per_leaf, m_padded;
+  const float* points;      /* [m_padded*d] leaf order, +inf pads */
+  const int* indir;         /* [m_padded] leaf-order position -> original index (>= m: a pad) */
+  const int* node_dim;      /* [n_nodes] heap order */
+  const float* node_val;    /* [n_nodes] */
+  const int* node_same_dim_ancestor;  /* [n_nodes] closest ancestor splitting the same dim, -1 none */
+  const int* orig2leaf;     /* [m_padded] */
+} annf_ocl_tree_view;
+
+/* Build the backend's tree over points [n*d] FP32 (device) with leaf_size as the default points
+ * per leaf. Replaces the buildKDtree entry (annfmp/openclopt/src/futhark/driverKNN.fut:142-151,
+ * buildKDtree.fut:17-157). At most 1024 points per leaf. */
+int annf_ocl_build_tree(annf_handle* h, const float* points, int n, int d, int leaf_size, void* stream);
+int annf_ocl_tree_get(const annf_handle* h, annf_ocl_tree_view* out);
+
+/* The NNF of image A against the tree over image B's reduced patches, from A's reduced patches
+ * ared [n_rows*n_cols*d] FP32: natural-leaf lists (findNaturalLeavesFixK, driverKNN.fut:153-204),
+ * the exact first row (exactKnnFixK, :231-290), row propagation (propagateFixK, :305-413), select
+ * best (selectBestNN, :90-133). Outputs: final_idx [n] original B indices; optional knn_out [n*8]
+ * original indices (-1: none), knn_sqdist_out [n*8] squared reduced distances, dist_out [n]
+ * raw-patch L2 of the choice. */
+int annf_ocl_rows(annf_handle* h, int* final_idx, const uint8_t* img_a, int ha, int wa, const uint8_t* img_b,
+                  int hb, int wb, int channels, int psize, const float* ared, int n_rows, int n_cols,
+                  int* knn_out, float* knn_sqdist_out, float* dist_out, void* stream);
+
 /* Set a per-handle option (ANNF_OPT_*). No counterpart in the reference: a knob of this
  * implementation that changes no result. */
 int annf_set_option(annf_handle* h, int option, int value);

@@ -273,6 +273,124 @@ def oracle_fit(image_a, image_b, n_neighbors=3, psize=8, dim_reduced=5, n_subset
 
 
 # ----------------------------------------------------------------------------------------------
+# the GPU backend's algorithm (openclopt), restated in ocl_oracle.c (parity unpinned: the
+# reference's Futhark path cannot run here)
+# ----------------------------------------------------------------------------------------------
+OCL_K = 8
+
+
+class _OclTree(ctypes.Structure):
+    _fields_ = [("m", ctypes.c_int), ("d", ctypes.c_int), ("h", ctypes.c_int), ("q", ctypes.c_int),
+                ("ppl", ctypes.c_int), ("mp", ctypes.c_int), ("pts", ctypes.c_void_p), ("indir", ctypes.c_void_p),
+                ("dims", ctypes.c_void_p), ("vals", ctypes.c_void_p), ("clanc", ctypes.c_void_p),
+                ("orig2leaf", ctypes.c_void_p)]
+
+
+def _ocl_lib():
+    if "ocl" in _LIBS:
+        return _LIBS["ocl"]
+    path = os.path.join(HERE, "libannf_ocl_oracle.so")
+    if not os.path.exists(path):
+        build_oracle()
+    lib = ctypes.CDLL(path)
+    vp, ip = ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)
+    lib.ocl_shape.argtypes = [ctypes.c_int, ctypes.c_int, ip, ip, ip, ip]
+    lib.ocl_build.argtypes = [ctypes.POINTER(_OclTree), vp]
+    lib.ocl_build.restype = ctypes.c_int
+    lib.ocl_natural.argtypes = [ctypes.POINTER(_OclTree), vp, ctypes.c_int, vp, vp, vp]
+    lib.ocl_exact.argtypes = [ctypes.POINTER(_OclTree), vp, ctypes.c_int, vp, vp, vp]
+    lib.ocl_propagate.argtypes = [ctypes.POINTER(_OclTree), vp, ctypes.c_int, ctypes.c_int, vp, vp, vp]
+    lib.ocl_propagate.restype = ctypes.c_int
+    lib.ocl_select.argtypes = [vp, ctypes.c_longlong, vp, vp, ctypes.c_int, vp, vp]
+    _LIBS["ocl"] = lib
+    return lib
+
+
+def ocl_shape(m: int, leaf_size: int):
+    """(h, q, ppl, m') of the GPU backend's tree (annfmp/openclopt/src/futhark/buildKDtree.fut:17-25)."""
+    v = [ctypes.c_int() for _ in range(4)]
+    _ocl_lib().ocl_shape(m, leaf_size, *[ctypes.byref(x) for x in v])
+    return tuple(x.value for x in v)
+
+
+class OclTree:
+    """The GPU backend's k-d tree (buildKDtree.fut), built by the C restatement."""
+
+    def __init__(self, X: np.ndarray, leaf_size: int):
+        X = np.ascontiguousarray(X, dtype=np.float32)
+        m, d = X.shape
+        self.h, self.q, self.ppl, self.mp = ocl_shape(m, leaf_size)
+        self.m, self.d = m, d
+        self.pts = np.empty((self.mp, d), np.float32)
+        self.indir = np.empty(self.mp, np.int32)
+        self.dims = np.empty(max(self.q, 1), np.int32)
+        self.vals = np.empty(max(self.q, 1), np.float32)
+        self.clanc = np.empty(max(self.q, 1), np.int32)
+        self.orig2leaf = np.empty(self.mp, np.int32)
+        self._s = _OclTree(m, d, self.h, self.q, self.ppl, self.mp, self.pts.ctypes.data, self.indir.ctypes.data,
+                           self.dims.ctypes.data, self.vals.ctypes.data, self.clanc.ctypes.data,
+                           self.orig2leaf.ctypes.data)
+        if _ocl_lib().ocl_build(ctypes.byref(self._s), X.ctypes.data) != 0:
+            raise ValueError("ocl_build rejected its input")
+        self.dims, self.vals, self.clanc = self.dims[:self.q], self.vals[:self.q], self.clanc[:self.q]
+
+    def natural(self, Q):
+        """(positions [n, 8], squared distances [n, 8], natural leaf [n])."""
+        Q = np.ascontiguousarray(Q, dtype=np.float32)
+        n = Q.shape[0]
+        ki, kd, nat = np.empty((n, OCL_K), np.int32), np.empty((n, OCL_K), np.float32), np.empty(n, np.int32)
+        _ocl_lib().ocl_natural(ctypes.byref(self._s), Q.ctypes.data, n, ki.ctypes.data, kd.ctypes.data, nat.ctypes.data)
+        return ki, kd, nat
+
+    def exact(self, Q, nat, ki, kd):
+        """Exact lists of the queries Q from their natural-leaf lists (in place)."""
+        Q = np.ascontiguousarray(Q, dtype=np.float32)
+        _ocl_lib().ocl_exact(ctypes.byref(self._s), Q.ctypes.data, Q.shape[0],
+                             np.ascontiguousarray(nat, dtype=np.int32).ctypes.data, ki.ctypes.data, kd.ctypes.data)
+
+    def rows(self, ared, n_rows, n_cols):
+        """The lists of every pixel: natural leaf, exact first row, row propagation (positions)."""
+        ki, kd, nat = self.natural(ared)
+        ki0, kd0 = ki[:n_cols].copy(), kd[:n_cols].copy()
+        self.exact(ared[:n_cols], nat[:n_cols], ki0, kd0)
+        ki[:n_cols], kd[:n_cols] = ki0, kd0
+        bad = _ocl_lib().ocl_propagate(ctypes.byref(self._s), np.ascontiguousarray(ared, np.float32).ctypes.data,
+                                       n_rows, n_cols, nat.ctypes.data, ki.ctypes.data, kd.ctypes.data)
+        return ki, kd, nat, bool(bad)
+
+
+def ocl_select(knn_orig, pa, pb):
+    """Select best by exact squared raw-patch distance (driverKNN.fut:90-133)."""
+    knn_orig = np.ascontiguousarray(knn_orig, dtype=np.int32)
+    n = knn_orig.shape[0]
+    best, bd = np.empty(n, np.int32), np.empty(n, np.float32)
+    _ocl_lib().ocl_select(knn_orig.ctypes.data, n, np.ascontiguousarray(pa).ctypes.data,
+                          np.ascontiguousarray(pb).ctypes.data, pa.shape[1], best.ctypes.data, bd.ctypes.data)
+    return best, bd
+
+
+def oracle_fit_openclopt(image_a, image_b, psize=8, dim_reduced=5, n_subset=1000, leaf_size=64, seed=0,
+                         return_all=False):
+    """ANNFieldPropKDTreeOpenCLOPT.fit (annfmp/openclopt/base.py:46-137, src/base.c:fit_extern):
+    the same PCA fit, K = 8 whatever n_neighbors is, the backend's tree, natural-leaf lists, exact
+    first row, row propagation, select best. The reduced patches are the plain pipeline's (FP64
+    transform rounded once; the backend's own FP32 reduction has no specified order)."""
+    comps, mean = pca_fit(image_a, image_b, psize, dim_reduced, n_subset, seed)
+    pa, pb = extract_patches(image_a, psize), extract_patches(image_b, psize)
+    ared = pca_transform(pa, comps, mean)
+    bred = pca_transform(pb, comps, mean)
+    n_rows, n_cols = image_a.shape[0] - psize + 1, image_a.shape[1] - psize + 1
+    tree = OclTree(bred, leaf_size)
+    ki, kd, nat, bad = tree.rows(ared, n_rows, n_cols)
+    knn_orig = np.where(ki >= 0, tree.indir[np.maximum(ki, 0)], -1).astype(np.int32)
+    nn, nd = ocl_select(knn_orig, pa, pb)
+    if return_all:
+        return dict(nn=nn, nn_sqdist=nd, knn=knn_orig, knn_pos=ki, knn_sqdist=kd, nat=nat, tree=tree, ared=ared,
+                    bred=bred, pa=pa, pb=pb, n_rows=n_rows, n_cols=n_cols, out_of_grid=bad)
+    return nn
+
+
+# ----------------------------------------------------------------------------------------------
 # the reference C core, compiled unmodified into oracle/_ref (present only where it was built)
 # ----------------------------------------------------------------------------------------------
 class KD_TREE_PARAMETERS(ctypes.Structure):

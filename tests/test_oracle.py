@@ -131,3 +131,31 @@ def test_live_reference_package_pipeline(oracle_mod):
     nn_ref = m.fit(a, b)
     nn_ora = O.oracle_fit(a, b, n_neighbors=2, psize=5, dim_reduced=6, n_subset=1600, leaf_size=8, seed=2)
     assert np.array_equal(nn_ref, nn_ora)
+
+
+def test_openclopt_oracle_first_row_is_exact(oracle_mod):
+    """The openclopt restatement's traversal (kd-traverse.fut:27-116) finds the exact 8 nearest:
+    the squared distances equal a brute force over every real point (pads excluded)."""
+    O = oracle_mod
+    rng = np.random.default_rng(4)
+    X = (rng.standard_normal((6000, 8)) * 10).astype(np.float32)
+    t = O.OclTree(X, 32)
+    assert (t.h, t.q, t.ppl, t.mp) == O.ocl_shape(6000, 32)
+    assert t.mp == (t.q + 1) * t.ppl and np.all(t.indir[t.indir >= 6000] >= 6000)
+    Q = (rng.standard_normal((200, 8)) * 10).astype(np.float32)
+    ki, kd, nat = t.natural(Q)
+    t.exact(Q, nat, ki, kd)
+    D = ((Q[:, None, :].astype(np.float64) - X[None].astype(np.float64)) ** 2).sum(-1)
+    want = np.sort(D, axis=1)[:, :8]
+    assert np.allclose(kd, want, rtol=2e-6)
+    assert np.all(np.diff(kd, axis=1) >= 0)
+
+
+def test_openclopt_tree_shape():
+    """Leaf count: the power of two nearest m / leaf_size, ties down (buildKDtree.fut:4-24)."""
+    from oracle import oracle as O
+    O.build_oracle()
+    assert O.ocl_shape(1000, 64) == (3, 15, 63, 1008)   # 16 leaves (15.6 -> 16)
+    assert O.ocl_shape(100, 64) == (0, 1, 50, 100)      # 2 leaves
+    assert O.ocl_shape(1536, 64) == (3, 15, 96, 1536)   # 24 leaves: 16 (tie goes down)
+    assert O.ocl_shape(30, 64) == (-1, 0, 30, 30)       # one leaf, no internal node
