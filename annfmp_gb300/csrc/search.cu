@@ -748,20 +748,29 @@ __global__ void __launch_bounds__(256, 3) leaf_chunk_scan_kernel(TreeView<T> tv,
       }
       const T seed = Ops::dist(seed_key[(long long)qi * K + K - 1]);
       for (int wi = 0; wi < w1 - w0; ++wi) {
-        uint32_t bits = __shfl_sync(kFull, myword, wi);
-        while (bits) {
-          const int leaf = ((w0 + wi) << 5) + __ffs(bits) - 1;
-          bits &= bits - 1;
+        const uint32_t bits = __shfl_sync(kFull, myword, wi);
+        const int nset = __popc(bits);
+        // lane i prepares the word's i-th marked leaf: its depth-first rank for this query (the
+        // node lookups of all leaves in flight together) and its point range
+        int pleaf = 0, pbeg = 0, pend = 0;
+        uint32_t phi = 0;
+        if (lane < nset) {
+          pleaf = ((w0 + wi) << 5) + (int)__fns(bits, 0, lane + 1);
           uint32_t rank = 0;  // the leaf's position in this query's depth-first visiting order
           for (int t = 0; t < depth; ++t) {
-            const int node = (1 << t) - 1 + (leaf >> (depth - t));
+            const int node = (1 << t) - 1 + (pleaf >> (depth - t));
             int ax;
             T s;
             nc.get(tv, node, ax, s);
-            rank = (rank << 1) | (uint32_t)(((leaf >> (depth - 1 - t)) & 1) ^ (sq[ax] >= s ? 1 : 0));
+            rank = (rank << 1) | (uint32_t)(((pleaf >> (depth - 1 - t)) & 1) ^ (sq[ax] >= s ? 1 : 0));
           }
-          const uint32_t hi = rank << tv.leaf_bits;
-          const int beg = __ldg(tv.leaf_begin + leaf), end = __ldg(tv.leaf_begin + leaf + 1);
+          phi = rank << tv.leaf_bits;
+          pbeg = __ldg(tv.leaf_begin + pleaf);
+          pend = __ldg(tv.leaf_begin + pleaf + 1);
+        }
+        for (int li = 0; li < nset; ++li) {
+          const uint32_t hi = __shfl_sync(kFull, phi, li);
+          const int beg = __shfl_sync(kFull, pbeg, li), end = __shfl_sync(kFull, pend, li);
           for (int pb = beg; pb < end; pb += 128) {
             int pp[4];
 #pragma unroll

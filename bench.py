@@ -58,10 +58,12 @@ GRAPH_WORKLOADS = {
 }
 L2_FLUSH_BYTES = 256 << 20
 # the arithmetic each form computes in
-DTYPES = {"plain": "f32", "parallel": "bf16", "learned": "bf16"}
+DTYPES = {"plain": "f32", "openclopt": "f32", "parallel": "bf16", "learned": "bf16"}
 ARITHMETIC = {
     "plain": "u8 images; FP64 covariance and eigendecomposition; exact FP32 projection; FP32 tree and "
              "leaf distances (no FMA, the reference's order); int32 raw-patch re-rank",
+    "openclopt": "u8 images; FP64 covariance and eigendecomposition; exact FP32 projection; FP32 tree (median "
+                 "of two middle values) and leaf distances; squared raw-patch re-rank",
     "parallel": "u8 images; FP64 covariance and Rayleigh-Ritz, FP32 subspace iteration; FP16 tensor-core "
                 "projection (FP32 accumulate); FP32 tree; BF16 hi/lo tensor-core leaf tiles (FP32 accumulate) "
                 "with an exact FP32 re-rank; int32 exact raw-patch SSD for every candidate",
@@ -308,6 +310,11 @@ def make_model(form, args, prm, local_rank, graph="auto"):
     tiles, parallel propagation; learned: parallel + the trained offset-proposal network. The
     parallel forms replay a captured CUDA graph from their third fit on (graph="auto")."""
     from annfmp_gb300 import ANNFieldPropKDTreeGB300
+    if form == "openclopt":  # the reference GPU backend's algorithm (K 8), eager
+        from annfmp_gb300 import ANNFieldPropKDTreeOpenCLOPTGB300
+        return ANNFieldPropKDTreeOpenCLOPTGB300(psize=prm["psize"], dim_reduced=prm["dim_reduced"],
+                                                n_subset=prm["n_subset"], leaf_size=prm["leaf_size"],
+                                                seed=prm["seed"], verbose=0, device_id=local_rank)
     kw = dict(verbose=0, device=local_rank, graph=graph, **prm)
     if form == "plain":
         return ANNFieldPropKDTreeGB300(**kw)
@@ -435,7 +442,7 @@ def run_gpu(args, w, rank, world, local_rank):
     # the other forms on the same pair, same timing rules (for the speed-up at equal error)
     forms = {args.form: {"ms_per_step": ms, "value": n_a / (ms / 1e3), "distance_error": quality}}
     if world == 1 and not args.no_compare:
-        for f in ("plain", "parallel", "learned"):
+        for f in ("plain", "parallel", "learned", "openclopt"):
             if f == args.form or (f == "learned" and not learned_available()):
                 continue
             fms, fnn = time_form(f, args, prm, local_rank, A, B, flush, max(2, args.steps // 2))
@@ -633,8 +640,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="large", choices=sorted(WORKLOADS) + sorted(GRAPH_WORKLOADS))
-    ap.add_argument("--form", default="learned", choices=["plain", "parallel", "learned"],
-                    help="plain: the reference's method; parallel: BF16 tensor-core form; learned: + proposals")
+    ap.add_argument("--form", default="learned", choices=["plain", "parallel", "learned", "openclopt"],
+                    help="plain: the reference's method; parallel: BF16 tensor-core form; learned: + proposals; "
+                         "openclopt: the reference GPU backend's algorithm")
     ap.add_argument("--iters", type=int, default=3, help="propagation passes of the parallel forms")
     ap.add_argument("--no-compare", action="store_true", help="time only --form (not the other forms)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
