@@ -14,7 +14,8 @@
 //   4. components = Q x, in decreasing Ritz value, each signed so that its largest |entry| is
 //      positive (the sign convention of the exact solver).
 // The covariance and the small eigenproblem stay in FP64; only the power steps that find the
-// subspace run in FP32. Used by the approximate NNF forms; the plain form keeps the exact solver.
+// subspace run in FP32. Used by the approximate NNF forms; the plain form runs the FP64 iteration
+// further down (subspace_exact_kernel), whose components agree with a full FP64 eigensolver.
 #include <algorithm>
 
 #include "common.cuh"

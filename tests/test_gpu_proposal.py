@@ -200,3 +200,21 @@ def test_seeded_start_equals_proposals_in_init(gpu_lib):
     best = np.where(ssd == mins[:, None], P, np.iinfo(np.int64).max).min(axis=1)  # smaller index on ties
     assert np.array_equal(seed[0], np.where(mins == none, -1, best))
     assert np.array_equal(seed[1][seed[0] >= 0], mins[seed[0] >= 0])
+
+
+def test_headline_form_within_one_percent(gpu_lib):
+    """The headline form (tensor-core leaf tiles + learned proposals, 3 passes) on the 2048x2048
+    flow pair (patch 9, PCA 16, leaf 64, k 4) stays within 1% mean distance-ratio error of the
+    exact raw-patch nearest neighbour on 4096 sampled pixels."""
+    from annfmp_gb300 import ANNFieldPropKDTreeGB300, gen, metrics
+    from annfmp_gb300.proposal import DEFAULT_WEIGHTS, ProposalNet
+    if not os.path.exists(DEFAULT_WEIGHTS):
+        pytest.skip("no trained weights")
+    a, b = gen.pair_flow(1, 2048)
+    n_b = (2048 - 8) ** 2
+    m = ANNFieldPropKDTreeGB300(n_neighbors=4, psize=9, dim_reduced=16, n_subset=int(round(0.1 * n_b)),
+                                leaf_size=64, seed=1, verbose=0, form="parallel", iters=3,
+                                proposal=ProposalNet.pretrained())
+    nn = m.fit(a, b)
+    err = metrics.distance_ratio_error(a, b, nn, 9, n_samples=4096, seed=8)
+    assert err["mean"] <= 0.01, err
