@@ -25,6 +25,7 @@ namespace annf {
 int num_sms();
 
 constexpr int kTcThreads = 128;                    // one warpgroup: thread t <-> TMEM lane t <-> query t
+constexpr int kTcQueue = 48;                       // columns a query queues for the exact re-rank
 constexpr long long kTcWaitCycles = 2000000000LL;  // ~1 s at 2 GHz: bound of every mbarrier wait
 
 // Operand precision of the leaf tiles. BF16 (PREC 0) splits every centred coordinate x into
@@ -301,6 +302,7 @@ __global__ void __launch_bounds__(kTcThreads) leaf_tc_kernel(TcLeafArgs a) {
   using PR = TcPrec<PREC>;
   constexpr int KT = PR::kSplit * KPAD;  // K extent of the tiles (elements)
   constexpr int RB = (KT * PR::kES + 31) / 32 * 32;  // tile row bytes: whole MMA K steps (32 bytes)
+  constexpr int KPS = KPAD + 4;  // FP32 point row stride: 16-byte rows that spread over the banks
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   const TreeView<float>& tv = a.tv;
   const int d = tv.d, L = 1 << tv.depth, npad = a.npad, K = a.K;
@@ -310,8 +312,8 @@ __global__ void __launch_bounds__(kTcThreads) leaf_tc_kernel(TcLeafArgs a) {
   p += kTcThreads * RB;
   unsigned char* sB = p;
   p += (size_t)npad * RB;
-  float* sP = reinterpret_cast<float*>(p);  // [npad][KPAD] FP32 leaf points (zero padded)
-  p += (size_t)npad * KPAD * 4;
+  float* sP = reinterpret_cast<float*>(p);  // [npad][KPS] FP32 leaf points (zero padded)
+  p += (size_t)npad * KPS * 4;
   float* sN = reinterpret_cast<float*>(p);
   p += (size_t)npad * 4;
   float* sC = reinterpret_cast<float*>(p);  // [KPAD] centre, then [KPAD] = R, [KPAD+1] = FP8 point scale
@@ -323,6 +325,8 @@ __global__ void __launch_bounds__(kTcThreads) leaf_tc_kernel(TcLeafArgs a) {
   p += 8;
   int* sflag = reinterpret_cast<int*>(p);  // [0] leaf, [1] abort
   p += 8;
+  unsigned char* sQ = p;  // [kTcQueue][kTcThreads] columns each query re-ranks
+  p += kTcQueue * kTcThreads;
   if (smem_overrun(smem_raw, p, tv.status)) return;
 
   const int tid = threadIdx.x, warp = tid >> 5;
@@ -472,7 +476,7 @@ __global__ void __launch_bounds__(kTcThreads) leaf_tc_kernel(TcLeafArgs a) {
       }
 #pragma unroll
       for (int j = 0; j < KPAD; j += 4)
-        *reinterpret_cast<float4*>(sP + r * KPAD + j) = make_float4(f[j], f[j + 1], f[j + 2], f[j + 3]);
+        *reinterpret_cast<float4*>(sP + r * KPS + j) = make_float4(f[j], f[j + 1], f[j + 2], f[j + 3]);
       sN[r] = r < np ? nrm : FLT_MAX;
     }
     }  // staging
@@ -576,6 +580,18 @@ __global__ void __launch_bounds__(kTcThreads) leaf_tc_kernel(TcLeafArgs a) {
         }
         tc::mma_commit(mbar);
       }
+      // while the MMAs run: start the next item's leaf points and queries on their way to L2
+      if (w + (int)gridDim.x < total) {
+        const int wn = w + (int)gridDim.x;
+        const int pbn = __ldg(tv.leaf_begin + l_next), pen = __ldg(tv.leaf_begin + l_next + 1);
+        const char* base = reinterpret_cast<const char*>(tv.pts + (size_t)pbn * d);
+        const int bytes = (pen - pbn) * d * 4;
+        for (int off = tid * 128; off < bytes; off += kTcThreads * 128)
+          asm volatile("prefetch.global.L2 [%0];" ::"l"(base + off));
+        const int qbn = __ldg(a.qoff + l_next) + (wn - __ldg(a.choff + l_next)) * kTcThreads;
+        if (qbn + tid < __ldg(a.qoff + l_next + 1))
+          asm volatile("prefetch.global.L2 [%0];" ::"l"(a.Q + (size_t)__ldg(a.qorder + qbn + tid) * d));
+      }
       if (!mbar_wait_clock(mbar, phase)) sflag[1] = 1;
       phase ^= 1u;
       __syncthreads();
@@ -586,18 +602,35 @@ __global__ void __launch_bounds__(kTcThreads) leaf_tc_kernel(TcLeafArgs a) {
       tc::fence_after_sync();
       // the tile holds dot products of scaled vectors (FP8: powers of two, exact to undo)
       const float dsc = PREC == 2 ? -2.f / (sa * sC[KPAD + 1]) : -2.f;
-      // pass 1: the KM smallest estimates (padding columns carry sN = FLT_MAX)
+      // pass 1: est_b, an upper bound of est_(k), the k-th smallest estimate: the k-th smallest
+      // of the minima of groups of four columns (k groups' minima are k distinct estimates, so
+      // their k-th smallest is at least est_(k)); padding columns carry sN = FLT_MAX
       float ev[KM];
 #pragma unroll
       for (int j = 0; j < KM; ++j) ev[j] = FLT_MAX;
       for (int c0 = 0; c0 < npad; c0 += 16) {
         uint32_t r[16];
         tc::tmem_ld16(trow + (uint32_t)c0, r);
+        float nv[16];
+#pragma unroll
+        for (int j = 0; j < 16; j += 4) {
+          const float4 n4 = *reinterpret_cast<const float4*>(sN + c0 + j);
+          nv[j] = n4.x;
+          nv[j + 1] = n4.y;
+          nv[j + 2] = n4.z;
+          nv[j + 3] = n4.w;
+        }
         tc::tmem_wait_ld();
 #pragma unroll
-        for (int j = 0; j < 16; ++j) smallest_insert<KM>(ev, fmaf(dsc, __uint_as_float(r[j]), sN[c0 + j]));
+        for (int g = 0; g < 16; g += 4) {
+          const float e0 = fmaf(dsc, __uint_as_float(r[g]), nv[g]);
+          const float e1 = fmaf(dsc, __uint_as_float(r[g + 1]), nv[g + 1]);
+          const float e2 = fmaf(dsc, __uint_as_float(r[g + 2]), nv[g + 2]);
+          const float e3 = fmaf(dsc, __uint_as_float(r[g + 3]), nv[g + 3]);
+          smallest_insert<KM>(ev, fminf(fminf(e0, e1), fminf(e2, e3)));
+        }
       }
-      // band: est_j <= est_(k) + 2 delta, delta = 2 kDot |a-c| R + FP32 slack
+      // band: est_j <= est_b + 2 delta, delta = 2 kDot |a-c| R + FP32 slack
       float evk = FLT_MAX;
 #pragma unroll
       for (int j = 0; j < KM; ++j)
@@ -611,7 +644,36 @@ __global__ void __launch_bounds__(kTcThreads) leaf_tc_kernel(TcLeafArgs a) {
       // FP16 cannot hold centred values beyond its range: such queries and leaves take every point
       const bool unsafe = PREC == 1 && (amax > 60000.f || R > 60000.f);
       const float tau = (evk >= FLT_MAX || unsafe) ? FLT_MAX : evk + 2.f * delta;
-      // pass 2: exact FP32 distance (reference order) of every point passing the bound
+      // pass 2: queue the columns whose estimate passes the bound, in column order (a query that
+      // takes every point, or whose queue overflows, re-ranks the whole leaf below)
+      const bool every = tau == FLT_MAX;
+      int cnt = 0;
+      for (int c0 = 0; c0 < npad; c0 += 16) {
+        uint32_t r[16];
+        tc::tmem_ld16(trow + (uint32_t)c0, r);
+        float nv[16];
+#pragma unroll
+        for (int j = 0; j < 16; j += 4) {
+          const float4 n4 = *reinterpret_cast<const float4*>(sN + c0 + j);
+          nv[j] = n4.x;
+          nv[j + 1] = n4.y;
+          nv[j + 2] = n4.z;
+          nv[j + 3] = n4.w;
+        }
+        tc::tmem_wait_ld();
+        unsigned pass = 0;
+#pragma unroll
+        for (int j = 0; j < 16; ++j) pass |= fmaf(dsc, __uint_as_float(r[j]), nv[j]) <= tau ? (1u << j) : 0u;
+        if (c0 + 16 > np) pass &= np > c0 ? (1u << (np - c0)) - 1u : 0u;
+        if (qi < 0 || every) pass = 0u;
+        while (pass) {
+          if (cnt < kTcQueue) sQ[cnt * kTcThreads + tid] = (unsigned char)(c0 + __ffs(pass) - 1);
+          pass &= pass - 1;
+          ++cnt;
+        }
+      }
+      // the exact FP32 distance (reference order) of every queued point; padding coordinates are
+      // zero on both sides and add exact zeros
       float xv[KM];
       int xi[KM];
 #pragma unroll
@@ -619,33 +681,17 @@ __global__ void __launch_bounds__(kTcThreads) leaf_tc_kernel(TcLeafArgs a) {
         xv[j] = FLT_MAX;
         xi[j] = -1;
       }
-      for (int c0 = 0; c0 < npad; c0 += 16) {
-        uint32_t r[16];
-        tc::tmem_ld16(trow + (uint32_t)c0, r);
-        tc::tmem_wait_ld();
-        if (qi >= 0) {
-          unsigned pass = 0;
+      if (qi >= 0) {
+        const bool whole = every || cnt > kTcQueue;
+        const int n_do = whole ? np : cnt;
+        for (int t = 0; t < n_do; ++t) {
+          const int col = whole ? t : (int)sQ[t * kTcThreads + tid];
+          const float* pp = sP + col * KPS;
+          float s = 0.f;
 #pragma unroll
-          for (int j = 0; j < 16; ++j) {
-            const float est = fmaf(dsc, __uint_as_float(r[j]), sN[c0 + j]);
-            pass |= (c0 + j < np && (est <= tau || tau == FLT_MAX)) ? (1u << j) : 0u;
-          }
-          while (pass) {
-            const int col = c0 + __ffs(pass) - 1;
-            pass &= pass - 1;
-            {
-              const float* pp = sP + col * KPAD;
-              float s = 0.f;
-#pragma unroll
-              for (int u = 0; u < KPAD; ++u) {
-                if (u < d) {
-                  const float t = __fsub_rn(qf[u], pp[u]);
-                  s = __fadd_rn(s, __fmul_rn(t, t));
-                }
-              }
-              sorted_insert<KM>(xv, xi, s, col);
-            }
-          }
+          for (int u = 0; u < KPAD; u += 4)
+            s = dist_step4(s, *reinterpret_cast<const float4*>(pp + u), qf[u], qf[u + 1], qf[u + 2], qf[u + 3]);
+          sorted_insert<KM>(xv, xi, s, col);
         }
       }
       if (qi >= 0) {
@@ -753,8 +799,8 @@ int natural_knn_tc(annf_handle* h, const float* Q, long long nq, int K, int prec
   // tile row bytes: K extent (BF16 / FP8 hi-lo splits: 3 terms) times the element size, in whole
   // 32-byte MMA K steps (the kernel's RB)
   const int rb = ((prec == 1 ? 1 : 3) * kpad * (prec == 2 ? 1 : 2) + 31) / 32 * 32;
-  const size_t carve = (size_t)kTcThreads * rb + (size_t)args.npad * rb + (size_t)args.npad * kpad * 4 +
-                       (size_t)args.npad * 4 + (kpad + 4) * 4 + 16 + 24 + 64;
+  const size_t carve = (size_t)kTcThreads * rb + (size_t)args.npad * rb + (size_t)args.npad * (kpad + 4) * 4 +
+                       (size_t)args.npad * 4 + (kpad + 4) * 4 + 16 + 24 + (size_t)kTcQueue * kTcThreads + 64;
   // at most 512 / ncols CTAs may hold TMEM on one SM: pad the shared memory so no more fit
   const int per_sm = std::max(1, 512 / args.ncols);
   const size_t cap = 227 * 1024;
