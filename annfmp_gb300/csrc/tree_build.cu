@@ -155,17 +155,22 @@ __global__ void hist_kernel(int n, int d, int t, int B, int shift, int width, bo
   const K hmask = (shift + width >= (int)(8 * sizeof(K))) ? (K)0 : (~(K)0 << (shift + width));
   const int ax = axis[s];
   const int lane = threadIdx.x & 31;
-  for (int base = c0 + (int)(threadIdx.x & ~31u); base < c1; base += blockDim.x) {
-    const int i = base + lane;
+  // every load of the thread's kItems elements first (all in flight at once), then the bins
+  K kv[kItems];
+#pragma unroll
+  for (int q = 0; q < kItems; ++q) {
+    const int i = c0 + (int)threadIdx.x + q * kThreads;
+    kv[q] = 0;
+    if (i < c1) kv[q] = extract ? (K)ord_key(pts[(long long)i * d + ax]) : keys[i];
+  }
+#pragma unroll
+  for (int q = 0; q < kItems; ++q) {
+    const int i = c0 + (int)threadIdx.x + q * kThreads;
+    if (c0 + q * kThreads >= c1) break;  // uniform: no element of this round in the chunk
     unsigned bin = kSelBins;
     if (i < c1) {
-      K k;
-      if (extract) {
-        k = ord_key(pts[(long long)i * d + ax]);
-        keys[i] = k;
-      } else {
-        k = keys[i];
-      }
+      const K k = kv[q];
+      if (extract) keys[i] = k;
       if (((k ^ pre) & hmask) == 0) bin = (unsigned)(k >> shift) & (unsigned)(nb - 1);
     }
     const unsigned peers = __match_any_sync(0xffffffffu, bin);
@@ -352,9 +357,19 @@ __global__ void __launch_bounds__(kThreads) scatter_kernel(
     const float4* src = reinterpret_cast<const float4*>(pts_in) + (long long)c0 * w;
     float4* dst4 = reinterpret_cast<float4*>(pts_out);
     if (cmin == nullptr) {
-      for (int e = threadIdx.x; e < m * w; e += blockDim.x) {
-        const int r = e / w, c = e - r * w;
-        dst4[(long long)sdst[r] * w + c] = src[e];
+      for (int e0 = threadIdx.x; e0 < m * w; e0 += 4 * kThreads) {
+        float4 v[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+          if (e0 + u * kThreads < m * w) v[u] = src[e0 + u * kThreads];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int e = e0 + u * kThreads;
+          if (e < m * w) {
+            const int r = e / w, c = e - r * w;
+            dst4[(long long)sdst[r] * w + c] = v[u];
+          }
+        }
       }
     } else {
       // the children's bounding boxes on the way: a thread always handles word c = tid mod w
@@ -369,21 +384,33 @@ __global__ void __launch_bounds__(kThreads) scatter_kernel(
           fmx[u][j] = -__int_as_float(0x7f800000);
         }
       bool has[2] = {false, false};  // (infinite coordinates are valid points: no sentinel test)
-      for (int e = threadIdx.x; e < m * w; e += blockDim.x) {
-        const int r = e / w, c = e - r * w;
-        const float4 v = src[e];
-        dst4[(long long)sdst[r] * w + c] = v;
-        const bool rt = sside[r] != 0;
-        has[0] |= !rt;
-        has[1] |= rt;
-        const float inf = __int_as_float(0x7f800000);
-        const float vv[4] = {v.x, v.y, v.z, v.w};
+      // four words per thread per round, their loads issued together (w divides the block, so
+      // every word of a thread is word tid mod w of its row)
+      for (int e0 = threadIdx.x; e0 < m * w; e0 += 4 * kThreads) {
+        float4 v4[4];
 #pragma unroll
-        for (int j = 0; j < 4; ++j) {
-          fmn[0][j] = fminf(fmn[0][j], rt ? inf : vv[j]);
-          fmx[0][j] = fmaxf(fmx[0][j], rt ? -inf : vv[j]);
-          fmn[1][j] = fminf(fmn[1][j], rt ? vv[j] : inf);
-          fmx[1][j] = fmaxf(fmx[1][j], rt ? vv[j] : -inf);
+        for (int u = 0; u < 4; ++u)
+          if (e0 + u * kThreads < m * w) v4[u] = src[e0 + u * kThreads];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int e = e0 + u * kThreads;
+          if (e < m * w) {
+            const int r = e / w, c = e - r * w;
+            const float4 v = v4[u];
+            dst4[(long long)sdst[r] * w + c] = v;
+            const bool rt = sside[r] != 0;
+            has[0] |= !rt;
+            has[1] |= rt;
+            const float inf = __int_as_float(0x7f800000);
+            const float vv[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+              fmn[0][j] = fminf(fmn[0][j], rt ? inf : vv[j]);
+              fmx[0][j] = fmaxf(fmx[0][j], rt ? -inf : vv[j]);
+              fmn[1][j] = fminf(fmn[1][j], rt ? vv[j] : inf);
+              fmx[1][j] = fmaxf(fmx[1][j], rt ? vv[j] : -inf);
+            }
+          }
         }
       }
       // to order keys (-0 and +0 fold together, so fminf's choice between them does not matter);
@@ -435,7 +462,17 @@ __global__ void __launch_bounds__(kThreads) scatter_kernel(
       pts_out[(long long)sdst[r] * d + c] = pts_in[(long long)(c0 + r) * d + c];
     }
   }
-  for (int i = threadIdx.x; i < m; i += blockDim.x) perm_out[sdst[i]] = perm_in[c0 + i];
+  int pv_[kItems];
+#pragma unroll
+  for (int q = 0; q < kItems; ++q) {
+    const int i = (int)threadIdx.x + q * kThreads;
+    if (i < m) pv_[q] = perm_in[c0 + i];
+  }
+#pragma unroll
+  for (int q = 0; q < kItems; ++q) {
+    const int i = (int)threadIdx.x + q * kThreads;
+    if (i < m) perm_out[sdst[i]] = pv_[q];
+  }
 }
 
 // one warp per segment: the reference's forward swap pass over the equal elements, then the node
