@@ -159,12 +159,18 @@ __global__ void fast_init_kernel(Img A, Img B, int nA, int K, const int* __restr
 
 // one pass: the four neighbours' matches at distance 'jump', shifted to this pixel, and 'nrand'
 // random offsets around the current match within 'radius'
+//
+// chg_in (optional): per pixel, whether its match changed in the previous pass (same jump). A
+// neighbour that did not change offers the candidate this pixel already tried in that pass,
+// against a best no better than the current one, so it is skipped: the result is the same as
+// trying it. chg_out receives this pass's flags.
 __global__ void fast_prop_kernel(Img A, Img B, int nA, int jump, int radius, int nrand, uint32_t seed, Match in,
-                                 Match out) {
+                                 Match out, const uint8_t* __restrict__ chg_in, uint8_t* __restrict__ chg_out) {
   const int nb_rows = B.h - B.psize + 1, na_rows = nA / A.ncols;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nA; i += gridDim.x * blockDim.x) {
     const int y = i / A.ncols, x = i - y * A.ncols;
-    int best = in.idx[i], bs = in.ssd[i];
+    const int start = in.idx[i];
+    int best = start, bs = in.ssd[i];
     const int b0y = best / B.ncols, b0x = best - b0y * B.ncols;
     auto consider = [&](int by, int bx) {
       if (by < 0 || bx < 0 || by >= nb_rows || bx >= B.ncols) return;
@@ -181,6 +187,7 @@ __global__ void fast_prop_kernel(Img A, Img B, int nA, int jump, int radius, int
     for (int t = 0; t < 4; ++t) {
       const int ny = y + dy[t] * jump, nx = x + dx[t] * jump;
       if (ny < 0 || nx < 0 || ny >= na_rows || nx >= A.ncols) continue;
+      if (chg_in && !chg_in[ny * A.ncols + nx]) continue;
       const int nb = in.idx[ny * A.ncols + nx];
       if (nb < 0) continue;
       const int nby = nb / B.ncols, nbx = nb - nby * B.ncols;
@@ -193,6 +200,7 @@ __global__ void fast_prop_kernel(Img A, Img B, int nA, int jump, int radius, int
     }
     out.idx[i] = best;
     out.ssd[i] = bs;
+    if (chg_out) chg_out[i] = best != start;
   }
 }
 
@@ -344,8 +352,55 @@ __device__ __forceinline__ void ssd_group_s(const unsigned* __restrict__ sa, int
   for (int g = 0; g < G; ++g) out[g] = cy[g] < 0 ? 0x7fffffff : (int)s[g];
 }
 
+// exact SSDs of G listed candidates, each against its own pixel's A patch in shared memory
+// (column pj[g] of sa, word j of patch row r at sa[(r * NW + j) * stride + pj[g]]); a candidate
+// stops once its partial sum exceeds lim[g] (its value is then > lim[g])
+template <int PS, int RL, int G>
+__device__ __forceinline__ void ssd_jobs(const unsigned* __restrict__ sa, int stride, const int (&pj)[G], const Img& B,
+                                         const int (&cy)[G], const int (&cx)[G], const int (&lim)[G], int (&out)[G]) {
+  constexpr int NW = (RL + 3) / 4;
+  unsigned s[G];
+  bool live[G];
+#pragma unroll
+  for (int g = 0; g < G; ++g) {
+    s[g] = 0;
+    live[g] = cy[g] >= 0;
+  }
+#pragma unroll 1
+  for (int r = 0; r < PS; ++r) {
+    bool any = false;
+#pragma unroll
+    for (int g = 0; g < G; ++g) any |= live[g];
+    if (!any) break;
+    unsigned bw[G][NW];
+#pragma unroll
+    for (int g = 0; g < G; ++g)
+      if (live[g]) row_words<RL>(B.p, ((long long)(cy[g] + r) * B.w + cx[g]) * B.c, B.bytes, bw[g]);
+#pragma unroll
+    for (int g = 0; g < G; ++g) {
+      if (!live[g]) continue;
+      const unsigned* a = sa + r * NW * stride + pj[g];
+#pragma unroll
+      for (int j = 0; j < NW; ++j) {
+        const unsigned dd = __vabsdiffu4(a[j * stride], bw[g][j]);
+        s[g] = __dp4a(dd, dd, s[g]);
+      }
+      if ((int)s[g] > lim[g]) live[g] = false;
+    }
+  }
+#pragma unroll
+  for (int g = 0; g < G; ++g) out[g] = cy[g] < 0 ? 0x7fffffff : (int)s[g];
+}
+
 constexpr int kPropThreads = 256;
-constexpr int kPropGroup = 5;  // a pass's four neighbour candidates and its first random offset
+constexpr int kPropGroup = 4;  // listed candidates per thread at a time
+constexpr int kPropSlots = 6;  // candidate slots per pixel of the listing pass: 4 neighbours + up to 2 random offsets
+
+// dynamic shared memory of fast_prop_t_kernel: best keys, aligned A patches, the candidate list
+static size_t prop_smem(int ps, int nw, int nrand) {
+  return (size_t)kPropThreads * (sizeof(unsigned long long) + (size_t)ps * nw * sizeof(unsigned) +
+                                 (size_t)(4 + nrand) * (sizeof(int) + 1));
+}
 
 // seed (optional, [2 nA]: B index, then SSD): a match to start from, e.g. the best proposal found
 // earlier; the result is the lexicographic minimum over the seed and the candidates either way
@@ -382,62 +437,146 @@ __global__ void __launch_bounds__(256, 3) fast_init_t_kernel(Img A, Img B, int n
 }
 
 // one pass: the four neighbours' matches at distance 'jump', shifted to this pixel, and 'nrand'
-// random offsets around the pass's starting match within 'radius', kPropGroup candidates at a
-// time (the neighbours and the first offset together). The pixel's A patch is aligned into shared
-// memory once and read by every group.
+// random offsets around the pass's starting match within 'radius'. A CTA takes 256 consecutive
+// pixels: each thread aligns its pixel's A patch into shared memory and lists the candidates that
+// can change the result (not the starting match, not a repeat of an earlier candidate of the
+// pixel, with chg_in not a neighbour whose match did not change in the previous pass:
+// fast_prop_kernel); the CTA then works through the listed candidates, kPropGroup per thread at a
+// time. The list is slot-major (every pixel's "up" candidate, then every "down", ..., then the
+// random offsets), so the 32 candidates of a warp come from neighbouring pixels and the same
+// direction, and their B rows share cache lines as they would in a thread-per-pixel pass, while
+// no lane idles on a candidate it does not have. Each candidate folds (SSD, index) into its
+// pixel's 64-bit best key with atomicMin: the lexicographic minimum, the same result as trying the
+// candidates one by one.
 template <int PS, int RL>
 __global__ void __launch_bounds__(kPropThreads, 3) fast_prop_t_kernel(Img A, Img B, int nA, int jump, int radius,
-                                                                   int nrand, uint32_t seed, Match in, Match out) {
+                                                                   int nrand, uint32_t seed, Match in, Match out,
+                                                                   const uint8_t* __restrict__ chg_in,
+                                                                   uint8_t* __restrict__ chg_out) {
   constexpr int NW = (RL + 3) / 4;
   constexpr int G = kPropGroup;
-  extern __shared__ unsigned sAw[];  // [PS * NW][kPropThreads]
-  unsigned* myA = sAw + threadIdx.x;
+  constexpr int kWarps = kPropThreads / 32;
+  extern __shared__ unsigned long long sdyn[];
+  unsigned long long* sbest = sdyn;                                      // [kPropThreads]
+  unsigned* sAw = reinterpret_cast<unsigned*>(sbest + kPropThreads);     // [PS * NW][kPropThreads]
+  int* sjob = reinterpret_cast<int*>(sAw + PS * NW * kPropThreads);      // [slots * kPropThreads]
+  unsigned char* sjp = reinterpret_cast<unsigned char*>(sjob + (4 + nrand) * kPropThreads);
+  __shared__ int swcnt[kPropSlots][kWarps];
   const int nb_rows = B.h - B.psize + 1, na_rows = nA / A.ncols;
-  const int nr = radius > 0 ? nrand : 0;
-  const int ngroups = 1 + (nr > G - 4 ? (nr - (G - 4) + G - 1) / G : 0);
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nA; i += gridDim.x * blockDim.x) {
-    const int y = i / A.ncols, x = i - y * A.ncols;
-    int best = in.idx[i], bs = in.ssd[i];
-    const int b0y = best / B.ncols, b0x = best - b0y * B.ncols;
+  const int nr = radius > 0 ? min(nrand, kPropSlots - 4) : 0;
+  const int slots = 4 + nr;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const unsigned lt_mask = (1u << lane) - 1u;
+  for (long long tile = (long long)blockIdx.x * kPropThreads; tile < nA; tile += (long long)gridDim.x * kPropThreads) {
+    const int i = (int)tile + threadIdx.x;
+    const bool have = i < nA;
+    int start = -1, y = 0, x = 0;
+    if (have) {
+      y = i / A.ncols;
+      x = i - y * A.ncols;
+      start = in.idx[i];
+      sbest[threadIdx.x] = ((unsigned long long)(unsigned)in.ssd[i] << 32) | (unsigned)start;
 #pragma unroll 1
-    for (int r = 0; r < PS; ++r) {
-      unsigned w[NW];
-      row_words<RL>(A.p, ((long long)(y + r) * A.w + x) * A.c, A.bytes, w);
+      for (int r = 0; r < PS; ++r) {
+        unsigned w[NW];
+        row_words<RL>(A.p, ((long long)(y + r) * A.w + x) * A.c, A.bytes, w);
 #pragma unroll
-      for (int j = 0; j < NW; ++j) myA[(r * NW + j) * kPropThreads] = w[j];
+        for (int j = 0; j < NW; ++j) sAw[(r * NW + j) * kPropThreads + threadIdx.x] = w[j];
+      }
     }
-    for (int grp = 0; grp < ngroups; ++grp) {
-      int cy[G], cx[G], ssd[G];
+    const int b0y = start / B.ncols, b0x = start - b0y * B.ncols;
+    // the candidate list: every slot's live candidates, warp counts, one scan, then slot g's
+    // entries of warp w follow those of warps < w, after all entries of slots < g
+    int cand[kPropSlots];
+    unsigned live[kPropSlots];
 #pragma unroll
-      for (int g = 0; g < G; ++g) {
-        cy[g] = -1;
-        cx[g] = 0;
-        int by, bx;
-        if (grp == 0 && g < 4) {
+    for (int g = 0; g < kPropSlots; ++g) {
+      cand[g] = -1;
+      if (have && g < slots) {
+        int by = -1, bx = 0;
+        if (g < 4) {
           const int ddy = g == 0 ? -1 : g == 1 ? 1 : 0, ddx = g == 2 ? -1 : g == 3 ? 1 : 0;
           const int ny = y + ddy * jump, nx = x + ddx * jump;
-          if (ny < 0 || nx < 0 || ny >= na_rows || nx >= A.ncols) continue;
-          const int nb = in.idx[ny * A.ncols + nx];
-          if (nb < 0) continue;
-          const int nby = nb / B.ncols;
-          by = nby - ddy * jump;
-          bx = nb - nby * B.ncols - ddx * jump;
+          if (ny >= 0 && nx >= 0 && ny < na_rows && nx < A.ncols && !(chg_in && !chg_in[ny * A.ncols + nx])) {
+            const int nb = in.idx[ny * A.ncols + nx];
+            if (nb >= 0) {
+              const int nby = nb / B.ncols;
+              by = nby - ddy * jump;
+              bx = nb - nby * B.ncols - ddx * jump;
+            }
+          }
         } else {
-          const int t = grp == 0 ? g - 4 : (G - 4) + (grp - 1) * G + g;
-          if (t >= nr) continue;
-          const uint32_t rr = hash3(seed, (uint32_t)i, (uint32_t)t);
+          const uint32_t rr = hash3(seed, (uint32_t)i, (uint32_t)(g - 4));
           by = b0y + (int)((rr >> 16) % (2 * radius + 1)) - radius;
           bx = b0x + (int)(rr % (2 * radius + 1)) - radius;
         }
-        if (by < 0 || bx < 0 || by >= nb_rows || bx >= B.ncols || by * B.ncols + bx == best) continue;
-        cy[g] = by;
-        cx[g] = bx;
+        if (by >= 0 && bx >= 0 && by < nb_rows && bx < B.ncols) {
+          const int c = by * B.ncols + bx;
+          bool repeat = c == start;
+#pragma unroll
+          for (int e = 0; e < g; ++e) repeat |= cand[e] == c;
+          if (!repeat) cand[g] = c;
+        }
       }
-      ssd_group_s<PS, RL, G>(myA, kPropThreads, B, cy, cx, bs, ssd);
-      take_best<G>(cy, cx, ssd, B.ncols, best, bs);
+      live[g] = __ballot_sync(0xffffffffu, cand[g] >= 0);
+      if (lane == 0 && g < slots) swcnt[g][warp] = __popc(live[g]);
     }
-    out.idx[i] = best;
-    out.ssd[i] = bs;
+    __syncthreads();
+    int base = 0;
+#pragma unroll
+    for (int g = 0; g < kPropSlots; ++g) {
+      if (g >= slots) break;
+      int off = base, tot = 0;
+#pragma unroll
+      for (int w = 0; w < kWarps; ++w) {
+        const int c = swcnt[g][w];
+        off += w < warp ? c : 0;
+        tot += c;
+      }
+      if (cand[g] >= 0) {
+        const int pos = off + __popc(live[g] & lt_mask);
+        sjob[pos] = cand[g];
+        sjp[pos] = (unsigned char)threadIdx.x;
+      }
+      base += tot;
+    }
+    __syncthreads();
+    // the listed candidates, kPropGroup per thread at a time (a warp's are consecutive entries)
+    const int njob = base;
+    for (int j0 = warp * 32 + lane; j0 < njob; j0 += G * kPropThreads) {
+      int cy[G], cx[G], pj[G], lim[G], ssd[G];
+#pragma unroll
+      for (int u = 0; u < G; ++u) {
+        const int j = j0 + u * kPropThreads;
+        cy[u] = -1;
+        cx[u] = 0;
+        pj[u] = 0;
+        lim[u] = 0;
+        if (j < njob) {
+          const int c = sjob[j];
+          pj[u] = sjp[j];
+          cy[u] = c / B.ncols;
+          cx[u] = c - cy[u] * B.ncols;
+          // the pixel's best so far (no better than its final best): a candidate whose partial
+          // sum passes it cannot win
+          lim[u] = (int)(*(volatile unsigned long long*)&sbest[pj[u]] >> 32);
+        }
+      }
+      ssd_jobs<PS, RL, G>(sAw, kPropThreads, pj, B, cy, cx, lim, ssd);
+#pragma unroll
+      for (int u = 0; u < G; ++u)
+        if (cy[u] >= 0 && ssd[u] <= lim[u])
+          atomicMin(&sbest[pj[u]], ((unsigned long long)(unsigned)ssd[u] << 32) | (unsigned)(cy[u] * B.ncols + cx[u]));
+    }
+    __syncthreads();
+    if (have) {
+      const unsigned long long k = sbest[threadIdx.x];
+      const int best = (int)(unsigned)(k & 0xffffffffu);
+      out.idx[i] = best;
+      out.ssd[i] = (int)(k >> 32);
+      if (chg_out) chg_out[i] = best != start;
+    }
+    __syncthreads();
   }
 }
 
@@ -467,19 +606,26 @@ int fast_search(annf_handle* h, const uint8_t* img_a, int ha, int wa, const uint
   Img A{img_a, ha, wa, c, psize, wa - psize + 1, (long long)ha * wa * c};
   Img B{img_b, hb, wb, c, psize, wb - psize + 1, (long long)hb * wb * c};
   const int nA = (ha - psize + 1) * A.ncols;
-  ANNF_ENSURE(h->fast_buf, (size_t)4 * nA * sizeof(int));
+  ANNF_ENSURE(h->fast_buf, (size_t)4 * nA * sizeof(int) + (size_t)2 * nA);
   int* base = h->fast_buf.as<int>();
   Match m0{base, base + nA}, m1{base + 2 * (size_t)nA, base + 3 * (size_t)nA};
+  // per-pixel "match changed" flags of the previous pass and of this one (none before pass 1:
+  // the initial choice tried no neighbour candidates)
+  uint8_t* chg[2] = {reinterpret_cast<uint8_t*>(base + 4 * (size_t)nA),
+                     reinterpret_cast<uint8_t*>(base + 4 * (size_t)nA) + nA};
   const int blocks = (int)std::min<long long>(ceil_div(nA, 256), 32LL * num_sms());
   // shape-specialised kernels for the common patches, the generic ones otherwise
   const int shape = psize * 100 + psize * c;
   const bool special = shape == 927 || shape == 721 || shape == 515 || shape == 1133;
+  // the listing pass holds up to kPropSlots - 4 random offsets per pixel; more go to the generic pass
+  const bool listed = special && rand_samples <= kPropSlots - 4;
+  const int prop_blocks = blocks;
 #define ANNF_FAST_INIT(PS, RL) fast_init_t_kernel<PS, RL><<<blocks, 256, 0, st>>>(A, B, nA, K, nat_pos, h->perm.as<int>(), prop, n_prop, seed_match, m0)
 #define ANNF_FAST_PROP(PS, RL, ...)                                                                     \
   do {                                                                                                  \
-    const size_t sm = (size_t)(PS) * (((RL) + 3) / 4) * kPropThreads * sizeof(unsigned);                \
+    const size_t sm = prop_smem(PS, ((RL) + 3) / 4, rand_samples);                                    \
     ANNF_CUDA_TRY(cudaFuncSetAttribute(fast_prop_t_kernel<PS, RL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm)); \
-    fast_prop_t_kernel<PS, RL><<<blocks, kPropThreads, sm, st>>>(__VA_ARGS__);                          \
+    fast_prop_t_kernel<PS, RL><<<prop_blocks, kPropThreads, sm, st>>>(__VA_ARGS__);                     \
   } while (0)
   switch (shape) {
     case 927: ANNF_FAST_INIT(9, 27); break;
@@ -495,15 +641,17 @@ int fast_search(annf_handle* h, const uint8_t* img_a, int ha, int wa, const uint
     const int jump = 1;
     const int radius = std::max(1, radius0 >> it);
     const uint32_t sd = seed * 7919u + (uint32_t)it;
-    if (special) {
+    const uint8_t* cin = it == 0 ? nullptr : chg[(it - 1) & 1];
+    uint8_t* cout = chg[it & 1];
+    if (listed) {
       switch (shape) {
-        case 927: ANNF_FAST_PROP(9, 27, A, B, nA, jump, radius, rand_samples, sd, m0, m1); break;
-        case 721: ANNF_FAST_PROP(7, 21, A, B, nA, jump, radius, rand_samples, sd, m0, m1); break;
-        case 515: ANNF_FAST_PROP(5, 15, A, B, nA, jump, radius, rand_samples, sd, m0, m1); break;
-        default: ANNF_FAST_PROP(11, 33, A, B, nA, jump, radius, rand_samples, sd, m0, m1); break;
+        case 927: ANNF_FAST_PROP(9, 27, A, B, nA, jump, radius, rand_samples, sd, m0, m1, cin, cout); break;
+        case 721: ANNF_FAST_PROP(7, 21, A, B, nA, jump, radius, rand_samples, sd, m0, m1, cin, cout); break;
+        case 515: ANNF_FAST_PROP(5, 15, A, B, nA, jump, radius, rand_samples, sd, m0, m1, cin, cout); break;
+        default: ANNF_FAST_PROP(11, 33, A, B, nA, jump, radius, rand_samples, sd, m0, m1, cin, cout); break;
       }
     } else {
-      fast_prop_kernel<<<blocks, 256, 0, st>>>(A, B, nA, jump, radius, rand_samples, sd, m0, m1);
+      fast_prop_kernel<<<blocks, 256, 0, st>>>(A, B, nA, jump, radius, rand_samples, sd, m0, m1, cin, cout);
     }
     ANNF_CHECK_LAUNCH();
     std::swap(m0, m1);

@@ -48,3 +48,49 @@ def test_parallel_form_other_leaf_precisions(gpu_lib, leaf_precision):
     ref = ANNFieldPropKDTreeGB300(leaf_precision="bf16", **kw).fit(a, b)
     got = ANNFieldPropKDTreeGB300(leaf_precision=leaf_precision, **kw).fit(a, b)
     assert np.array_equal(ref, got)
+
+
+class _RandomProposals:
+    """Fixed random B indices as offset proposals (some -1 = none), passed in as candidates."""
+
+    def __init__(self, n_prop, rng_seed):
+        self.n_prop, self.rng_seed = n_prop, rng_seed
+        self.last = None
+
+    def propose(self, A, B, psize):
+        import torch
+        n_a = (A.shape[0] - psize + 1) * (A.shape[1] - psize + 1)
+        n_b = (B.shape[0] - psize + 1) * (B.shape[1] - psize + 1)
+        rng = np.random.default_rng(self.rng_seed)
+        p = rng.integers(-1, n_b, (n_a, self.n_prop)).astype(np.int32)
+        self.last = p
+        return torch.from_numpy(p).to(A.device)
+
+
+@pytest.mark.parametrize("psize,ha,wa,hb,wb,iters,n_prop", [
+    (9, 160, 160, 160, 160, 3, 0),    # the headline patch (specialised 9x27-byte kernels)
+    (7, 150, 170, 161, 143, 4, 2),    # uneven sizes, proposals in the initial choice
+    (6, 120, 128, 128, 120, 3, 1),    # a patch without a specialised kernel (generic kernels)
+])
+def test_parallel_search_matches_restatement(gpu_lib, psize, ha, wa, hb, wb, iters, n_prop):
+    """The parallel form's NNF and distances equal the CPU restatement of its search
+    (oracle/parallel.py) started from the same natural-leaf neighbours: the initial choice and
+    every propagation / random-search pass, index for index. Candidates the GPU does not load
+    (repeats, neighbours unchanged since the previous pass) cannot change this result."""
+    from annfmp_gb300 import ANNFieldPropKDTreeGB300, gen
+    from oracle import parallel as PR
+    rng = np.random.default_rng(psize)
+    a = gen.spectral_noise(ha, wa, rng)
+    b = gen.flow_warp(gen.spectral_noise(max(ha, hb), max(wa, wb), np.random.default_rng(psize))[:hb, :wb],
+                      4.0, 16.0, 4.0, rng)
+    prop = _RandomProposals(n_prop, 5) if n_prop else None
+    k = 4
+    m = ANNFieldPropKDTreeGB300(n_neighbors=k, psize=psize, dim_reduced=8, n_subset=4000, leaf_size=32, seed=3,
+                                verbose=0, form="parallel", iters=iters, graph=False, proposal=prop)
+    nn = m.fit(a, b)
+    nat = m.kdtree.natural_kneighbors(m.patches_a_reduced_, k, "bf16").cpu().numpy()
+    want, ssd = PR.parallel_search(a, b, psize, nat, proposals=prop.last if prop else None, iters=iters,
+                                   seed=3, nrand=m.search[0], radius0=m.search[1])
+    assert np.array_equal(nn, want), float((nn == want).mean())
+    got_d = m.nn_distances_.cpu().numpy()
+    assert np.array_equal(got_d, np.sqrt(ssd.astype(np.float32)))
