@@ -352,13 +352,17 @@ __device__ __forceinline__ void ssd_group_s(const unsigned* __restrict__ sa, int
   for (int g = 0; g < G; ++g) out[g] = cy[g] < 0 ? 0x7fffffff : (int)s[g];
 }
 
-// exact SSDs of G listed candidates, each against its own pixel's A patch in shared memory
-// (column pj[g] of sa, word j of patch row r at sa[(r * NW + j) * stride + pj[g]]); a candidate
-// stops once its partial sum exceeds lim[g] (its value is then > lim[g])
+// exact SSDs of G listed candidates, each against its own pixel's A patch, read from the CTA's A
+// strip in shared memory: strip row r holds image row y + r from the tile's first pixel on as
+// aligned words (its first byte at offset delta_r = row start & 3 of word 0), so pixel p's patch
+// row starts at byte delta_r + p * c and its words are funnel shifts of neighbouring strip words.
+// A candidate stops once its partial sum exceeds lim[g] (its value is then > lim[g]).
 template <int PS, int RL, int G>
-__device__ __forceinline__ void ssd_jobs(const unsigned* __restrict__ sa, int stride, const int (&pj)[G], const Img& B,
-                                         const int (&cy)[G], const int (&cx)[G], const int (&lim)[G], int (&out)[G]) {
+__device__ __forceinline__ void ssd_jobs(const unsigned* __restrict__ strip, int sw, long long row0, long long rstep,
+                                         int c, const int (&pj)[G], const Img& B, const int (&cy)[G],
+                                         const int (&cx)[G], const int (&lim)[G], int (&out)[G]) {
   constexpr int NW = (RL + 3) / 4;
+  constexpr unsigned kLastMask = (RL % 4) ? (1u << (8 * (RL % 4))) - 1u : 0xffffffffu;
   unsigned s[G];
   bool live[G];
 #pragma unroll
@@ -376,13 +380,21 @@ __device__ __forceinline__ void ssd_jobs(const unsigned* __restrict__ sa, int st
 #pragma unroll
     for (int g = 0; g < G; ++g)
       if (live[g]) row_words<RL>(B.p, ((long long)(cy[g] + r) * B.w + cx[g]) * B.c, B.bytes, bw[g]);
+    const int delta = (int)((row0 + r * rstep) & 3);
 #pragma unroll
     for (int g = 0; g < G; ++g) {
       if (!live[g]) continue;
-      const unsigned* a = sa + r * NW * stride + pj[g];
+      const int o = delta + pj[g] * c;
+      const unsigned* a = strip + r * sw + (o >> 2);
+      const int sh = (o & 3) * 8;
+      unsigned lo = a[0];
 #pragma unroll
       for (int j = 0; j < NW; ++j) {
-        const unsigned dd = __vabsdiffu4(a[j * stride], bw[g][j]);
+        const unsigned hi = a[j + 1];
+        unsigned aw = __funnelshift_r(lo, hi, sh);
+        if (j == NW - 1) aw &= kLastMask;
+        lo = hi;
+        const unsigned dd = __vabsdiffu4(aw, bw[g][j]);
         s[g] = __dp4a(dd, dd, s[g]);
       }
       if ((int)s[g] > lim[g]) live[g] = false;
@@ -396,10 +408,16 @@ constexpr int kPropThreads = 256;
 constexpr int kPropGroup = 4;  // listed candidates per thread at a time
 constexpr int kPropSlots = 6;  // candidate slots per pixel of the listing pass: 4 neighbours + up to 2 random offsets
 
-// dynamic shared memory of fast_prop_t_kernel: best keys, aligned A patches, the candidate list
-static size_t prop_smem(int ps, int nw, int nrand) {
-  return (size_t)kPropThreads * (sizeof(unsigned long long) + (size_t)ps * nw * sizeof(unsigned) +
-                                 (size_t)(4 + nrand) * (sizeof(int) + 1));
+// words per A strip row of fast_prop_t_kernel: a tile's kPropThreads patches of psize pixels of c
+// bytes from an unaligned start, plus a word of slack for the funnel shifts
+__host__ __device__ __forceinline__ int prop_strip_words(int psize, int c) {
+  return ((kPropThreads + psize - 1) * c + 3) / 4 + 3;
+}
+
+// dynamic shared memory of fast_prop_t_kernel: best keys, the A strip, the candidate list
+static size_t prop_smem(int ps, int c, int nrand) {
+  return (size_t)kPropThreads * (sizeof(unsigned long long) + (size_t)(4 + nrand) * (sizeof(int) + 1)) +
+         (size_t)ps * prop_strip_words(ps, c) * sizeof(unsigned);
 }
 
 // seed (optional, [2 nA]: B index, then SSD): a match to start from, e.g. the best proposal found
@@ -437,52 +455,63 @@ __global__ void __launch_bounds__(256, 3) fast_init_t_kernel(Img A, Img B, int n
 }
 
 // one pass: the four neighbours' matches at distance 'jump', shifted to this pixel, and 'nrand'
-// random offsets around the pass's starting match within 'radius'. A CTA takes 256 consecutive
-// pixels: each thread aligns its pixel's A patch into shared memory and lists the candidates that
-// can change the result (not the starting match, not a repeat of an earlier candidate of the
-// pixel, with chg_in not a neighbour whose match did not change in the previous pass:
-// fast_prop_kernel); the CTA then works through the listed candidates, kPropGroup per thread at a
-// time. The list is slot-major (every pixel's "up" candidate, then every "down", ..., then the
-// random offsets), so the 32 candidates of a warp come from neighbouring pixels and the same
-// direction, and their B rows share cache lines as they would in a thread-per-pixel pass, while
-// no lane idles on a candidate it does not have. Each candidate folds (SSD, index) into its
-// pixel's 64-bit best key with atomicMin: the lexicographic minimum, the same result as trying the
-// candidates one by one.
+// random offsets around the pass's starting match within 'radius'. A CTA takes a tile of up to
+// kPropThreads pixels of one row: it stages the tile's A strip (the psize image rows under the
+// tile, aligned words) in shared memory, and each thread lists its pixel's candidates that can
+// change the result (not the starting match, not a repeat of an earlier candidate of the pixel,
+// with chg_in not a neighbour whose match did not change in the previous pass: fast_prop_kernel).
+// The CTA then works through the listed candidates, kPropGroup per thread at a time. The list is
+// slot-major (every pixel's "up" candidate, then every "down", ..., then the random offsets), so
+// the 32 candidates of a warp come from neighbouring pixels and the same direction, and their B
+// rows share cache lines as they would in a thread-per-pixel pass, while no lane idles on a
+// candidate it does not have. Each candidate folds (SSD, index) into its pixel's 64-bit best key
+// with atomicMin: the lexicographic minimum, the same result as trying the candidates one by one.
 template <int PS, int RL>
 __global__ void __launch_bounds__(kPropThreads, 3) fast_prop_t_kernel(Img A, Img B, int nA, int jump, int radius,
                                                                    int nrand, uint32_t seed, Match in, Match out,
                                                                    const uint8_t* __restrict__ chg_in,
                                                                    uint8_t* __restrict__ chg_out) {
-  constexpr int NW = (RL + 3) / 4;
   constexpr int G = kPropGroup;
   constexpr int kWarps = kPropThreads / 32;
   extern __shared__ unsigned long long sdyn[];
-  unsigned long long* sbest = sdyn;                                      // [kPropThreads]
-  unsigned* sAw = reinterpret_cast<unsigned*>(sbest + kPropThreads);     // [PS * NW][kPropThreads]
-  int* sjob = reinterpret_cast<int*>(sAw + PS * NW * kPropThreads);      // [slots * kPropThreads]
-  unsigned char* sjp = reinterpret_cast<unsigned char*>(sjob + (4 + nrand) * kPropThreads);
+  const int sw = prop_strip_words(PS, A.c);
+  unsigned long long* sbest = sdyn;                                        // [kPropThreads]
+  int* sjob = reinterpret_cast<int*>(sbest + kPropThreads);                // [slots * kPropThreads]
+  unsigned* strip = reinterpret_cast<unsigned*>(sjob + (4 + nrand) * kPropThreads);  // [PS][sw]
+  unsigned char* sjp = reinterpret_cast<unsigned char*>(strip + PS * sw);  // [slots * kPropThreads]
   __shared__ int swcnt[kPropSlots][kWarps];
   const int nb_rows = B.h - B.psize + 1, na_rows = nA / A.ncols;
   const int nr = radius > 0 ? min(nrand, kPropSlots - 4) : 0;
   const int slots = 4 + nr;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const unsigned lt_mask = (1u << lane) - 1u;
-  for (long long tile = (long long)blockIdx.x * kPropThreads; tile < nA; tile += (long long)gridDim.x * kPropThreads) {
-    const int i = (int)tile + threadIdx.x;
-    const bool have = i < nA;
-    int start = -1, y = 0, x = 0;
+  const int tpr = (A.ncols + kPropThreads - 1) / kPropThreads;  // tiles per row
+  const long long ntiles = (long long)na_rows * tpr;
+  const long long rstep = (long long)A.w * A.c;
+  for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const int y = (int)(tile / tpr), x0 = (int)(tile - (long long)y * tpr) * kPropThreads;
+    const int x = x0 + threadIdx.x;
+    const bool have = x < A.ncols;
+    const int i = y * A.ncols + x;
+    const long long row0 = ((long long)y * A.w + x0) * A.c;  // strip row 0's first byte
+    // the A strip: aligned words of rows y .. y + PS - 1 from the tile's first pixel on
+    for (int e = threadIdx.x; e < PS * sw; e += kPropThreads) {
+      const int r = e / sw, w = e - r * sw;
+      const long long a = ((row0 + r * rstep) & ~3LL) + 4LL * w;
+      unsigned v = 0;
+      if (a + 4 <= A.bytes) {
+        v = __ldg(reinterpret_cast<const unsigned*>(A.p + a));
+      } else {
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+          if (a + u < A.bytes) v |= (unsigned)__ldg(A.p + a + u) << (8 * u);
+      }
+      strip[e] = v;
+    }
+    int start = -1;
     if (have) {
-      y = i / A.ncols;
-      x = i - y * A.ncols;
       start = in.idx[i];
       sbest[threadIdx.x] = ((unsigned long long)(unsigned)in.ssd[i] << 32) | (unsigned)start;
-#pragma unroll 1
-      for (int r = 0; r < PS; ++r) {
-        unsigned w[NW];
-        row_words<RL>(A.p, ((long long)(y + r) * A.w + x) * A.c, A.bytes, w);
-#pragma unroll
-        for (int j = 0; j < NW; ++j) sAw[(r * NW + j) * kPropThreads + threadIdx.x] = w[j];
-      }
     }
     const int b0y = start / B.ncols, b0x = start - b0y * B.ncols;
     // the candidate list: every slot's live candidates, warp counts, one scan, then slot g's
@@ -562,7 +591,7 @@ __global__ void __launch_bounds__(kPropThreads, 3) fast_prop_t_kernel(Img A, Img
           lim[u] = (int)(*(volatile unsigned long long*)&sbest[pj[u]] >> 32);
         }
       }
-      ssd_jobs<PS, RL, G>(sAw, kPropThreads, pj, B, cy, cx, lim, ssd);
+      ssd_jobs<PS, RL, G>(strip, sw, row0, rstep, A.c, pj, B, cy, cx, lim, ssd);
 #pragma unroll
       for (int u = 0; u < G; ++u)
         if (cy[u] >= 0 && ssd[u] <= lim[u])
@@ -619,11 +648,12 @@ int fast_search(annf_handle* h, const uint8_t* img_a, int ha, int wa, const uint
   const bool special = shape == 927 || shape == 721 || shape == 515 || shape == 1133;
   // the listing pass holds up to kPropSlots - 4 random offsets per pixel; more go to the generic pass
   const bool listed = special && rand_samples <= kPropSlots - 4;
-  const int prop_blocks = blocks;
+  const long long prop_tiles = (long long)(ha - psize + 1) * ceil_div(A.ncols, kPropThreads);
+  const int prop_blocks = (int)std::min<long long>(prop_tiles, 32LL * num_sms());
 #define ANNF_FAST_INIT(PS, RL) fast_init_t_kernel<PS, RL><<<blocks, 256, 0, st>>>(A, B, nA, K, nat_pos, h->perm.as<int>(), prop, n_prop, seed_match, m0)
 #define ANNF_FAST_PROP(PS, RL, ...)                                                                     \
   do {                                                                                                  \
-    const size_t sm = prop_smem(PS, ((RL) + 3) / 4, rand_samples);                                    \
+    const size_t sm = prop_smem(PS, c, rand_samples);                                    \
     ANNF_CUDA_TRY(cudaFuncSetAttribute(fast_prop_t_kernel<PS, RL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm)); \
     fast_prop_t_kernel<PS, RL><<<prop_blocks, kPropThreads, sm, st>>>(__VA_ARGS__);                     \
   } while (0)
