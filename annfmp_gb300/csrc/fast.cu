@@ -311,47 +311,6 @@ __device__ __forceinline__ void take_best(const int (&cy)[G], const int (&cx)[G]
 
 constexpr int kGroup = 4;  // candidates evaluated together (initial choice)
 
-// ssd_group with the A patch already word-aligned in shared memory: word j of patch row r at
-// sa[(r * NW + j) * stride] (one column per thread, so a warp's reads hit 32 banks)
-template <int PS, int RL, int G>
-__device__ __forceinline__ void ssd_group_s(const unsigned* __restrict__ sa, int stride, const Img& B,
-                                            const int (&cy)[G], const int (&cx)[G], int limit, int (&out)[G]) {
-  constexpr int NW = (RL + 3) / 4;
-  unsigned s[G];
-  bool live[G];
-#pragma unroll
-  for (int g = 0; g < G; ++g) {
-    s[g] = 0;
-    live[g] = cy[g] >= 0;
-  }
-#pragma unroll 1
-  for (int r = 0; r < PS; ++r) {
-    bool any = false;
-#pragma unroll
-    for (int g = 0; g < G; ++g) any |= live[g];
-    if (!any) break;
-    unsigned bw[G][NW];
-#pragma unroll
-    for (int g = 0; g < G; ++g)
-      if (live[g]) row_words<RL>(B.p, ((long long)(cy[g] + r) * B.w + cx[g]) * B.c, B.bytes, bw[g]);
-    unsigned aw[NW];
-#pragma unroll
-    for (int j = 0; j < NW; ++j) aw[j] = sa[(r * NW + j) * stride];
-#pragma unroll
-    for (int g = 0; g < G; ++g) {
-      if (!live[g]) continue;
-#pragma unroll
-      for (int j = 0; j < NW; ++j) {
-        const unsigned dd = __vabsdiffu4(aw[j], bw[g][j]);
-        s[g] = __dp4a(dd, dd, s[g]);
-      }
-      if ((int)s[g] > limit) live[g] = false;
-    }
-  }
-#pragma unroll
-  for (int g = 0; g < G; ++g) out[g] = cy[g] < 0 ? 0x7fffffff : (int)s[g];
-}
-
 // exact SSDs of G listed candidates, each against its own pixel's A patch, read from the CTA's A
 // strip in shared memory: strip row r holds image row y + r from the tile's first pixel on as
 // aligned words (its first byte at offset delta_r = row start & 3 of word 0), so pixel p's patch

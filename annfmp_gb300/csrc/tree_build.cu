@@ -23,8 +23,9 @@
 
 namespace annf {
 
+int num_sms();
+
 constexpr int kChunk = 2048;     // positions per CTA in the global levels
-constexpr int kMaxFusedD = 128;  // dimensions for which the scatter also computes the children's boxes
 constexpr int kThreads = 256;
 constexpr int kItems = kChunk / kThreads;
 
@@ -60,36 +61,86 @@ __global__ void iota_kernel(int* a, int n) {
 // ---------------------------------------------------------------------------------------------
 // global levels
 // ---------------------------------------------------------------------------------------------
-// bounding box: threads are laid out so that each one always reads the same dimension
+// Between the input and the finisher the points are column-major ([d][n]): a level reads its
+// split coordinate as one contiguous column, and the scatter moves columns.
+//
+// row-major [n][d] -> column-major [d][n] through shared memory (tile rows of stride d | 1), and
+// the bounding box of all points as order keys (level 0's box): a reading thread always reads the
+// same dimension
 template <typename T>
-__global__ void bbox_kernel(int n, int d, int t, int B, const T* __restrict__ pts,
-                            typename key_of<T>::type* gmin, typename key_of<T>::type* gmax) {
+__host__ __device__ __forceinline__ int col_tile_rows(int d) {
+  const int r = 16384 / ((d | 1) * (int)sizeof(T));
+  return r < 32 ? 32 : (r > 256 ? 256 : r);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kThreads) to_columns_kernel(int n, int d, const T* __restrict__ in,
+                                                              T* __restrict__ out, typename key_of<T>::type* gmin,
+                                                              typename key_of<T>::type* gmax) {
   using K = typename key_of<T>::type;
-  __shared__ K smin[kThreads], smax[kThreads];
-  const int s = blockIdx.x / B, bb = blockIdx.x % B;
-  int lo, hi;
-  seg_range(n, t, s, lo, hi);
-  const int c0 = lo + bb * kChunk, c1 = min(hi, c0 + kChunk);
-  const int used = (kThreads / d) * d;  // stride that keeps each thread on one dimension
+  extern __shared__ __align__(16) unsigned char csm[];
+  T* tile = reinterpret_cast<T*>(csm);
+  const int rows = col_tile_rows<T>(d), ds = d | 1;
+  const int per = kThreads / d, used = per * d;  // readers: thread t reads dimension t % d of rows t / d + k * per
+  const int rj = (int)threadIdx.x % d, rr = (int)threadIdx.x / d;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   K kmn = key_max<K>(), kmx = 0;
-  if ((int)threadIdx.x < used && c0 < c1) {
-    const long long e0 = (long long)c0 * d, e1 = (long long)c1 * d;
-    for (long long e = e0 + threadIdx.x; e < e1; e += used) {
-      K k = ord_key(pts[e]);
-      kmn = k < kmn ? k : kmn;
-      kmx = k > kmx ? k : kmx;
+  for (long long r0 = (long long)blockIdx.x * rows; r0 < n; r0 += (long long)gridDim.x * rows) {
+    const int m = (int)(n - r0 < rows ? n - r0 : rows);
+    if ((int)threadIdx.x < used) {
+      const T* src = in + r0 * d + rj;
+#pragma unroll 4
+      for (int r = rr; r < m; r += per) {
+        const T v = src[(long long)r * d];
+        tile[r * ds + rj] = v;
+        const K k = (K)ord_key(v);
+        kmn = k < kmn ? k : kmn;
+        kmx = k > kmx ? k : kmx;
+      }
     }
+    __syncthreads();
+    for (int j = warp; j < d; j += kThreads / 32) {
+      T* dst = out + (long long)j * n + r0;
+#pragma unroll 4
+      for (int r = lane; r < m; r += 32) dst[r] = tile[r * ds + j];
+    }
+    __syncthreads();
   }
+  __shared__ K smin[kThreads], smax[kThreads];
   smin[threadIdx.x] = kmn;
   smax[threadIdx.x] = kmx;
   __syncthreads();
-  if ((int)threadIdx.x < d && c0 < c1) {
+  if ((int)threadIdx.x < d) {
     for (int u = threadIdx.x + d; u < used; u += d) {
       kmn = smin[u] < kmn ? smin[u] : kmn;
       kmx = smax[u] > kmx ? smax[u] : kmx;
     }
-    atomicMin(&gmin[(long long)s * d + threadIdx.x], kmn);
-    atomicMax(&gmax[(long long)s * d + threadIdx.x], kmx);
+    if (kmn != key_max<K>()) atomicMin(&gmin[threadIdx.x], kmn);
+    if (kmx != (K)0) atomicMax(&gmax[threadIdx.x], kmx);
+  }
+}
+
+// column-major [d][n] -> row-major [n][d] (the leaves when no level fits the finisher)
+template <typename T>
+__global__ void __launch_bounds__(kThreads) to_rows_kernel(int n, int d, const T* __restrict__ in, T* __restrict__ out) {
+  extern __shared__ __align__(16) unsigned char csm[];
+  T* tile = reinterpret_cast<T*>(csm);
+  const int rows = col_tile_rows<T>(d), ds = d | 1;
+  const int per = kThreads / d, used = per * d;
+  const int rj = (int)threadIdx.x % d, rr = (int)threadIdx.x / d;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (long long r0 = (long long)blockIdx.x * rows; r0 < n; r0 += (long long)gridDim.x * rows) {
+    const int m = (int)(n - r0 < rows ? n - r0 : rows);
+    for (int j = warp; j < d; j += kThreads / 32) {
+      const T* src = in + (long long)j * n + r0;
+      for (int r = lane; r < m; r += 32) tile[r * ds + j] = src[r];
+    }
+    __syncthreads();
+    if ((int)threadIdx.x < used) {
+      T* dst = out + r0 * d + rj;
+      for (int r = rr; r < m; r += per) dst[(long long)r * d] = tile[r * ds + rj];
+    }
+    __syncthreads();
   }
 }
 
@@ -161,7 +212,7 @@ __global__ void hist_kernel(int n, int d, int t, int B, int shift, int width, bo
   for (int q = 0; q < kItems; ++q) {
     const int i = c0 + (int)threadIdx.x + q * kThreads;
     kv[q] = 0;
-    if (i < c1) kv[q] = extract ? (K)ord_key(pts[(long long)i * d + ax]) : keys[i];
+    if (i < c1) kv[q] = extract ? (K)ord_key(pts[(long long)ax * n + i]) : keys[i];
   }
 #pragma unroll
   for (int q = 0; q < kItems; ++q) {
@@ -351,115 +402,65 @@ __global__ void __launch_bounds__(kThreads) scatter_kernel(
     }
   }
   __syncthreads();
-  // rows move whole: a group of lanes per row, 16-byte words when rows allow it
-  if (sizeof(T) == 4 && (d & 3) == 0) {
-    const int w = d >> 2;  // float4 words per row
-    const float4* src = reinterpret_cast<const float4*>(pts_in) + (long long)c0 * w;
-    float4* dst4 = reinterpret_cast<float4*>(pts_out);
-    if (cmin == nullptr) {
-      for (int e0 = threadIdx.x; e0 < m * w; e0 += 4 * kThreads) {
-        float4 v[4];
+  // the columns move one at a time, a warp per column, lanes on consecutive positions (coalesced
+  // reads; a warp's writes fall in the two runs of its children). With cmin, the children's
+  // bounding boxes on the way, as order keys (the same keys as to_columns_kernel's)
+  constexpr int kU = 8;  // loads in flight per lane
+  const int lane = threadIdx.x & 31;
+  for (int j = threadIdx.x >> 5; j < d; j += kThreads / 32) {
+    const T* src = pts_in + (long long)j * n + c0;
+    T* dcol = pts_out + (long long)j * n;
+    K mn0 = key_max<K>(), mx0 = (K)0, mn1 = key_max<K>(), mx1 = (K)0;
+    bool h0 = false, h1 = false;
+    for (int r0 = lane; r0 < m; r0 += 32 * kU) {
+      T v[kU];
 #pragma unroll
-        for (int u = 0; u < 4; ++u)
-          if (e0 + u * kThreads < m * w) v[u] = src[e0 + u * kThreads];
+      for (int u = 0; u < kU; ++u)
+        if (r0 + 32 * u < m) v[u] = src[r0 + 32 * u];
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
-          const int e = e0 + u * kThreads;
-          if (e < m * w) {
-            const int r = e / w, c = e - r * w;
-            dst4[(long long)sdst[r] * w + c] = v[u];
-          }
-        }
-      }
-    } else {
-      // the children's bounding boxes on the way: a thread always handles word c = tid mod w
-      // (w divides the block), keeping its four coordinates' minima and maxima per child as
-      // floats (branch-free: the other child's update sees +-inf); order keys only at the end
-      float fmn[2][4], fmx[2][4];
-#pragma unroll
-      for (int u = 0; u < 2; ++u)
-#pragma unroll
-        for (int j = 0; j < 4; ++j) {
-          fmn[u][j] = __int_as_float(0x7f800000);
-          fmx[u][j] = -__int_as_float(0x7f800000);
-        }
-      bool has[2] = {false, false};  // (infinite coordinates are valid points: no sentinel test)
-      // four words per thread per round, their loads issued together (w divides the block, so
-      // every word of a thread is word tid mod w of its row)
-      for (int e0 = threadIdx.x; e0 < m * w; e0 += 4 * kThreads) {
-        float4 v4[4];
-#pragma unroll
-        for (int u = 0; u < 4; ++u)
-          if (e0 + u * kThreads < m * w) v4[u] = src[e0 + u * kThreads];
-#pragma unroll
-        for (int u = 0; u < 4; ++u) {
-          const int e = e0 + u * kThreads;
-          if (e < m * w) {
-            const int r = e / w, c = e - r * w;
-            const float4 v = v4[u];
-            dst4[(long long)sdst[r] * w + c] = v;
-            const bool rt = sside[r] != 0;
-            has[0] |= !rt;
-            has[1] |= rt;
-            const float inf = __int_as_float(0x7f800000);
-            const float vv[4] = {v.x, v.y, v.z, v.w};
-#pragma unroll
-            for (int j = 0; j < 4; ++j) {
-              fmn[0][j] = fminf(fmn[0][j], rt ? inf : vv[j]);
-              fmx[0][j] = fmaxf(fmx[0][j], rt ? -inf : vv[j]);
-              fmn[1][j] = fminf(fmn[1][j], rt ? vv[j] : inf);
-              fmx[1][j] = fmaxf(fmx[1][j], rt ? vv[j] : -inf);
+      for (int u = 0; u < kU; ++u) {
+        const int r = r0 + 32 * u;
+        if (r < m) {
+          dcol[sdst[r]] = v[u];
+          if (cmin != nullptr) {
+            const K k = (K)ord_key(v[u]);
+            if (sside[r]) {
+              h1 = true;
+              mn1 = k < mn1 ? k : mn1;
+              mx1 = k > mx1 ? k : mx1;
+            } else {
+              h0 = true;
+              mn0 = k < mn0 ? k : mn0;
+              mx0 = k > mx0 ? k : mx0;
             }
           }
         }
       }
-      // to order keys (-0 and +0 fold together, so fminf's choice between them does not matter);
-      // a side without elements keeps the neutral keys
-      K mn[2][4], mx[2][4];
-#pragma unroll
-      for (int u = 0; u < 2; ++u)
-#pragma unroll
-        for (int j = 0; j < 4; ++j) {
-          mn[u][j] = has[u] ? (K)ord_key(fmn[u][j]) : key_max<K>();
-          mx[u][j] = has[u] ? (K)ord_key(fmx[u][j]) : (K)0;
-        }
-      // lanes of a warp with the same word: xor offsets w, 2w, ..., 16
-      for (int o = w; o < 32; o <<= 1) {
-#pragma unroll
-        for (int u = 0; u < 2; ++u)
-#pragma unroll
-          for (int j = 0; j < 4; ++j) {
-            const K a = __shfl_xor_sync(0xffffffffu, mn[u][j], o), b = __shfl_xor_sync(0xffffffffu, mx[u][j], o);
-            mn[u][j] = a < mn[u][j] ? a : mn[u][j];
-            mx[u][j] = b > mx[u][j] ? b : mx[u][j];
-          }
-      }
-      __shared__ K sbmn[2 * kMaxFusedD], sbmx[2 * kMaxFusedD];
-      for (int j = threadIdx.x; j < 2 * d; j += blockDim.x) {
-        sbmn[j] = key_max<K>();
-        sbmx[j] = (K)0;
-      }
-      __syncthreads();
-      const int lane = threadIdx.x & 31;
-      if (lane < w) {
-#pragma unroll
-        for (int u = 0; u < 2; ++u)
-#pragma unroll
-          for (int j = 0; j < 4; ++j) {
-            if (mn[u][j] != key_max<K>()) atomicMin(&sbmn[u * d + 4 * lane + j], mn[u][j]);
-            if (mx[u][j] != (K)0) atomicMax(&sbmx[u * d + 4 * lane + j], mx[u][j]);
-          }
-      }
-      __syncthreads();
-      for (int j = threadIdx.x; j < 2 * d; j += blockDim.x) {
-        if (sbmn[j] != key_max<K>()) atomicMin(&cmin[(long long)2 * s * d + j], sbmn[j]);
-        if (sbmx[j] != (K)0) atomicMax(&cmax[(long long)2 * s * d + j], sbmx[j]);
-      }
     }
-  } else {
-    for (int e = threadIdx.x; e < m * d; e += blockDim.x) {
-      const int r = e / d, c = e - r * d;
-      pts_out[(long long)sdst[r] * d + c] = pts_in[(long long)(c0 + r) * d + c];
+    if (cmin != nullptr) {
+#pragma unroll
+      for (int o = 16; o; o >>= 1) {
+        K x = __shfl_xor_sync(0xffffffffu, mn0, o);
+        mn0 = x < mn0 ? x : mn0;
+        x = __shfl_xor_sync(0xffffffffu, mx0, o);
+        mx0 = x > mx0 ? x : mx0;
+        x = __shfl_xor_sync(0xffffffffu, mn1, o);
+        mn1 = x < mn1 ? x : mn1;
+        x = __shfl_xor_sync(0xffffffffu, mx1, o);
+        mx1 = x > mx1 ? x : mx1;
+      }
+      h0 = __any_sync(0xffffffffu, h0);
+      h1 = __any_sync(0xffffffffu, h1);
+      if (lane == 0) {
+        if (h0) {
+          atomicMin(&cmin[(long long)(2 * s) * d + j], mn0);
+          atomicMax(&cmax[(long long)(2 * s) * d + j], mx0);
+        }
+        if (h1) {
+          atomicMin(&cmin[(long long)(2 * s + 1) * d + j], mn1);
+          atomicMax(&cmax[(long long)(2 * s + 1) * d + j], mx1);
+        }
+      }
     }
   }
   int pv_[kItems];
@@ -490,9 +491,9 @@ __global__ void fixup_kernel(int n, int d, int t, int S, const int* __restrict__
     const int p = eqpos[lo + j], q = h0 + j;
     if (p != q) {
       for (int c = lane; c < d; c += 32) {
-        T a = pts[(long long)p * d + c];
-        pts[(long long)p * d + c] = pts[(long long)q * d + c];
-        pts[(long long)q * d + c] = a;
+        T a = pts[(long long)c * n + p];
+        pts[(long long)c * n + p] = pts[(long long)c * n + q];
+        pts[(long long)c * n + q] = a;
       }
       if (lane == 0) {
         int a = perm[p];
@@ -506,7 +507,7 @@ __global__ void fixup_kernel(int n, int d, int t, int S, const int* __restrict__
     const int node = (1 << t) - 1 + s;
     const int ax = axis[s];
     node_axis[node] = ax;
-    node_split[node] = pts[(long long)(lo + (hi - lo) / 2) * d + ax];
+    node_split[node] = pts[(long long)ax * n + lo + (hi - lo) / 2];
   }
 }
 
@@ -665,6 +666,43 @@ __device__ __forceinline__ void warp_finish_split(const T* spts, int ds, uint16_
   }
 }
 
+// bounding box of rows [ca, cb) (through cur) over dimensions [j0, j0 + 16) by one warp, row by
+// row: each lane keeps the minima and the negated maxima of its rows (32 values), then a
+// recursive-halving reduction (31 shuffles) leaves slot l in lane l: slots 0..15 the minima of
+// dimensions j0.., slots 16..31 the negated maxima. Start values as the per-dimension loops used
+// (big, -big); only widths are taken from these boxes, so the order of the reduction is free.
+template <typename T>
+__device__ __forceinline__ T warp_box16(const T* spts, int ds, const uint16_t* cur, int ca, int cb, int j0, int d,
+                                        int lane) {
+  T v[32];
+#pragma unroll
+  for (int k = 0; k < 32; ++k) v[k] = real_traits<T>::big();
+  const int nj = d - j0;
+  for (int i = ca + lane; i < cb; i += 32) {
+    const T* row = spts + (size_t)cur[i] * ds + j0;
+#pragma unroll
+    for (int k = 0; k < 16; ++k) {
+      if (k < nj) {
+        const T x = row[k];
+        v[k] = x < v[k] ? x : v[k];
+        v[16 + k] = -x < v[16 + k] ? -x : v[16 + k];
+      }
+    }
+  }
+#pragma unroll
+  for (int o = 16; o; o >>= 1) {
+    const bool up = (lane & o) != 0;
+#pragma unroll
+    for (int k = 0; k < o; ++k) {
+      const T send = up ? v[k] : v[k + o];
+      const T keep = up ? v[k + o] : v[k];
+      const T recv = __shfl_xor_sync(0xffffffffu, send, o);
+      v[k] = recv < keep ? recv : keep;
+    }
+  }
+  return v[0];
+}
+
 template <typename T>
 __global__ void __launch_bounds__(kSubThreads) subtree_kernel(
     int n, int d, int depth, int t0, int smax, int splitting, const T* __restrict__ pts_in,
@@ -696,34 +734,16 @@ __global__ void __launch_bounds__(kSubThreads) subtree_kernel(
   const int cnt = hi - lo;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 
-  if (sizeof(T) == 4 && (d & 3) == 0) {
-    // 16-byte loads, eight in flight per thread, spread to the padded rows
-    const float4* src = reinterpret_cast<const float4*>(pts_in + (long long)lo * d);
-    const int nq = cnt * d / 4, qpr = d / 4;
-    for (int e0 = threadIdx.x; e0 < nq; e0 += 8 * kSubThreads) {
-      float4 v[8];
+  // the segment's columns (column-major points), sixteen loads in flight per thread, into padded rows
+  for (int j0 = 0; j0 < d; j0 += 16) {
+    for (int r = threadIdx.x; r < cnt; r += kSubThreads) {
+      T v[16];
 #pragma unroll
-      for (int u = 0; u < 8; ++u) {
-        const int e = e0 + u * kSubThreads;
-        if (e < nq) v[u] = __ldg(src + e);
-      }
+      for (int u = 0; u < 16; ++u)
+        if (j0 + u < d) v[u] = __ldg(pts_in + (long long)(j0 + u) * n + lo + r);
 #pragma unroll
-      for (int u = 0; u < 8; ++u) {
-        const int e = e0 + u * kSubThreads;
-        if (e < nq) {
-          const int r = e / qpr, c = (e - r * qpr) * 4;
-          float* dst = reinterpret_cast<float*>(spts) + (size_t)r * ds + c;
-          dst[0] = v[u].x;
-          dst[1] = v[u].y;
-          dst[2] = v[u].z;
-          dst[3] = v[u].w;
-        }
-      }
-    }
-  } else {
-    for (long long e = threadIdx.x; e < (long long)cnt * d; e += blockDim.x) {
-      const int r = (int)(e / d), c = (int)(e - (long long)r * d);
-      spts[(size_t)r * ds + c] = pts_in[(long long)lo * d + e];
+      for (int u = 0; u < 16; ++u)
+        if (j0 + u < d) spts[(size_t)r * ds + j0 + u] = v[u];
     }
   }
   for (int i = threadIdx.x; i < cnt; i += blockDim.x) {
@@ -746,23 +766,25 @@ __global__ void __launch_bounds__(kSubThreads) subtree_kernel(
         const int half = (b - a) / 2;
         T best = 0;
         int axis = splitting == 0 ? l % d : 0;
-        for (int j = 0; splitting != 0 && j < d; ++j) {
-          T mn = real_traits<T>::big(), mx = -real_traits<T>::big();
-          for (int i = a + lane; i < b; i += 32) {
-            const T v = spts[(size_t)cur[i] * ds + j];
-            mn = v < mn ? v : mn;
-            mx = v > mx ? v : mx;
-          }
+        for (int j0 = 0; splitting != 0 && j0 < d; j0 += 16) {
+          // widths of dimensions j0 + lane (lanes < 16), then the serial rule: the first strictly
+          // widest, over the chunk's lanes in order and across chunks
+          const T r = warp_box16<T>(spts, ds, cur, a, b, j0, d, lane);
+          const T mx = -__shfl_sync(0xffffffffu, r, (lane & 15) + 16);
+          T bw = (lane < 16 && j0 + lane < d) ? real_traits<T>::sub(mx, r) : -real_traits<T>::big();
+          int bj = j0 + lane;
 #pragma unroll
           for (int o = 16; o; o >>= 1) {
-            const T omn = __shfl_xor_sync(0xffffffffu, mn, o), omx = __shfl_xor_sync(0xffffffffu, mx, o);
-            mn = omn < mn ? omn : mn;
-            mx = omx > mx ? omx : mx;
+            const T ow = __shfl_xor_sync(0xffffffffu, bw, o);
+            const int oj = __shfl_xor_sync(0xffffffffu, bj, o);
+            if (ow > bw || (ow == bw && oj < bj)) {
+              bw = ow;
+              bj = oj;
+            }
           }
-          const T wd = real_traits<T>::sub(mx, mn);
-          if (wd > best) {
-            best = wd;
-            axis = j;
+          if (bw > best) {
+            best = bw;
+            axis = bj;
           }
         }
         for (int i = a + lane; i < b; i += 32) skey[i] = ord_key(spts[(size_t)cur[i] * ds + axis]);
@@ -796,22 +818,12 @@ __global__ void __launch_bounds__(kSubThreads) subtree_kernel(
       const int cs = (((b - a) + G - 1) / G + 31) & ~31;
       const int ca = min(b, a + gw * cs), cb = min(b, ca + cs);
       if (splitting != 0) {
-        for (int j = 0; j < d; ++j) {
-          T mn = real_traits<T>::big(), mx = -real_traits<T>::big();
-          for (int i = ca + lane; i < cb; i += 32) {
-            const T v = spts[(size_t)cur[i] * ds + j];
-            mn = v < mn ? v : mn;
-            mx = v > mx ? v : mx;
-          }
-#pragma unroll
-          for (int o = 16; o; o >>= 1) {
-            const T omn = __shfl_xor_sync(0xffffffffu, mn, o), omx = __shfl_xor_sync(0xffffffffu, mx, o);
-            mn = omn < mn ? omn : mn;
-            mx = omx > mx ? omx : mx;
-          }
-          if (lane == 0) {
-            spmn[warp * d + j] = mn;
-            spmx[warp * d + j] = mx;
+        for (int j0 = 0; j0 < d; j0 += 16) {
+          const T r = warp_box16<T>(spts, ds, cur, ca, cb, j0, d, lane);
+          const int j = j0 + (lane & 15);
+          if (j < d) {
+            if (lane < 16) spmn[warp * d + j] = r;
+            else spmx[warp * d + j] = -r;
           }
         }
       }
@@ -994,7 +1006,6 @@ static int build_impl(annf_handle* h, const T* points, int n, int d, int depth, 
   int* cur_perm = h->perm.as<int>();
   int* alt_perm = h->perm_tmp.as<int>();
   prof_mark(h, "build:begin", st);
-  ANNF_CUDA_TRY(cudaMemcpyAsync(cur_pts, points, (size_t)n * d * sizeof(T), cudaMemcpyDeviceToDevice, st));
   iota_kernel<<<std::min(ceil_div(n, 256), 4096), 256, 0, st>>>(cur_perm, n);
   ANNF_CHECK_LAUNCH();
 
@@ -1005,9 +1016,6 @@ static int build_impl(annf_handle* h, const T* points, int n, int d, int depth, 
   int tg = 0;
   while (tg < depth && ((long long)n + (1LL << tg) - 1) / (1LL << tg) > smax) ++tg;
   const long long cap = 1LL << tg;  // segments of the deepest level that needs a box
-  // from level 1 on the scatter computes the children's boxes when a row is whole float4 words, a
-  // power of two of them (a thread then always handles the same word)
-  const bool fused = sizeof(T) == 4 && (d & 3) == 0 && d <= kMaxFusedD && ((d >> 2) & ((d >> 2) - 1)) == 0;
   if (tg > 0) {
     ANNF_ENSURE(h->bmin, (size_t)2 * cap * d * sizeof(K));
     ANNF_ENSURE(h->bmax, (size_t)2 * cap * d * sizeof(K));
@@ -1015,6 +1023,28 @@ static int build_impl(annf_handle* h, const T* points, int n, int d, int depth, 
     ANNF_CUDA_TRY(cudaMemsetAsync(h->hist.p, 0, (size_t)(cap / 2) * kSelBins * sizeof(unsigned), st));  // picks re-zero it
   }
   ANNF_ENSURE(h->leaf_box, (size_t)2 * L * d * sizeof(T));
+  // the points, column-major from here to the finisher (or to the leaves); level 0's box on the way
+  const int crows = col_tile_rows<T>(d);
+  const size_t csmem = (size_t)crows * (d | 1) * sizeof(T);
+  const int cblocks = std::min(ceil_div(n, crows), 16 * num_sms());
+  if (depth == 0) {
+    ANNF_CUDA_TRY(cudaMemcpyAsync(cur_pts, points, (size_t)n * d * sizeof(T), cudaMemcpyDeviceToDevice, st));
+  } else {
+    K* gmin0 = h->bmin.as<K>();
+    K* gmax0 = h->bmax.as<K>();
+    if (tg == 0) {  // the finisher takes the root: no level needs a box, but the kernel wants two
+      ANNF_ENSURE(h->bmin, (size_t)2 * d * sizeof(K));
+      ANNF_ENSURE(h->bmax, (size_t)2 * d * sizeof(K));
+      gmin0 = h->bmin.as<K>();
+      gmax0 = h->bmax.as<K>();
+    }
+    fill_keys_kernel<K><<<1, 256, 0, st>>>(gmin0, d, ~(K)0);
+    ANNF_CHECK_LAUNCH();
+    fill_keys_kernel<K><<<1, 256, 0, st>>>(gmax0, d, (K)0);
+    ANNF_CHECK_LAUNCH();
+    to_columns_kernel<T><<<cblocks, kThreads, csmem, st>>>(n, d, points, cur_pts, gmin0, gmax0);
+    ANNF_CHECK_LAUNCH();
+  }
   bool finished = false;
   for (int t = 0; t < depth; ++t) {
     const int S = 1 << t;
@@ -1047,18 +1077,10 @@ static int build_impl(annf_handle* h, const T* points, int n, int d, int depth, 
     ANNF_ENSURE(h->blk_eq, (size_t)nblk * sizeof(int));
     K* gmin = h->bmin.as<K>() + (size_t)(t & 1) * cap * d;
     K* gmax = h->bmax.as<K>() + (size_t)(t & 1) * cap * d;
-    // the children's boxes, when the next level is a global one and the scatter can compute them
-    K* cmin = (fused && t + 1 < tg) ? h->bmin.as<K>() + (size_t)((t + 1) & 1) * cap * d : nullptr;
-    K* cmax = (fused && t + 1 < tg) ? h->bmax.as<K>() + (size_t)((t + 1) & 1) * cap * d : nullptr;
-    if (t == 0 || !fused) {
-      const int fb = std::min(ceil_div((long long)S * d, 256), 4096);
-      fill_keys_kernel<K><<<fb, 256, 0, st>>>(gmin, (long long)S * d, ~(K)0);
-      ANNF_CHECK_LAUNCH();
-      fill_keys_kernel<K><<<fb, 256, 0, st>>>(gmax, (long long)S * d, (K)0);
-      ANNF_CHECK_LAUNCH();
-      bbox_kernel<T><<<(unsigned)nblk, kThreads, 0, st>>>(n, d, t, B, cur_pts, gmin, gmax);
-      ANNF_CHECK_LAUNCH();
-    }
+    // the children's boxes, when the next level is a global one: the scatter computes them (level
+    // 0's came with the column-major copy)
+    K* cmin = t + 1 < tg ? h->bmin.as<K>() + (size_t)((t + 1) & 1) * cap * d : nullptr;
+    K* cmax = t + 1 < tg ? h->bmax.as<K>() + (size_t)((t + 1) & 1) * cap * d : nullptr;
     axis_kernel<T><<<ceil_div(S, 128), 128, 0, st>>>(n, d, t, S, splitting, gmin, gmax, h->axis.as<int>(),
                                                    h->sel_prefix.as<K>(), h->sel_rank.as<int>(),
                                                    h->sel_nlt.as<int>(), cmin, cmax);
@@ -1100,6 +1122,11 @@ static int build_impl(annf_handle* h, const T* points, int n, int d, int depth, 
     leaves_kernel<<<(unsigned)((long long)S * B), kThreads, 0, st>>>(n, depth, B, cur_perm,
                                                                     h->leaf_begin.as<int>(), h->point_leaf.as<int>());
     ANNF_CHECK_LAUNCH();
+    if (depth > 0) {  // the leaves' points back to rows
+      to_rows_kernel<T><<<cblocks, kThreads, csmem, st>>>(n, d, cur_pts, alt_pts);
+      ANNF_CHECK_LAUNCH();
+      std::swap(cur_pts, alt_pts);
+    }
   }
   // the final arrays live in h->pts / h->perm
   if (cur_pts != h->pts.as<T>()) std::swap(h->pts, h->pts_tmp);
