@@ -49,7 +49,10 @@ class _SubsetCache:
             rs = numpy.random.RandomState(seed)
             i_s = rs.randint(n_h, size=m)
             j_s = rs.randint(n_w, size=m)
-            pos = torch.from_numpy(numpy.stack([i_s, j_s], axis=1).astype(numpy.int32)).to(device)
+            # in image order: the covariance is an exact integer sum over the samples (the same bits
+            # in any order), and the gather then walks the images row by row
+            order = numpy.lexsort((j_s, i_s))
+            pos = torch.from_numpy(numpy.stack([i_s[order], j_s[order]], axis=1).astype(numpy.int32)).to(device)
         self._d[key] = pos
         while len(self._d) > 1024:
             self._d.popitem(last=False)

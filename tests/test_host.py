@@ -118,8 +118,13 @@ def test_subset_positions_match_sklearn_sampling():
     img = img.astype(np.uint8)
     pos = _SubsetCache().get(26, 36, 50, 7, torch.device("cpu")).numpy()
     ref = sk.extract_patches_2d(img, (5, 5), max_patches=50, random_state=7)
-    got = np.stack([img[y:y + 5, x:x + 5] for y, x in pos])
-    assert np.array_equal(got, ref)
+    # sklearn's draws (rows, then columns) give its patches in its order ...
+    rs = np.random.RandomState(7)
+    i_s, j_s = rs.randint(26, size=50), rs.randint(36, size=50)
+    assert np.array_equal(np.stack([img[y:y + 5, x:x + 5] for y, x in zip(i_s, j_s)]), ref)
+    # ... and the cache holds the same positions in image order (the covariance is an exact sum)
+    order = np.lexsort((j_s, i_s))
+    assert np.array_equal(pos, np.stack([i_s[order], j_s[order]], axis=1))
 
 
 def test_generators_are_seeded():
