@@ -133,7 +133,7 @@ void annf_destroy(annf_handle* h) {
   if (h->solver) cusolverDnDestroy(reinterpret_cast<cusolverDnHandle_t>(h->solver));
   DevBuf* bufs[] = {&h->pts, &h->pts_tmp, &h->perm, &h->perm_tmp, &h->node_axis, &h->node_split, &h->leaf_begin,
                     &h->point_leaf, &h->leaf_box, &h->bmin, &h->bmax, &h->axis, &h->keys, &h->hist, &h->sel_prefix,
-                    &h->sel_rank, &h->sel_nlt, &h->sel_neq, &h->blk_lt, &h->blk_eq, &h->off_lt, &h->off_eq,
+                    &h->sel_rank, &h->sel_nlt, &h->sel_neq, &h->chunk_state, &h->off_lt, &h->off_eq,
                     &h->eqpos, &h->nat_keys, &h->nat_pos, &h->lists, &h->next_range, &h->part_keys,
                     &h->part_pos, &h->fast_buf, &h->fast_nat, &h->tc_buf, &h->pj_buf, &h->gram, &h->colsum, &h->subset_t, &h->cov, &h->eigval, &h->digits,
                     &h->meanproj, &h->solver_ws, &h->solver_info, &h->eig_ws, &h->status, &h->leaf_marks,

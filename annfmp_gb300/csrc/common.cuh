@@ -58,6 +58,7 @@ enum : unsigned {
   DEV_SMEM_CARVE = 8u,  // a kernel's shared-memory carve exceeded its launch allocation
   DEV_TC_TIMEOUT = 16u, // a tensor-core kernel's bounded wait on its MMA ran out
   DEV_GRID_TIMEOUT = 32u, // a bounded grid-wide barrier gave up waiting for the other CTAs
+  DEV_LOOKBACK_TIMEOUT = 64u, // a scatter chunk's bounded wait for its predecessors' counts ran out
 };
 
 __device__ __forceinline__ unsigned dyn_smem_size() {

@@ -364,7 +364,7 @@ __device__ __forceinline__ void ssd_jobs(const unsigned* __restrict__ strip, int
 }
 
 constexpr int kPropThreads = 256;
-constexpr int kPropGroup = 4;  // listed candidates per thread at a time
+constexpr int kPropGroup = 2;  // listed candidates per thread at a time (two keep five CTAs per SM)
 constexpr int kPropSlots = 6;  // candidate slots per pixel of the listing pass: 4 neighbours + up to 2 random offsets
 
 // words per A strip row of fast_prop_t_kernel: a tile's kPropThreads patches of psize pixels of c
@@ -426,7 +426,7 @@ __global__ void __launch_bounds__(256, 3) fast_init_t_kernel(Img A, Img B, int n
 // candidate it does not have. Each candidate folds (SSD, index) into its pixel's 64-bit best key
 // with atomicMin: the lexicographic minimum, the same result as trying the candidates one by one.
 template <int PS, int RL>
-__global__ void __launch_bounds__(kPropThreads, 3) fast_prop_t_kernel(Img A, Img B, int nA, int jump, int radius,
+__global__ void __launch_bounds__(kPropThreads, 5) fast_prop_t_kernel(Img A, Img B, int nA, int jump, int radius,
                                                                    int nrand, uint32_t seed, Match in, Match out,
                                                                    const uint8_t* __restrict__ chg_in,
                                                                    uint8_t* __restrict__ chg_out) {

@@ -61,7 +61,7 @@ struct annf_handle {
   int n = 0, d = 0, depth = 0, real_type = ANNF_REAL_F32, leaf_bits = 1, max_leaf = 0;
   annf::DevBuf pts, pts_tmp, perm, perm_tmp, node_axis, node_split, leaf_begin, point_leaf, leaf_box;
   // ---- build scratch ----
-  annf::DevBuf bmin, bmax, axis, keys, hist, sel_prefix, sel_rank, sel_nlt, sel_neq, blk_lt, blk_eq,
+  annf::DevBuf bmin, bmax, axis, keys, hist, sel_prefix, sel_rank, sel_nlt, sel_neq, chunk_state,
       off_lt, off_eq, eqpos;
   // ---- query scratch ----
   annf::DevBuf nat_keys, nat_pos, lists, next_range, part_keys, part_pos, leaf_marks;

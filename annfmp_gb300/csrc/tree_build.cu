@@ -302,33 +302,51 @@ __global__ void pick_kernel(int shift, bool last, unsigned* ghist, K* prefix, in
   }
 }
 
-template <typename K>
-__global__ void count_kernel(int n, int t, int B, const K* __restrict__ keys, const K* __restrict__ pivot,
-                             int* blk_lt, int* blk_eq) {
-  const int s = blockIdx.x / B, bb = blockIdx.x % B;
-  int lo, hi;
-  seg_range(n, t, s, lo, hi);
-  const int c0 = lo + bb * kChunk, c1 = min(hi, c0 + kChunk);
-  const K pv = pivot[s];
-  int lt = 0, eq = 0;
-  for (int i = c0 + threadIdx.x; i < c1; i += blockDim.x) {
-    K k = keys[i];
-    lt += k < pv;
-    eq += k == pv;
+// Per-chunk state of a level's scatter (decoupled look-back, zeroed before the level): a 64-bit
+// word per chunk, flag in bits 62-63 (0 not ready, 1 the chunk's own counts, 2 the inclusive
+// counts of the segment's chunks up to it), "<" count in bits 31-61, "==" count in bits 0-30.
+constexpr long long kLookSpins = 1LL << 21;  // bound of a chunk's wait for a predecessor (~0.1 s)
+__device__ __forceinline__ unsigned long long chunk_word(unsigned flag, int lt, int eq) {
+  return ((unsigned long long)flag << 62) | ((unsigned long long)(unsigned)lt << 31) | (unsigned)eq;
+}
+
+// the counts of the segment's chunks before chunk bb ("<" and "==" of the pivot), by thread 0;
+// publishes this chunk's own counts first and its inclusive counts last. Predecessors have lower
+// block indices, so they started first; a wait that runs out sets DEV_LOOKBACK_TIMEOUT.
+__device__ __forceinline__ void chunk_lookback(unsigned long long* st, int bb, int lt, int eq, int& pre_lt,
+                                               int& pre_eq, unsigned* status) {
+  pre_lt = 0;
+  pre_eq = 0;
+  if (bb == 0) {
+    atomicExch(st, chunk_word(2u, lt, eq));
+    return;
   }
-  int e1, e2, t1, t2;
-  block_excl_scan2(lt, eq, e1, e2, t1, t2);
-  if (threadIdx.x == 0) {
-    blk_lt[blockIdx.x] = t1;
-    blk_eq[blockIdx.x] = t2;
+  atomicExch(st + bb, chunk_word(1u, lt, eq));
+  long long spins = 0;
+  for (int u = bb - 1; u >= 0;) {
+    const unsigned long long v = *reinterpret_cast<volatile unsigned long long*>(st + u);
+    const unsigned flag = (unsigned)(v >> 62);
+    if (flag == 0u) {
+      if (++spins > kLookSpins) {
+        atomicOr(status, DEV_LOOKBACK_TIMEOUT);
+        break;
+      }
+      __nanosleep(32);
+      continue;
+    }
+    pre_lt += (int)((v >> 31) & 0x7fffffffu);
+    pre_eq += (int)(v & 0x7fffffffu);
+    if (flag == 2u) break;
+    --u;
   }
+  atomicExch(st + bb, chunk_word(2u, pre_lt + lt, pre_eq + eq));
 }
 
 template <typename T>
 __global__ void __launch_bounds__(kThreads) scatter_kernel(
     int n, int d, int t, int B, const typename key_of<T>::type* __restrict__ keys,
     const typename key_of<T>::type* __restrict__ pivot, const int* __restrict__ nlt,
-    const int* __restrict__ neq, const int* __restrict__ blk_lt, const int* __restrict__ blk_eq,
+    const int* __restrict__ neq, unsigned long long* __restrict__ chunk_st, unsigned* status,
     const T* __restrict__ pts_in, const int* __restrict__ perm_in, T* __restrict__ pts_out,
     int* __restrict__ perm_out, int* __restrict__ eqpos, typename key_of<T>::type* cmin,
     typename key_of<T>::type* cmax) {
@@ -362,16 +380,18 @@ __global__ void __launch_bounds__(kThreads) scatter_kernel(
       }
     }
   }
-  // this chunk's offsets among its segment's chunks: a block-wide sum over the chunks before it
-  int pl = 0, pe = 0;
-  for (int u = threadIdx.x; u < bb; u += blockDim.x) {
-    pl += blk_lt[(long long)s * B + u];
-    pe += blk_eq[(long long)s * B + u];
-  }
-  int d1, d2, sum_lt, sum_eq;
-  block_excl_scan2(pl, pe, d1, d2, sum_lt, sum_eq);
   int elt, eeq, tl, te;
   block_excl_scan2(mlt, meq, elt, eeq, tl, te);
+  // this chunk's offsets among its segment's chunks
+  __shared__ int spre[2];
+  if (threadIdx.x == 0) {
+    int pl, pe;
+    chunk_lookback(chunk_st + (long long)s * B, bb, tl, te, pl, pe, status);
+    spre[0] = pl;
+    spre[1] = pe;
+  }
+  __syncthreads();
+  const int sum_lt = spre[0], sum_eq = spre[1];
   int lt_before = sum_lt + elt;
   int eq_before = sum_eq + eeq;
   const int seg_neq = neq[s];
@@ -562,7 +582,7 @@ __global__ void leaf_box_kernel(int L, int d, const T* __restrict__ pts, const i
 // result is the one a single warp walking the segment in order produces. From the level with one
 // segment per warp on, each warp splits its segments alone.
 // ---------------------------------------------------------------------------------------------
-constexpr int kSubThreads = 256;
+constexpr int kSubThreads = 512;
 constexpr int kSubWarps = kSubThreads / 32;
 
 __host__ __device__ __forceinline__ int sub_stride(int d) { return d | 1; }
@@ -980,7 +1000,7 @@ static size_t subtree_smem(int smax, int d) {
 
 template <typename T>
 static int subtree_capacity(int d) {
-  const size_t budget = 100 * 1024;  // two finisher CTAs per SM
+  const size_t budget = 112 * 1024;  // two finisher CTAs per SM
   int smax = 4096;
   while (smax > 1 && subtree_smem<T>(smax, d) > budget) smax >>= 1;
   return smax;
@@ -1073,8 +1093,7 @@ static int build_impl(annf_handle* h, const T* points, int n, int d, int depth, 
     ANNF_ENSURE(h->sel_rank, (size_t)S * sizeof(int));
     ANNF_ENSURE(h->sel_nlt, (size_t)S * sizeof(int));
     ANNF_ENSURE(h->sel_neq, (size_t)S * sizeof(int));
-    ANNF_ENSURE(h->blk_lt, (size_t)nblk * sizeof(int));
-    ANNF_ENSURE(h->blk_eq, (size_t)nblk * sizeof(int));
+    ANNF_ENSURE(h->chunk_state, (size_t)nblk * sizeof(unsigned long long));
     K* gmin = h->bmin.as<K>() + (size_t)(t & 1) * cap * d;
     K* gmax = h->bmax.as<K>() + (size_t)(t & 1) * cap * d;
     // the children's boxes, when the next level is a global one: the scatter computes them (level
@@ -1099,13 +1118,11 @@ static int build_impl(annf_handle* h, const T* points, int n, int d, int depth, 
       ANNF_CHECK_LAUNCH();
       hi_bit -= width;
     }
-    count_kernel<K><<<(unsigned)nblk, kThreads, 0, st>>>(n, t, B, h->keys.as<K>(), h->sel_prefix.as<K>(),
-                                                        h->blk_lt.as<int>(), h->blk_eq.as<int>());
-    ANNF_CHECK_LAUNCH();
+    ANNF_CUDA_TRY(cudaMemsetAsync(h->chunk_state.p, 0, (size_t)nblk * sizeof(unsigned long long), st));
     scatter_kernel<T><<<(unsigned)nblk, kThreads, 0, st>>>(
         n, d, t, B, h->keys.as<K>(), h->sel_prefix.as<K>(), h->sel_nlt.as<int>(), h->sel_neq.as<int>(),
-        h->blk_lt.as<int>(), h->blk_eq.as<int>(), cur_pts, cur_perm, alt_pts, alt_perm, h->eqpos.as<int>(), cmin,
-        cmax);
+        h->chunk_state.as<unsigned long long>(), h->status.as<unsigned>(), cur_pts, cur_perm, alt_pts, alt_perm,
+        h->eqpos.as<int>(), cmin, cmax);
     ANNF_CHECK_LAUNCH();
     fixup_kernel<T><<<ceil_div((long long)S * 32, 256), 256, 0, st>>>(
         n, d, t, S, h->axis.as<int>(), h->sel_nlt.as<int>(), h->sel_neq.as<int>(), h->eqpos.as<int>(),
