@@ -156,8 +156,8 @@ def stage_bytes(stage, w, n_a, n_b, depth, n_cols, it=1, nrand=1, n_prop=0, coun
     n_sub = int(round(0.1 * n_b))
     if stage == "chain":  # per query: query + k propagated leaves + leaf spans + natural list + k-list out
         return rows_q * (4 * d + k * ppl * 4 * d + 8 * k + 12 * k + 4 * k)
-    if stage == "natural_knn":  # query + node path + natural leaf + list out
-        return n_a * (4 * d + 8 * depth + ppl * 4 * d + 4 * k)
+    if stage == "natural_knn":  # tensor-core tiles: every leaf's points staged once, each query in, list out
+        return n_b * 4 * d + n_a * (4 * d + 4 + 4 * k)
     if stage == "natural_leaf":  # query + node path + leaf id out
         return n_a * (4 * d + 8 * depth + 4)
     if stage == "next_range":  # per tree position: its row-below position's leaf span
@@ -471,7 +471,11 @@ def run_gpu(args, w, rank, world, local_rank):
                 "d2h_bytes_per_step": int(nn_host.numel() * nn_host.element_size())},
         "gpu_launches": int(launches),
         "roofline": roof,
-        "roofline_stages": {k: {"ms": v, "algorithmic_bytes": sb(k), "frac": (sb(k) or 0) / (v / 1e3) / 1e9 / peak}
+        # per stage: algorithmic bytes over the HBM copy peak, and the unit ncu found binding (a
+        # stage bound elsewhere, e.g. L1, can show an HBM fraction above 1.0: its bytes come from
+        # L1/L2, so that fraction is not a bandwidth result)
+        "roofline_stages": {k: {"ms": v, "algorithmic_bytes": sb(k), "frac": (sb(k) or 0) / (v / 1e3) / 1e9 / peak,
+                                "bound": BINDING[k][0] if k in BINDING else "hbm"}
                             for k, v in sorted(kernel_stages.items(), key=lambda kv: -kv[1])},
         "distance_error": quality,
         "forms": forms,
@@ -492,10 +496,12 @@ def run_gpu(args, w, rank, world, local_rank):
 
 # where ncu located the binding unit of a stage's main kernel (committed summaries)
 BINDING = {
-    "fast_propagate": ("l1", "profiles/fast_prop_t_kernel_medium_learned.md: L1 throughput 83%, DRAM 1%"),
-    "natural_knn": ("issue (per-query selection and exact re-rank)", "profiles/leaf_tc_kernel_medium_learned.md"),
+    "fast_propagate": ("l1", "profiles/fast_prop_t_kernel_medium_learned.md: L1 throughput 88% in pass 1, DRAM < 2%"),
+    "fast_init": ("l1", "profiles/fast_init_t_kernel_medium_learned.md: L1 throughput 91%, DRAM 2%"),
+    "natural_knn": ("issue (per-query selection and exact re-rank)",
+                    "profiles/leaf_tc_kernel_medium_learned.md: tensor pipe 3.5%, 16 warps per SM (TMEM limit)"),
+    "build_subtree": ("barrier", "profiles/subtree_kernel_medium_learned.md: barrier stalls 4.0 per issue"),
     "chain": ("latency (long-scoreboard stalls, leaf re-reads from L2)", "profiles/chain_sel_kernel_medium_plain.md"),
-    "first_row": ("latency (one warp per query, few warps active)", "profiles/exact_scan_kernel_medium_plain.md"),
 }
 
 
