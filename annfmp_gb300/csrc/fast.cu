@@ -226,7 +226,9 @@ __device__ __forceinline__ void row_words(const uint8_t* __restrict__ img, long 
   if (c0 + 48 <= nbytes) {
     const uint4 q0 = __ldg(reinterpret_cast<const uint4*>(img + c0));
     const uint4 q1 = __ldg(reinterpret_cast<const uint4*>(img + c0 + 16));
-    const uint4 q2 = __ldg(reinterpret_cast<const uint4*>(img + c0 + 32));
+    // the third 16 bytes only when the row reaches past the first 32 (lanes whose row fits skip it)
+    uint4 q2 = make_uint4(0u, 0u, 0u, 0u);
+    if (RL > 32 || s + RL > 32) q2 = __ldg(reinterpret_cast<const uint4*>(img + c0 + 32));
     const unsigned x[13] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w, q2.x, q2.y, q2.z, q2.w, 0u};
     // w[j] = bytes s + 4j .. s + 4j + 3: pick the word pair (s >> 2) + j in two branch-free steps
     // (lanes of a warp have different alignments), then shift
@@ -364,7 +366,7 @@ __device__ __forceinline__ void ssd_jobs(const unsigned* __restrict__ strip, int
 }
 
 constexpr int kPropThreads = 256;
-constexpr int kPropGroup = 2;  // listed candidates per thread at a time (two keep five CTAs per SM)
+constexpr int kPropGroup = 1;  // listed candidates per thread at a time (one keeps six CTAs per SM)
 constexpr int kPropSlots = 6;  // candidate slots per pixel of the listing pass: 4 neighbours + up to 2 random offsets
 
 // words per A strip row of fast_prop_t_kernel: a tile's kPropThreads patches of psize pixels of c
@@ -426,7 +428,7 @@ __global__ void __launch_bounds__(256, 3) fast_init_t_kernel(Img A, Img B, int n
 // candidate it does not have. Each candidate folds (SSD, index) into its pixel's 64-bit best key
 // with atomicMin: the lexicographic minimum, the same result as trying the candidates one by one.
 template <int PS, int RL>
-__global__ void __launch_bounds__(kPropThreads, 5) fast_prop_t_kernel(Img A, Img B, int nA, int jump, int radius,
+__global__ void __launch_bounds__(kPropThreads, 6) fast_prop_t_kernel(Img A, Img B, int nA, int jump, int radius,
                                                                    int nrand, uint32_t seed, Match in, Match out,
                                                                    const uint8_t* __restrict__ chg_in,
                                                                    uint8_t* __restrict__ chg_out) {
