@@ -318,8 +318,8 @@ __global__ void __launch_bounds__(kPrThreads) project_rows_tc_kernel(
   unsigned char* ring = p;  // [psize + 1 slots][even, odd][pe pixels][8 bytes]
   p += (size_t)nslot * 2 * pe * 8;
   p = reinterpret_cast<unsigned char*>(((uintptr_t)p + 15) & ~uintptr_t(15));
-  uint64_t* mbar = reinterpret_cast<uint64_t*>(p);
-  p += 8;
+  uint64_t* mbar = reinterpret_cast<uint64_t*>(p);  // [2]: one per accumulator
+  p += 16;
   uint32_t* tslot = reinterpret_cast<uint32_t*>(p);
   p += 8;
   int* sflag = reinterpret_cast<int*>(p);
@@ -328,11 +328,12 @@ __global__ void __launch_bounds__(kPrThreads) project_rows_tc_kernel(
   if (yb >= nrows) return;  // uniform per block
   const int tid = threadIdx.x, warp = tid >> 5;
   if (warp == 0) {
-    tc::tmem_alloc(tslot, 2 * NPAD);
+    tc::tmem_alloc(tslot, 4 * NPAD);  // two accumulators x (even, odd) x NPAD columns
     tc::tmem_relinquish();
   }
   if (tid == 0) {
     tc::mbar_init(mbar, 1);
+    tc::mbar_init(mbar + 1, 1);
     tc::mbar_fence_init();
     sflag[0] = 0;
   }
@@ -351,38 +352,53 @@ __global__ void __launch_bounds__(kPrThreads) project_rows_tc_kernel(
   tc::fence_after_sync();
   const uint32_t tmem = *tslot;
   const uint32_t idesc = tc::idesc_f16(128, NPAD);
-  uint32_t phase = 0;
-  for (int y = yb; y < ye; ++y) {
-    // rows y .. y + psize - 1 are converted (and fenced for the tensor cores) by now
-    if (tid == 0) {
-      tc::fence_after_sync();
-      for (int half = 0; half < 2; ++half) {
-        for (int r = 0; r < psize; ++r) {
-          const unsigned char* a = reinterpret_cast<const unsigned char*>(half ? slot_odd(y + r) : slot_even(y + r));
-          const unsigned char* b = sB + (size_t)r * NPAD * KR * 2;
+  // the MMAs of output row y (image rows y .. y + psize - 1) into accumulator buf
+  auto issue = [&](int y, int buf) {
+    for (int half = 0; half < 2; ++half) {
+      for (int r = 0; r < psize; ++r) {
+        const unsigned char* a = reinterpret_cast<const unsigned char*>(half ? slot_odd(y + r) : slot_even(y + r));
+        const unsigned char* b = sB + (size_t)r * NPAD * KR * 2;
 #pragma unroll
-          for (int kk = 0; kk < KS; ++kk)
-            tc::mma_bf16(tmem + (uint32_t)(half * NPAD), tc::sdesc(a + kk * 32, 16, 128),
-                         tc::sdesc(b + kk * 256, 128, (KR / 8) * 128), idesc, (r > 0 || kk > 0) ? 1u : 0u);
-        }
+        for (int kk = 0; kk < KS; ++kk)
+          tc::mma_bf16(tmem + (uint32_t)(buf * 2 * NPAD + half * NPAD), tc::sdesc(a + kk * 32, 16, 128),
+                       tc::sdesc(b + kk * 256, 128, (KR / 8) * 128), idesc, (r > 0 || kk > 0) ? 1u : 0u);
       }
-      tc::mma_commit(mbar);
     }
-    // meanwhile the next output row's newest image row goes to the spare slot (that of row y - 1,
-    // whose MMAs finished before the previous wait)
+    tc::mma_commit(mbar + buf);
+  };
+  uint32_t phase = 0u;    // bit b: the parity to wait for on mbar[b]
+  uint32_t pending = 1u;  // bit b: a commit on mbar[b] not waited for yet
+  if (tid == 0) issue(yb, 0);
+  for (int y = yb; y < ye; ++y) {
+    const int buf = (y - yb) & 1;
+    // the image row the next output row adds goes to the slot of row y - 1, whose MMAs were waited
+    // for in the previous iteration (row y's MMAs do not read it)
     if (y + 1 < ye) {
       pr_convert_row(img, W, C, y + psize, x0, pe, slot_even(y + psize), slot_odd(y + psize));
       tc::fence_async_smem();
     }
-    if (!pj_wait(mbar, phase)) sflag[0] = 1;
-    phase ^= 1u;
     tc::fence_before_sync();
-    __syncthreads();
+    __syncthreads();  // the row is converted, and the epilogue of row y - 1 has left accumulator buf ^ 1
     if (sflag[0]) break;
+    // the next output row's MMAs run while this row's epilogue reads accumulator buf
+    if (y + 1 < ye) {
+      if (tid == 0) {
+        tc::fence_after_sync();
+        issue(y + 1, buf ^ 1);
+      }
+      pending |= 2u >> buf;  // bit buf ^ 1
+    }
+    const bool ok = __all_sync(0xffffffffu, pj_wait(mbar + buf, (phase >> buf) & 1u));
+    phase ^= 1u << buf;
+    pending &= ~(1u << buf);
+    if (!ok) {
+      if ((tid & 31) == 0) sflag[0] = 1;
+      continue;
+    }
     tc::fence_after_sync();
     // epilogue: lane i holds patch x0 + 2 i (columns 0..NPAD) and x0 + 2 i + 1 (NPAD..2 NPAD)
     {
-      const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16);
+      const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(buf * 2 * NPAD);
 #pragma unroll
       for (int half = 0; half < 2; ++half) {
         uint32_t r[NPAD];
@@ -413,16 +429,14 @@ __global__ void __launch_bounds__(kPrThreads) project_rows_tc_kernel(
         }
       }
     }
-    tc::fence_before_sync();
-    __syncthreads();
   }
-  if (sflag[0]) {
-    if (tid == 0) atomicOr(status, DEV_TC_TIMEOUT);
-    pj_wait(mbar, phase ^ 1u);
-  }
+  if (sflag[0] && tid == 0) atomicOr(status, DEV_TC_TIMEOUT);
+  // no MMA may still write TMEM when it is freed (after a time-out the next row's may be in flight)
+  for (int b = 0; b < 2; ++b)
+    if ((pending >> b) & 1u) pj_wait(mbar + b, (phase >> b) & 1u);
   tc::fence_before_sync();
   __syncthreads();
-  if (warp == 0) tc::tmem_dealloc(tmem, 2 * NPAD);
+  if (warp == 0) tc::tmem_dealloc(tmem, 4 * NPAD);
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -696,9 +710,11 @@ static int project_rows_tc(annf_handle* h, const uint8_t* img, int H, int W, int
   pr_prep_kernel<<<std::max(1, std::min(ceil_div((int)(bbytes / 2), 256), 64)), 256, 0, st>>>(
       comps, mean, ncomp, P, psize, c, npad, kr, bmat, mterm);
   ANNF_CHECK_LAUNCH();
-  // with 64 TMEM columns per CTA (npad 32) at most 8 CTAs may share an SM's 512 columns: the
-  // shared memory request keeps any more from being resident
-  const size_t smem = std::max(bbytes + (size_t)(psize + 1) * 2 * pe * 8 + 16 + 24 + 64, npad == 32 ? (size_t)28 * 1024 : 0);
+  // 4 npad TMEM columns per CTA (two accumulators): at most 512 / (4 npad) CTAs may share an SM's
+  // columns, and the shared memory request keeps any more from being resident
+  const int tmem_per_sm = 512 / (4 * npad);
+  const size_t smem = std::max(bbytes + (size_t)(psize + 1) * 2 * pe * 8 + 16 + 32 + 64,
+                               (size_t)233472 / (tmem_per_sm + 1) + 1024);
   ANNF_REQUIRE(smem <= 227 * 1024, "annf_project_f16: tile too large for shared memory");
   const int ncols = W - psize + 1, nrows = H - psize + 1;
   const long long blocks = (long long)((ncols + 255) / 256) * ((nrows + kPrRows - 1) / kPrRows);
