@@ -501,7 +501,8 @@ BINDING = {
     "natural_knn": ("issue (per-query selection and exact re-rank)",
                     "profiles/leaf_tc_kernel_medium_learned.md: tensor pipe 3.5%, 16 warps per SM (TMEM limit)"),
     "build_subtree": ("barrier", "profiles/subtree_kernel_medium_learned.md: barrier stalls 4.0 per issue"),
-    "chain": ("latency (long-scoreboard stalls, leaf re-reads from L2)", "profiles/chain_sel_kernel_medium_plain.md"),
+    "chain": ("latency (dependent loads per row step; 20.3 GB of DRAM re-reads per fit)",
+              "profiles/chain_sel_kernel_medium_plain.md, profiles/dram_large_plain.md"),
 }
 
 
