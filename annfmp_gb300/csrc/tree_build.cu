@@ -188,17 +188,19 @@ __global__ void axis_kernel(int n, int d, int t, int S, int splitting, const typ
 // points and writes the keys. Lanes of a warp that hit the same bin (common: a segment's keys share
 // their high digits) add once, together.
 constexpr int kSelBits = 11;                 // widest digit: 32-bit keys take three passes (11, 11, 10)
+constexpr int kHistChunks = 2;               // chunks per histogram CTA
 constexpr int kSelBins = 1 << kSelBits;
 template <typename T>
-__global__ void hist_kernel(int n, int d, int t, int B, int shift, int width, bool extract, const T* __restrict__ pts,
+__global__ void hist_kernel(int n, int d, int t, int HB, int shift, int width, bool extract, const T* __restrict__ pts,
                             const int* __restrict__ axis, typename key_of<T>::type* __restrict__ keys,
                             const typename key_of<T>::type* __restrict__ prefix, unsigned* ghist) {
   using K = typename key_of<T>::type;
   __shared__ unsigned h[kSelBins];
-  const int s = blockIdx.x / B, bb = blockIdx.x % B;
+  // a CTA takes kHistChunks consecutive chunks of its segment (HB CTAs per segment): one shared
+  // histogram, flushed once
+  const int s = blockIdx.x / HB, bb = blockIdx.x % HB;
   int lo, hi;
   seg_range(n, t, s, lo, hi);
-  const int c0 = lo + bb * kChunk, c1 = min(hi, c0 + kChunk);
   const int nb = 1 << width;
   for (int z = threadIdx.x; z < nb; z += blockDim.x) h[z] = 0;
   __syncthreads();
@@ -206,26 +208,30 @@ __global__ void hist_kernel(int n, int d, int t, int B, int shift, int width, bo
   const K hmask = (shift + width >= (int)(8 * sizeof(K))) ? (K)0 : (~(K)0 << (shift + width));
   const int ax = axis[s];
   const int lane = threadIdx.x & 31;
-  // every load of the thread's kItems elements first (all in flight at once), then the bins
-  K kv[kItems];
+  for (int cc = 0; cc < kHistChunks; ++cc) {
+    const int c0 = lo + (bb * kHistChunks + cc) * kChunk, c1 = min(hi, c0 + kChunk);
+    if (c0 >= c1) break;  // uniform per block
+    // every load of the thread's kItems elements first (all in flight at once), then the bins
+    K kv[kItems];
 #pragma unroll
-  for (int q = 0; q < kItems; ++q) {
-    const int i = c0 + (int)threadIdx.x + q * kThreads;
-    kv[q] = 0;
-    if (i < c1) kv[q] = extract ? (K)ord_key(pts[(long long)ax * n + i]) : keys[i];
-  }
-#pragma unroll
-  for (int q = 0; q < kItems; ++q) {
-    const int i = c0 + (int)threadIdx.x + q * kThreads;
-    if (c0 + q * kThreads >= c1) break;  // uniform: no element of this round in the chunk
-    unsigned bin = kSelBins;
-    if (i < c1) {
-      const K k = kv[q];
-      if (extract) keys[i] = k;
-      if (((k ^ pre) & hmask) == 0) bin = (unsigned)(k >> shift) & (unsigned)(nb - 1);
+    for (int q = 0; q < kItems; ++q) {
+      const int i = c0 + (int)threadIdx.x + q * kThreads;
+      kv[q] = 0;
+      if (i < c1) kv[q] = extract ? (K)ord_key(pts[(long long)ax * n + i]) : keys[i];
     }
-    const unsigned peers = __match_any_sync(0xffffffffu, bin);
-    if (bin != (unsigned)kSelBins && lane == __ffs(peers) - 1) atomicAdd(&h[bin], (unsigned)__popc(peers));
+#pragma unroll
+    for (int q = 0; q < kItems; ++q) {
+      const int i = c0 + (int)threadIdx.x + q * kThreads;
+      if (c0 + q * kThreads >= c1) break;  // uniform: no element of this round in the chunk
+      unsigned bin = kSelBins;
+      if (i < c1) {
+        const K k = kv[q];
+        if (extract) keys[i] = k;
+        if (((k ^ pre) & hmask) == 0) bin = (unsigned)(k >> shift) & (unsigned)(nb - 1);
+      }
+      const unsigned peers = __match_any_sync(0xffffffffu, bin);
+      if (bin != (unsigned)kSelBins && lane == __ffs(peers) - 1) atomicAdd(&h[bin], (unsigned)__popc(peers));
+    }
   }
   __syncthreads();
   for (int z = threadIdx.x; z < nb; z += blockDim.x) {
@@ -1084,6 +1090,7 @@ static int build_impl(annf_handle* h, const T* points, int n, int d, int depth, 
     }
     const int B = ceil_div(maxcnt, kChunk);
     const long long nblk = (long long)S * B;
+    const int HB = ceil_div(B, kHistChunks);  // histogram CTAs per segment
     if (nblk > 0x7fffffffLL) {
       set_error("tree too large for the level kernels");
       return ANNF_ERR_UNSUPPORTED;
@@ -1109,7 +1116,7 @@ static int build_impl(annf_handle* h, const T* points, int n, int d, int depth, 
     for (int hi_bit = kBits; hi_bit > 0;) {
       const int width = hi_bit >= 2 * kSelBits ? kSelBits : (hi_bit > kSelBits ? hi_bit - hi_bit / 2 : hi_bit);
       const int shift = hi_bit - width;
-      hist_kernel<T><<<(unsigned)nblk, 256, 0, st>>>(n, d, t, B, shift, width, hi_bit == kBits, cur_pts,
+      hist_kernel<T><<<(unsigned)((long long)S * HB), 256, 0, st>>>(n, d, t, HB, shift, width, hi_bit == kBits, cur_pts,
                                                      h->axis.as<int>(), h->keys.as<K>(), h->sel_prefix.as<K>(),
                                                      h->hist.as<unsigned>());
       ANNF_CHECK_LAUNCH();
