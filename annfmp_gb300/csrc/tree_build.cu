@@ -10,11 +10,14 @@
 //     in reverse input order, then a forward pass that swaps the elements equal to the pivot, in
 //     the order met, to the front of the ">=" block; split value = element at position count/2.
 //
-// Large segments (top levels) are processed by many CTAs per segment: bounding box (atomics on
-// order-preserving keys), an 8-bit-digit radix select, per-chunk counts + scan + a stable scatter,
+// Large segments (top levels) are processed by many CTAs per segment, with the points column-major
+// (a level's split coordinate is one contiguous column): an 11/11/10-bit radix select of the median
+// over the split column, a stable scatter of every column that finds each chunk's offset by a
+// decoupled look-back and forms the children's bounding boxes (atomics on order-preserving keys),
 // and a one-warp fix-up for the equal elements. When a level's segments fit in shared memory, one
-// CTA per segment finishes the whole subtree in shared memory (bounding box, radix select and
-// stable partition on a 16-bit index permutation) and writes the points out once, in leaf order.
+// CTA per segment finishes the whole subtree in shared memory (bounding box, 8-bit-digit radix
+// select and stable partition on a 16-bit index permutation) and writes the points out once, row
+// by row, in leaf order.
 #include <algorithm>
 #include <vector>
 
