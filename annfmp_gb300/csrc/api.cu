@@ -175,7 +175,8 @@ int annf_tree_get(const annf_handle* h, annf_tree_view* out) {
   return ANNF_OK;
 }
 
-static int check_k(const annf_handle* h, int k, long long max_leaves) {
+// max_k: the largest K the entry point's kernels take (kneighbors: the reference's 1000)
+static int check_k(const annf_handle* h, int k, long long max_leaves, int max_k = kMaxK) {
   if (!h->built) {
     set_error("no tree has been built (call annf_build_tree first)");
     return ANNF_ERR_STATE;
@@ -184,8 +185,8 @@ static int check_k(const annf_handle* h, int k, long long max_leaves) {
     set_error("k must be in [1, 1000]");
     return ANNF_ERR_INVALID;
   }
-  if (k > kMaxK) {
-    set_error("k > 32 is not supported by the GPU kernels");
+  if (k > max_k) {
+    set_error("k > 32 is not supported by this entry point's GPU kernels");
     return ANNF_ERR_UNSUPPORTED;
   }
   if (max_leaves < 0) {  // annfmp/openmp/kdtree/base.py:129-130
@@ -199,7 +200,7 @@ int annf_kneighbors(annf_handle* h, const void* queries, int nq, int k, long lon
                     int* indices, void* stream) {
   ANNF_API_HANDLE(h);
   ANNF_REQUIRE(ANNF_ALIGNED(queries, 16), "annf_kneighbors: queries must be 16-byte aligned");
-  int rc = check_k(h, k, max_leaves);
+  int rc = check_k(h, k, max_leaves, 1000);
   if (rc != ANNF_OK) return rc;
   ANNF_REQUIRE(nq >= 0, "annf_kneighbors: nq < 0");
   if (nq == 0) return ANNF_OK;

@@ -446,6 +446,216 @@ __global__ void __launch_bounds__(32 * kDfsWarps) exact_dfs_kernel(TreeView<T> t
 }
 
 // ---------------------------------------------------------------------------------------------
+// the same backtracking search for K above 32 (the reference accepts K up to 1000): one CTA per
+// query. The K-list lives in shared memory, sorted by key; warp 0's lane 0 runs the traversal
+// (the same stack, pruning and leaf budget as exact_dfs_kernel) and hands each leaf to the CTA,
+// which computes the leaf's distances kBigBatch points at a time, keeps those below the current
+// K-th key, sorts them (bitonic) and merges them into the list by rank. Keys are unique (distance,
+// the leaf's depth-first rank, the offset), so the merged list is the one the reference's
+// one-by-one insertion builds.
+// ---------------------------------------------------------------------------------------------
+constexpr int kBigThreads = 256;
+constexpr int kBigBatch = 256;  // candidates merged at a time (a power of two <= kBigThreads)
+constexpr int kBigStack = 64;  // > the deepest tree (30 levels) + 1
+
+template <typename T>
+static size_t dfs_big_smem(int depth, int K) {
+  using Kt = typename KeyOps<T>::K;
+  return NodeCache<T>::bytes(depth) + 2 * (size_t)K * (sizeof(Kt) + sizeof(int)) +
+         (size_t)kBigBatch * (sizeof(Kt) + sizeof(int)) + kMaxDynD * sizeof(T) +
+         (size_t)kBigStack * (sizeof(T) + sizeof(int) + sizeof(uint32_t)) + 8 * sizeof(int) + 128;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kBigThreads) exact_dfs_big_kernel(TreeView<T> tv, const T* __restrict__ Q, int nq,
+                                                                    int K, long long max_leaves, int mode,
+                                                                    int* __restrict__ out_pos,
+                                                                    T* __restrict__ out_dist,
+                                                                    int* __restrict__ out_idx) {
+  using Ops = KeyOps<T>;
+  using Kt = typename Ops::K;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  unsigned char* p = smem_raw;
+  NodeCache<T> nc;
+  nc.carve(p, tv.depth);
+  auto align16 = [](unsigned char* q) { return reinterpret_cast<unsigned char*>(((uintptr_t)q + 15) & ~uintptr_t(15)); };
+  p = align16(p);
+  Kt* lk[2];
+  int* lp[2];
+  lk[0] = reinterpret_cast<Kt*>(p);
+  lk[1] = lk[0] + K;
+  p = align16(reinterpret_cast<unsigned char*>(lk[1] + K));
+  Kt* ck = reinterpret_cast<Kt*>(p);  // [kBigBatch] this batch's candidates
+  p = align16(reinterpret_cast<unsigned char*>(ck + kBigBatch));
+  lp[0] = reinterpret_cast<int*>(p);
+  lp[1] = lp[0] + K;
+  int* cp = lp[1] + K;                       // [kBigBatch]
+  T* sq = reinterpret_cast<T*>(align16(reinterpret_cast<unsigned char*>(cp + kBigBatch)));  // [kMaxDynD]
+  T* sbound = sq + kMaxDynD;                 // [kBigStack]
+  int* snode = reinterpret_cast<int*>(sbound + kBigStack);
+  uint32_t* srank = reinterpret_cast<uint32_t*>(snode + kBigStack);
+  int* sctl = reinterpret_cast<int*>(srank + kBigStack);  // [0] leaf, [1] rank, [2] candidates
+  if (smem_overrun(smem_raw, sctl + 8, tv.status)) return;
+  nc.fill(tv);
+  __syncthreads();
+  const int tid = threadIdx.x, d = tv.d, depth = tv.depth;
+  const int first_leaf = (1 << depth) - 1;
+  QReg<T, 0> qr;
+  qr.v = sq;
+  qr.d = d;
+  for (int qi = blockIdx.x; qi < nq; qi += gridDim.x) {
+    for (int j = tid; j < d; j += kBigThreads) sq[j] = Q[(long long)qi * d + j];
+    for (int i = tid; i < K; i += kBigThreads) {
+      lk[0][i] = Ops::init();  // (max real, position 0) fill any shortfall, as the reference
+      lp[0][i] = 0;
+    }
+    int cur = 0;
+    int sp = 1;  // traversal state: lane 0 of warp 0 only
+    long long budget = max_leaves;
+    if (tid == 0) {
+      snode[0] = 0;
+      srank[0] = 0;
+      sbound[0] = T(0);
+    }
+    __syncthreads();
+    while (true) {
+      if (tid == 0) {
+        int leaf = -1;
+        uint32_t lrank = 0;
+        const T kth = Ops::dist(lk[cur][K - 1]);
+        while (sp > 0) {
+          --sp;
+          int node = snode[sp];
+          uint32_t rank = srank[sp];
+          if (sbound[sp] > kth) continue;  // (q-s)^2 > d_min[K-1]: skip (kdtree.c:219, 236)
+          int level = 31 - __clz(node + 1);
+          while (level < depth) {  // depth <= 30: at most depth entries pending, below kBigStack
+            int ax;
+            T s;
+            nc.get(tv, node, ax, s);
+            const T diff = real_traits<T>::sub(sq[ax], s);
+            const bool right = diff >= T(0);
+            snode[sp] = right ? 2 * node + 1 : 2 * node + 2;
+            srank[sp] = (rank << 1) | 1u;
+            sbound[sp] = real_traits<T>::mul(diff, diff);
+            ++sp;
+            node = right ? 2 * node + 2 : 2 * node + 1;
+            rank <<= 1;
+            ++level;
+          }
+          if (budget <= 0) {  // the reference stops at the leaf that exceeds max_leaves
+            sp = 0;
+            break;
+          }
+          --budget;
+          leaf = node - first_leaf;
+          lrank = rank;
+          break;
+        }
+        sctl[0] = leaf;
+        sctl[1] = (int)lrank;
+      }
+      __syncthreads();
+      const int leaf = sctl[0];
+      const uint32_t hi = (uint32_t)sctl[1] << tv.leaf_bits;
+      __syncthreads();  // every thread has read the hand-off before lane 0 writes the next one
+      if (leaf < 0) break;  // uniform
+      const int beg = __ldg(tv.leaf_begin + leaf), end = __ldg(tv.leaf_begin + leaf + 1);
+      for (int base = beg; base < end; base += kBigBatch) {
+        // this batch's points whose keys beat the current K-th, compacted in point order
+        const Kt thr = lk[cur][K - 1];
+        const int pp = base + tid;
+        Kt key = Ops::inf();
+        bool take = false;
+        if (tid < kBigBatch && pp < end) {
+          key = Ops::make(qr.dist(tv.pts + (long long)pp * d, d), hi | (uint32_t)(pp - beg));
+          take = Ops::lt(key, thr);
+        }
+        if (tid == 0) sctl[2] = 0;
+        __syncthreads();
+        const unsigned bal = __ballot_sync(0xffffffffu, take);
+        int wbase = 0;
+        if ((tid & 31) == 0 && bal) wbase = atomicAdd(&sctl[2], __popc(bal));
+        wbase = __shfl_sync(0xffffffffu, wbase, 0);
+        if (take) {
+          const int at = wbase + __popc(bal & ((1u << (tid & 31)) - 1u));
+          ck[at] = key;
+          cp[at] = pp;
+        }
+        __syncthreads();
+        const int m = sctl[2];
+        __syncthreads();  // every thread has read the count before the next batch resets it
+        if (m == 0) continue;  // uniform
+        int M = 1;
+        while (M < m) M <<= 1;
+        for (int i = m + tid; i < M; i += kBigThreads) ck[i] = Ops::inf();
+        __syncthreads();
+        // bitonic sort of ck[0 .. M) (ascending), positions with their keys
+        for (int k2 = 2; k2 <= M; k2 <<= 1) {
+          for (int j = k2 >> 1; j > 0; j >>= 1) {
+            for (int i = tid; i < M; i += kBigThreads) {
+              const int ixj = i ^ j;
+              if (ixj > i) {
+                const Kt a = ck[i], b = ck[ixj];
+                const bool asc = (i & k2) == 0;
+                if (asc ? Ops::lt(b, a) : Ops::lt(a, b)) {
+                  ck[i] = b;
+                  ck[ixj] = a;
+                  const int t = cp[i];
+                  cp[i] = cp[ixj];
+                  cp[ixj] = t;
+                }
+              }
+            }
+            __syncthreads();
+          }
+        }
+        // merge by rank into the other buffer: an entry's place is its index plus the number of
+        // the other list's keys below it (no key of one list equals a key of the other)
+        const int nxt = cur ^ 1;
+        for (int i = tid; i < K; i += kBigThreads) {
+          const Kt t = lk[cur][i];
+          int lo = 0, hi2 = m;
+          while (lo < hi2) {
+            const int mid = (lo + hi2) >> 1;
+            if (Ops::lt(ck[mid], t)) lo = mid + 1; else hi2 = mid;
+          }
+          const int r = i + lo;
+          if (r < K) {
+            lk[nxt][r] = t;
+            lp[nxt][r] = lp[cur][i];
+          }
+        }
+        for (int j = tid; j < m; j += kBigThreads) {
+          const Kt c = ck[j];
+          int lo = 0, hi2 = K;
+          while (lo < hi2) {
+            const int mid = (lo + hi2) >> 1;
+            if (Ops::lt(lk[cur][mid], c)) lo = mid + 1; else hi2 = mid;
+          }
+          const int r = j + lo;
+          if (r < K) {
+            lk[nxt][r] = c;
+            lp[nxt][r] = cp[j];
+          }
+        }
+        __syncthreads();
+        cur = nxt;
+      }
+    }
+    for (int i = tid; i < K; i += kBigThreads) {
+      if (mode == 0) {
+        out_pos[(long long)qi * K + i] = lp[cur][i];
+      } else {
+        out_dist[(long long)qi * K + i] = real_traits<T>::sqrt_(Ops::dist(lk[cur][i]));
+        out_idx[(long long)qi * K + i] = __ldg(tv.perm + lp[cur][i]);
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------------------------------------------
 // exact kNN without a leaf budget: the same result as the backtracking search (top-K by key over
 // all points), computed as a tiled brute force over the leaves that cannot be skipped. A leaf is
 // skipped when the distance from the query to its bounding box, evaluated with the same rounded
@@ -1264,9 +1474,25 @@ static int exact_box_launch(annf_handle* h, const T* Q, int nq, int K, int mode,
   return ANNF_OK;
 }
 
+template <typename T>
+static int exact_dfs_big_launch(annf_handle* h, const T* Q, int nq, int K, long long max_leaves, int mode,
+                                int* out_pos, T* out_dist, int* out_idx, cudaStream_t st) {
+  TreeView<T> tv = view_of<T>(h);
+  const size_t smem = dfs_big_smem<T>(h->depth, K);
+  ANNF_REQUIRE(smem <= 227 * 1024, "kneighbors: K too large for the shared-memory list");
+  ANNF_CUDA_TRY(cudaFuncSetAttribute(exact_dfs_big_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  const int blocks = std::max(1, std::min(nq, 8 * num_sms()));
+  exact_dfs_big_kernel<T><<<blocks, kBigThreads, smem, st>>>(tv, Q, nq, K, max_leaves, mode, out_pos, out_dist,
+                                                              out_idx);
+  ANNF_CHECK_LAUNCH();
+  return ANNF_OK;
+}
+
 template <typename T, int D>
 static int exact_knn_typed(annf_handle* h, const T* Q, int nq, int K, long long max_leaves, int mode, int* out_pos,
                            T* out_dist, int* out_idx, cudaStream_t st) {
+  if (K > 32)  // the warp-list kernels hold at most 32 entries
+    return exact_dfs_big_launch<T>(h, Q, nq, K, max_leaves, mode, out_pos, out_dist, out_idx, st);
   const size_t box_smem = NodeCache<T>::bytes(h->depth) + (size_t)kBoxThreads * (h->d + 1) * sizeof(T) +
                           2 * h->d * sizeof(T) + 32 + (size_t)h->max_leaf * h->d * sizeof(T) + 64;
   if (max_leaves < (1LL << h->depth) || box_smem > 200 * 1024)  // budgeted search: the reference's order

@@ -27,7 +27,7 @@ extern "C" {
 
 #define ANNF_OK 0
 #define ANNF_ERR_INVALID -1     /* bad argument (shape, range, null pointer) */
-#define ANNF_ERR_UNSUPPORTED -2 /* valid for the reference, not supported here (e.g. k > 32) */
+#define ANNF_ERR_UNSUPPORTED -2 /* valid for the reference, not supported here (e.g. k > 32 in process_rows) */
 #define ANNF_ERR_CUDA -3        /* a CUDA runtime call or launch failed */
 #define ANNF_ERR_ALLOC -4       /* device allocation failed */
 #define ANNF_ERR_STATE -5       /* call order (e.g. query before a tree was built) */
@@ -92,7 +92,8 @@ int annf_tree_get(const annf_handle* h, annf_tree_view* out);
 /* Exact k nearest neighbours of nq queries ([nq*d], real_type of the tree). distances [nq*k]
  * (Euclidean, i.e. square-rooted) and indices [nq*k] (original point indices), best first.
  * At most max_leaves leaves are scanned, in the reference's depth-first order (exact when
- * max_leaves >= 2^depth; the reference's default is 2147483640).
+ * max_leaves >= 2^depth; the reference's default is 2147483640). 1 <= k <= 1000 as in the
+ * reference (k above 32 runs a kernel with the k-list in shared memory, one CTA per query).
  * Replaces neighbors_extern (annfmp/openmp/kdtree/src/base.c:88-132, include/base.h:67-78). */
 int annf_kneighbors(annf_handle* h, const void* queries, int nq, int k, long long max_leaves,
                     void* distances, int* indices, void* stream);

@@ -136,6 +136,31 @@ def test_kneighbors_leaf_budget_vs_oracle(gpu_lib, oracle_mod, max_leaves, K):
     assert np.array_equal(_bits(dg), _bits(do))
 
 
+@pytest.mark.parametrize("K,max_leaves", [(33, 2147483640), (100, 2147483640), (1000, 2147483640), (100, 1),
+                                          (100, 7), (257, 0)])
+@pytest.mark.parametrize("dtype,d", [(np.float32, 8), (np.float64, 5)])
+def test_kneighbors_large_k_vs_oracle(gpu_lib, oracle_mod, K, max_leaves, dtype, d):
+    """k above 32 (the reference accepts up to 1000, helper.c:32-35): the shared-memory K-list
+    kernel gives the reference traversal's indices and distance bits, with and without a leaf
+    budget, including lists longer than the leaves scanned (the (max real, 0) fill)."""
+    from annfmp_gb300 import KDTree
+    O = oracle_mod
+    rng = np.random.default_rng(K + d + max_leaves % 97)
+    n = 6000
+    X = (rng.standard_normal((n, d)) * 5).astype(dtype)
+    X[::5] = np.round(X[::5])
+    Q = (rng.standard_normal((150, d)) * 5).astype(dtype)
+    Q[::3] = X[rng.integers(0, n, 50)]  # exact hits -> zero distances and ties
+    depth = O.tree_depth(n, 32)
+    ot = O.OracleTree(X, depth)
+    kd = KDTree(n_neighbors=K, tree_depth=depth, float_type="float" if dtype == np.float32 else "double",
+                splitting_type="longest", max_leaves=max_leaves).fit(X)
+    dg, ig = kd.kneighbors(Q)
+    do, io = ot.kneighbors(Q, K, max_leaves=max_leaves)
+    assert np.array_equal(ig, io)
+    assert np.array_equal(_bits(dg), _bits(do))
+
+
 # ---------------------------------------------------------------------------------------------
 # row propagation (reference process_rows_extern)
 # ---------------------------------------------------------------------------------------------

@@ -159,3 +159,27 @@ def test_openclopt_tree_shape():
     assert O.ocl_shape(100, 64) == (0, 1, 50, 100)      # 2 leaves
     assert O.ocl_shape(1536, 64) == (3, 15, 96, 1536)   # 24 leaves: 16 (tie goes down)
     assert O.ocl_shape(30, 64) == (-1, 0, 30, 30)       # one leaf, no internal node
+
+
+def test_large_k_against_reference(oracle_mod):
+    """The oracle's exact search and row propagation with k above 32 (the reference accepts up to
+    1000, helper.c:32-35) against the reference C core built from source."""
+    O = oracle_mod
+    if not O.reference_available():
+        if not os.path.isdir(REF_ROOT):
+            pytest.skip("reference tree not present")
+        O.build_reference(REF_ROOT)
+    rng = np.random.default_rng(77)
+    for trial, (nr, nc, d, K) in enumerate([(20, 24, 4, 40), (16, 30, 6, 100), (12, 13, 3, 33)]):
+        X = rng.standard_normal((nr * nc, d)).astype(np.float32)
+        A = rng.standard_normal((nr * nc, d)).astype(np.float32)
+        if trial == 2:
+            X, A = np.round(X).astype(np.float32), np.round(A).astype(np.float32)
+        pa = rng.integers(0, 256, (nr * nc, 7), dtype=np.uint8)
+        pb = rng.integers(0, 256, (nr * nc, 7), dtype=np.uint8)
+        depth = O.tree_depth(nr * nc, K + 8)
+        rt = O.reference_tree(X, depth)
+        ot = O.OracleTree(X, depth)
+        fr = O.reference_process_rows(rt, A, pa, pb, nr, nc, K, True, True)
+        fo, _ = ot.process_rows(A, pa, pb, nr, nc, K, True, True)
+        assert np.array_equal(fr, fo), trial
