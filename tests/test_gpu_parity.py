@@ -478,8 +478,10 @@ def test_errors(gpu_lib):
     from annfmp_gb300 import ANNFieldPropKDTreeGB300, KDTree, _lib
     X = np.random.default_rng(0).standard_normal((1000, 4)).astype(np.float32)
     kd = KDTree(n_neighbors=33, leaf_size=64, float_type="float").fit(X)
-    with pytest.raises(NotImplementedError):
-        kd.kneighbors(X[:5])
+    dist, idx = kd.kneighbors(X[:5])  # k up to 1000, as the reference
+    assert idx.shape == (5, 33) and dist.shape == (5, 33)
+    with pytest.raises(NotImplementedError):  # the row propagation takes k <= 32
+        kd.process_rows(np.zeros(4, np.int32), np.zeros((4, 3), np.uint8), np.zeros((1000, 3), np.uint8), X[:4], 2, 2)
     with pytest.raises(Exception, match="max_leaves"):
         KDTree(n_neighbors=2, leaf_size=8, float_type="float", max_leaves=-1).fit(X)
     with pytest.raises(ValueError):
