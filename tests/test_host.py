@@ -157,3 +157,34 @@ def test_mean_patch_l2_is_the_example_score():
     diff = pa.astype(np.float32) - pb[nnf].astype(np.float32)
     score = np.mean(np.linalg.norm(diff, axis=1))
     assert np.isclose(metrics.mean_patch_l2(a, b, nnf, psize), float(score), rtol=1e-6, atol=0)
+
+
+def test_parallel_restatement_hash_and_invariants():
+    """oracle/parallel.py (the CPU restatement the parallel form's GPU search is checked against):
+    its 32-bit hash gives the values of the kernels' C expression, the initial choice is the
+    lexicographic minimum of (SSD, index) over the candidates, and passes never worsen a match."""
+    import sys
+    sys.path.insert(0, ROOT)
+    from oracle import parallel as PR
+    from oracle.oracle import extract_patches
+    # values of the C expression (uint32 arithmetic) for these arguments
+    assert list(PR.hash3(np.uint64(7919 * 3), np.arange(3, dtype=np.uint64), np.uint64(0))) == \
+        [281888702, 4242423128, 3081578064]
+    assert int(PR.hash3(np.uint64(0xFFFFFFFF), np.uint64(4000000000), np.uint64(5))) == 865287707
+    rng = np.random.default_rng(5)
+    a = rng.integers(0, 256, (20, 23, 3), dtype=np.uint8)
+    b = rng.integers(0, 256, (21, 19, 3), dtype=np.uint8)
+    ps = 4
+    n_a = (20 - ps + 1) * (23 - ps + 1)
+    n_b = (21 - ps + 1) * (19 - ps + 1)
+    nat = rng.integers(0, n_b, (n_a, 3))
+    idx0, ssd0 = PR.parallel_search(a, b, ps, nat, iters=0)
+    pa = extract_patches(a, ps).astype(np.int64)
+    pb = extract_patches(b, ps).astype(np.int64)
+    s = ((pa[:, None, :] - pb[nat]) ** 2).sum(-1)
+    best = np.lexsort((nat, s), axis=1)[:, 0]
+    assert np.array_equal(idx0, nat[np.arange(n_a), best])
+    assert np.array_equal(ssd0, s[np.arange(n_a), best])
+    idx3, ssd3 = PR.parallel_search(a, b, ps, nat, iters=3, seed=9)
+    assert np.all(ssd3 <= ssd0)
+    assert np.array_equal(ssd3, ((pa - pb[idx3]) ** 2).sum(-1))
