@@ -455,6 +455,90 @@ def test_natural_knn_all_precisions_vs_oracle(gpu_lib, oracle_mod, kind, leaf, k
         assert same.all(), (kind, prec, float(same.mean()), np.nonzero(~same)[0][:8])
 
 
+def test_process_rows_ragged_vs_oracle(gpu_lib, oracle_mod):
+    """Ragged and degenerate grids (a single row, a single column, one patch), one- to six-dimensional
+    points, patches of 1 to 19 bytes, leaves barely larger than k, every propagate / select_best
+    combination: final indices and k-lists equal the oracle's, which the reference's own C core pins
+    on the same kind of draws."""
+    O = oracle_mod
+    rng = np.random.default_rng(4048)
+    shapes = [(1, 1), (1, 17), (23, 1), (2, 2)] + [(int(rng.integers(1, 25)), int(rng.integers(1, 25)))
+                                                     for _ in range(20)]
+    for trial, (nr, nc) in enumerate(shapes):
+        d, P, K = int(rng.integers(1, 7)), int(rng.integers(1, 20)), int(rng.integers(1, 5))
+        nA = nr * nc
+        X = rng.standard_normal((nA, d)).astype(np.float32)
+        A = rng.standard_normal((nA, d)).astype(np.float32)
+        if trial % 2:
+            X, A = np.round(X).astype(np.float32), np.round(A).astype(np.float32)
+        pa = rng.integers(0, 256, (nA, P), dtype=np.uint8)
+        pb = rng.integers(0, 256, (nA, P), dtype=np.uint8)
+        depth = O.tree_depth(nA, int(rng.integers(K + 1, K + 9)))
+        prop, sel = bool(rng.integers(0, 2)), bool(rng.integers(0, 2))
+        ot = O.OracleTree(X, depth)
+        fo, ko = ot.process_rows(A, pa, pb, nr, nc, K, prop, sel)
+        kd = gpu_tree(X, depth, K=K)
+        out = np.zeros(nA, np.int32)
+        kd.process_rows(out, pa, pb, A, nr, nc, K, prop, sel)
+        tag = (trial, nr, nc, d, P, K, depth, prop, sel)
+        assert np.array_equal(kd.knn_indices_.cpu().numpy(), ko), tag
+        assert np.array_equal(out, fo), tag
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 5, 9, 40])
+@pytest.mark.parametrize("K", [1, 4, 32, 40])
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+def test_kneighbors_tiny_trees_vs_oracle(gpu_lib, oracle_mod, n, K, dtype):
+    """Trees of one to a few leaves, and k above the number of points: the lists are filled as the
+    reference fills them (its initial maximum distance, position 0), indices and distance bits
+    equal the oracle's."""
+    O = oracle_mod
+    rng = np.random.default_rng(100 * n + K)
+    X = rng.standard_normal((n, 3)).astype(dtype)
+    Q = np.concatenate([rng.standard_normal((13, 3)).astype(dtype), X[:2]])
+    depth = O.tree_depth(n, 2)
+    ot = O.OracleTree(X, depth)
+    kd = gpu_tree(X, depth, K=K)
+    dg, ig = kd.kneighbors(Q)
+    do, io = ot.kneighbors(Q, K)
+    assert np.array_equal(ig, io)
+    assert np.array_equal(_bits(dg), _bits(do))
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+def test_dimension_limit_vs_oracle(gpu_lib, oracle_mod, dtype):
+    """d = 128, the largest dimension the kernels take: tree, exact kNN (k 4 and 40) and row
+    propagation equal the oracle's."""
+    O = oracle_mod
+    rng = np.random.default_rng(128)
+    nr, nc, d = 24, 40, 128
+    nA = nr * nc
+    X = (rng.standard_normal((nA, d)) * 4).astype(dtype)
+    X[::6] = np.round(X[::6])
+    A = (np.roll(X.reshape(nr, nc, d), (1, 2), axis=(0, 1)).reshape(nA, d)
+         + rng.standard_normal((nA, d))).astype(dtype)
+    depth = O.tree_depth(nA, 16)
+    ot = O.OracleTree(X, depth)
+    for K in (4, 40):
+        kd = gpu_tree(X, depth, K=K)
+        arrs = kd.tree_arrays()
+        assert np.array_equal(arrs["perm"], ot.perm) and np.array_equal(arrs["node_axis"], ot.node_axis)
+        Q = np.concatenate([A[:200], X[:50]])
+        dg, ig = kd.kneighbors(Q)
+        do, io = ot.kneighbors(Q, K)
+        assert np.array_equal(ig, io), K
+        assert np.array_equal(_bits(dg), _bits(do)), K
+    K, P = 3, 30
+    pa = rng.integers(0, 256, (nA, P), dtype=np.uint8)
+    pb = rng.integers(0, 256, (nA, P), dtype=np.uint8)
+    fo, ko = ot.process_rows(A, pa, pb, nr, nc, K, True, True)
+    kd = gpu_tree(X, depth, K=K)
+    out = np.zeros(nA, np.int32)
+    kd.process_rows(out, pa, pb, A, nr, nc, K, True, True)
+    assert np.array_equal(kd.knn_indices_.cpu().numpy(), ko)
+    assert np.array_equal(out, fo)
+
+
 def test_image_and_array_paths_agree(gpu_lib, golden):
     """annf_process_rows_img (patches read from the images) == annf_process_rows (patch arrays)."""
     from oracle import oracle as O

@@ -183,3 +183,25 @@ def test_large_k_against_reference(oracle_mod):
         fr = O.reference_process_rows(rt, A, pa, pb, nr, nc, K, True, True)
         fo, _ = ot.process_rows(A, pa, pb, nr, nc, K, True, True)
         assert np.array_equal(fr, fo), trial
+
+
+@pytest.mark.skipif(not os.path.isdir(REF_ROOT), reason="reference tree not present")
+def test_kneighbors_tiny_trees_against_reference(oracle_mod):
+    """Trees of one to a few leaves and k above the number of points, through the unmodified
+    reference KDTree: the oracle fills short lists as the reference does (its initial maximum
+    distance, tree position 0 mapped to that point's original index)."""
+    O = oracle_mod
+    O.reference_annfmp(REF_ROOT)  # the reference package, its C core behind ctypes
+    from annfmp.openmp.kdtree.base import KDTree as RefKDTree
+    for n in (1, 2, 3, 5, 9, 40):
+        for K in (1, 4, 32, 40):
+            for dt, ft in ((np.float32, "float"), (np.float64, "double")):
+                rng = np.random.default_rng(100 * n + K)
+                X = rng.standard_normal((n, 3)).astype(dt)
+                Q = np.concatenate([rng.standard_normal((13, 3)).astype(dt), X[:2]])
+                depth = O.tree_depth(n, 2)
+                do, io = O.OracleTree(X, depth).kneighbors(Q, K)
+                rk = RefKDTree(n_neighbors=K, tree_depth=depth, float_type=ft, splitting_type="longest").fit(X)
+                dr, ir = rk.kneighbors(Q)
+                assert np.array_equal(ir, io), (n, K, ft)
+                assert np.array_equal(np.asarray(dr, dt).view(np.uint8), do.view(np.uint8)), (n, K, ft)
