@@ -71,6 +71,25 @@ def test_library_eigensolver_is_never_captured():
     assert ANNFieldPropKDTreeGB300(verbose=0)._graph_wanted()
 
 
+def test_null_handle_is_rejected_by_every_entry_point(built_lib):
+    """Every status-returning call that takes a handle answers a NULL handle with ANNF_ERR_INVALID
+    and an error message, before any CUDA call (the reference prints and exits instead,
+    helper.c:30-52); annf_destroy(NULL) is a no-op."""
+    from annfmp_gb300 import _lib
+    lib = _lib.load(built_lib)
+    checked = 0
+    for name, (res, args) in sorted(_lib.SIGNATURES.items()):
+        if res is not _lib._i or not args or name == "annf_create":
+            continue
+        vals = [0.0 if a is ctypes.c_float else 0 if a in (_lib._i, _lib._u, _lib._ll, ctypes.c_longlong) else None
+                for a in args]
+        assert getattr(lib, name)(*vals) == _lib.ANNF_ERR_INVALID, name
+        assert "NULL" in lib.annf_last_error().decode(), name
+        checked += 1
+    assert checked == len(_declared_symbols()) - 6  # all but version, last_error, create, destroy, two counters
+    lib.annf_destroy(None)
+
+
 def test_missing_library_fails_loudly(tmp_path):
     from annfmp_gb300 import _lib
     saved = _lib._lib
