@@ -1,5 +1,5 @@
-"""The multi-rank side of bench.py on CPU (gloo, world size 2): max over ranks, whole-job value,
-and the reference arm's non-zero ranks exiting without work."""
+"""bench.py on CPU: the multi-rank side (gloo, world size 2: max over ranks, whole-job value, the
+reference arm's non-zero ranks exiting without work) and the reference arm's JSON line."""
 import os
 import socket
 import sys
@@ -55,3 +55,26 @@ def test_single_rank_reduce_is_identity():
     import bench
     assert bench.reduce_max(3.5, 1) == 3.5
     assert bench.replica_value(100, 10.0, 1) == pytest.approx(1e4)
+
+
+def test_reference_arm_line_keeps_the_contract():
+    """`bench.py --impl reference` (the CPU arm: the oracle's full plain-method fit of the pair,
+    nothing extrapolated) prints one JSON line with the keys the GPU arm's line carries."""
+    import json
+    import subprocess
+    out = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--workload", "small",
+                          "--steps", "1", "--warmup", "0"], capture_output=True, text=True, timeout=600, cwd=ROOT)
+    assert out.returncode == 0, out.stderr[-2000:]
+    lines = [ln for ln in out.stdout.splitlines() if ln.startswith("{")]
+    assert len(lines) == 1
+    rec = json.loads(lines[0])
+    for key in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better", "scaling",
+                "vs_baseline", "dtype", "data", "config", "impl", "cpu_baseline", "e2e"):
+        assert key in rec, key
+    assert rec["impl"] == "reference" and rec["higher_is_better"] is True and rec["steps"] == 1
+    assert rec["metric"] == rec["unit"] == "query patches/s"
+    assert rec["value"] == pytest.approx((512 - 7 + 1) ** 2 / (rec["ms_per_step"] / 1e3), rel=1e-6)
+    assert rec["cpu_baseline"]["value"] == rec["value"] and rec["cpu_baseline"]["cores"] >= 1
+    assert rec["cpu_baseline"]["kind"] in ("port", "reference")
+    assert rec["e2e"] == {"value": rec["value"], "unit": rec["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+    assert "workload" in rec["config"]
