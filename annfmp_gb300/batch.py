@@ -9,9 +9,9 @@ the same device tensors on every replay, so a stream of frames copies new images
 replays (``BatchNNF.inputs``).
 
 The captured calls are free of host synchronisation and of device allocation (the library's
-buffers are already large enough, torch's outputs come from the graph's private pool); the
-plain form is not captured because its exact eigensolver (cuSOLVER) queries its workspace on the
-host.
+buffers are already large enough, torch's outputs come from the graph's private pool). A batch
+runs the parallel form; a single pair's plain form replays as its own graph
+(``ANNFieldPropKDTreeGB300``'s default ``graph="auto"``).
 """
 from __future__ import annotations
 
@@ -28,7 +28,7 @@ from .field import ANNFieldPropKDTreeGB300
 
 
 def _size_class(h: int, w: int) -> int:
-    """Pairs are tuned per power-of-two class of their patch count."""
+    """Pairs are tuned per power-of-two class of their pixel count (A's image)."""
     return int(np.ceil(np.log2(max(h * w, 1))))
 
 
@@ -49,6 +49,13 @@ class Autotuner:
         if path and os.path.exists(path):
             with open(path) as f:
                 self.table = json.load(f)
+
+    @staticmethod
+    def pick(trials, max_error):
+        """From (seconds, mean error, leaf, iters) trials: the fastest within ``max_error``, else
+        the most accurate (ties broken by the tuple order)."""
+        ok = [t for t in trials if t[1] <= max_error]
+        return min(ok) if ok else min(trials, key=lambda t: (t[1], t[0], t[2], t[3]))
 
     def key(self, A, psize, d, k, leaf_precision):
         return f"{_size_class(A.shape[0], A.shape[1])}:{psize}:{d}:{k}:{leaf_precision}"
@@ -75,8 +82,7 @@ class Autotuner:
                 err = metrics.distance_ratio_error(A, B, nn, base_kw["psize"], n_samples=self.samples, seed=17,
                                                    device=A.device)["mean"]
                 trials.append((dt, err, leaf, it))
-        ok = [t for t in trials if t[1] <= self.max_error]
-        best = min(ok) if ok else min(trials, key=lambda t: t[1])
+        best = self.pick(trials, self.max_error)
         self.table[key] = {"choice": [best[2], best[3]], "trials": [list(t) for t in trials]}
         if self.path:
             with open(self.path, "w") as f:

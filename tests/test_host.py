@@ -207,3 +207,20 @@ def test_parallel_restatement_hash_and_invariants():
     idx3, ssd3 = PR.parallel_search(a, b, ps, nat, iters=3, seed=9)
     assert np.all(ssd3 <= ssd0)
     assert np.array_equal(ssd3, ((pa - pb[idx3]) ** 2).sum(-1))
+
+
+def test_autotuner_rule_and_cached_choices(tmp_path):
+    """The batch autotuner's rule: the fastest (leaf, passes) trial within the error budget, else
+    the most accurate; a size class already in its JSON table is answered from the table."""
+    from annfmp_gb300.batch import Autotuner
+    trials = [(3.0, 0.004, 16, 3), (1.0, 0.02, 16, 1), (2.0, 0.008, 32, 2), (2.5, 0.006, 64, 2)]
+    assert Autotuner.pick(trials, 0.01) == (2.0, 0.008, 32, 2)
+    assert Autotuner.pick(trials, 0.001) == (3.0, 0.004, 16, 3)
+    assert Autotuner.pick(trials, 1.0) == (1.0, 0.02, 16, 1)
+    A = np.zeros((300, 500, 3), np.uint8)
+    tuner = Autotuner(path=str(tmp_path / "t.json"))
+    kw = dict(psize=7, dim_reduced=8, n_neighbors=1)
+    key = tuner.key(A, 7, 8, 1, "bf16")
+    (tmp_path / "t.json").write_text('{"%s": {"choice": [32, 2], "trials": []}}' % key)
+    assert Autotuner(path=str(tmp_path / "t.json")).choose(A, A, kw) == (32, 2)  # no GPU touched
+    assert key.startswith("18:")  # 300 x 500 = 150000 pixels -> the 2^18 class
