@@ -1,17 +1,21 @@
 // pca.cu -- PCA fit and patch projection on the GPU (sm_103a).
 //
 // Fit (annfmp/openmp/base.py:168-191 -> scikit-learn PCA, covariance_eigh solver):
-//   G = X^T X and the column sums are integer sums of uint8 products, accumulated EXACTLY with
-//   dp4a into int32 partials that are flushed to 64-bit integers; the covariance is then finished
-//   in FP64 in the solver's own operation order (mean = sum / n; C = G - (n*mean_i)*mean_j;
-//   C /= n-1), so C is bit-identical to the CPU's; eigen-decomposition by cuSOLVER (FP64),
-//   eigenvectors reordered by decreasing eigenvalue and signed so that each component's largest
-//   |entry| is positive (sklearn svd_flip with u_based_decision=False).
+//   G = X^T X and the column sums are integer sums of uint8 products, accumulated EXACTLY: on the
+//   tensor cores (gram_tc.cu) where the shape fits, else with dp4a into int32 partials flushed to
+//   64-bit integers (gram_kernel); the covariance is then finished in FP64 in the solver's own
+//   operation order (mean = sum / n; C = G - (n*mean_i)*mean_j; C /= n-1), so C is bit-identical
+//   to the CPU's. Its leading eigenvectors come from the library's FP64 subspace solver (eig.cu,
+//   the default), cuSOLVER's full FP64 eigh (on request), or FP32 subspace steps with an FP64
+//   Rayleigh-Ritz step (the approximate forms); they are ordered by decreasing eigenvalue and
+//   signed so that each component's largest |entry| is positive (sklearn svd_flip with
+//   u_based_decision=False).
 // Projection (annfmp/openmp/base.py:193-200 -> X @ C^T - mean @ C^T in FP64, cast):
 //   each FP64 coefficient is split into 8 signed 7-bit digits (c = 2^-E * sum_k s_k 2^-7k, exact
 //   to ~2^-55 of the component's largest entry); every patch . digit-vector product is an exact
-//   int32 dp4a sum over the uint8 patch bytes, read straight from the image; the partial sums are
-//   recombined in FP64, the mean term subtracted, and the result rounded once to FP32.
+//   integer sum over the uint8 patch bytes, read straight from the image (on the tensor cores in
+//   proj_tc.cu where the shape fits, else the dp4a project_kernel here); the partial sums are
+//   recombined, the mean term subtracted, and the result rounded once to FP32.
 #include <cusolverDn.h>
 
 #include <algorithm>
