@@ -1,6 +1,10 @@
 // proj_tc.cu -- patch extraction fused with the PCA projection on the tensor cores (sm_103a).
 //
-// For the approximate NNF forms: every psize x psize x c patch of an image times the FP16-rounded
+// Three kernels: the row form (project_rows_tc_kernel, images of at most 4 channels) and the tile
+// form (project_tc_kernel, any channel count) of the approximate forms' FP16 projection, and the
+// exact projection (project_exact_tc_kernel, the drop-in form's; its dp4a twin is in pca.cu).
+//
+// Tile form: every psize x psize x c patch of an image times the FP16-rounded
 // components, FP32 accumulation, minus the projected mean. One tile = 128 consecutive patches of one
 // row: the psize image rows they cover are staged in shared memory (aligned 32-bit loads), each thread
 // pair expands one patch into the K-major FP16 A tile (core-matrix layout; K runs over the patch
@@ -10,7 +14,6 @@
 // the mean term and writes FP32 reduced patches. Pixel values 0..255 are exact in FP16 and every
 // product is exact in FP32, so the only rounding beyond FP32 summation is that of the components
 // (FP16: 11 significant bits).
-// The exact projection (pca.cu) remains the drop-in path.
 #include <cuda_fp16.h>
 
 #include <algorithm>

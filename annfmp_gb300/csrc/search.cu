@@ -17,7 +17,8 @@
 // Lists. A warp owns one query at a time and keeps its K-list distributed over lanes (lane j holds
 // entry j, sorted); each batch of 32 candidates is checked against the K-th key with one ballot
 // and the few that qualify are inserted with a shuffle-shift, so the pruning threshold is always
-// exact.
+// exact. Lists longer than 32 (kneighbors takes k up to 1000, helper.c:32-35) belong to one CTA
+// per query and stay sorted in shared memory (exact_dfs_big_kernel).
 #include <algorithm>
 #include <atomic>
 
