@@ -5,8 +5,9 @@ Same constructor parameters, ``fit(image_a, image_b)`` returning one int32 B-pat
 pixel (row-major), ``patches_a`` / ``patches_b`` properties and per-stage ``_timers``. Stages:
 
 1. PCA fit on n_subset/2 sampled patches of A (RandomState(seed)) and of B (seed+1), exactly as
-   scikit-learn's extract_patches_2d samples them; exact Gram matrix, FP64 covariance, FP64 eigh,
-   all on the GPU (``annf_pca_fit``);
+   scikit-learn's extract_patches_2d samples them; exact Gram matrix, FP64 covariance, its leading
+   eigenvectors in FP64 (the library's subspace solver; cuSOLVER's full eigh with
+   ``pca_solver="full"``), all on the GPU (``annf_pca_covariance`` + ``annf_pca_components``);
 2. patch extraction fused into the projection: every patch of A and B is projected straight from
    the image (``annf_project``) -- the reference's 1 GB-scale uint8 patch arrays and 8 GB FP64
    copies never exist;
@@ -15,7 +16,9 @@ pixel (row-major), ``patches_a`` / ``patches_b`` properties and per-stage ``_tim
 
 Extensions (not in the reference): ``nn_distances_`` (raw-patch L2 of each chosen index),
 ``knn_indices_`` (each pixel's k-list), torch CUDA tensors accepted as images (results then stay
-on the device).
+on the device), repeated fits replayed as one CUDA graph, and ``form="parallel"``: no row chain
+(natural-leaf candidates from tensor-core tiles, optional learned proposals, parallel
+propagation passes, every candidate verified by its exact raw-patch distance).
 """
 from __future__ import annotations
 
