@@ -3,9 +3,9 @@
 //
 // The plain form follows the reference's row-sequential propagation (each row waits for the one
 // above). This form has no such dependency: every pixel gets candidates from its natural leaf
-// (approximate leaf distances, top-4k re-ranked exactly in FP32), from offset proposals (a learned
-// predictor, optional), and from a few parallel propagation / random-search passes over its
-// neighbours' current matches. Every candidate is verified with the exact integer raw-patch SSD,
+// (tensor-core leaf distances, every point within their proven error bound re-ranked exactly in
+// FP32, so the FP32 scan's k-list), from offset proposals (a learned predictor, optional), and
+// from a few parallel propagation / random-search passes over its neighbours' current matches. Every candidate is verified with the exact integer raw-patch SSD,
 // so the answer is always a real patch distance.
 #include <algorithm>
 

@@ -42,7 +42,8 @@ extern "C" {
 #define ANNF_SPLIT_CYCLIC 0  /* axis = node depth mod d */
 #define ANNF_SPLIT_LONGEST 1 /* first axis of strictly largest bounding-box width */
 
-/* leaf-distance precision of annf_process_rows* (the plain form is ANNF_LEAF_EXACT) */
+/* leaf-distance precision of annf_natural_knn and annf_parallel_nnf* (the row propagation of
+ * annf_process_rows* always scans its leaves exactly) */
 #define ANNF_LEAF_EXACT 0 /* FP32/FP64 with the reference's summation order */
 #define ANNF_LEAF_BF16 1  /* BF16 tensor-core tiles (FP32 accumulate) + exact FP32 re-rank of the survivors */
 #define ANNF_LEAF_FP16 2  /* the same with FP16 tiles (tighter bound, fewer survivors) */
@@ -234,8 +235,9 @@ int annf_project_f16(annf_handle* h, const uint8_t* img, int hgt, int wid, int c
 
 /* The parallel NNF form (an addition beside the reference's row-sequential method, which has no
  * counterpart for it): every pixel's natural-leaf k-list (leaf_precision ANNF_LEAF_EXACT: FP32
- * leaf scan; ANNF_LEAF_BF16: queries grouped by leaf, BF16 tensor-core distance tiles, exact FP32
- * re-rank of the 4k best), optional offset proposals
+ * leaf scan; ANNF_LEAF_BF16 / _FP16 / _FP8: queries grouped by leaf, tensor-core distance tiles,
+ * exact FP32 re-rank of every point within the tiles' proven error bound, so the same k-list as
+ * the FP32 scan), optional offset proposals
  * (proposals [n_rows*n_cols*n_prop] B patch indices, -1 = none) and `iters` parallel passes of
  * neighbour propagation and random search (rand_samples offsets per pass within radius0 >> pass
  * of the current match, at least 1); every candidate is verified with the exact integer
@@ -274,8 +276,9 @@ int annf_raw_nn(annf_handle* h, const uint8_t* img_a, int ha, int wa, const uint
 /* The k nearest points of each query inside the leaf its descent reaches (no backtracking; the
  * reference's traversal with max_leaves = 1, kdtree.c:129-268 with only_leaf_idx). out_pos
  * [nq*k] tree positions (annf_tree_view.perm maps them to original indices), nearest first.
- * ANNF_LEAF_EXACT scans the leaf in FP32 (reference order); ANNF_LEAF_BF16 groups the queries by
- * leaf and computes BF16 tensor-core distance tiles, re-ranking the best 4k exactly in FP32. */
+ * ANNF_LEAF_EXACT scans the leaf in FP32 (reference order); ANNF_LEAF_BF16 / _FP16 / _FP8 group
+ * the queries by leaf and compute tensor-core distance tiles, re-ranking exactly in FP32 every
+ * point within the tiles' proven error bound, so the k-lists equal the FP32 scan's. */
 int annf_natural_knn(annf_handle* h, const void* queries, long long nq, int k, int leaf_precision,
                      int* out_pos, void* stream);
 
