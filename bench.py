@@ -1,14 +1,16 @@
 """Benchmark: query patches/s of the NNF hot path on one GB300 (or N replicas).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
-                    [--workload large|medium|small] [--form learned|parallel|plain] [--iters N]
+                    [--workload large|medium|small|batch|stream] [--form learned|parallel|plain|openclopt]
+                    [--iters N] [--no-compare] [--no-cpu-baseline]
 
 A step is one full NNF of one image pair, from device-resident uint8 images to the device-resident
-NNF. Forms: "plain" is the reference's method (PCA fit with the exact FP64 eigendecomposition, exact
+NNF. Forms: "plain" is the reference's method (PCA fit with the FP64 eigensolver, exact
 projection, k-d tree, exact first row, row propagation, raw-patch re-rank); "parallel" is the BF16
-form (subspace PCA with an FP64 Rayleigh-Ritz step, BF16 tensor-core projection, the same tree,
+form (subspace PCA with an FP64 Rayleigh-Ritz step, FP16 tensor-core projection, the same tree,
 BF16 tensor-core natural-leaf tiles with exact FP32 re-rank, parallel propagation with exact
-raw-patch verification); "learned" adds the trained offset-proposal network. value = query patches
+raw-patch verification); "learned" adds the trained offset-proposal network; "openclopt" is the
+reference GPU backend's algorithm on this library's kernels. value = query patches
 (A patch positions) per second over all ranks; distance_error = mean / p99 of d_found/d_exact - 1
 over 4096 sampled pixels against the exact raw-patch nearest neighbour; "forms" times the other
 forms on the same pair. e2e = the same through the public API from pinned host images to the host
