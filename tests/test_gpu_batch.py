@@ -1,5 +1,4 @@
 """Batched uneven pairs under one CUDA graph, and the autotuner."""
-import numpy as np
 import pytest
 
 pytestmark = pytest.mark.gpu

@@ -10,7 +10,6 @@ pytestmark = pytest.mark.gpu
 
 
 def _gpu_tree(X, leaf):
-    from annfmp_gb300 import _lib
     from annfmp_gb300._torch import ptr, stream_ptr
     from annfmp_gb300.openclopt import ANNFieldPropKDTreeOpenCLOPTGB300
     dev = torch.device("cuda", 0)
